@@ -1,0 +1,1220 @@
+/*
+ * vta_oracle.c -- CPU oracle for the VectorTA indicator hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is a plain-C restatement of the
+ * VectorTA crate's scalar f64 CPU paths (the src/indicators/ Rust files, the
+ * `Kernel::Scalar` / `Kernel::ScalarBatch` row functions).  It is used by the
+ * test-suite, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg
+ * as the checker.  The product (vectorta_gb300/) never links or calls it.
+ *
+ * Arithmetic rules followed so results match the Rust code bit for bit on the
+ * same host libm:
+ *   - compiled with -ffp-contract=off (Rust never contracts a*b+c);
+ *   - fma() exactly where the Rust source calls f64::mul_add;
+ *   - the same summation order / unrolling as the cited row function;
+ *   - fmax/fmin where the Rust calls f64::max/min (NaN-ignoring semantics).
+ *
+ * Every function cites the reference file:line it restates (paths relative to
+ * the VectorTA project root).  Status codes: 0 ok, otherwise a VTO_E* code.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define VTO_OK 0
+#define VTO_E_EMPTY 1
+#define VTO_E_ALL_NAN 2
+#define VTO_E_INVALID_PERIOD 3
+#define VTO_E_NOT_ENOUGH_VALID 4
+#define VTO_E_INVALID_PARAM 5
+#define VTO_E_INVALID_RANGE 6
+#define VTO_E_NOT_ENOUGH_DATA 7
+
+static const double QNAN = __builtin_nan("");
+
+static size_t first_valid(const double *x, size_t n) {
+    size_t i = 0;
+    while (i < n && isnan(x[i])) i++;
+    return i;
+}
+
+static void fill_nan(double *o, size_t n) {
+    for (size_t i = 0; i < n; i++) o[i] = QNAN;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Parameter-grid expansion.                                                  */
+/* Ascending ranges are identical across the crate; descending ranges differ  */
+/* per indicator, so the mode is explicit.                                    */
+/* ------------------------------------------------------------------------ */
+enum {
+    VTO_AX_DESC = 0,     /* start, start-step, ... while >= end
+                            (alma.rs:1199-1222, dema.rs:780-809, sma.rs:705-...) */
+    VTO_AX_SWAP = 1,     /* descending swapped to ascending
+                            (ema.rs:691-702, rsi.rs:513-542, trima.rs:1024-1049) */
+    VTO_AX_REV_FROM_END = 2, /* (end..=start).step_by(step) reversed (atr.rs:917-936) */
+    VTO_AX_DESC_PLUS_END = 3 /* DESC then `end` appended if missing (wma.rs:552-576) */
+};
+
+/* Returns the number of values written (<= cap) or the count needed when out
+ * is NULL.  0 means an empty (invalid) range. */
+size_t vto_axis_usize(size_t start, size_t end, size_t step, int mode,
+                      size_t *out, size_t cap) {
+    size_t n = 0;
+#define PUSH(v)                            \
+    do {                                   \
+        if (out && n < cap) out[n] = (v);  \
+        n++;                               \
+    } while (0)
+    if (step == 0 || start == end) {
+        PUSH(start);
+        return n;
+    }
+    if (start < end) {
+        for (size_t v = start; v <= end; v += step) {
+            PUSH(v);
+            if (v > (size_t)-1 - step) break;
+        }
+        return n;
+    }
+    switch (mode) {
+    case VTO_AX_SWAP:
+        for (size_t v = end; v <= start; v += step) {
+            PUSH(v);
+            if (v > (size_t)-1 - step) break;
+        }
+        break;
+    case VTO_AX_REV_FROM_END: {
+        size_t cnt = (start - end) / step + 1;
+        for (size_t k = cnt; k-- > 0;) PUSH(end + k * step);
+        break;
+    }
+    case VTO_AX_DESC_PLUS_END:
+    case VTO_AX_DESC:
+    default: {
+        size_t v = start, last = start;
+        for (;;) {
+            PUSH(v);
+            last = v;
+            if (v < end + step) break; /* next would drop below end */
+            v -= step;
+        }
+        if (mode == VTO_AX_DESC_PLUS_END && last != end) PUSH(end);
+        break;
+    }
+    }
+#undef PUSH
+    return n;
+}
+
+/* f64 axis with the crate's 1e-12 slack and accumulated x += step
+ * (alma.rs:1224-1260; same in stddev.rs:721, bollinger_bands.rs:1250,
+ * percentile_nearest_rank.rs:945, supertrend.rs:1253, zscore.rs:964). */
+size_t vto_axis_f64(double start, double end, double step, double *out, size_t cap) {
+    size_t n = 0;
+    if (fabs(step) < 1e-12 || fabs(start - end) < 1e-12) {
+        if (out && cap) out[0] = start;
+        return 1;
+    }
+    double st = fabs(step);
+    if (start < end) {
+        for (double x = start; x <= end + 1e-12; x += st) {
+            if (out && n < cap) out[n] = x;
+            n++;
+        }
+    } else {
+        for (double x = start; x + 1e-12 >= end; x -= st) {
+            if (out && n < cap) out[n] = x;
+            n++;
+        }
+    }
+    return n;
+}
+
+/* ------------------------------------------------------------------------ */
+/* ALMA                                                                       */
+/* ------------------------------------------------------------------------ */
+
+/* alma_prepare weights (alma.rs:315-332): w_i = exp(-diff*diff*inv_s2). */
+static void alma_weights_single(size_t period, double offset, double sigma,
+                                double *w, double *inv_norm) {
+    double m = offset * (double)(period - 1);
+    double s = (double)period / sigma;
+    double s2 = 2.0 * s * s;
+    double inv_s2 = 1.0 / s2;
+    double norm = 0.0;
+    for (size_t i = 0; i < period; i++) {
+        double diff = (double)i - m;
+        double wi = exp(-diff * diff * inv_s2);
+        w[i] = wi;
+        norm += wi;
+    }
+    *inv_norm = 1.0 / norm;
+}
+
+/* Batch weights (alma.rs:1426-1437): w = exp(-(i-m).powi(2) / s2). */
+void vto_alma_weights_batch(size_t period, double offset, double sigma,
+                            double *w, double *inv_norm) {
+    double m = offset * (double)(period - 1);
+    double s = (double)period / sigma;
+    double s2 = 2.0 * s * s;
+    double norm = 0.0;
+    for (size_t i = 0; i < period; i++) {
+        double d = (double)i - m;
+        double wi = exp(-(d * d) / s2);
+        w[i] = wi;
+        norm += wi;
+    }
+    *inv_norm = 1.0 / norm;
+}
+
+/* alma_scalar / alma_row_scalar (alma.rs:426-463, alma.rs:1505-1527):
+ * 4-wide unrolled dot, sum += ((d0w0 + d1w1) + d2w2) + d3w3, no FMA. */
+static void alma_row(const double *x, size_t n, size_t first, size_t period,
+                     const double *w, double inv_n, double *out) {
+    size_t p4 = period & ~(size_t)3;
+    for (size_t i = first + period - 1; i < n; i++) {
+        size_t start = i + 1 - period;
+        double sum = 0.0;
+        for (size_t k = 0; k < p4; k += 4) {
+            const double *d = x + start + k;
+            sum += d[0] * w[k] + d[1] * w[k + 1] + d[2] * w[k + 2] + d[3] * w[k + 3];
+        }
+        for (size_t k = p4; k < period; k++) sum += x[start + k] * w[k];
+        out[i] = sum * inv_n;
+    }
+}
+
+/* alma() single series (alma.rs:236-347). */
+int vto_alma(const double *x, size_t n, size_t period, double offset, double sigma,
+             double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    if (!(sigma > 0.0)) return VTO_E_INVALID_PARAM;
+    if (!(offset >= 0.0 && offset <= 1.0)) return VTO_E_INVALID_PARAM;
+    double *w = (double *)malloc(sizeof(double) * period);
+    double inv_n;
+    alma_weights_single(period, offset, sigma, w, &inv_n);
+    fill_nan(out, first + period - 1);
+    alma_row(x, n, first, period, w, inv_n, out);
+    free(w);
+    return VTO_OK;
+}
+
+/* alma_batch_with_kernel(ScalarBatch) row semantics (alma.rs:1368-1527).
+ * periods/offsets/sigmas give the expanded grid (period-major). */
+int vto_alma_batch(const double *x, size_t n, size_t rows, const size_t *periods,
+                   const double *offsets, const double *sigmas, double *out) {
+    if (n == 0) return VTO_E_ALL_NAN;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    size_t max_p = 0;
+    for (size_t r = 0; r < rows; r++) {
+        size_t p8 = (periods[r] + 7) & ~(size_t)7;
+        if (p8 > max_p) max_p = p8;
+    }
+    if (n - first < max_p) return VTO_E_NOT_ENOUGH_VALID;
+    double *w = (double *)malloc(sizeof(double) * (max_p ? max_p : 1));
+    for (size_t r = 0; r < rows; r++) {
+        size_t p = periods[r];
+        if (!(sigmas[r] > 0.0)) { free(w); return VTO_E_INVALID_PARAM; }
+        if (!(offsets[r] >= 0.0 && offsets[r] <= 1.0)) { free(w); return VTO_E_INVALID_PARAM; }
+        double inv_n;
+        vto_alma_weights_batch(p, offsets[r], sigmas[r], w, &inv_n);
+        double *o = out + r * n;
+        fill_nan(o, first + p - 1);
+        alma_row(x, n, first, p, w, inv_n, o);
+    }
+    free(w);
+    return VTO_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* EMA / DEMA / TEMA                                                          */
+/* ------------------------------------------------------------------------ */
+
+static int is_finite_bits(double v) { return isfinite(v); }
+
+/* ema_scalar_into / ema_row_scalar (ema.rs:430-469, ema.rs:858-893).
+ * Warmup: running mean over [first, first+p) of finite values; then
+ * prev = beta.mul_add(prev, alpha*x), non-finite x skipped.  NaN prefix =
+ * first only (ema.rs:362). */
+int vto_ema(const double *x, size_t n, size_t period, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    double alpha = 2.0 / ((double)period + 1.0);
+    double beta = 1.0 - alpha;
+    fill_nan(out, first);
+    double mean = x[first];
+    out[first] = mean;
+    size_t vc = 1;
+    size_t wend = first + period < n ? first + period : n;
+    for (size_t i = first + 1; i < wend; i++) {
+        double v = x[i];
+        if (is_finite_bits(v)) {
+            vc++;
+            double fvc = (double)vc;
+            mean = ((fvc - 1.0) * mean + v) / fvc;
+        }
+        out[i] = mean;
+    }
+    double prev = mean;
+    for (size_t i = wend; i < n; i++) {
+        double v = x[i];
+        if (is_finite_bits(v)) prev = fma(beta, prev, alpha * v);
+        out[i] = prev;
+    }
+    return VTO_OK;
+}
+
+/* dema_scalar, x86_64 variant (dema.rs:291-354): ema1 = ema2 = x[first],
+ * ema1 = ema1.mul_add(a, x*alpha); ema2 = ema2.mul_add(a, ema1*alpha);
+ * out = ema1.mul_add(2, -ema2).  NaN prefix first+p-1 (dema.rs:235).
+ * Needs len-first >= 2(p-1) (dema.rs:215-223). */
+static void dema_row(const double *x, size_t n, size_t first, size_t period, double *out) {
+    double alpha = 2.0 / ((double)period + 1.0);
+    double a = 1.0 - alpha;
+    double e1 = x[first], e2 = e1;
+    out[first] = e1;
+    for (size_t i = first + 1; i < n; i++) {
+        e1 = fma(e1, a, x[i] * alpha);
+        e2 = fma(e2, a, e1 * alpha);
+        out[i] = fma(e1, 2.0, -e2);
+    }
+    fill_nan(out, first + period - 1);
+}
+
+int vto_dema(const double *x, size_t n, size_t period, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period < 1 || period > n) return VTO_E_INVALID_PERIOD;
+    size_t needed = 2 * (period - 1);
+    if (n < needed) return VTO_E_NOT_ENOUGH_DATA;
+    if (n - first < needed) return VTO_E_NOT_ENOUGH_VALID;
+    dema_row(x, n, first, period, out);
+    return VTO_OK;
+}
+
+/* tema_scalar (tema.rs:228-298): three cascaded EMAs started at first,
+ * first+(p-1), first+2(p-1); out = 3*e1 - 3*e2 + e3 from first+3(p-1). */
+static void tema_row(const double *x, size_t n, size_t first, size_t period, double *out) {
+    size_t warm = first + (period - 1) * 3;
+    fill_nan(out, warm < n ? warm : n);
+    double per = 2.0 / ((double)period + 1.0);
+    double per1 = 1.0 - per;
+    size_t p1 = period - 1;
+    size_t start2 = first + p1, start3 = first + 2 * p1, start_out = first + 3 * p1;
+    if (period == 1) {
+        for (size_t i = first; i < n; i++) out[i] = x[i];
+        return;
+    }
+    double e1 = x[first], e2 = 0.0, e3 = 0.0;
+    size_t end0 = start2 < n ? start2 : n;
+    for (size_t i = first; i < end0; i++) e1 = e1 * per1 + x[i] * per;
+    if (start2 < n) {
+        e1 = e1 * per1 + x[start2] * per;
+        e2 = e1;
+        e2 = e2 * per1 + e1 * per;
+        size_t end1 = start3 < n ? start3 : n;
+        for (size_t i = start2 + 1; i < end1; i++) {
+            e1 = e1 * per1 + x[i] * per;
+            e2 = e2 * per1 + e1 * per;
+        }
+        if (start3 < n) {
+            e1 = e1 * per1 + x[start3] * per;
+            e2 = e2 * per1 + e1 * per;
+            e3 = e2;
+            e3 = e3 * per1 + e2 * per;
+            size_t end2 = start_out < n ? start_out : n;
+            for (size_t i = start3 + 1; i < end2; i++) {
+                e1 = e1 * per1 + x[i] * per;
+                e2 = e2 * per1 + e1 * per;
+                e3 = e3 * per1 + e2 * per;
+            }
+            for (size_t i = start_out; i < n; i++) {
+                e1 = e1 * per1 + x[i] * per;
+                e2 = e2 * per1 + e1 * per;
+                e3 = e3 * per1 + e2 * per;
+                out[i] = 3.0 * e1 - 3.0 * e2 + e3;
+            }
+        }
+    }
+}
+
+/* tema_prepare (tema.rs:1396-1435). */
+int vto_tema(const double *x, size_t n, size_t period, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    tema_row(x, n, first, period, out);
+    return VTO_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* RSI / Wilders                                                              */
+/* ------------------------------------------------------------------------ */
+
+static double rsi_val(double g, double l) {
+    double d = g + l;
+    return d == 0.0 ? 50.0 : 100.0 * g / d;
+}
+
+/* rsi_compute_into_scalar (rsi.rs:327-414).  Single-series path: a NaN delta
+ * in the warmup poisons the row; later NaN deltas count as 0 gain/loss. */
+int vto_rsi(const double *x, size_t n, size_t period, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    size_t warm = first + period;
+    fill_nan(out, warm < n ? warm : n);
+    double inv_p = 1.0 / (double)period, beta = 1.0 - inv_p;
+    double ag = 0.0, al = 0.0;
+    int has_nan = 0;
+    size_t warm_last = first + period < n - 1 ? first + period : (n ? n - 1 : 0);
+    for (size_t i = first + 1; i <= warm_last; i++) {
+        double d = x[i] - x[i - 1];
+        if (!isfinite(d)) { has_nan = 1; break; }
+        if (d > 0.0) ag += d;
+        else if (d < 0.0) al -= d;
+    }
+    size_t idx0 = first + period;
+    if (has_nan) {
+        ag = QNAN; al = QNAN;
+        if (idx0 < n) out[idx0] = QNAN;
+    } else {
+        ag *= inv_p; al *= inv_p;
+        if (idx0 < n) out[idx0] = rsi_val(ag, al);
+    }
+    for (size_t j = idx0 + 1; j < n; j++) {
+        double d = x[j] - x[j - 1];
+        double g = d > 0.0 ? d : 0.0;
+        double l = d < 0.0 ? -d : 0.0;
+        ag = fma(ag, beta, inv_p * g);
+        al = fma(al, beta, inv_p * l);
+        out[j] = rsi_val(ag, al);
+    }
+    return VTO_OK;
+}
+
+/* rsi_batch_inner (rsi.rs:568-697): shared gains/losses (NaN for non-finite
+ * deltas, so any later NaN delta poisons the row) and prefix sums pg/pl; the
+ * warmup average is (pg[idx0]-pg[first])*inv_p. */
+int vto_rsi_batch(const double *x, size_t n, size_t rows, const size_t *periods, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    size_t max_p = 0;
+    for (size_t r = 0; r < rows; r++) if (periods[r] > max_p) max_p = periods[r];
+    if (n - first < max_p) return VTO_E_NOT_ENOUGH_VALID;
+    double *gains = (double *)calloc(n, sizeof(double));
+    double *losses = (double *)calloc(n, sizeof(double));
+    double *pg = (double *)calloc(n, sizeof(double));
+    double *pl = (double *)calloc(n, sizeof(double));
+    for (size_t i = first + 1; i < n; i++) {
+        double d = x[i] - x[i - 1];
+        if (isfinite(d)) {
+            if (d > 0.0) gains[i] = d;
+            else if (d < 0.0) losses[i] = -d;
+        } else {
+            gains[i] = QNAN; losses[i] = QNAN;
+        }
+    }
+    for (size_t i = 1; i < n; i++) {
+        pg[i] = pg[i - 1] + gains[i];
+        pl[i] = pl[i - 1] + losses[i];
+    }
+    for (size_t r = 0; r < rows; r++) {
+        size_t period = periods[r];
+        double *o = out + r * n;
+        size_t idx0 = first + period;
+        fill_nan(o, idx0 < n ? idx0 : n);
+        if (idx0 >= n) continue;
+        double inv_p = 1.0 / (double)period, beta = 1.0 - inv_p;
+        double sg = pg[idx0] - pg[first], sl = pl[idx0] - pl[first];
+        double ag = sg * inv_p, al = sl * inv_p;
+        if (isnan(sg) || isnan(sl)) {
+            ag = QNAN; al = QNAN; o[idx0] = QNAN;
+        } else {
+            o[idx0] = rsi_val(ag, al);
+        }
+        for (size_t j = idx0 + 1; j < n; j++) {
+            ag = fma(ag, beta, inv_p * gains[j]);
+            al = fma(al, beta, inv_p * losses[j]);
+            o[j] = rsi_val(ag, al);
+        }
+    }
+    free(gains); free(losses); free(pg); free(pl);
+    return VTO_OK;
+}
+
+/* wilders_scalar (wilders.rs:262-322): seed = mean of the first p values
+ * (4-way chunked sum), then y = (x - y).mul_add(alpha, y).  The first p values
+ * must be finite (wilders.rs:223-230). */
+int vto_wilders(const double *x, size_t n, size_t period, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    for (size_t i = 0; i < period; i++)
+        if (!isfinite(x[first + i])) return VTO_E_NOT_ENOUGH_VALID;
+    size_t ws = first + period - 1;
+    fill_nan(out, ws);
+    const double *p = x + first;
+    double sum = 0.0;
+    size_t c4 = period / 4;
+    for (size_t c = 0; c < c4; c++, p += 4) sum += p[0] + p[1] + p[2] + p[3];
+    switch (period - c4 * 4) {
+    case 3: sum += p[0] + p[1] + p[2]; break;
+    case 2: sum += p[0] + p[1]; break;
+    case 1: sum += p[0]; break;
+    default: break;
+    }
+    double inv_n = 1.0 / (double)period;
+    double y = sum * inv_n;
+    out[ws] = y;
+    if (period == 1) {
+        for (size_t i = ws + 1; i < n; i++) out[i] = x[i];
+        return VTO_OK;
+    }
+    for (size_t i = ws + 1; i < n; i++) {
+        y = fma(x[i] - y, inv_n, y);
+        out[i] = y;
+    }
+    return VTO_OK;
+}
+
+/* wilders_batch_inner_into (wilders.rs:997-1110): seed from a prefix sum of
+ * data[first..] (sum = pref[period] - pref[0]); rows otherwise as scalar. */
+int vto_wilders_batch(const double *x, size_t n, size_t rows, const size_t *periods, double *out) {
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    size_t max_p = 0;
+    for (size_t r = 0; r < rows; r++) if (periods[r] > max_p) max_p = periods[r];
+    if (n - first < max_p) return VTO_E_NOT_ENOUGH_VALID;
+    double *pref = (double *)malloc(sizeof(double) * (n - first + 1));
+    pref[0] = 0.0;
+    double acc = 0.0;
+    for (size_t i = first; i < n; i++) { acc += x[i]; pref[i - first + 1] = acc; }
+    for (size_t r = 0; r < rows; r++) {
+        size_t period = periods[r];
+        double *o = out + r * n;
+        size_t ws = first + period - 1;
+        fill_nan(o, ws);
+        double sum = pref[period] - pref[0];
+        double inv_n = 1.0 / (double)period;
+        double y = sum * inv_n;
+        o[ws] = y;
+        if (period == 1) {
+            for (size_t i = ws + 1; i < n; i++) o[i] = x[i];
+            continue;
+        }
+        for (size_t i = ws + 1; i < n; i++) {
+            y = fma(x[i] - y, inv_n, y);
+            o[i] = y;
+        }
+    }
+    free(pref);
+    return VTO_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* ATR / ADX / SuperTrend                                                     */
+/* ------------------------------------------------------------------------ */
+
+static size_t first_valid_hlc(const double *h, const double *l, const double *c, size_t n) {
+    size_t i = 0;
+    while (i < n && (isnan(h[i]) || isnan(l[i]) || isnan(c[i]))) i++;
+    return i;
+}
+
+/* atr_compute_into_scalar (atr.rs:329-460): seed = mean TR over
+ * [first, first+len), TR(first) = h-l; rma = (-alpha).mul_add(rma, rma) +
+ * alpha*tr.  NaN prefix first+len-1 (atr.rs:229). */
+int vto_atr(const double *h, const double *l, const double *c, size_t n, size_t length,
+            double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    if (length == 0) return VTO_E_INVALID_PERIOD;
+    size_t first = first_valid_hlc(h, l, c, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (n - first < length) return VTO_E_NOT_ENOUGH_VALID;
+    size_t warm = first + length - 1;
+    fill_nan(out, warm);
+    double alpha = 1.0 / (double)length;
+    double sum_tr = h[first] - l[first];
+    if (warm > first) {
+        double pc = c[first];
+        for (size_t i = first + 1; i <= warm; i++) {
+            double tr = h[i] - l[i];
+            double hc = fabs(h[i] - pc);
+            if (hc > tr) tr = hc;
+            double lc = fabs(l[i] - pc);
+            if (lc > tr) tr = lc;
+            sum_tr += tr;
+            pc = c[i];
+        }
+    }
+    double rma = sum_tr / (double)length;
+    out[warm] = rma;
+    for (size_t i = warm + 1; i < n; i++) {
+        double pc = c[i - 1];
+        double tr = h[i] - l[i];
+        double hc = fabs(h[i] - pc);
+        if (hc > tr) tr = hc;
+        double lc = fabs(l[i] - pc);
+        if (lc > tr) tr = lc;
+        rma = fma(-alpha, rma, rma) + alpha * tr;
+        out[i] = rma;
+    }
+    return VTO_OK;
+}
+
+/* adx_scalar on the slices from first (adx.rs:299-421, called at
+ * adx.rs:265-272).  first = max of the per-field first valid indices
+ * (adx.rs:190-198); needs len-first >= p+1; NaN prefix first+2p-1. */
+int vto_adx(const double *h, const double *l, const double *c, size_t n, size_t period,
+            double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    size_t fh = first_valid(h, n), fl = first_valid(l, n), fc = first_valid(c, n);
+    if (fh >= n || fl >= n || fc >= n) return VTO_E_ALL_NAN;
+    size_t first = fh > fl ? fh : fl;
+    if (fc > first) first = fc;
+    if (n - first < period + 1) return VTO_E_NOT_ENOUGH_VALID;
+    size_t warm_end = first + 2 * period - 1;
+    fill_nan(out, warm_end < n ? warm_end : n);
+    const double *H = h + first, *L = l + first, *C = c + first;
+    double *O = out + first;
+    size_t len = n - first;
+    if (len <= period) return VTO_OK;
+    double pf = (double)period, rp = 1.0 / pf, omr = 1.0 - rp, pm1 = pf - 1.0;
+    double tr_sum = 0.0, pdm_sum = 0.0, mdm_sum = 0.0;
+    double ph = H[0], pl = L[0], pc = C[0];
+    for (size_t i = 1; i <= period; i++) {
+        double ch = H[i], cl = L[i];
+        double tr = fmax(fmax(ch - cl, fabs(ch - pc)), fabs(cl - pc));
+        double up = ch - ph, down = pl - cl;
+        if (up > down && up > 0.0) pdm_sum += up;
+        if (down > up && down > 0.0) mdm_sum += down;
+        tr_sum += tr;
+        ph = ch; pl = cl; pc = C[i];
+    }
+    double atr = tr_sum, pdm = pdm_sum, mdm = mdm_sum;
+    double pdi0 = 0.0, mdi0 = 0.0;
+    if (atr != 0.0) { pdi0 = (pdm / atr) * 100.0; mdi0 = (mdm / atr) * 100.0; }
+    double sdi0 = pdi0 + mdi0;
+    double dx_sum = sdi0 != 0.0 ? (fabs(pdi0 - mdi0) / sdi0) * 100.0 : 0.0;
+    size_t dx_count = 1;
+    double last_adx = 0.0;
+    ph = H[period]; pl = L[period]; pc = C[period];
+    for (size_t i = period + 1; i < len; i++) {
+        double ch = H[i], cl = L[i];
+        double tr = fmax(fmax(ch - cl, fabs(ch - pc)), fabs(cl - pc));
+        double up = ch - ph, down = pl - cl;
+        double pdmv = (up > down && up > 0.0) ? up : 0.0;
+        double mdmv = (down > up && down > 0.0) ? down : 0.0;
+        atr = atr * omr + tr;
+        pdm = pdm * omr + pdmv;
+        mdm = mdm * omr + mdmv;
+        double pdi = 0.0, mdi = 0.0;
+        if (atr != 0.0) { pdi = (pdm / atr) * 100.0; mdi = (mdm / atr) * 100.0; }
+        double sdi = pdi + mdi;
+        double dx = sdi != 0.0 ? (fabs(pdi - mdi) / sdi) * 100.0 : 0.0;
+        if (dx_count < period) {
+            dx_sum += dx;
+            dx_count++;
+            if (dx_count == period) {
+                last_adx = dx_sum * rp;
+                O[i] = last_adx;
+            }
+        } else {
+            last_adx = (last_adx * pm1 + dx) * rp;
+            O[i] = last_adx;
+        }
+        ph = ch; pl = cl; pc = C[i];
+    }
+    return VTO_OK;
+}
+
+/* supertrend_prepare + supertrend_scalar (supertrend.rs:223-302,
+ * supertrend.rs:457-550).  ATR is taken on the slices from first
+ * (atr() on &high[first..] etc.); outputs trend and changed with a NaN prefix
+ * first+p-1. */
+int vto_supertrend(const double *h, const double *l, const double *c, size_t n,
+                   size_t period, double factor, double *trend, double *changed) {
+    if (n == 0) return VTO_E_EMPTY;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    size_t first = first_valid_hlc(h, l, c, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    size_t m = n - first;
+    double *atr = (double *)malloc(sizeof(double) * m);
+    int st = vto_atr(h + first, l + first, c + first, m, period, atr);
+    if (st) { free(atr); return st; }
+    size_t warm = first + period - 1;
+    fill_nan(trend, warm);
+    fill_nan(changed, warm);
+    size_t start = first + period;
+    if (start > n) { free(atr); return VTO_OK; }
+    double hl2w = (h[warm] + l[warm]) * 0.5;
+    double atrw = atr[period - 1];
+    double pub = hl2w + factor * atrw;
+    double plb = hl2w - factor * atrw;
+    double last_close = c[warm];
+    int upper_state;
+    if (last_close <= pub) { trend[warm] = pub; upper_state = 1; }
+    else { trend[warm] = plb; upper_state = 0; }
+    changed[warm] = 0.0;
+    size_t ai = warm + 1 - first;
+    for (size_t i = warm + 1; i < n; i++, ai++) {
+        double a = atr[ai];
+        double hl2 = (h[i] + l[i]) * 0.5;
+        double ub = fma(factor, a, hl2);
+        double lb = fma(-factor, a, hl2);
+        double pcl = last_close;
+        double cub = ub;
+        if (pcl <= pub) cub = fmin(cub, pub);
+        double clb = lb;
+        if (pcl >= plb) clb = fmax(clb, plb);
+        double cc = c[i];
+        if (upper_state) {
+            if (cc <= cub) { trend[i] = cub; changed[i] = 0.0; }
+            else { trend[i] = clb; changed[i] = 1.0; upper_state = 0; }
+        } else {
+            if (cc >= clb) { trend[i] = clb; changed[i] = 0.0; }
+            else { trend[i] = cub; changed[i] = 1.0; upper_state = 1; }
+        }
+        pub = cub; plb = clb; last_close = cc;
+    }
+    free(atr);
+    return VTO_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* SMA / StdDev / Z-score / Bollinger                                         */
+/* ------------------------------------------------------------------------ */
+
+/* sma_scalar (sma.rs:302-330): running sum. */
+int vto_sma(const double *x, size_t n, size_t period, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    fill_nan(out, first + period - 1);
+    if (period == 1) {
+        for (size_t i = first; i < n; i++) out[i] = x[i];
+        return VTO_OK;
+    }
+    double sum = 0.0;
+    for (size_t k = 0; k < period; k++) sum += x[first + k];
+    double inv = 1.0 / (double)period;
+    out[first + period - 1] = sum * inv;
+    for (size_t i = first + period; i < n; i++) {
+        sum += x[i] - x[i - period];
+        out[i] = sum * inv;
+    }
+    return VTO_OK;
+}
+
+/* sma_batch_inner_into (sma.rs:909-1020): inclusive prefix ps starting at
+ * first; out[i] = (ps[i] - ps[i-p]) * inv. */
+int vto_sma_batch(const double *x, size_t n, size_t rows, const size_t *periods, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    size_t max_p = 0;
+    for (size_t r = 0; r < rows; r++) if (periods[r] > max_p) max_p = periods[r];
+    if (n - first < max_p) return VTO_E_NOT_ENOUGH_VALID;
+    double *ps = (double *)calloc(n, sizeof(double));
+    ps[first] = x[first];
+    for (size_t i = first + 1; i < n; i++) ps[i] = ps[i - 1] + x[i];
+    for (size_t r = 0; r < rows; r++) {
+        size_t p = periods[r];
+        double *o = out + r * n;
+        size_t warm = first + p - 1;
+        fill_nan(o, warm < n ? warm : n);
+        if (warm >= n) continue;
+        double inv = 1.0 / (double)p;
+        for (size_t i = warm; i < n; i++) {
+            double lo = i >= p ? ps[i - p] : 0.0;
+            o[i] = (ps[i] - lo) * inv;
+        }
+    }
+    free(ps);
+    return VTO_OK;
+}
+
+/* stddev_scalar (stddev.rs:358-409): population variance from running sum
+ * and sum of squares; var <= 0 -> 0; result * nbdev.  Same for batch rows
+ * (stddev.rs:1097-1105). */
+static void stddev_row(const double *x, size_t n, size_t first, size_t period, double nbdev,
+                       double *out) {
+    double inv = 1.0 / (double)period;
+    double sum = 0.0, sq = 0.0;
+    for (size_t k = 0; k < period; k++) {
+        double v = x[first + k];
+        sum += v;
+        sq += v * v;
+    }
+    size_t i0 = first + period - 1;
+    fill_nan(out, i0);
+    double mean = sum * inv;
+    double var = (sq * inv) - (mean * mean);
+    out[i0] = var <= 0.0 ? 0.0 : sqrt(var) * nbdev;
+    for (size_t j = first + period; j < n; j++) {
+        double old = x[j - period], nw = x[j];
+        sum += nw - old;
+        sq += nw * nw - old * old;
+        double m = sum * inv;
+        double v = (sq * inv) - (m * m);
+        out[j] = v <= 0.0 ? 0.0 : sqrt(v) * nbdev;
+    }
+}
+
+int vto_stddev(const double *x, size_t n, size_t period, double nbdev, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (!isfinite(nbdev) || nbdev < 0.0) return VTO_E_INVALID_PARAM;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    stddev_row(x, n, first, period, nbdev, out);
+    return VTO_OK;
+}
+
+/* zscore_scalar_classic_sma (zscore.rs:359-431), single-series path with
+ * mul_add: sum_sqr = v.mul_add(v, sum_sqr); variance = (-mean).mul_add(mean,
+ * sum_sqr*inv); sd==0 or NaN -> NaN. */
+int vto_zscore(const double *x, size_t n, size_t period, double nbdev, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    size_t we = first + period - 1;
+    fill_nan(out, we);
+    double inv = 1.0 / (double)period;
+    double sum = 0.0, sq = 0.0;
+    for (size_t j = first; j <= we; j++) {
+        double v = x[j];
+        sum += v;
+        sq = fma(v, v, sq);
+    }
+    double mean = sum * inv;
+    double var = fma(-mean, mean, sq * inv);
+    if (var < 0.0) var = 0.0;
+    double sd = var == 0.0 ? 0.0 : sqrt(var) * nbdev;
+    out[we] = (sd == 0.0 || isnan(sd)) ? QNAN : (x[we] - mean) / sd;
+    for (size_t i = we + 1; i < n; i++) {
+        double ov = x[i - period], nv = x[i];
+        double dd = nv - ov;
+        sum += dd;
+        sq = fma(nv + ov, dd, sq);
+        mean = sum * inv;
+        var = fma(-mean, mean, sq * inv);
+        if (var < 0.0) var = 0.0;
+        sd = var == 0.0 ? 0.0 : sqrt(var) * nbdev;
+        out[i] = (sd == 0.0 || isnan(sd)) ? QNAN : (nv - mean) / sd;
+    }
+    return VTO_OK;
+}
+
+/* zscore_row_scalar_classic_sma (zscore.rs:1344-1403): batch row, no FMA. */
+int vto_zscore_batch_row(const double *x, size_t n, size_t period, double nbdev, double *out) {
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (n - first < period || period == 0) return VTO_E_NOT_ENOUGH_VALID;
+    size_t we = first + period - 1;
+    fill_nan(out, we);
+    double sum = 0.0, sq = 0.0;
+    for (size_t j = first; j <= we; j++) { sum += x[j]; sq += x[j] * x[j]; }
+    double mean = sum / (double)period;
+    double var = (sq / (double)period) - (mean * mean);
+    double sd = var <= 0.0 ? 0.0 : sqrt(var) * nbdev;
+    out[we] = (sd == 0.0 || isnan(sd)) ? QNAN : (x[we] - mean) / sd;
+    for (size_t i = we + 1; i < n; i++) {
+        double ov = x[i - period], nv = x[i];
+        sum += nv - ov;
+        sq += nv * nv - ov * ov;
+        mean = sum / (double)period;
+        var = (sq / (double)period) - (mean * mean);
+        sd = var <= 0.0 ? 0.0 : sqrt(var) * nbdev;
+        out[i] = (sd == 0.0 || isnan(sd)) ? QNAN : (nv - mean) / sd;
+    }
+    return VTO_OK;
+}
+
+/* bb_row_scalar_classic_sma, devtype 0 (bollinger_bands.rs:566-670):
+ * population std; upper = m + devup*sd; lower = m - devdn*sd. */
+int vto_bollinger(const double *x, size_t n, size_t period, double devup, double devdn,
+                  double *up, double *mid, double *lo) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    size_t warm = first + period - 1;
+    fill_nan(up, warm); fill_nan(mid, warm); fill_nan(lo, warm);
+    double inv_n = 1.0 / (double)period;
+    double sum = 0.0, sq = 0.0;
+    for (size_t k = 0; k < period; k++) {
+        double v = x[first + k];
+        sum += v;
+        sq += v * v;
+    }
+    double mean = sum * inv_n;
+    double var0 = (sq * inv_n) - (mean * mean);
+    double sd0 = sqrt(fmax(var0, 0.0));
+    mid[warm] = mean;
+    up[warm] = mean + devup * sd0;
+    lo[warm] = mean - devdn * sd0;
+    for (size_t i = warm + 1; i < n; i++) {
+        double nw = x[i], old = x[i - period];
+        sum += nw - old;
+        sq = (sq - old * old) + nw * nw;
+        double m = sum * inv_n;
+        double var = (sq * inv_n) - (m * m);
+        double sd = sqrt(fmax(var, 0.0));
+        mid[i] = m;
+        up[i] = m + devup * sd;
+        lo[i] = m - devdn * sd;
+    }
+    return VTO_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Donchian / WillR / Percentile                                              */
+/* ------------------------------------------------------------------------ */
+
+/* donchian_scalar (donchian.rs:278-517).  Max/min are exact selections, so a
+ * direct window scan gives the same bits as the crate's block-prefix path.
+ * Window validity: p <= 32 uses is_nan, p > 32 uses is_finite. */
+int vto_donchian(const double *h, const double *l, size_t n, size_t period,
+                 double *up, double *mid, double *lo) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t fh = first_valid(h, n), fl = first_valid(l, n);
+    if (fh >= n || fl >= n) return VTO_E_ALL_NAN;
+    size_t first = fh > fl ? fh : fl;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    size_t warm = first + period - 1;
+    fill_nan(up, warm); fill_nan(mid, warm); fill_nan(lo, warm);
+    int finite_rule = period > 32;
+    for (size_t i = warm; i < n; i++) {
+        double mx = -INFINITY, mn = INFINITY;
+        int bad = 0;
+        for (size_t j = i + 1 - period; j <= i; j++) {
+            double hv = h[j], lv = l[j];
+            if (finite_rule ? !(isfinite(hv) && isfinite(lv)) : (isnan(hv) || isnan(lv))) {
+                bad = 1;
+                break;
+            }
+            if (hv > mx) mx = hv;
+            if (lv < mn) mn = lv;
+        }
+        if (bad) { up[i] = mid[i] = lo[i] = QNAN; }
+        else { up[i] = mx; lo[i] = mn; mid[i] = fma(mx - mn, 0.5, mn); }
+    }
+    return VTO_OK;
+}
+
+/* willr_scalar (willr.rs:327-445) and willr_row_shared_core
+ * (willr.rs:1386-1425): window containing a NaN high/low -> NaN, NaN close
+ * -> NaN, denom == 0 -> 0, else (-100).mul_add((h-c)/denom, 0). */
+int vto_willr(const double *h, const double *l, const double *c, size_t n, size_t period,
+              double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    size_t first = first_valid_hlc(h, l, c, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    size_t warm = first + period - 1;
+    fill_nan(out, warm);
+    for (size_t i = warm; i < n; i++) {
+        double cv = c[i];
+        if (isnan(cv)) { out[i] = QNAN; continue; }
+        double hh = -INFINITY, ll = INFINITY;
+        int bad = 0;
+        for (size_t j = i + 1 - period; j <= i; j++) {
+            if (isnan(h[j]) || isnan(l[j])) { bad = 1; break; }
+            if (h[j] > hh) hh = h[j];
+            if (l[j] < ll) ll = l[j];
+        }
+        if (bad || !(isfinite(hh) && isfinite(ll))) { out[i] = QNAN; continue; }
+        double den = hh - ll;
+        out[i] = den == 0.0 ? 0.0 : fma(-100.0, (hh - cv) / den, 0.0);
+    }
+    return VTO_OK;
+}
+
+static int cmp_dbl(const void *a, const void *b) {
+    double x = *(const double *)a, y = *(const double *)b;
+    return (x > y) - (x < y);
+}
+
+/* nearest-rank index: round(p_frac.mul_add(wl, 0)) - 1 clamped to [0, wl-1]
+ * (percentile_nearest_rank.rs:221-229); Rust round = C round(). */
+static size_t pnr_rank(double p_frac, size_t wl) {
+    double raw_f = round(fma(p_frac, (double)wl, 0.0));
+    long long raw = (long long)raw_f - 1;
+    size_t k = raw <= 0 ? 0 : (size_t)raw;
+    if (k >= wl) k = wl - 1;
+    return k;
+}
+
+/* pnr_compute_into (percentile_nearest_rank.rs:190-266): sorted window of the
+ * non-NaN values; out = sorted[k]; empty window -> NaN. */
+int vto_percentile_nearest_rank(const double *x, size_t n, size_t length, double percentage,
+                                double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (length == 0 || length > n) return VTO_E_INVALID_PERIOD;
+    if (!(percentage >= 0.0 && percentage <= 100.0)) return VTO_E_INVALID_PARAM;
+    if (n - first < length) return VTO_E_NOT_ENOUGH_VALID;
+    size_t start_i = first + length - 1;
+    fill_nan(out, start_i);
+    double p_frac = percentage * 0.01;
+    double *buf = (double *)malloc(sizeof(double) * length);
+    for (size_t i = start_i; i < n; i++) {
+        size_t wl = 0;
+        for (size_t j = i + 1 - length; j <= i; j++)
+            if (!isnan(x[j])) buf[wl++] = x[j];
+        if (wl == 0) { out[i] = QNAN; continue; }
+        qsort(buf, wl, sizeof(double), cmp_dbl);
+        out[i] = buf[pnr_rank(p_frac, wl)];
+    }
+    free(buf);
+    return VTO_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Weighted-window moving averages                                            */
+/* ------------------------------------------------------------------------ */
+
+/* wma_scalar (wma.rs:295-336): running weighted sum; p >= 2 (wma.rs:260). */
+int vto_wma(const double *x, size_t n, size_t period, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period < 2 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    fill_nan(out, first + period - 1);
+    size_t lb = period - 1;
+    double pf = (double)period;
+    double weights = pf * (pf + 1.0) * 0.5;
+    const double *base = x + first;
+    double sum = 0.0, ws = 0.0;
+    for (size_t k = 0; k < lb; k++) {
+        double v = base[k];
+        ws += v * ((double)k + 1.0);
+        sum += v;
+    }
+    for (size_t i = first + lb, old = first; i < n; i++, old++) {
+        double v = x[i];
+        ws += v * pf;
+        sum += v;
+        out[i] = ws / weights;
+        ws -= sum;
+        sum -= x[old];
+    }
+    return VTO_OK;
+}
+
+/* swma_scalar (swma.rs:406-482): triangle = SMA(a) of SMA(b) via a ring of
+ * running sums; a,b from the parity of p; p==1 copy, p==2 pairwise mean. */
+int vto_swma(const double *x, size_t n, size_t period, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    fill_nan(out, first + period - 1);
+    size_t a, b;
+    if (period & 1) { a = b = (period + 1) >> 1; }
+    else { a = period >> 1; b = a + 1; }
+    if (period == 1) {
+        for (size_t i = first; i < n; i++) out[i] = x[i];
+        return VTO_OK;
+    }
+    if (period == 2) {
+        for (size_t i = first + 1; i < n; i++) out[i] = (x[i - 1] + x[i]) * 0.5;
+        return VTO_OK;
+    }
+    double inv_ab = 1.0 / ((double)a * (double)b);
+    size_t sfa = first + a - 1, sfab = first + period - 1;
+    double *ring = (double *)calloc(b, sizeof(double));
+    size_t rb = 0;
+    double s1 = 0.0, s2 = 0.0;
+    for (size_t i = first; i < n; i++) {
+        s1 += x[i];
+        if (i >= sfa) {
+            double old = ring[rb];
+            s2 = s2 + (s1 - old);
+            ring[rb] = s1;
+            if (++rb == b) rb = 0;
+            if (i >= sfab) out[i] = s2 * inv_ab;
+            s1 -= x[i + 1 - a];
+        }
+    }
+    free(ring);
+    return VTO_OK;
+}
+
+/* combination_f64 / pascal_weights (pwma.rs:1367-1408). */
+void vto_pwma_weights(size_t period, double *w) {
+    size_t nn = period - 1;
+    double sum = 0.0;
+    for (size_t r = 0; r <= nn; r++) {
+        size_t rr = r < nn - r ? r : nn - r;
+        double res = 1.0;
+        for (size_t i = 0; i < rr; i++) {
+            res *= (double)(nn - i);
+            res /= (double)(i + 1);
+        }
+        w[r] = res;
+    }
+    for (size_t r = 0; r <= nn; r++) sum += w[r];
+    for (size_t r = 0; r <= nn; r++) w[r] /= sum;
+}
+
+/* pwma_scalar (pwma.rs:345-400): 4 FMA accumulators, (s0+s1)+(s2+s3), tail
+ * by mul_add.  `batch` selects pwma_row_scalar's 8 accumulators
+ * (pwma.rs:1126-1196). */
+static void pwma_row(const double *x, size_t n, size_t first, size_t period, const double *w,
+                     int batch, double *out) {
+    for (size_t i = first + period - 1; i < n; i++) {
+        const double *d = x + i + 1 - period;
+        double sum;
+        size_t k = 0;
+        if (!batch) {
+            double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+            size_t ke = period & ~(size_t)3;
+            for (; k < ke; k += 4) {
+                s0 = fma(d[k], w[k], s0);
+                s1 = fma(d[k + 1], w[k + 1], s1);
+                s2 = fma(d[k + 2], w[k + 2], s2);
+                s3 = fma(d[k + 3], w[k + 3], s3);
+            }
+            sum = (s0 + s1) + (s2 + s3);
+        } else {
+            double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            size_t ke = period & ~(size_t)7;
+            for (; k < ke; k += 8)
+                for (int u = 0; u < 8; u++) s[u] = fma(d[k + u], w[k + u], s[u]);
+            sum = (((s[0] + s[1]) + (s[2] + s[3])) + (s[4] + s[5])) + (s[6] + s[7]);
+        }
+        for (; k < period; k++) sum = fma(d[k], w[k], sum);
+        out[i] = sum;
+    }
+}
+
+int vto_pwma(const double *x, size_t n, size_t period, int batch, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    double *w = (double *)malloc(sizeof(double) * period);
+    vto_pwma_weights(period, w);
+    fill_nan(out, first + period - 1);
+    pwma_row(x, n, first, period, w, batch, out);
+    free(w);
+    return VTO_OK;
+}
+
+/* sinwma_prepare weights (sinwma.rs:271-289) and sinwma_scalar
+ * (sinwma.rs:353-389, same 4-wide unrolled dot as ALMA, no inv_norm). */
+void vto_sinwma_weights(size_t period, double *w) {
+    double sum = 0.0;
+    for (size_t k = 0; k < period; k++) {
+        double ang = ((double)k + 1.0) * M_PI / ((double)period + 1.0);
+        w[k] = sin(ang);
+        sum += w[k];
+    }
+    double inv = 1.0 / sum;
+    for (size_t k = 0; k < period; k++) w[k] *= inv;
+}
+
+int vto_sinwma(const double *x, size_t n, size_t period, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    double *w = (double *)malloc(sizeof(double) * period);
+    vto_sinwma_weights(period, w);
+    fill_nan(out, first + period - 1);
+    size_t p4 = period & ~(size_t)3;
+    for (size_t i = first + period - 1; i < n; i++) {
+        const double *d = x + i + 1 - period;
+        double sum = 0.0;
+        for (size_t k = 0; k < p4; k += 4)
+            sum += d[k] * w[k] + d[k + 1] * w[k + 1] + d[k + 2] * w[k + 2] + d[k + 3] * w[k + 3];
+        for (size_t k = p4; k < period; k++) sum += d[k] * w[k];
+        out[i] = sum;
+    }
+    free(w);
+    return VTO_OK;
+}
+
+/* trima_scalar_optimized (trima.rs:277-364): SMA(m1) then SMA(m2) over a
+ * ring of SMA1 values; m1 = (p+1)/2, m2 = p - m1 + 1; p > 3. */
+int vto_trima(const double *x, size_t n, size_t period, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    if (period <= 3) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    size_t m1 = (period + 1) / 2, m2 = period - m1 + 1;
+    size_t warm = first + period - 1;
+    fill_nan(out, warm);
+    double inv1 = 1.0 / (double)m1, inv2 = 1.0 / (double)m2;
+    const double *base = x + first;
+    double sum1 = 0.0;
+    size_t j = 0, eu = m1 & ~(size_t)3;
+    for (; j < eu; j += 4) sum1 += base[j] + base[j + 1] + base[j + 2] + base[j + 3];
+    for (; j < m1; j++) sum1 += base[j];
+    double *ring = (double *)malloc(sizeof(double) * m2);
+    size_t rl = 0;
+    double sum2 = 0.0;
+    size_t t = first + m1 - 1;
+    size_t pn = first + m1, po = first;
+    double s1 = sum1 * inv1;
+    ring[rl++] = s1;
+    sum2 += s1;
+    while (rl < m2) {
+        t++;
+        sum1 += x[pn++] - x[po++];
+        s1 = sum1 * inv1;
+        ring[rl++] = s1;
+        sum2 += s1;
+    }
+    out[warm] = sum2 * inv2;
+    size_t head = 0;
+    for (t = t + 1; t < n; t++) {
+        sum1 += x[pn++] - x[po++];
+        double ns1 = sum1 * inv1;
+        double os1 = ring[head];
+        sum2 += ns1 - os1;
+        ring[head] = ns1;
+        if (++head == m2) head = 0;
+        out[t] = sum2 * inv2;
+    }
+    free(ring);
+    return VTO_OK;
+}
