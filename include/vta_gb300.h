@@ -1,0 +1,528 @@
+/*
+ * vta_gb300.h -- C ABI of the GB300-native VectorTA indicator hot path.
+ *
+ * One shared library (libvta_gb300.so) replaces the crate's per-indicator CUDA
+ * wrappers (the src/cuda X_wrapper.rs files: `CudaX` structs driving PTX through
+ * `cust`).  Every entry point is plain C: host or device pointers, sizes and
+ * small parameter structs; no CUDA, torch or Rust types cross the boundary.
+ *
+ * Conventions (the crate's, kept so existing callers port one-to-one):
+ *   - batch ("one series, many params"): output is row-major
+ *     [n_combos][len], rows in the crate's expand_grid order (period-major);
+ *   - many-series ("time-major"): input and output are [rows][cols] with
+ *     element (t, s) at t*cols + s; one parameter set for all series;
+ *   - warm-up cells are quiet NaN at exactly the crate's positions;
+ *   - *_dev functions take host inputs and return device arrays owned by the
+ *     caller (free with vta_device_array_free); *_device functions take device
+ *     inputs and write into caller-provided device outputs (the crate's
+ *     x_batch_device / x_many_series_one_param_device); *_into_host_f32
+ *     writes host outputs (the crate's x_batch_into_host_f32);
+ *   - every call is stream-ordered on the context's stream and synchronous on
+ *     return, like the crate's wrappers (which end with stream.synchronize()).
+ * Thread safety: a vta_ctx is used by one thread at a time (as a CudaX is).
+ */
+#ifndef VTA_GB300_H
+#define VTA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes map the crate's CudaXError variants one-to-one
+ * (src/cuda/moving_averages/alma_wrapper.rs:72-101). */
+typedef enum vta_status {
+    VTA_OK = 0,
+    VTA_ERR_CUDA = 1,                   /* Cuda(CudaError) */
+    VTA_ERR_OUT_OF_MEMORY = 2,          /* OutOfMemory{required, free, headroom} */
+    VTA_ERR_MISSING_KERNEL_SYMBOL = 3,  /* MissingKernelSymbol{name} */
+    VTA_ERR_INVALID_INPUT = 4,          /* InvalidInput(String) */
+    VTA_ERR_INVALID_POLICY = 5,         /* InvalidPolicy(&str) */
+    VTA_ERR_LAUNCH_CONFIG_TOO_LARGE = 6,/* LaunchConfigTooLarge{grid, block} */
+    VTA_ERR_DEVICE_MISMATCH = 7,        /* DeviceMismatch{buf, current} */
+    VTA_ERR_NOT_IMPLEMENTED = 8         /* NotImplemented */
+} vta_status;
+
+/* Message of the last failure on the calling thread (the Display text of the
+ * crate's error enums). */
+const char* vta_last_error(void);
+const char* vta_version(void);
+
+/* Number of CUDA devices (crate: cuda_device_count, src/cuda/mod.rs:560-575);
+ * 0 when no driver or device is present. */
+int vta_device_count(void);
+
+/* ---- context: CudaX::new(device_id) (alma_wrapper.rs:133-169) ---------- */
+typedef struct vta_ctx vta_ctx;
+vta_status vta_ctx_create(int device_id, vta_ctx** out);
+vta_status vta_ctx_destroy(vta_ctx* ctx);
+/* CudaX::synchronize (alma_wrapper.rs:171-173). */
+vta_status vta_ctx_synchronize(vta_ctx* ctx);
+/* Run on a caller-owned cudaStream_t instead of the context's own stream
+ * (NULL restores the context stream). */
+vta_status vta_ctx_set_stream(vta_ctx* ctx, void* cuda_stream);
+void* vta_ctx_get_stream(vta_ctx* ctx);
+/* CudaXPolicy / set_policy (alma_wrapper.rs:18-70): keys
+ *   "wma_batch"   = "auto" | "plain" | "tc_fp16x3" | "tc_bf16x3"
+ *   "recur_chunk" = "auto" | "sequential" | <positive multiple of 32>     */
+vta_status vta_ctx_set_policy(vta_ctx* ctx, const char* key, const char* value);
+/* selected_batch_kernel() (alma_wrapper.rs:239-245): name of the last kernel
+ * path used by this context. */
+const char* vta_ctx_last_kernel(vta_ctx* ctx);
+/* Device workspace currently held by the context (bytes). */
+size_t vta_ctx_scratch_bytes(vta_ctx* ctx);
+
+/* ---- device arrays: DeviceArrayF32 (alma_wrapper.rs:103-117) ----------- */
+typedef struct vta_device_array {
+    float* ptr;     /* device pointer, rows*cols floats, owned */
+    size_t rows;
+    size_t cols;
+    int device;
+} vta_device_array;
+vta_status vta_device_array_free(vta_device_array* arr);
+vta_status vta_device_array_copy_to_host(vta_ctx* ctx, const vta_device_array* arr,
+                                         float* host, size_t n);
+
+/* Page-locked host buffers for fast copies (the crate's LockedBuffer,
+ * alma_wrapper.rs:810-815). */
+vta_status vta_pinned_alloc(size_t bytes, void** out);
+vta_status vta_pinned_free(void* p);
+/* Plain device buffers for callers without their own allocator. */
+vta_status vta_device_alloc(vta_ctx* ctx, size_t bytes, void** out);
+vta_status vta_device_free(vta_ctx* ctx, void* p);
+vta_status vta_memcpy_h2d(vta_ctx* ctx, void* dst, const void* src, size_t bytes);
+vta_status vta_memcpy_d2h(vta_ctx* ctx, void* dst, const void* src, size_t bytes);
+
+/* ---- parameter sweeps: (start, end, step) like the crate's BatchRange --- */
+typedef struct vta_range_usize { size_t start, end, step; } vta_range_usize;
+typedef struct vta_range_f64 { double start, end, step; } vta_range_f64;
+
+/* AlmaBatchRange / AlmaParams (alma.rs:66-80, 1068-1082) */
+typedef struct vta_alma_batch_range { vta_range_usize period; vta_range_f64 offset, sigma; } vta_alma_batch_range;
+typedef struct vta_alma_params { size_t period; double offset, sigma; } vta_alma_params;
+/* period-only sweeps: EMA, DEMA, TEMA, RSI, Wilders, SMA, WMA, SWMA, PWMA,
+ * SINWMA, TRIMA, ATR (`length`), ADX, Donchian, WillR */
+typedef struct vta_period_batch_range { vta_range_usize period; } vta_period_batch_range;
+typedef struct vta_period_params { size_t period; } vta_period_params;
+/* StdDevBatchRange (stddev.rs:573-585) */
+typedef struct vta_stddev_batch_range { vta_range_usize period; vta_range_f64 nbdev; } vta_stddev_batch_range;
+typedef struct vta_stddev_params { size_t period; double nbdev; } vta_stddev_params;
+/* ZscoreBatchRange (zscore.rs:786-802), ma_type "sma" and devtype 0 */
+typedef struct vta_zscore_batch_range { vta_range_usize period; vta_range_f64 nbdev; } vta_zscore_batch_range;
+typedef struct vta_zscore_params { size_t period; double nbdev; } vta_zscore_params;
+/* BollingerBandsBatchRange (bollinger_bands.rs:1087-1104), matype "sma", devtype 0 */
+typedef struct vta_bollinger_batch_range { vta_range_usize period; vta_range_f64 devup, devdn; } vta_bollinger_batch_range;
+typedef struct vta_bollinger_params { size_t period; double devup, devdn; } vta_bollinger_params;
+/* SuperTrendBatchRange (supertrend.rs:1223-1300) */
+typedef struct vta_supertrend_batch_range { vta_range_usize period; vta_range_f64 factor; } vta_supertrend_batch_range;
+typedef struct vta_supertrend_params { size_t period; double factor; } vta_supertrend_params;
+/* PercentileNearestRankBatchRange (percentile_nearest_rank.rs:815-827) */
+typedef struct vta_percentile_batch_range { vta_range_usize length; vta_range_f64 percentage; } vta_percentile_batch_range;
+typedef struct vta_percentile_params { size_t length; double percentage; } vta_percentile_params;
+
+/* ==== alma (src/cuda/moving_averages/alma_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_alma_expand_grid(const vta_alma_batch_range* sweep, vta_alma_params* out, size_t cap, size_t* n_combos);
+/* alma_batch_dev (alma_wrapper.rs:625) */
+vta_status vta_alma_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_alma_batch_range* sweep, vta_device_array* out);
+/* alma_batch_device / _from_device_prices (alma_wrapper.rs:671); first_valid as in the crate. */
+vta_status vta_alma_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_alma_batch_range* sweep, float* d_out);
+/* alma_batch_into_host_f32 (alma_wrapper.rs:783); each output holds out_len >= rows*cols floats. */
+vta_status vta_alma_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_alma_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* alma_many_series_one_param_time_major_dev (alma_wrapper.rs:819) */
+vta_status vta_alma_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_alma_params* params, vta_device_array* out);
+/* alma_many_series_one_param_device (alma_wrapper.rs:1521) */
+vta_status vta_alma_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_alma_params* params, float* d_out);
+
+/* ==== ema (src/cuda/moving_averages/ema_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_ema_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* ema_batch_dev (ema_wrapper.rs:193) */
+vta_status vta_ema_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* ema_batch_device / _from_device_prices (ema_wrapper.rs:256); first_valid as in the crate. */
+vta_status vta_ema_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* ema_batch_into_host_f32 (ema_wrapper.rs:309); each output holds out_len >= rows*cols floats. */
+vta_status vta_ema_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* ema_many_series_one_param_time_major_dev (ema_wrapper.rs:325) */
+vta_status vta_ema_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* ema_many_series_one_param_device (ema_wrapper.rs:381) */
+vta_status vta_ema_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== dema (src/cuda/moving_averages/dema_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_dema_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* dema_batch_dev (dema_wrapper.rs:219) */
+vta_status vta_dema_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* dema_batch_device / _from_device_prices (dema_wrapper.rs:305); first_valid as in the crate. */
+vta_status vta_dema_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* dema_batch_into_host_f32 (dema_wrapper.rs:379); each output holds out_len >= rows*cols floats. */
+vta_status vta_dema_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* dema_many_series_one_param_time_major_dev (dema_wrapper.rs:516) */
+vta_status vta_dema_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* dema_many_series_one_param_device (dema_wrapper.rs:554) */
+vta_status vta_dema_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== tema (src/cuda/moving_averages/tema_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_tema_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* tema_batch_dev (tema_wrapper.rs:336) */
+vta_status vta_tema_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* tema_batch_device / _from_device_prices (tema_wrapper.rs:367); first_valid as in the crate. */
+vta_status vta_tema_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* tema_batch_into_host_f32 (tema_wrapper.rs:345); each output holds out_len >= rows*cols floats. */
+vta_status vta_tema_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* tema_many_series_one_param_time_major_dev (tema_wrapper.rs:430) */
+vta_status vta_tema_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* tema_many_series_one_param_device (tema_wrapper.rs:397) */
+vta_status vta_tema_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== rsi (src/cuda/rsi_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_rsi_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* rsi_batch_dev (rsi_wrapper.rs:152) */
+vta_status vta_rsi_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* rsi_batch_device / _from_device_prices (device-input form of rsi_wrapper.rs:152); first_valid as in the crate. */
+vta_status vta_rsi_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* rsi_batch_into_host_f32 (host-output form of rsi_wrapper.rs:152); each output holds out_len >= rows*cols floats. */
+vta_status vta_rsi_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* rsi_many_series_one_param_time_major_dev (rsi_wrapper.rs:271) */
+vta_status vta_rsi_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* rsi_many_series_one_param_device (device-input form of rsi_wrapper.rs:271) */
+vta_status vta_rsi_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== wilders (src/cuda/moving_averages/wilders_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_wilders_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* wilders_batch_dev (wilders_wrapper.rs:134) */
+vta_status vta_wilders_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* wilders_batch_device / _from_device_prices (wilders_wrapper.rs:252); first_valid as in the crate. */
+vta_status vta_wilders_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* wilders_batch_into_host_f32 (host-output form of wilders_wrapper.rs:134); each output holds out_len >= rows*cols floats. */
+vta_status vta_wilders_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* wilders_many_series_one_param_time_major_dev (wilders_wrapper.rs:600) */
+vta_status vta_wilders_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* wilders_many_series_one_param_device (wilders_wrapper.rs:662) */
+vta_status vta_wilders_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== sma (src/cuda/moving_averages/sma_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_sma_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* sma_batch_dev (sma_wrapper.rs:548) */
+vta_status vta_sma_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* sma_batch_device / _from_device_prices (sma_wrapper.rs:830); first_valid as in the crate. */
+vta_status vta_sma_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* sma_batch_into_host_f32 (sma_wrapper.rs:558); each output holds out_len >= rows*cols floats. */
+vta_status vta_sma_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* sma_many_series_one_param_time_major_dev (sma_wrapper.rs:750) */
+vta_status vta_sma_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* sma_many_series_one_param_device (sma_wrapper.rs:982) */
+vta_status vta_sma_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== wma (src/cuda/moving_averages/wma_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_wma_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* wma_batch_dev (wma_wrapper.rs:713) */
+vta_status vta_wma_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* wma_batch_device / _from_device_prices (wma_wrapper.rs:747); first_valid as in the crate. */
+vta_status vta_wma_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* wma_batch_into_host_f32 (wma_wrapper.rs:723); each output holds out_len >= rows*cols floats. */
+vta_status vta_wma_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* wma_many_series_one_param_time_major_dev (wma_wrapper.rs:1014) */
+vta_status vta_wma_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* wma_many_series_one_param_device (wma_wrapper.rs:1049) */
+vta_status vta_wma_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== swma (src/cuda/moving_averages/swma_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_swma_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* swma_batch_dev (swma_wrapper.rs:678) */
+vta_status vta_swma_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* swma_batch_device / _from_device_prices (swma_wrapper.rs:663); first_valid as in the crate. */
+vta_status vta_swma_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* swma_batch_into_host_f32 (host-output form of swma_wrapper.rs:678); each output holds out_len >= rows*cols floats. */
+vta_status vta_swma_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* swma_many_series_one_param_time_major_dev (swma_wrapper.rs:825) */
+vta_status vta_swma_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* swma_many_series_one_param_device (swma_wrapper.rs:787) */
+vta_status vta_swma_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== pwma (src/cuda/moving_averages/pwma_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_pwma_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* pwma_batch_dev (pwma_wrapper.rs:385) */
+vta_status vta_pwma_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* pwma_batch_device / _from_device_prices (pwma_wrapper.rs:369); first_valid as in the crate. */
+vta_status vta_pwma_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* pwma_batch_into_host_f32 (host-output form of pwma_wrapper.rs:385); each output holds out_len >= rows*cols floats. */
+vta_status vta_pwma_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* pwma_many_series_one_param_time_major_dev (pwma_wrapper.rs:723) */
+vta_status vta_pwma_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* pwma_many_series_one_param_device (pwma_wrapper.rs:696) */
+vta_status vta_pwma_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== sinwma (src/cuda/moving_averages/sinwma_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_sinwma_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* sinwma_batch_dev (sinwma_wrapper.rs:609) */
+vta_status vta_sinwma_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* sinwma_batch_device / _from_device_prices (sinwma_wrapper.rs:643); first_valid as in the crate. */
+vta_status vta_sinwma_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* sinwma_batch_into_host_f32 (sinwma_wrapper.rs:619); each output holds out_len >= rows*cols floats. */
+vta_status vta_sinwma_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* sinwma_many_series_one_param_time_major_dev (sinwma_wrapper.rs:841) */
+vta_status vta_sinwma_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* sinwma_many_series_one_param_device (sinwma_wrapper.rs:873) */
+vta_status vta_sinwma_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== trima (src/cuda/moving_averages/trima_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_trima_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* trima_batch_dev (trima_wrapper.rs:722) */
+vta_status vta_trima_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* trima_batch_device / _from_device_prices (trima_wrapper.rs:707); first_valid as in the crate. */
+vta_status vta_trima_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* trima_batch_into_host_f32 (host-output form of trima_wrapper.rs:722); each output holds out_len >= rows*cols floats. */
+vta_status vta_trima_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* trima_many_series_one_param_time_major_dev (trima_wrapper.rs:855) */
+vta_status vta_trima_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* trima_many_series_one_param_device (trima_wrapper.rs:829) */
+vta_status vta_trima_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== stddev (src/cuda/stddev_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_stddev_expand_grid(const vta_stddev_batch_range* sweep, vta_stddev_params* out, size_t cap, size_t* n_combos);
+/* stddev_batch_dev (stddev_wrapper.rs:509) */
+vta_status vta_stddev_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_stddev_batch_range* sweep, vta_device_array* out);
+/* stddev_batch_device / _from_device_prices (device-input form of stddev_wrapper.rs:509); first_valid as in the crate. */
+vta_status vta_stddev_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_stddev_batch_range* sweep, float* d_out);
+/* stddev_batch_into_host_f32 (stddev_wrapper.rs:606); each output holds out_len >= rows*cols floats. */
+vta_status vta_stddev_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_stddev_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* stddev_many_series_one_param_time_major_dev (stddev_wrapper.rs:630) */
+vta_status vta_stddev_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_stddev_params* params, vta_device_array* out);
+/* stddev_many_series_one_param_device (device-input form of stddev_wrapper.rs:630) */
+vta_status vta_stddev_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_stddev_params* params, float* d_out);
+
+/* ==== zscore (src/cuda/zscore_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_zscore_expand_grid(const vta_zscore_batch_range* sweep, vta_zscore_params* out, size_t cap, size_t* n_combos);
+/* zscore_batch_dev (zscore_wrapper.rs:620) */
+vta_status vta_zscore_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_zscore_batch_range* sweep, vta_device_array* out);
+/* zscore_batch_device / _from_device_prices (device-input form of zscore_wrapper.rs:620); first_valid as in the crate. */
+vta_status vta_zscore_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_zscore_batch_range* sweep, float* d_out);
+/* zscore_batch_into_host_f32 (zscore_wrapper.rs:663); each output holds out_len >= rows*cols floats. */
+vta_status vta_zscore_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_zscore_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* zscore_many_series_one_param_time_major_dev (zscore_wrapper.rs:720) */
+vta_status vta_zscore_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_zscore_params* params, vta_device_array* out);
+/* zscore_many_series_one_param_device (device-input form of zscore_wrapper.rs:720) */
+vta_status vta_zscore_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_zscore_params* params, float* d_out);
+
+/* ==== bollinger_bands (src/cuda/bollinger_bands_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_bollinger_bands_expand_grid(const vta_bollinger_batch_range* sweep, vta_bollinger_params* out, size_t cap, size_t* n_combos);
+/* bollinger_bands_batch_dev (bollinger_bands_wrapper.rs:567) */
+vta_status vta_bollinger_bands_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_bollinger_batch_range* sweep, vta_device_array* out_upper, vta_device_array* out_middle, vta_device_array* out_lower);
+/* bollinger_bands_batch_device / _from_device_prices (device-input form of bollinger_bands_wrapper.rs:567); first_valid as in the crate. */
+vta_status vta_bollinger_bands_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_bollinger_batch_range* sweep, float* d_out_upper, float* d_out_middle, float* d_out_lower);
+/* bollinger_bands_batch_into_host_f32 (host-output form of bollinger_bands_wrapper.rs:567); each output holds out_len >= rows*cols floats. */
+vta_status vta_bollinger_bands_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_bollinger_batch_range* sweep, float* out_upper, float* out_middle, float* out_lower, size_t out_len, size_t* rows, size_t* cols);
+/* bollinger_bands_many_series_one_param_time_major_dev (bollinger_bands_wrapper.rs:605) */
+vta_status vta_bollinger_bands_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_bollinger_params* params, vta_device_array* out_upper, vta_device_array* out_middle, vta_device_array* out_lower);
+/* bollinger_bands_many_series_one_param_device (device-input form of bollinger_bands_wrapper.rs:605) */
+vta_status vta_bollinger_bands_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_bollinger_params* params, float* d_out_upper, float* d_out_middle, float* d_out_lower);
+
+/* ==== atr (src/cuda/atr_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_atr_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* atr_batch_dev (atr_wrapper.rs:270) */
+vta_status vta_atr_batch_dev(vta_ctx* ctx, const float* high, const float* low, const float* close, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* atr_batch_device / _from_device_prices (atr_wrapper.rs:626); first_valid as in the crate. */
+vta_status vta_atr_batch_device(vta_ctx* ctx, const float* d_high, const float* d_low, const float* d_close, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* atr_batch_into_host_f32 (host-output form of atr_wrapper.rs:270); each output holds out_len >= rows*cols floats. */
+vta_status vta_atr_batch_into_host_f32(vta_ctx* ctx, const float* high, const float* low, const float* close, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* atr_many_series_one_param_time_major_dev (atr_wrapper.rs:834) */
+vta_status vta_atr_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* high_tm, const float* low_tm, const float* close_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* atr_many_series_one_param_device (device-input form of atr_wrapper.rs:834) */
+vta_status vta_atr_many_series_one_param_device(vta_ctx* ctx, const float* d_high_tm, const float* d_low_tm, const float* d_close_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== adx (src/cuda/adx_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_adx_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* adx_batch_dev (adx_wrapper.rs:199) */
+vta_status vta_adx_batch_dev(vta_ctx* ctx, const float* high, const float* low, const float* close, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* adx_batch_device / _from_device_prices (device-input form of adx_wrapper.rs:199); first_valid as in the crate. */
+vta_status vta_adx_batch_device(vta_ctx* ctx, const float* d_high, const float* d_low, const float* d_close, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* adx_batch_into_host_f32 (adx_wrapper.rs:253); each output holds out_len >= rows*cols floats. */
+vta_status vta_adx_batch_into_host_f32(vta_ctx* ctx, const float* high, const float* low, const float* close, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* adx_many_series_one_param_time_major_dev (adx_wrapper.rs:340) */
+vta_status vta_adx_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* high_tm, const float* low_tm, const float* close_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* adx_many_series_one_param_device (device-input form of adx_wrapper.rs:340) */
+vta_status vta_adx_many_series_one_param_device(vta_ctx* ctx, const float* d_high_tm, const float* d_low_tm, const float* d_close_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== supertrend (src/cuda/supertrend_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_supertrend_expand_grid(const vta_supertrend_batch_range* sweep, vta_supertrend_params* out, size_t cap, size_t* n_combos);
+/* supertrend_batch_dev (supertrend_wrapper.rs:179) */
+vta_status vta_supertrend_batch_dev(vta_ctx* ctx, const float* high, const float* low, const float* close, size_t len,
+    const vta_supertrend_batch_range* sweep, vta_device_array* out_trend, vta_device_array* out_changed);
+/* supertrend_batch_device / _from_device_prices (device-input form of supertrend_wrapper.rs:179); first_valid as in the crate. */
+vta_status vta_supertrend_batch_device(vta_ctx* ctx, const float* d_high, const float* d_low, const float* d_close, size_t len,
+    size_t first_valid, const vta_supertrend_batch_range* sweep, float* d_out_trend, float* d_out_changed);
+/* supertrend_batch_into_host_f32 (host-output form of supertrend_wrapper.rs:179); each output holds out_len >= rows*cols floats. */
+vta_status vta_supertrend_batch_into_host_f32(vta_ctx* ctx, const float* high, const float* low, const float* close, size_t len,
+    const vta_supertrend_batch_range* sweep, float* out_trend, float* out_changed, size_t out_len, size_t* rows, size_t* cols);
+/* supertrend_many_series_one_param_time_major_dev (supertrend_wrapper.rs:337) */
+vta_status vta_supertrend_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* high_tm, const float* low_tm, const float* close_tm,
+    size_t cols, size_t rows, const vta_supertrend_params* params, vta_device_array* out_trend, vta_device_array* out_changed);
+/* supertrend_many_series_one_param_device (device-input form of supertrend_wrapper.rs:337) */
+vta_status vta_supertrend_many_series_one_param_device(vta_ctx* ctx, const float* d_high_tm, const float* d_low_tm, const float* d_close_tm,
+    size_t cols, size_t rows, const vta_supertrend_params* params, float* d_out_trend, float* d_out_changed);
+
+/* ==== donchian (src/cuda/donchian_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_donchian_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* donchian_batch_dev (donchian_wrapper.rs:344) */
+vta_status vta_donchian_batch_dev(vta_ctx* ctx, const float* high, const float* low, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out_upper, vta_device_array* out_middle, vta_device_array* out_lower);
+/* donchian_batch_device / _from_device_prices (device-input form of donchian_wrapper.rs:344); first_valid as in the crate. */
+vta_status vta_donchian_batch_device(vta_ctx* ctx, const float* d_high, const float* d_low, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out_upper, float* d_out_middle, float* d_out_lower);
+/* donchian_batch_into_host_f32 (host-output form of donchian_wrapper.rs:344); each output holds out_len >= rows*cols floats. */
+vta_status vta_donchian_batch_into_host_f32(vta_ctx* ctx, const float* high, const float* low, size_t len,
+    const vta_period_batch_range* sweep, float* out_upper, float* out_middle, float* out_lower, size_t out_len, size_t* rows, size_t* cols);
+/* donchian_many_series_one_param_time_major_dev (donchian_wrapper.rs:593) */
+vta_status vta_donchian_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* high_tm, const float* low_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out_upper, vta_device_array* out_middle, vta_device_array* out_lower);
+/* donchian_many_series_one_param_device (device-input form of donchian_wrapper.rs:593) */
+vta_status vta_donchian_many_series_one_param_device(vta_ctx* ctx, const float* d_high_tm, const float* d_low_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out_upper, float* d_out_middle, float* d_out_lower);
+
+/* ==== willr (src/cuda/willr_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_willr_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* willr_batch_dev (willr_wrapper.rs:132) */
+vta_status vta_willr_batch_dev(vta_ctx* ctx, const float* high, const float* low, const float* close, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* willr_batch_device / _from_device_prices (willr_wrapper.rs:236); first_valid as in the crate. */
+vta_status vta_willr_batch_device(vta_ctx* ctx, const float* d_high, const float* d_low, const float* d_close, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* willr_batch_into_host_f32 (host-output form of willr_wrapper.rs:132); each output holds out_len >= rows*cols floats. */
+vta_status vta_willr_batch_into_host_f32(vta_ctx* ctx, const float* high, const float* low, const float* close, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* willr_many_series_one_param_time_major_dev (willr_wrapper.rs:583) */
+vta_status vta_willr_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* high_tm, const float* low_tm, const float* close_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* willr_many_series_one_param_device (willr_wrapper.rs:642) */
+vta_status vta_willr_many_series_one_param_device(vta_ctx* ctx, const float* d_high_tm, const float* d_low_tm, const float* d_close_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== percentile_nearest_rank (src/cuda/percentile_nearest_rank_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_percentile_nearest_rank_expand_grid(const vta_percentile_batch_range* sweep, vta_percentile_params* out, size_t cap, size_t* n_combos);
+/* percentile_nearest_rank_batch_dev (percentile_nearest_rank_wrapper.rs:365) */
+vta_status vta_percentile_nearest_rank_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_percentile_batch_range* sweep, vta_device_array* out);
+/* percentile_nearest_rank_batch_device / _from_device_prices (device-input form of percentile_nearest_rank_wrapper.rs:365); first_valid as in the crate. */
+vta_status vta_percentile_nearest_rank_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_percentile_batch_range* sweep, float* d_out);
+/* percentile_nearest_rank_batch_into_host_f32 (host-output form of percentile_nearest_rank_wrapper.rs:365); each output holds out_len >= rows*cols floats. */
+vta_status vta_percentile_nearest_rank_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_percentile_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* percentile_nearest_rank_many_series_one_param_time_major_dev (percentile_nearest_rank_wrapper.rs:623) */
+vta_status vta_percentile_nearest_rank_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_percentile_params* params, vta_device_array* out);
+/* percentile_nearest_rank_many_series_one_param_device (device-input form of percentile_nearest_rank_wrapper.rs:623) */
+vta_status vta_percentile_nearest_rank_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_percentile_params* params, float* d_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VTA_GB300_H */

@@ -1,0 +1,167 @@
+"""Loads libvta_gb300.so (built in-tree by vectorta_gb300/build.py) and
+declares the ctypes signatures of its C ABI (include/vta_gb300.h).
+
+There is no CPU fallback: if the library is missing this module raises, and
+every GPU entry point returns an error status when no sm_103a device exists.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "_lib", "libvta_gb300.so")
+HEADER = os.path.join(ROOT, "include", "vta_gb300.h")
+
+STATUS = {
+    0: "OK", 1: "Cuda", 2: "OutOfMemory", 3: "MissingKernelSymbol", 4: "InvalidInput",
+    5: "InvalidPolicy", 6: "LaunchConfigTooLarge", 7: "DeviceMismatch", 8: "NotImplemented",
+}
+
+
+class VtaError(RuntimeError):
+    """Mirrors the crate's CudaXError enums: `kind` is the variant name."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        self.kind = STATUS.get(status, f"status{status}")
+        super().__init__(f"{self.kind}: {message}")
+
+
+class RangeUsize(C.Structure):
+    _fields_ = [("start", C.c_size_t), ("end", C.c_size_t), ("step", C.c_size_t)]
+
+
+class RangeF64(C.Structure):
+    _fields_ = [("start", C.c_double), ("end", C.c_double), ("step", C.c_double)]
+
+
+class DeviceArrayC(C.Structure):
+    _fields_ = [("ptr", C.c_void_p), ("rows", C.c_size_t), ("cols", C.c_size_t), ("device", C.c_int)]
+
+
+# sweep / params structs (field order as in the header)
+def _struct(name, fields):
+    return type(name, (C.Structure,), {"_fields_": fields})
+
+
+SWEEPS = {
+    "alma": _struct("vta_alma_batch_range", [("period", RangeUsize), ("offset", RangeF64), ("sigma", RangeF64)]),
+    "period": _struct("vta_period_batch_range", [("period", RangeUsize)]),
+    "stddev": _struct("vta_stddev_batch_range", [("period", RangeUsize), ("nbdev", RangeF64)]),
+    "zscore": _struct("vta_zscore_batch_range", [("period", RangeUsize), ("nbdev", RangeF64)]),
+    "bollinger": _struct("vta_bollinger_batch_range",
+                         [("period", RangeUsize), ("devup", RangeF64), ("devdn", RangeF64)]),
+    "supertrend": _struct("vta_supertrend_batch_range", [("period", RangeUsize), ("factor", RangeF64)]),
+    "percentile": _struct("vta_percentile_batch_range", [("length", RangeUsize), ("percentage", RangeF64)]),
+}
+PARAMS = {
+    "alma": _struct("vta_alma_params", [("period", C.c_size_t), ("offset", C.c_double), ("sigma", C.c_double)]),
+    "period": _struct("vta_period_params", [("period", C.c_size_t)]),
+    "stddev": _struct("vta_stddev_params", [("period", C.c_size_t), ("nbdev", C.c_double)]),
+    "zscore": _struct("vta_zscore_params", [("period", C.c_size_t), ("nbdev", C.c_double)]),
+    "bollinger": _struct("vta_bollinger_params",
+                         [("period", C.c_size_t), ("devup", C.c_double), ("devdn", C.c_double)]),
+    "supertrend": _struct("vta_supertrend_params", [("period", C.c_size_t), ("factor", C.c_double)]),
+    "percentile": _struct("vta_percentile_params", [("length", C.c_size_t), ("percentage", C.c_double)]),
+}
+
+# name -> (input kind, outputs, sweep/params family)
+INDICATORS = {
+    "alma": ("x", ["out"], "alma"),
+    "ema": ("x", ["out"], "period"),
+    "dema": ("x", ["out"], "period"),
+    "tema": ("x", ["out"], "period"),
+    "rsi": ("x", ["out"], "period"),
+    "wilders": ("x", ["out"], "period"),
+    "sma": ("x", ["out"], "period"),
+    "wma": ("x", ["out"], "period"),
+    "swma": ("x", ["out"], "period"),
+    "pwma": ("x", ["out"], "period"),
+    "sinwma": ("x", ["out"], "period"),
+    "trima": ("x", ["out"], "period"),
+    "stddev": ("x", ["out"], "stddev"),
+    "zscore": ("x", ["out"], "zscore"),
+    "bollinger_bands": ("x", ["upper", "middle", "lower"], "bollinger"),
+    "atr": ("hlc", ["out"], "period"),
+    "adx": ("hlc", ["out"], "period"),
+    "supertrend": ("hlc", ["trend", "changed"], "supertrend"),
+    "donchian": ("hl", ["upper", "middle", "lower"], "period"),
+    "willr": ("hlc", ["out"], "period"),
+    "percentile_nearest_rank": ("x", ["out"], "percentile"),
+}
+N_IN = {"x": 1, "hl": 2, "hlc": 3}
+
+_lib = None
+
+
+def header_symbols() -> list[str]:
+    """Every function the public header declares."""
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const char\*|vta_status|int|void\*|size_t)\s+(vta_\w+)\s*\(",
+                                 text, re.M)))
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"libvta_gb300.so not built ({LIB_PATH}); run vectorta_gb300.build.build()")
+    L = C.CDLL(LIB_PATH)
+    vp, sz, st = C.c_void_p, C.c_size_t, C.c_int
+    fp = C.POINTER(C.c_float)
+    L.vta_last_error.restype = C.c_char_p
+    L.vta_version.restype = C.c_char_p
+    L.vta_device_count.restype = C.c_int
+    L.vta_ctx_create.argtypes = [C.c_int, C.POINTER(vp)]
+    L.vta_ctx_destroy.argtypes = [vp]
+    L.vta_ctx_synchronize.argtypes = [vp]
+    L.vta_ctx_set_stream.argtypes = [vp, vp]
+    L.vta_ctx_get_stream.argtypes = [vp]
+    L.vta_ctx_get_stream.restype = vp
+    L.vta_ctx_set_policy.argtypes = [vp, C.c_char_p, C.c_char_p]
+    L.vta_ctx_last_kernel.argtypes = [vp]
+    L.vta_ctx_last_kernel.restype = C.c_char_p
+    L.vta_ctx_scratch_bytes.argtypes = [vp]
+    L.vta_ctx_scratch_bytes.restype = sz
+    L.vta_device_array_free.argtypes = [C.POINTER(DeviceArrayC)]
+    L.vta_device_array_copy_to_host.argtypes = [vp, C.POINTER(DeviceArrayC), fp, sz]
+    L.vta_pinned_alloc.argtypes = [sz, C.POINTER(vp)]
+    L.vta_pinned_free.argtypes = [vp]
+    L.vta_device_alloc.argtypes = [vp, sz, C.POINTER(vp)]
+    L.vta_device_free.argtypes = [vp, vp]
+    L.vta_memcpy_h2d.argtypes = [vp, vp, vp, sz]
+    L.vta_memcpy_d2h.argtypes = [vp, vp, vp, sz]
+    for name, (kind, outs, fam) in INDICATORS.items():
+        R, P = C.POINTER(SWEEPS[fam]), C.POINTER(PARAMS[fam])
+        nin, nout = N_IN[kind], len(outs)
+        da = C.POINTER(DeviceArrayC)
+        f = getattr(L, f"vta_{name}_expand_grid")
+        f.argtypes = [R, P, sz, C.POINTER(sz)]
+        getattr(L, f"vta_{name}_batch_dev").argtypes = [vp] + [vp] * nin + [sz, R] + [da] * nout
+        getattr(L, f"vta_{name}_batch_device").argtypes = [vp] + [vp] * nin + [sz, sz, R] + [vp] * nout
+        getattr(L, f"vta_{name}_batch_into_host_f32").argtypes = (
+            [vp] + [vp] * nin + [sz, R] + [vp] * nout + [sz, C.POINTER(sz), C.POINTER(sz)])
+        getattr(L, f"vta_{name}_many_series_one_param_time_major_dev").argtypes = (
+            [vp] + [vp] * nin + [sz, sz, P] + [da] * nout)
+        getattr(L, f"vta_{name}_many_series_one_param_device").argtypes = (
+            [vp] + [vp] * nin + [sz, sz, P] + [vp] * nout)
+        for suffix in ("expand_grid", "batch_dev", "batch_device", "batch_into_host_f32",
+                       "many_series_one_param_time_major_dev", "many_series_one_param_device"):
+            getattr(L, f"vta_{name}_{suffix}").restype = st
+    for fn in ("vta_ctx_create", "vta_ctx_destroy", "vta_ctx_synchronize", "vta_ctx_set_stream",
+               "vta_ctx_set_policy", "vta_device_array_free", "vta_device_array_copy_to_host",
+               "vta_pinned_alloc", "vta_pinned_free", "vta_device_alloc", "vta_device_free",
+               "vta_memcpy_h2d", "vta_memcpy_d2h"):
+        getattr(L, fn).restype = st
+    _lib = L
+    return L
+
+
+def check(status: int):
+    if status != 0:
+        msg = lib().vta_last_error()
+        raise VtaError(status, msg.decode() if msg else "")

@@ -1,0 +1,255 @@
+"""Generates the C ABI of the library from one table of indicators:
+
+* include/vta_gb300.h                      -- the public declarations;
+* vectorta_gb300/csrc/vta_abi_gen.inc      -- the extern "C" definitions that
+  forward each entry point to the generic drivers in vta_api.cu.
+
+Run from the repository root after changing the table:
+    python vectorta_gb300/csrc/gen_abi.py
+"""
+IND = [
+ # name, wrapper file, input kind, outputs, range type, params type, cites (new, batch_dev, batch_device, into_host, tm_dev, tm_device)
+ ("alma","src/cuda/moving_averages/alma_wrapper.rs","x",["out"],"alma","alma",(133,625,671,783,819,1521)),
+ ("ema","src/cuda/moving_averages/ema_wrapper.rs","x",["out"],"period","period",(125,193,256,309,325,381)),
+ ("dema","src/cuda/moving_averages/dema_wrapper.rs","x",["out"],"period","period",(115,219,305,379,516,554)),
+ ("tema","src/cuda/moving_averages/tema_wrapper.rs","x",["out"],"period","period",(159,336,367,345,430,397)),
+ ("rsi","src/cuda/rsi_wrapper.rs","x",["out"],"period","period",(62,152,None,None,271,None)),
+ ("wilders","src/cuda/moving_averages/wilders_wrapper.rs","x",["out"],"period","period",(101,134,252,None,600,662)),
+ ("sma","src/cuda/moving_averages/sma_wrapper.rs","x",["out"],"period","period",(56,548,830,558,750,982)),
+ ("wma","src/cuda/moving_averages/wma_wrapper.rs","x",["out"],"period","period",(151,713,747,723,1014,1049)),
+ ("swma","src/cuda/moving_averages/swma_wrapper.rs","x",["out"],"period","period",(121,678,663,None,825,787)),
+ ("pwma","src/cuda/moving_averages/pwma_wrapper.rs","x",["out"],"period","period",(93,385,369,None,723,696)),
+ ("sinwma","src/cuda/moving_averages/sinwma_wrapper.rs","x",["out"],"period","period",(116,609,643,619,841,873)),
+ ("trima","src/cuda/moving_averages/trima_wrapper.rs","x",["out"],"period","period",(123,722,707,None,855,829)),
+ ("stddev","src/cuda/stddev_wrapper.rs","x",["out"],"stddev","stddev",(101,509,None,606,630,None)),
+ ("zscore","src/cuda/zscore_wrapper.rs","x",["out"],"zscore","zscore",(86,620,None,663,720,None)),
+ ("bollinger_bands","src/cuda/bollinger_bands_wrapper.rs","x",["out_upper","out_middle","out_lower"],"bollinger","bollinger",(85,567,None,None,605,None)),
+ ("atr","src/cuda/atr_wrapper.rs","hlc",["out"],"period","period",(110,270,626,None,834,None)),
+ ("adx","src/cuda/adx_wrapper.rs","hlc",["out"],"period","period",(88,199,None,253,340,None)),
+ ("supertrend","src/cuda/supertrend_wrapper.rs","hlc",["out_trend","out_changed"],"supertrend","supertrend",(88,179,None,None,337,None)),
+ ("donchian","src/cuda/donchian_wrapper.rs","hl",["out_upper","out_middle","out_lower"],"period","period",(128,344,None,None,593,None)),
+ ("willr","src/cuda/willr_wrapper.rs","hlc",["out"],"period","period",(75,132,236,None,583,642)),
+ ("percentile_nearest_rank","src/cuda/percentile_nearest_rank_wrapper.rs","x",["out"],"percentile","percentile",(99,365,None,None,623,None)),
+]
+RANGES = {
+ "alma": ("vta_alma_batch_range", "vta_alma_params"),
+ "period": ("vta_period_batch_range", "vta_period_params"),
+ "stddev": ("vta_stddev_batch_range", "vta_stddev_params"),
+ "zscore": ("vta_zscore_batch_range", "vta_zscore_params"),
+ "bollinger": ("vta_bollinger_batch_range", "vta_bollinger_params"),
+ "supertrend": ("vta_supertrend_batch_range", "vta_supertrend_params"),
+ "percentile": ("vta_percentile_batch_range", "vta_percentile_params"),
+}
+def inputs(kind, dev, tm):
+    pre = "d_" if dev else ""
+    suf = "_tm" if tm else ""
+    if kind == "x": return [f"const float* {pre}data{suf}"]
+    if kind == "hl": return [f"const float* {pre}high{suf}", f"const float* {pre}low{suf}"]
+    return [f"const float* {pre}high{suf}", f"const float* {pre}low{suf}", f"const float* {pre}close{suf}"]
+
+out = []
+w = out.append
+w("""/*
+ * vta_gb300.h -- C ABI of the GB300-native VectorTA indicator hot path.
+ *
+ * One shared library (libvta_gb300.so) replaces the crate's per-indicator CUDA
+ * wrappers (the src/cuda X_wrapper.rs files: `CudaX` structs driving PTX through
+ * `cust`).  Every entry point is plain C: host or device pointers, sizes and
+ * small parameter structs; no CUDA, torch or Rust types cross the boundary.
+ *
+ * Conventions (the crate's, kept so existing callers port one-to-one):
+ *   - batch ("one series, many params"): output is row-major
+ *     [n_combos][len], rows in the crate's expand_grid order (period-major);
+ *   - many-series ("time-major"): input and output are [rows][cols] with
+ *     element (t, s) at t*cols + s; one parameter set for all series;
+ *   - warm-up cells are quiet NaN at exactly the crate's positions;
+ *   - *_dev functions take host inputs and return device arrays owned by the
+ *     caller (free with vta_device_array_free); *_device functions take device
+ *     inputs and write into caller-provided device outputs (the crate's
+ *     x_batch_device / x_many_series_one_param_device); *_into_host_f32
+ *     writes host outputs (the crate's x_batch_into_host_f32);
+ *   - every call is stream-ordered on the context's stream and synchronous on
+ *     return, like the crate's wrappers (which end with stream.synchronize()).
+ * Thread safety: a vta_ctx is used by one thread at a time (as a CudaX is).
+ */
+#ifndef VTA_GB300_H
+#define VTA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes map the crate's CudaXError variants one-to-one
+ * (src/cuda/moving_averages/alma_wrapper.rs:72-101). */
+typedef enum vta_status {
+    VTA_OK = 0,
+    VTA_ERR_CUDA = 1,                   /* Cuda(CudaError) */
+    VTA_ERR_OUT_OF_MEMORY = 2,          /* OutOfMemory{required, free, headroom} */
+    VTA_ERR_MISSING_KERNEL_SYMBOL = 3,  /* MissingKernelSymbol{name} */
+    VTA_ERR_INVALID_INPUT = 4,          /* InvalidInput(String) */
+    VTA_ERR_INVALID_POLICY = 5,         /* InvalidPolicy(&str) */
+    VTA_ERR_LAUNCH_CONFIG_TOO_LARGE = 6,/* LaunchConfigTooLarge{grid, block} */
+    VTA_ERR_DEVICE_MISMATCH = 7,        /* DeviceMismatch{buf, current} */
+    VTA_ERR_NOT_IMPLEMENTED = 8         /* NotImplemented */
+} vta_status;
+
+/* Message of the last failure on the calling thread (the Display text of the
+ * crate's error enums). */
+const char* vta_last_error(void);
+const char* vta_version(void);
+
+/* Number of CUDA devices (crate: cuda_device_count, src/cuda/mod.rs:560-575);
+ * 0 when no driver or device is present. */
+int vta_device_count(void);
+
+/* ---- context: CudaX::new(device_id) (alma_wrapper.rs:133-169) ---------- */
+typedef struct vta_ctx vta_ctx;
+vta_status vta_ctx_create(int device_id, vta_ctx** out);
+vta_status vta_ctx_destroy(vta_ctx* ctx);
+/* CudaX::synchronize (alma_wrapper.rs:171-173). */
+vta_status vta_ctx_synchronize(vta_ctx* ctx);
+/* Run on a caller-owned cudaStream_t instead of the context's own stream
+ * (NULL restores the context stream). */
+vta_status vta_ctx_set_stream(vta_ctx* ctx, void* cuda_stream);
+void* vta_ctx_get_stream(vta_ctx* ctx);
+/* CudaXPolicy / set_policy (alma_wrapper.rs:18-70): keys
+ *   "wma_batch"   = "auto" | "plain" | "tc_fp16x3" | "tc_bf16x3"
+ *   "recur_chunk" = "auto" | "sequential" | <positive multiple of 32>     */
+vta_status vta_ctx_set_policy(vta_ctx* ctx, const char* key, const char* value);
+/* selected_batch_kernel() (alma_wrapper.rs:239-245): name of the last kernel
+ * path used by this context. */
+const char* vta_ctx_last_kernel(vta_ctx* ctx);
+/* Device workspace currently held by the context (bytes). */
+size_t vta_ctx_scratch_bytes(vta_ctx* ctx);
+
+/* ---- device arrays: DeviceArrayF32 (alma_wrapper.rs:103-117) ----------- */
+typedef struct vta_device_array {
+    float* ptr;     /* device pointer, rows*cols floats, owned */
+    size_t rows;
+    size_t cols;
+    int device;
+} vta_device_array;
+vta_status vta_device_array_free(vta_device_array* arr);
+vta_status vta_device_array_copy_to_host(vta_ctx* ctx, const vta_device_array* arr,
+                                         float* host, size_t n);
+
+/* Page-locked host buffers for fast copies (the crate's LockedBuffer,
+ * alma_wrapper.rs:810-815). */
+vta_status vta_pinned_alloc(size_t bytes, void** out);
+vta_status vta_pinned_free(void* p);
+/* Plain device buffers for callers without their own allocator. */
+vta_status vta_device_alloc(vta_ctx* ctx, size_t bytes, void** out);
+vta_status vta_device_free(vta_ctx* ctx, void* p);
+vta_status vta_memcpy_h2d(vta_ctx* ctx, void* dst, const void* src, size_t bytes);
+vta_status vta_memcpy_d2h(vta_ctx* ctx, void* dst, const void* src, size_t bytes);
+
+/* ---- parameter sweeps: (start, end, step) like the crate's BatchRange --- */
+typedef struct vta_range_usize { size_t start, end, step; } vta_range_usize;
+typedef struct vta_range_f64 { double start, end, step; } vta_range_f64;
+
+/* AlmaBatchRange / AlmaParams (alma.rs:66-80, 1068-1082) */
+typedef struct vta_alma_batch_range { vta_range_usize period; vta_range_f64 offset, sigma; } vta_alma_batch_range;
+typedef struct vta_alma_params { size_t period; double offset, sigma; } vta_alma_params;
+/* period-only sweeps: EMA, DEMA, TEMA, RSI, Wilders, SMA, WMA, SWMA, PWMA,
+ * SINWMA, TRIMA, ATR (`length`), ADX, Donchian, WillR */
+typedef struct vta_period_batch_range { vta_range_usize period; } vta_period_batch_range;
+typedef struct vta_period_params { size_t period; } vta_period_params;
+/* StdDevBatchRange (stddev.rs:573-585) */
+typedef struct vta_stddev_batch_range { vta_range_usize period; vta_range_f64 nbdev; } vta_stddev_batch_range;
+typedef struct vta_stddev_params { size_t period; double nbdev; } vta_stddev_params;
+/* ZscoreBatchRange (zscore.rs:786-802), ma_type "sma" and devtype 0 */
+typedef struct vta_zscore_batch_range { vta_range_usize period; vta_range_f64 nbdev; } vta_zscore_batch_range;
+typedef struct vta_zscore_params { size_t period; double nbdev; } vta_zscore_params;
+/* BollingerBandsBatchRange (bollinger_bands.rs:1087-1104), matype "sma", devtype 0 */
+typedef struct vta_bollinger_batch_range { vta_range_usize period; vta_range_f64 devup, devdn; } vta_bollinger_batch_range;
+typedef struct vta_bollinger_params { size_t period; double devup, devdn; } vta_bollinger_params;
+/* SuperTrendBatchRange (supertrend.rs:1223-1300) */
+typedef struct vta_supertrend_batch_range { vta_range_usize period; vta_range_f64 factor; } vta_supertrend_batch_range;
+typedef struct vta_supertrend_params { size_t period; double factor; } vta_supertrend_params;
+/* PercentileNearestRankBatchRange (percentile_nearest_rank.rs:815-827) */
+typedef struct vta_percentile_batch_range { vta_range_usize length; vta_range_f64 percentage; } vta_percentile_batch_range;
+typedef struct vta_percentile_params { size_t length; double percentage; } vta_percentile_params;
+""")
+for (name, wf, kind, outs, rng, prm, cites) in IND:
+    R, P = RANGES[rng]
+    c_new, c_bd, c_bdev, c_ih, c_tm, c_tmd = cites
+    wn = wf.split("/")[-1]
+    w(f"/* ==== {name} ({wf}) ==== */")
+    w(f"/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */")
+    w(f"vta_status vta_{name}_expand_grid(const {R}* sweep, {P}* out, size_t cap, size_t* n_combos);")
+    outs_dev = ", ".join(f"vta_device_array* {o}" for o in outs)
+    w(f"/* {name}_batch_dev ({wn}:{c_bd}) */")
+    w(f"vta_status vta_{name}_batch_dev(vta_ctx* ctx, {', '.join(inputs(kind, False, False))}, size_t len,\n    const {R}* sweep, {outs_dev});")
+    cite = f"{wn}:{c_bdev}" if c_bdev else f"device-input form of {wn}:{c_bd}"
+    outs_d = ", ".join(f"float* d_{o}" for o in outs)
+    w(f"/* {name}_batch_device / _from_device_prices ({cite}); first_valid as in the crate. */")
+    w(f"vta_status vta_{name}_batch_device(vta_ctx* ctx, {', '.join(inputs(kind, True, False))}, size_t len,\n    size_t first_valid, const {R}* sweep, {outs_d});")
+    cite = f"{wn}:{c_ih}" if c_ih else f"host-output form of {wn}:{c_bd}"
+    outs_h = ", ".join(f"float* {o}" for o in outs)
+    w(f"/* {name}_batch_into_host_f32 ({cite}); each output holds out_len >= rows*cols floats. */")
+    w(f"vta_status vta_{name}_batch_into_host_f32(vta_ctx* ctx, {', '.join(inputs(kind, False, False))}, size_t len,\n    const {R}* sweep, {outs_h}, size_t out_len, size_t* rows, size_t* cols);")
+    w(f"/* {name}_many_series_one_param_time_major_dev ({wn}:{c_tm}) */")
+    w(f"vta_status vta_{name}_many_series_one_param_time_major_dev(vta_ctx* ctx, {', '.join(inputs(kind, False, True))},\n    size_t cols, size_t rows, const {P}* params, {outs_dev});")
+    cite = f"{wn}:{c_tmd}" if c_tmd else f"device-input form of {wn}:{c_tm}"
+    w(f"/* {name}_many_series_one_param_device ({cite}) */")
+    w(f"vta_status vta_{name}_many_series_one_param_device(vta_ctx* ctx, {', '.join(inputs(kind, True, True))},\n    size_t cols, size_t rows, const {P}* params, {outs_d});")
+    w("")
+w("""#ifdef __cplusplus
+}
+#endif
+
+#endif /* VTA_GB300_H */""")
+open("include/vta_gb300.h","w").write("\n".join(out)+"\n")
+
+# ---------------------------------------------------------------- .inc ----
+ENUM = {"alma":"I_ALMA","ema":"I_EMA","dema":"I_DEMA","tema":"I_TEMA","rsi":"I_RSI","wilders":"I_WILDERS",
+        "sma":"I_SMA","wma":"I_WMA","swma":"I_SWMA","pwma":"I_PWMA","sinwma":"I_SINWMA","trima":"I_TRIMA",
+        "stddev":"I_STDDEV","zscore":"I_ZSCORE","bollinger_bands":"I_BB","atr":"I_ATR","adx":"I_ADX",
+        "supertrend":"I_SUPERTREND","donchian":"I_DONCHIAN","willr":"I_WILLR",
+        "percentile_nearest_rank":"I_PNR"}
+def names(kind, dev, tm):
+    return [a.split()[-1] for a in inputs(kind, dev, tm)]
+inc = ["// Generated by gen_abi.py: extern \"C\" entry points forwarding to the drivers of",
+       "// vta_api.cu (included inside its extern \"C\" block).  Do not edit by hand.", ""]
+for (name, wf, kind, outs, rng, prm, cites) in IND:
+    R, P = RANGES[rng]
+    E = ENUM[name]
+    ih = ", ".join(inputs(kind, False, False)); id_ = ", ".join(inputs(kind, True, False))
+    ith = ", ".join(inputs(kind, False, True)); itd = ", ".join(inputs(kind, True, True))
+    nh = ", ".join(names(kind, False, False)); nd = ", ".join(names(kind, True, False))
+    nth = ", ".join(names(kind, False, True)); ntd = ", ".join(names(kind, True, True))
+    oa = ", ".join(f"vta_device_array* {o}" for o in outs)
+    od = ", ".join(f"float* d_{o}" for o in outs)
+    oh = ", ".join(f"float* {o}" for o in outs)
+    on = ", ".join(outs); odn = ", ".join(f"d_{o}" for o in outs)
+    inc.append(f"vta_status vta_{name}_expand_grid(const {R}* sweep, {P}* out, size_t cap, size_t* n_combos) {{")
+    inc.append(f"    return expand({E}, sweep, out, cap, n_combos);\n}}")
+    inc.append(f"vta_status vta_{name}_batch_dev(vta_ctx* ctx, {ih}, size_t len, const {R}* sweep, {oa}) {{")
+    inc.append(f"    if (!sweep) return fail(VTA_ERR_INVALID_INPUT, \"null sweep\");")
+    inc.append(f"    const float* in[] = {{{nh}}};\n    vta_device_array* outs[] = {{{on}}};")
+    inc.append(f"    for (vta_device_array* o : outs) if (!o) return fail(VTA_ERR_INVALID_INPUT, \"null output\");")
+    inc.append(f"    return batch_host(ctx, {E}, in, len, grid_of({E}, sweep), outs, nullptr, 0, nullptr, nullptr);\n}}")
+    inc.append(f"vta_status vta_{name}_batch_device(vta_ctx* ctx, {id_}, size_t len, size_t first_valid, const {R}* sweep, {od}) {{")
+    inc.append(f"    if (!sweep) return fail(VTA_ERR_INVALID_INPUT, \"null sweep\");")
+    inc.append(f"    const float* in[] = {{{nd}}};\n    float* outs[] = {{{odn}}};")
+    inc.append(f"    return batch_device(ctx, {E}, in, len, first_valid, grid_of({E}, sweep), outs);\n}}")
+    inc.append(f"vta_status vta_{name}_batch_into_host_f32(vta_ctx* ctx, {ih}, size_t len, const {R}* sweep, {oh}, size_t out_len, size_t* rows, size_t* cols) {{")
+    inc.append(f"    if (!sweep) return fail(VTA_ERR_INVALID_INPUT, \"null sweep\");")
+    inc.append(f"    const float* in[] = {{{nh}}};\n    float* outs[] = {{{on}}};")
+    inc.append(f"    for (float* o : outs) if (!o) return fail(VTA_ERR_INVALID_INPUT, \"null output\");")
+    inc.append(f"    return batch_host(ctx, {E}, in, len, grid_of({E}, sweep), nullptr, outs, out_len, rows, cols);\n}}")
+    inc.append(f"vta_status vta_{name}_many_series_one_param_time_major_dev(vta_ctx* ctx, {ith}, size_t cols, size_t rows, const {P}* params, {oa}) {{")
+    inc.append(f"    if (!params) return fail(VTA_ERR_INVALID_INPUT, \"null params\");")
+    inc.append(f"    const float* in[] = {{{nth}}};\n    vta_device_array* outs[] = {{{on}}};")
+    inc.append(f"    for (vta_device_array* o : outs) if (!o) return fail(VTA_ERR_INVALID_INPUT, \"null output\");")
+    inc.append(f"    return tm_host(ctx, {E}, in, cols, rows, combo_of(params), outs);\n}}")
+    inc.append(f"vta_status vta_{name}_many_series_one_param_device(vta_ctx* ctx, {itd}, size_t cols, size_t rows, const {P}* params, {od}) {{")
+    inc.append(f"    if (!params) return fail(VTA_ERR_INVALID_INPUT, \"null params\");")
+    inc.append(f"    const float* in[] = {{{ntd}}};\n    float* outs[] = {{{odn}}};")
+    inc.append(f"    return tm_device(ctx, {E}, in, cols, rows, combo_of(params), outs);\n}}")
+    inc.append("")
+open("vectorta_gb300/csrc/vta_abi_gen.inc","w").write("\n".join(inc)+"\n")
+print("ok")

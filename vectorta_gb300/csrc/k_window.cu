@@ -1,0 +1,501 @@
+// Window indicators: prefix-sum windows (SMA, StdDev, Z-score, Bollinger),
+// sliding min/max (Donchian, Williams %R) and nearest-rank percentile.
+//
+// Precision plan (GB300's FP64 rate is a small fraction of FP32):
+//   * batch: the series prefix sums are built once in FP64 and packed as
+//     double-single float2; every output is then a difference of two prefix
+//     entries evaluated in double-single FP32 arithmetic (error-free
+//     two-sum / FMA products), and the variance is formed as
+//     (p*S2 - S1^2) / p^2 so the cancellation happens in ~48-bit precision;
+//   * time-major: each thread slides compensated (double-single) running sums
+//     over its time chunk, re-initialised exactly at the chunk start.
+// NaN semantics follow the crate's running-sum code: a NaN after the first
+// valid index poisons every later output of that series.
+#include "vta_internal.h"
+
+namespace vta {
+namespace {
+
+__device__ __forceinline__ float qnan() { return __int_as_float(0x7fc00000); }
+
+// ------------------------------------------------- double-single helpers --
+struct DS {
+    float hi, lo;
+};
+__device__ __forceinline__ DS two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    const float e = (a - (s - bb)) + (b - bb);
+    return {s, e};
+}
+__device__ __forceinline__ DS fast_two_sum(float a, float b) {
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+__device__ __forceinline__ DS ds_sub2(float2 a, float2 b) {
+    const DS s = two_sum(a.x, -b.x);
+    return fast_two_sum(s.hi, s.lo + (a.y - b.y));
+}
+__device__ __forceinline__ DS ds_sub(DS a, DS b) {
+    const DS s = two_sum(a.hi, -b.hi);
+    return fast_two_sum(s.hi, s.lo + (a.lo - b.lo));
+}
+__device__ __forceinline__ DS ds_add_f(DS a, float b) {
+    const DS s = two_sum(a.hi, b);
+    return fast_two_sum(s.hi, s.lo + a.lo);
+}
+__device__ __forceinline__ DS ds_mul_f(DS a, float b) {
+    const float p = a.hi * b;
+    float e = fmaf(a.hi, b, -p);
+    e = fmaf(a.lo, b, e);
+    return fast_two_sum(p, e);
+}
+__device__ __forceinline__ DS ds_sqr(DS a) {
+    const float p = a.hi * a.hi;
+    float e = fmaf(a.hi, a.hi, -p);
+    e = fmaf(2.f * a.hi, a.lo, e);
+    return fast_two_sum(p, e);
+}
+__device__ __forceinline__ float ds_f(DS a) { return a.hi + a.lo; }
+
+// Evaluates one prefix-window output family from the window sums S1, S2.
+struct WinOut {
+    float o0, o1, o2;
+};
+__device__ __forceinline__ WinOut window_eval(int kind, DS s1, DS s2, float pf, float xt,
+                                              float k1, float k2) {
+    WinOut r;
+    const float mean = ds_f(s1) / pf;
+    if (kind == WK_SMA) {
+        r.o0 = mean;
+        return r;
+    }
+    // p*S2 - S1^2 = p^2 * var
+    const DS num = ds_sub(ds_mul_f(s2, pf), ds_sqr(s1));
+    const float var = ds_f(num) / (pf * pf);
+    if (kind == WK_STDDEV) {
+        r.o0 = var <= 0.f ? 0.f : sqrtf(var) * k1;
+        return r;
+    }
+    if (kind == WK_ZSCORE) {
+        const float sd = var <= 0.f ? 0.f : sqrtf(var) * k1;
+        // (x - mean) with the mean kept in double-single
+        const DS m = {ds_f(s1), 0.f};
+        (void)m;
+        const float dev = xt - mean;
+        r.o0 = (sd == 0.f || isnan(sd)) ? qnan() : dev / sd;
+        return r;
+    }
+    // Bollinger (population std, devtype 0)
+    const float sd = sqrtf(fmaxf(var, 0.f));
+    r.o1 = mean;
+    r.o0 = mean + k1 * sd;
+    r.o2 = mean - k2 * sd;
+    return r;
+}
+
+// ---------------------------------------------- prefix windows, batch ------
+constexpr int kPwThreads = 256;
+constexpr int kPwCombos = 4;  // combos per thread (reuses the P[t] loads)
+
+__global__ void __launch_bounds__(kPwThreads)
+k_prefix_window_batch(PrefixWinArgs a) {
+    const int t = blockIdx.x * kPwThreads + threadIdx.x;
+    if (t >= a.n) return;
+    const int c_base = blockIdx.y * kPwCombos;
+    const float2 z = make_float2(0.f, 0.f);
+    const float2 p1t = a.p1[t];
+    const float2 p2t = a.kind == WK_SMA ? z : a.p2[t];
+    const float xt = a.kind == WK_ZSCORE ? a.x[t] : 0.f;
+#pragma unroll
+    for (int j = 0; j < kPwCombos; ++j) {
+        const int c = c_base + j;
+        if (c >= a.n_combos) break;
+        const int p = a.periods[c];
+        const size_t o = (size_t)c * a.n + t;
+        if (t < a.first + p - 1) {
+            a.out0[o] = qnan();
+            if (a.kind == WK_BB) { a.out1[o] = qnan(); a.out2[o] = qnan(); }
+            continue;
+        }
+        const int tb = t - p;
+        const float2 p1b = tb >= 0 ? a.p1[tb] : z;
+        const DS s1 = ds_sub2(p1t, p1b);
+        DS s2 = {0.f, 0.f};
+        if (a.kind != WK_SMA) {
+            const float2 p2b = tb >= 0 ? a.p2[tb] : z;
+            s2 = ds_sub2(p2t, p2b);
+        }
+        const float k1 = a.k1 ? a.k1[c] : 1.f;
+        const float k2 = a.k2 ? a.k2[c] : 1.f;
+        const WinOut r = window_eval(a.kind, s1, s2, (float)p, xt, k1, k2);
+        a.out0[o] = r.o0;
+        if (a.kind == WK_BB) { a.out1[o] = r.o1; a.out2[o] = r.o2; }
+    }
+}
+
+// ---------------------------------------------- prefix windows, time-major -
+constexpr int kTmChunk = 512;
+
+__global__ void k_prefix_window_tm(PrefixWinTmArgs a, const int* first_nan) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.cols) return;
+    const int c0 = blockIdx.y * kTmChunk;
+    const int c1 = min(c0 + kTmChunk, a.rows);
+    const int f = a.first[s];
+    const int fn = first_nan[s];
+    const int p = a.period;
+    const int warm = f + p - 1;
+    const size_t S = a.cols;
+    const float pf = (float)p;
+    auto X = [&](int t) { return __ldg(a.x_tm + (size_t)t * S + s); };
+    int t = c0;
+    for (; t < c1 && t < warm; ++t) {
+        a.out0[(size_t)t * S + s] = qnan();
+        if (a.kind == WK_BB) { a.out1[(size_t)t * S + s] = qnan(); a.out2[(size_t)t * S + s] = qnan(); }
+    }
+    if (t >= c1) return;
+    DS s1 = {0.f, 0.f}, s2 = {0.f, 0.f};
+    for (int k = t - p + 1; k <= t; ++k) {
+        const float v = X(k);
+        s1 = ds_add_f(s1, v);
+        const float vv = v * v;
+        s2 = ds_add_f(ds_add_f(s2, vv), fmaf(v, v, -vv));
+    }
+    for (; t < c1; ++t) {
+        if (t > c0 && t > warm) {
+            const float vn = X(t), vo = X(t - p);
+            s1 = ds_add_f(ds_add_f(s1, vn), -vo);
+            const float nn = vn * vn, oo = vo * vo;
+            s2 = ds_add_f(ds_add_f(s2, nn), fmaf(vn, vn, -nn));
+            s2 = ds_add_f(ds_add_f(s2, -oo), -fmaf(vo, vo, -oo));
+        }
+        const size_t o = (size_t)t * S + s;
+        if (t >= fn) {
+            a.out0[o] = qnan();
+            if (a.kind == WK_BB) { a.out1[o] = qnan(); a.out2[o] = qnan(); }
+            continue;
+        }
+        const WinOut r = window_eval(a.kind, s1, s2, pf, a.kind == WK_ZSCORE ? X(t) : 0.f, a.k1, a.k2);
+        a.out0[o] = r.o0;
+        if (a.kind == WK_BB) { a.out1[o] = r.o1; a.out2[o] = r.o2; }
+    }
+}
+
+// First NaN strictly after the first valid index, per time-major series.
+__global__ void k_first_nan_after_tm(const float* __restrict__ x, int cols, int rows,
+                                     const int* first, int* out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= cols) return;
+    int t = first[s] + 1;
+    while (t < rows && !isnan(x[(size_t)t * cols + s])) ++t;
+    out[s] = t < rows ? t : rows;
+}
+
+// ------------------------------------------------- min/max, batch ----------
+// One block per output time tile; a sparse table of window maxima of `high`
+// and minima of `low` over the tile's input span lives in shared memory and
+// serves every combo: max over [t-p+1, t] = max(M_k[t-p+1], M_k[t-2^k+1])
+// with k = floor(log2 p).  Invalid inputs are counted in prefix arrays so a
+// window containing one yields NaN (NaN rule for WillR and Donchian p <= 32,
+// non-finite rule for Donchian p > 32, donchian.rs:327-346 / 413-480).
+constexpr int kMmThreads = 512;
+
+__global__ void __launch_bounds__(kMmThreads)
+k_minmax_batch(MinMaxArgs a, int tile, int levels) {
+    extern __shared__ float sm[];
+    const int t0 = blockIdx.x * tile;
+    const int lo_i = t0 - (a.pmax - 1);  // global index of smem slot 0
+    const int nloc = tile + a.pmax - 1;
+    float* mx = sm;                          // [levels][nloc]
+    float* mn = sm + (size_t)levels * nloc;  // [levels][nloc]
+    int* bad_nan = reinterpret_cast<int*>(mn + (size_t)levels * nloc);  // [nloc+1]
+    int* bad_fin = bad_nan + nloc + 1;                                   // [nloc+1]
+    // level 0 + invalid flags
+    for (int i = threadIdx.x; i < nloc; i += blockDim.x) {
+        const int g = lo_i + i;
+        float hv = -INFINITY, lv = INFINITY;
+        int fnan = 0, ffin = 0;
+        if (g >= 0 && g < a.n) {
+            const float h = a.h[g], l = a.l[g];
+            fnan = (isnan(h) || isnan(l)) ? 1 : 0;
+            ffin = (isfinite(h) && isfinite(l)) ? 0 : 1;
+            if (!fnan) { hv = h; lv = l; }
+        }
+        mx[i] = hv;
+        mn[i] = lv;
+        bad_nan[i + 1] = fnan;
+        bad_fin[i + 1] = ffin;
+    }
+    if (threadIdx.x == 0) { bad_nan[0] = 0; bad_fin[0] = 0; }
+    __syncthreads();
+    // prefix counts (single warp, sequential per lane-strided segments)
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        const int seg = (nloc + 31) / 32;
+        const int b = 1 + lane * seg, e = min(nloc + 1, b + seg);
+        int cn = 0, cf = 0;
+        for (int i = b; i < e; ++i) { cn += bad_nan[i]; cf += bad_fin[i]; bad_nan[i] = cn; bad_fin[i] = cf; }
+        int on = cn, of = cf;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int un = __shfl_up_sync(0xffffffffu, on, o);
+            const int uf = __shfl_up_sync(0xffffffffu, of, o);
+            if (lane >= o) { on += un; of += uf; }
+        }
+        on -= cn; of -= cf;  // exclusive offsets
+        for (int i = b; i < e; ++i) { bad_nan[i] += on; bad_fin[i] += of; }
+    }
+    // higher levels
+    for (int k = 1; k < levels; ++k) {
+        __syncthreads();
+        const int half = 1 << (k - 1);
+        const float* pmx = mx + (size_t)(k - 1) * nloc;
+        const float* pmn = mn + (size_t)(k - 1) * nloc;
+        float* cmx = mx + (size_t)k * nloc;
+        float* cmn = mn + (size_t)k * nloc;
+        for (int i = threadIdx.x; i + half < nloc; i += blockDim.x) {
+            cmx[i] = fmaxf(pmx[i], pmx[i + half]);
+            cmn[i] = fminf(pmn[i], pmn[i + half]);
+        }
+    }
+    __syncthreads();
+    for (int tt = threadIdx.x; tt < tile; tt += blockDim.x) {
+        const int t = t0 + tt;
+        if (t >= a.n) break;
+        const float cl = a.kind == MM_WILLR ? a.c[t] : 0.f;
+        const int ie = t - lo_i;  // local index of t
+        for (int c = 0; c < a.n_combos; ++c) {
+            const int p = a.periods[c];
+            const size_t o = (size_t)c * a.n + t;
+            float r0 = qnan(), r1 = qnan(), r2 = qnan();
+            if (t >= a.first + p - 1) {
+                const int ib = ie - p + 1;
+                const int k = 31 - __clz(p);
+                const int ib2 = ie - (1 << k) + 1;
+                const float hmax = fmaxf(mx[(size_t)k * nloc + ib], mx[(size_t)k * nloc + ib2]);
+                const float lmin = fminf(mn[(size_t)k * nloc + ib], mn[(size_t)k * nloc + ib2]);
+                const int nn = bad_nan[ie + 1] - bad_nan[ib];
+                if (a.kind == MM_DONCHIAN) {
+                    const int nb = p > 32 ? bad_fin[ie + 1] - bad_fin[ib] : nn;
+                    if (nb == 0) {
+                        r0 = hmax;
+                        r2 = lmin;
+                        r1 = fmaf(hmax - lmin, 0.5f, lmin);
+                    }
+                } else {
+                    if (!isnan(cl) && nn == 0 && isfinite(hmax) && isfinite(lmin)) {
+                        const float den = hmax - lmin;
+                        r0 = den == 0.f ? 0.f : fmaf(-100.f, (hmax - cl) / den, 0.f);
+                    }
+                }
+            }
+            a.out0[o] = r0;
+            if (a.kind == MM_DONCHIAN) { a.out1[o] = r1; a.out2[o] = r2; }
+        }
+    }
+}
+
+// Direct window scan (large windows that do not fit the shared-memory table).
+__global__ void k_minmax_batch_naive(MinMaxArgs a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (t >= a.n || c >= a.n_combos) return;
+    const int p = a.periods[c];
+    const size_t o = (size_t)c * a.n + t;
+    float r0 = qnan(), r1 = qnan(), r2 = qnan();
+    if (t >= a.first + p - 1) {
+        float hmax = -INFINITY, lmin = INFINITY;
+        bool bad_n = false, bad_f = false;
+        for (int j = t - p + 1; j <= t; ++j) {
+            const float h = a.h[j], l = a.l[j];
+            if (isnan(h) || isnan(l)) { bad_n = true; bad_f = true; break; }
+            if (!isfinite(h) || !isfinite(l)) bad_f = true;
+            hmax = fmaxf(hmax, h);
+            lmin = fminf(lmin, l);
+        }
+        if (a.kind == MM_DONCHIAN) {
+            if (!(p > 32 ? bad_f : bad_n)) { r0 = hmax; r2 = lmin; r1 = fmaf(hmax - lmin, 0.5f, lmin); }
+        } else {
+            const float cl = a.c[t];
+            if (!isnan(cl) && !bad_n && isfinite(hmax) && isfinite(lmin)) {
+                const float den = hmax - lmin;
+                r0 = den == 0.f ? 0.f : fmaf(-100.f, (hmax - cl) / den, 0.f);
+            }
+        }
+    }
+    a.out0[o] = r0;
+    if (a.kind == MM_DONCHIAN) { a.out1[o] = r1; a.out2[o] = r2; }
+}
+
+// ------------------------------------------------- min/max, time-major -----
+constexpr int kMmTmChunk = 256;
+
+__global__ void k_minmax_tm(MinMaxTmArgs a) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.cols) return;
+    const int c0 = blockIdx.y * kMmTmChunk;
+    const int c1 = min(c0 + kMmTmChunk, a.rows);
+    const int p = a.period, f = a.first[s];
+    const size_t S = a.cols;
+    for (int t = c0; t < c1; ++t) {
+        const size_t o = (size_t)t * S + s;
+        float r0 = qnan(), r1 = qnan(), r2 = qnan();
+        if (t >= f + p - 1) {
+            float hmax = -INFINITY, lmin = INFINITY;
+            bool bad_n = false, bad_f = false;
+            for (int j = t - p + 1; j <= t; ++j) {
+                const float h = __ldg(a.h + (size_t)j * S + s), l = __ldg(a.l + (size_t)j * S + s);
+                if (isnan(h) || isnan(l)) { bad_n = true; bad_f = true; break; }
+                if (!isfinite(h) || !isfinite(l)) bad_f = true;
+                hmax = fmaxf(hmax, h);
+                lmin = fminf(lmin, l);
+            }
+            if (a.kind == MM_DONCHIAN) {
+                if (!(p > 32 ? bad_f : bad_n)) { r0 = hmax; r2 = lmin; r1 = fmaf(hmax - lmin, 0.5f, lmin); }
+            } else {
+                const float cl = a.c[o];
+                if (!isnan(cl) && !bad_n && isfinite(hmax) && isfinite(lmin)) {
+                    const float den = hmax - lmin;
+                    r0 = den == 0.f ? 0.f : fmaf(-100.f, (hmax - cl) / den, 0.f);
+                }
+            }
+        }
+        a.out0[o] = r0;
+        if (a.kind == MM_DONCHIAN) { a.out1[o] = r1; a.out2[o] = r2; }
+    }
+}
+
+// ------------------------------------------------- percentile --------------
+// Sorted window of the non-NaN values (percentile_nearest_rank.rs:190-266):
+// binary-search removal of the value leaving and insertion of the value
+// entering; out = sorted[k], k = round(p*wl) - 1 clamped.  Exact selection,
+// so results are bit-identical to the crate on the same f32 inputs.
+constexpr int kPnrChunk = 256;
+constexpr int kPnrLocal = 64;
+
+__device__ __forceinline__ int pnr_rank(double pf, int wl) {
+    long long raw = (long long)round(fma(pf, (double)wl, 0.0)) - 1;
+    int k = raw <= 0 ? 0 : (int)raw;
+    return k >= wl ? wl - 1 : k;
+}
+
+__device__ __forceinline__ int lower_bound(const float* w, int n, float v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (w[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ void pnr_lane(const float* x, size_t stride, int n, int f, int len, double pf, int c0,
+                         int c1, float* out, size_t ostride, float* win) {
+    const int start = f + len - 1;
+    int t = c0;
+    for (; t < c1 && t < start; ++t) out[(size_t)t * ostride] = qnan();
+    if (t >= c1) return;
+    int wl = 0;
+    for (int j = t - len + 1; j <= t; ++j) {
+        const float v = x[(size_t)j * stride];
+        if (isnan(v)) continue;
+        int pos = wl;
+        while (pos > 0 && win[pos - 1] > v) { win[pos] = win[pos - 1]; --pos; }
+        win[pos] = v;
+        ++wl;
+    }
+    const int kfull = pnr_rank(pf, len);
+    for (;;) {
+        float r = qnan();
+        if (wl > 0) r = win[wl == len ? kfull : pnr_rank(pf, wl)];
+        out[(size_t)t * ostride] = r;
+        if (t + 1 >= c1) break;
+        const float vo = x[(size_t)(t + 1 - len) * stride];
+        if (!isnan(vo)) {
+            int pos = lower_bound(win, wl, vo);
+            if (pos < wl && win[pos] == vo) {
+                for (int k = pos; k + 1 < wl; ++k) win[k] = win[k + 1];
+                --wl;
+            }
+        }
+        const float vi = x[(size_t)(t + 1) * stride];
+        if (!isnan(vi)) {
+            int pos = lower_bound(win, wl, vi);
+            for (int k = wl; k > pos; --k) win[k] = win[k - 1];
+            win[pos] = vi;
+            ++wl;
+        }
+        ++t;
+    }
+}
+
+__global__ void k_percentile(PnrArgs a) {
+    const int li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= a.n_lanes) return;
+    const int c0 = blockIdx.y * kPnrChunk;
+    const int c1 = min(c0 + kPnrChunk, a.n);
+    if (c0 >= a.n) return;
+    float local[kPnrLocal];
+    if (a.layout == 0) {
+        const int len = a.lengths[li];
+        float* win = len <= kPnrLocal ? local
+                                      : a.scratch + ((size_t)blockIdx.y * a.n_lanes + li) * (size_t)a.length;
+        pnr_lane(a.x, 1, a.n, a.first, len, (double)a.pfrac[li], c0, c1, a.out + (size_t)li * a.n, 1, win);
+    } else {
+        float* win = a.length <= kPnrLocal
+                         ? local
+                         : a.scratch + ((size_t)blockIdx.y * a.n_lanes + li) * (size_t)a.length;
+        pnr_lane(a.x + li, a.cols, a.n, a.first_tm[li], a.length, (double)a.p_frac, c0, c1, a.out + li,
+                 a.cols, win);
+    }
+}
+
+}  // namespace
+
+vta_status launch_prefix_window_batch(const PrefixWinArgs& a, cudaStream_t st) {
+    dim3 grid(ceil_div(a.n, kPwThreads), ceil_div(a.n_combos, kPwCombos));
+    if (grid.y > 65535) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "prefix window: too many combos");
+    k_prefix_window_batch<<<grid, kPwThreads, 0, st>>>(a);
+    return check_launch("k_prefix_window_batch");
+}
+
+// first_nan scratch is carved by the caller right after `first`
+vta_status launch_prefix_window_tm(const PrefixWinTmArgs& a, cudaStream_t st) {
+    int* first_nan = const_cast<int*>(a.first) + a.cols;
+    k_first_nan_after_tm<<<ceil_div(a.cols, 128), 128, 0, st>>>(a.x_tm, a.cols, a.rows, a.first, first_nan);
+    VTA_TRY(check_launch("k_first_nan_after_tm"));
+    dim3 grid(ceil_div(a.cols, 128), ceil_div(a.rows, kTmChunk));
+    k_prefix_window_tm<<<grid, 128, 0, st>>>(a, first_nan);
+    return check_launch("k_prefix_window_tm");
+}
+
+vta_status launch_minmax_batch(const MinMaxArgs& a, size_t smem_optin, cudaStream_t st) {
+    const int levels = 32 - __builtin_clz((unsigned)a.pmax);  // floor(log2 pmax) + 1
+    for (int tile = 2048; tile >= 256; tile >>= 1) {
+        const size_t nloc = (size_t)tile + a.pmax - 1;
+        const size_t bytes = nloc * levels * 2 * sizeof(float) + 2 * (nloc + 1) * sizeof(int);
+        if (bytes <= smem_optin && (tile <= 512 || (size_t)a.n >= (size_t)tile * 8 * kNumSMs)) {
+            VTA_CUDA_TRY(cudaFuncSetAttribute(k_minmax_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)bytes));
+            k_minmax_batch<<<ceil_div(a.n, tile), kMmThreads, bytes, st>>>(a, tile, levels);
+            return check_launch("k_minmax_batch");
+        }
+    }
+    dim3 grid(ceil_div(a.n, 256), a.n_combos);
+    k_minmax_batch_naive<<<grid, 256, 0, st>>>(a);
+    return check_launch("k_minmax_batch_naive");
+}
+
+vta_status launch_minmax_tm(const MinMaxTmArgs& a, cudaStream_t st) {
+    dim3 grid(ceil_div(a.cols, 128), ceil_div(a.rows, kMmTmChunk));
+    k_minmax_tm<<<grid, 128, 0, st>>>(a);
+    return check_launch("k_minmax_tm");
+}
+
+vta_status launch_percentile(const PnrArgs& a, cudaStream_t st) {
+    dim3 grid(ceil_div(a.n_lanes, 64), ceil_div(a.n, kPnrChunk));
+    k_percentile<<<grid, 64, 0, st>>>(a);
+    return check_launch("k_percentile");
+}
+
+}  // namespace vta

@@ -1,0 +1,1026 @@
+// Host side of the C ABI: contexts, device arrays, parameter grids, input
+// validation and kernel orchestration for every indicator.
+//
+// Each public entry point funnels into one of two internal drivers:
+//   run_batch(ctx, ind, device inputs, len, first, combos, device outputs)
+//   run_tm(ctx, ind, device inputs, cols, rows, params, device outputs)
+// which enqueue kernels on the context stream.  The *_dev / *_into_host_f32
+// / *_many_series_*_dev forms add the crate's host-side validation, the
+// host->device copies and the output allocation around them.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <memory>
+
+#include "vta_internal.h"
+
+// ============================================================ errors =======
+namespace vta {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string& msg) { g_err = msg; }
+vta_status fail(vta_status st, const std::string& msg) {
+    g_err = msg;
+    return st;
+}
+vta_status cuda_fail(cudaError_t e, const char* what) {
+    g_err = std::string("cuda error: ") + cudaGetErrorString(e) + " (" + what + ")";
+    return VTA_ERR_CUDA;
+}
+vta_status check_launch(const char* kernel) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, kernel);
+    return VTA_OK;
+}
+
+vta_status Arena::commit() {
+    if (total_ <= ctx_->scratch_bytes) return VTA_OK;
+    if (ctx_->scratch) {
+        VTA_CUDA_TRY(cudaStreamSynchronize(ctx_->stream));
+        cudaFree(ctx_->scratch);
+        ctx_->scratch = nullptr;
+        ctx_->scratch_bytes = 0;
+    }
+    size_t want = std::max(total_, size_t(1) << 20);
+    want = (want + (size_t(1) << 20) - 1) & ~((size_t(1) << 20) - 1);
+    VTA_TRY(vram_check(want));
+    VTA_CUDA_TRY(cudaMalloc(&ctx_->scratch, want));
+    ctx_->scratch_bytes = want;
+    return VTA_OK;
+}
+
+vta_status vram_check(size_t required) {
+    const char* env = std::getenv("VTA_MEM_CHECK");
+    if (env && (env[0] == '0' || env[0] == 'f' || env[0] == 'F')) return VTA_OK;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return VTA_OK;
+    const size_t headroom = size_t(64) << 20;
+    if (required + headroom > free_b) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "out of memory: required=%zu free=%zu headroom=%zu", required, free_b,
+                      headroom);
+        return fail(VTA_ERR_OUT_OF_MEMORY, buf);
+    }
+    return VTA_OK;
+}
+
+// ============================================================ grids ========
+enum AxisMode { AX_DESC = 0, AX_SWAP = 1, AX_REV_FROM_END = 2, AX_DESC_PLUS_END = 3 };
+
+// usize axis of the crate's expand_grid functions.  Ascending ranges are the
+// same everywhere; descending ones differ per indicator (see AxisMode users).
+static std::vector<size_t> axis_usize(vta_range_usize r, int mode) {
+    std::vector<size_t> v;
+    if (r.step == 0 || r.start == r.end) return {r.start};
+    if (r.start < r.end) {
+        for (size_t x = r.start; x <= r.end; x += r.step) {
+            v.push_back(x);
+            if (x > SIZE_MAX - r.step) break;
+        }
+        return v;
+    }
+    switch (mode) {
+        case AX_SWAP:
+            for (size_t x = r.end; x <= r.start; x += r.step) {
+                v.push_back(x);
+                if (x > SIZE_MAX - r.step) break;
+            }
+            break;
+        case AX_REV_FROM_END: {
+            const size_t cnt = (r.start - r.end) / r.step + 1;
+            for (size_t k = cnt; k-- > 0;) v.push_back(r.end + k * r.step);
+            break;
+        }
+        default: {
+            size_t x = r.start;
+            for (;;) {
+                v.push_back(x);
+                if (x < r.end + r.step) break;
+                x -= r.step;
+            }
+            if (mode == AX_DESC_PLUS_END && v.back() != r.end) v.push_back(r.end);
+        }
+    }
+    return v;
+}
+
+// f64 axis: accumulated x += step with the crate's 1e-12 slack
+// (alma.rs:1224-1260 and the same helper in the other indicators).
+static std::vector<double> axis_f64(vta_range_f64 r) {
+    std::vector<double> v;
+    if (std::fabs(r.step) < 1e-12 || std::fabs(r.start - r.end) < 1e-12) return {r.start};
+    const double st = std::fabs(r.step);
+    if (r.start < r.end) {
+        for (double x = r.start; x <= r.end + 1e-12; x += st) v.push_back(x);
+    } else {
+        for (double x = r.start; x + 1e-12 >= r.end; x -= st) v.push_back(x);
+    }
+    return v;
+}
+
+// ============================================================ indicators ===
+enum Ind {
+    I_ALMA, I_EMA, I_DEMA, I_TEMA, I_RSI, I_WILDERS, I_SMA, I_WMA, I_SWMA, I_PWMA, I_SINWMA, I_TRIMA,
+    I_STDDEV, I_ZSCORE, I_BB, I_ATR, I_ADX, I_SUPERTREND, I_DONCHIAN, I_WILLR, I_PNR
+};
+enum InKind { IN_X = 1, IN_HL = 2, IN_HLC = 3 };
+
+struct IndInfo {
+    const char* name;
+    int in;       // InKind == number of input series
+    int n_out;
+    int axis;     // AxisMode of the period axis
+};
+static const IndInfo kInfo[] = {
+    {"alma", IN_X, 1, AX_DESC},        {"ema", IN_X, 1, AX_SWAP},         {"dema", IN_X, 1, AX_DESC},
+    {"tema", IN_X, 1, AX_DESC},        {"rsi", IN_X, 1, AX_SWAP},         {"wilders", IN_X, 1, AX_DESC},
+    {"sma", IN_X, 1, AX_DESC},         {"wma", IN_X, 1, AX_DESC_PLUS_END}, {"swma", IN_X, 1, AX_DESC},
+    {"pwma", IN_X, 1, AX_DESC},        {"sinwma", IN_X, 1, AX_DESC},      {"trima", IN_X, 1, AX_SWAP},
+    {"stddev", IN_X, 1, AX_DESC},      {"zscore", IN_X, 1, AX_DESC},      {"bollinger_bands", IN_X, 3, AX_DESC},
+    {"atr", IN_HLC, 1, AX_REV_FROM_END}, {"adx", IN_HLC, 1, AX_DESC},     {"supertrend", IN_HLC, 2, AX_DESC},
+    {"donchian", IN_HL, 3, AX_DESC},   {"willr", IN_HLC, 1, AX_DESC},     {"percentile_nearest_rank", IN_X, 1, AX_DESC},
+};
+
+// One parameter set: period plus up to two f64 parameters
+// (alma: offset, sigma; stddev/zscore: nbdev; bb: devup, devdn;
+//  supertrend: factor; percentile: percentage).
+struct Combo {
+    size_t period;
+    double a, b;
+};
+
+static bool is_wwma(Ind i) {
+    return i == I_ALMA || i == I_WMA || i == I_SWMA || i == I_PWMA || i == I_SINWMA || i == I_TRIMA;
+}
+
+// minimum valid length after `first` a combo needs (the crate's checks)
+static size_t needed_len(Ind ind, size_t p) {
+    switch (ind) {
+        case I_DEMA: return p > 0 ? 2 * (p - 1) : 0;
+        case I_ADX: return p + 1;
+        default: return p;
+    }
+}
+
+static vta_status validate_combo(Ind ind, const Combo& c, size_t len) {
+    const IndInfo& in = kInfo[ind];
+    char buf[200];
+    auto bad = [&](const char* why) {
+        std::snprintf(buf, sizeof buf, "%s: invalid params: period=%zu a=%g b=%g (%s)", in.name, c.period, c.a,
+                      c.b, why);
+        return fail(VTA_ERR_INVALID_INPUT, buf);
+    };
+    if (c.period == 0) return bad("period must be > 0");
+    if (c.period > len) return bad("period exceeds data length");
+    if (c.period > (size_t)INT32_MAX) return bad("period too large");
+    switch (ind) {
+        case I_ALMA:
+            if (!(c.b > 0.0)) return bad("sigma must be > 0");
+            if (!(c.a >= 0.0 && c.a <= 1.0)) return bad("offset must be in [0, 1]");
+            break;
+        case I_WMA:
+            if (c.period < 2) return bad("period must be >= 2");
+            break;
+        case I_TRIMA:
+            if (c.period <= 3) return bad("period must be > 3");
+            break;
+        case I_STDDEV:
+            if (!std::isfinite(c.a) || c.a < 0.0) return bad("nbdev must be finite and >= 0");
+            break;
+        case I_PNR:
+            if (!(c.a >= 0.0 && c.a <= 100.0)) return bad("percentage must be in [0, 100]");
+            break;
+        default:
+            break;
+    }
+    return VTA_OK;
+}
+
+static vta_status validate_combos(Ind ind, const std::vector<Combo>& cs, size_t len, size_t first) {
+    if (cs.empty()) return fail(VTA_ERR_INVALID_INPUT, std::string(kInfo[ind].name) + ": no parameter combinations");
+    size_t need = 0;
+    for (const Combo& c : cs) {
+        VTA_TRY(validate_combo(ind, c, len));
+        need = std::max(need, needed_len(ind, c.period));
+    }
+    if (first >= len) return fail(VTA_ERR_INVALID_INPUT, std::string(kInfo[ind].name) + ": all values are NaN");
+    if (len - first < need) {
+        char buf[200];
+        std::snprintf(buf, sizeof buf, "%s: not enough valid data (needed >= %zu, valid = %zu)", kInfo[ind].name,
+                      need, len - first);
+        return fail(VTA_ERR_INVALID_INPUT, buf);
+    }
+    return VTA_OK;
+}
+
+// first valid index as each indicator defines it
+static size_t host_first(Ind ind, const float* const* in, size_t n, size_t stride = 1, size_t off = 0) {
+    auto at = [&](int k, size_t t) { return in[k][t * stride + off]; };
+    if (kInfo[ind].in == IN_X) {
+        size_t t = 0;
+        while (t < n && std::isnan(at(0, t))) ++t;
+        return t;
+    }
+    if (ind == I_ADX || ind == I_DONCHIAN) {  // max of the per-field firsts (adx.rs:190-198)
+        size_t f = 0;
+        for (int k = 0; k < kInfo[ind].in; ++k) {
+            size_t t = 0;
+            while (t < n && std::isnan(at(k, t))) ++t;
+            if (t >= n) return n;
+            f = std::max(f, t);
+        }
+        return f;
+    }
+    size_t t = 0;  // first index where h, l, c are all non-NaN (atr.rs:197-207)
+    while (t < n && (std::isnan(at(0, t)) || std::isnan(at(1, t)) || std::isnan(at(2, t)))) ++t;
+    return t;
+}
+
+// ------------------------------------------------------------ batch run ----
+struct DevIn {
+    const float* p[3];
+};
+
+static int pick_chunk(vta_ctx* ctx, int n, int lanes) {
+    const int pol = ctx->policy.recur_chunk;
+    if (pol == 1) return ((n + 31) / 32) * 32;
+    if (pol > 1) return pol;
+    const long lane_warps = (lanes + 31) / 32;
+    const long target = (long)ctx->num_sms * 64;  // warps in flight we aim for
+    long chunks = std::max(1L, target / std::max(1L, lane_warps));
+    long len = (n + chunks - 1) / chunks;
+    len = std::max<long>(len, kChunkMin);
+    len = ((len + 31) / 32) * 32;
+    while ((n + len - 1) / len > 65535) len *= 2;
+    return (int)len;
+}
+
+static vta_status upload(vta_ctx* ctx, void* dst, const void* src, size_t bytes) {
+    if (!bytes) return VTA_OK;
+    VTA_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    return VTA_OK;
+}
+
+static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, size_t first,
+                            const std::vector<Combo>& cs, float* const* out) {
+    cudaStream_t st = ctx->stream;
+    const int n = (int)len;
+    const int nc = (int)cs.size();
+    if (len > (size_t)INT32_MAX) return fail(VTA_ERR_INVALID_INPUT, "series longer than 2^31-1");
+    std::vector<int> periods(nc);
+    std::vector<double> pa(nc), pb(nc);
+    std::vector<float> fa(nc), fb(nc);
+    int pmax = 0;
+    for (int i = 0; i < nc; ++i) {
+        periods[i] = (int)cs[i].period;
+        pa[i] = cs[i].a;
+        pb[i] = cs[i].b;
+        fa[i] = (float)cs[i].a;
+        fb[i] = (float)cs[i].b;
+        pmax = std::max(pmax, periods[i]);
+    }
+    Arena ar(ctx);
+    ar.need(nc * sizeof(int));
+    ar.need(nc * sizeof(double));
+    ar.need(nc * sizeof(double));
+    ar.need(nc * sizeof(float));
+    ar.need(nc * sizeof(float));
+
+    if (is_wwma(ind)) {
+        const int kmax = pmax;
+        const int ntile = (nc + 15) / 16;
+        ar.need((size_t)nc * kmax * sizeof(float));
+        ar.need(ntile * sizeof(int));
+        ar.need(len * sizeof(double));
+        ar.need(prefix_tmp_doubles(n) * sizeof(double));
+        VTA_TRY(ar.commit());
+        int* d_per = ar.take<int>(nc);
+        double* d_pa = ar.take<double>(nc);
+        double* d_pb = ar.take<double>(nc);
+        ar.take<float>(nc);
+        ar.take<float>(nc);
+        float* d_w = ar.take<float>((size_t)nc * kmax);
+        int* d_tk = ar.take<int>(ntile);
+        double* d_nanp = ar.take<double>(len);
+        double* d_tmp = ar.take<double>(prefix_tmp_doubles(n));
+        std::vector<int> tk(ntile, 0);
+        for (int i = 0; i < nc; ++i) tk[i / 16] = std::max(tk[i / 16], periods[i]);
+        VTA_TRY(upload(ctx, d_per, periods.data(), nc * sizeof(int)));
+        VTA_TRY(upload(ctx, d_pa, pa.data(), nc * sizeof(double)));
+        VTA_TRY(upload(ctx, d_pb, pb.data(), nc * sizeof(double)));
+        VTA_TRY(upload(ctx, d_tk, tk.data(), ntile * sizeof(int)));
+        int wk = WT_ALMA;
+        switch (ind) {
+            case I_WMA: wk = WT_WMA; break;
+            case I_SWMA: wk = WT_SWMA; break;
+            case I_PWMA: wk = WT_PWMA; break;
+            case I_SINWMA: wk = WT_SINWMA; break;
+            case I_TRIMA: wk = WT_TRIMA; break;
+            default: break;
+        }
+        VTA_TRY(launch_weights(wk, d_per, d_pa, d_pb, nc, kmax, d_w, st));
+        VTA_TRY(launch_prefix_f64(in.p[0], n, (int)first, PK_NAN, d_nanp, nullptr, d_tmp, st));
+        WwmaBatchArgs a{};
+        a.x = in.p[0];
+        a.n = n;
+        a.first = (int)first;
+        a.w = d_w;
+        a.periods = d_per;
+        a.tile_kmax = d_tk;
+        a.kmax = kmax;
+        a.n_combos = nc;
+        // running-sum indicators (WMA, SWMA, TRIMA) keep a NaN forever
+        a.nan_mode = (ind == I_WMA || ind == I_SWMA || ind == I_TRIMA) ? 1 : 0;
+        a.nanp = d_nanp;
+        a.out = out[0];
+        const int pol = ctx->policy.wma_batch;
+        if (pol == 0 || pol >= 2) {
+            const vta_status s = launch_wwma_batch_tc(a, pol == 3 ? 1 : 0, ctx, st);
+            if (s == VTA_OK) {
+                ctx->last_kernel = pol == 3 ? "wwma_tc_bf16x3" : "wwma_tc_fp16x3";
+                return VTA_OK;
+            }
+            if (s != VTA_ERR_NOT_IMPLEMENTED || pol >= 2) return s;
+        }
+        ctx->last_kernel = "wwma_plain_f32";
+        return launch_wwma_batch_plain(a, st);
+    }
+
+    switch (ind) {
+        case I_EMA: case I_DEMA: case I_TEMA: case I_RSI: case I_WILDERS: case I_ATR: {
+            const int chunk = pick_chunk(ctx, n, nc);
+            const int nch = (n + chunk - 1) / chunk;
+            ar.need((size_t)nch * nc * 16);
+            ar.need((size_t)nch * nc * 16);
+            VTA_TRY(ar.commit());
+            int* d_per = ar.take<int>(nc);
+            ar.take<double>(nc);
+            ar.take<double>(nc);
+            ar.take<float>(nc);
+            ar.take<float>(nc);
+            float* d_agg = ar.take<float>((size_t)nch * nc * 4);
+            float* d_carry = ar.take<float>((size_t)nch * nc * 4);
+            VTA_TRY(upload(ctx, d_per, periods.data(), nc * sizeof(int)));
+            RecurArgs a{};
+            a.kind = ind == I_EMA ? RK_EMA : ind == I_DEMA ? RK_DEMA : ind == I_TEMA ? RK_TEMA
+                   : ind == I_RSI ? RK_RSI : ind == I_WILDERS ? RK_WILDERS : RK_ATR;
+            a.layout = 0;
+            a.x = in.p[0];
+            if (ind == I_ATR) { a.h = in.p[0]; a.l = in.p[1]; a.c = in.p[2]; a.x = in.p[2]; }
+            a.n = n;
+            a.first = (int)first;
+            a.periods = d_per;
+            a.n_lanes = nc;
+            a.chunk = chunk;
+            a.out = out[0];
+            a.agg = d_agg;
+            a.carry = d_carry;
+            ctx->last_kernel = nch > 1 ? "recurrence_chunked" : "recurrence_sequential";
+            return launch_recurrence(a, st);
+        }
+        case I_ADX: case I_SUPERTREND: {
+            VTA_TRY(ar.commit());
+            int* d_per = ar.take<int>(nc);
+            ar.take<double>(nc);
+            ar.take<double>(nc);
+            float* d_fa = ar.take<float>(nc);
+            ar.take<float>(nc);
+            VTA_TRY(upload(ctx, d_per, periods.data(), nc * sizeof(int)));
+            VTA_TRY(upload(ctx, d_fa, fa.data(), nc * sizeof(float)));
+            HlcArgs a{};
+            a.layout = 0;
+            a.h = in.p[0]; a.l = in.p[1]; a.c = in.p[2];
+            a.n = n;
+            a.first = (int)first;
+            a.periods = d_per;
+            a.factors = d_fa;
+            a.n_lanes = nc;
+            a.out0 = out[0];
+            a.out1 = ind == I_SUPERTREND ? out[1] : nullptr;
+            ctx->last_kernel = ind == I_ADX ? "adx_sequential" : "supertrend_sequential";
+            return ind == I_ADX ? launch_adx(a, st) : launch_supertrend(a, st);
+        }
+        case I_SMA: case I_STDDEV: case I_ZSCORE: case I_BB: {
+            const bool need2 = ind != I_SMA;
+            ar.need(len * sizeof(float2));
+            ar.need(need2 ? len * sizeof(float2) : 0);
+            ar.need(prefix_tmp_doubles(n) * sizeof(double));
+            VTA_TRY(ar.commit());
+            int* d_per = ar.take<int>(nc);
+            ar.take<double>(nc);
+            ar.take<double>(nc);
+            float* d_fa = ar.take<float>(nc);
+            float* d_fb = ar.take<float>(nc);
+            float2* d_p1 = ar.take<float2>(len);
+            float2* d_p2 = need2 ? ar.take<float2>(len) : nullptr;
+            double* d_tmp = ar.take<double>(prefix_tmp_doubles(n));
+            VTA_TRY(upload(ctx, d_per, periods.data(), nc * sizeof(int)));
+            VTA_TRY(upload(ctx, d_fa, fa.data(), nc * sizeof(float)));
+            VTA_TRY(upload(ctx, d_fb, fb.data(), nc * sizeof(float)));
+            VTA_TRY(launch_prefix_f64(in.p[0], n, (int)first, PK_X, nullptr, d_p1, d_tmp, st));
+            if (need2) VTA_TRY(launch_prefix_f64(in.p[0], n, (int)first, PK_X2, nullptr, d_p2, d_tmp, st));
+            PrefixWinArgs a{};
+            a.kind = ind == I_SMA ? WK_SMA : ind == I_STDDEV ? WK_STDDEV : ind == I_ZSCORE ? WK_ZSCORE : WK_BB;
+            a.x = in.p[0];
+            a.p1 = d_p1;
+            a.p2 = d_p2;
+            a.n = n;
+            a.first = (int)first;
+            a.periods = d_per;
+            a.k1 = d_fa;
+            a.k2 = d_fb;
+            a.n_combos = nc;
+            a.out0 = out[0];
+            if (ind == I_BB) { a.out0 = out[0]; a.out1 = out[1]; a.out2 = out[2]; }
+            ctx->last_kernel = "prefix_window_ds";
+            return launch_prefix_window_batch(a, st);
+        }
+        case I_DONCHIAN: case I_WILLR: {
+            VTA_TRY(ar.commit());
+            int* d_per = ar.take<int>(nc);
+            VTA_TRY(upload(ctx, d_per, periods.data(), nc * sizeof(int)));
+            MinMaxArgs a{};
+            a.kind = ind == I_DONCHIAN ? MM_DONCHIAN : MM_WILLR;
+            a.h = in.p[0]; a.l = in.p[1];
+            a.c = ind == I_WILLR ? in.p[2] : nullptr;
+            a.n = n;
+            a.first = (int)first;
+            a.periods = d_per;
+            a.n_combos = nc;
+            a.pmax = pmax;
+            a.out0 = out[0];
+            if (ind == I_DONCHIAN) { a.out1 = out[1]; a.out2 = out[2]; }
+            ctx->last_kernel = "minmax_sparse_table";
+            return launch_minmax_batch(a, ctx->smem_optin, st);
+        }
+        case I_PNR: {
+            const int nchunk = (n + 255) / 256;
+            const size_t sc = pmax > 64 ? (size_t)nchunk * nc * pmax : 0;
+            ar.need(sc * sizeof(float));
+            VTA_TRY(ar.commit());
+            int* d_per = ar.take<int>(nc);
+            ar.take<double>(nc);
+            ar.take<double>(nc);
+            float* d_fa = ar.take<float>(nc);
+            ar.take<float>(nc);
+            float* d_sc = sc ? ar.take<float>(sc) : nullptr;
+            std::vector<float> pf(nc);
+            // p_frac = percentage * 0.01 in f64 (percentile_nearest_rank.rs:213)
+            std::vector<double> pfd(nc);
+            for (int i = 0; i < nc; ++i) pf[i] = (float)(cs[i].a * 0.01);
+            VTA_TRY(upload(ctx, d_per, periods.data(), nc * sizeof(int)));
+            VTA_TRY(upload(ctx, d_fa, pf.data(), nc * sizeof(float)));
+            PnrArgs a{};
+            a.layout = 0;
+            a.x = in.p[0];
+            a.n = n;
+            a.first = (int)first;
+            a.lengths = d_per;
+            a.pfrac = d_fa;
+            a.length = pmax;
+            a.n_lanes = nc;
+            a.out = out[0];
+            a.scratch = d_sc;
+            ctx->last_kernel = "percentile_sorted_window";
+            return launch_percentile(a, st);
+        }
+        default:
+            return fail(VTA_ERR_NOT_IMPLEMENTED, "indicator not implemented");
+    }
+}
+
+// ------------------------------------------------------------ tm run -------
+static vta_status run_tm(vta_ctx* ctx, Ind ind, const DevIn& in, size_t cols, size_t rows, const Combo& c,
+                         float* const* out) {
+    cudaStream_t st = ctx->stream;
+    if (rows > (size_t)INT32_MAX || cols > (size_t)INT32_MAX)
+        return fail(VTA_ERR_INVALID_INPUT, "matrix too large");
+    const int C = (int)cols, R = (int)rows;
+    const int p = (int)c.period;
+    Arena ar(ctx);
+    ar.need(2 * cols * sizeof(int));  // first + first_nan
+    const bool recur = ind == I_EMA || ind == I_DEMA || ind == I_TEMA || ind == I_RSI || ind == I_WILDERS ||
+                       ind == I_ATR;
+    int chunk = 0, nch = 0;
+    if (recur) {
+        chunk = pick_chunk(ctx, R, C);
+        nch = (R + chunk - 1) / chunk;
+        ar.need((size_t)nch * cols * 16);
+        ar.need((size_t)nch * cols * 16);
+    }
+    const int pw = is_wwma(ind) ? p : 0;
+    ar.need(pw * sizeof(float));
+    ar.need(sizeof(int));
+    ar.need(2 * sizeof(double));
+    const size_t pnr_sc = (ind == I_PNR && p > 64) ? (size_t)((R + 255) / 256) * cols * p : 0;
+    ar.need(pnr_sc * sizeof(float));
+    VTA_TRY(ar.commit());
+    int* d_first = ar.take<int>(2 * cols);
+    float* d_agg = recur ? ar.take<float>((size_t)nch * cols * 4) : nullptr;
+    float* d_carry = recur ? ar.take<float>((size_t)nch * cols * 4) : nullptr;
+    float* d_w = ar.take<float>(pw);
+    int* d_p1 = ar.take<int>(1);
+    double* d_ab = ar.take<double>(2);
+    float* d_sc = pnr_sc ? ar.take<float>(pnr_sc) : nullptr;
+
+    if (kInfo[ind].in == IN_X) VTA_TRY(launch_first_valid_tm(in.p[0], C, R, d_first, st));
+    else if (ind == I_DONCHIAN) VTA_TRY(launch_first_valid_tm_hlc(in.p[0], in.p[1], in.p[1], C, R, d_first, st));
+    else VTA_TRY(launch_first_valid_tm_hlc(in.p[0], in.p[1], in.p[2], C, R, d_first, st));
+
+    if (is_wwma(ind)) {
+        int wk = ind == I_ALMA ? WT_ALMA : ind == I_WMA ? WT_WMA : ind == I_SWMA ? WT_SWMA
+               : ind == I_PWMA ? WT_PWMA : ind == I_SINWMA ? WT_SINWMA : WT_TRIMA;
+        const double ab[2] = {c.a, c.b};
+        VTA_TRY(upload(ctx, d_p1, &p, sizeof(int)));
+        VTA_TRY(upload(ctx, d_ab, ab, sizeof ab));
+        VTA_TRY(launch_weights(wk, d_p1, d_ab, d_ab + 1, 1, p, d_w, st));
+        WwmaTmArgs a{};
+        a.x_tm = in.p[0];
+        a.cols = C;
+        a.rows = R;
+        a.first = d_first;
+        a.w = d_w;
+        a.period = p;
+        a.nan_mode = (ind == I_WMA || ind == I_SWMA || ind == I_TRIMA) ? 1 : 0;
+        a.out_tm = out[0];
+        ctx->last_kernel = "wwma_tm_f32";
+        return launch_wwma_tm(a, st);
+    }
+    if (recur) {
+        RecurArgs a{};
+        a.kind = ind == I_EMA ? RK_EMA : ind == I_DEMA ? RK_DEMA : ind == I_TEMA ? RK_TEMA
+               : ind == I_RSI ? RK_RSI : ind == I_WILDERS ? RK_WILDERS : RK_ATR;
+        a.layout = 1;
+        a.x = in.p[0];
+        if (ind == I_ATR) { a.h = in.p[0]; a.l = in.p[1]; a.c = in.p[2]; a.x = in.p[2]; }
+        a.n = R;
+        a.cols = C;
+        a.first_tm = d_first;
+        a.period = p;
+        a.n_lanes = C;
+        a.chunk = chunk;
+        a.out = out[0];
+        a.agg = d_agg;
+        a.carry = d_carry;
+        ctx->last_kernel = "recurrence_tm";
+        return launch_recurrence(a, st);
+    }
+    switch (ind) {
+        case I_ADX: case I_SUPERTREND: {
+            HlcArgs a{};
+            a.layout = 1;
+            a.h = in.p[0]; a.l = in.p[1]; a.c = in.p[2];
+            a.n = R;
+            a.cols = C;
+            a.first_tm = d_first;
+            a.period = p;
+            a.factor = (float)c.a;
+            a.n_lanes = C;
+            a.out0 = out[0];
+            a.out1 = ind == I_SUPERTREND ? out[1] : nullptr;
+            ctx->last_kernel = ind == I_ADX ? "adx_tm" : "supertrend_tm";
+            return ind == I_ADX ? launch_adx(a, st) : launch_supertrend(a, st);
+        }
+        case I_SMA: case I_STDDEV: case I_ZSCORE: case I_BB: {
+            PrefixWinTmArgs a{};
+            a.kind = ind == I_SMA ? WK_SMA : ind == I_STDDEV ? WK_STDDEV : ind == I_ZSCORE ? WK_ZSCORE : WK_BB;
+            a.x_tm = in.p[0];
+            a.cols = C;
+            a.rows = R;
+            a.first = d_first;
+            a.period = p;
+            a.k1 = (float)c.a;
+            a.k2 = (float)c.b;
+            a.out0 = out[0];
+            if (ind == I_BB) { a.out1 = out[1]; a.out2 = out[2]; }
+            ctx->last_kernel = "prefix_window_tm";
+            return launch_prefix_window_tm(a, st);
+        }
+        case I_DONCHIAN: case I_WILLR: {
+            MinMaxTmArgs a{};
+            a.kind = ind == I_DONCHIAN ? MM_DONCHIAN : MM_WILLR;
+            a.h = in.p[0]; a.l = in.p[1];
+            a.c = ind == I_WILLR ? in.p[2] : nullptr;
+            a.cols = C;
+            a.rows = R;
+            a.first = d_first;
+            a.period = p;
+            a.out0 = out[0];
+            if (ind == I_DONCHIAN) { a.out1 = out[1]; a.out2 = out[2]; }
+            ctx->last_kernel = "minmax_tm";
+            return launch_minmax_tm(a, st);
+        }
+        case I_PNR: {
+            PnrArgs a{};
+            a.layout = 1;
+            a.x = in.p[0];
+            a.n = R;
+            a.cols = C;
+            a.first_tm = d_first;
+            a.length = p;
+            a.p_frac = (float)(c.a * 0.01);
+            a.n_lanes = C;
+            a.out = out[0];
+            a.scratch = d_sc;
+            ctx->last_kernel = "percentile_tm";
+            return launch_percentile(a, st);
+        }
+        default:
+            return fail(VTA_ERR_NOT_IMPLEMENTED, "indicator not implemented");
+    }
+}
+
+// ------------------------------------------------------------ drivers ------
+static vta_status check_ctx(vta_ctx* ctx) {
+    if (!ctx) return fail(VTA_ERR_INVALID_INPUT, "null context");
+    VTA_CUDA_TRY(cudaSetDevice(ctx->device));
+    return VTA_OK;
+}
+
+static vta_status sync(vta_ctx* ctx) {
+    VTA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return check_launch("stream");
+}
+
+// host inputs -> device outputs (`out_dev` non-null: caller's device buffers;
+// `out_host` non-null: copy results into host buffers of out_len floats)
+static vta_status batch_host(vta_ctx* ctx, Ind ind, const float* const* hin, size_t len,
+                             const std::vector<Combo>& cs, vta_device_array* const* out_arr, float* const* out_host,
+                             size_t out_len, size_t* rows, size_t* cols) {
+    VTA_TRY(check_ctx(ctx));
+    const int nin = kInfo[ind].in, nout = kInfo[ind].n_out;
+    if (len == 0) return fail(VTA_ERR_INVALID_INPUT, std::string(kInfo[ind].name) + ": empty data");
+    for (int k = 0; k < nin; ++k)
+        if (!hin[k]) return fail(VTA_ERR_INVALID_INPUT, "null input pointer");
+    const size_t first = host_first(ind, hin, len);
+    VTA_TRY(validate_combos(ind, cs, len, first));
+    const size_t nc = cs.size();
+    if (nc > SIZE_MAX / len) return fail(VTA_ERR_INVALID_INPUT, "rows*cols overflow");
+    const size_t out_elems = nc * len;
+    if (out_host && out_len < out_elems) return fail(VTA_ERR_INVALID_INPUT, "output buffer too small");
+    VTA_TRY(vram_check(out_elems * sizeof(float) * nout + len * sizeof(float) * nin));
+    // inputs -> device
+    float* d_in = nullptr;
+    VTA_CUDA_TRY(cudaMalloc((void**)&d_in, len * sizeof(float) * nin));
+    std::unique_ptr<void, void (*)(void*)> in_guard(d_in, [](void* p) { cudaFree(p); });
+    DevIn din{};
+    for (int k = 0; k < nin; ++k) {
+        din.p[k] = d_in + (size_t)k * len;
+        VTA_TRY(upload(ctx, d_in + (size_t)k * len, hin[k], len * sizeof(float)));
+    }
+    float* d_out[3] = {nullptr, nullptr, nullptr};
+    for (int k = 0; k < nout; ++k) {
+        cudaError_t e = cudaMalloc((void**)&d_out[k], out_elems * sizeof(float));
+        if (e != cudaSuccess) {
+            for (int j = 0; j < k; ++j) cudaFree(d_out[j]);
+            return cuda_fail(e, "cudaMalloc(output)");
+        }
+    }
+    vta_status s = run_batch(ctx, ind, din, len, first, cs, d_out);
+    if (s == VTA_OK && out_host) {
+        for (int k = 0; k < nout && s == VTA_OK; ++k) {
+            cudaError_t e = cudaMemcpyAsync(out_host[k], d_out[k], out_elems * sizeof(float),
+                                            cudaMemcpyDeviceToHost, ctx->stream);
+            if (e != cudaSuccess) s = cuda_fail(e, "cudaMemcpyAsync(D2H)");
+        }
+    }
+    if (s == VTA_OK) s = sync(ctx);
+    cudaStreamSynchronize(ctx->stream);
+    if (s != VTA_OK || out_host) {
+        for (int k = 0; k < nout; ++k) cudaFree(d_out[k]);
+        if (s != VTA_OK) return s;
+    } else {
+        for (int k = 0; k < nout; ++k) *out_arr[k] = vta_device_array{d_out[k], nc, len, ctx->device};
+    }
+    if (rows) *rows = nc;
+    if (cols) *cols = len;
+    return VTA_OK;
+}
+
+static vta_status batch_device(vta_ctx* ctx, Ind ind, const float* const* din_p, size_t len, size_t first,
+                               const std::vector<Combo>& cs, float* const* d_out) {
+    VTA_TRY(check_ctx(ctx));
+    const int nin = kInfo[ind].in, nout = kInfo[ind].n_out;
+    if (len == 0) return fail(VTA_ERR_INVALID_INPUT, std::string(kInfo[ind].name) + ": empty data");
+    for (int k = 0; k < nin; ++k)
+        if (!din_p[k]) return fail(VTA_ERR_INVALID_INPUT, "null input pointer");
+    for (int k = 0; k < nout; ++k)
+        if (!d_out[k]) return fail(VTA_ERR_INVALID_INPUT, "null output pointer");
+    VTA_TRY(validate_combos(ind, cs, len, first));
+    DevIn din{};
+    for (int k = 0; k < nin; ++k) din.p[k] = din_p[k];
+    VTA_TRY(run_batch(ctx, ind, din, len, first, cs, d_out));
+    return sync(ctx);
+}
+
+static vta_status tm_validate_host(Ind ind, const float* const* hin, size_t cols, size_t rows, const Combo& c) {
+    VTA_TRY(validate_combo(ind, c, rows));
+    for (size_t s = 0; s < cols; ++s) {
+        const size_t f = host_first(ind, hin, rows, cols, s);
+        char buf[160];
+        if (f >= rows) {
+            std::snprintf(buf, sizeof buf, "%s: series %zu all NaN", kInfo[ind].name, s);
+            return fail(VTA_ERR_INVALID_INPUT, buf);
+        }
+        const size_t need = needed_len(ind, c.period);
+        if (rows - f < need) {
+            std::snprintf(buf, sizeof buf, "%s: series %zu not enough valid data (needed >= %zu, valid = %zu)",
+                          kInfo[ind].name, s, need, rows - f);
+            return fail(VTA_ERR_INVALID_INPUT, buf);
+        }
+    }
+    return VTA_OK;
+}
+
+static vta_status tm_host(vta_ctx* ctx, Ind ind, const float* const* hin, size_t cols, size_t rows, const Combo& c,
+                          vta_device_array* const* out_arr) {
+    VTA_TRY(check_ctx(ctx));
+    const int nin = kInfo[ind].in, nout = kInfo[ind].n_out;
+    if (cols == 0 || rows == 0) return fail(VTA_ERR_INVALID_INPUT, "empty matrix");
+    if (cols > SIZE_MAX / rows) return fail(VTA_ERR_INVALID_INPUT, "rows*cols overflow");
+    for (int k = 0; k < nin; ++k)
+        if (!hin[k]) return fail(VTA_ERR_INVALID_INPUT, "null input pointer");
+    VTA_TRY(tm_validate_host(ind, hin, cols, rows, c));
+    const size_t elems = cols * rows;
+    VTA_TRY(vram_check(elems * sizeof(float) * (nin + nout)));
+    float* d_in = nullptr;
+    VTA_CUDA_TRY(cudaMalloc((void**)&d_in, elems * sizeof(float) * nin));
+    std::unique_ptr<void, void (*)(void*)> in_guard(d_in, [](void* p) { cudaFree(p); });
+    DevIn din{};
+    for (int k = 0; k < nin; ++k) {
+        din.p[k] = d_in + (size_t)k * elems;
+        VTA_TRY(upload(ctx, d_in + (size_t)k * elems, hin[k], elems * sizeof(float)));
+    }
+    float* d_out[3] = {nullptr, nullptr, nullptr};
+    for (int k = 0; k < nout; ++k) {
+        cudaError_t e = cudaMalloc((void**)&d_out[k], elems * sizeof(float));
+        if (e != cudaSuccess) {
+            for (int j = 0; j < k; ++j) cudaFree(d_out[j]);
+            return cuda_fail(e, "cudaMalloc(output)");
+        }
+    }
+    vta_status s = run_tm(ctx, ind, din, cols, rows, c, d_out);
+    if (s == VTA_OK) s = sync(ctx);
+    cudaStreamSynchronize(ctx->stream);
+    if (s != VTA_OK) {
+        for (int k = 0; k < nout; ++k) cudaFree(d_out[k]);
+        return s;
+    }
+    for (int k = 0; k < nout; ++k) *out_arr[k] = vta_device_array{d_out[k], rows, cols, ctx->device};
+    return VTA_OK;
+}
+
+static vta_status tm_device(vta_ctx* ctx, Ind ind, const float* const* din_p, size_t cols, size_t rows,
+                            const Combo& c, float* const* d_out) {
+    VTA_TRY(check_ctx(ctx));
+    const int nin = kInfo[ind].in, nout = kInfo[ind].n_out;
+    if (cols == 0 || rows == 0) return fail(VTA_ERR_INVALID_INPUT, "empty matrix");
+    for (int k = 0; k < nin; ++k)
+        if (!din_p[k]) return fail(VTA_ERR_INVALID_INPUT, "null input pointer");
+    for (int k = 0; k < nout; ++k)
+        if (!d_out[k]) return fail(VTA_ERR_INVALID_INPUT, "null output pointer");
+    VTA_TRY(validate_combo(ind, c, rows));
+    DevIn din{};
+    for (int k = 0; k < nin; ++k) din.p[k] = din_p[k];
+    VTA_TRY(run_tm(ctx, ind, din, cols, rows, c, d_out));
+    return sync(ctx);
+}
+
+// ------------------------------------------------------------ grids --------
+static std::vector<Combo> grid_period(Ind ind, const vta_period_batch_range* r) {
+    std::vector<Combo> cs;
+    for (size_t p : axis_usize(r->period, kInfo[ind].axis)) cs.push_back({p, 0.0, 0.0});
+    return cs;
+}
+static std::vector<Combo> grid_alma(const vta_alma_batch_range* r) {
+    std::vector<Combo> cs;
+    for (size_t p : axis_usize(r->period, AX_DESC))
+        for (double o : axis_f64(r->offset))
+            for (double s : axis_f64(r->sigma)) cs.push_back({p, o, s});
+    return cs;
+}
+static std::vector<Combo> grid_p1(Ind ind, vta_range_usize pr, vta_range_f64 ar_) {
+    std::vector<Combo> cs;
+    for (size_t p : axis_usize(pr, kInfo[ind].axis))
+        for (double a : axis_f64(ar_)) cs.push_back({p, a, 0.0});
+    return cs;
+}
+static std::vector<Combo> grid_bb(const vta_bollinger_batch_range* r) {
+    std::vector<Combo> cs;
+    for (size_t p : axis_usize(r->period, AX_DESC))
+        for (double u : axis_f64(r->devup))
+            for (double d : axis_f64(r->devdn)) cs.push_back({p, u, d});
+    return cs;
+}
+
+static std::vector<Combo> grid_of(Ind, const vta_alma_batch_range* r) { return grid_alma(r); }
+static std::vector<Combo> grid_of(Ind ind, const vta_period_batch_range* r) { return grid_period(ind, r); }
+static std::vector<Combo> grid_of(Ind ind, const vta_stddev_batch_range* r) { return grid_p1(ind, r->period, r->nbdev); }
+static std::vector<Combo> grid_of(Ind ind, const vta_zscore_batch_range* r) { return grid_p1(ind, r->period, r->nbdev); }
+static std::vector<Combo> grid_of(Ind, const vta_bollinger_batch_range* r) { return grid_bb(r); }
+static std::vector<Combo> grid_of(Ind ind, const vta_supertrend_batch_range* r) { return grid_p1(ind, r->period, r->factor); }
+static std::vector<Combo> grid_of(Ind ind, const vta_percentile_batch_range* r) { return grid_p1(ind, r->length, r->percentage); }
+
+static Combo combo_of(const vta_alma_params* p) { return {p->period, p->offset, p->sigma}; }
+static Combo combo_of(const vta_period_params* p) { return {p->period, 0.0, 0.0}; }
+static Combo combo_of(const vta_stddev_params* p) { return {p->period, p->nbdev, 0.0}; }
+static Combo combo_of(const vta_zscore_params* p) { return {p->period, p->nbdev, 0.0}; }
+static Combo combo_of(const vta_bollinger_params* p) { return {p->period, p->devup, p->devdn}; }
+static Combo combo_of(const vta_supertrend_params* p) { return {p->period, p->factor, 0.0}; }
+static Combo combo_of(const vta_percentile_params* p) { return {p->length, p->percentage, 0.0}; }
+
+static void params_of(const Combo& c, vta_alma_params* p) { *p = {c.period, c.a, c.b}; }
+static void params_of(const Combo& c, vta_period_params* p) { *p = {c.period}; }
+static void params_of(const Combo& c, vta_stddev_params* p) { *p = {c.period, c.a}; }
+static void params_of(const Combo& c, vta_zscore_params* p) { *p = {c.period, c.a}; }
+static void params_of(const Combo& c, vta_bollinger_params* p) { *p = {c.period, c.a, c.b}; }
+static void params_of(const Combo& c, vta_supertrend_params* p) { *p = {c.period, c.a}; }
+static void params_of(const Combo& c, vta_percentile_params* p) { *p = {c.period, c.a}; }
+
+template <class R, class P>
+static vta_status expand(Ind ind, const R* r, P* out, size_t cap, size_t* n) {
+    if (!r) return fail(VTA_ERR_INVALID_INPUT, "null sweep");
+    std::vector<Combo> cs = grid_of(ind, r);
+    if (n) *n = cs.size();
+    if (out)
+        for (size_t i = 0; i < cs.size() && i < cap; ++i) params_of(cs[i], &out[i]);
+    return cs.empty() ? fail(VTA_ERR_INVALID_INPUT, "empty range") : VTA_OK;
+}
+
+}  // namespace vta
+
+using namespace vta;
+
+// ============================================================ C ABI ========
+extern "C" {
+
+const char* vta_last_error(void) { return g_err.c_str(); }
+const char* vta_version(void) { return "vta_gb300 0.1.0 (sm_103a)"; }
+
+int vta_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+vta_status vta_ctx_create(int device_id, vta_ctx** out) {
+    if (!out) return fail(VTA_ERR_INVALID_INPUT, "null out");
+    *out = nullptr;
+    int n = 0;
+    VTA_CUDA_TRY(cudaGetDeviceCount(&n));
+    if (device_id < 0 || device_id >= n) return fail(VTA_ERR_INVALID_INPUT, "device id out of range");
+    VTA_CUDA_TRY(cudaSetDevice(device_id));
+    auto* c = new vta_ctx();
+    c->device = device_id;
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, device_id) == cudaSuccess) {
+        c->num_sms = prop.multiProcessorCount;
+        c->smem_optin = prop.sharedMemPerBlockOptin;
+        if (prop.major != 10 || prop.minor != 3) {
+            // the kernels are built for sm_103a only
+            char buf[128];
+            std::snprintf(buf, sizeof buf, "device %d is sm_%d%d; this library is built for sm_103a", device_id,
+                          prop.major, prop.minor);
+            delete c;
+            return fail(VTA_ERR_MISSING_KERNEL_SYMBOL, buf);
+        }
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "cudaStreamCreate");
+    }
+    const char* pol = std::getenv("VTA_WMA_BATCH");
+    if (pol) vta_ctx_set_policy(c, "wma_batch", pol);
+    *out = c;
+    return VTA_OK;
+}
+
+vta_status vta_ctx_destroy(vta_ctx* ctx) {
+    if (!ctx) return VTA_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return VTA_OK;
+}
+
+vta_status vta_ctx_synchronize(vta_ctx* ctx) {
+    VTA_TRY(check_ctx(ctx));
+    return sync(ctx);
+}
+
+vta_status vta_ctx_set_stream(vta_ctx* ctx, void* stream) {
+    VTA_TRY(check_ctx(ctx));
+    if (stream) {
+        if (ctx->own_stream && ctx->stream) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaStreamDestroy(ctx->stream);
+        }
+        ctx->stream = (cudaStream_t)stream;
+        ctx->own_stream = false;
+    } else if (!ctx->own_stream) {
+        VTA_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        ctx->own_stream = true;
+    }
+    return VTA_OK;
+}
+
+void* vta_ctx_get_stream(vta_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+vta_status vta_ctx_set_policy(vta_ctx* ctx, const char* key, const char* value) {
+    if (!ctx || !key || !value) return fail(VTA_ERR_INVALID_POLICY, "null policy argument");
+    const std::string k(key), v(value);
+    if (k == "wma_batch") {
+        if (v == "auto") ctx->policy.wma_batch = 0;
+        else if (v == "plain") ctx->policy.wma_batch = 1;
+        else if (v == "tc_fp16x3") ctx->policy.wma_batch = 2;
+        else if (v == "tc_bf16x3") ctx->policy.wma_batch = 3;
+        else return fail(VTA_ERR_INVALID_POLICY, "wma_batch: auto|plain|tc_fp16x3|tc_bf16x3");
+        return VTA_OK;
+    }
+    if (k == "recur_chunk") {
+        if (v == "auto") ctx->policy.recur_chunk = 0;
+        else if (v == "sequential") ctx->policy.recur_chunk = 1;
+        else {
+            char* end = nullptr;
+            long x = std::strtol(v.c_str(), &end, 10);
+            if (!end || *end || x < 32 || x % 32) return fail(VTA_ERR_INVALID_POLICY, "recur_chunk: multiple of 32");
+            ctx->policy.recur_chunk = (int)x;
+        }
+        return VTA_OK;
+    }
+    return fail(VTA_ERR_INVALID_POLICY, "unknown policy key");
+}
+
+const char* vta_ctx_last_kernel(vta_ctx* ctx) { return ctx ? ctx->last_kernel.c_str() : ""; }
+size_t vta_ctx_scratch_bytes(vta_ctx* ctx) { return ctx ? ctx->scratch_bytes : 0; }
+
+vta_status vta_device_array_free(vta_device_array* a) {
+    if (!a || !a->ptr) return VTA_OK;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(a->device);
+    cudaError_t e = cudaFree(a->ptr);
+    cudaSetDevice(cur);
+    a->ptr = nullptr;
+    a->rows = a->cols = 0;
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFree");
+    return VTA_OK;
+}
+
+vta_status vta_device_array_copy_to_host(vta_ctx* ctx, const vta_device_array* a, float* host, size_t n) {
+    VTA_TRY(check_ctx(ctx));
+    if (!a || !host) return fail(VTA_ERR_INVALID_INPUT, "null argument");
+    if (a->device != ctx->device) {
+        char buf[96];
+        std::snprintf(buf, sizeof buf, "device mismatch: buf=%d current=%d", a->device, ctx->device);
+        return fail(VTA_ERR_DEVICE_MISMATCH, buf);
+    }
+    if (n < a->rows * a->cols) return fail(VTA_ERR_INVALID_INPUT, "host buffer too small");
+    VTA_CUDA_TRY(cudaMemcpyAsync(host, a->ptr, a->rows * a->cols * sizeof(float), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    return sync(ctx);
+}
+
+vta_status vta_pinned_alloc(size_t bytes, void** out) {
+    if (!out) return fail(VTA_ERR_INVALID_INPUT, "null out");
+    VTA_CUDA_TRY(cudaHostAlloc(out, bytes, cudaHostAllocDefault));
+    return VTA_OK;
+}
+vta_status vta_pinned_free(void* p) {
+    if (p) VTA_CUDA_TRY(cudaFreeHost(p));
+    return VTA_OK;
+}
+vta_status vta_device_alloc(vta_ctx* ctx, size_t bytes, void** out) {
+    VTA_TRY(check_ctx(ctx));
+    if (!out) return fail(VTA_ERR_INVALID_INPUT, "null out");
+    VTA_TRY(vram_check(bytes));
+    VTA_CUDA_TRY(cudaMalloc(out, bytes));
+    return VTA_OK;
+}
+vta_status vta_device_free(vta_ctx* ctx, void* p) {
+    VTA_TRY(check_ctx(ctx));
+    if (p) VTA_CUDA_TRY(cudaFree(p));
+    return VTA_OK;
+}
+vta_status vta_memcpy_h2d(vta_ctx* ctx, void* dst, const void* src, size_t bytes) {
+    VTA_TRY(check_ctx(ctx));
+    VTA_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    return sync(ctx);
+}
+vta_status vta_memcpy_d2h(vta_ctx* ctx, void* dst, const void* src, size_t bytes) {
+    VTA_TRY(check_ctx(ctx));
+    VTA_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return sync(ctx);
+}
+
+// ---------------------------------------------------- per-indicator ABI ----
+#include "vta_abi_gen.inc"
+
+}  // extern "C"

@@ -1,0 +1,277 @@
+// Internal declarations shared by the host API (vta_api.cu) and the kernel
+// translation units.  Nothing here is part of the C ABI (include/vta_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <cstddef>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "../../include/vta_gb300.h"
+
+namespace vta {
+
+// ---------------------------------------------------------------- errors ---
+void set_error(const std::string& msg);
+vta_status fail(vta_status st, const std::string& msg);
+vta_status cuda_fail(cudaError_t e, const char* what);
+
+#define VTA_CUDA_TRY(expr)                                         \
+    do {                                                           \
+        cudaError_t _e = (expr);                                   \
+        if (_e != cudaSuccess) return ::vta::cuda_fail(_e, #expr); \
+    } while (0)
+
+#define VTA_TRY(expr)                        \
+    do {                                     \
+        vta_status _s = (expr);              \
+        if (_s != VTA_OK) return _s;         \
+    } while (0)
+
+// Checks the launch that was just enqueued.
+vta_status check_launch(const char* kernel);
+
+// ---------------------------------------------------------------- launch ---
+constexpr int kNumSMs = 152;     // GB300: 2 dies x 76 SMs (re-read at ctx create)
+constexpr int kChunkMin = 256;   // smallest time chunk of the chunked scans
+
+struct Policy {
+    // weighted-window batch kernel: 0 = auto, 1 = plain FP32, 2 = tcgen05 fp16x3,
+    // 3 = tcgen05 bf16x3
+    int wma_batch = 0;
+    // recurrence time-chunk length (0 = auto); 1 = whole series (plain
+    // sequential per-combo kernel)
+    int recur_chunk = 0;
+};
+
+}  // namespace vta
+
+// The opaque context of the C ABI.
+struct vta_ctx {
+    int device = 0;
+    int num_sms = vta::kNumSMs;
+    size_t smem_optin = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = true;
+    void* scratch = nullptr;  // growing device workspace, owned by the ctx
+    size_t scratch_bytes = 0;
+    vta::Policy policy;
+    std::string last_kernel;
+};
+
+namespace vta {
+
+// Bump allocator over the ctx workspace.  Usage: first `need()` every piece,
+// then `commit()` (grows the workspace with cudaMalloc when too small), then
+// `take()` the pieces in the same order.  Pieces are 256-byte aligned.
+class Arena {
+   public:
+    explicit Arena(vta_ctx* c) : ctx_(c) {}
+    void need(size_t bytes) { total_ += align(bytes); }
+    vta_status commit();
+    template <class T>
+    T* take(size_t count) {
+        char* p = static_cast<char*>(ctx_->scratch) + off_;
+        off_ += align(count * sizeof(T));
+        return reinterpret_cast<T*>(p);
+    }
+    size_t total() const { return total_; }
+
+   private:
+    static size_t align(size_t b) { return (b + 255) & ~size_t(255); }
+    vta_ctx* ctx_;
+    size_t total_ = 0;
+    size_t off_ = 0;
+};
+
+// VRAM admission check mirroring the crate's wrappers: required + 64 MiB
+// headroom must fit in free memory (disabled with VTA_MEM_CHECK=0).
+vta_status vram_check(size_t required_bytes);
+
+inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+// ------------------------------------------------------- kernel launchers ---
+// Every launcher enqueues on `st` and returns the launch status.
+
+// First valid (non-NaN) index of each time-major series; rows if all NaN.
+vta_status launch_first_valid_tm(const float* x_tm, int cols, int rows, int* first, cudaStream_t st);
+// Same over the three HLC inputs (first index where all three are non-NaN).
+vta_status launch_first_valid_tm_hlc(const float* h, const float* l, const float* c, int cols,
+                                     int rows, int* first, cudaStream_t st);
+
+// Inclusive f64 prefix of f(x[i]) for i >= first (0 before first), with
+// f selected by `kind`; optionally packed to double-single float2.
+enum PrefixKind { PK_X = 0, PK_X2 = 1, PK_GAIN = 2, PK_LOSS = 3, PK_NAN = 4 };
+vta_status launch_prefix_f64(const float* x, int n, int first, int kind, double* out_f64,
+                             float2* out_ds, double* block_tmp, cudaStream_t st);
+size_t prefix_tmp_doubles(int n);
+
+// --- weighted-window moving averages (ALMA/WMA/SWMA/PWMA/SINWMA/TRIMA) ----
+// Row weights are right-aligned into a [n_combos][kmax] f32 matrix.
+struct WwmaBatchArgs {
+    const float* x;        // series (device)
+    int n;                 // series length
+    int first;             // first valid index
+    const float* w;        // [n_combos][kmax] normalised weights, right-aligned
+    const int* periods;    // [n_combos]
+    const int* tile_kmax;  // per 16-combo tile: max period (K of the tile)
+    int kmax;
+    int n_combos;
+    int nan_mode;          // 0: window NaN -> NaN; 1: NaN poisons all later outputs
+    const double* nanp;    // [n] count of NaN in x[first..i] (null: series has none)
+    float* out;            // [n_combos][n]
+};
+enum WeightKind { WT_ALMA = 0, WT_WMA = 1, WT_SWMA = 2, WT_PWMA = 3, WT_SINWMA = 4, WT_TRIMA = 5 };
+vta_status launch_weights(int kind, const int* periods, const double* pa, const double* pb, int n_combos,
+                          int kmax, float* w, cudaStream_t st);
+vta_status launch_wwma_batch_plain(const WwmaBatchArgs& a, cudaStream_t st);
+// tcgen05 split-precision contraction; returns VTA_ERR_NOT_IMPLEMENTED when
+// the shape is unsupported (caller falls back to the plain kernel).
+vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ctx,
+                                cudaStream_t st);
+
+struct WwmaTmArgs {
+    const float* x_tm;
+    int cols, rows;
+    const int* first;      // per-series first valid
+    const float* w;        // [period] normalised weights
+    int period;
+    int nan_mode;
+    float* out_tm;
+};
+vta_status launch_wwma_tm(const WwmaTmArgs& a, cudaStream_t st);
+
+// ------------------------------------------------- chunked recurrences -----
+enum RecurKind { RK_EMA = 0, RK_DEMA = 1, RK_TEMA = 2, RK_RSI = 3, RK_WILDERS = 4, RK_ATR = 5 };
+
+struct RecurArgs {
+    int kind;
+    int layout;            // 0 = batch (one series, lane = combo), 1 = time-major
+    // inputs: batch -> x[n] (or h,l,c); tm -> x_tm[t*cols+s]
+    const float* x;
+    const float* h;
+    const float* l;
+    const float* c;
+    int n;                 // series length (batch) / rows (tm)
+    int cols;              // tm: number of series
+    int first;             // batch: first valid index
+    const int* first_tm;   // tm: per-series first valid
+    const int* periods;    // batch: per combo period; tm: null
+    int period;            // tm: the single period
+    int n_lanes;           // batch: n_combos; tm: cols
+    // f64 prefixes for seeds (batch): EMA/Wilders: x; RSI: gains, losses
+    const double* p0;
+    const double* p1;
+    int chunk;             // time chunk length (multiple of 32)
+    float* out;            // batch [n_combos][n]; tm [n][cols]
+    // scratch
+    float* agg;            // [n_chunks][n_lanes] float4 (state, applied steps)
+    float* carry;          // [n_chunks][n_lanes] float4 (carry-in state)
+};
+vta_status launch_recurrence(const RecurArgs& a, cudaStream_t st);
+int recur_state_dim(int kind);
+
+// ADX (two-level recurrence) and SuperTrend (state machine).
+struct HlcArgs {
+    int layout;
+    const float* h;
+    const float* l;
+    const float* c;
+    int n, cols, first;
+    const int* first_tm;
+    const int* periods;    // batch
+    const float* factors;  // supertrend batch
+    int period;
+    float factor;
+    int n_lanes;
+    float* out0;           // adx / trend
+    float* out1;           // changed
+};
+vta_status launch_adx(const HlcArgs& a, cudaStream_t st);
+vta_status launch_supertrend(const HlcArgs& a, cudaStream_t st);
+
+// ------------------------------------------------- prefix-sum windows ------
+enum WinKind { WK_SMA = 0, WK_STDDEV = 1, WK_ZSCORE = 2, WK_BB = 3 };
+struct PrefixWinArgs {
+    int kind;
+    const float* x;
+    const float2* p1;      // double-single prefix of x  (index i -> sum x[first..i])
+    const float2* p2;      // double-single prefix of x^2
+    int n, first;
+    const int* periods;
+    const float* k1;       // stddev/zscore nbdev; bb devup
+    const float* k2;       // bb devdn
+    int n_combos;
+    float* out0;           // sma/stddev/zscore/bb upper
+    float* out1;           // bb middle
+    float* out2;           // bb lower
+};
+vta_status launch_prefix_window_batch(const PrefixWinArgs& a, cudaStream_t st);
+
+struct PrefixWinTmArgs {
+    int kind;
+    const float* x_tm;
+    int cols, rows;
+    const int* first;
+    int period;
+    float k1, k2;
+    float* out0;
+    float* out1;
+    float* out2;
+};
+vta_status launch_prefix_window_tm(const PrefixWinTmArgs& a, cudaStream_t st);
+
+// ------------------------------------------------- min/max windows ---------
+enum MinMaxKind { MM_DONCHIAN = 0, MM_WILLR = 1 };
+struct MinMaxArgs {
+    int kind;
+    const float* h;
+    const float* l;
+    const float* c;        // willr only
+    int n, first;
+    const int* periods;
+    int n_combos;
+    int pmax;
+    float* out0;           // donchian upper / willr
+    float* out1;           // donchian middle
+    float* out2;           // donchian lower
+};
+vta_status launch_minmax_batch(const MinMaxArgs& a, size_t smem_optin, cudaStream_t st);
+
+struct MinMaxTmArgs {
+    int kind;
+    const float* h;
+    const float* l;
+    const float* c;
+    int cols, rows;
+    const int* first;
+    int period;
+    float* out0;
+    float* out1;
+    float* out2;
+};
+vta_status launch_minmax_tm(const MinMaxTmArgs& a, cudaStream_t st);
+
+// ------------------------------------------------- nearest-rank percentile -
+struct PnrArgs {
+    int layout;
+    const float* x;
+    int n, cols, first;
+    const int* first_tm;
+    const int* lengths;     // batch per combo
+    const float* pfrac;     // batch per combo (percentage * 0.01)
+    int length;             // tm
+    float p_frac;           // tm
+    int n_lanes;
+    float* out;
+    float* scratch;         // batch: per-thread sorted windows
+    size_t scratch_floats;
+};
+vta_status launch_percentile(const PnrArgs& a, cudaStream_t st);
+
+}  // namespace vta

@@ -1,0 +1,382 @@
+"""Python mirror of the crate's per-indicator CUDA wrappers (src/cuda/*).
+
+For every indicator X there is a class ``CudaX`` (``CudaAlma``, ``CudaEma`` ...)
+whose constructor takes a device id like ``CudaAlma::new(device_id)``
+(alma_wrapper.rs:133) and whose methods keep the wrapper names:
+
+    x_batch_dev(data_f32, sweep)                          -> DeviceArrayF32
+    x_batch_into_host_f32(data_f32, sweep)                -> (ndarray, rows, cols)
+    x_batch_device(d_data, len, first_valid, sweep, d_out)
+    x_many_series_one_param_time_major_dev(data_tm, params) -> DeviceArrayF32
+    x_many_series_one_param_device(d_data_tm, cols, rows, params, d_out)
+    expand_grid(sweep)                                    -> list of params
+
+High/low/close indicators take ``high, low, close`` (Donchian: ``high, low``)
+where the crate does; multi-output indicators return tuples.  Sweeps are the
+crate's ``XBatchRange`` as plain tuples ``(start, end, step)``; errors raise
+``VtaError`` whose ``kind`` is the crate's error variant.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field, fields
+from typing import Any
+
+import numpy as np
+
+from . import _native as N
+
+__all__ = ["DeviceArrayF32", "Context", "VtaError"]
+VtaError = N.VtaError
+
+
+# ------------------------------------------------------------------ sweeps --
+@dataclass
+class AlmaBatchRange:
+    period: tuple = (9, 258, 1)       # alma.rs:1074-1082
+    offset: tuple = (0.85, 0.85, 0.0)
+    sigma: tuple = (6.0, 6.0, 0.0)
+
+
+@dataclass
+class PeriodBatchRange:
+    period: tuple = (9, 258, 1)
+
+
+@dataclass
+class StdDevBatchRange:
+    period: tuple = (5, 254, 1)       # stddev.rs:578-585
+    nbdev: tuple = (1.0, 1.0, 0.0)
+
+
+@dataclass
+class ZscoreBatchRange:
+    period: tuple = (14, 263, 1)      # zscore.rs:793-802 (ma_type "sma", devtype 0)
+    nbdev: tuple = (1.0, 1.0, 0.0)
+
+
+@dataclass
+class BollingerBandsBatchRange:
+    period: tuple = (20, 269, 1)      # bollinger_bands.rs:1095-1104
+    devup: tuple = (2.0, 2.0, 0.0)
+    devdn: tuple = (2.0, 2.0, 0.0)
+
+
+@dataclass
+class SuperTrendBatchRange:
+    period: tuple = (10, 10, 0)
+    factor: tuple = (3.0, 3.0, 0.0)
+
+
+@dataclass
+class PercentileNearestRankBatchRange:
+    length: tuple = (15, 264, 1)      # percentile_nearest_rank.rs:820-827
+    percentage: tuple = (50.0, 50.0, 0.0)
+
+
+@dataclass
+class AlmaParams:
+    period: int = 9
+    offset: float = 0.85
+    sigma: float = 6.0
+
+
+@dataclass
+class PeriodParams:
+    period: int = 9
+
+
+@dataclass
+class StdDevParams:
+    period: int = 5
+    nbdev: float = 1.0
+
+
+@dataclass
+class ZscoreParams:
+    period: int = 14
+    nbdev: float = 1.0
+
+
+@dataclass
+class BollingerBandsParams:
+    period: int = 20
+    devup: float = 2.0
+    devdn: float = 2.0
+
+
+@dataclass
+class SuperTrendParams:
+    period: int = 10
+    factor: float = 3.0
+
+
+@dataclass
+class PercentileNearestRankParams:
+    length: int = 15
+    percentage: float = 50.0
+
+
+_RANGE_CLS = {"alma": AlmaBatchRange, "period": PeriodBatchRange, "stddev": StdDevBatchRange,
+              "zscore": ZscoreBatchRange, "bollinger": BollingerBandsBatchRange,
+              "supertrend": SuperTrendBatchRange, "percentile": PercentileNearestRankBatchRange}
+_PARAM_CLS = {"alma": AlmaParams, "period": PeriodParams, "stddev": StdDevParams,
+              "zscore": ZscoreParams, "bollinger": BollingerBandsParams,
+              "supertrend": SuperTrendParams, "percentile": PercentileNearestRankParams}
+
+
+def _to_sweep(fam: str, sweep) -> Any:
+    S = N.SWEEPS[fam]
+    if sweep is None:
+        sweep = _RANGE_CLS[fam]()
+    s = S()
+    for fname, ftype in S._fields_:
+        v = getattr(sweep, fname) if not isinstance(sweep, dict) else sweep[fname]
+        if ftype is N.RangeUsize:
+            setattr(s, fname, N.RangeUsize(int(v[0]), int(v[1]), int(v[2])))
+        else:
+            setattr(s, fname, N.RangeF64(float(v[0]), float(v[1]), float(v[2])))
+    return s
+
+
+def _to_params(fam: str, params) -> Any:
+    P = N.PARAMS[fam]
+    if params is None:
+        params = _PARAM_CLS[fam]()
+    p = P()
+    for fname, ftype in P._fields_:
+        v = getattr(params, fname) if not isinstance(params, dict) else params[fname]
+        setattr(p, fname, int(v) if ftype is C.c_size_t else float(v))
+    return p
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _dptr(obj) -> int:
+    """Device pointer of a torch tensor, a __cuda_array_interface__ object or an int."""
+    if isinstance(obj, int):
+        return obj
+    if hasattr(obj, "data_ptr"):
+        return int(obj.data_ptr())
+    if hasattr(obj, "__cuda_array_interface__"):
+        return int(obj.__cuda_array_interface__["data"][0])
+    if isinstance(obj, DeviceArrayF32):
+        return obj.ptr
+    raise TypeError(f"not a device buffer: {type(obj)!r}")
+
+
+# ------------------------------------------------------------------ context --
+class Context:
+    """Owns a vta_ctx (one stream and a scratch workspace on one device)."""
+
+    def __init__(self, device_id: int = 0):
+        L = N.lib()
+        h = C.c_void_p()
+        N.check(L.vta_ctx_create(int(device_id), C.byref(h)))
+        self.handle = h
+        self.device_id = int(device_id)
+
+    def synchronize(self):
+        N.check(N.lib().vta_ctx_synchronize(self.handle))
+
+    def set_policy(self, key: str, value: str):
+        N.check(N.lib().vta_ctx_set_policy(self.handle, key.encode(), str(value).encode()))
+
+    def set_stream(self, cuda_stream: int | None):
+        N.check(N.lib().vta_ctx_set_stream(self.handle, C.c_void_p(cuda_stream or 0)))
+
+    @property
+    def stream(self) -> int:
+        return int(N.lib().vta_ctx_get_stream(self.handle) or 0)
+
+    @property
+    def last_kernel(self) -> str:
+        return N.lib().vta_ctx_last_kernel(self.handle).decode()
+
+    @property
+    def scratch_bytes(self) -> int:
+        return int(N.lib().vta_ctx_scratch_bytes(self.handle))
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            N.lib().vta_ctx_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceArrayF32:
+    """Owned device array (alma_wrapper.rs:103-117) with zero-copy export via
+    ``__cuda_array_interface__`` (torch.as_tensor / cupy.asarray work on it),
+    as the crate's DeviceArrayF32Py does (dlpack_cuda.rs:267-374)."""
+
+    def __init__(self, c: N.DeviceArrayC, ctx: Context):
+        self._c = c
+        self._ctx = ctx  # keeps the context (and its device) alive
+
+    @property
+    def ptr(self) -> int:
+        return int(self._c.ptr or 0)
+
+    @property
+    def rows(self) -> int:
+        return int(self._c.rows)
+
+    @property
+    def cols(self) -> int:
+        return int(self._c.cols)
+
+    @property
+    def shape(self):
+        return (self.rows, self.cols)
+
+    def __len__(self):
+        return self.rows * self.cols
+
+    @property
+    def __cuda_array_interface__(self):
+        return {"shape": (self.rows, self.cols), "typestr": "<f4", "data": (self.ptr, False),
+                "version": 3, "strides": None}
+
+    def to_host(self) -> np.ndarray:
+        out = np.empty((self.rows, self.cols), dtype=np.float32)
+        N.check(N.lib().vta_device_array_copy_to_host(
+            self._ctx.handle, C.byref(self._c), out.ctypes.data_as(C.POINTER(C.c_float)), out.size))
+        return out
+
+    def free(self):
+        if self._c.ptr:
+            N.lib().vta_device_array_free(C.byref(self._c))
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------- indicators --
+class _CudaIndicator:
+    NAME = ""
+
+    def __init__(self, device_id: int = 0):
+        self.ctx = Context(device_id)
+        kind, outs, fam = N.INDICATORS[self.NAME]
+        self._kind, self._outs, self._fam = kind, outs, fam
+        self._nin = N.N_IN[kind]
+
+    # crate: CudaX::synchronize / set_policy / selected kernel
+    def synchronize(self):
+        self.ctx.synchronize()
+
+    def set_policy(self, key: str, value: str):
+        self.ctx.set_policy(key, value)
+
+    @property
+    def last_kernel(self) -> str:
+        return self.ctx.last_kernel
+
+    def _fn(self, suffix):
+        return getattr(N.lib(), f"vta_{self.NAME}_{suffix}")
+
+    def _wrap(self, arrs):
+        res = [DeviceArrayF32(a, self.ctx) for a in arrs]
+        return res[0] if len(res) == 1 else tuple(res)
+
+    def expand_grid(self, sweep=None) -> list:
+        s = _to_sweep(self._fam, sweep)
+        n = C.c_size_t()
+        self._fn("expand_grid")(C.byref(s), None, 0, C.byref(n))
+        P = N.PARAMS[self._fam]
+        buf = (P * max(n.value, 1))()
+        N.check(self._fn("expand_grid")(C.byref(s), buf, n.value, C.byref(n)))
+        return [{f: getattr(buf[i], f) for f, _ in P._fields_} for i in range(n.value)]
+
+    def batch_dev(self, *inputs, sweep=None):
+        ins = [_f32(a) for a in inputs]
+        assert len(ins) == self._nin, f"{self.NAME} takes {self._nin} input series"
+        n = ins[0].size
+        assert all(a.size == n for a in ins), "inconsistent input lengths"
+        outs = [N.DeviceArrayC() for _ in self._outs]
+        N.check(self._fn("batch_dev")(self.ctx.handle, *[a.ctypes.data for a in ins], n,
+                                      C.byref(_to_sweep(self._fam, sweep)), *[C.byref(o) for o in outs]))
+        return self._wrap(outs)
+
+    def batch_into_host_f32(self, *inputs, sweep=None, out=None):
+        ins = [_f32(a) for a in inputs]
+        n = ins[0].size
+        s = _to_sweep(self._fam, sweep)
+        rows = len(self.expand_grid(sweep))
+        hs = out if out is not None else [np.empty((rows, n), dtype=np.float32) for _ in self._outs]
+        r, c = C.c_size_t(), C.c_size_t()
+        N.check(self._fn("batch_into_host_f32")(self.ctx.handle, *[a.ctypes.data for a in ins], n, C.byref(s),
+                                                *[h.ctypes.data for h in hs], rows * n, C.byref(r), C.byref(c)))
+        res = hs[0] if len(hs) == 1 else tuple(hs)
+        return res, r.value, c.value
+
+    def batch_device(self, d_inputs, length: int, first_valid: int, sweep, d_outs):
+        d_inputs = d_inputs if isinstance(d_inputs, (list, tuple)) else [d_inputs]
+        d_outs = d_outs if isinstance(d_outs, (list, tuple)) else [d_outs]
+        N.check(self._fn("batch_device")(self.ctx.handle, *[_dptr(x) for x in d_inputs], int(length),
+                                         int(first_valid), C.byref(_to_sweep(self._fam, sweep)),
+                                         *[_dptr(o) for o in d_outs]))
+
+    def many_series_one_param_time_major_dev(self, *inputs_tm, params=None):
+        ins = [_f32(a) for a in inputs_tm]
+        assert len(ins) == self._nin
+        rows, cols = ins[0].shape
+        outs = [N.DeviceArrayC() for _ in self._outs]
+        N.check(self._fn("many_series_one_param_time_major_dev")(
+            self.ctx.handle, *[a.ctypes.data for a in ins], cols, rows,
+            C.byref(_to_params(self._fam, params)), *[C.byref(o) for o in outs]))
+        return self._wrap(outs)
+
+    def many_series_one_param_device(self, d_inputs_tm, cols: int, rows: int, params, d_outs):
+        d_inputs_tm = d_inputs_tm if isinstance(d_inputs_tm, (list, tuple)) else [d_inputs_tm]
+        d_outs = d_outs if isinstance(d_outs, (list, tuple)) else [d_outs]
+        N.check(self._fn("many_series_one_param_device")(
+            self.ctx.handle, *[_dptr(x) for x in d_inputs_tm], int(cols), int(rows),
+            C.byref(_to_params(self._fam, params)), *[_dptr(o) for o in d_outs]))
+
+
+def _make(name: str, cls_name: str):
+    def method(suffix):
+        def f(self, *a, **k):
+            return getattr(_CudaIndicator, suffix)(self, *a, **k)
+        f.__name__ = f"{name}_{suffix}"
+        return f
+
+    ns = {"NAME": name}
+    for suffix in ("batch_dev", "batch_into_host_f32", "batch_device",
+                   "many_series_one_param_time_major_dev", "many_series_one_param_device"):
+        ns[f"{name}_{suffix}"] = method(suffix)
+    cls = type(cls_name, (_CudaIndicator,), ns)
+    globals()[cls_name] = cls
+    __all__.append(cls_name)
+    return cls
+
+
+_CLASS_NAMES = {
+    "alma": "CudaAlma", "ema": "CudaEma", "dema": "CudaDema", "tema": "CudaTema", "rsi": "CudaRsi",
+    "wilders": "CudaWilders", "sma": "CudaSma", "wma": "CudaWma", "swma": "CudaSwma", "pwma": "CudaPwma",
+    "sinwma": "CudaSinwma", "trima": "CudaTrima", "stddev": "CudaStddev", "zscore": "CudaZscore",
+    "bollinger_bands": "CudaBollingerBands", "atr": "CudaAtr", "adx": "CudaAdx",
+    "supertrend": "CudaSupertrend", "donchian": "CudaDonchian", "willr": "CudaWillr",
+    "percentile_nearest_rank": "CudaPercentileNearestRank",
+}
+CLASSES = {name: _make(name, cls) for name, cls in _CLASS_NAMES.items()}
+__all__ += ["AlmaBatchRange", "PeriodBatchRange", "StdDevBatchRange", "ZscoreBatchRange",
+            "BollingerBandsBatchRange", "SuperTrendBatchRange", "PercentileNearestRankBatchRange",
+            "AlmaParams", "PeriodParams", "StdDevParams", "ZscoreParams", "BollingerBandsParams",
+            "SuperTrendParams", "PercentileNearestRankParams", "CLASSES", "device_count"]
+
+
+def device_count() -> int:
+    """cuda_device_count() (src/cuda/mod.rs:560-575)."""
+    return int(N.lib().vta_device_count())

@@ -1,0 +1,86 @@
+"""Seeded synthetic market data with the shapes of the benchmark workloads.
+
+Counter-based RNG: splitmix64 over (seed, stream, index) -> 53-bit uniform ->
+Box-Muller normal.  Prices are a geometric random walk x_0 = 100,
+x_{t+1} = x_t * exp(eps_t), eps ~ N(0, sigma^2).  The same function of
+(seed, length) always yields the same float64 series, on any machine.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+_G = np.uint64(0x9E3779B97F4A7C15)
+
+
+def splitmix64(x: np.ndarray) -> np.ndarray:
+    with np.errstate(over="ignore"):
+        z = x + _G
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        return z ^ (z >> np.uint64(31))
+
+
+def uniform(seed: int, stream: int, n: int, offset: int = 0) -> np.ndarray:
+    """(0, 1) uniforms: 53 high bits of splitmix64(seed<<40 | stream<<32 | i)."""
+    base = (np.uint64(seed & 0xFFFFFF) << np.uint64(40)) | (np.uint64(stream & 0xFF) << np.uint64(32))
+    k = np.arange(offset, offset + n, dtype=np.uint64) + base
+    return ((splitmix64(k) >> np.uint64(11)).astype(np.float64) + 0.5) * (1.0 / 9007199254740992.0)
+
+
+def normal(seed: int, stream: int, n: int) -> np.ndarray:
+    u1 = uniform(seed, 2 * stream, n)
+    u2 = uniform(seed, 2 * stream + 1, n)
+    return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+
+
+def random_walk(n: int, seed: int, sigma: float = 0.01, start: float = 100.0, nan_lead: int = 0) -> np.ndarray:
+    eps = sigma * normal(seed, 0, max(n - 1, 0))
+    x = np.empty(n, dtype=np.float64)
+    if n:
+        x[0] = 0.0
+        np.cumsum(eps, out=x[1:])
+        x = start * np.exp(x)
+    x[:nan_lead] = np.nan
+    return x
+
+
+def high_low(close: np.ndarray, seed: int, sigma: float = 0.005):
+    """high/low = close * (1 +- |N(0, sigma^2)|) (the recurrence/window sweep workload)."""
+    n = close.size
+    hi = close * (1.0 + np.abs(sigma * normal(seed, 1, n)))
+    lo = close * (1.0 - np.abs(sigma * normal(seed, 2, n)))
+    return hi, lo
+
+
+def ohlcv(n: int, seed: int, nan_lead: int = 0, sigma: float = 0.01, hl_sigma: float = 0.004):
+    """open = previous close; high/low = max/min(open, close) * (1 +- |N(0, hl_sigma^2)|);
+    volume lognormal(10, 1)."""
+    close = random_walk(n, seed, sigma)
+    opn = np.empty_like(close)
+    opn[0] = close[0]
+    opn[1:] = close[:-1]
+    hi = np.maximum(opn, close) * (1.0 + np.abs(hl_sigma * normal(seed, 1, n)))
+    lo = np.minimum(opn, close) * (1.0 - np.abs(hl_sigma * normal(seed, 2, n)))
+    vol = np.exp(10.0 + normal(seed, 3, n))
+    for a in (opn, hi, lo, close, vol):
+        a[:nan_lead] = np.nan
+    return {"open": opn, "high": hi, "low": lo, "close": close, "volume": vol}
+
+
+def ragged_many_series(n_series: int, seed: int, min_len: int = 1000, max_len: int = 50000,
+                       max_nan_lead: int = 500):
+    """Many OHLCV series of uneven length and NaN lead, stacked time-major
+    [max_len][n_series] as float32 with a NaN tail past each series' end."""
+    u_len = uniform(seed, 10, n_series)
+    u_lead = uniform(seed, 11, n_series)
+    lens = (min_len + np.floor(u_len * (max_len - min_len + 1))).astype(np.int64)
+    leads = np.floor(u_lead * (max_nan_lead + 1)).astype(np.int64)
+    rows = int(lens.max())
+    out = {k: np.full((rows, n_series), np.nan, dtype=np.float32) for k in ("open", "high", "low", "close", "volume")}
+    for s in range(n_series):
+        d = ohlcv(int(lens[s]), seed * 100003 + s, nan_lead=int(leads[s]))
+        for k in out:
+            out[k][: lens[s], s] = d[k]
+    return out, lens, leads
