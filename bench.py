@@ -1,0 +1,410 @@
+"""Benchmark of the GB300 indicator hot path.
+
+Default workload (the recurrence and window sweeps): one close series of
+1,000,000 bars (geometric random walk, seed 1, first 200 NaN) and
+high/low = close * (1 +- |N(0, 0.005^2)|); one step computes
+  EMA, DEMA, TEMA, RSI           periods 2..1000 step 1 (999 combos each)
+  SMA, StdDev, Z-score           windows 5..500 step 5 (100 combos each)
+  Donchian (3 bands), Williams %R windows 5..500 step 5
+= 4.696e9 f32 outputs (18.8 GB written per step, which also flushes L2).
+`--workload alma_grid` runs the ALMA grid instead (200,000 bars, seed 2,
+periods 5..260 x offsets 0.50..0.95/0.05 x sigmas 3..9 = 17,920 combos).
+
+Metric: indicator outputs per second (higher is better).
+  value: inputs resident in HBM, outputs into preallocated device buffers,
+         through the crate-facing *_batch_device C-ABI calls; CUDA events on
+         the calls' stream around exactly K steps.
+  e2e:   the *_batch_into_host_f32 C-ABI calls from pinned host inputs to
+         pinned host outputs (H2D + kernels + D2H of every output).
+`--impl reference` times the CPU reference restatement (oracle, all host
+threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# measured peaks of this GPU pool (HBM copy GB/s); fallback 6800 if absent
+_FALLBACK_HBM = 6800.0
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return _FALLBACK_HBM, "fallback"
+
+
+# ------------------------------------------------------------- workloads ----
+def workload_sweeps():
+    from vectorta_gb300 import datagen
+
+    n = 1_000_000
+    close = datagen.random_walk(n, seed=1, nan_lead=200)
+    hi, lo = datagen.high_low(close, seed=1)
+    hi[:200] = np.nan
+    lo[:200] = np.nan
+    series = {"close": close.astype(np.float32), "high": hi.astype(np.float32), "low": lo.astype(np.float32)}
+    rec = {"period": (2, 1000, 1)}
+    win = {"period": (5, 500, 5)}
+    jobs = [
+        ("ema", ["close"], rec), ("dema", ["close"], rec), ("tema", ["close"], rec), ("rsi", ["close"], rec),
+        ("sma", ["close"], win), ("stddev", ["close"], {"period": (5, 500, 5), "nbdev": (1.0, 1.0, 0.0)}),
+        ("zscore", ["close"], {"period": (5, 500, 5), "nbdev": (1.0, 1.0, 0.0)}),
+        ("donchian", ["high", "low"], win), ("willr", ["high", "low", "close"], win),
+    ]
+    return {"name": "recurrence_window_sweeps", "n": n, "series": series, "jobs": jobs, "dominant": "ema",
+            "config": {"workload": "recurrence_window_sweeps", "bars": n, "nan_lead": 200, "seed": 1,
+                       "recurrences": "EMA/DEMA/TEMA/RSI periods 2..1000 (999 each)",
+                       "windows": "SMA/StdDev/Zscore/Donchian/WillR 5..500 step 5 (100 each)"}}
+
+
+def workload_alma_grid():
+    from vectorta_gb300 import datagen
+
+    n = 200_000
+    close = datagen.random_walk(n, seed=2)
+    sweep = {"period": (5, 260, 1), "offset": (0.50, 0.95, 0.05), "sigma": (3.0, 9.0, 1.0)}
+    return {"name": "alma_grid", "n": n, "series": {"close": close.astype(np.float32)},
+            "jobs": [("alma", ["close"], sweep)], "dominant": "alma",
+            "config": {"workload": "alma_grid", "bars": n, "seed": 2, "combos": 17920,
+                       "sweep": "periods 5..260 x offsets 0.50..0.95/0.05 x sigmas 3..9"}}
+
+
+WORKLOADS = {"sweeps": workload_sweeps, "alma_grid": workload_alma_grid}
+
+
+# ------------------------------------------------------------- clocks -------
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------- CPU side -----
+def cpu_sample(wl, budget_rows=None):
+    """Bounded sample of the workload for the CPU reference: every k-th combo
+    of each sweep over the full series.  Returns a list of (callable, outputs)."""
+    from oracle import oracle as O
+
+    s = {k: v.astype(np.float64) for k, v in wl["series"].items()}
+    tasks = []
+    for name, ins, sweep in wl["jobs"]:
+        if name == "alma":
+            ps = O.axis_usize(sweep["period"])[::16]
+            for p in ps:
+                tasks.append((lambda p=p: O.alma_batch(s["close"], (p, p, 0), sweep["offset"], sweep["sigma"]),
+                              wl["n"] * len(O.axis_f64(sweep["offset"])) * len(O.axis_f64(sweep["sigma"]))))
+            continue
+        ps = O.periods_of(name, sweep["period"])
+        stride = 25 if len(ps) > 500 else 5
+        for p in ps[::stride]:
+            if name in ("ema", "dema", "tema"):
+                fn = {"ema": O.ema, "dema": O.dema, "tema": O.tema}[name]
+                tasks.append((lambda fn=fn, p=p: fn(s["close"], p), wl["n"]))
+            elif name == "rsi":
+                tasks.append((lambda p=p: O.rsi_batch(s["close"], [p]), wl["n"]))
+            elif name == "sma":
+                tasks.append((lambda p=p: O.sma_batch(s["close"], [p]), wl["n"]))
+            elif name == "stddev":
+                tasks.append((lambda p=p: O.stddev(s["close"], p, 1.0), wl["n"]))
+            elif name == "zscore":
+                tasks.append((lambda p=p: O.zscore_batch_row(s["close"], p, 1.0), wl["n"]))
+            elif name == "donchian":
+                tasks.append((lambda p=p: O.donchian(s["high"], s["low"], p, fast=True), 3 * wl["n"]))
+            elif name == "willr":
+                tasks.append((lambda p=p: O.willr(s["high"], s["low"], s["close"], p, fast=True), wl["n"]))
+    return tasks
+
+
+def run_cpu(tasks, threads):
+    from concurrent.futures import ThreadPoolExecutor
+
+    t0 = time.perf_counter()
+    if threads <= 1:
+        for fn, _ in tasks:
+            fn()
+    else:
+        with ThreadPoolExecutor(threads) as ex:
+            list(ex.map(lambda t: t[0](), tasks))
+    dt = time.perf_counter() - t0
+    outs = sum(o for _, o in tasks)
+    return outs / dt, dt, outs
+
+
+# ------------------------------------------------------------- GPU side -----
+def gpu_bench(args, wl):
+    import torch
+
+    from vectorta_gb300 import cuda as V
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    ctx = V.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)  # events below and the calls share one stream
+    ctx.set_policy("timing", "on")
+    inds = {name: V.CLASSES[name](0, ctx=ctx) for name, _, _ in wl["jobs"]}
+    d_series = {k: torch.from_numpy(v).to(dev) for k, v in wl["series"].items()}
+    firsts = {}
+    for name, ins, _ in wl["jobs"]:
+        arr = np.stack([wl["series"][k] for k in ins])
+        firsts[name] = int(np.argmax(~np.isnan(arr).any(axis=0)))
+    n = wl["n"]
+    outs, rows = {}, {}
+    for name, ins, sweep in wl["jobs"]:
+        r = len(inds[name].expand_grid(sweep))  # the library's own grid expansion
+        rows[name] = r
+        nout = len(V.N.INDICATORS[name][1])
+        outs[name] = [torch.empty((r, n), dtype=torch.float32, device=dev) for _ in range(nout)]
+    out_per_step = sum(rows[nm] * n * len(outs[nm]) for nm in rows)
+
+    kernel_ms = {nm: [] for nm in rows}
+
+    def step(record=False):
+        for name, ins, sweep in wl["jobs"]:
+            inds[name].batch_device([d_series[k] for k in ins], n, firsts[name], sweep, outs[name])
+            if record:
+                kernel_ms[name].append(ctx.kernel_ms)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    launches0 = V.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step(record=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = V.launch_count() - launches0
+    ms = e0.elapsed_time(e1)
+    ms_per_step = ms / args.steps
+    value = out_per_step / (ms_per_step / 1e3)
+
+    # roofline of the dominant kernel: algorithmic bytes per launch / event-timed duration
+    dom = wl["dominant"]
+    dom_ms = float(np.mean([x for x in kernel_ms[dom] if x > 0]))
+    in_bytes = sum(wl["series"][k].nbytes for k in dict((j[0], j[1]) for j in wl["jobs"])[dom])
+    dom_bytes = rows[dom] * n * 4 * len(outs[dom]) + in_bytes
+    hbm, src = peaks()
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    share = {nm: float(np.mean(v)) for nm, v in kernel_ms.items()}
+
+    # e2e through the host-in / host-out C-ABI calls, pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_bench(args, wl, inds, rows, out_per_step)
+    return {
+        "value": value, "ms_per_step": ms_per_step, "gpu_launches": int(launches), "clocks": clk.summary(),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": TRAFFIC.get(wl["name"]),
+                     "kernel": KERNEL_NAME.get(wl["name"]), "peak_source": src,
+                     "bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
+        "kernel_ms_per_call": share, "outputs_per_step": out_per_step, "e2e": e2e,
+    }
+
+
+def e2e_bench(args, wl, inds, rows, out_per_step):
+    import ctypes as C
+
+    import torch
+
+    from vectorta_gb300 import _native as N
+
+    L = N.lib()
+    n = wl["n"]
+    # pinned host inputs
+    host_in = {}
+    for k, v in wl["series"].items():
+        p = C.c_void_p()
+        N.check(L.vta_pinned_alloc(v.nbytes, C.byref(p)))
+        a = np.ctypeslib.as_array((C.c_float * v.size).from_address(p.value))
+        a[:] = v
+        host_in[k] = (p, a)
+    biggest = max(rows[nm] * n for nm in rows)
+    nout_max = max(len(N.INDICATORS[nm][1]) for nm in rows)
+    host_out = []
+    for _ in range(nout_max):
+        p = C.c_void_p()
+        N.check(L.vta_pinned_alloc(biggest * 4, C.byref(p)))
+        host_out.append(p)
+    h2d = sum(sum(wl["series"][k].nbytes for k in ins) for _, ins, _ in wl["jobs"])
+    d2h = out_per_step * 4
+
+    def step():
+        for name, ins, sweep in wl["jobs"]:
+            ind = inds[name]
+            nout = len(N.INDICATORS[name][1])
+            import vectorta_gb300.cuda as V
+
+            s = V._to_sweep(ind._fam, sweep)
+            r, c = C.c_size_t(), C.c_size_t()
+            N.check(ind._fn("batch_into_host_f32")(
+                ind.ctx.handle, *[host_in[k][0].value for k in ins], n, C.byref(s),
+                *[host_out[i].value for i in range(nout)], rows[name] * n, C.byref(r), C.byref(c)))
+
+    steps = max(1, min(args.steps, 2))
+    step()  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / steps
+    for p, _ in host_in.values():
+        L.vta_pinned_free(p)
+    for p in host_out:
+        L.vta_pinned_free(p)
+    return {"value": out_per_step / dt, "unit": "outputs/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3, "steps": steps}
+
+
+# dram bytes per launch of the dominant kernel from the committed ncu capture
+# (profiles/*.md); None until captured
+TRAFFIC = {}
+KERNEL_NAME = {"recurrence_window_sweeps": "k_recur<OpEma, batch, EMIT>", "alma_grid": "wwma batch kernel"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="sweeps", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    wl = WORKLOADS[args.workload]()
+    cfg = dict(wl["config"], l2="each step writes >> 129 MB of outputs, flushing L2",
+               parallelism="replicas" if world > 1 else "single GPU")
+    base = {"metric": "indicator outputs/s at stated err vs FP64 oracle", "unit": "outputs/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded random walk)",
+            "config": cfg}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        threads = os.cpu_count() or 1
+        tasks = cpu_sample(wl)
+        run_cpu(tasks[: max(1, len(tasks) // 8)], threads)  # warm caches / page in
+        vals = []
+        for _ in range(max(1, args.warmup)):
+            run_cpu(tasks, threads)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            v, dt, outs = run_cpu(tasks, threads)
+            vals.append(v)
+        wall = (time.perf_counter() - t0) / args.steps
+        v = float(np.median(vals))
+        line = dict(base, impl="reference", value=v, ms_per_step=wall * 1e3,
+                    cpu_baseline={"value": v, "unit": "outputs/s", "cores": threads, "kind": "port",
+                                  "sample": f"{len(tasks)} rows of the workload's sweeps over the full series "
+                                            f"({outs:.3g} outputs per step), C oracle, {threads} threads"},
+                    e2e={"value": v, "unit": "outputs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    res = gpu_bench(args, wl)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([res["ms_per_step"]], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        res["ms_per_step"] = float(t.item())
+        res["value"] = res["outputs_per_step"] * world / (res["ms_per_step"] / 1e3)
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        tasks = cpu_sample(wl)
+        v, dt, outs = run_cpu(tasks, threads)
+        cpu = {"value": v, "unit": "outputs/s", "cores": threads, "kind": "port",
+               "sample": f"{len(tasks)} rows of the workload's sweeps over the full series ({outs:.3g} outputs, "
+                         f"{dt:.1f} s), C oracle, {threads} threads"}
+    line = dict(base, value=res["value"], ms_per_step=res["ms_per_step"], gpu_launches=res["gpu_launches"],
+                clocks=res["clocks"], roofline=res["roofline"], cpu_baseline=cpu, e2e=res["e2e"],
+                kernel_ms_per_call=res["kernel_ms_per_call"], outputs_per_step=res["outputs_per_step"])
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -28,7 +28,7 @@ AXIS_MODE = {
     "alma": AX_DESC, "ema": AX_SWAP, "dema": AX_DESC, "tema": AX_DESC,
     "rsi": AX_SWAP, "wilders": AX_DESC, "atr": AX_REV_FROM_END, "adx": AX_DESC,
     "supertrend": AX_DESC, "sma": AX_DESC, "stddev": AX_DESC, "zscore": AX_DESC,
-    "bollinger": AX_DESC, "donchian": AX_DESC, "willr": AX_DESC,
+    "bollinger": AX_DESC, "bollinger_bands": AX_DESC, "donchian": AX_DESC, "willr": AX_DESC,
     "percentile_nearest_rank": AX_DESC, "wma": AX_DESC_PLUS_END, "swma": AX_DESC,
     "pwma": AX_DESC, "sinwma": AX_DESC, "trima": AX_SWAP,
 }
@@ -88,6 +88,8 @@ def lib():
             "vto_sinwma": ([dp, sz, sz, dp], ip),
             "vto_sinwma_weights": ([sz, dp], None),
             "vto_trima": ([dp, sz, sz, dp], ip),
+            "vto_donchian_fast": ([dp, dp, sz, sz, dp, dp, dp], ip),
+            "vto_willr_fast": ([dp, dp, dp, sz, sz, dp], ip),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -237,17 +239,19 @@ def supertrend(h, l, c, period=10, factor=3.0):
     return tr, ch
 
 
-def willr(h, l, c, period=14):
+def willr(h, l, c, period=14, fast=False):
     h, l, c = _hlc(h, l, c)
     out = np.empty_like(c)
-    _check(lib().vto_willr(_p(h), _p(l), _p(c), c.size, period, _p(out)), "willr")
+    fn = lib().vto_willr_fast if fast else lib().vto_willr
+    _check(fn(_p(h), _p(l), _p(c), c.size, period, _p(out)), "willr")
     return out
 
 
-def donchian(h, l, period=20):
+def donchian(h, l, period=20, fast=False):
     h, l = _f64(h), _f64(l)
     u, m, lo = np.empty_like(h), np.empty_like(h), np.empty_like(h)
-    _check(lib().vto_donchian(_p(h), _p(l), h.size, period, _p(u), _p(m), _p(lo)), "donchian")
+    fn = lib().vto_donchian_fast if fast else lib().vto_donchian
+    _check(fn(_p(h), _p(l), h.size, period, _p(u), _p(m), _p(lo)), "donchian")
     return u, m, lo
 
 

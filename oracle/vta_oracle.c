@@ -1218,3 +1218,105 @@ int vto_trima(const double *x, size_t n, size_t period, double *out) {
     free(ring);
     return VTO_OK;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Fast min/max windows with the crate's own algorithms (used to time the    */
+/* CPU baseline).  Max/min are exact selections, so these return the same    */
+/* bits as vto_donchian / vto_willr.                                         */
+/* ------------------------------------------------------------------------ */
+
+/* donchian_scalar p > 32 (donchian.rs:413-517): block-prefix maxima g_max /
+ * minima g_min over blocks of p, reverse running block-suffix extrema, and a
+ * valid-count prefix; p <= 32 falls back to the direct scan. */
+int vto_donchian_fast(const double *h, const double *l, size_t n, size_t period,
+                      double *up, double *mid, double *lo) {
+    if (period <= 32) return vto_donchian(h, l, n, period, up, mid, lo);
+    if (n == 0) return VTO_E_EMPTY;
+    size_t fh = first_valid(h, n), fl = first_valid(l, n);
+    if (fh >= n || fl >= n) return VTO_E_ALL_NAN;
+    size_t first = fh > fl ? fh : fl;
+    if (period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    size_t warm = first + period - 1;
+    fill_nan(up, warm); fill_nan(mid, warm); fill_nan(lo, warm);
+    double *gmax = (double *)malloc(sizeof(double) * n);
+    double *gmin = (double *)malloc(sizeof(double) * n);
+    unsigned *ps = (unsigned *)malloc(sizeof(unsigned) * (n + 1));
+    double amax = -INFINITY, amin = INFINITY;
+    size_t k = 0;
+    ps[0] = 0;
+    for (size_t i = 0; i < n; i++) {
+        int ok = isfinite(h[i]) && isfinite(l[i]);
+        double hv = ok ? h[i] : -INFINITY, lv = ok ? l[i] : INFINITY;
+        if (k == 0) { amax = hv; amin = lv; }
+        else { if (hv > amax) amax = hv; if (lv < amin) amin = lv; }
+        gmax[i] = amax; gmin[i] = amin;
+        if (++k == period) k = 0;
+        ps[i + 1] = ps[i] + (unsigned)ok;
+    }
+    amax = -INFINITY; amin = INFINITY;
+    for (size_t j = n; j-- > 0;) {
+        int ok = isfinite(h[j]) && isfinite(l[j]);
+        double hv = ok ? h[j] : -INFINITY, lv = ok ? l[j] : INFINITY;
+        if (j == n - 1 || ((j + 1) % period) == 0) { amax = hv; amin = lv; }
+        else { if (hv > amax) amax = hv; if (lv < amin) amin = lv; }
+        size_t i = j + period - 1;
+        if (i >= n || i < warm) continue;
+        if (ps[i + 1] - ps[i + 1 - period] == (unsigned)period) {
+            double mx = amax > gmax[i] ? amax : gmax[i];
+            double mn = amin < gmin[i] ? amin : gmin[i];
+            up[i] = mx; lo[i] = mn; mid[i] = fma(mx - mn, 0.5, mn);
+        } else {
+            up[i] = mid[i] = lo[i] = QNAN;
+        }
+    }
+    free(gmax); free(gmin); free(ps);
+    return VTO_OK;
+}
+
+/* willr_scalar p > 32 (willr.rs:447-622): monotonic deques of indices for the
+ * window max of high and min of low plus a NaN counter; p <= 32 falls back to
+ * the direct scan. */
+int vto_willr_fast(const double *h, const double *l, const double *c, size_t n, size_t period,
+                   double *out) {
+    if (period <= 32) return vto_willr(h, l, c, n, period, out);
+    if (n == 0) return VTO_E_EMPTY;
+    if (period > n) return VTO_E_INVALID_PERIOD;
+    size_t first = first_valid_hlc(h, l, c, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    size_t warm = first + period - 1;
+    fill_nan(out, warm);
+    size_t *dqx = (size_t *)malloc(sizeof(size_t) * (period + 1));
+    size_t *dqn = (size_t *)malloc(sizeof(size_t) * (period + 1));
+    size_t hx = 0, tx = 0, hn = 0, tn = 0; /* deque = [head, tail) in a ring of period+1 */
+    size_t cap = period + 1, nan_cnt = 0;
+    for (size_t i = warm + 1 - period; i < n; i++) {
+        /* push i */
+        if (isnan(h[i]) || isnan(l[i])) nan_cnt++;
+        else {
+            while (hx != tx && h[dqx[(tx + cap - 1) % cap]] <= h[i]) tx = (tx + cap - 1) % cap;
+            dqx[tx] = i; tx = (tx + 1) % cap;
+            while (hn != tn && l[dqn[(tn + cap - 1) % cap]] >= l[i]) tn = (tn + cap - 1) % cap;
+            dqn[tn] = i; tn = (tn + 1) % cap;
+        }
+        if (i < warm) continue;
+        size_t lo_i = i + 1 - period;
+        while (hx != tx && dqx[hx] < lo_i) hx = (hx + 1) % cap;
+        while (hn != tn && dqn[hn] < lo_i) hn = (hn + 1) % cap;
+        double cv = c[i];
+        if (isnan(cv) || nan_cnt > 0 || hx == tx || hn == tn) out[i] = QNAN;
+        else {
+            double hh = h[dqx[hx]], ll = l[dqn[hn]];
+            if (!(isfinite(hh) && isfinite(ll))) out[i] = QNAN;
+            else {
+                double den = hh - ll;
+                out[i] = den == 0.0 ? 0.0 : fma(-100.0, (hh - cv) / den, 0.0);
+            }
+        }
+        /* pop the element leaving next step */
+        if (isnan(h[lo_i]) || isnan(l[lo_i])) nan_cnt--;
+    }
+    free(dqx); free(dqn);
+    return VTO_OK;
+}

@@ -147,3 +147,20 @@ def test_oracle_error_cases():
         O.alma(np.arange(10.0), 3, 1.5, 6.0)
     with pytest.raises(O.OracleError):
         O.ema(np.array([]), 3)
+
+
+def test_oracle_fast_minmax_equals_direct_scan():
+    """The crate's block-extrema / deque paths select the same values as a
+    direct window scan (bit-identical), including NaN windows."""
+    from vectorta_gb300 import datagen
+
+    c = datagen.random_walk(3000, seed=5, nan_lead=7)
+    h, l = datagen.high_low(c, seed=6)
+    h[1500] = np.nan
+    l[2200] = np.nan
+    for p in (33, 50, 97, 256):
+        a = O.donchian(h, l, p)
+        b = O.donchian(h, l, p, fast=True)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y, equal_nan=True), p
+        assert np.array_equal(O.willr(h, l, c, p), O.willr(h, l, c, p, fast=True), equal_nan=True), p

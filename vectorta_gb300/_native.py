@@ -100,7 +100,7 @@ _lib = None
 def header_symbols() -> list[str]:
     """Every function the public header declares."""
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:const char\*|vta_status|int|void\*|size_t)\s+(vta_\w+)\s*\(",
+    return sorted(set(re.findall(r"^\s*(?:const char\*|vta_status|int|void\*|size_t|float|uint64_t)\s+(vta_\w+)\s*\(",
                                  text, re.M)))
 
 
@@ -127,6 +127,9 @@ def lib() -> C.CDLL:
     L.vta_ctx_last_kernel.restype = C.c_char_p
     L.vta_ctx_scratch_bytes.argtypes = [vp]
     L.vta_ctx_scratch_bytes.restype = sz
+    L.vta_ctx_kernel_ms.argtypes = [vp]
+    L.vta_ctx_kernel_ms.restype = C.c_float
+    L.vta_launch_count.restype = C.c_uint64
     L.vta_device_array_free.argtypes = [C.POINTER(DeviceArrayC)]
     L.vta_device_array_copy_to_host.argtypes = [vp, C.POINTER(DeviceArrayC), fp, sz]
     L.vta_pinned_alloc.argtypes = [sz, C.POINTER(vp)]

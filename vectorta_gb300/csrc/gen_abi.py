@@ -117,13 +117,20 @@ vta_status vta_ctx_set_stream(vta_ctx* ctx, void* cuda_stream);
 void* vta_ctx_get_stream(vta_ctx* ctx);
 /* CudaXPolicy / set_policy (alma_wrapper.rs:18-70): keys
  *   "wma_batch"   = "auto" | "plain" | "tc_fp16x3" | "tc_bf16x3"
- *   "recur_chunk" = "auto" | "sequential" | <positive multiple of 32>     */
+ *   "recur_chunk" = "auto" | "sequential" | <positive multiple of 32>
+ *   "timing"      = "on" | "off"                                         */
 vta_status vta_ctx_set_policy(vta_ctx* ctx, const char* key, const char* value);
 /* selected_batch_kernel() (alma_wrapper.rs:239-245): name of the last kernel
  * path used by this context. */
 const char* vta_ctx_last_kernel(vta_ctx* ctx);
 /* Device workspace currently held by the context (bytes). */
 size_t vta_ctx_scratch_bytes(vta_ctx* ctx);
+/* With policy "timing" = "on", each call records CUDA events on the context
+ * stream around its main output kernel; this returns that kernel's duration
+ * in ms for the last call (-1 when not recorded). */
+float vta_ctx_kernel_ms(vta_ctx* ctx);
+/* Number of kernels this library has launched in the process. */
+uint64_t vta_launch_count(void);
 
 /* ---- device arrays: DeviceArrayF32 (alma_wrapper.rs:103-117) ----------- */
 typedef struct vta_device_array {

@@ -215,15 +215,19 @@ __global__ void __launch_bounds__(kWarps * 32) k_supertrend(HlcArgs a) {
 
 vta_status launch_adx(const HlcArgs& a, cudaStream_t st) {
     const unsigned blocks = ceil_div(ceil_div(a.n_lanes, 32), kWarps);
+    ktimer_begin(st);
     if (a.layout) k_adx<true><<<blocks, kWarps * 32, 0, st>>>(a);
     else k_adx<false><<<blocks, kWarps * 32, 0, st>>>(a);
+    ktimer_end(st);
     return check_launch("k_adx");
 }
 
 vta_status launch_supertrend(const HlcArgs& a, cudaStream_t st) {
     const unsigned blocks = ceil_div(ceil_div(a.n_lanes, 32), kWarps);
+    ktimer_begin(st);
     if (a.layout) k_supertrend<true><<<blocks, kWarps * 32, 0, st>>>(a);
     else k_supertrend<false><<<blocks, kWarps * 32, 0, st>>>(a);
+    ktimer_end(st);
     return check_launch("k_supertrend");
 }
 

@@ -65,24 +65,31 @@ __device__ __forceinline__ double warp_incl_scan(double v) {
     return v;
 }
 
-// Block-wide inclusive scan of one double per thread; returns the inclusive
-// value and leaves the block total in *total.
-__device__ double block_incl_scan(double v, double* total) {
-    __shared__ double wsum[kScanThreads / 32];
+// Block-wide exclusive scan of one double per thread (true exclusive: a NaN
+// in thread i reaches threads > i only); leaves the block total in *total.
+__device__ double block_excl_scan(double v, double* total) {
+    constexpr int kW = kScanThreads / 32;
+    __shared__ double wsum[kW];
+    __shared__ double wtot;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    v = warp_incl_scan(v);
-    if (lane == 31) wsum[warp] = v;
+    const double inc = warp_incl_scan(v);
+    double exc = __shfl_up_sync(0xffffffffu, inc, 1);
+    if (lane == 0) exc = 0.0;
+    if (lane == 31) wsum[warp] = inc;
     __syncthreads();
     if (warp == 0) {
-        double w = lane < kScanThreads / 32 ? wsum[lane] : 0.0;
-        w = warp_incl_scan(w);
-        if (lane < kScanThreads / 32) wsum[lane] = w;
+        const double w = lane < kW ? wsum[lane] : 0.0;
+        const double wi = warp_incl_scan(w);
+        double we = __shfl_up_sync(0xffffffffu, wi, 1);
+        if (lane == 0) we = 0.0;
+        if (lane < kW) wsum[lane] = we;  // exclusive warp offsets
+        if (lane == kW - 1) wtot = wi;
     }
     __syncthreads();
-    const double off = warp > 0 ? wsum[warp - 1] : 0.0;
-    *total = wsum[kScanThreads / 32 - 1];
+    const double res = wsum[warp] + exc;
+    *total = wtot;
     __syncthreads();
-    return v + off;
+    return res;
 }
 
 __global__ void k_prefix_reduce(const float* __restrict__ x, int n, int first, int kind,
@@ -95,7 +102,7 @@ __global__ void k_prefix_reduce(const float* __restrict__ x, int n, int first, i
         if (i < n) s += prefix_value(x, i, first, kind);
     }
     double total;
-    block_incl_scan(s, &total);
+    block_excl_scan(s, &total);
     if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
 }
 
@@ -106,8 +113,8 @@ __global__ void k_prefix_scan_blocks(double* block_sums, int nb) {
         const int i = base + threadIdx.x;
         const double v = i < nb ? block_sums[i] : 0.0;
         double total;
-        const double inc = block_incl_scan(v, &total);
-        if (i < nb) block_sums[i] = carry + inc - v;
+        const double exc = block_excl_scan(v, &total);
+        if (i < nb) block_sums[i] = carry + exc;
         carry += total;
     }
 }
@@ -125,8 +132,7 @@ __global__ void k_prefix_apply(const float* __restrict__ x, int n, int first, in
         s += v[k];
     }
     double total;
-    const double inc = block_incl_scan(s, &total);
-    double run = block_offsets[blockIdx.x] + inc - s;
+    double run = block_offsets[blockIdx.x] + block_excl_scan(s, &total);
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
         const int i = base + k;

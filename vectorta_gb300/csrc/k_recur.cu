@@ -466,7 +466,9 @@ vta_status run(const RecurArgs& a, cudaStream_t st) {
         k_recur_carry<Op><<<ceil_div(a.n_lanes, 128), 128, 0, st>>>(a, n_chunks);
         VTA_TRY(check_launch("k_recur_carry"));
     }
+    ktimer_begin(st);
     k_recur<Op, TM, PASS_EMIT><<<grid, kWarps * 32, 0, st>>>(a);
+    ktimer_end(st);
     return check_launch("k_recur_emit");
 }
 

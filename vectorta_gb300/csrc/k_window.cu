@@ -455,7 +455,9 @@ __global__ void k_percentile(PnrArgs a) {
 vta_status launch_prefix_window_batch(const PrefixWinArgs& a, cudaStream_t st) {
     dim3 grid(ceil_div(a.n, kPwThreads), ceil_div(a.n_combos, kPwCombos));
     if (grid.y > 65535) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "prefix window: too many combos");
+    ktimer_begin(st);
     k_prefix_window_batch<<<grid, kPwThreads, 0, st>>>(a);
+    ktimer_end(st);
     return check_launch("k_prefix_window_batch");
 }
 
@@ -465,7 +467,9 @@ vta_status launch_prefix_window_tm(const PrefixWinTmArgs& a, cudaStream_t st) {
     k_first_nan_after_tm<<<ceil_div(a.cols, 128), 128, 0, st>>>(a.x_tm, a.cols, a.rows, a.first, first_nan);
     VTA_TRY(check_launch("k_first_nan_after_tm"));
     dim3 grid(ceil_div(a.cols, 128), ceil_div(a.rows, kTmChunk));
+    ktimer_begin(st);
     k_prefix_window_tm<<<grid, 128, 0, st>>>(a, first_nan);
+    ktimer_end(st);
     return check_launch("k_prefix_window_tm");
 }
 
@@ -477,24 +481,32 @@ vta_status launch_minmax_batch(const MinMaxArgs& a, size_t smem_optin, cudaStrea
         if (bytes <= smem_optin && (tile <= 512 || (size_t)a.n >= (size_t)tile * 8 * kNumSMs)) {
             VTA_CUDA_TRY(cudaFuncSetAttribute(k_minmax_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)bytes));
+            ktimer_begin(st);
             k_minmax_batch<<<ceil_div(a.n, tile), kMmThreads, bytes, st>>>(a, tile, levels);
+            ktimer_end(st);
             return check_launch("k_minmax_batch");
         }
     }
     dim3 grid(ceil_div(a.n, 256), a.n_combos);
+    ktimer_begin(st);
     k_minmax_batch_naive<<<grid, 256, 0, st>>>(a);
+    ktimer_end(st);
     return check_launch("k_minmax_batch_naive");
 }
 
 vta_status launch_minmax_tm(const MinMaxTmArgs& a, cudaStream_t st) {
     dim3 grid(ceil_div(a.cols, 128), ceil_div(a.rows, kMmTmChunk));
+    ktimer_begin(st);
     k_minmax_tm<<<grid, 128, 0, st>>>(a);
+    ktimer_end(st);
     return check_launch("k_minmax_tm");
 }
 
 vta_status launch_percentile(const PnrArgs& a, cudaStream_t st) {
     dim3 grid(ceil_div(a.n_lanes, 64), ceil_div(a.n, kPnrChunk));
+    ktimer_begin(st);
     k_percentile<<<grid, 64, 0, st>>>(a);
+    ktimer_end(st);
     return check_launch("k_percentile");
 }
 

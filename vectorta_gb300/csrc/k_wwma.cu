@@ -176,7 +176,9 @@ vta_status launch_wwma_batch_plain(const WwmaBatchArgs& a, cudaStream_t st) {
                                       (int)smem));
     dim3 grid(ceil_div(a.n, kBT), ceil_div(a.n_combos, kBC));
     if (grid.y > 65535) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "wwma: too many combos");
+    ktimer_begin(st);
     k_wwma_batch_plain<<<grid, kThreads, smem, st>>>(a);
+    ktimer_end(st);
     return check_launch("k_wwma_batch_plain");
 }
 
@@ -194,7 +196,9 @@ vta_status launch_wwma_tm(const WwmaTmArgs& a, cudaStream_t st) {
     if (smem > 227 * 1024) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "wwma tm: period too large");
     if (smem > 48 * 1024)
         VTA_CUDA_TRY(cudaFuncSetAttribute(k_wwma_tm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ktimer_begin(st);
     k_wwma_tm<<<grid, 128, smem, st>>>(a, fn);
+    ktimer_end(st);
     return check_launch("k_wwma_tm");
 }
 

@@ -8,6 +8,7 @@
 // / *_many_series_*_dev forms add the crate's host-side validation, the
 // host->device copies and the output allocation around them.
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <memory>
@@ -28,7 +29,24 @@ vta_status cuda_fail(cudaError_t e, const char* what) {
     g_err = std::string("cuda error: ") + cudaGetErrorString(e) + " (" + what + ")";
     return VTA_ERR_CUDA;
 }
+static std::atomic<uint64_t> g_launches{0};
+static thread_local vta_ctx* g_cur = nullptr;  // context of the call in progress
+
+void ktimer_begin(cudaStream_t st) {
+    if (g_cur && g_cur->timing && g_cur->ev0) {
+        cudaEventRecord(g_cur->ev0, st);
+        g_cur->timed = false;
+    }
+}
+void ktimer_end(cudaStream_t st) {
+    if (g_cur && g_cur->timing && g_cur->ev1) {
+        cudaEventRecord(g_cur->ev1, st);
+        g_cur->timed = true;
+    }
+}
+
 vta_status check_launch(const char* kernel) {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, kernel);
     return VTA_OK;
@@ -635,6 +653,8 @@ static vta_status run_tm(vta_ctx* ctx, Ind ind, const DevIn& in, size_t cols, si
 static vta_status check_ctx(vta_ctx* ctx) {
     if (!ctx) return fail(VTA_ERR_INVALID_INPUT, "null context");
     VTA_CUDA_TRY(cudaSetDevice(ctx->device));
+    g_cur = ctx;
+    ctx->timed = false;
     return VTA_OK;
 }
 
@@ -905,6 +925,9 @@ vta_status vta_ctx_destroy(vta_ctx* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (g_cur == ctx) g_cur = nullptr;
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return VTA_OK;
@@ -944,6 +967,21 @@ vta_status vta_ctx_set_policy(vta_ctx* ctx, const char* key, const char* value) 
         else return fail(VTA_ERR_INVALID_POLICY, "wma_batch: auto|plain|tc_fp16x3|tc_bf16x3");
         return VTA_OK;
     }
+    if (k == "timing") {
+        if (v == "on") {
+            if (!ctx->ev0) {
+                VTA_CUDA_TRY(cudaSetDevice(ctx->device));
+                VTA_CUDA_TRY(cudaEventCreate(&ctx->ev0));
+                VTA_CUDA_TRY(cudaEventCreate(&ctx->ev1));
+            }
+            ctx->timing = true;
+        } else if (v == "off") {
+            ctx->timing = false;
+        } else {
+            return fail(VTA_ERR_INVALID_POLICY, "timing: on|off");
+        }
+        return VTA_OK;
+    }
     if (k == "recur_chunk") {
         if (v == "auto") ctx->policy.recur_chunk = 0;
         else if (v == "sequential") ctx->policy.recur_chunk = 1;
@@ -959,6 +997,18 @@ vta_status vta_ctx_set_policy(vta_ctx* ctx, const char* key, const char* value) 
 }
 
 const char* vta_ctx_last_kernel(vta_ctx* ctx) { return ctx ? ctx->last_kernel.c_str() : ""; }
+
+float vta_ctx_kernel_ms(vta_ctx* ctx) {
+    if (!ctx || !ctx->timing || !ctx->timed) return -1.f;
+    float ms = -1.f;
+    if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) != cudaSuccess) {
+        cudaGetLastError();
+        return -1.f;
+    }
+    return ms;
+}
+
+uint64_t vta_launch_count(void) { return g_launches.load(); }
 size_t vta_ctx_scratch_bytes(vta_ctx* ctx) { return ctx ? ctx->scratch_bytes : 0; }
 
 vta_status vta_device_array_free(vta_device_array* a) {

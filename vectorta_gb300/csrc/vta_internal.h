@@ -33,8 +33,13 @@ vta_status cuda_fail(cudaError_t e, const char* what);
         if (_s != VTA_OK) return _s;         \
     } while (0)
 
-// Checks the launch that was just enqueued.
+// Checks the launch that was just enqueued (and counts it).
 vta_status check_launch(const char* kernel);
+
+// Event timer around a call's main output kernel, on the launching stream;
+// active only when the current context has policy "timing" = "on".
+void ktimer_begin(cudaStream_t st);
+void ktimer_end(cudaStream_t st);
 
 // ---------------------------------------------------------------- launch ---
 constexpr int kNumSMs = 152;     // GB300: 2 dies x 76 SMs (re-read at ctx create)
@@ -62,6 +67,9 @@ struct vta_ctx {
     size_t scratch_bytes = 0;
     vta::Policy policy;
     std::string last_kernel;
+    bool timing = false;
+    bool timed = false;  // the last call recorded both events
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
 namespace vta {

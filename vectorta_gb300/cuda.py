@@ -199,6 +199,11 @@ class Context:
     def scratch_bytes(self) -> int:
         return int(N.lib().vta_ctx_scratch_bytes(self.handle))
 
+    @property
+    def kernel_ms(self) -> float:
+        """Duration of the last call's main kernel (policy timing=on), else -1."""
+        return float(N.lib().vta_ctx_kernel_ms(self.handle))
+
     def close(self):
         if getattr(self, "handle", None) is not None and self.handle.value:
             N.lib().vta_ctx_destroy(self.handle)
@@ -265,8 +270,8 @@ class DeviceArrayF32:
 class _CudaIndicator:
     NAME = ""
 
-    def __init__(self, device_id: int = 0):
-        self.ctx = Context(device_id)
+    def __init__(self, device_id: int = 0, ctx: "Context | None" = None):
+        self.ctx = ctx if ctx is not None else Context(device_id)
         kind, outs, fam = N.INDICATORS[self.NAME]
         self._kind, self._outs, self._fam = kind, outs, fam
         self._nin = N.N_IN[kind]
@@ -374,7 +379,12 @@ CLASSES = {name: _make(name, cls) for name, cls in _CLASS_NAMES.items()}
 __all__ += ["AlmaBatchRange", "PeriodBatchRange", "StdDevBatchRange", "ZscoreBatchRange",
             "BollingerBandsBatchRange", "SuperTrendBatchRange", "PercentileNearestRankBatchRange",
             "AlmaParams", "PeriodParams", "StdDevParams", "ZscoreParams", "BollingerBandsParams",
-            "SuperTrendParams", "PercentileNearestRankParams", "CLASSES", "device_count"]
+            "SuperTrendParams", "PercentileNearestRankParams", "CLASSES", "device_count", "launch_count"]
+
+
+def launch_count() -> int:
+    """Kernels launched by the library so far in this process."""
+    return int(N.lib().vta_launch_count())
 
 
 def device_count() -> int:
