@@ -83,7 +83,19 @@ def workload_alma_grid():
                        "sweep": "periods 5..260 x offsets 0.50..0.95/0.05 x sigmas 3..9"}}
 
 
-WORKLOADS = {"sweeps": workload_sweeps, "alma_grid": workload_alma_grid}
+def workload_ema_small():
+    """Profiling case: one EMA sweep (periods 2..1000) on 200,000 bars
+    (0.8 GB of outputs: larger than L2, a few GB on the device at most)."""
+    from vectorta_gb300 import datagen
+
+    n = 200_000
+    close = datagen.random_walk(n, seed=1, nan_lead=200)
+    return {"name": "ema_small", "n": n, "series": {"close": close.astype(np.float32)},
+            "jobs": [("ema", ["close"], {"period": (2, 1000, 1)})], "dominant": "ema",
+            "config": {"workload": "ema_small", "bars": n, "seed": 1, "combos": 999}}
+
+
+WORKLOADS = {"sweeps": workload_sweeps, "alma_grid": workload_alma_grid, "ema_small": workload_ema_small}
 
 
 # ------------------------------------------------------------- clocks -------
@@ -159,7 +171,7 @@ def cpu_sample(wl, budget_rows=None):
                               wl["n"] * len(O.axis_f64(sweep["offset"])) * len(O.axis_f64(sweep["sigma"]))))
             continue
         ps = O.periods_of(name, sweep["period"])
-        stride = 25 if len(ps) > 500 else 5
+        stride = 8 if len(ps) > 500 else 2
         for p in ps[::stride]:
             if name in ("ema", "dema", "tema"):
                 fn = {"ema": O.ema, "dema": O.dema, "tema": O.tema}[name]
@@ -327,7 +339,8 @@ def e2e_bench(args, wl, inds, rows, out_per_step):
 # dram bytes per launch of the dominant kernel from the committed ncu capture
 # (profiles/*.md); None until captured
 TRAFFIC = {}
-KERNEL_NAME = {"recurrence_window_sweeps": "k_recur<OpEma, batch, EMIT>", "alma_grid": "wwma batch kernel"}
+KERNEL_NAME = {"recurrence_window_sweeps": "k_recur<OpEma, batch, EMIT>", "alma_grid": "wwma batch kernel",
+               "ema_small": "k_recur<OpEma, batch, EMIT>"}
 
 
 def main():

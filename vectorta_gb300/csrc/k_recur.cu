@@ -15,6 +15,8 @@
 // series of a time-major matrix (coalesced loads and stores directly).
 // The warm-up rules (seed index, NaN prefix, running-mean outputs) follow the
 // crate's scalar paths cited on each op.
+#include <climits>
+
 #include "vta_internal.h"
 
 namespace vta {
@@ -83,6 +85,14 @@ struct OpEma {
     __device__ void zero() { y = 0.f; }
     __device__ float get(int) const { return y; }
     __device__ void set(int, float v) { y = v; }
+    // running step + output without phase checks; returns applied-step flag
+    template <class In> __device__ float fast(const In& in, int t, int& applied) {
+        const float v = in.X(t);
+        const bool ok = isfinite(v);
+        y = ok ? fmaf(beta, y, alpha * v) : y;
+        applied += ok;
+        return y;
+    }
     static __device__ void propagate(double* S, double n, int p) {
         double b = 1.0 - 2.0 / ((double)p + 1.0);
         S[0] *= pow(b, n);
@@ -116,6 +126,13 @@ struct OpDema {
     __device__ void zero() { e1 = 0.f; e2 = 0.f; }
     __device__ float get(int i) const { return i == 0 ? e1 : e2; }
     __device__ void set(int i, float v) { if (i == 0) e1 = v; else e2 = v; }
+    template <class In> __device__ float fast(const In& in, int t, int& applied) {
+        const float v = in.X(t);
+        e1 = fmaf(e1, a, v * alpha);
+        e2 = fmaf(e2, a, e1 * alpha);
+        ++applied;
+        return fmaf(e1, 2.f, -e2);
+    }
     static __device__ void propagate(double* S, double n, int p) {
         double al = 2.0 / ((double)p + 1.0);
         double an = pow(1.0 - al, n);
@@ -164,6 +181,15 @@ struct OpTema {
     }
     __device__ float warm_value(int) const { return qnan(); }
     __device__ void zero() { e1 = e2 = e3 = 0.f; }
+    template <class In> __device__ float fast(const In& in, int t, int& applied) {
+        const float v = in.X(t);
+        ++applied;
+        if (p1 == 0) { e1 = v; return v; }
+        e1 = e1 * per1 + v * per;
+        e2 = e2 * per1 + e1 * per;
+        e3 = e3 * per1 + e2 * per;
+        return 3.f * e1 - 3.f * e2 + e3;
+    }
     __device__ float get(int i) const { return i == 0 ? e1 : (i == 1 ? e2 : e3); }
     __device__ void set(int i, float v) { if (i == 0) e1 = v; else if (i == 1) e2 = v; else e3 = v; }
     static __device__ void propagate(double* S, double n, int p) {
@@ -224,10 +250,21 @@ struct OpRsi {
     }
     template <class In> __device__ float value(const In&, int) const {
         float den = ag + al;
-        return den == 0.f ? 50.f : 100.f * ag / den;
+        return den == 0.f ? 50.f : __fdividef(100.f * ag, den);
     }
     __device__ float warm_value(int) const { return qnan(); }
     __device__ void zero() { ag = 0.f; al = 0.f; }
+    template <class In> __device__ float fast(const In& in, int t, int& applied) {
+        const float v = in.X(t);
+        const float d = v - in.X(t - 1);
+        float g = d > 0.f ? d : 0.f, lo = d < 0.f ? -d : 0.f;
+        if (kBatchSem && !isfinite(d)) { g = qnan(); lo = qnan(); }
+        ag = fmaf(ag, beta, inv_p * g);
+        al = fmaf(al, beta, inv_p * lo);
+        ++applied;
+        const float den = ag + al;
+        return den == 0.f ? 50.f : __fdividef(100.f * ag, den);
+    }
     __device__ float get(int i) const { return i == 0 ? ag : al; }
     __device__ void set(int i, float v) { if (i == 0) ag = v; else al = v; }
     static __device__ void propagate(double* S, double n, int p) {
@@ -262,6 +299,12 @@ struct OpWilders {
     __device__ void zero() { y = 0.f; }
     __device__ float get(int) const { return y; }
     __device__ void set(int, float v) { y = v; }
+    template <class In> __device__ float fast(const In& in, int t, int& applied) {
+        const float v = in.X(t);
+        y = (p == 1) ? v : fmaf(v - y, alpha, y);
+        ++applied;
+        return y;
+    }
     static __device__ void propagate(double* S, double n, int p) {
         S[0] = (p == 1) ? 0.0 : S[0] * pow(1.0 - 1.0 / (double)p, n);
     }
@@ -306,6 +349,12 @@ struct OpAtr {
     __device__ void zero() { y = 0.f; }
     __device__ float get(int) const { return y; }
     __device__ void set(int, float v) { y = v; }
+    template <class In> __device__ float fast(const In& in, int t, int& applied) {
+        const float tr = true_range(in.H(t), in.L(t), in.C(t - 1));
+        y = fmaf(-alpha, y, y) + alpha * tr;
+        ++applied;
+        return y;
+    }
     static __device__ void propagate(double* S, double n, int p) {
         S[0] *= pow(1.0 - 1.0 / (double)p, n);
     }
@@ -315,6 +364,16 @@ struct OpAtr {
 enum { PASS_AGG = 0, PASS_EMIT = 1 };
 constexpr float kBeforeSeed = -2.f, kAbsolute = -1.f;
 
+__device__ __forceinline__ int warp_max(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// One warp = 32 lanes x one time chunk.  Tiles of 32 steps where every lane
+// of the warp is past its seed and warm-up take the fast path (no phase
+// checks: 2-6 FP ops per step); the few tiles around warm-up take the general
+// per-step state machine.
 template <class Op, bool TM, int PASS>
 __global__ void __launch_bounds__(kWarps * 32)
 k_recur(RecurArgs a) {
@@ -324,7 +383,6 @@ k_recur(RecurArgs a) {
     const int li = group * 32 + lane;
     const bool valid = li < a.n_lanes;
     const int chunk = blockIdx.y;
-    const int n_chunks = gridDim.y;
     const int c0 = chunk * a.chunk;
     const int c1 = min(c0 + a.chunk, a.n);
     if (c0 >= a.n) return;
@@ -361,50 +419,61 @@ k_recur(RecurArgs a) {
             running = true;
         } else if (c0 > op.f) {
             // the chunk starts inside the warm-up: accumulate [f, c0) first
-            int end = min(c0, op.s + 1);
+            const int end = min(c0, op.s + 1);
             for (int t = op.f; t < end; ++t) op.accum(in, t);
         }
     }
+    // first time index from which this lane needs no phase checks; lanes that
+    // never write (invalid / all-NaN) do not hold the warp back
+    const int run_from = (active && seeded_ever) ? max(op.s + 1, op.warm) : (valid ? INT_MAX : INT_MIN);
+    const int warp_run_from = warp_max(run_from);
 
     int steps = 0;
-    const bool need_loop = (PASS == PASS_EMIT) || (active && c1 > op.f && seeded_ever);
-    if (PASS == PASS_AGG && !need_loop) {
-        if (valid) {
-            reinterpret_cast<float4*>(a.agg)[(size_t)chunk * a.n_lanes + li] =
-                make_float4(0.f, 0.f, 0.f, kBeforeSeed);
-        }
-        return;
-    }
-    // PASS_AGG: lanes of one warp may disagree on need_loop; inactive lanes
-    // just run the loop body producing nothing.
     for (int tb = c0; tb < c1; tb += 32) {
         const int te = min(tb + 32, c1);
-        for (int t = tb; t < te; ++t) {
-            float v = qnan();
-            if (active && t >= op.f && seeded_ever) {
-                if (running) {
-                    steps += op.step(in, t);
-                    v = op.value(in, t);
-                } else if (t <= op.s) {
-                    op.accum(in, t);
-                    if (t == op.s) {
-                        op.seed();
-                        running = true;
-                        v = op.value(in, t);
-                    } else {
-                        v = op.warm_value(t);
-                    }
-                }
-            } else if (active && t >= op.f && !seeded_ever) {
-                // never seeded (s >= n): only warm-up style outputs
-                op.accum(in, t);
-                v = op.warm_value(t);
-            }
-            if (PASS == PASS_EMIT) {
-                if (TM) {
+        if (tb >= warp_run_from) {
+            // ---- fast path: every lane running and past warm-up
+            if (PASS == PASS_EMIT && !TM) {
+#pragma unroll 8
+                for (int t = tb; t < te; ++t) stage[warp][lane][t - tb] = op.fast(in, t, steps);
+            } else if (PASS == PASS_EMIT) {
+#pragma unroll 8
+                for (int t = tb; t < te; ++t) {
+                    const float v = op.fast(in, t, steps);
                     if (valid) a.out[(size_t)t * a.cols + li] = v;
-                } else {
-                    stage[warp][lane][t - tb] = v;
+                }
+            } else {
+#pragma unroll 8
+                for (int t = tb; t < te; ++t) op.fast(in, t, steps);
+            }
+        } else {
+            // ---- general path
+            for (int t = tb; t < te; ++t) {
+                float v = qnan();
+                if (active && t >= op.f && seeded_ever) {
+                    if (running) {
+                        steps += op.step(in, t);
+                        v = op.value(in, t);
+                    } else if (t <= op.s) {
+                        op.accum(in, t);
+                        if (t == op.s) {
+                            op.seed();
+                            running = true;
+                            v = op.value(in, t);
+                        } else {
+                            v = op.warm_value(t);
+                        }
+                    }
+                } else if (active && t >= op.f && !seeded_ever) {
+                    op.accum(in, t);  // never seeded (s >= n): warm-up style outputs only
+                    v = op.warm_value(t);
+                }
+                if (PASS == PASS_EMIT) {
+                    if (TM) {
+                        if (valid) a.out[(size_t)t * a.cols + li] = v;
+                    } else {
+                        stage[warp][lane][t - tb] = v;
+                    }
                 }
             }
         }
@@ -412,9 +481,11 @@ k_recur(RecurArgs a) {
             __syncwarp();
             const int row0 = group * 32;
             const int t = tb + lane;
-            for (int r = 0; r < 32; ++r) {
-                const int row = row0 + r;
-                if (row < a.n_lanes && t < te) a.out[(size_t)row * a.n + t] = stage[warp][r][lane];
+            if (t < te) {
+                float* o = a.out + (size_t)row0 * a.n + t;
+                const int rows = min(32, a.n_lanes - row0);
+#pragma unroll 4
+                for (int r = 0; r < rows; ++r) o[(size_t)r * a.n] = stage[warp][r][lane];
             }
             __syncwarp();
         }
@@ -432,24 +503,40 @@ k_recur(RecurArgs a) {
     }
 }
 
+// Per lane, composes the chunk transforms in f64.  The transition for a full
+// chunk (the common case) is computed once by propagating basis vectors.
 template <class Op>
 __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
     const int li = blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= a.n_lanes) return;
     const int p = a.layout ? a.period : a.periods[li];
+    // M^chunk as a 3x3 matrix: columns = propagate(e_k)
+    double M[3][3];
+    for (int k = 0; k < 3; ++k) {
+        double e[3] = {0.0, 0.0, 0.0};
+        e[k] = 1.0;
+        Op::propagate(e, (double)a.chunk, p);
+        for (int r = 0; r < 3; ++r) M[r][k] = e[r];
+    }
     double S[3] = {0.0, 0.0, 0.0};
     const float4* agg = reinterpret_cast<const float4*>(a.agg);
     float4* carry = reinterpret_cast<float4*>(a.carry);
-    // M^chunk for full chunks is the common case: propagate a probe once
     for (int k = 0; k < n_chunks; ++k) {
         carry[(size_t)k * a.n_lanes + li] = make_float4((float)S[0], (float)S[1], (float)S[2], 0.f);
-        float4 g = agg[(size_t)k * a.n_lanes + li];
+        const float4 g = agg[(size_t)k * a.n_lanes + li];
         if (g.w == kBeforeSeed) continue;
         if (g.w == kAbsolute) {
             S[0] = g.x; S[1] = g.y; S[2] = g.z;
             continue;
         }
-        Op::propagate(S, (double)g.w, p);
+        if (g.w == (float)a.chunk) {
+            const double s0 = S[0], s1 = S[1], s2 = S[2];
+            S[0] = M[0][0] * s0 + M[0][1] * s1 + M[0][2] * s2;
+            S[1] = M[1][0] * s0 + M[1][1] * s1 + M[1][2] * s2;
+            S[2] = M[2][0] * s0 + M[2][1] * s1 + M[2][2] * s2;
+        } else {
+            Op::propagate(S, (double)g.w, p);
+        }
         S[0] += g.x; S[1] += g.y; S[2] += g.z;
     }
 }

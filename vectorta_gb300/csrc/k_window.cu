@@ -95,42 +95,63 @@ __device__ __forceinline__ WinOut window_eval(int kind, DS s1, DS s2, float pf, 
 }
 
 // ---------------------------------------------- prefix windows, batch ------
+// One block per time tile of kPwTile steps serves every combo: the tile's
+// prefix span [t0 - pmax, t0 + kPwTile) is staged in shared memory once, each
+// thread keeps P[t] for its kPwPer times in registers and loops over combos.
 constexpr int kPwThreads = 256;
-constexpr int kPwCombos = 4;  // combos per thread (reuses the P[t] loads)
+constexpr int kPwPer = 4;
+constexpr int kPwTile = kPwThreads * kPwPer;
 
 __global__ void __launch_bounds__(kPwThreads)
-k_prefix_window_batch(PrefixWinArgs a) {
-    const int t = blockIdx.x * kPwThreads + threadIdx.x;
-    if (t >= a.n) return;
-    const int c_base = blockIdx.y * kPwCombos;
+k_prefix_window_batch(PrefixWinArgs a, int pmax) {
+    extern __shared__ float2 psm[];
+    const int t0 = blockIdx.x * kPwTile;
+    const int span = kPwTile + pmax;
+    const int base = t0 - pmax;  // global index of slot 0
+    const bool two = a.kind != WK_SMA;
+    float2* s1 = psm;
+    float2* s2 = psm + span;
     const float2 z = make_float2(0.f, 0.f);
-    const float2 p1t = a.p1[t];
-    const float2 p2t = a.kind == WK_SMA ? z : a.p2[t];
-    const float xt = a.kind == WK_ZSCORE ? a.x[t] : 0.f;
+    for (int i = threadIdx.x; i < span; i += kPwThreads) {
+        const int g = base + i;
+        const bool in = g >= 0 && g < a.n;
+        s1[i] = in ? a.p1[g] : z;
+        if (two) s2[i] = in ? a.p2[g] : z;
+    }
+    __syncthreads();
+    float2 p1t[kPwPer], p2t[kPwPer];
+    float xt[kPwPer];
 #pragma unroll
-    for (int j = 0; j < kPwCombos; ++j) {
-        const int c = c_base + j;
-        if (c >= a.n_combos) break;
+    for (int k = 0; k < kPwPer; ++k) {
+        const int l = pmax + threadIdx.x + k * kPwThreads;  // local index of t
+        const int t = t0 + threadIdx.x + k * kPwThreads;
+        p1t[k] = s1[l];
+        p2t[k] = two ? s2[l] : z;
+        xt[k] = (a.kind == WK_ZSCORE && t < a.n) ? a.x[t] : 0.f;
+    }
+    for (int c = 0; c < a.n_combos; ++c) {
         const int p = a.periods[c];
-        const size_t o = (size_t)c * a.n + t;
-        if (t < a.first + p - 1) {
-            a.out0[o] = qnan();
-            if (a.kind == WK_BB) { a.out1[o] = qnan(); a.out2[o] = qnan(); }
-            continue;
-        }
-        const int tb = t - p;
-        const float2 p1b = tb >= 0 ? a.p1[tb] : z;
-        const DS s1 = ds_sub2(p1t, p1b);
-        DS s2 = {0.f, 0.f};
-        if (a.kind != WK_SMA) {
-            const float2 p2b = tb >= 0 ? a.p2[tb] : z;
-            s2 = ds_sub2(p2t, p2b);
-        }
+        const int warm = a.first + p - 1;
         const float k1 = a.k1 ? a.k1[c] : 1.f;
         const float k2 = a.k2 ? a.k2[c] : 1.f;
-        const WinOut r = window_eval(a.kind, s1, s2, (float)p, xt, k1, k2);
-        a.out0[o] = r.o0;
-        if (a.kind == WK_BB) { a.out1[o] = r.o1; a.out2[o] = r.o2; }
+        const float pf = (float)p;
+#pragma unroll
+        for (int k = 0; k < kPwPer; ++k) {
+            const int t = t0 + threadIdx.x + k * kPwThreads;
+            if (t >= a.n) break;
+            const size_t o = (size_t)c * a.n + t;
+            if (t < warm) {
+                a.out0[o] = qnan();
+                if (a.kind == WK_BB) { a.out1[o] = qnan(); a.out2[o] = qnan(); }
+                continue;
+            }
+            const int lb = pmax + threadIdx.x + k * kPwThreads - p;  // local index of t - p
+            const DS w1 = ds_sub2(p1t[k], s1[lb]);
+            const DS w2 = two ? ds_sub2(p2t[k], s2[lb]) : DS{0.f, 0.f};
+            const WinOut r = window_eval(a.kind, w1, w2, pf, xt[k], k1, k2);
+            a.out0[o] = r.o0;
+            if (a.kind == WK_BB) { a.out1[o] = r.o1; a.out2[o] = r.o2; }
+        }
     }
 }
 
@@ -452,11 +473,12 @@ __global__ void k_percentile(PnrArgs a) {
 
 }  // namespace
 
-vta_status launch_prefix_window_batch(const PrefixWinArgs& a, cudaStream_t st) {
-    dim3 grid(ceil_div(a.n, kPwThreads), ceil_div(a.n_combos, kPwCombos));
-    if (grid.y > 65535) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "prefix window: too many combos");
+vta_status launch_prefix_window_batch(const PrefixWinArgs& a, int pmax, size_t smem_optin, cudaStream_t st) {
+    const size_t smem = (size_t)(kPwTile + pmax) * sizeof(float2) * (a.kind == WK_SMA ? 1 : 2);
+    if (smem > smem_optin) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "prefix window: period too large");
+    VTA_CUDA_TRY(cudaFuncSetAttribute(k_prefix_window_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     ktimer_begin(st);
-    k_prefix_window_batch<<<grid, kPwThreads, 0, st>>>(a);
+    k_prefix_window_batch<<<ceil_div(a.n, kPwTile), kPwThreads, smem, st>>>(a, pmax);
     ktimer_end(st);
     return check_launch("k_prefix_window_batch");
 }

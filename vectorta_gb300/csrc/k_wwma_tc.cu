@@ -1,12 +1,606 @@
-// tcgen05 split-precision Hankel contraction for the weighted-window moving
-// averages (placeholder until the tensor-core kernel lands: reports
-// NOT_IMPLEMENTED so the caller takes the FP32 CUDA-core kernel).
+// Weighted-window moving averages as a split-precision tcgen05 contraction.
+//
+//   out[c][t] = sum_k W[c][k] * x[t - K + 1 + k]        (rows of W right-aligned)
+//
+// is a GEMM D[M = combos][N = times] = A[M][K] * B[K][N] whose B operand is the
+// Hankel matrix B[k][n] = x[base + k + n].  Per CTA: one tile of 128 combos
+// (A, K-major, packed in core-matrix order and bulk-copied to shared memory
+// once with cp.async.bulk) and a run of 256-wide time tiles.  B is never
+// materialised as a K x 256 tile: the producer writes an "8-shift expanded
+// strip" E[q] = x16[base + q .. base + q + 7] (16 bytes per q), so the 8x8 core
+// matrix (kc, nc) of the MN-major canonical layout is the contiguous 128-byte
+// block at q = 8*(kc + nc) and both descriptor strides are 128 bytes.  A K x 256
+// tile therefore costs (K/8 + 31) * 128 bytes of shared memory, and stepping K
+// by 16 just advances the descriptor start by 256 bytes.
+//
+// Precision: operands are split into FP16 hi + lo parts after exact power-of-
+// two scaling (per weight row; per time tile after centring x on a tile
+// reference value r, using sum_k w_k = S_c):
+//   y = 2^-(e_c + e_x) * (Ah Bh + Ah Bl + Al Bh) + r * S_c,
+// three tcgen05.mma.kind::f16 per K step with FP32 accumulation in TMEM.  The
+// split keeps ~22 significant bits per operand (FP16 has 11), so the result is
+// within ~1e-7 relative of the FP64 sum.  A BF16 hi/lo variant (8-bit
+// significands, ~16 bits per operand) is selectable for comparison.
+//
+// Pipeline (256 threads): warpgroup 0 builds strips (double-buffered) and its
+// thread 0 issues the MMAs into one of two 256-column TMEM accumulators;
+// warpgroup 1 drains the other accumulator (tcgen05.ld), applies scale,
+// centring, warm-up / NaN masks and stores.  mbarriers hand buffers back and
+// forth; every wait is bounded by a time limit after which the kernel records
+// an error code, stops issuing work, drains its own MMAs and frees TMEM.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include "vta_internal.h"
 
 namespace vta {
+namespace {
 
-vta_status launch_wwma_batch_tc(const WwmaBatchArgs&, int, vta_ctx*, cudaStream_t) {
-    return fail(VTA_ERR_NOT_IMPLEMENTED, "tcgen05 contraction not built");
+constexpr int kM = 128;          // combos per tile (MMA M)
+constexpr int kN = 256;          // times per tile (MMA N)
+constexpr int kThreads = 256;
+constexpr int kMaxK = 352;       // largest tile K (period) the shared memory holds
+constexpr uint32_t kTmemCols = 512;
+constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
+
+__device__ __forceinline__ float qnan() { return __int_as_float(0x7fc00000); }
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ unsigned long long now_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// ------------------------------------------------------------ mbarrier ----
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: false on timeout or when another thread raised the abort flag.
+__device__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag) {
+    const unsigned long long t0 = now_ns();
+    for (;;) {
+        if (mbar_try(b, parity)) return true;
+        if (*abort_flag) return false;
+        if (now_ns() - t0 > kWaitNs) return false;
+    }
+}
+
+// ------------------------------------------------------------ tcgen05 -----
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor, no swizzle: start, leading / stride byte
+// offsets (>> 4), descriptor version 1 at bits 46-47.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: D f32, A/B f16 (0) or bf16 (1),
+// A K-major, B MN-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t instr_desc(uint32_t ab_type) {
+    return (1u << 4) | (ab_type << 7) | (ab_type << 10) | (0u << 15) | (1u << 16) | ((uint32_t)(kN >> 3) << 17) |
+           ((uint32_t)(kM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(bar))
+                 : "memory");
+}
+
+#define TC_LD32(taddr, r)                                                                                   \
+    asm volatile(                                                                                           \
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16," \
+        "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"                              \
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),   \
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),          \
+          "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),        \
+          "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),        \
+          "=r"(r[29]), "=r"(r[30]), "=r"(r[31])                                                              \
+        : "r"(taddr))
+
+// ------------------------------------------------------------ splitting ---
+template <int VARIANT>
+struct Split;
+template <>
+struct Split<0> {  // FP16 hi/lo
+    static __device__ __forceinline__ void run(float v, uint16_t& hi, uint16_t& lo) {
+        const __half h = __float2half_rn(v);
+        const __half l = __float2half_rn(v - __half2float(h));
+        hi = __half_as_ushort(h);
+        lo = __half_as_ushort(l);
+    }
+};
+template <>
+struct Split<1> {  // BF16 hi/lo
+    static __device__ __forceinline__ void run(float v, uint16_t& hi, uint16_t& lo) {
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+        hi = __bfloat16_as_ushort(h);
+        lo = __bfloat16_as_ushort(l);
+    }
+};
+
+// ------------------------------------------------------------ A packing ---
+// Per combo tile m (rows c = 128 m + r): K_m = roundup16(max period), the last
+// K_m columns of the right-aligned weight matrix, scaled by 2^e_r so the row
+// maximum lies in [2^13, 2^14), split hi/lo and laid out as core matrices
+// [K_m/8][16 row groups][8 rows][8 elements].
+struct PackArgs {
+    const float* w;
+    int kmax, n_combos;
+    const int* tile_k;          // [tiles] K_m
+    const long long* tile_off;  // [tiles] offset (elements) of the hi block; lo follows
+    uint16_t* packed;
+    float* row_scale;           // [tiles*128] 2^-e_r
+    float* row_sum;             // [tiles*128] sum of the f32 weights
+};
+
+template <int VARIANT>
+__global__ void k_pack_a(PackArgs a) {
+    const int m = blockIdx.x;
+    const int K = a.tile_k[m];
+    const int r = threadIdx.x;  // 128 threads: one row each
+    const int c = m * kM + r;
+    float mx = 0.f;
+    double sum = 0.0;
+    if (c < a.n_combos) {
+        const float* row = a.w + (size_t)c * a.kmax + (a.kmax - K);
+        for (int k = 0; k < K; ++k) {
+            const float v = (a.kmax - K + k) >= 0 ? row[k] : 0.f;
+            mx = fmaxf(mx, fabsf(v));
+            sum += (double)v;
+        }
+    }
+    int e = 0;
+    if (mx > 0.f) {
+        int ex;
+        frexpf(mx, &ex);  // mx = f * 2^ex, f in [0.5, 1)
+        e = 14 - ex;
+    }
+    const float sc = ldexpf(1.f, e);
+    a.row_scale[(size_t)m * kM + r] = mx > 0.f ? ldexpf(1.f, -e) : 0.f;
+    a.row_sum[(size_t)m * kM + r] = (float)sum;
+    uint16_t* hi = a.packed + a.tile_off[m];
+    uint16_t* lo = hi + (size_t)kM * K;
+    const int g = r >> 3, rr = r & 7;
+    for (int k = 0; k < K; ++k) {
+        float v = 0.f;
+        if (c < a.n_combos && (a.kmax - K + k) >= 0) v = a.w[(size_t)c * a.kmax + (a.kmax - K + k)] * sc;
+        uint16_t h, l;
+        Split<VARIANT>::run(v, h, l);
+        const size_t o = ((size_t)(k >> 3) * 16 + g) * 64 + rr * 8 + (k & 7);
+        hi[o] = h;
+        lo[o] = l;
+    }
+}
+
+// ------------------------------------------------------------ main kernel -
+struct TcArgs {
+    const float* x;
+    int n, first;
+    const int* periods;
+    int n_combos;
+    const int* tile_k;
+    const long long* tile_off;
+    const uint16_t* packed;
+    const float* row_scale;
+    const float* row_sum;
+    int nan_mode;
+    const double* nanp;
+    float* out;
+    int tiles_per_chunk;  // time tiles per CTA
+    int* err;             // error word (0 = ok)
+};
+
+struct __align__(16) SmemCtl {
+    uint64_t a_full;
+    uint64_t mma_done[2];
+    uint64_t acc_empty[2];
+    uint64_t params_full[2];
+    uint32_t tmem_base;
+    int abort_flag;
+    int stop;
+    int issued;  // tiles whose MMAs were committed
+    float ref[2];
+    float xscale[2];  // 2^-e_x
+    float red[8];
+};
+
+template <int VARIANT>
+__global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    const int m = blockIdx.y;
+    const int K = a.tile_k[m];
+    const int KC = K >> 3;                 // 8-column chunks
+    const int J = KC + (kN >> 3) - 1;      // strip blocks of 8 shifts
+    const int span = K + kN + 8;           // linear x values per tile (with slack)
+    // layout: A hi | A lo | strip[2] hi | strip[2] lo | linear[2] hi/lo | ctl
+    uint8_t* p = smem_raw;
+    uint16_t* a_hi = reinterpret_cast<uint16_t*>(p);
+    p += (size_t)kM * K * 2;
+    uint16_t* a_lo = reinterpret_cast<uint16_t*>(p);
+    p += (size_t)kM * K * 2;
+    const size_t strip_bytes = (size_t)J * 8 * 16;
+    uint8_t* strip_hi[2] = {p, p + strip_bytes};
+    p += 2 * strip_bytes;
+    uint8_t* strip_lo[2] = {p, p + strip_bytes};
+    p += 2 * strip_bytes;
+    const size_t lin_bytes = (size_t)((span + 15) & ~15) * 2;
+    uint16_t* lin_hi = reinterpret_cast<uint16_t*>(p);
+    p += lin_bytes;
+    uint16_t* lin_lo = reinterpret_cast<uint16_t*>(p);
+    p += lin_bytes;
+    SmemCtl* ctl = reinterpret_cast<SmemCtl*>(p);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int n_time_tiles = (a.n + kN - 1) / kN;
+    const int tile_begin = blockIdx.x * a.tiles_per_chunk;
+    const int tile_end = min(tile_begin + a.tiles_per_chunk, n_time_tiles);
+    const int ntiles = tile_end - tile_begin;
+    volatile int* abort_flag = &ctl->abort_flag;
+
+    if (tid == 0) {
+        mbar_init(&ctl->a_full, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&ctl->mma_done[b], 1);
+            mbar_init(&ctl->acc_empty[b], kThreads / 2);
+            mbar_init(&ctl->params_full[b], 1);
+        }
+        ctl->abort_flag = 0;
+        ctl->stop = 0;
+        ctl->issued = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&ctl->tmem_base)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = ctl->tmem_base;
+
+    if (tid == 0 && ntiles > 0) {
+        // A tile -> shared memory with two bulk copies completing on a_full
+        const uint32_t bytes = (uint32_t)kM * K * 2;
+        const uint16_t* src = a.packed + a.tile_off[m];
+        mbar_arrive_tx(&ctl->a_full, 2 * bytes);
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_u32(a_hi)),
+            "l"(src), "r"(bytes), "r"(smem_u32(&ctl->a_full))
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_u32(a_lo)),
+            "l"(src + (size_t)kM * K), "r"(bytes), "r"(smem_u32(&ctl->a_full))
+            : "memory");
+    }
+
+    if (warp < 4) {
+        // ================= producer warpgroup (+ MMA issue by tid 0) ========
+        // All waits are made by tid 0 and broadcast through ctl->stop after a
+        // named barrier, so the 128 producer threads leave the loop together.
+        const uint32_t idesc = instr_desc(VARIANT);
+        for (int i = 0; i < ntiles; ++i) {
+            const int b = i & 1;
+            const int t0 = (tile_begin + i) * kN;
+            const int base = t0 - K + 1;
+            if (tid == 0) {
+                // buffer b (strip, tile parameters, TMEM columns) is free once the
+                // MMAs of tile i-2 completed and its epilogue released it
+                bool ok = true;
+                if (i >= 2) {
+                    ok = mbar_wait(&ctl->mma_done[b], ((i >> 1) - 1) & 1, abort_flag) &&
+                         mbar_wait(&ctl->acc_empty[b], ((i >> 1) - 1) & 1, abort_flag);
+                }
+                if (!ok) ctl->abort_flag = 1;
+                ctl->stop = ctl->abort_flag;
+            }
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            if (ctl->stop) break;
+            // reference value (a valid x near the tile end) and max |x - r|
+            float ref = 0.f;
+            {
+                const int g = min(t0 + kN - 1, a.n - 1);
+                const float v = (g >= a.first && g >= 0) ? a.x[g] : 0.f;
+                ref = isfinite(v) ? v : 0.f;
+            }
+            float mx = 0.f;
+            for (int q = tid; q < span; q += 128) {
+                const int g = base + q;
+                float v = 0.f;
+                if (g >= a.first && g < a.n) {
+                    v = a.x[g];
+                    v = isfinite(v) ? v - ref : 0.f;
+                }
+                mx = fmaxf(mx, fabsf(v));
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            if (lane == 0) ctl->red[warp] = mx;
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            mx = fmaxf(fmaxf(ctl->red[0], ctl->red[1]), fmaxf(ctl->red[2], ctl->red[3]));
+            int ex = 0;
+            if (mx > 0.f) {
+                int e2;
+                frexpf(mx, &e2);
+                ex = 13 - e2;
+            }
+            const float sc = ldexpf(1.f, ex);
+            // linear hi/lo of the span, then the expanded strip E[q] = lin[q .. q+7]
+            for (int q = tid; q < span; q += 128) {
+                const int g = base + q;
+                float v = 0.f;
+                if (g >= a.first && g < a.n) {
+                    v = a.x[g];
+                    v = isfinite(v) ? (v - ref) * sc : 0.f;
+                }
+                uint16_t h, l;
+                Split<VARIANT>::run(v, h, l);
+                lin_hi[q] = h;
+                lin_lo[q] = l;
+            }
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            const uint32_t* lh = reinterpret_cast<const uint32_t*>(lin_hi);
+            const uint32_t* ll = reinterpret_cast<const uint32_t*>(lin_lo);
+            for (int q = tid; q < J * 8; q += 128) {
+                const int w0 = q >> 1;
+                uint4 oh, ol;
+                if (q & 1) {
+                    oh.x = __byte_perm(lh[w0], lh[w0 + 1], 0x5432);
+                    oh.y = __byte_perm(lh[w0 + 1], lh[w0 + 2], 0x5432);
+                    oh.z = __byte_perm(lh[w0 + 2], lh[w0 + 3], 0x5432);
+                    oh.w = __byte_perm(lh[w0 + 3], lh[w0 + 4], 0x5432);
+                    ol.x = __byte_perm(ll[w0], ll[w0 + 1], 0x5432);
+                    ol.y = __byte_perm(ll[w0 + 1], ll[w0 + 2], 0x5432);
+                    ol.z = __byte_perm(ll[w0 + 2], ll[w0 + 3], 0x5432);
+                    ol.w = __byte_perm(ll[w0 + 3], ll[w0 + 4], 0x5432);
+                } else {
+                    oh = make_uint4(lh[w0], lh[w0 + 1], lh[w0 + 2], lh[w0 + 3]);
+                    ol = make_uint4(ll[w0], ll[w0 + 1], ll[w0 + 2], ll[w0 + 3]);
+                }
+                reinterpret_cast<uint4*>(strip_hi[b])[q] = oh;
+                reinterpret_cast<uint4*>(strip_lo[b])[q] = ol;
+            }
+            if (tid == 0) {
+                ctl->ref[b] = ref;
+                ctl->xscale[b] = ldexpf(1.f, -ex);
+            }
+            // generic-proxy smem writes -> visible to the tensor core (async proxy)
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            if (tid == 0) {
+                mbar_arrive(&ctl->params_full[b]);
+                const bool ok = (i > 0) || mbar_wait(&ctl->a_full, 0, abort_flag);
+                if (!ok) {
+                    ctl->abort_flag = 1;
+                } else {
+                    tc_fence_after();
+                    const uint32_t d = tmem + (uint32_t)(b * kN);
+                    const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
+                    const uint32_t bh = smem_u32(strip_hi[b]), bl = smem_u32(strip_lo[b]);
+                    for (int ks = 0; ks < (K >> 4); ++ks) {
+                        // A: next 2 K-chunks (16 row groups * 128 B each); B: next 2 strip blocks
+                        const uint32_t ao = (uint32_t)ks * 2 * 16 * 128, bo = (uint32_t)ks * 256;
+                        const uint64_t dah = smem_desc(ah + ao, 16 * 128, 128);
+                        const uint64_t dal = smem_desc(al + ao, 16 * 128, 128);
+                        const uint64_t dbh = smem_desc(bh + bo, 128, 128);
+                        const uint64_t dbl = smem_desc(bl + bo, 128, 128);
+                        tc_mma(d, dah, dbh, idesc, ks > 0 ? 1u : 0u);
+                        tc_mma(d, dah, dbl, idesc, 1u);
+                        tc_mma(d, dal, dbh, idesc, 1u);
+                    }
+                    tc_commit(&ctl->mma_done[b]);
+                    ctl->issued = i + 1;
+                }
+            }
+        }
+    } else {
+        // ================= epilogue warpgroup ================================
+        const int q4 = warp & 3;
+        const int r = q4 * 32 + lane;  // accumulator row = combo within tile
+        const int c = m * kM + r;
+        const bool row_ok = c < a.n_combos;
+        const int p = row_ok ? a.periods[c] : 1;
+        const int warm = a.first + p - 1;
+        const float rscale = a.row_scale[(size_t)m * kM + r];
+        const float rsum = a.row_sum[(size_t)m * kM + r];
+        const bool vec_ok = (a.n & 3) == 0;
+        const bool has_nan = a.nanp != nullptr && a.nanp[a.n - 1] > 0.5;
+        for (int i = 0; i < ntiles; ++i) {
+            const int b = i & 1;
+            const int t0 = (tile_begin + i) * kN;
+            // one lane waits, the warp follows (tcgen05.ld is warp-collective)
+            int ok = 1;
+            if (lane == 0) {
+                ok = mbar_wait(&ctl->mma_done[b], (i >> 1) & 1, abort_flag) &&
+                     mbar_wait(&ctl->params_full[b], (i >> 1) & 1, abort_flag);
+                if (!ok) ctl->abort_flag = 1;
+            }
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) break;
+            tc_fence_after();
+            const float ref = ctl->ref[b];
+            const float scale = rscale * ctl->xscale[b];
+            const float off = ref * rsum;
+            float* orow = a.out + (size_t)c * a.n;
+            for (int cb = 0; cb < kN; cb += 32) {
+                uint32_t v[32];
+                const uint32_t taddr = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * kN + cb);
+                TC_LD32(taddr, v);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (!row_ok) continue;
+                float y[32];
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int t = t0 + cb + j;
+                    float val = fmaf(__uint_as_float(v[j]), scale, off);
+                    if (t < warm) val = qnan();
+                    else if (has_nan && t < a.n) {
+                        const double hi = a.nanp[t];
+                        const double lo = (a.nan_mode == 0 && t - p >= 0) ? a.nanp[t - p] : 0.0;
+                        if (hi - lo > 0.5) val = qnan();
+                    }
+                    y[j] = val;
+                }
+                const int tb = t0 + cb;
+                if (vec_ok && tb + 32 <= a.n) {
+                    float4* o4 = reinterpret_cast<float4*>(orow + tb);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) o4[j] = make_float4(y[4 * j], y[4 * j + 1], y[4 * j + 2], y[4 * j + 3]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j)
+                        if (tb + j < a.n) orow[tb + j] = y[j];
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(&ctl->acc_empty[b]);
+        }
+    }
+
+    // drain: the last committed MMAs must have completed before TMEM is freed
+    __syncthreads();
+    if (tid == 0) {
+        const int last = ctl->issued - 1;
+        if (last >= 0) {
+            const unsigned long long t0 = now_ns();
+            while (!mbar_try(&ctl->mma_done[last & 1], (last >> 1) & 1) && now_ns() - t0 < kWaitNs) {
+            }
+        }
+        if (ctl->abort_flag) atomicExch(a.err, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols)
+                     : "memory");
+    }
+}
+
+size_t smem_bytes_for(int K) {
+    const int J = K / 8 + kN / 8 - 1;
+    const int span = K + kN + 8;
+    return (size_t)kM * K * 2 * 2 + 4 * (size_t)J * 8 * 16 + 2 * (size_t)(((span + 15) & ~15) * 2) +
+           sizeof(SmemCtl) + 128;
+}
+
+}  // namespace
+
+vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ctx, cudaStream_t st) {
+    const int n_tiles_m = (a.n_combos + kM - 1) / kM;
+    const int* per = a.periods_host;
+    std::vector<int> tk(n_tiles_m);
+    std::vector<long long> toff(n_tiles_m);
+    long long off = 0;
+    int kbig = 16;
+    for (int mt = 0; mt < n_tiles_m; ++mt) {
+        int mx = 1;
+        for (int r = 0; r < kM && mt * kM + r < a.n_combos; ++r) mx = std::max(mx, per[mt * kM + r]);
+        const int K = (mx + 15) & ~15;
+        if (K > kMaxK) return fail(VTA_ERR_NOT_IMPLEMENTED, "tcgen05 path: period above the shared-memory limit");
+        tk[mt] = K;
+        toff[mt] = off;
+        off += 2LL * kM * K;
+        kbig = std::max(kbig, K);
+    }
+    // never below 160 KB: every descriptor address stays inside the allocation
+    const size_t smem = std::max<size_t>(smem_bytes_for(kbig), 160 * 1024);
+    if (smem > ctx->smem_optin) return fail(VTA_ERR_NOT_IMPLEMENTED, "tcgen05 path: shared memory");
+    // packed operands in a stream-ordered buffer of their own (the context
+    // workspace holds the caller's weights and periods during this call)
+    auto al256 = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t total = al256(n_tiles_m * sizeof(int)) + al256(n_tiles_m * sizeof(long long)) +
+                         al256((size_t)off * sizeof(uint16_t)) + 2 * al256((size_t)n_tiles_m * kM * sizeof(float)) +
+                         al256(sizeof(int));
+    void* buf = nullptr;
+    VTA_CUDA_TRY(cudaMallocAsync(&buf, total, st));
+    char* bp = static_cast<char*>(buf);
+    auto take = [&](size_t bytes) {
+        char* r = bp;
+        bp += (bytes + 255) & ~size_t(255);
+        return r;
+    };
+    int* d_tk = reinterpret_cast<int*>(take(n_tiles_m * sizeof(int)));
+    long long* d_toff = reinterpret_cast<long long*>(take(n_tiles_m * sizeof(long long)));
+    uint16_t* d_packed = reinterpret_cast<uint16_t*>(take((size_t)off * sizeof(uint16_t)));
+    float* d_rs = reinterpret_cast<float*>(take((size_t)n_tiles_m * kM * sizeof(float)));
+    float* d_rsum = reinterpret_cast<float*>(take((size_t)n_tiles_m * kM * sizeof(float)));
+    int* d_err = reinterpret_cast<int*>(take(sizeof(int)));
+    VTA_CUDA_TRY(cudaMemcpyAsync(d_tk, tk.data(), n_tiles_m * sizeof(int), cudaMemcpyHostToDevice, st));
+    VTA_CUDA_TRY(cudaMemcpyAsync(d_toff, toff.data(), n_tiles_m * sizeof(long long), cudaMemcpyHostToDevice, st));
+    VTA_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+    PackArgs pa{a.w, a.kmax, a.n_combos, d_tk, d_toff, d_packed, d_rs, d_rsum};
+    if (variant == 1) k_pack_a<1><<<n_tiles_m, kM, 0, st>>>(pa);
+    else k_pack_a<0><<<n_tiles_m, kM, 0, st>>>(pa);
+    VTA_TRY(check_launch("k_pack_a"));
+
+    TcArgs t{};
+    t.x = a.x;
+    t.n = a.n;
+    t.first = a.first;
+    t.periods = a.periods;
+    t.n_combos = a.n_combos;
+    t.tile_k = d_tk;
+    t.tile_off = d_toff;
+    t.packed = d_packed;
+    t.row_scale = d_rs;
+    t.row_sum = d_rsum;
+    t.nan_mode = a.nan_mode;
+    t.nanp = a.nanp;
+    t.out = a.out;
+    t.err = d_err;
+    const int n_time_tiles = (a.n + kN - 1) / kN;
+    const int target = ctx->num_sms * 6;
+    int chunks = std::max(1, std::min(n_time_tiles, (target + n_tiles_m - 1) / n_tiles_m));
+    t.tiles_per_chunk = (n_time_tiles + chunks - 1) / chunks;
+    chunks = (n_time_tiles + t.tiles_per_chunk - 1) / t.tiles_per_chunk;
+    dim3 grid(chunks, n_tiles_m);
+    if (n_tiles_m > 65535) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "tcgen05 path: too many combo tiles");
+    auto kern = variant == 1 ? k_wwma_tc<1> : k_wwma_tc<0>;
+    VTA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ktimer_begin(st);
+    kern<<<grid, kThreads, smem, st>>>(t);
+    ktimer_end(st);
+    VTA_TRY(check_launch("k_wwma_tc"));
+    int err = 0;
+    VTA_CUDA_TRY(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    VTA_CUDA_TRY(cudaStreamSynchronize(st));
+    cudaFreeAsync(buf, st);
+    if (err) return fail(VTA_ERR_CUDA, "tcgen05 contraction: pipeline wait timed out");
+    return VTA_OK;
 }
 
 }  // namespace vta

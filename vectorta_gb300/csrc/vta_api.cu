@@ -345,6 +345,7 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
         a.first = (int)first;
         a.w = d_w;
         a.periods = d_per;
+        a.periods_host = periods.data();
         a.tile_kmax = d_tk;
         a.kmax = kmax;
         a.n_combos = nc;
@@ -452,7 +453,7 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             a.out0 = out[0];
             if (ind == I_BB) { a.out0 = out[0]; a.out1 = out[1]; a.out2 = out[2]; }
             ctx->last_kernel = "prefix_window_ds";
-            return launch_prefix_window_batch(a, st);
+            return launch_prefix_window_batch(a, pmax, ctx->smem_optin, st);
         }
         case I_DONCHIAN: case I_WILLR: {
             VTA_TRY(ar.commit());

@@ -127,6 +127,7 @@ struct WwmaBatchArgs {
     int first;             // first valid index
     const float* w;        // [n_combos][kmax] normalised weights, right-aligned
     const int* periods;    // [n_combos]
+    const int* periods_host;  // [n_combos] host copy (tile sizing)
     const int* tile_kmax;  // per 16-combo tile: max period (K of the tile)
     int kmax;
     int n_combos;
@@ -219,7 +220,7 @@ struct PrefixWinArgs {
     float* out1;           // bb middle
     float* out2;           // bb lower
 };
-vta_status launch_prefix_window_batch(const PrefixWinArgs& a, cudaStream_t st);
+vta_status launch_prefix_window_batch(const PrefixWinArgs& a, int pmax, size_t smem_optin, cudaStream_t st);
 
 struct PrefixWinTmArgs {
     int kind;
