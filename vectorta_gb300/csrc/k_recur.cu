@@ -386,6 +386,9 @@ k_recur(RecurArgs a) {
     const int c0 = chunk * a.chunk;
     const int c1 = min(c0 + a.chunk, a.n);
     if (c0 >= a.n) return;
+    // a warp with no valid lane has nothing to compute (whole warp leaves; the
+    // kernel has no block-wide barrier)
+    if (group * 32 >= a.n_lanes) return;
 
     Op op;
     int p = 0, first = a.n;
