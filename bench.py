@@ -95,7 +95,20 @@ def workload_ema_small():
             "config": {"workload": "ema_small", "bars": n, "seed": 1, "combos": 999}}
 
 
-WORKLOADS = {"sweeps": workload_sweeps, "alma_grid": workload_alma_grid, "ema_small": workload_ema_small}
+def workload_alma_small():
+    """Profiling case: the 17,920-combo ALMA grid on 20,000 bars (1.4 GB of
+    outputs: larger than L2, a few GB on the device at most)."""
+    w = workload_alma_grid()
+    from vectorta_gb300 import datagen
+
+    n = 20_000
+    w.update(name="alma_small", n=n, series={"close": datagen.random_walk(n, seed=2).astype(np.float32)})
+    w["config"] = dict(w["config"], workload="alma_small", bars=n)
+    return w
+
+
+WORKLOADS = {"sweeps": workload_sweeps, "alma_grid": workload_alma_grid, "ema_small": workload_ema_small,
+             "alma_small": workload_alma_small}
 
 
 # ------------------------------------------------------------- clocks -------
@@ -171,7 +184,7 @@ def cpu_sample(wl, budget_rows=None):
                               wl["n"] * len(O.axis_f64(sweep["offset"])) * len(O.axis_f64(sweep["sigma"]))))
             continue
         ps = O.periods_of(name, sweep["period"])
-        stride = 8 if len(ps) > 500 else 2
+        stride = 4 if len(ps) > 500 else 1
         for p in ps[::stride]:
             if name in ("ema", "dema", "tema"):
                 fn = {"ema": O.ema, "dema": O.dema, "tema": O.tema}[name]
@@ -339,8 +352,8 @@ def e2e_bench(args, wl, inds, rows, out_per_step):
 # dram bytes per launch of the dominant kernel from the committed ncu capture
 # (profiles/*.md); None until captured
 TRAFFIC = {}
-KERNEL_NAME = {"recurrence_window_sweeps": "k_recur<OpEma, batch, EMIT>", "alma_grid": "wwma batch kernel",
-               "ema_small": "k_recur<OpEma, batch, EMIT>"}
+KERNEL_NAME = {"recurrence_window_sweeps": "k_recur<OpEma, batch, EMIT>", "alma_grid": "k_wwma_tc<fp16x3>",
+               "ema_small": "k_recur<OpEma, batch, EMIT>", "alma_small": "k_wwma_tc<fp16x3>"}
 
 
 def main():
