@@ -42,6 +42,27 @@ struct InTm {
     __device__ float C(int t) const { return __ldg(c + (size_t)t * cols + s); }
 };
 
+// One 32-step tile of a single shared series held in registers: lane l holds
+// x[tb + l]; X(t) is a warp shuffle (t - 1 < tb reads the value before the
+// tile).  Used by the batch fast path so each step costs no memory access.
+struct InTile {
+    float xv, hv, lv, cv;  // this lane's element of the tile
+    float xb, cb;          // x[tb-1], c[tb-1]
+    int tb;
+    __device__ float X(int t) const {
+        const int j = t - tb;
+        const float v = __shfl_sync(0xffffffffu, xv, j & 31);
+        return j >= 0 ? v : xb;
+    }
+    __device__ float H(int t) const { return __shfl_sync(0xffffffffu, hv, (t - tb) & 31); }
+    __device__ float L(int t) const { return __shfl_sync(0xffffffffu, lv, (t - tb) & 31); }
+    __device__ float C(int t) const {
+        const int j = t - tb;
+        const float v = __shfl_sync(0xffffffffu, cv, j & 31);
+        return j >= 0 ? v : cb;
+    }
+};
+
 // ------------------------------------------------------------ ops ----------
 // Common op interface:
 //   init(p, f)            lane constants; sets f (first valid), s (seed index),
@@ -57,6 +78,7 @@ struct InTm {
 // EMA: ema.rs:430-469 / 858-893.  Warm-up outputs are the running mean of the
 // finite values of [f, t]; NaN prefix is [0, f); non-finite x is skipped.
 struct OpEma {
+    static constexpr bool kHlc = false;
     static constexpr int NS = 1;
     float alpha, beta, y;
     int f, s, warm;
@@ -102,6 +124,7 @@ struct OpEma {
 // DEMA: dema.rs:291-354 (x86 mul_add form).  Seed x[f] at f; NaN prefix
 // [0, f+p-1); out = 2*e1 - e2.
 struct OpDema {
+    static constexpr bool kHlc = false;
     static constexpr int NS = 2;
     float alpha, a, e1, e2, xf;
     int f, s, warm;
@@ -146,6 +169,7 @@ struct OpDema {
 // as the crate staggers them; running from s = f+2(p-1); NaN prefix
 // [0, f+3(p-1)); out = 3*e1 - 3*e2 + e3; p == 1 copies x.
 struct OpTema {
+    static constexpr bool kHlc = false;
     static constexpr int NS = 3;
     float per, per1, e1, e2, e3;
     int f, s, warm, start2, p1;
@@ -210,6 +234,7 @@ struct OpTema {
 // only inside the warm-up, later ones count as 0).  NaN prefix [0, f+p).
 template <bool kBatchSem>
 struct OpRsi {
+    static constexpr bool kHlc = false;
     static constexpr int NS = 2;
     float inv_p, beta, ag, al, xprev;
     int f, s, warm;
@@ -277,6 +302,7 @@ struct OpRsi {
 // Wilders: wilders.rs:262-322.  Seed = mean of x[f..f+p); y = (x-y)*a + y;
 // NaN prefix [0, f+p-1); p == 1 copies x.
 struct OpWilders {
+    static constexpr bool kHlc = false;
     static constexpr int NS = 1;
     float alpha, y;
     int f, s, warm, p;
@@ -324,6 +350,7 @@ __device__ __forceinline__ float true_range(float hi, float lo, float pc) {
 // rma = (-a).mul_add(rma, rma) + a*tr; NaN prefix [0, f+L-1).
 struct OpAtr {
     static constexpr int NS = 1;
+    static constexpr bool kHlc = true;
     float alpha, y;
     int f, s, warm, p;
     double wsum;
@@ -436,7 +463,29 @@ k_recur(RecurArgs a) {
         const int te = min(tb + 32, c1);
         if (tb >= warp_run_from) {
             // ---- fast path: every lane running and past warm-up
-            if (PASS == PASS_EMIT && !TM) {
+            if (!TM && te - tb == 32) {
+                // the tile's inputs in registers, one coalesced load per lane
+                InTile ti;
+                ti.tb = tb;
+                if constexpr (Op::kHlc) {
+                    ti.hv = __ldg(a.h + tb + lane);
+                    ti.lv = __ldg(a.l + tb + lane);
+                    ti.cv = __ldg(a.c + tb + lane);
+                    ti.cb = __ldg(a.c + tb - 1);
+                    ti.xv = ti.cv;
+                    ti.xb = ti.cb;
+                } else {
+                    ti.xv = __ldg(a.x + tb + lane);
+                    ti.xb = __ldg(a.x + tb - 1);
+                }
+                if (PASS == PASS_EMIT) {
+#pragma unroll 8
+                    for (int j = 0; j < 32; ++j) stage[warp][lane][j] = op.fast(ti, tb + j, steps);
+                } else {
+#pragma unroll 8
+                    for (int j = 0; j < 32; ++j) op.fast(ti, tb + j, steps);
+                }
+            } else if (PASS == PASS_EMIT && !TM) {
 #pragma unroll 8
                 for (int t = tb; t < te; ++t) stage[warp][lane][t - tb] = op.fast(in, t, steps);
             } else if (PASS == PASS_EMIT) {
@@ -506,41 +555,115 @@ k_recur(RecurArgs a) {
     }
 }
 
-// Per lane, composes the chunk transforms in f64.  The transition for a full
-// chunk (the common case) is computed once by propagating basis vectors.
+// Carry-in of every chunk: an exclusive scan, over the chunks of one lane, of
+// the affine chunk maps S -> M_k S + b_k (f64).  One warp per lane: each
+// thread composes a contiguous run of chunks, a Kogge-Stone scan across the
+// warp combines the runs, then each thread re-walks its run writing carries.
+struct Aff {
+    double m[3][3];
+    double b[3];
+};
+
+__device__ __forceinline__ void aff_identity(Aff& a) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) a.m[r][c] = r == c ? 1.0 : 0.0;
+        a.b[r] = 0.0;
+    }
+}
+// returns second o first (apply `first`, then `second`)
+__device__ __forceinline__ Aff aff_then(const Aff& first, const Aff& second) {
+    Aff o;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            o.m[r][c] = second.m[r][0] * first.m[0][c] + second.m[r][1] * first.m[1][c] + second.m[r][2] * first.m[2][c];
+        o.b[r] = second.m[r][0] * first.b[0] + second.m[r][1] * first.b[1] + second.m[r][2] * first.b[2] + second.b[r];
+    }
+    return o;
+}
+__device__ __forceinline__ Aff aff_shfl_up(const Aff& a, int d) {
+    Aff o;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) o.m[r][c] = __shfl_up_sync(0xffffffffu, a.m[r][c], d);
+        o.b[r] = __shfl_up_sync(0xffffffffu, a.b[r], d);
+    }
+    return o;
+}
+
+template <class Op>
+__device__ void chunk_map(const float4 g, int p, int chunk, const double (&ml)[3][3], Aff& a) {
+    if (g.w == kBeforeSeed) {
+        aff_identity(a);
+        return;
+    }
+    if (g.w == kAbsolute) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) a.m[r][c] = 0.0;
+    } else if (g.w == (float)chunk) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) a.m[r][c] = ml[r][c];
+    } else {
+        for (int c = 0; c < 3; ++c) {
+            double e[3] = {0.0, 0.0, 0.0};
+            e[c] = 1.0;
+            Op::propagate(e, (double)g.w, p);
+            for (int r = 0; r < 3; ++r) a.m[r][c] = e[r];
+        }
+    }
+    a.b[0] = g.x;
+    a.b[1] = g.y;
+    a.b[2] = g.z;
+}
+
 template <class Op>
 __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
-    const int li = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int li = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // one warp per lane of the scan
     if (li >= a.n_lanes) return;
     const int p = a.layout ? a.period : a.periods[li];
-    // M^chunk as a 3x3 matrix: columns = propagate(e_k)
-    double M[3][3];
-    for (int k = 0; k < 3; ++k) {
+    double ml[3][3];  // transition of a full chunk
+    for (int c = 0; c < 3; ++c) {
         double e[3] = {0.0, 0.0, 0.0};
-        e[k] = 1.0;
+        e[c] = 1.0;
         Op::propagate(e, (double)a.chunk, p);
-        for (int r = 0; r < 3; ++r) M[r][k] = e[r];
+        for (int r = 0; r < 3; ++r) ml[r][c] = e[r];
     }
-    double S[3] = {0.0, 0.0, 0.0};
     const float4* agg = reinterpret_cast<const float4*>(a.agg);
     float4* carry = reinterpret_cast<float4*>(a.carry);
-    for (int k = 0; k < n_chunks; ++k) {
+    const int per = (n_chunks + 31) / 32;
+    const int k0 = min(lane * per, n_chunks), k1 = min(k0 + per, n_chunks);
+    Aff run;
+    aff_identity(run);
+    for (int k = k0; k < k1; ++k) {
+        Aff ak;
+        chunk_map<Op>(agg[(size_t)k * a.n_lanes + li], p, a.chunk, ml, ak);
+        run = aff_then(run, ak);
+    }
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const Aff up = aff_shfl_up(run, d);
+        if (lane >= d) run = aff_then(up, run);
+    }
+    Aff ex = aff_shfl_up(run, 1);
+    if (lane == 0) aff_identity(ex);
+    double S[3] = {ex.b[0], ex.b[1], ex.b[2]};  // state at the start of chunk k0
+    for (int k = k0; k < k1; ++k) {
         carry[(size_t)k * a.n_lanes + li] = make_float4((float)S[0], (float)S[1], (float)S[2], 0.f);
-        const float4 g = agg[(size_t)k * a.n_lanes + li];
-        if (g.w == kBeforeSeed) continue;
-        if (g.w == kAbsolute) {
-            S[0] = g.x; S[1] = g.y; S[2] = g.z;
-            continue;
-        }
-        if (g.w == (float)a.chunk) {
-            const double s0 = S[0], s1 = S[1], s2 = S[2];
-            S[0] = M[0][0] * s0 + M[0][1] * s1 + M[0][2] * s2;
-            S[1] = M[1][0] * s0 + M[1][1] * s1 + M[1][2] * s2;
-            S[2] = M[2][0] * s0 + M[2][1] * s1 + M[2][2] * s2;
-        } else {
-            Op::propagate(S, (double)g.w, p);
-        }
-        S[0] += g.x; S[1] += g.y; S[2] += g.z;
+        Aff ak;
+        chunk_map<Op>(agg[(size_t)k * a.n_lanes + li], p, a.chunk, ml, ak);
+        double t[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) t[r] = ak.m[r][0] * S[0] + ak.m[r][1] * S[1] + ak.m[r][2] * S[2] + ak.b[r];
+        S[0] = t[0]; S[1] = t[1]; S[2] = t[2];
     }
 }
 
@@ -553,7 +676,7 @@ vta_status run(const RecurArgs& a, cudaStream_t st) {
     if (n_chunks > 1) {
         k_recur<Op, TM, PASS_AGG><<<grid, kWarps * 32, 0, st>>>(a);
         VTA_TRY(check_launch("k_recur_agg"));
-        k_recur_carry<Op><<<ceil_div(a.n_lanes, 128), 128, 0, st>>>(a, n_chunks);
+        k_recur_carry<Op><<<ceil_div((size_t)a.n_lanes * 32, 128), 128, 0, st>>>(a, n_chunks);
         VTA_TRY(check_launch("k_recur_carry"));
     }
     ktimer_begin(st);

@@ -39,7 +39,9 @@ namespace {
 constexpr int kM = 128;          // combos per tile (MMA M)
 constexpr int kN = 256;          // times per tile (MMA N)
 constexpr int kThreads = 256;
-constexpr int kMaxK = 352;       // largest tile K (period) the shared memory holds
+constexpr int kMaxK = 320;       // largest tile K (period) the shared memory holds
+constexpr int kStageLd = 36;     // epilogue staging row stride (floats): 16-B aligned, conflict-free
+constexpr int kSpanRegs = 5;     // x values per producer thread: (kMaxK + kN + 8) / 128 rounded up
 constexpr uint32_t kTmemCols = 512;
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 
@@ -257,6 +259,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
     p += lin_bytes;
     uint16_t* lin_lo = reinterpret_cast<uint16_t*>(p);
     p += lin_bytes;
+    float* stage = reinterpret_cast<float*>(p);  // [4 epilogue warps][32][kStageLd]
+    p += (size_t)4 * 32 * kStageLd * sizeof(float);
     SmemCtl* ctl = reinterpret_cast<SmemCtl*>(p);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -329,23 +333,29 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
             }
             asm volatile("bar.sync 1, 128;" ::: "memory");
             if (ctl->stop) break;
-            // reference value (a valid x near the tile end) and max |x - r|
-            float ref = 0.f;
-            {
-                const int g = min(t0 + kN - 1, a.n - 1);
-                const float v = (g >= a.first && g >= 0) ? a.x[g] : 0.f;
-                ref = isfinite(v) ? v : 0.f;
-            }
-            float mx = 0.f;
-            for (int q = tid; q < span; q += 128) {
+            // the tile's x span is loaded once into registers; reference value r =
+            // the last bar of the tile (a valid x), scale from max |x - r|
+            float xv[kSpanRegs];
+            const int gref = min(t0 + kN - 1, a.n - 1);
+            const float vref = (gref >= a.first && gref >= 0) ? __ldg(a.x + gref) : 0.f;
+#pragma unroll
+            for (int k = 0; k < kSpanRegs; ++k) {
+                const int q = tid + 128 * k;
                 const int g = base + q;
                 float v = 0.f;
-                if (g >= a.first && g < a.n) {
-                    v = a.x[g];
-                    v = isfinite(v) ? v - ref : 0.f;
+                if (q < span && g >= a.first && g < a.n) {
+                    v = __ldg(a.x + g);
+                    if (!isfinite(v)) v = __int_as_float(0x7fc00000);
+                } else {
+                    v = __int_as_float(0x7fc00000);  // outside the series: zero after centring
                 }
-                mx = fmaxf(mx, fabsf(v));
+                xv[k] = v;
             }
+            const float ref = isfinite(vref) ? vref : 0.f;
+            float mx = 0.f;
+#pragma unroll
+            for (int k = 0; k < kSpanRegs; ++k)
+                if (!isnan(xv[k])) mx = fmaxf(mx, fabsf(xv[k] - ref));
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
             if (lane == 0) ctl->red[warp] = mx;
@@ -359,17 +369,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
             }
             const float sc = ldexpf(1.f, ex);
             // linear hi/lo of the span, then the expanded strip E[q] = lin[q .. q+7]
-            for (int q = tid; q < span; q += 128) {
-                const int g = base + q;
-                float v = 0.f;
-                if (g >= a.first && g < a.n) {
-                    v = a.x[g];
-                    v = isfinite(v) ? (v - ref) * sc : 0.f;
+#pragma unroll
+            for (int k = 0; k < kSpanRegs; ++k) {
+                const int q = tid + 128 * k;
+                if (q < span) {
+                    const float v = isnan(xv[k]) ? 0.f : (xv[k] - ref) * sc;
+                    uint16_t h, l;
+                    Split<VARIANT>::run(v, h, l);
+                    lin_hi[q] = h;
+                    lin_lo[q] = l;
                 }
-                uint16_t h, l;
-                Split<VARIANT>::run(v, h, l);
-                lin_hi[q] = h;
-                lin_lo[q] = l;
             }
             asm volatile("bar.sync 1, 128;" ::: "memory");
             const uint32_t* lh = reinterpret_cast<const uint32_t*>(lin_hi);
@@ -432,6 +441,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
         const int r = q4 * 32 + lane;  // accumulator row = combo within tile
         const int c = m * kM + r;
         const bool row_ok = c < a.n_combos;
+        (void)row_ok;
         const int p = row_ok ? a.periods[c] : 1;
         const int warm = a.first + p - 1;
         const float rscale = a.row_scale[(size_t)m * kM + r];
@@ -454,36 +464,54 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
             const float ref = ctl->ref[b];
             const float scale = rscale * ctl->xscale[b];
             const float off = ref * rsum;
-            float* orow = a.out + (size_t)c * a.n;
+            float* st = stage + (size_t)q4 * 32 * kStageLd;
+            const int rbase = m * kM + q4 * 32;  // first combo of this warp's rows
             for (int cb = 0; cb < kN; cb += 32) {
                 uint32_t v[32];
                 const uint32_t taddr = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * kN + cb);
                 TC_LD32(taddr, v);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (!row_ok) continue;
-                float y[32];
+                // this thread's row (combo c), 32 consecutive times -> staging row
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int t = t0 + cb + j;
-                    float val = fmaf(__uint_as_float(v[j]), scale, off);
-                    if (t < warm) val = qnan();
-                    else if (has_nan && t < a.n) {
-                        const double hi = a.nanp[t];
-                        const double lo = (a.nan_mode == 0 && t - p >= 0) ? a.nanp[t - p] : 0.0;
-                        if (hi - lo > 0.5) val = qnan();
+                for (int j4 = 0; j4 < 8; ++j4) {
+                    float y4[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int j = 4 * j4 + u;
+                        const int t = t0 + cb + j;
+                        float val = fmaf(__uint_as_float(v[j]), scale, off);
+                        if (t < warm) val = qnan();
+                        else if (has_nan && t < a.n) {
+                            const double hi = a.nanp[t];
+                            const double lo = (a.nan_mode == 0 && t - p >= 0) ? a.nanp[t - p] : 0.0;
+                            if (hi - lo > 0.5) val = qnan();
+                        }
+                        y4[u] = val;
                     }
-                    y[j] = val;
+                    *reinterpret_cast<float4*>(st + lane * kStageLd + 4 * j4) = make_float4(y4[0], y4[1], y4[2], y4[3]);
                 }
-                const int tb = t0 + cb;
-                if (vec_ok && tb + 32 <= a.n) {
-                    float4* o4 = reinterpret_cast<float4*>(orow + tb);
+                __syncwarp();
+                // 8 lanes per row: each store instruction writes 4 rows x 128 B
+                const int c4 = lane & 7;
+                const int tcol = t0 + cb + 4 * c4;
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) o4[j] = make_float4(y[4 * j], y[4 * j + 1], y[4 * j + 2], y[4 * j + 3]);
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 32; ++j)
-                        if (tb + j < a.n) orow[tb + j] = y[j];
+                for (int k = 0; k < 8; ++k) {
+                    const int rr = 4 * k + (lane >> 3);
+                    const int cr = rbase + rr;
+                    if (cr < a.n_combos) {
+                        const float4 y = *reinterpret_cast<const float4*>(st + rr * kStageLd + 4 * c4);
+                        float* o = a.out + (size_t)cr * a.n + tcol;
+                        if (vec_ok && tcol + 4 <= a.n) {
+                            *reinterpret_cast<float4*>(o) = y;
+                        } else {
+                            if (tcol < a.n) o[0] = y.x;
+                            if (tcol + 1 < a.n) o[1] = y.y;
+                            if (tcol + 2 < a.n) o[2] = y.z;
+                            if (tcol + 3 < a.n) o[3] = y.w;
+                        }
+                    }
                 }
+                __syncwarp();
             }
             tc_fence_before();
             mbar_arrive(&ctl->acc_empty[b]);
@@ -514,7 +542,7 @@ size_t smem_bytes_for(int K) {
     const int J = K / 8 + kN / 8 - 1;
     const int span = K + kN + 8;
     return (size_t)kM * K * 2 * 2 + 4 * (size_t)J * 8 * 16 + 2 * (size_t)(((span + 15) & ~15) * 2) +
-           sizeof(SmemCtl) + 128;
+           (size_t)4 * 32 * kStageLd * sizeof(float) + sizeof(SmemCtl) + 128;
 }
 
 }  // namespace
