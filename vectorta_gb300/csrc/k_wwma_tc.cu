@@ -38,8 +38,9 @@ namespace {
 
 constexpr int kM = 128;          // combos per tile (MMA M)
 constexpr int kN = 256;          // times per tile (MMA N)
-constexpr int kThreads = 256;
-constexpr int kMaxK = 320;       // largest tile K (period) the shared memory holds
+constexpr int kThreads = 384;     // warpgroup 0: producer + MMA; warpgroups 1-2: epilogue
+constexpr int kEpiThreads = 256;
+constexpr int kMaxK = 288;       // largest tile K (period) the shared memory holds
 constexpr int kStageLd = 36;     // epilogue staging row stride (floats): 16-B aligned, conflict-free
 constexpr int kSpanRegs = 5;     // x values per producer thread: (kMaxK + kN + 8) / 128 rounded up
 constexpr uint32_t kTmemCols = 512;
@@ -225,13 +226,13 @@ struct __align__(16) SmemCtl {
     uint64_t a_full;
     uint64_t mma_done[2];
     uint64_t acc_empty[2];
-    uint64_t params_full[2];
+    uint64_t params_full[4];  // per-tile parameters: a ring of 4 slots
     uint32_t tmem_base;
     int abort_flag;
     int stop;
     int issued;  // tiles whose MMAs were committed
-    float ref[2];
-    float xscale[2];  // 2^-e_x
+    float ref[4];
+    float xscale[4];  // 2^-e_x
     float red[8];
 };
 
@@ -259,8 +260,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
     p += lin_bytes;
     uint16_t* lin_lo = reinterpret_cast<uint16_t*>(p);
     p += lin_bytes;
-    float* stage = reinterpret_cast<float*>(p);  // [4 epilogue warps][32][kStageLd]
-    p += (size_t)4 * 32 * kStageLd * sizeof(float);
+    float* stage = reinterpret_cast<float*>(p);  // [8 epilogue warps][32][kStageLd]
+    p += (size_t)8 * 32 * kStageLd * sizeof(float);
     SmemCtl* ctl = reinterpret_cast<SmemCtl*>(p);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -274,9 +275,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
         mbar_init(&ctl->a_full, 1);
         for (int b = 0; b < 2; ++b) {
             mbar_init(&ctl->mma_done[b], 1);
-            mbar_init(&ctl->acc_empty[b], kThreads / 2);
-            mbar_init(&ctl->params_full[b], 1);
+            mbar_init(&ctl->acc_empty[b], kEpiThreads);
         }
+        for (int b = 0; b < 4; ++b) mbar_init(&ctl->params_full[b], 1);
         ctl->abort_flag = 0;
         ctl->stop = 0;
         ctl->issued = 0;
@@ -321,13 +322,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
             const int t0 = (tile_begin + i) * kN;
             const int base = t0 - K + 1;
             if (tid == 0) {
-                // buffer b (strip, tile parameters, TMEM columns) is free once the
-                // MMAs of tile i-2 completed and its epilogue released it
+                // strip b is free once the MMAs of tile i-2 completed (the TMEM
+                // columns are reclaimed from the epilogue just before the MMA issue)
                 bool ok = true;
-                if (i >= 2) {
-                    ok = mbar_wait(&ctl->mma_done[b], ((i >> 1) - 1) & 1, abort_flag) &&
-                         mbar_wait(&ctl->acc_empty[b], ((i >> 1) - 1) & 1, abort_flag);
-                }
+                if (i >= 2) ok = mbar_wait(&ctl->mma_done[b], ((i >> 1) - 1) & 1, abort_flag);
                 if (!ok) ctl->abort_flag = 1;
                 ctl->stop = ctl->abort_flag;
             }
@@ -403,15 +401,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
                 reinterpret_cast<uint4*>(strip_lo[b])[q] = ol;
             }
             if (tid == 0) {
-                ctl->ref[b] = ref;
-                ctl->xscale[b] = ldexpf(1.f, -ex);
+                ctl->ref[i & 3] = ref;
+                ctl->xscale[i & 3] = ldexpf(1.f, -ex);
             }
             // generic-proxy smem writes -> visible to the tensor core (async proxy)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("bar.sync 1, 128;" ::: "memory");
             if (tid == 0) {
-                mbar_arrive(&ctl->params_full[b]);
-                const bool ok = (i > 0) || mbar_wait(&ctl->a_full, 0, abort_flag);
+                mbar_arrive(&ctl->params_full[i & 3]);
+                bool ok = (i > 0) || mbar_wait(&ctl->a_full, 0, abort_flag);
+                if (ok && i >= 2) ok = mbar_wait(&ctl->acc_empty[b], ((i >> 1) - 1) & 1, abort_flag);
                 if (!ok) {
                     ctl->abort_flag = 1;
                 } else {
@@ -436,18 +435,22 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
             }
         }
     } else {
-        // ================= epilogue warpgroup ================================
+        // ================= epilogue warpgroups ===============================
+        // warp w (4..11): TMEM lane quarter q4 = w % 4 (the combo rows it may
+        // read), column half (w - 4) / 4 of the 256 times of a tile.
         const int q4 = warp & 3;
+        const int half = (warp - 4) >> 2;
         const int r = q4 * 32 + lane;  // accumulator row = combo within tile
         const int c = m * kM + r;
         const bool row_ok = c < a.n_combos;
-        (void)row_ok;
         const int p = row_ok ? a.periods[c] : 1;
         const int warm = a.first + p - 1;
         const float rscale = a.row_scale[(size_t)m * kM + r];
         const float rsum = a.row_sum[(size_t)m * kM + r];
         const bool vec_ok = (a.n & 3) == 0;
         const bool has_nan = a.nanp != nullptr && a.nanp[a.n - 1] > 0.5;
+        float* st = stage + (size_t)(warp - 4) * 32 * kStageLd;
+        const int rbase = m * kM + q4 * 32;  // first combo of this warp's rows
         for (int i = 0; i < ntiles; ++i) {
             const int b = i & 1;
             const int t0 = (tile_begin + i) * kN;
@@ -455,36 +458,42 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
             int ok = 1;
             if (lane == 0) {
                 ok = mbar_wait(&ctl->mma_done[b], (i >> 1) & 1, abort_flag) &&
-                     mbar_wait(&ctl->params_full[b], (i >> 1) & 1, abort_flag);
+                     mbar_wait(&ctl->params_full[i & 3], (i >> 2) & 1, abort_flag);
                 if (!ok) ctl->abort_flag = 1;
             }
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) break;
+            __syncwarp();  // orders lane 0's acquire before the other lanes' reads
             tc_fence_after();
-            const float ref = ctl->ref[b];
-            const float scale = rscale * ctl->xscale[b];
+            const float ref = ctl->ref[i & 3];
+            const float scale = rscale * ctl->xscale[i & 3];
             const float off = ref * rsum;
-            float* st = stage + (size_t)q4 * 32 * kStageLd;
-            const int rbase = m * kM + q4 * 32;  // first combo of this warp's rows
-            for (int cb = 0; cb < kN; cb += 32) {
-                uint32_t v[32];
-                const uint32_t taddr = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * kN + cb);
-                TC_LD32(taddr, v);
+            // tiles past every row's warm-up with a NaN-free series need no masks
+            const bool plain = !has_nan && __all_sync(0xffffffffu, t0 >= warm);
+            const uint32_t tbase = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * kN + half * 128);
+            uint32_t v[2][32];
+            TC_LD32(tbase, v[0]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                // this thread's row (combo c), 32 consecutive times -> staging row
+                if (k + 1 < 4) TC_LD32(tbase + (uint32_t)((k + 1) * 32), v[(k + 1) & 1]);
+                const uint32_t* vk = v[k & 1];
+                const int cb = half * 128 + k * 32;
 #pragma unroll
                 for (int j4 = 0; j4 < 8; ++j4) {
                     float y4[4];
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
                         const int j = 4 * j4 + u;
-                        const int t = t0 + cb + j;
-                        float val = fmaf(__uint_as_float(v[j]), scale, off);
-                        if (t < warm) val = qnan();
-                        else if (has_nan && t < a.n) {
-                            const double hi = a.nanp[t];
-                            const double lo = (a.nan_mode == 0 && t - p >= 0) ? a.nanp[t - p] : 0.0;
-                            if (hi - lo > 0.5) val = qnan();
+                        float val = fmaf(__uint_as_float(vk[j]), scale, off);
+                        if (!plain) {
+                            const int t = t0 + cb + j;
+                            if (t < warm) val = qnan();
+                            else if (has_nan && t < a.n) {
+                                const double hi = a.nanp[t];
+                                const double lo = (a.nan_mode == 0 && t - p >= 0) ? a.nanp[t - p] : 0.0;
+                                if (hi - lo > 0.5) val = qnan();
+                            }
                         }
                         y4[u] = val;
                     }
@@ -495,8 +504,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
                 const int c4 = lane & 7;
                 const int tcol = t0 + cb + 4 * c4;
 #pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    const int rr = 4 * k + (lane >> 3);
+                for (int kk = 0; kk < 8; ++kk) {
+                    const int rr = 4 * kk + (lane >> 3);
                     const int cr = rbase + rr;
                     if (cr < a.n_combos) {
                         const float4 y = *reinterpret_cast<const float4*>(st + rr * kStageLd + 4 * c4);
@@ -542,7 +551,7 @@ size_t smem_bytes_for(int K) {
     const int J = K / 8 + kN / 8 - 1;
     const int span = K + kN + 8;
     return (size_t)kM * K * 2 * 2 + 4 * (size_t)J * 8 * 16 + 2 * (size_t)(((span + 15) & ~15) * 2) +
-           (size_t)4 * 32 * kStageLd * sizeof(float) + sizeof(SmemCtl) + 128;
+           (size_t)8 * 32 * kStageLd * sizeof(float) + sizeof(SmemCtl) + 128;
 }
 
 }  // namespace
