@@ -28,8 +28,15 @@
 // centring, warm-up / NaN masks and stores.  mbarriers hand buffers back and
 // forth; every wait is bounded by a time limit after which the kernel records
 // an error code, stops issuing work, drains its own MMAs and frees TMEM.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
 
 #include "vta_internal.h"
 
@@ -41,7 +48,8 @@ constexpr int kN = 256;          // times per tile (MMA N)
 constexpr int kThreads = 384;     // warpgroup 0: producer + MMA; warpgroups 1-2: epilogue
 constexpr int kEpiThreads = 256;
 constexpr int kMaxK = 288;       // largest tile K (period) the shared memory holds
-constexpr int kStageLd = 36;     // epilogue staging row stride (floats): 16-B aligned, conflict-free
+constexpr int kStageLd = 36;     // epilogue staging row stride (floats) of the st.global path
+constexpr int kStageTma = 32 * 32 * 4;  // epilogue staging per warp for a TMA store (bytes)
 constexpr int kSpanRegs = 5;     // x values per producer thread: (kMaxK + kN + 8) / 128 rounded up
 constexpr uint32_t kTmemCols = 512;
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
@@ -220,7 +228,12 @@ struct TcArgs {
     float* out;
     int tiles_per_chunk;  // time tiles per CTA
     int* err;             // error word (0 = ok)
+    unsigned long long* trace;  // optional pipeline trace of CTA (0, 0): [tile][event]
 };
+// trace events per tile (globaltimer ns)
+enum { TR_P_START = 0, TR_P_X = 1, TR_P_STRIP = 2, TR_P_ACC = 3, TR_P_ISSUED = 4, TR_E_START = 5,
+       TR_E_END = 6, TR_N = 8 };
+constexpr int kTraceTiles = 64;
 
 struct __align__(16) SmemCtl {
     uint64_t a_full;
@@ -236,8 +249,8 @@ struct __align__(16) SmemCtl {
     float red[8];
 };
 
-template <int VARIANT>
-__global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
+template <int VARIANT, bool TMA_STORE>
+__global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_constant__ CUtensorMap tmap_out) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     const int m = blockIdx.y;
     const int K = a.tile_k[m];
@@ -260,7 +273,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
     p += lin_bytes;
     uint16_t* lin_lo = reinterpret_cast<uint16_t*>(p);
     p += lin_bytes;
-    float* stage = reinterpret_cast<float*>(p);  // [8 epilogue warps][32][kStageLd]
+    p = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
+    float* stage = reinterpret_cast<float*>(p);  // [8 epilogue warps][32][kStageLd] or [8][4 KB swizzled]
     p += (size_t)8 * 32 * kStageLd * sizeof(float);
     SmemCtl* ctl = reinterpret_cast<SmemCtl*>(p);
 
@@ -326,6 +340,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
                 // columns are reclaimed from the epilogue just before the MMA issue)
                 bool ok = true;
                 if (i >= 2) ok = mbar_wait(&ctl->mma_done[b], ((i >> 1) - 1) & 1, abort_flag);
+                if (a.trace && blockIdx.x == 0 && blockIdx.y == 0 && i < kTraceTiles)
+                    a.trace[i * TR_N + TR_P_START] = now_ns();
                 if (!ok) ctl->abort_flag = 1;
                 ctl->stop = ctl->abort_flag;
             }
@@ -350,6 +366,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
                 xv[k] = v;
             }
             const float ref = isfinite(vref) ? vref : 0.f;
+            if (a.trace && tid == 0 && blockIdx.x == 0 && blockIdx.y == 0 && i < kTraceTiles)
+                a.trace[i * TR_N + TR_P_X] = now_ns();
             float mx = 0.f;
 #pragma unroll
             for (int k = 0; k < kSpanRegs; ++k)
@@ -408,9 +426,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("bar.sync 1, 128;" ::: "memory");
             if (tid == 0) {
+                const bool tr = a.trace && blockIdx.x == 0 && blockIdx.y == 0 && i < kTraceTiles;
+                if (tr) a.trace[i * TR_N + TR_P_STRIP] = now_ns();
                 mbar_arrive(&ctl->params_full[i & 3]);
                 bool ok = (i > 0) || mbar_wait(&ctl->a_full, 0, abort_flag);
                 if (ok && i >= 2) ok = mbar_wait(&ctl->acc_empty[b], ((i >> 1) - 1) & 1, abort_flag);
+                if (tr) a.trace[i * TR_N + TR_P_ACC] = now_ns();
                 if (!ok) {
                     ctl->abort_flag = 1;
                 } else {
@@ -431,6 +452,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
                     }
                     tc_commit(&ctl->mma_done[b]);
                     ctl->issued = i + 1;
+                    if (tr) a.trace[i * TR_N + TR_P_ISSUED] = now_ns();
                 }
             }
         }
@@ -449,7 +471,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
         const float rsum = a.row_sum[(size_t)m * kM + r];
         const bool vec_ok = (a.n & 3) == 0;
         const bool has_nan = a.nanp != nullptr && a.nanp[a.n - 1] > 0.5;
-        float* st = stage + (size_t)(warp - 4) * 32 * kStageLd;
+        float* st = TMA_STORE ? reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(stage) + (size_t)(warp - 4) * kStageTma)
+                              : stage + (size_t)(warp - 4) * 32 * kStageLd;
         const int rbase = m * kM + q4 * 32;  // first combo of this warp's rows
         for (int i = 0; i < ntiles; ++i) {
             const int b = i & 1;
@@ -464,6 +487,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) break;
             __syncwarp();  // orders lane 0's acquire before the other lanes' reads
+            const bool tr = a.trace && warp == 4 && lane == 0 && blockIdx.x == 0 && blockIdx.y == 0 &&
+                            i < kTraceTiles;
+            if (tr) a.trace[i * TR_N + TR_E_START] = now_ns();
             tc_fence_after();
             const float ref = ctl->ref[i & 3];
             const float scale = rscale * ctl->xscale[i & 3];
@@ -497,36 +523,63 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a) {
                         }
                         y4[u] = val;
                     }
-                    *reinterpret_cast<float4*>(st + lane * kStageLd + 4 * j4) = make_float4(y4[0], y4[1], y4[2], y4[3]);
-                }
-                __syncwarp();
-                // 8 lanes per row: each store instruction writes 4 rows x 128 B
-                const int c4 = lane & 7;
-                const int tcol = t0 + cb + 4 * c4;
-#pragma unroll
-                for (int kk = 0; kk < 8; ++kk) {
-                    const int rr = 4 * kk + (lane >> 3);
-                    const int cr = rbase + rr;
-                    if (cr < a.n_combos) {
-                        const float4 y = *reinterpret_cast<const float4*>(st + rr * kStageLd + 4 * c4);
-                        float* o = a.out + (size_t)cr * a.n + tcol;
-                        if (vec_ok && tcol + 4 <= a.n) {
-                            *reinterpret_cast<float4*>(o) = y;
-                        } else {
-                            if (tcol < a.n) o[0] = y.x;
-                            if (tcol + 1 < a.n) o[1] = y.y;
-                            if (tcol + 2 < a.n) o[2] = y.z;
-                            if (tcol + 3 < a.n) o[3] = y.w;
-                        }
+                    if constexpr (TMA_STORE) {
+                        // 128-byte swizzle: 16-byte chunk j4 of row `lane` goes to chunk j4 ^ (lane & 7)
+                        uint8_t* st8 = reinterpret_cast<uint8_t*>(st);
+                        *reinterpret_cast<float4*>(st8 + lane * 128 + ((j4 ^ (lane & 7)) << 4)) =
+                            make_float4(y4[0], y4[1], y4[2], y4[3]);
+                    } else {
+                        *reinterpret_cast<float4*>(st + lane * kStageLd + 4 * j4) =
+                            make_float4(y4[0], y4[1], y4[2], y4[3]);
                     }
                 }
-                __syncwarp();
+                if constexpr (TMA_STORE) {
+                    // the TMA engine writes the 32 x 32 block (clipping rows / times past the ends)
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) {
+                        asm volatile(
+                            "cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                                reinterpret_cast<uint64_t>(&tmap_out)),
+                            "r"(t0 + cb), "r"(rbase), "r"(smem_u32(st))
+                            : "memory");
+                        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                        // the staging block is rewritten for the next chunk: wait until read
+                        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                    }
+                    __syncwarp();
+                } else {
+                    __syncwarp();
+                    // 8 lanes per row: each store instruction writes 4 rows x 128 B
+                    const int c4 = lane & 7;
+                    const int tcol = t0 + cb + 4 * c4;
+#pragma unroll
+                    for (int kk = 0; kk < 8; ++kk) {
+                        const int rr = 4 * kk + (lane >> 3);
+                        const int cr = rbase + rr;
+                        if (cr < a.n_combos) {
+                            const float4 y = *reinterpret_cast<const float4*>(st + rr * kStageLd + 4 * c4);
+                            float* o = a.out + (size_t)cr * a.n + tcol;
+                            if (vec_ok && tcol + 4 <= a.n) {
+                                *reinterpret_cast<float4*>(o) = y;
+                            } else {
+                                if (tcol < a.n) o[0] = y.x;
+                                if (tcol + 1 < a.n) o[1] = y.y;
+                                if (tcol + 2 < a.n) o[2] = y.z;
+                                if (tcol + 3 < a.n) o[3] = y.w;
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
             }
             tc_fence_before();
             mbar_arrive(&ctl->acc_empty[b]);
+            if (tr) a.trace[i * TR_N + TR_E_END] = now_ns();
         }
     }
 
+    if (TMA_STORE && warp >= 4 && lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     // drain: the last committed MMAs must have completed before TMEM is freed
     __syncthreads();
     if (tid == 0) {
@@ -551,7 +604,7 @@ size_t smem_bytes_for(int K) {
     const int J = K / 8 + kN / 8 - 1;
     const int span = K + kN + 8;
     return (size_t)kM * K * 2 * 2 + 4 * (size_t)J * 8 * 16 + 2 * (size_t)(((span + 15) & ~15) * 2) +
-           (size_t)8 * 32 * kStageLd * sizeof(float) + sizeof(SmemCtl) + 128;
+           (size_t)8 * 32 * kStageLd * sizeof(float) + 1024 + sizeof(SmemCtl) + 128;
 }
 
 }  // namespace
@@ -619,6 +672,13 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
     t.nanp = a.nanp;
     t.out = a.out;
     t.err = d_err;
+    unsigned long long* d_trace = nullptr;
+    const char* tr_env = std::getenv("VTA_TC_TRACE");
+    if (tr_env && tr_env[0] == '1') {
+        VTA_CUDA_TRY(cudaMallocAsync((void**)&d_trace, kTraceTiles * TR_N * 8, st));
+        VTA_CUDA_TRY(cudaMemsetAsync(d_trace, 0, kTraceTiles * TR_N * 8, st));
+    }
+    t.trace = d_trace;
     const int n_time_tiles = (a.n + kN - 1) / kN;
     const int target = ctx->num_sms * 6;
     int chunks = std::max(1, std::min(n_time_tiles, (target + n_tiles_m - 1) / n_tiles_m));
@@ -626,16 +686,51 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
     chunks = (n_time_tiles + t.tiles_per_chunk - 1) / t.tiles_per_chunk;
     dim3 grid(chunks, n_tiles_m);
     if (n_tiles_m > 65535) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "tcgen05 path: too many combo tiles");
-    auto kern = variant == 1 ? k_wwma_tc<1> : k_wwma_tc<0>;
+    // TMA store path when rows are 16-byte aligned (len % 4 == 0); st.global otherwise
+    CUtensorMap tmap;
+    std::memset(&tmap, 0, sizeof tmap);
+    bool use_tma = (a.n % 4) == 0 && (reinterpret_cast<uintptr_t>(a.out) & 15) == 0;
+    if (use_tma) {
+        static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+        if (!encode) {
+            cudaDriverEntryPointQueryResult q;
+            void* fn = nullptr;
+            if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                    cudaSuccess && q == cudaDriverEntryPointSuccess)
+                encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+            cudaGetLastError();
+        }
+        const cuuint64_t dims[2] = {(cuuint64_t)a.n, (cuuint64_t)a.n_combos};
+        const cuuint64_t strides[1] = {(cuuint64_t)a.n * sizeof(float)};
+        const cuuint32_t box[2] = {32, 32};
+        const cuuint32_t estr[2] = {1, 1};
+        use_tma = encode && encode(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, a.out, dims, strides, box, estr,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                   CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    }
+    auto kern = variant == 1 ? (use_tma ? k_wwma_tc<1, true> : k_wwma_tc<1, false>)
+                             : (use_tma ? k_wwma_tc<0, true> : k_wwma_tc<0, false>);
     VTA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     ktimer_begin(st);
-    kern<<<grid, kThreads, smem, st>>>(t);
+    kern<<<grid, kThreads, smem, st>>>(t, tmap);
     ktimer_end(st);
     VTA_TRY(check_launch("k_wwma_tc"));
     int err = 0;
     VTA_CUDA_TRY(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     VTA_CUDA_TRY(cudaStreamSynchronize(st));
     cudaFreeAsync(buf, st);
+    if (d_trace) {
+        std::vector<unsigned long long> h(kTraceTiles * TR_N);
+        cudaMemcpy(h.data(), d_trace, h.size() * 8, cudaMemcpyDeviceToHost);
+        cudaFree(d_trace);
+        const unsigned long long t0 = h[0];
+        std::fprintf(stderr, "tc trace (ns from first tile start): tile p_start p_x p_strip p_acc p_issued e_start e_end\n");
+        for (int i = 0; i < std::min(kTraceTiles, t.tiles_per_chunk); ++i) {
+            std::fprintf(stderr, "%3d", i);
+            for (int e = 0; e < 7; ++e) std::fprintf(stderr, " %8lld", h[i * TR_N + e] ? (long long)(h[i * TR_N + e] - t0) : -1LL);
+            std::fprintf(stderr, "\n");
+        }
+    }
     if (err) return fail(VTA_ERR_CUDA, "tcgen05 contraction: pipeline wait timed out");
     return VTA_OK;
 }
