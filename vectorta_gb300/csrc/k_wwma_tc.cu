@@ -212,6 +212,26 @@ __global__ void k_pack_a(PackArgs a) {
     }
 }
 
+// Warm-up / NaN masks of one staged row of 32 consecutive outputs (tiles that
+// need them are few; kept out of line so the hot epilogue loop stays small).
+// `swz` selects the 128-byte-swizzled staging layout of the TMA store path.
+__device__ __noinline__ void mask_staged(float* row, bool swz, int lane, int tb, int warm, int p, bool has_nan,
+                                         int n, int nan_mode, const double* nanp) {
+    for (int j = 0; j < 32; ++j) {
+        const int t = tb + j;
+        bool bad = t < warm;
+        if (!bad && has_nan && t < n) {
+            const double hi = nanp[t];
+            const double lo = (nan_mode == 0 && t - p >= 0) ? nanp[t - p] : 0.0;
+            bad = hi - lo > 0.5;
+        }
+        if (bad) {
+            const int pos = swz ? ((((j >> 2) ^ (lane & 7)) << 2) | (j & 3)) : j;
+            row[pos] = qnan();
+        }
+    }
+}
+
 // ------------------------------------------------------------ main kernel -
 struct TcArgs {
     const float* x;
@@ -497,43 +517,25 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
             // tiles past every row's warm-up with a NaN-free series need no masks
             const bool plain = !has_nan && __all_sync(0xffffffffu, t0 >= warm);
             const uint32_t tbase = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * kN + half * 128);
-            uint32_t v[2][32];
-            TC_LD32(tbase, v[0]);
-#pragma unroll
+#pragma unroll 1
             for (int k = 0; k < 4; ++k) {
+                uint32_t v[32];
+                TC_LD32(tbase + (uint32_t)(k * 32), v);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (k + 1 < 4) TC_LD32(tbase + (uint32_t)((k + 1) * 32), v[(k + 1) & 1]);
-                const uint32_t* vk = v[k & 1];
                 const int cb = half * 128 + k * 32;
+                float y[32];
 #pragma unroll
-                for (int j4 = 0; j4 < 8; ++j4) {
-                    float y4[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int j = 4 * j4 + u;
-                        float val = fmaf(__uint_as_float(vk[j]), scale, off);
-                        if (!plain) {
-                            const int t = t0 + cb + j;
-                            if (t < warm) val = qnan();
-                            else if (has_nan && t < a.n) {
-                                const double hi = a.nanp[t];
-                                const double lo = (a.nan_mode == 0 && t - p >= 0) ? a.nanp[t - p] : 0.0;
-                                if (hi - lo > 0.5) val = qnan();
-                            }
-                        }
-                        y4[u] = val;
-                    }
-                    if constexpr (TMA_STORE) {
-                        // 128-byte swizzle: 16-byte chunk j4 of row `lane` goes to chunk j4 ^ (lane & 7)
-                        uint8_t* st8 = reinterpret_cast<uint8_t*>(st);
-                        *reinterpret_cast<float4*>(st8 + lane * 128 + ((j4 ^ (lane & 7)) << 4)) =
-                            make_float4(y4[0], y4[1], y4[2], y4[3]);
-                    } else {
-                        *reinterpret_cast<float4*>(st + lane * kStageLd + 4 * j4) =
-                            make_float4(y4[0], y4[1], y4[2], y4[3]);
-                    }
-                }
+                for (int j = 0; j < 32; ++j) y[j] = fmaf(__uint_as_float(v[j]), scale, off);
                 if constexpr (TMA_STORE) {
+                    // 128-byte swizzle: 16-byte chunk j4 of row `lane` goes to chunk j4 ^ (lane & 7)
+                    uint8_t* row8 = reinterpret_cast<uint8_t*>(st) + lane * 128;
+#pragma unroll
+                    for (int j4 = 0; j4 < 8; ++j4)
+                        *reinterpret_cast<float4*>(row8 + ((j4 ^ (lane & 7)) << 4)) =
+                            make_float4(y[4 * j4], y[4 * j4 + 1], y[4 * j4 + 2], y[4 * j4 + 3]);
+                    if (!plain)
+                        mask_staged(reinterpret_cast<float*>(row8), true, lane, t0 + cb, warm, p, has_nan, a.n,
+                                    a.nan_mode, a.nanp);
                     // the TMA engine writes the 32 x 32 block (clipping rows / times past the ends)
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     __syncwarp();
@@ -549,6 +551,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
                     }
                     __syncwarp();
                 } else {
+#pragma unroll
+                    for (int j4 = 0; j4 < 8; ++j4)
+                        *reinterpret_cast<float4*>(st + lane * kStageLd + 4 * j4) =
+                            make_float4(y[4 * j4], y[4 * j4 + 1], y[4 * j4 + 2], y[4 * j4 + 3]);
+                    if (!plain)
+                        mask_staged(st + lane * kStageLd, false, lane, t0 + cb, warm, p, has_nan, a.n, a.nan_mode,
+                                    a.nanp);
                     __syncwarp();
                     // 8 lanes per row: each store instruction writes 4 rows x 128 B
                     const int c4 = lane & 7;
@@ -558,15 +567,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
                         const int rr = 4 * kk + (lane >> 3);
                         const int cr = rbase + rr;
                         if (cr < a.n_combos) {
-                            const float4 y = *reinterpret_cast<const float4*>(st + rr * kStageLd + 4 * c4);
+                            const float4 yv = *reinterpret_cast<const float4*>(st + rr * kStageLd + 4 * c4);
                             float* o = a.out + (size_t)cr * a.n + tcol;
                             if (vec_ok && tcol + 4 <= a.n) {
-                                *reinterpret_cast<float4*>(o) = y;
+                                *reinterpret_cast<float4*>(o) = yv;
                             } else {
-                                if (tcol < a.n) o[0] = y.x;
-                                if (tcol + 1 < a.n) o[1] = y.y;
-                                if (tcol + 2 < a.n) o[2] = y.z;
-                                if (tcol + 3 < a.n) o[3] = y.w;
+                                if (tcol < a.n) o[0] = yv.x;
+                                if (tcol + 1 < a.n) o[1] = yv.y;
+                                if (tcol + 2 < a.n) o[2] = yv.z;
+                                if (tcol + 3 < a.n) o[3] = yv.w;
                             }
                         }
                     }
