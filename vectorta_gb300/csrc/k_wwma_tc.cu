@@ -45,12 +45,11 @@ namespace {
 
 constexpr int kM = 128;          // combos per tile (MMA M)
 constexpr int kN = 256;          // times per tile (MMA N)
-constexpr int kThreads = 384;     // warpgroup 0: producer + MMA; warpgroups 1-2: epilogue
+constexpr int kThreads = 288;     // warp 0: TMA + MMA issue; warps 1-8: epilogue
 constexpr int kEpiThreads = 256;
-constexpr int kMaxK = 288;       // largest tile K (period) the shared memory holds
+constexpr int kMaxK = 272;       // largest tile K (period) the shared memory holds
 constexpr int kStageLd = 36;     // epilogue staging row stride (floats) of the st.global path
 constexpr int kStageTma = 32 * 32 * 4;  // epilogue staging per warp for a TMA store (bytes)
-constexpr int kSpanRegs = 5;     // x values per producer thread: (kMaxK + kN + 8) / 128 rounded up
 constexpr uint32_t kTmemCols = 512;
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 
@@ -232,9 +231,94 @@ __device__ __noinline__ void mask_staged(float* row, bool swz, int lane, int tb,
     }
 }
 
+// ------------------------------------------------------------ B strips ----
+// One expanded Hankel strip per 256-wide time tile, built once for the largest
+// tile K (Kmax) and shared by every combo tile: E[q] = lin[q .. q+7] (16 bytes)
+// with lin[i] = split((x[base + i] - r) * 2^e_x), base = t0 - Kmax + 1.  A
+// combo tile with K < Kmax uses the same strip from block (Kmax - K) on.
+struct StripArgs {
+    const float* x;
+    int n, first;
+    int kmax;
+    int jmax;                 // strip blocks of 8 shifts: Kmax/8 + 31
+    uint8_t* strips_hi;       // [n_time_tiles][jmax * 8 * 16]
+    uint8_t* strips_lo;
+    float* ref;               // [n_time_tiles] centring value r
+    float* xscale;            // [n_time_tiles] 2^-e_x
+};
+
+template <int VARIANT>
+__global__ void __launch_bounds__(128) k_hankel_strips(StripArgs a) {
+    extern __shared__ uint8_t sm[];
+    const int g = blockIdx.x;
+    const int t0 = g * kN;
+    const int base = t0 - a.kmax + 1;
+    const int L = a.jmax * 8 + 8;  // linear values needed
+    float* xf = reinterpret_cast<float*>(sm);
+    uint16_t* lh = reinterpret_cast<uint16_t*>(xf + L);
+    uint16_t* ll = lh + ((L + 7) & ~7);
+    __shared__ float red[4];
+    const int gref = min(t0 + kN - 1, a.n - 1);
+    const float vref = (gref >= a.first && gref >= 0) ? a.x[gref] : 0.f;
+    const float ref = isfinite(vref) ? vref : 0.f;
+    float mx = 0.f;
+    for (int q = threadIdx.x; q < L; q += 128) {
+        const int gi = base + q;
+        float v = __int_as_float(0x7fc00000);  // outside the series / not finite: zero after centring
+        if (gi >= a.first && gi < a.n) {
+            const float u = a.x[gi];
+            if (isfinite(u)) v = u;
+        }
+        xf[q] = v;
+        if (!isnan(v)) mx = fmaxf(mx, fabsf(v - ref));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    mx = fmaxf(fmaxf(red[0], red[1]), fmaxf(red[2], red[3]));
+    int ex = 0;
+    if (mx > 0.f) {
+        int e2;
+        frexpf(mx, &e2);
+        ex = 13 - e2;
+    }
+    const float sc = ldexpf(1.f, ex);
+    for (int q = threadIdx.x; q < L; q += 128) {
+        const float v = isnan(xf[q]) ? 0.f : (xf[q] - ref) * sc;
+        uint16_t h, l;
+        Split<VARIANT>::run(v, h, l);
+        lh[q] = h;
+        ll[q] = l;
+    }
+    if (threadIdx.x == 0) {
+        a.ref[g] = ref;
+        a.xscale[g] = ldexpf(1.f, -ex);
+    }
+    __syncthreads();
+    const uint32_t* wh = reinterpret_cast<const uint32_t*>(lh);
+    const uint32_t* wl = reinterpret_cast<const uint32_t*>(ll);
+    uint4* oh = reinterpret_cast<uint4*>(a.strips_hi + (size_t)g * a.jmax * 128);
+    uint4* ol = reinterpret_cast<uint4*>(a.strips_lo + (size_t)g * a.jmax * 128);
+    for (int q = threadIdx.x; q < a.jmax * 8; q += 128) {
+        const int w0 = q >> 1;
+        uint4 h4, l4;
+        if (q & 1) {
+            h4 = make_uint4(__byte_perm(wh[w0], wh[w0 + 1], 0x5432), __byte_perm(wh[w0 + 1], wh[w0 + 2], 0x5432),
+                            __byte_perm(wh[w0 + 2], wh[w0 + 3], 0x5432), __byte_perm(wh[w0 + 3], wh[w0 + 4], 0x5432));
+            l4 = make_uint4(__byte_perm(wl[w0], wl[w0 + 1], 0x5432), __byte_perm(wl[w0 + 1], wl[w0 + 2], 0x5432),
+                            __byte_perm(wl[w0 + 2], wl[w0 + 3], 0x5432), __byte_perm(wl[w0 + 3], wl[w0 + 4], 0x5432));
+        } else {
+            h4 = make_uint4(wh[w0], wh[w0 + 1], wh[w0 + 2], wh[w0 + 3]);
+            l4 = make_uint4(wl[w0], wl[w0 + 1], wl[w0 + 2], wl[w0 + 3]);
+        }
+        oh[q] = h4;
+        ol[q] = l4;
+    }
+}
+
 // ------------------------------------------------------------ main kernel -
 struct TcArgs {
-    const float* x;
     int n, first;
     const int* periods;
     int n_combos;
@@ -243,6 +327,11 @@ struct TcArgs {
     const uint16_t* packed;
     const float* row_scale;
     const float* row_sum;
+    int kmax, jmax;
+    const uint8_t* strips_hi;
+    const uint8_t* strips_lo;
+    const float* ref;
+    const float* xscale;
     int nan_mode;
     const double* nanp;
     float* out;
@@ -251,48 +340,44 @@ struct TcArgs {
     unsigned long long* trace;  // optional pipeline trace of CTA (0, 0): [tile][event]
 };
 // trace events per tile (globaltimer ns)
-enum { TR_P_START = 0, TR_P_X = 1, TR_P_STRIP = 2, TR_P_ACC = 3, TR_P_ISSUED = 4, TR_E_START = 5,
-       TR_E_END = 6, TR_N = 8 };
+enum { TR_P_STRIP = 0, TR_P_ACC = 1, TR_P_ISSUED = 2, TR_E_START = 3, TR_E_END = 4, TR_N = 8 };
 constexpr int kTraceTiles = 64;
 
 struct __align__(16) SmemCtl {
     uint64_t a_full;
+    uint64_t strip_full[2];
     uint64_t mma_done[2];
     uint64_t acc_empty[2];
-    uint64_t params_full[4];  // per-tile parameters: a ring of 4 slots
     uint32_t tmem_base;
     int abort_flag;
-    int stop;
     int issued;  // tiles whose MMAs were committed
-    float ref[4];
-    float xscale[4];  // 2^-e_x
-    float red[8];
 };
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
 
 template <int VARIANT, bool TMA_STORE>
 __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_constant__ CUtensorMap tmap_out) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     const int m = blockIdx.y;
     const int K = a.tile_k[m];
-    const int KC = K >> 3;                 // 8-column chunks
-    const int J = KC + (kN >> 3) - 1;      // strip blocks of 8 shifts
-    const int span = K + kN + 8;           // linear x values per tile (with slack)
-    // layout: A hi | A lo | strip[2] hi | strip[2] lo | linear[2] hi/lo | ctl
+    const int J = K / 8 + kN / 8 - 1;  // strip blocks this tile reads
+    const uint32_t strip_bytes = (uint32_t)J * 128;
+    const size_t strip_off = (size_t)(a.kmax - K) * 16;  // into the Kmax strip
+    // layout: A hi | A lo | strip[2] hi | strip[2] lo | staging (1024-aligned) | ctl
     uint8_t* p = smem_raw;
     uint16_t* a_hi = reinterpret_cast<uint16_t*>(p);
     p += (size_t)kM * K * 2;
     uint16_t* a_lo = reinterpret_cast<uint16_t*>(p);
     p += (size_t)kM * K * 2;
-    const size_t strip_bytes = (size_t)J * 8 * 16;
     uint8_t* strip_hi[2] = {p, p + strip_bytes};
-    p += 2 * strip_bytes;
+    p += 2 * (size_t)strip_bytes;
     uint8_t* strip_lo[2] = {p, p + strip_bytes};
-    p += 2 * strip_bytes;
-    const size_t lin_bytes = (size_t)((span + 15) & ~15) * 2;
-    uint16_t* lin_hi = reinterpret_cast<uint16_t*>(p);
-    p += lin_bytes;
-    uint16_t* lin_lo = reinterpret_cast<uint16_t*>(p);
-    p += lin_bytes;
+    p += 2 * (size_t)strip_bytes;
     p = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
     float* stage = reinterpret_cast<float*>(p);  // [8 epilogue warps][32][kStageLd] or [8][4 KB swizzled]
     p += (size_t)8 * 32 * kStageLd * sizeof(float);
@@ -304,16 +389,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
     const int tile_end = min(tile_begin + a.tiles_per_chunk, n_time_tiles);
     const int ntiles = tile_end - tile_begin;
     volatile int* abort_flag = &ctl->abort_flag;
+    const bool tracing = a.trace != nullptr && blockIdx.x == 0 && blockIdx.y == 0;
 
     if (tid == 0) {
         mbar_init(&ctl->a_full, 1);
         for (int b = 0; b < 2; ++b) {
+            mbar_init(&ctl->strip_full[b], 1);
             mbar_init(&ctl->mma_done[b], 1);
             mbar_init(&ctl->acc_empty[b], kEpiThreads);
         }
-        for (int b = 0; b < 4; ++b) mbar_init(&ctl->params_full[b], 1);
         ctl->abort_flag = 0;
-        ctl->stop = 0;
         ctl->issued = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -329,159 +414,63 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
     tc_fence_after();
     const uint32_t tmem = ctl->tmem_base;
 
-    if (tid == 0 && ntiles > 0) {
-        // A tile -> shared memory with two bulk copies completing on a_full
-        const uint32_t bytes = (uint32_t)kM * K * 2;
-        const uint16_t* src = a.packed + a.tile_off[m];
-        mbar_arrive_tx(&ctl->a_full, 2 * bytes);
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                smem_u32(a_hi)),
-            "l"(src), "r"(bytes), "r"(smem_u32(&ctl->a_full))
-            : "memory");
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                smem_u32(a_lo)),
-            "l"(src + (size_t)kM * K), "r"(bytes), "r"(smem_u32(&ctl->a_full))
-            : "memory");
-    }
-
-    if (warp < 4) {
-        // ================= producer warpgroup (+ MMA issue by tid 0) ========
-        // All waits are made by tid 0 and broadcast through ctl->stop after a
-        // named barrier, so the 128 producer threads leave the loop together.
+    if (tid == 0) {
+        // ================= producer: TMA copies + MMA issue (one thread) ======
         const uint32_t idesc = instr_desc(VARIANT);
-        for (int i = 0; i < ntiles; ++i) {
+        const uint32_t abytes = (uint32_t)kM * K * 2;
+        auto copy_strip = [&](int i) {
+            const int bb = i & 1;
+            const size_t g = (size_t)(tile_begin + i) * a.jmax * 128 + strip_off;
+            mbar_arrive_tx(&ctl->strip_full[bb], 2 * strip_bytes);
+            bulk_g2s(strip_hi[bb], a.strips_hi + g, strip_bytes, &ctl->strip_full[bb]);
+            bulk_g2s(strip_lo[bb], a.strips_lo + g, strip_bytes, &ctl->strip_full[bb]);
+        };
+        if (ntiles > 0) {
+            const uint16_t* src = a.packed + a.tile_off[m];
+            mbar_arrive_tx(&ctl->a_full, 2 * abytes);
+            bulk_g2s(a_hi, src, abytes, &ctl->a_full);
+            bulk_g2s(a_lo, src + (size_t)kM * K, abytes, &ctl->a_full);
+            copy_strip(0);
+        }
+        bool ok = ntiles == 0 || mbar_wait(&ctl->a_full, 0, abort_flag);
+        for (int i = 0; ok && i < ntiles; ++i) {
             const int b = i & 1;
-            const int t0 = (tile_begin + i) * kN;
-            const int base = t0 - K + 1;
-            if (tid == 0) {
-                // strip b is free once the MMAs of tile i-2 completed (the TMEM
-                // columns are reclaimed from the epilogue just before the MMA issue)
-                bool ok = true;
-                if (i >= 2) ok = mbar_wait(&ctl->mma_done[b], ((i >> 1) - 1) & 1, abort_flag);
-                if (a.trace && blockIdx.x == 0 && blockIdx.y == 0 && i < kTraceTiles)
-                    a.trace[i * TR_N + TR_P_START] = now_ns();
-                if (!ok) ctl->abort_flag = 1;
-                ctl->stop = ctl->abort_flag;
+            ok = mbar_wait(&ctl->strip_full[b], (i >> 1) & 1, abort_flag);
+            if (tracing && i < kTraceTiles) a.trace[i * TR_N + TR_P_STRIP] = now_ns();
+            if (ok && i >= 2) ok = mbar_wait(&ctl->acc_empty[b], ((i >> 1) - 1) & 1, abort_flag);
+            if (!ok) break;
+            if (tracing && i < kTraceTiles) a.trace[i * TR_N + TR_P_ACC] = now_ns();
+            tc_fence_after();
+            const uint32_t d = tmem + (uint32_t)(b * kN);
+            const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
+            const uint32_t bh = smem_u32(strip_hi[b]), bl = smem_u32(strip_lo[b]);
+            for (int ks = 0; ks < (K >> 4); ++ks) {
+                // A: next 2 K-chunks (16 row groups * 128 B each); B: next 2 strip blocks
+                const uint32_t ao = (uint32_t)ks * 2 * 16 * 128, bo = (uint32_t)ks * 256;
+                const uint64_t dah = smem_desc(ah + ao, 16 * 128, 128);
+                const uint64_t dal = smem_desc(al + ao, 16 * 128, 128);
+                const uint64_t dbh = smem_desc(bh + bo, 128, 128);
+                const uint64_t dbl = smem_desc(bl + bo, 128, 128);
+                tc_mma(d, dah, dbh, idesc, ks > 0 ? 1u : 0u);
+                tc_mma(d, dah, dbl, idesc, 1u);
+                tc_mma(d, dal, dbh, idesc, 1u);
             }
-            asm volatile("bar.sync 1, 128;" ::: "memory");
-            if (ctl->stop) break;
-            // the tile's x span is loaded once into registers; reference value r =
-            // the last bar of the tile (a valid x), scale from max |x - r|
-            float xv[kSpanRegs];
-            const int gref = min(t0 + kN - 1, a.n - 1);
-            const float vref = (gref >= a.first && gref >= 0) ? __ldg(a.x + gref) : 0.f;
-#pragma unroll
-            for (int k = 0; k < kSpanRegs; ++k) {
-                const int q = tid + 128 * k;
-                const int g = base + q;
-                float v = 0.f;
-                if (q < span && g >= a.first && g < a.n) {
-                    v = __ldg(a.x + g);
-                    if (!isfinite(v)) v = __int_as_float(0x7fc00000);
-                } else {
-                    v = __int_as_float(0x7fc00000);  // outside the series: zero after centring
-                }
-                xv[k] = v;
-            }
-            const float ref = isfinite(vref) ? vref : 0.f;
-            if (a.trace && tid == 0 && blockIdx.x == 0 && blockIdx.y == 0 && i < kTraceTiles)
-                a.trace[i * TR_N + TR_P_X] = now_ns();
-            float mx = 0.f;
-#pragma unroll
-            for (int k = 0; k < kSpanRegs; ++k)
-                if (!isnan(xv[k])) mx = fmaxf(mx, fabsf(xv[k] - ref));
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            if (lane == 0) ctl->red[warp] = mx;
-            asm volatile("bar.sync 1, 128;" ::: "memory");
-            mx = fmaxf(fmaxf(ctl->red[0], ctl->red[1]), fmaxf(ctl->red[2], ctl->red[3]));
-            int ex = 0;
-            if (mx > 0.f) {
-                int e2;
-                frexpf(mx, &e2);
-                ex = 13 - e2;
-            }
-            const float sc = ldexpf(1.f, ex);
-            // linear hi/lo of the span, then the expanded strip E[q] = lin[q .. q+7]
-#pragma unroll
-            for (int k = 0; k < kSpanRegs; ++k) {
-                const int q = tid + 128 * k;
-                if (q < span) {
-                    const float v = isnan(xv[k]) ? 0.f : (xv[k] - ref) * sc;
-                    uint16_t h, l;
-                    Split<VARIANT>::run(v, h, l);
-                    lin_hi[q] = h;
-                    lin_lo[q] = l;
-                }
-            }
-            asm volatile("bar.sync 1, 128;" ::: "memory");
-            const uint32_t* lh = reinterpret_cast<const uint32_t*>(lin_hi);
-            const uint32_t* ll = reinterpret_cast<const uint32_t*>(lin_lo);
-            for (int q = tid; q < J * 8; q += 128) {
-                const int w0 = q >> 1;
-                uint4 oh, ol;
-                if (q & 1) {
-                    oh.x = __byte_perm(lh[w0], lh[w0 + 1], 0x5432);
-                    oh.y = __byte_perm(lh[w0 + 1], lh[w0 + 2], 0x5432);
-                    oh.z = __byte_perm(lh[w0 + 2], lh[w0 + 3], 0x5432);
-                    oh.w = __byte_perm(lh[w0 + 3], lh[w0 + 4], 0x5432);
-                    ol.x = __byte_perm(ll[w0], ll[w0 + 1], 0x5432);
-                    ol.y = __byte_perm(ll[w0 + 1], ll[w0 + 2], 0x5432);
-                    ol.z = __byte_perm(ll[w0 + 2], ll[w0 + 3], 0x5432);
-                    ol.w = __byte_perm(ll[w0 + 3], ll[w0 + 4], 0x5432);
-                } else {
-                    oh = make_uint4(lh[w0], lh[w0 + 1], lh[w0 + 2], lh[w0 + 3]);
-                    ol = make_uint4(ll[w0], ll[w0 + 1], ll[w0 + 2], ll[w0 + 3]);
-                }
-                reinterpret_cast<uint4*>(strip_hi[b])[q] = oh;
-                reinterpret_cast<uint4*>(strip_lo[b])[q] = ol;
-            }
-            if (tid == 0) {
-                ctl->ref[i & 3] = ref;
-                ctl->xscale[i & 3] = ldexpf(1.f, -ex);
-            }
-            // generic-proxy smem writes -> visible to the tensor core (async proxy)
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            asm volatile("bar.sync 1, 128;" ::: "memory");
-            if (tid == 0) {
-                const bool tr = a.trace && blockIdx.x == 0 && blockIdx.y == 0 && i < kTraceTiles;
-                if (tr) a.trace[i * TR_N + TR_P_STRIP] = now_ns();
-                mbar_arrive(&ctl->params_full[i & 3]);
-                bool ok = (i > 0) || mbar_wait(&ctl->a_full, 0, abort_flag);
-                if (ok && i >= 2) ok = mbar_wait(&ctl->acc_empty[b], ((i >> 1) - 1) & 1, abort_flag);
-                if (tr) a.trace[i * TR_N + TR_P_ACC] = now_ns();
-                if (!ok) {
-                    ctl->abort_flag = 1;
-                } else {
-                    tc_fence_after();
-                    const uint32_t d = tmem + (uint32_t)(b * kN);
-                    const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
-                    const uint32_t bh = smem_u32(strip_hi[b]), bl = smem_u32(strip_lo[b]);
-                    for (int ks = 0; ks < (K >> 4); ++ks) {
-                        // A: next 2 K-chunks (16 row groups * 128 B each); B: next 2 strip blocks
-                        const uint32_t ao = (uint32_t)ks * 2 * 16 * 128, bo = (uint32_t)ks * 256;
-                        const uint64_t dah = smem_desc(ah + ao, 16 * 128, 128);
-                        const uint64_t dal = smem_desc(al + ao, 16 * 128, 128);
-                        const uint64_t dbh = smem_desc(bh + bo, 128, 128);
-                        const uint64_t dbl = smem_desc(bl + bo, 128, 128);
-                        tc_mma(d, dah, dbh, idesc, ks > 0 ? 1u : 0u);
-                        tc_mma(d, dah, dbl, idesc, 1u);
-                        tc_mma(d, dal, dbh, idesc, 1u);
-                    }
-                    tc_commit(&ctl->mma_done[b]);
-                    ctl->issued = i + 1;
-                    if (tr) a.trace[i * TR_N + TR_P_ISSUED] = now_ns();
-                }
+            tc_commit(&ctl->mma_done[b]);
+            ctl->issued = i + 1;
+            if (tracing && i < kTraceTiles) a.trace[i * TR_N + TR_P_ISSUED] = now_ns();
+            // next strip into the other buffer once the MMAs of tile i-1 (its last reader) are done
+            if (i + 1 < ntiles) {
+                if (i >= 1) ok = mbar_wait(&ctl->mma_done[b ^ 1], ((i - 1) >> 1) & 1, abort_flag);
+                if (ok) copy_strip(i + 1);
             }
         }
-    } else {
-        // ================= epilogue warpgroups ===============================
-        // warp w (4..11): TMEM lane quarter q4 = w % 4 (the combo rows it may
-        // read), column half (w - 4) / 4 of the 256 times of a tile.
+        if (!ok) ctl->abort_flag = 1;
+    } else if (warp >= 1) {
+        // ================= epilogue: warps 1-8 ================================
+        // warp w reads TMEM lane quarter w % 4 (its 32 combo rows) and column
+        // half (w - 1) / 4 of the 256 times of a tile.
         const int q4 = warp & 3;
-        const int half = (warp - 4) >> 2;
+        const int half = (warp - 1) >> 2;
         const int r = q4 * 32 + lane;  // accumulator row = combo within tile
         const int c = m * kM + r;
         const bool row_ok = c < a.n_combos;
@@ -491,28 +480,27 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
         const float rsum = a.row_sum[(size_t)m * kM + r];
         const bool vec_ok = (a.n & 3) == 0;
         const bool has_nan = a.nanp != nullptr && a.nanp[a.n - 1] > 0.5;
-        float* st = TMA_STORE ? reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(stage) + (size_t)(warp - 4) * kStageTma)
-                              : stage + (size_t)(warp - 4) * 32 * kStageLd;
+        float* st = TMA_STORE ? reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(stage) + (size_t)(warp - 1) * kStageTma)
+                              : stage + (size_t)(warp - 1) * 32 * kStageLd;
         const int rbase = m * kM + q4 * 32;  // first combo of this warp's rows
         for (int i = 0; i < ntiles; ++i) {
             const int b = i & 1;
-            const int t0 = (tile_begin + i) * kN;
+            const int g = tile_begin + i;
+            const int t0 = g * kN;
+            const float ref = __ldg(a.ref + g), xs = __ldg(a.xscale + g);
             // one lane waits, the warp follows (tcgen05.ld is warp-collective)
             int ok = 1;
             if (lane == 0) {
-                ok = mbar_wait(&ctl->mma_done[b], (i >> 1) & 1, abort_flag) &&
-                     mbar_wait(&ctl->params_full[i & 3], (i >> 2) & 1, abort_flag);
+                ok = mbar_wait(&ctl->mma_done[b], (i >> 1) & 1, abort_flag);
                 if (!ok) ctl->abort_flag = 1;
             }
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) break;
-            __syncwarp();  // orders lane 0's acquire before the other lanes' reads
-            const bool tr = a.trace && warp == 4 && lane == 0 && blockIdx.x == 0 && blockIdx.y == 0 &&
-                            i < kTraceTiles;
-            if (tr) a.trace[i * TR_N + TR_E_START] = now_ns();
+            __syncwarp();
             tc_fence_after();
-            const float ref = ctl->ref[i & 3];
-            const float scale = rscale * ctl->xscale[i & 3];
+            const bool tr = tracing && warp == 1 && lane == 0 && i < kTraceTiles;
+            if (tr) a.trace[i * TR_N + TR_E_START] = now_ns();
+            const float scale = rscale * xs;
             const float off = ref * rsum;
             // tiles past every row's warm-up with a NaN-free series need no masks
             const bool plain = !has_nan && __all_sync(0xffffffffu, t0 >= warm);
@@ -586,9 +574,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
             mbar_arrive(&ctl->acc_empty[b]);
             if (tr) a.trace[i * TR_N + TR_E_END] = now_ns();
         }
+        if (TMA_STORE && lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     }
 
-    if (TMA_STORE && warp >= 4 && lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     // drain: the last committed MMAs must have completed before TMEM is freed
     __syncthreads();
     if (tid == 0) {
@@ -611,9 +599,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
 
 size_t smem_bytes_for(int K) {
     const int J = K / 8 + kN / 8 - 1;
-    const int span = K + kN + 8;
-    return (size_t)kM * K * 2 * 2 + 4 * (size_t)J * 8 * 16 + 2 * (size_t)(((span + 15) & ~15) * 2) +
-           (size_t)8 * 32 * kStageLd * sizeof(float) + 1024 + sizeof(SmemCtl) + 128;
+    return (size_t)kM * K * 2 * 2 + 4 * (size_t)J * 128 + 1024 + (size_t)8 * 32 * kStageLd * sizeof(float) +
+           sizeof(SmemCtl) + 128;
 }
 
 }  // namespace
@@ -635,21 +622,24 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
         off += 2LL * kM * K;
         kbig = std::max(kbig, K);
     }
-    // never below 160 KB: every descriptor address stays inside the allocation
     const size_t smem = std::max<size_t>(smem_bytes_for(kbig), 160 * 1024);
     if (smem > ctx->smem_optin) return fail(VTA_ERR_NOT_IMPLEMENTED, "tcgen05 path: shared memory");
-    // packed operands in a stream-ordered buffer of their own (the context
-    // workspace holds the caller's weights and periods during this call)
+    const int n_time_tiles = (a.n + kN - 1) / kN;
+    const int jmax = kbig / 8 + kN / 8 - 1;
+    const size_t strip_tile = (size_t)jmax * 128;
+    // operands in a stream-ordered buffer of their own (the context workspace
+    // holds the caller's weights and periods during this call)
     auto al256 = [](size_t b) { return (b + 255) & ~size_t(255); };
     const size_t total = al256(n_tiles_m * sizeof(int)) + al256(n_tiles_m * sizeof(long long)) +
                          al256((size_t)off * sizeof(uint16_t)) + 2 * al256((size_t)n_tiles_m * kM * sizeof(float)) +
+                         2 * al256(strip_tile * n_time_tiles) + 2 * al256(n_time_tiles * sizeof(float)) +
                          al256(sizeof(int));
     void* buf = nullptr;
     VTA_CUDA_TRY(cudaMallocAsync(&buf, total, st));
     char* bp = static_cast<char*>(buf);
     auto take = [&](size_t bytes) {
         char* r = bp;
-        bp += (bytes + 255) & ~size_t(255);
+        bp += al256(bytes);
         return r;
     };
     int* d_tk = reinterpret_cast<int*>(take(n_tiles_m * sizeof(int)));
@@ -657,6 +647,10 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
     uint16_t* d_packed = reinterpret_cast<uint16_t*>(take((size_t)off * sizeof(uint16_t)));
     float* d_rs = reinterpret_cast<float*>(take((size_t)n_tiles_m * kM * sizeof(float)));
     float* d_rsum = reinterpret_cast<float*>(take((size_t)n_tiles_m * kM * sizeof(float)));
+    uint8_t* d_sh = reinterpret_cast<uint8_t*>(take(strip_tile * n_time_tiles));
+    uint8_t* d_sl = reinterpret_cast<uint8_t*>(take(strip_tile * n_time_tiles));
+    float* d_ref = reinterpret_cast<float*>(take(n_time_tiles * sizeof(float)));
+    float* d_xs = reinterpret_cast<float*>(take(n_time_tiles * sizeof(float)));
     int* d_err = reinterpret_cast<int*>(take(sizeof(int)));
     VTA_CUDA_TRY(cudaMemcpyAsync(d_tk, tk.data(), n_tiles_m * sizeof(int), cudaMemcpyHostToDevice, st));
     VTA_CUDA_TRY(cudaMemcpyAsync(d_toff, toff.data(), n_tiles_m * sizeof(long long), cudaMemcpyHostToDevice, st));
@@ -665,9 +659,14 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
     if (variant == 1) k_pack_a<1><<<n_tiles_m, kM, 0, st>>>(pa);
     else k_pack_a<0><<<n_tiles_m, kM, 0, st>>>(pa);
     VTA_TRY(check_launch("k_pack_a"));
+    StripArgs sa{a.x, a.n, a.first, kbig, jmax, d_sh, d_sl, d_ref, d_xs};
+    const int L = jmax * 8 + 8;
+    const size_t ssmem = (size_t)L * 4 + 2 * (size_t)((L + 7) & ~7) * 2 + 64;
+    if (variant == 1) k_hankel_strips<1><<<n_time_tiles, 128, ssmem, st>>>(sa);
+    else k_hankel_strips<0><<<n_time_tiles, 128, ssmem, st>>>(sa);
+    VTA_TRY(check_launch("k_hankel_strips"));
 
     TcArgs t{};
-    t.x = a.x;
     t.n = a.n;
     t.first = a.first;
     t.periods = a.periods;
@@ -677,6 +676,12 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
     t.packed = d_packed;
     t.row_scale = d_rs;
     t.row_sum = d_rsum;
+    t.kmax = kbig;
+    t.jmax = jmax;
+    t.strips_hi = d_sh;
+    t.strips_lo = d_sl;
+    t.ref = d_ref;
+    t.xscale = d_xs;
     t.nan_mode = a.nan_mode;
     t.nanp = a.nanp;
     t.out = a.out;
@@ -688,7 +693,6 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
         VTA_CUDA_TRY(cudaMemsetAsync(d_trace, 0, kTraceTiles * TR_N * 8, st));
     }
     t.trace = d_trace;
-    const int n_time_tiles = (a.n + kN - 1) / kN;
     const int target = ctx->num_sms * 6;
     int chunks = std::max(1, std::min(n_time_tiles, (target + n_tiles_m - 1) / n_tiles_m));
     t.tiles_per_chunk = (n_time_tiles + chunks - 1) / chunks;
@@ -733,10 +737,11 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
         cudaMemcpy(h.data(), d_trace, h.size() * 8, cudaMemcpyDeviceToHost);
         cudaFree(d_trace);
         const unsigned long long t0 = h[0];
-        std::fprintf(stderr, "tc trace (ns from first tile start): tile p_start p_x p_strip p_acc p_issued e_start e_end\n");
+        std::fprintf(stderr, "tc trace (ns): tile strip_in acc_free issued e_start e_end\n");
         for (int i = 0; i < std::min(kTraceTiles, t.tiles_per_chunk); ++i) {
             std::fprintf(stderr, "%3d", i);
-            for (int e = 0; e < 7; ++e) std::fprintf(stderr, " %8lld", h[i * TR_N + e] ? (long long)(h[i * TR_N + e] - t0) : -1LL);
+            for (int e = 0; e < 5; ++e)
+                std::fprintf(stderr, " %8lld", h[i * TR_N + e] ? (long long)(h[i * TR_N + e] - t0) : -1LL);
             std::fprintf(stderr, "\n");
         }
     }
