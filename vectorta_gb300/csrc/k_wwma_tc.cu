@@ -22,12 +22,20 @@
 // within ~1e-7 relative of the FP64 sum.  A BF16 hi/lo variant (8-bit
 // significands, ~16 bits per operand) is selectable for comparison.
 //
-// Pipeline (256 threads): warpgroup 0 builds strips (double-buffered) and its
-// thread 0 issues the MMAs into one of two 256-column TMEM accumulators;
-// warpgroup 1 drains the other accumulator (tcgen05.ld), applies scale,
-// centring, warm-up / NaN masks and stores.  mbarriers hand buffers back and
-// forth; every wait is bounded by a time limit after which the kernel records
-// an error code, stops issuing work, drains its own MMAs and frees TMEM.
+// Two kernels.  k_hankel_strips builds, once per 256-wide time tile, the hi/lo
+// strips for the largest period in the sweep (plus the tile's centring value
+// and x scale) in global memory; a combo tile of smaller period K reads the
+// same strip starting 16 * (Kmax - K) bytes in, so every combo tile shares it.
+// k_wwma_tc (288 threads): thread 0 bulk-copies the weights once, then per time
+// tile waits for its strip (double-buffered, cp.async.bulk + mbarrier
+// complete_tx), issues the MMAs into one of two 256-column TMEM accumulators,
+// and starts the copy of the next strip as soon as the MMAs that read that
+// buffer have completed.  Warps 1-8 drain the other accumulator (tcgen05.ld),
+// apply scale and centring, stage 32x32 blocks in 128-byte-swizzled shared
+// memory, patch warm-up / NaN positions there, and write them with TMA tensor
+// stores.  Every mbarrier wait is bounded by a time limit after which the
+// kernel records an error code, stops issuing work, drains its own MMAs and
+// bulk copies and frees TMEM.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
