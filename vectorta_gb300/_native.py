@@ -155,6 +155,8 @@ def lib() -> C.CDLL:
         for suffix in ("expand_grid", "batch_dev", "batch_device", "batch_into_host_f32",
                        "many_series_one_param_time_major_dev", "many_series_one_param_device"):
             getattr(L, f"vta_{name}_{suffix}").restype = st
+    L.vta_sma_batch_device_noalloc.argtypes = [vp, vp, sz, sz, C.POINTER(SWEEPS["period"]), vp]
+    L.vta_sma_batch_device_noalloc.restype = st
     for fn in ("vta_ctx_create", "vta_ctx_destroy", "vta_ctx_synchronize", "vta_ctx_set_stream",
                "vta_ctx_set_policy", "vta_device_array_free", "vta_device_array_copy_to_host",
                "vta_pinned_alloc", "vta_pinned_free", "vta_device_alloc", "vta_device_free",

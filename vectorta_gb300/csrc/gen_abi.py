@@ -204,6 +204,39 @@ for (name, wf, kind, outs, rng, prm, cites) in IND:
     w(f"/* {name}_many_series_one_param_device ({cite}) */")
     w(f"vta_status vta_{name}_many_series_one_param_device(vta_ctx* ctx, {', '.join(inputs(kind, True, True))},\n    size_t cols, size_t rows, const {P}* params, {outs_d});")
     w("")
+w("""/* ==== sma without device allocation ====
+ * No counterpart in the crate: its wrappers allocate device memory on every
+ * call (sma_batch_dev_from_device, sma_wrapper.rs:830-841, allocates the
+ * period list, the prefix and the output), and so do the other entry points
+ * here.  vta_sma_batch_device_noalloc returns what vta_sma_batch_device
+ * returns (same arguments, checks and errors) but never allocates device
+ * memory: its working buffers live in one fixed scratch area of the library's
+ * static device memory (VTA_NOALLOC_SCRATCH_BYTES, about 8 MiB per device,
+ * reserved on a device when the function is first called there).
+ * It is for callers that may not allocate once running: cudaMalloc and
+ * cudaFree can synchronise the whole device and take unbounded time, which a
+ * latency-bound loop (re-running a sweep on every new bar of a live feed)
+ * cannot absorb, and a process whose own memory pool already holds the
+ * device's free memory would see a mid-session allocation fail.
+ *   - At most VTA_NOALLOC_MAX_LEN bars and VTA_NOALLOC_MAX_COMBOS periods;
+ *     larger requests fail with VTA_ERR_INVALID_INPUT and a message naming
+ *     the limit (vta_sma_batch_device has no such limit).
+ *   - The first call on each device does one-time setup (it looks up the
+ *     scratch address, which loads the library's device code there); make
+ *     that first call before any stream capture on that device.
+ *   - There is one scratch area per device per process.  Calls that overlap
+ *     in time on the same device (from several host threads, whatever their
+ *     contexts or streams) race on it and corrupt each other's results:
+ *     serialise them.  Each call returns only when its work has finished, so
+ *     consecutive calls from one thread never overlap.
+ *   - Nothing in the scratch has to start at zero; each call writes every
+ *     scratch cell it reads. */
+#define VTA_NOALLOC_MAX_LEN 1048576
+#define VTA_NOALLOC_MAX_COMBOS 4096
+#define VTA_NOALLOC_SCRATCH_BYTES 8437760
+vta_status vta_sma_batch_device_noalloc(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+""")
 w("""#ifdef __cplusplus
 }
 #endif

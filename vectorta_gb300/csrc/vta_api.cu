@@ -869,6 +869,25 @@ static vta_status expand(Ind ind, const R* r, P* out, size_t cap, size_t* n) {
     return cs.empty() ? fail(VTA_ERR_INVALID_INPUT, "empty range") : VTA_OK;
 }
 
+// ---- hooks for the no-allocation SMA entry point (vta_noalloc.cu) --------
+vta_status enter_call(vta_ctx* ctx) { return check_ctx(ctx); }
+
+vta_status validate_sma_periods(const vta_period_params* p, size_t n, size_t len, size_t first) {
+    if (n == 0) return fail(VTA_ERR_INVALID_INPUT, "sma: no parameter combinations");
+    size_t need = 0;
+    for (size_t i = 0; i < n; ++i) {
+        VTA_TRY(validate_combo(I_SMA, Combo{p[i].period, 0.0, 0.0}, len));
+        need = std::max(need, needed_len(I_SMA, p[i].period));
+    }
+    if (first >= len) return fail(VTA_ERR_INVALID_INPUT, "sma: all values are NaN");
+    if (len - first < need) {
+        char buf[200];
+        std::snprintf(buf, sizeof buf, "sma: not enough valid data (needed >= %zu, valid = %zu)", need, len - first);
+        return fail(VTA_ERR_INVALID_INPUT, buf);
+    }
+    return VTA_OK;
+}
+
 }  // namespace vta
 
 using namespace vta;

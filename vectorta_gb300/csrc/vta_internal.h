@@ -283,4 +283,10 @@ struct PnrArgs {
 };
 vta_status launch_percentile(const PnrArgs& a, cudaStream_t st);
 
+// ------------------------------------------------- no-allocation SMA -------
+// Binds a call to `ctx` (device current, timing events), as every entry does.
+vta_status enter_call(vta_ctx* ctx);
+// The allocating SMA entry points' parameter and length checks, same messages.
+vta_status validate_sma_periods(const vta_period_params* p, size_t n, size_t len, size_t first);
+
 }  // namespace vta
