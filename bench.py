@@ -349,9 +349,17 @@ def e2e_bench(args, wl, inds, rows, out_per_step):
             "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3, "steps": steps}
 
 
-# dram bytes per launch of the dominant kernel from the committed ncu capture
-# (profiles/*.md); None until captured
-TRAFFIC = {}
+# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
+# capture each of the EMA sweep on 200,000 bars and of the ALMA grid on 20,000
+# bars (ema_small / alma_small).  Their per-launch bytes are scaled by the
+# output count to the full workloads (x5 and x10): these kernels' traffic is
+# linear in the outputs they write.
+TRAFFIC = {
+    "recurrence_window_sweeps": (5.709056e6 + 738.209024e6) * 5,
+    "ema_small": 5.709056e6 + 738.209024e6,
+    "alma_grid": (15.215616e6 + 1382.070e6) * 10,
+    "alma_small": 15.215616e6 + 1382.070e6,
+}
 KERNEL_NAME = {"recurrence_window_sweeps": "k_recur<OpEma, batch, EMIT>", "alma_grid": "k_wwma_tc<fp16x3>",
                "ema_small": "k_recur<OpEma, batch, EMIT>", "alma_small": "k_wwma_tc<fp16x3>"}
 
