@@ -113,18 +113,63 @@ WORKLOADS = {"sweeps": workload_sweeps, "alma_grid": workload_alma_grid, "ema_sm
 
 # ------------------------------------------------------------- clocks -------
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    """SM clocks and clock-event (throttle) reasons sampled while the timed
+    region runs: NVML read-only queries every 10 ms through ctypes, or
+    `nvidia-smi -lms 200` when NVML cannot be loaded."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # NVML clock-event reason bits
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40}
 
     def __init__(self, device=0):
         self.device = device
         self.proc = None
         self.lines = []
+        self.samples = []  # (sm_mhz, max_mhz, reason bits)
+        self._nvml = None
+        self._stop = threading.Event()
+
+    def _nvml_open(self):
+        import ctypes as C
+        lib = C.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            return None
+        h = C.c_void_p()
+        ok = False
+        try:
+            import torch
+            pr = torch.cuda.get_device_properties(self.device)
+            bus = f"{pr.pci_domain_id:08X}:{pr.pci_bus_id:02X}:{pr.pci_device_id:02X}.0".encode()
+            ok = lib.nvmlDeviceGetHandleByPciBusId_v2(C.c_char_p(bus), C.byref(h)) == 0
+        except Exception:
+            ok = False
+        if not ok and lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.device), C.byref(h)) != 0:
+            return None
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        return lib, h, reasons
+
+    def _nvml_loop(self):
+        import ctypes as C
+        lib, h, reasons = self._nvml
+        sm, mx, rb = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        while not self._stop.is_set():
+            if (lib.nvmlDeviceGetClockInfo(h, 1, C.byref(sm)) == 0 and
+                    lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0 and reasons(h, C.byref(rb)) == 0):
+                self.samples.append((float(sm.value), float(mx.value), int(rb.value)))
+            self._stop.wait(0.01)
 
     def __enter__(self):
+        try:
+            self._nvml = self._nvml_open()
+        except Exception:
+            self._nvml = None
+        if self._nvml:
+            self._t = threading.Thread(target=self._nvml_loop, daemon=True)
+            self._t.start()
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
@@ -140,6 +185,13 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        self._stop.set()
+        if self._nvml:
+            self._t.join(timeout=2)
+            try:
+                self._nvml[0].nvmlShutdown()
+            except Exception:
+                pass
         if self.proc:
             self.proc.terminate()
             try:
@@ -149,6 +201,10 @@ class ClockSampler:
 
     def summary(self):
         sm, mx, reasons = [], [], set()
+        for s_mhz, m_mhz, bits in self.samples:
+            sm.append(s_mhz)
+            mx.append(m_mhz)
+            reasons.update(nm for nm, b in self.BITS.items() if bits & b)
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.lines:
             f = [x.strip() for x in line.split(",")]
@@ -165,7 +221,7 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvml" if self.samples else "nvidia-smi"}
 
 
 # ------------------------------------------------------------- CPU side -----

@@ -108,8 +108,14 @@ struct OpEma {
     __device__ float get(int) const { return y; }
     __device__ void set(int, float v) { y = v; }
     // running step + output without phase checks; returns applied-step flag
-    template <class In> __device__ float fast(const In& in, int t, int& applied) {
+    // FIN: every input of the step is known finite (no skip logic)
+    template <bool FIN = false, class In> __device__ float fast(const In& in, int t, int& applied) {
         const float v = in.X(t);
+        if (FIN) {
+            y = fmaf(beta, y, alpha * v);
+            ++applied;
+            return y;
+        }
         const bool ok = isfinite(v);
         y = ok ? fmaf(beta, y, alpha * v) : y;
         applied += ok;
@@ -149,7 +155,7 @@ struct OpDema {
     __device__ void zero() { e1 = 0.f; e2 = 0.f; }
     __device__ float get(int i) const { return i == 0 ? e1 : e2; }
     __device__ void set(int i, float v) { if (i == 0) e1 = v; else e2 = v; }
-    template <class In> __device__ float fast(const In& in, int t, int& applied) {
+    template <bool FIN = false, class In> __device__ float fast(const In& in, int t, int& applied) {
         const float v = in.X(t);
         e1 = fmaf(e1, a, v * alpha);
         e2 = fmaf(e2, a, e1 * alpha);
@@ -205,7 +211,7 @@ struct OpTema {
     }
     __device__ float warm_value(int) const { return qnan(); }
     __device__ void zero() { e1 = e2 = e3 = 0.f; }
-    template <class In> __device__ float fast(const In& in, int t, int& applied) {
+    template <bool FIN = false, class In> __device__ float fast(const In& in, int t, int& applied) {
         const float v = in.X(t);
         ++applied;
         if (p1 == 0) { e1 = v; return v; }
@@ -279,11 +285,11 @@ struct OpRsi {
     }
     __device__ float warm_value(int) const { return qnan(); }
     __device__ void zero() { ag = 0.f; al = 0.f; }
-    template <class In> __device__ float fast(const In& in, int t, int& applied) {
+    template <bool FIN = false, class In> __device__ float fast(const In& in, int t, int& applied) {
         const float v = in.X(t);
         const float d = v - in.X(t - 1);
         float g = d > 0.f ? d : 0.f, lo = d < 0.f ? -d : 0.f;
-        if (kBatchSem && !isfinite(d)) { g = qnan(); lo = qnan(); }
+        if (!FIN && kBatchSem && !isfinite(d)) { g = qnan(); lo = qnan(); }
         ag = fmaf(ag, beta, inv_p * g);
         al = fmaf(al, beta, inv_p * lo);
         ++applied;
@@ -325,7 +331,7 @@ struct OpWilders {
     __device__ void zero() { y = 0.f; }
     __device__ float get(int) const { return y; }
     __device__ void set(int, float v) { y = v; }
-    template <class In> __device__ float fast(const In& in, int t, int& applied) {
+    template <bool FIN = false, class In> __device__ float fast(const In& in, int t, int& applied) {
         const float v = in.X(t);
         y = (p == 1) ? v : fmaf(v - y, alpha, y);
         ++applied;
@@ -376,7 +382,7 @@ struct OpAtr {
     __device__ void zero() { y = 0.f; }
     __device__ float get(int) const { return y; }
     __device__ void set(int, float v) { y = v; }
-    template <class In> __device__ float fast(const In& in, int t, int& applied) {
+    template <bool FIN = false, class In> __device__ float fast(const In& in, int t, int& applied) {
         const float tr = true_range(in.H(t), in.L(t), in.C(t - 1));
         y = fmaf(-alpha, y, y) + alpha * tr;
         ++applied;
@@ -401,6 +407,17 @@ __device__ __forceinline__ int warp_max(int v) {
 // of the warp is past its seed and warm-up take the fast path (no phase
 // checks: 2-6 FP ops per step); the few tiles around warm-up take the general
 // per-step state machine.
+// The 32 steps of one register tile, fully unrolled so every shuffle source
+// lane is a constant; EMIT stages the outputs in this lane's row.
+template <bool FIN, int PASS, class Op>
+__device__ __forceinline__ void run_tile(Op& op, const InTile& ti, float* row, int& steps) {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        const float y = op.template fast<FIN>(ti, ti.tb + j, steps);
+        if (PASS == PASS_EMIT) row[j] = y;
+    }
+}
+
 template <class Op, bool TM, int PASS>
 __global__ void __launch_bounds__(kWarps * 32)
 k_recur(RecurArgs a) {
@@ -478,13 +495,17 @@ k_recur(RecurArgs a) {
                     ti.xv = __ldg(a.x + tb + lane);
                     ti.xb = __ldg(a.x + tb - 1);
                 }
-                if (PASS == PASS_EMIT) {
-#pragma unroll 8
-                    for (int j = 0; j < 32; ++j) stage[warp][lane][j] = op.fast(ti, tb + j, steps);
+                // a tile whose inputs (and the value before it) are all finite
+                // runs without per-step skip / NaN logic
+                bool fin;
+                if constexpr (Op::kHlc) {
+                    fin = __all_sync(0xffffffffu, isfinite(ti.hv) && isfinite(ti.lv) && isfinite(ti.cv) &&
+                                                      isfinite(ti.cb));
                 } else {
-#pragma unroll 8
-                    for (int j = 0; j < 32; ++j) op.fast(ti, tb + j, steps);
+                    fin = __all_sync(0xffffffffu, isfinite(ti.xv) && isfinite(ti.xb));
                 }
+                if (fin) run_tile<true, PASS>(op, ti, stage[warp][lane], steps);
+                else run_tile<false, PASS>(op, ti, stage[warp][lane], steps);
             } else if (PASS == PASS_EMIT && !TM) {
 #pragma unroll 8
                 for (int t = tb; t < te; ++t) stage[warp][lane][t - tb] = op.fast(in, t, steps);

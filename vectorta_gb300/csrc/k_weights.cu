@@ -4,39 +4,77 @@
 //
 // Weight definitions follow the crate:
 //   ALMA   w_i = exp(-(i - m)^2 / (2 s^2)), m = offset (p-1), s = p / sigma
-//          (alma.rs:1426-1437; the exponent is formed in f64 and exponentiated
-//          as expf(a_hi) * (1 + a_lo) so the weights keep ~1e-7 accuracy)
+//          (alma.rs:1426-1437)
 //   WMA    w_i = (i + 1) / (p (p + 1) / 2)                       (wma.rs:295-336)
 //   SWMA   symmetric triangle = box(a) * box(b)        (swma.rs:320-400, 406-482)
 //   PWMA   binomial row C(p-1, r) / sum                  (pwma.rs:1367-1408)
 //   SINWMA w_k = sin((k+1) pi / (p+1)) / sum             (sinwma.rs:271-289)
 //   TRIMA  box(m1) * box(m2), m1 = (p+1)/2, m2 = p - m1 + 1 (trima.rs:277-364)
+//
+// Arithmetic: GB300's FP64 rate is a small fraction of its FP32 rate, so only
+// the per-combo constants (ALMA's centre m and 1/(2 s^2), the row sum's
+// reciprocal) are formed in f64, once per block.  Each weight is evaluated in
+// double-single FP32 (error-free products through FMA): the ALMA exponent
+// e = (i - m)^2 / (2 s^2) is carried as e_hi + e_lo and exponentiated as
+// expf(-e_hi) * (1 - e_lo), and the row sum is accumulated as a double-single
+// value, so the stored f32 weights stay within ~2 ulp of the f64 ones.
 #include "vta_internal.h"
 
 namespace vta {
 
 namespace {
 
-__device__ double raw_weight(int kind, int i, int p, double a, double b) {
+constexpr int kWThreads = 256;
+
+struct DS {
+    float hi, lo;
+};
+
+__device__ __forceinline__ DS two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ DS quick_two_sum(float a, float b) {
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+__device__ __forceinline__ DS ds_add(DS a, DS b) {
+    const DS s = two_sum(a.hi, b.hi);
+    return quick_two_sum(s.hi, s.lo + a.lo + b.lo);
+}
+__device__ __forceinline__ DS ds_mul(DS a, DS b) {
+    const float p = a.hi * b.hi;
+    const float e = fmaf(a.hi, b.hi, -p);
+    return quick_two_sum(p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e)));
+}
+__device__ __forceinline__ DS split(double v) {
+    const float hi = (float)v;
+    return {hi, (float)(v - (double)hi)};
+}
+
+struct RowConst {
+    DS m;        // ALMA centre offset (p - 1)
+    DS inv2s2;   // ALMA 1 / (2 s^2) = sigma^2 / (2 p^2)
+};
+
+__device__ DS raw_weight(int kind, int i, int p, const RowConst& rc) {
     switch (kind) {
         case WT_ALMA: {
-            const double m = a * (double)(p - 1);
-            const double s = (double)p / b;
-            const double s2 = 2.0 * s * s;
-            const double d = (double)i - m;
-            const double e = -(d * d) / s2;
-            const float hi = (float)e;
-            const float lo = (float)(e - (double)hi);
-            return (double)expf(hi) * (1.0 + (double)lo);
+            const DS d = ds_add(DS{(float)i, 0.f}, DS{-rc.m.hi, -rc.m.lo});
+            const DS e = ds_mul(ds_mul(d, d), rc.inv2s2);
+            const float w = expf(-e.hi);
+            return {w, -w * e.lo};
         }
-        case WT_WMA: return (double)(i + 1);
+        case WT_WMA: return {(float)(i + 1), 0.f};
         case WT_SWMA: {
             int aa, bb;
             if (p & 1) { aa = bb = (p + 1) >> 1; }
             else { aa = p >> 1; bb = aa + 1; }
-            return (double)min(min(i + 1, p - i), min(aa, bb));
+            return {(float)min(min(i + 1, p - i), min(aa, bb)), 0.f};
         }
         case WT_PWMA: {
+            // binomial C(p-1, r): integer-valued, exact in f64 up to 2^53
             const int n = p - 1;
             const int r = min(i, n - i);
             double res = 1.0;
@@ -44,37 +82,63 @@ __device__ double raw_weight(int kind, int i, int p, double a, double b) {
                 res *= (double)(n - k);
                 res /= (double)(k + 1);
             }
-            return res;
+            return split(res);
         }
-        case WT_SINWMA: return (double)sinpif((float)(i + 1) / (float)(p + 1));
+        case WT_SINWMA: return {sinpif((float)(i + 1) / (float)(p + 1)), 0.f};
         case WT_TRIMA: {
             const int m1 = (p + 1) / 2, m2 = p - m1 + 1;
-            return (double)min(min(i + 1, p - i), min(m1, m2));
+            return {(float)min(min(i + 1, p - i), min(m1, m2)), 0.f};
         }
     }
-    return 0.0;
+    return {0.f, 0.f};
 }
 
-// One block per combo: raw weights, f64 block sum, normalise, store.
-__global__ void k_weights(int kind, const int* periods, const double* pa, const double* pb, int kmax,
-                          float* w) {
-    __shared__ double red[256];
+// One block per combo: raw weights summed in double-single, block reduction,
+// then a second pass writes raw * (1 / sum).
+__global__ void __launch_bounds__(kWThreads) k_weights(int kind, const int* periods, const double* pa,
+                                                       const double* pb, int kmax, float* w) {
+    __shared__ float red_hi[kWThreads / 32], red_lo[kWThreads / 32];
+    __shared__ float inv_sh[2];
     const int c = blockIdx.x;
     const int p = periods[c];
-    const double a = pa ? pa[c] : 0.0, b = pb ? pb[c] : 0.0;
-    double s = 0.0;
-    for (int i = threadIdx.x; i < p; i += blockDim.x) s += raw_weight(kind, i, p, a, b);
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-        __syncthreads();
+    RowConst rc{};
+    if (kind == WT_ALMA) {
+        const double a = pa[c], b = pb[c];
+        rc.m = split(a * (double)(p - 1));
+        rc.inv2s2 = split(b * b / (2.0 * (double)p * (double)p));
     }
-    const double inv = 1.0 / red[0];
+    DS s{0.f, 0.f};
+    for (int i = threadIdx.x; i < p; i += kWThreads) s = ds_add(s, raw_weight(kind, i, p, rc));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const DS t{__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)};
+        s = ds_add(s, t);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        red_hi[warp] = s.hi;
+        red_lo[warp] = s.lo;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int k = 0; k < kWThreads / 32; ++k) tot += (double)red_hi[k] + (double)red_lo[k];
+        const DS inv = split(1.0 / tot);
+        inv_sh[0] = inv.hi;
+        inv_sh[1] = inv.lo;
+    }
+    __syncthreads();
+    const DS inv{inv_sh[0], inv_sh[1]};
     float* row = w + (size_t)c * kmax;
-    for (int k = threadIdx.x; k < kmax; k += blockDim.x) {
-        const int i = k - (kmax - p);
-        row[k] = i >= 0 ? (float)(raw_weight(kind, i, p, a, b) * inv) : 0.f;
+    const int lead = kmax - p;
+    for (int k = threadIdx.x; k < kmax; k += kWThreads) {
+        const int i = k - lead;
+        float v = 0.f;
+        if (i >= 0) {
+            const DS r = ds_mul(raw_weight(kind, i, p, rc), inv);
+            v = r.hi + r.lo;
+        }
+        row[k] = v;
     }
 }
 
@@ -82,7 +146,7 @@ __global__ void k_weights(int kind, const int* periods, const double* pa, const 
 
 vta_status launch_weights(int kind, const int* periods, const double* pa, const double* pb, int n_combos,
                           int kmax, float* w, cudaStream_t st) {
-    k_weights<<<n_combos, 256, 0, st>>>(kind, periods, pa, pb, kmax, w);
+    k_weights<<<n_combos, kWThreads, 0, st>>>(kind, periods, pa, pb, kmax, w);
     return check_launch("k_weights");
 }
 

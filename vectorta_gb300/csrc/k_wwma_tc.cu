@@ -3,9 +3,11 @@
 //   out[c][t] = sum_k W[c][k] * x[t - K + 1 + k]        (rows of W right-aligned)
 //
 // is a GEMM D[M = combos][N = times] = A[M][K] * B[K][N] whose B operand is the
-// Hankel matrix B[k][n] = x[base + k + n].  Per CTA: one tile of 128 combos
-// (A, K-major, packed in core-matrix order and bulk-copied to shared memory
-// once with cp.async.bulk) and a run of 256-wide time tiles.  B is never
+// Hankel matrix B[k][n] = x[base + k + n].  Work items are (tile of 128
+// combos, 256-wide time tile) pairs, combo-tile major, cut into short chunks
+// that a persistent grid of one CTA per SM takes round-robin (ItemIter).  A
+// (K-major, packed in core-matrix order) is bulk-copied to shared memory with
+// cp.async.bulk whenever a CTA enters a new combo tile.  B is never
 // materialised as a K x 256 tile: the producer writes an "8-shift expanded
 // strip" E[q] = x16[base + q .. base + q + 7] (16 bytes per q), so the 8x8 core
 // matrix (kc, nc) of the MN-major canonical layout is the contiguous 128-byte
@@ -26,8 +28,8 @@
 // strips for the largest period in the sweep (plus the tile's centring value
 // and x scale) in global memory; a combo tile of smaller period K reads the
 // same strip starting 16 * (Kmax - K) bytes in, so every combo tile shares it.
-// k_wwma_tc (288 threads): thread 0 bulk-copies the weights once, then per time
-// tile waits for its strip (double-buffered, cp.async.bulk + mbarrier
+// k_wwma_tc (288 threads): thread 0 bulk-copies the weights of the current
+// combo tile, then per item waits for its strip (double-buffered, cp.async.bulk + mbarrier
 // complete_tx), issues the MMAs into one of two 256-column TMEM accumulators,
 // and starts the copy of the next strip as soon as the MMAs that read that
 // buffer have completed.  Warps 1-8 drain the other accumulator (tcgen05.ld),
@@ -343,7 +345,9 @@ struct TcArgs {
     int nan_mode;
     const double* nanp;
     float* out;
-    int tiles_per_chunk;  // time tiles per CTA
+    int n_time_tiles;     // time tiles per combo tile
+    int items;            // combo tiles x time tiles, combo-tile major
+    int nchunks;          // items are cut into nchunks near-equal runs; CTA b takes b, b+G, ...
     int* err;             // error word (0 = ok)
     unsigned long long* trace;  // optional pipeline trace of CTA (0, 0): [tile][event]
 };
@@ -368,36 +372,60 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                  : "memory");
 }
 
+// Walks a CTA's items: chunk c holds items [c*items/nchunks, (c+1)*items/nchunks),
+// and a CTA takes chunks blockIdx.x, blockIdx.x + gridDim.x, ...  At any moment
+// the grid works on a window of about gridDim.x consecutive chunks, i.e. a few
+// combo tiles, which keeps the output rows being written (and their pages)
+// few, while every CTA gets the same number of items to within one.
+struct ItemIter {
+    int q, end, chunk;
+    // combo tile of the current item.  Combos are period-major, so tile K
+    // grows with the tile index; the item order visits tiles 0, n-1, 1, n-2, ...
+    // so the grid's window mixes tensor-heavy (large K) and write-heavy (small
+    // K) tiles instead of running all SMs through one kind at a time.
+    __device__ int tile(const TcArgs& a) const {
+        const int j = q / a.n_time_tiles;
+        const int n = a.items / a.n_time_tiles;
+        return (j & 1) ? n - 1 - (j >> 1) : (j >> 1);
+    }
+    __device__ int time_tile(const TcArgs& a) const { return q % a.n_time_tiles; }
+    __device__ void start(const TcArgs& a, int c) {
+        chunk = c;
+        q = (int)((long long)c * a.items / a.nchunks);
+        end = (int)((long long)(c + 1) * a.items / a.nchunks);
+    }
+    __device__ void advance(const TcArgs& a) {
+        if (++q >= end) start(a, chunk + (int)gridDim.x);
+    }
+};
+
 template <int VARIANT, bool TMA_STORE>
 __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_constant__ CUtensorMap tmap_out) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
-    const int m = blockIdx.y;
-    const int K = a.tile_k[m];
-    const int J = K / 8 + kN / 8 - 1;  // strip blocks this tile reads
-    const uint32_t strip_bytes = (uint32_t)J * 128;
-    const size_t strip_off = (size_t)(a.kmax - K) * 16;  // into the Kmax strip
-    // layout: A hi | A lo | strip[2] hi | strip[2] lo | staging (1024-aligned) | ctl
+    // layout (capacities for the largest tile K): A hi | A lo | strip[2] hi |
+    // strip[2] lo | staging (1024-aligned) | ctl
+    const uint32_t strip_cap = (uint32_t)a.jmax * 128;
     uint8_t* p = smem_raw;
     uint16_t* a_hi = reinterpret_cast<uint16_t*>(p);
-    p += (size_t)kM * K * 2;
+    p += (size_t)kM * a.kmax * 2;
     uint16_t* a_lo = reinterpret_cast<uint16_t*>(p);
-    p += (size_t)kM * K * 2;
-    uint8_t* strip_hi[2] = {p, p + strip_bytes};
-    p += 2 * (size_t)strip_bytes;
-    uint8_t* strip_lo[2] = {p, p + strip_bytes};
-    p += 2 * (size_t)strip_bytes;
+    p += (size_t)kM * a.kmax * 2;
+    uint8_t* strip_hi[2] = {p, p + strip_cap};
+    p += 2 * (size_t)strip_cap;
+    uint8_t* strip_lo[2] = {p, p + strip_cap};
+    p += 2 * (size_t)strip_cap;
     p = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
     float* stage = reinterpret_cast<float*>(p);  // [8 epilogue warps][32][kStageLd] or [8][4 KB swizzled]
     p += (size_t)8 * 32 * kStageLd * sizeof(float);
     SmemCtl* ctl = reinterpret_cast<SmemCtl*>(p);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int n_time_tiles = (a.n + kN - 1) / kN;
-    const int tile_begin = blockIdx.x * a.tiles_per_chunk;
-    const int tile_end = min(tile_begin + a.tiles_per_chunk, n_time_tiles);
-    const int ntiles = tile_end - tile_begin;
+    // persistent schedule (ItemIter): this CTA's item count
+    int ntiles = 0;
+    for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x)
+        ntiles += (int)((long long)(c + 1) * a.items / a.nchunks - (long long)c * a.items / a.nchunks);
     volatile int* abort_flag = &ctl->abort_flag;
-    const bool tracing = a.trace != nullptr && blockIdx.x == 0 && blockIdx.y == 0;
+    const bool tracing = a.trace != nullptr && blockIdx.x == 0;
 
     if (tid == 0) {
         mbar_init(&ctl->a_full, 1);
@@ -425,29 +453,54 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
     if (tid == 0) {
         // ================= producer: TMA copies + MMA issue (one thread) ======
         const uint32_t idesc = instr_desc(VARIANT);
-        const uint32_t abytes = (uint32_t)kM * K * 2;
-        auto copy_strip = [&](int i) {
+        // strip of item i: the Kmax strip of its time tile, entered 16 (Kmax - K) bytes in
+        auto copy_strip = [&](int i, const ItemIter& itm) {
             const int bb = i & 1;
-            const size_t g = (size_t)(tile_begin + i) * a.jmax * 128 + strip_off;
-            mbar_arrive_tx(&ctl->strip_full[bb], 2 * strip_bytes);
-            bulk_g2s(strip_hi[bb], a.strips_hi + g, strip_bytes, &ctl->strip_full[bb]);
-            bulk_g2s(strip_lo[bb], a.strips_lo + g, strip_bytes, &ctl->strip_full[bb]);
+            const int Ki = a.tile_k[itm.tile(a)];
+            const uint32_t sb = (uint32_t)(Ki / 8 + kN / 8 - 1) * 128;
+            const size_t g = (size_t)itm.time_tile(a) * a.jmax * 128 + (size_t)(a.kmax - Ki) * 16;
+            mbar_arrive_tx(&ctl->strip_full[bb], 2 * sb);
+            bulk_g2s(strip_hi[bb], a.strips_hi + g, sb, &ctl->strip_full[bb]);
+            bulk_g2s(strip_lo[bb], a.strips_lo + g, sb, &ctl->strip_full[bb]);
         };
-        if (ntiles > 0) {
-            const uint16_t* src = a.packed + a.tile_off[m];
+        int a_mt = -1, a_loads = 0;
+        auto load_a = [&](int mt) {
+            const int Km = a.tile_k[mt];
+            const uint32_t abytes = (uint32_t)kM * Km * 2;
+            const uint16_t* src = a.packed + a.tile_off[mt];
             mbar_arrive_tx(&ctl->a_full, 2 * abytes);
             bulk_g2s(a_hi, src, abytes, &ctl->a_full);
-            bulk_g2s(a_lo, src + (size_t)kM * K, abytes, &ctl->a_full);
-            copy_strip(0);
+            bulk_g2s(a_lo, src + (size_t)kM * Km, abytes, &ctl->a_full);
+            a_mt = mt;
+        };
+        bool ok = true;
+        ItemIter cur;
+        cur.start(a, blockIdx.x);
+        if (ntiles > 0) {
+            load_a(cur.tile(a));
+            copy_strip(0, cur);
+            ok = mbar_wait(&ctl->a_full, 0, abort_flag);
+            a_loads = 1;
         }
-        bool ok = ntiles == 0 || mbar_wait(&ctl->a_full, 0, abort_flag);
         for (int i = 0; ok && i < ntiles; ++i) {
             const int b = i & 1;
+            const int mt = cur.tile(a);
             ok = mbar_wait(&ctl->strip_full[b], (i >> 1) & 1, abort_flag);
             if (tracing && i < kTraceTiles) a.trace[i * TR_N + TR_P_STRIP] = now_ns();
             if (ok && i >= 2) ok = mbar_wait(&ctl->acc_empty[b], ((i >> 1) - 1) & 1, abort_flag);
+            if (ok && mt != a_mt) {
+                // new combo tile: every MMA that reads the current A (tile i-1 and
+                // earlier) must have completed before A is overwritten
+                ok = mbar_wait(&ctl->mma_done[(i - 1) & 1], ((i - 1) >> 1) & 1, abort_flag);
+                if (ok) {
+                    load_a(mt);
+                    ok = mbar_wait(&ctl->a_full, a_loads & 1, abort_flag);
+                    ++a_loads;
+                }
+            }
             if (!ok) break;
             if (tracing && i < kTraceTiles) a.trace[i * TR_N + TR_P_ACC] = now_ns();
+            const int K = a.tile_k[mt];
             tc_fence_after();
             const uint32_t d = tmem + (uint32_t)(b * kN);
             const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
@@ -467,9 +520,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
             ctl->issued = i + 1;
             if (tracing && i < kTraceTiles) a.trace[i * TR_N + TR_P_ISSUED] = now_ns();
             // next strip into the other buffer once the MMAs of tile i-1 (its last reader) are done
+            cur.advance(a);
             if (i + 1 < ntiles) {
                 if (i >= 1) ok = mbar_wait(&ctl->mma_done[b ^ 1], ((i - 1) >> 1) & 1, abort_flag);
-                if (ok) copy_strip(i + 1);
+                if (ok) copy_strip(i + 1, cur);
             }
         }
         if (!ok) ctl->abort_flag = 1;
@@ -480,21 +534,28 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
         const int q4 = warp & 3;
         const int half = (warp - 1) >> 2;
         const int r = q4 * 32 + lane;  // accumulator row = combo within tile
-        const int c = m * kM + r;
-        const bool row_ok = c < a.n_combos;
-        const int p = row_ok ? a.periods[c] : 1;
-        const int warm = a.first + p - 1;
-        const float rscale = a.row_scale[(size_t)m * kM + r];
-        const float rsum = a.row_sum[(size_t)m * kM + r];
+        int cur_mt = -1, p = 1, warm = 0, rbase = 0;
+        float rscale = 0.f, rsum = 0.f;
         const bool vec_ok = (a.n & 3) == 0;
         const bool has_nan = a.nanp != nullptr && a.nanp[a.n - 1] > 0.5;
         float* st = TMA_STORE ? reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(stage) + (size_t)(warp - 1) * kStageTma)
                               : stage + (size_t)(warp - 1) * 32 * kStageLd;
-        const int rbase = m * kM + q4 * 32;  // first combo of this warp's rows
-        for (int i = 0; i < ntiles; ++i) {
+        ItemIter it;
+        it.start(a, blockIdx.x);
+        for (int i = 0; i < ntiles; ++i, it.advance(a)) {
             const int b = i & 1;
-            const int g = tile_begin + i;
+            const int mt = it.tile(a);
+            const int g = it.time_tile(a);
             const int t0 = g * kN;
+            if (mt != cur_mt) {
+                cur_mt = mt;
+                const int c = mt * kM + r;
+                p = c < a.n_combos ? a.periods[c] : 1;
+                warm = a.first + p - 1;
+                rscale = a.row_scale[(size_t)mt * kM + r];
+                rsum = a.row_sum[(size_t)mt * kM + r];
+                rbase = mt * kM + q4 * 32;  // first combo of this warp's rows
+            }
             const float ref = __ldg(a.ref + g), xs = __ldg(a.xscale + g);
             // one lane waits, the warp follows (tcgen05.ld is warp-collective)
             int ok = 1;
@@ -635,15 +696,15 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
     const int n_time_tiles = (a.n + kN - 1) / kN;
     const int jmax = kbig / 8 + kN / 8 - 1;
     const size_t strip_tile = (size_t)jmax * 128;
-    // operands in a stream-ordered buffer of their own (the context workspace
-    // holds the caller's weights and periods during this call)
+    // operands in the context's second workspace (the first holds the
+    // caller's weights and periods during this call)
     auto al256 = [](size_t b) { return (b + 255) & ~size_t(255); };
     const size_t total = al256(n_tiles_m * sizeof(int)) + al256(n_tiles_m * sizeof(long long)) +
                          al256((size_t)off * sizeof(uint16_t)) + 2 * al256((size_t)n_tiles_m * kM * sizeof(float)) +
                          2 * al256(strip_tile * n_time_tiles) + 2 * al256(n_time_tiles * sizeof(float)) +
                          al256(sizeof(int));
     void* buf = nullptr;
-    VTA_CUDA_TRY(cudaMallocAsync(&buf, total, st));
+    VTA_TRY(ctx_aux(ctx, total, &buf));
     char* bp = static_cast<char*>(buf);
     auto take = [&](size_t bytes) {
         char* r = bp;
@@ -660,8 +721,8 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
     float* d_ref = reinterpret_cast<float*>(take(n_time_tiles * sizeof(float)));
     float* d_xs = reinterpret_cast<float*>(take(n_time_tiles * sizeof(float)));
     int* d_err = reinterpret_cast<int*>(take(sizeof(int)));
-    VTA_CUDA_TRY(cudaMemcpyAsync(d_tk, tk.data(), n_tiles_m * sizeof(int), cudaMemcpyHostToDevice, st));
-    VTA_CUDA_TRY(cudaMemcpyAsync(d_toff, toff.data(), n_tiles_m * sizeof(long long), cudaMemcpyHostToDevice, st));
+    VTA_TRY(upload_async(ctx, d_tk, tk.data(), n_tiles_m * sizeof(int), st));
+    VTA_TRY(upload_async(ctx, d_toff, toff.data(), n_tiles_m * sizeof(long long), st));
     VTA_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
     PackArgs pa{a.w, a.kmax, a.n_combos, d_tk, d_toff, d_packed, d_rs, d_rsum};
     if (variant == 1) k_pack_a<1><<<n_tiles_m, kM, 0, st>>>(pa);
@@ -701,12 +762,16 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
         VTA_CUDA_TRY(cudaMemsetAsync(d_trace, 0, kTraceTiles * TR_N * 8, st));
     }
     t.trace = d_trace;
-    const int target = ctx->num_sms * 6;
-    int chunks = std::max(1, std::min(n_time_tiles, (target + n_tiles_m - 1) / n_tiles_m));
-    t.tiles_per_chunk = (n_time_tiles + chunks - 1) / chunks;
-    chunks = (n_time_tiles + t.tiles_per_chunk - 1) / t.tiles_per_chunk;
-    dim3 grid(chunks, n_tiles_m);
-    if (n_tiles_m > 65535) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "tcgen05 path: too many combo tiles");
+    // persistent: one CTA per SM (the shared memory allows one); the items are
+    // cut into grid * k chunks of ~24 items that the CTAs take round-robin
+    const long long items = (long long)n_tiles_m * n_time_tiles;
+    if (items > INT32_MAX / 2) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "tcgen05 path: too many tiles");
+    const int G = (int)std::min<long long>(items, ctx->num_sms);
+    const int k = std::max(1, (int)std::llround((double)items / ((double)G * 24.0)));
+    t.n_time_tiles = n_time_tiles;
+    t.items = (int)items;
+    t.nchunks = G * k;
+    dim3 grid((unsigned)G);
     // TMA store path when rows are 16-byte aligned (len % 4 == 0); st.global otherwise
     CUtensorMap tmap;
     std::memset(&tmap, 0, sizeof tmap);
@@ -739,14 +804,13 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
     int err = 0;
     VTA_CUDA_TRY(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     VTA_CUDA_TRY(cudaStreamSynchronize(st));
-    cudaFreeAsync(buf, st);
     if (d_trace) {
         std::vector<unsigned long long> h(kTraceTiles * TR_N);
         cudaMemcpy(h.data(), d_trace, h.size() * 8, cudaMemcpyDeviceToHost);
         cudaFree(d_trace);
         const unsigned long long t0 = h[0];
         std::fprintf(stderr, "tc trace (ns): tile strip_in acc_free issued e_start e_end\n");
-        for (int i = 0; i < std::min(kTraceTiles, t.tiles_per_chunk); ++i) {
+        for (int i = 0; i < std::min<long long>(kTraceTiles, items / grid.x); ++i) {
             std::fprintf(stderr, "%3d", i);
             for (int e = 0; e < 5; ++e)
                 std::fprintf(stderr, " %8lld", h[i * TR_N + e] ? (long long)(h[i * TR_N + e] - t0) : -1LL);

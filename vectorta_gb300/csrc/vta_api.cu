@@ -274,10 +274,39 @@ static int pick_chunk(vta_ctx* ctx, int n, int lanes) {
     return (int)len;
 }
 
-static vta_status upload(vta_ctx* ctx, void* dst, const void* src, size_t bytes) {
+vta_status upload_async(vta_ctx* ctx, void* dst, const void* src, size_t bytes, cudaStream_t st) {
     if (!bytes) return VTA_OK;
-    VTA_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    const size_t off = (ctx->host_stage_off + 255) & ~size_t(255);
+    if (ctx->host_stage && off + bytes <= ctx->host_stage_bytes) {
+        // the staging region is not reused before this call's final synchronize
+        char* h = static_cast<char*>(ctx->host_stage) + off;
+        std::memcpy(h, src, bytes);
+        ctx->host_stage_off = off + bytes;
+        VTA_CUDA_TRY(cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, st));
+        return VTA_OK;
+    }
+    VTA_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
     return VTA_OK;
+}
+
+vta_status ctx_aux(vta_ctx* ctx, size_t bytes, void** out) {
+    if (bytes > ctx->aux_bytes) {
+        if (ctx->aux) {
+            VTA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+            cudaFree(ctx->aux);
+            ctx->aux = nullptr;
+            ctx->aux_bytes = 0;
+        }
+        VTA_TRY(vram_check(bytes));
+        VTA_CUDA_TRY(cudaMalloc(&ctx->aux, bytes));
+        ctx->aux_bytes = bytes;
+    }
+    *out = ctx->aux;
+    return VTA_OK;
+}
+
+static vta_status upload(vta_ctx* ctx, void* dst, const void* src, size_t bytes) {
+    return upload_async(ctx, dst, src, bytes, ctx->stream);
 }
 
 static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, size_t first,
@@ -656,6 +685,7 @@ static vta_status check_ctx(vta_ctx* ctx) {
     VTA_CUDA_TRY(cudaSetDevice(ctx->device));
     g_cur = ctx;
     ctx->timed = false;
+    ctx->host_stage_off = 0;  // the previous call has synchronised
     return VTA_OK;
 }
 
@@ -934,6 +964,12 @@ vta_status vta_ctx_create(int device_id, vta_ctx** out) {
         delete c;
         return cuda_fail(e, "cudaStreamCreate");
     }
+    if (cudaHostAlloc(&c->host_stage, size_t(1) << 20, cudaHostAllocDefault) == cudaSuccess) {
+        c->host_stage_bytes = size_t(1) << 20;
+    } else {
+        c->host_stage = nullptr;  // uploads fall back to pageable copies
+        cudaGetLastError();
+    }
     const char* pol = std::getenv("VTA_WMA_BATCH");
     if (pol) vta_ctx_set_policy(c, "wma_batch", pol);
     *out = c;
@@ -945,6 +981,8 @@ vta_status vta_ctx_destroy(vta_ctx* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->aux) cudaFree(ctx->aux);
+    if (ctx->host_stage) cudaFreeHost(ctx->host_stage);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (g_cur == ctx) g_cur = nullptr;

@@ -65,6 +65,11 @@ struct vta_ctx {
     bool own_stream = true;
     void* scratch = nullptr;  // growing device workspace, owned by the ctx
     size_t scratch_bytes = 0;
+    void* aux = nullptr;      // second growing device workspace (operands a launcher
+    size_t aux_bytes = 0;     // builds after the call's arena pieces are taken)
+    void* host_stage = nullptr;  // pinned staging of small uploads, reused per call
+    size_t host_stage_bytes = 0;
+    size_t host_stage_off = 0;
     vta::Policy policy;
     std::string last_kernel;
     bool timing = false;
@@ -96,6 +101,13 @@ class Arena {
     size_t total_ = 0;
     size_t off_ = 0;
 };
+
+// Device workspace of at least `bytes` in ctx->aux (grown with cudaMalloc;
+// valid until the next ctx_aux call on the same context).
+vta_status ctx_aux(vta_ctx* ctx, size_t bytes, void** out);
+// Host -> device copy on `st`, staged through the context's pinned buffer when
+// it fits (the copy is then fully asynchronous), else a pageable copy.
+vta_status upload_async(vta_ctx* ctx, void* dst, const void* src, size_t bytes, cudaStream_t st);
 
 // VRAM admission check mirroring the crate's wrappers: required + 64 MiB
 // headroom must fit in free memory (disabled with VTA_MEM_CHECK=0).
