@@ -94,6 +94,19 @@ INDICATORS = {
 }
 N_IN = {"x": 1, "hl": 2, "hlc": 3}
 
+
+# many-series plans (vta_tm_job / vta_tm_plan_info)
+class TmJobC(C.Structure):
+    _fields_ = [("kind", C.c_int), ("period", C.c_size_t), ("param", C.c_double),
+                ("d_out0", C.c_void_p), ("d_out1", C.c_void_p)]
+
+
+class TmPlanInfoC(C.Structure):
+    _fields_ = [("n_items", C.c_size_t), ("chunk", C.c_size_t * 8), ("fixups", C.c_size_t), ("tuned", C.c_int)]
+
+
+TM_KINDS = {"atr": 0, "adx": 1, "supertrend": 2, "percentile_nearest_rank": 3}
+
 _lib = None
 
 
@@ -155,6 +168,12 @@ def lib() -> C.CDLL:
         for suffix in ("expand_grid", "batch_dev", "batch_device", "batch_into_host_f32",
                        "many_series_one_param_time_major_dev", "many_series_one_param_device"):
             getattr(L, f"vta_{name}_{suffix}").restype = st
+    L.vta_tm_plan_create.argtypes = [vp, vp, vp, vp, sz, sz, C.POINTER(sz), C.POINTER(TmJobC), sz, C.POINTER(vp)]
+    L.vta_tm_plan_run.argtypes = [vp]
+    L.vta_tm_plan_info_get.argtypes = [vp, C.POINTER(TmPlanInfoC)]
+    L.vta_tm_plan_destroy.argtypes = [vp]
+    for fn in ("vta_tm_plan_create", "vta_tm_plan_run", "vta_tm_plan_info_get", "vta_tm_plan_destroy"):
+        getattr(L, fn).restype = st
     L.vta_sma_batch_device_noalloc.argtypes = [vp, vp, sz, sz, C.POINTER(SWEEPS["period"]), vp]
     L.vta_sma_batch_device_noalloc.restype = st
     for fn in ("vta_ctx_create", "vta_ctx_destroy", "vta_ctx_synchronize", "vta_ctx_set_stream",

@@ -118,6 +118,8 @@ void* vta_ctx_get_stream(vta_ctx* ctx);
 /* CudaXPolicy / set_policy (alma_wrapper.rs:18-70): keys
  *   "wma_batch"   = "auto" | "plain" | "tc_fp16x3" | "tc_bf16x3"
  *   "recur_chunk" = "auto" | "sequential" | <positive multiple of 32>
+ *   "tm_chunk"    = "auto" | "sequential" | <steps>   (many-series plans)
+ *   "tm_warm"     = "auto" | <steps>                  (many-series plans)
  *   "timing"      = "on" | "off"                                         */
 vta_status vta_ctx_set_policy(vta_ctx* ctx, const char* key, const char* value);
 /* selected_batch_kernel() (alma_wrapper.rs:239-245): name of the last kernel
@@ -204,6 +206,50 @@ for (name, wf, kind, outs, rng, prm, cites) in IND:
     w(f"/* {name}_many_series_one_param_device ({cite}) */")
     w(f"vta_status vta_{name}_many_series_one_param_device(vta_ctx* ctx, {', '.join(inputs(kind, True, True))},\n    size_t cols, size_t rows, const {P}* params, {outs_d});")
     w("")
+w("""/* ==== many-series work-list plans ====
+ * No counterpart in the crate, whose many-series entry points run one
+ * indicator per call over a rectangular time-major matrix.  A plan runs
+ * several indicators over one set of time-major OHLC series [rows][cols]
+ * whose lengths differ: series s has lengths[s] <= rows valid rows (rows
+ * past it are neither read nor written, in inputs and outputs alike).  All
+ * jobs run in one persistent launch over a work list of (job, 32 series,
+ * time chunk) items, captured once in a CUDA graph at creation and replayed
+ * by vta_tm_plan_run.  The time-chunk length of each job is picked by timing
+ * candidates on the plan's own data at creation (cached per indicator,
+ * period, length and series count for the process); the context policies
+ * "tm_chunk" and "tm_warm" override it.  Results are bit-identical to one
+ * sequential pass per series (the chunking is verified and repaired on the
+ * device), and per cell they follow the crate's many-series semantics:
+ *   ATR    atr.rs:329-460             out0 = atr            (period = length)
+ *   ADX    adx.rs:299-421             out0 = adx
+ *   ST     supertrend.rs:457-550      out0 = trend, out1 = changed (param = factor)
+ *   PNR    percentile_nearest_rank.rs:190-266 on close, out0 (period = length
+ *          <= 64, param = percentage)
+ * The input and output buffers are bound at creation; to run on new data,
+ * write it into the same buffers and call vta_tm_plan_run again. */
+typedef enum vta_tm_kind { VTA_TM_ATR = 0, VTA_TM_ADX = 1, VTA_TM_SUPERTREND = 2, VTA_TM_PERCENTILE = 3 } vta_tm_kind;
+typedef struct vta_tm_job {
+    int kind;          /* vta_tm_kind */
+    size_t period;
+    double param;      /* SuperTrend factor / percentile percentage; else 0 */
+    float* d_out0;     /* [rows][cols] device */
+    float* d_out1;     /* SuperTrend changed [rows][cols]; else NULL */
+} vta_tm_job;
+typedef struct vta_tm_plan vta_tm_plan;
+typedef struct vta_tm_plan_info {
+    size_t n_items;      /* work items of one run */
+    size_t chunk[8];     /* time-chunk length per job (first 8 jobs) */
+    size_t fixups;       /* chunks recomputed by the last run's verification */
+    int tuned;           /* 1 if the chunk lengths were timed at creation */
+} vta_tm_plan_info;
+/* lengths: host array of cols series lengths, or NULL (every series has rows). */
+vta_status vta_tm_plan_create(vta_ctx* ctx, const float* d_high, const float* d_low, const float* d_close,
+    size_t cols, size_t rows, const size_t* lengths, const vta_tm_job* jobs, size_t n_jobs, vta_tm_plan** out);
+/* Replays the plan's graph on the context stream; synchronous. */
+vta_status vta_tm_plan_run(vta_tm_plan* plan);
+vta_status vta_tm_plan_info_get(const vta_tm_plan* plan, vta_tm_plan_info* info);
+vta_status vta_tm_plan_destroy(vta_tm_plan* plan);
+""")
 w("""/* ==== sma without device allocation ====
  * No counterpart in the crate: its wrappers allocate device memory on every
  * call (sma_batch_dev_from_device, sma_wrapper.rs:830-841, allocates the

@@ -1,0 +1,517 @@
+// Many-series work-list kernels: several indicators over one set of ragged
+// time-major OHLC series in one persistent launch.
+//
+// Work items are (job, tile of 32 consecutive series, time chunk).  A warp
+// takes items from a global counter; lane l of the warp owns series
+// 32 * tile + l, so every load and store of a time step is one coalesced
+// 128-byte row segment.  Series of uneven length stop at their own length:
+// cells past it are neither read nor written.
+//
+// Recurrent jobs (ATR, ADX, SuperTrend) are cut into time chunks with a
+// verified warm restart.  Chunk k (c0 = k * chunk) that starts past the
+// indicator's seeding phase runs `warm` steps before c0 from a state guessed
+// from the inputs; since every state component decays by (1 - 1/p) per step
+// the guess is forgotten, and the state it reaches at c0 is recorded.  Every
+// chunk also records its state at its end.  k_tm_fixup then walks each
+// series' chunks in order and compares (bit for bit) the recorded start state
+// of chunk k with the end state of chunk k - 1; where they differ it recomputes
+// chunk k from that exact end state.  The outputs are therefore bit-identical
+// to one sequential pass over the series, whatever the chunk and warm lengths.
+// The percentile job is exact per chunk by construction (its window is
+// rebuilt from the `length` inputs before c0).
+#include <cfloat>
+
+#include "vta_internal.h"
+#include "vta_plan.h"
+
+namespace vta {
+namespace {
+
+constexpr int kPlanWarps = 4;
+__device__ __forceinline__ float qnan() { return __int_as_float(0x7fc00000); }
+
+struct TmIn {
+    const float *h, *l, *c;
+    size_t cols, s;
+    __device__ float H(int t) const { return __ldg(h + (size_t)t * cols + s); }
+    __device__ float L(int t) const { return __ldg(l + (size_t)t * cols + s); }
+    __device__ float C(int t) const { return __ldg(c + (size_t)t * cols + s); }
+};
+
+// True range with the crate's NaN-skipping comparisons (atr.rs:352-366).
+__device__ __forceinline__ float true_range(float hi, float lo, float pc) {
+    float tr = hi - lo;
+    const float hc = fabsf(hi - pc);
+    if (hc > tr) tr = hc;
+    const float lc = fabsf(lo - pc);
+    if (lc > tr) tr = lc;
+    return tr;
+}
+
+// Op interface (lane-level, one series):
+//   init(job, f)                 constants; f = first valid index
+//   run_from() -> int            first t whose entering state is a running
+//                                state (everything before is seeding)
+//   start_exact()                state entering t = f
+//   start_warm(in, t0)           guessed running state entering t0 > run_from()
+//   load(w, in, t0)              exact running state entering t0 from 8 words
+//   save(w)                      running state as 8 words
+//   step(in, t, o1) -> o0        process t (any phase), outputs for t
+//
+// ATR: atr_compute_into_scalar (atr.rs:329-460); TR(f) = h - l, seed = mean
+// of the first p TRs at s = f + p - 1, then rma = fma(-a, rma, rma) + a * tr.
+struct PAtr {
+    static constexpr bool kTwo = false;
+    int p, f;
+    float alpha, rma, pc;
+    double tr_sum;
+    __device__ void init(const PlanJob& j, int first) {
+        p = j.period;
+        f = first;
+        alpha = (float)(1.0 / (double)p);
+    }
+    __device__ int run_from() const { return f + p; }
+    __device__ void start_exact() { tr_sum = 0.0; rma = 0.f; pc = 0.f; }
+    __device__ void start_warm(const TmIn& in, int t0) {
+        pc = in.C(t0 - 1);
+        rma = in.H(t0 - 1) - in.L(t0 - 1);
+    }
+    __device__ void load(const float* w, const TmIn& in, int t0) {
+        rma = w[0];
+        pc = in.C(t0 - 1);
+    }
+    __device__ void save(float* w) const {
+        w[0] = rma;
+        w[1] = w[2] = w[3] = w[4] = w[5] = w[6] = w[7] = 0.f;
+    }
+    __device__ float step(const TmIn& in, int t, float&) {
+        if (t < f) return qnan();
+        const float hi = in.H(t), lo = in.L(t), cl = in.C(t);
+        const float tr = (t == f) ? hi - lo : true_range(hi, lo, pc);
+        pc = cl;
+        const int s = f + p - 1;
+        if (t < s) {
+            tr_sum += (double)tr;
+            return qnan();
+        }
+        if (t == s) {
+            tr_sum += (double)tr;
+            rma = (float)(tr_sum / (double)p);
+            return rma;
+        }
+        rma = fmaf(-alpha, rma, rma) + alpha * tr;
+        return rma;
+    }
+};
+
+// ADX: adx_scalar on the slice from f (adx.rs:299-421): Wilder sums over
+// relative indices 1..=p, DX from the smoothed DM/TR, ADX = mean of the
+// first p DX, then (adx * (p - 1) + dx) / p; first output at f + 2p - 1.
+// The arithmetic is the sequential time-major kernel's (k_adx).
+struct PAdx {
+    static constexpr bool kTwo = false;
+    int p, f, dx_count;
+    float rp, omr, pm1;
+    float atr, pdm, mdm, dx_sum, adx, ph, pl, pc;
+    __device__ void init(const PlanJob& j, int first) {
+        p = j.period;
+        f = first;
+        rp = (float)(1.0 / (double)p);
+        omr = (float)(1.0 - 1.0 / (double)p);
+        pm1 = (float)p - 1.f;
+    }
+    __device__ int run_from() const { return f + 2 * p; }
+    __device__ void start_exact() {
+        atr = pdm = mdm = dx_sum = adx = ph = pl = pc = 0.f;
+        dx_count = 0;
+    }
+    __device__ void prev_inputs(const TmIn& in, int t0) {
+        ph = in.H(t0 - 1);
+        pl = in.L(t0 - 1);
+        pc = in.C(t0 - 1);
+    }
+    __device__ void start_warm(const TmIn& in, int t0) {
+        prev_inputs(in, t0);
+        atr = (float)p * (ph - pl);
+        pdm = mdm = 0.f;
+        adx = 0.f;
+        dx_count = p;
+    }
+    __device__ void load(const float* w, const TmIn& in, int t0) {
+        atr = w[0]; pdm = w[1]; mdm = w[2]; adx = w[3];
+        dx_count = p;
+        prev_inputs(in, t0);
+    }
+    __device__ void save(float* w) const {
+        w[0] = atr; w[1] = pdm; w[2] = mdm; w[3] = adx;
+        w[4] = w[5] = w[6] = w[7] = 0.f;
+    }
+    __device__ float dx_now() const {
+        float pdi = 0.f, mdi = 0.f;
+        if (atr != 0.f) { pdi = (pdm / atr) * 100.f; mdi = (mdm / atr) * 100.f; }
+        const float sdi = pdi + mdi;
+        return sdi != 0.f ? (fabsf(pdi - mdi) / sdi) * 100.f : 0.f;
+    }
+    __device__ float step(const TmIn& in, int t, float&) {
+        if (t < f) return qnan();
+        const float ch = in.H(t), cl = in.L(t), cc = in.C(t);
+        const int r = t - f;
+        float v = qnan();
+        if (r > 0) {
+            const float tr = fmaxf(fmaxf(ch - cl, fabsf(ch - pc)), fabsf(cl - pc));
+            const float up = ch - ph, down = pl - cl;
+            const float dp = (up > down && up > 0.f) ? up : 0.f;
+            const float dm = (down > up && down > 0.f) ? down : 0.f;
+            if (r <= p) {
+                atr += tr; pdm += dp; mdm += dm;
+                if (r == p) {
+                    dx_sum = dx_now();
+                    dx_count = 1;
+                }
+            } else {
+                atr = atr * omr + tr;
+                pdm = pdm * omr + dp;
+                mdm = mdm * omr + dm;
+                const float dx = dx_now();
+                if (dx_count < p) {
+                    dx_sum += dx;
+                    dx_count += 1;
+                    if (dx_count == p) { adx = dx_sum * rp; v = adx; }
+                } else {
+                    adx = (adx * pm1 + dx) * rp;
+                    v = adx;
+                }
+            }
+        }
+        ph = ch; pl = cl; pc = cc;
+        return v;
+    }
+};
+
+// SuperTrend: supertrend_scalar (supertrend.rs:457-550) with the ATR of the
+// slice from f computed inline; outputs trend and changed, first at f + p - 1.
+// The arithmetic is the sequential time-major kernel's (k_supertrend).
+struct PSuperTrend {
+    static constexpr bool kTwo = true;
+    int p, f;
+    float alpha, fac, atr, pub, plb, last_close, pc;
+    bool upper;
+    double tr_sum;
+    __device__ void init(const PlanJob& j, int first) {
+        p = j.period;
+        f = first;
+        alpha = (float)(1.0 / (double)p);
+        fac = j.param;
+    }
+    __device__ int run_from() const { return f + p; }
+    __device__ void start_exact() {
+        tr_sum = 0.0;
+        atr = pub = plb = last_close = pc = 0.f;
+        upper = false;
+    }
+    __device__ void start_warm(const TmIn& in, int t0) {
+        const float hi = in.H(t0 - 1), lo = in.L(t0 - 1), cl = in.C(t0 - 1);
+        atr = hi - lo;
+        const float hl2 = (hi + lo) * 0.5f;
+        pub = hl2 + fac * atr;
+        plb = hl2 - fac * atr;
+        last_close = pc = cl;
+        upper = cl <= pub;
+    }
+    __device__ void load(const float* w, const TmIn& in, int t0) {
+        atr = w[0]; pub = w[1]; plb = w[2];
+        upper = w[3] != 0.f;
+        last_close = pc = in.C(t0 - 1);
+    }
+    __device__ void save(float* w) const {
+        w[0] = atr; w[1] = pub; w[2] = plb; w[3] = upper ? 1.f : 0.f;
+        w[4] = w[5] = w[6] = w[7] = 0.f;
+    }
+    __device__ float step(const TmIn& in, int t, float& v1) {
+        v1 = qnan();
+        if (t < f) return qnan();
+        const float hi = in.H(t), lo = in.L(t), cl = in.C(t);
+        float tr = hi - lo;
+        if (t != f) {
+            const float hc = fabsf(hi - pc);
+            if (hc > tr) tr = hc;
+            const float lc = fabsf(lo - pc);
+            if (lc > tr) tr = lc;
+        }
+        pc = cl;
+        const int warm = f + p - 1;
+        float v0 = qnan();
+        if (t < warm) {
+            tr_sum += (double)tr;
+        } else if (t == warm) {
+            tr_sum += (double)tr;
+            atr = (float)(tr_sum / (double)p);
+            const float hl2 = (hi + lo) * 0.5f;
+            pub = hl2 + fac * atr;
+            plb = hl2 - fac * atr;
+            last_close = cl;
+            if (cl <= pub) { v0 = pub; upper = true; }
+            else { v0 = plb; upper = false; }
+            v1 = 0.f;
+        } else {
+            atr = fmaf(-alpha, atr, atr) + alpha * tr;
+            const float hl2 = (hi + lo) * 0.5f;
+            const float ub = fmaf(fac, atr, hl2);
+            const float lb = fmaf(-fac, atr, hl2);
+            float cub = ub, clb = lb;
+            if (last_close <= pub) cub = fminf(cub, pub);
+            if (last_close >= plb) clb = fmaxf(clb, plb);
+            if (upper) {
+                if (cl <= cub) { v0 = cub; v1 = 0.f; }
+                else { v0 = clb; v1 = 1.f; upper = false; }
+            } else {
+                if (cl >= clb) { v0 = clb; v1 = 0.f; }
+                else { v0 = cub; v1 = 1.f; upper = true; }
+            }
+            pub = cub; plb = clb; last_close = cl;
+        }
+        return v0;
+    }
+};
+
+// ------------------------------------------------ nearest-rank percentile ---
+// percentile_nearest_rank over a window of `len` values (NaN excluded),
+// out = sorted[k], k = round(p * wl) - 1 clamped (percentile_nearest_rank.rs:
+// 190-266).  The sorted window lives in W registers padded with +inf; insertion
+// and removal are branch-free compare/select passes with constant indices.
+__device__ __forceinline__ int pnr_rank(double pf, int wl) {
+    const long long raw = (long long)round(fma(pf, (double)wl, 0.0)) - 1;
+    const int k = raw <= 0 ? 0 : (int)raw;
+    return k >= wl ? wl - 1 : k;
+}
+template <int W>
+__device__ __forceinline__ void reg_insert(float (&w)[W], float v) {
+#pragma unroll
+    for (int i = W - 1; i > 0; --i) w[i] = (w[i] < v) ? w[i] : ((w[i - 1] < v) ? v : w[i - 1]);
+    w[0] = (w[0] < v) ? w[0] : v;
+}
+// removes one element equal to v (v is in the window)
+template <int W>
+__device__ __forceinline__ void reg_remove(float (&w)[W], float v) {
+#pragma unroll
+    for (int i = 0; i < W - 1; ++i) w[i] = (w[i] < v) ? w[i] : w[i + 1];
+    w[W - 1] = (w[W - 1] < v) ? w[W - 1] : __int_as_float(0x7f800000);
+}
+template <int W>
+__device__ void pnr_chunk(const TmIn& in, int f, int len, double pf, int c0, int c1, float* out,
+                          size_t cols, size_t s) {
+    const int start = f + len - 1;
+    int t = c0;
+    for (; t < c1 && t < start; ++t) out[(size_t)t * cols + s] = qnan();
+    if (t >= c1) return;
+    float w[W];
+#pragma unroll
+    for (int i = 0; i < W; ++i) w[i] = __int_as_float(0x7f800000);
+    int wl = 0;
+    for (int j = t - len + 1; j <= t; ++j) {
+        const float v = in.C(j);
+        if (!isnan(v)) {
+            reg_insert(w, v);
+            ++wl;
+        }
+    }
+    const int kfull = pnr_rank(pf, len);
+    for (;;) {
+        const int k = wl == len ? kfull : (wl > 0 ? pnr_rank(pf, wl) : 0);
+        float r = w[0];
+#pragma unroll
+        for (int i = 1; i < W; ++i) r = (i == k) ? w[i] : r;
+        out[(size_t)t * cols + s] = wl > 0 ? r : qnan();
+        if (t + 1 >= c1) break;
+        const float vo = in.C(t + 1 - len);
+        if (!isnan(vo)) {
+            reg_remove(w, vo);
+            --wl;
+        }
+        const float vi = in.C(t + 1);
+        if (!isnan(vi)) {
+            reg_insert(w, vi);
+            ++wl;
+        }
+        ++t;
+    }
+}
+
+// ------------------------------------------------ chunk runners -------------
+template <class Op>
+__device__ void run_chunk(const PlanArgs& a, const PlanJob& J, int s, int k) {
+    const int L = a.len[s];
+    const int c0 = k * J.chunk;
+    if (c0 >= L) return;
+    const int c1 = min(c0 + J.chunk, L);
+    const int f = a.first_hlc[s];
+    Op op;
+    op.init(J, f);
+    const TmIn in{a.h, a.l, a.c, (size_t)a.cols, (size_t)s};
+    const size_t sidx = (size_t)k * a.cols + s;
+    int t;
+    bool exact = true;
+    if (k > 0 && f < L && c0 - J.warm >= op.run_from()) {
+        t = c0 - J.warm;
+        op.start_warm(in, t);
+        exact = false;
+    } else {
+        t = min(f, c0);
+        op.start_exact();
+    }
+    float o1;
+    for (; t < c0; ++t) op.step(in, t, o1);
+    float w[8];
+    if (k > 0) {
+        op.save(w);
+        float4* d = reinterpret_cast<float4*>(J.st_start + sidx * 8);
+        d[0] = make_float4(w[0], w[1], w[2], w[3]);
+        d[1] = make_float4(w[4], w[5], w[6], w[7]);
+        J.exact[sidx] = exact ? 1 : 0;
+    }
+    for (; t < c1; ++t) {
+        const float o0 = op.step(in, t, o1);
+        J.out0[(size_t)t * a.cols + s] = o0;
+        if (Op::kTwo) J.out1[(size_t)t * a.cols + s] = o1;
+    }
+    op.save(w);
+    float4* d = reinterpret_cast<float4*>(J.st_end + sidx * 8);
+    d[0] = make_float4(w[0], w[1], w[2], w[3]);
+    d[1] = make_float4(w[4], w[5], w[6], w[7]);
+}
+
+__device__ void run_pnr(const PlanArgs& a, const PlanJob& J, int s, int k) {
+    const int L = a.len[s];
+    const int c0 = k * J.chunk;
+    if (c0 >= L) return;
+    const int c1 = min(c0 + J.chunk, L);
+    const TmIn in{a.h, a.l, a.c, (size_t)a.cols, (size_t)s};
+    const int f = a.first_c[s];
+    if (J.period <= 16) pnr_chunk<16>(in, f, J.period, J.pfrac, c0, c1, J.out0, a.cols, s);
+    else if (J.period <= 32) pnr_chunk<32>(in, f, J.period, J.pfrac, c0, c1, J.out0, a.cols, s);
+    else pnr_chunk<64>(in, f, J.period, J.pfrac, c0, c1, J.out0, a.cols, s);
+}
+
+// Persistent work-list kernel: each warp takes items until the list is done.
+__global__ void __launch_bounds__(kPlanWarps * 32) k_tm_plan(PlanArgs a) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int it = 0;
+        if (lane == 0) it = atomicAdd(a.counter, 1);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= a.n_items) break;
+        const int4 w = a.items[it];
+        const int s = w.y * 32 + lane;
+        if (s >= a.cols) continue;
+        const PlanJob& J = a.jobs[w.x];
+        switch (J.kind) {
+            case PJ_ATR: run_chunk<PAtr>(a, J, s, w.z); break;
+            case PJ_ADX: run_chunk<PAdx>(a, J, s, w.z); break;
+            case PJ_SUPERTREND: run_chunk<PSuperTrend>(a, J, s, w.z); break;
+            default: run_pnr(a, J, s, w.z); break;
+        }
+    }
+}
+
+// Fix-up: per (recurrent job, series), chunks in order; a warm-restarted
+// chunk whose recorded start state differs from the previous chunk's end
+// state is recomputed from that end state.
+template <class Op>
+__device__ void fixup_series(const PlanArgs& a, const PlanJob& J, int s) {
+    const int L = a.len[s];
+    const TmIn in{a.h, a.l, a.c, (size_t)a.cols, (size_t)s};
+    for (int k = 1; k * J.chunk < L; ++k) {
+        const size_t sidx = (size_t)k * a.cols + s;
+        if (J.exact[sidx]) continue;
+        const size_t pidx = sidx - a.cols;
+        const uint4* ps = reinterpret_cast<const uint4*>(J.st_start + sidx * 8);
+        const uint4* pe = reinterpret_cast<const uint4*>(J.st_end + pidx * 8);
+        const uint4 s0 = ps[0], s1 = ps[1], e0 = pe[0], e1 = pe[1];
+        if (s0.x == e0.x && s0.y == e0.y && s0.z == e0.z && s0.w == e0.w && s1.x == e1.x && s1.y == e1.y &&
+            s1.z == e1.z && s1.w == e1.w)
+            continue;
+        const int c0 = k * J.chunk;
+        const int c1 = min(c0 + J.chunk, L);
+        Op op;
+        op.init(J, a.first_hlc[s]);
+        const float* we = J.st_end + pidx * 8;
+        float w[8];
+        for (int i = 0; i < 8; ++i) w[i] = we[i];
+        op.load(w, in, c0);
+        float o1;
+        for (int t = c0; t < c1; ++t) {
+            const float o0 = op.step(in, t, o1);
+            J.out0[(size_t)t * a.cols + s] = o0;
+            if (Op::kTwo) J.out1[(size_t)t * a.cols + s] = o1;
+        }
+        op.save(w);
+        float4* d = reinterpret_cast<float4*>(J.st_end + sidx * 8);
+        d[0] = make_float4(w[0], w[1], w[2], w[3]);
+        d[1] = make_float4(w[4], w[5], w[6], w[7]);
+        atomicAdd(&a.stats[0], 1);
+    }
+}
+
+__global__ void k_tm_fixup(PlanArgs a) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = (int)(g / a.cols), s = (int)(g % a.cols);
+    if (j >= a.n_jobs) return;
+    const PlanJob& J = a.jobs[j];
+    switch (J.kind) {
+        case PJ_ATR: fixup_series<PAtr>(a, J, s); break;
+        case PJ_ADX: fixup_series<PAdx>(a, J, s); break;
+        case PJ_SUPERTREND: fixup_series<PSuperTrend>(a, J, s); break;
+        default: break;
+    }
+}
+
+// First valid index per series within its own length: close alone and
+// high, low and close together (len[s] when there is none).
+__global__ void k_plan_first(PlanArgs a, int* first_hlc, int* first_c) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.cols) return;
+    const int L = a.len[s];
+    const TmIn in{a.h, a.l, a.c, (size_t)a.cols, (size_t)s};
+    int fc = L, fh = L;
+    for (int t = 0; t < L; ++t) {
+        const float cl = in.C(t);
+        if (isnan(cl)) continue;
+        if (fc == L) fc = t;
+        if (!isnan(in.H(t)) && !isnan(in.L(t))) {
+            fh = t;
+            break;
+        }
+    }
+    first_c[s] = fc;
+    first_hlc[s] = fh;
+}
+
+}  // namespace
+
+vta_status launch_plan_first(const PlanArgs& a, int* first_hlc, int* first_c, cudaStream_t st) {
+    k_plan_first<<<(a.cols + 127) / 128, 128, 0, st>>>(a, first_hlc, first_c);
+    return check_launch("k_plan_first");
+}
+
+int tm_plan_blocks(int num_sms) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tm_plan, kPlanWarps * 32, 0) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    return num_sms * per_sm;
+}
+
+vta_status launch_tm_plan(const PlanArgs& a, int blocks, cudaStream_t st) {
+    k_tm_plan<<<blocks, kPlanWarps * 32, 0, st>>>(a);
+    return check_launch("k_tm_plan");
+}
+
+vta_status launch_tm_fixup(const PlanArgs& a, cudaStream_t st) {
+    const long long n = (long long)a.n_jobs * a.cols;
+    k_tm_fixup<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(a);
+    return check_launch("k_tm_fixup");
+}
+
+}  // namespace vta

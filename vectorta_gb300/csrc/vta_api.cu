@@ -1051,6 +1051,20 @@ vta_status vta_ctx_set_policy(vta_ctx* ctx, const char* key, const char* value) 
         }
         return VTA_OK;
     }
+    if (k == "tm_chunk" || k == "tm_warm") {
+        // many-series plans: time-chunk length ("sequential" = one chunk per
+        // series) and warm-restart steps; "auto" = timed / derived
+        int& dst = k == "tm_chunk" ? ctx->policy.tm_chunk : ctx->policy.tm_warm;
+        if (v == "auto") dst = 0;
+        else if (k == "tm_chunk" && v == "sequential") dst = -1;
+        else {
+            char* end = nullptr;
+            long x = std::strtol(v.c_str(), &end, 10);
+            if (!end || *end || x < 1 || x > (1L << 30)) return fail(VTA_ERR_INVALID_POLICY, (k + ": positive integer").c_str());
+            dst = (int)x;
+        }
+        return VTA_OK;
+    }
     return fail(VTA_ERR_INVALID_POLICY, "unknown policy key");
 }
 

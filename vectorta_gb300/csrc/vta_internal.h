@@ -52,6 +52,10 @@ struct Policy {
     // recurrence time-chunk length (0 = auto); 1 = whole series (plain
     // sequential per-combo kernel)
     int recur_chunk = 0;
+    // many-series plans: time-chunk length (0 = timed at plan creation,
+    // -1 = one chunk per series) and warm-restart steps (0 = 32 p + 64)
+    int tm_chunk = 0;
+    int tm_warm = 0;
 };
 
 }  // namespace vta

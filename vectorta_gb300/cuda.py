@@ -26,7 +26,7 @@ import numpy as np
 
 from . import _native as N
 
-__all__ = ["DeviceArrayF32", "Context", "VtaError"]
+__all__ = ["DeviceArrayF32", "Context", "VtaError", "TmPlan"]
 VtaError = N.VtaError
 
 
@@ -380,6 +380,57 @@ __all__ += ["AlmaBatchRange", "PeriodBatchRange", "StdDevBatchRange", "ZscoreBat
             "BollingerBandsBatchRange", "SuperTrendBatchRange", "PercentileNearestRankBatchRange",
             "AlmaParams", "PeriodParams", "StdDevParams", "ZscoreParams", "BollingerBandsParams",
             "SuperTrendParams", "PercentileNearestRankParams", "CLASSES", "device_count", "launch_count"]
+
+
+class TmPlan:
+    """Several indicators over ragged time-major OHLC series in one persistent,
+    graph-captured launch (vta_tm_plan_*).
+
+    high/low/close: device [rows][cols] float32 (torch tensors or pointers);
+    lengths: per-series valid rows (None = all rows); jobs: dicts with
+    kind in {"atr", "adx", "supertrend", "percentile_nearest_rank"}, period,
+    param (SuperTrend factor / percentile percentage) and device outputs out0
+    (and out1 for SuperTrend).  The buffers stay bound to the plan.
+    """
+
+    def __init__(self, high, low, close, cols: int, rows: int, lengths, jobs, ctx: "Context | None" = None,
+                 device_id: int = 0):
+        self.ctx = ctx or Context(device_id)
+        self._keep = (high, low, close, jobs)
+        arr = (N.TmJobC * len(jobs))()
+        for i, j in enumerate(jobs):
+            arr[i].kind = N.TM_KINDS[j["kind"]]
+            arr[i].period = int(j["period"])
+            arr[i].param = float(j.get("param", 0.0))
+            arr[i].d_out0 = _dptr(j["out0"])
+            arr[i].d_out1 = _dptr(j["out1"]) if j.get("out1") is not None else None
+        lens = None
+        if lengths is not None:
+            self._lens = (C.c_size_t * cols)(*[int(v) for v in lengths])
+            lens = self._lens
+        h = C.c_void_p()
+        N.check(N.lib().vta_tm_plan_create(self.ctx.handle, _dptr(high), _dptr(low), _dptr(close), int(cols),
+                                           int(rows), lens, arr, len(jobs), C.byref(h)))
+        self.handle = h
+
+    def run(self):
+        N.check(N.lib().vta_tm_plan_run(self.handle))
+
+    def info(self) -> dict:
+        i = N.TmPlanInfoC()
+        N.check(N.lib().vta_tm_plan_info_get(self.handle, C.byref(i)))
+        return {"n_items": i.n_items, "chunk": list(i.chunk), "fixups": i.fixups, "tuned": bool(i.tuned)}
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            N.lib().vta_tm_plan_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def launch_count() -> int:
