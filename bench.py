@@ -107,7 +107,23 @@ def workload_alma_small():
     return w
 
 
-WORKLOADS = {"sweeps": workload_sweeps, "alma_grid": workload_alma_grid, "ema_small": workload_ema_small,
+def workload_ragged_tm():
+    """4,096 OHLCV series of uneven length (U[1000, 50000]) and NaN lead
+    (U[0, 500]), time-major and padded with NaN, through one many-series plan
+    running ATR(14), ADX(14), SuperTrend(10, 3.0) and percentile(50, 50%)."""
+    from vectorta_gb300 import datagen
+
+    d, lens, leads = datagen.ragged_many_series(4096, seed=4, fields=("high", "low", "close"))
+    jobs = [("atr", 14, 0.0, 1), ("adx", 14, 0.0, 1), ("supertrend", 10, 3.0, 2),
+            ("percentile_nearest_rank", 50, 50.0, 1)]
+    return {"name": "ragged_tm", "kind": "plan", "tm": d, "lens": lens, "plan_jobs": jobs,
+            "config": {"workload": "ragged_many_series_plan", "series": 4096, "rows": int(d["close"].shape[0]),
+                       "lengths": "U[1000, 50000]", "nan_lead": "U[0, 500]", "sum_lengths": int(lens.sum()),
+                       "seed": 4, "indicators": "ATR(14), ADX(14), SuperTrend(10, 3.0), percentile(50, 50%)",
+                       "layout": "time-major f32, NaN tail past each series (not read, not written)"}}
+
+
+WORKLOADS = {"sweeps": workload_sweeps, "ragged_tm": workload_ragged_tm, "alma_grid": workload_alma_grid, "ema_small": workload_ema_small,
              "alma_small": workload_alma_small}
 
 
@@ -260,6 +276,13 @@ def cpu_sample(wl, budget_rows=None):
     return tasks
 
 
+def sample_desc(wl, tasks, outs, dt, threads):
+    what = (f"{len(tasks) // 4} of the workload's series (every 64th) x its 4 indicators"
+            if wl.get("kind") == "plan" else f"{len(tasks)} rows of the workload's sweeps over the full series")
+    took = f", {dt:.1f} s" if dt is not None else " per step"
+    return f"{what} ({outs:.3g} outputs{took}), C oracle, {threads} threads"
+
+
 def run_cpu(tasks, threads):
     from concurrent.futures import ThreadPoolExecutor
 
@@ -348,6 +371,128 @@ def gpu_bench(args, wl):
                      "bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
         "kernel_ms_per_call": share, "outputs_per_step": out_per_step, "e2e": e2e,
     }
+
+
+PLAN_BYTES = {"atr": 16, "adx": 16, "supertrend": 20, "percentile_nearest_rank": 8}  # per (series, row)
+PLAIN_PARAMS = {"atr": {"period": 14}, "adx": {"period": 14}, "supertrend": {"period": 10, "factor": 3.0},
+                "percentile_nearest_rank": {"length": 50, "percentage": 50.0}}
+
+
+def gpu_bench_plan(args, wl):
+    """Many-series plan: every step replays the plan's graph over all series.
+    Beside it, the plain per-request path: the four many-series entry points
+    one after another over the same padded matrix."""
+    import torch
+
+    from vectorta_gb300 import cuda as V
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    ctx = V.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_policy("timing", "on")
+    tm, lens = wl["tm"], wl["lens"]
+    rows, cols = tm["close"].shape
+    d_in = [torch.from_numpy(tm[k]).to(dev) for k in ("high", "low", "close")]
+    outs, jobs = [], []
+    for kind, p, prm, nout in wl["plan_jobs"]:
+        o = [torch.empty(rows, cols, device=dev) for _ in range(nout)]
+        outs.append(o)
+        jobs.append({"kind": kind, "period": p, "param": prm, "out0": o[0], "out1": o[1] if nout > 1 else None})
+    t0 = time.perf_counter()
+    plan = V.TmPlan(*d_in, cols, rows, lens, jobs, ctx=ctx)
+    create_s = time.perf_counter() - t0
+    sum_len = int(lens.sum())
+    out_per_step = sum_len * sum(j[3] for j in wl["plan_jobs"])
+    for _ in range(args.warmup):
+        plan.run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    graph_ms = []
+    with ClockSampler(0) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            plan.run()
+            graph_ms.append(ctx.kernel_ms)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    info = plan.info()
+    g_ms = float(np.median(graph_ms))
+    alg = sum_len * sum(PLAN_BYTES[j[0]] for j in wl["plan_jobs"])
+    hbm, src = peaks()
+
+    # plain per-request path: one many-series call per indicator, padded matrix
+    inds = {k: V.CLASSES[k](0, ctx=ctx) for k in PLAIN_PARAMS}
+    p_out = {k: [torch.empty(rows, cols, device=dev) for _ in range(2 if k == "supertrend" else 1)]
+             for k in PLAIN_PARAMS}
+
+    def plain_step():
+        for k, ind in inds.items():
+            ins = [d_in[2]] if k == "percentile_nearest_rank" else d_in
+            ind.many_series_one_param_device(ins, cols, rows, PLAIN_PARAMS[k], p_out[k])
+
+    for _ in range(max(1, args.warmup)):
+        plain_step()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        plain_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1) / args.steps
+
+    e2e = None
+    if not args.no_e2e:
+        h_in = [torch.from_numpy(tm[k]).pin_memory() for k in ("high", "low", "close")]
+        h_out = [torch.empty(rows, cols).pin_memory() for o in outs for _ in o]
+        d_out = [t for o in outs for t in o]
+        plan.run()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for d, h in zip(d_in, h_in):
+                d.copy_(h, non_blocking=True)
+            plan.run()
+            for h, d in zip(h_out, d_out):
+                h.copy_(d, non_blocking=True)
+            torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / args.steps
+        e2e = {"value": out_per_step / dt, "unit": "outputs/s", "ms_per_step": dt * 1e3,
+               "h2d_bytes_per_step": int(sum(t.numel() * 4 for t in h_in)),
+               "d2h_bytes_per_step": int(sum(t.numel() * 4 for t in h_out)), "steps": args.steps}
+    plan.close()
+    return {
+        "value": out_per_step / (ms / 1e3), "ms_per_step": ms, "gpu_launches": 3 * args.steps,
+        "clocks": clk.summary(),
+        "roofline": {"bound": "hbm", "achieved": alg / (g_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": alg / (g_ms / 1e3) / 1e9 / hbm, "traffic": TRAFFIC.get(wl["name"]),
+                     "kernel": "tm plan graph (k_plan_first + k_tm_plan + k_tm_fixup)", "peak_source": src,
+                     "bytes_per_launch": alg, "ms_per_launch": g_ms},
+        "kernel_ms_per_call": {"plan_graph": g_ms}, "outputs_per_step": out_per_step, "e2e": e2e,
+        "plan": {"create_s": create_s, "tuned": info["tuned"], "chunk": info["chunk"][:len(jobs)],
+                 "n_items": info["n_items"], "fixups_last_run": info["fixups"]},
+        "plain_per_request": {"ms_per_step": plain_ms, "value": out_per_step / (plain_ms / 1e3),
+                              "note": "ATR/ADX/SuperTrend/percentile many-series entry points, one call each, "
+                                      "over the padded matrix"},
+    }
+
+
+def cpu_sample_plan(wl, every=64):
+    """Every `every`-th series of the plan workload through the oracle."""
+    from oracle import oracle as O
+
+    tm, lens = wl["tm"], wl["lens"]
+    tasks = []
+    for s in range(0, tm["close"].shape[1], every):
+        L = int(lens[s])
+        h, l, c = (tm[k][:L, s].astype(np.float64) for k in ("high", "low", "close"))
+        tasks.append((lambda h=h, l=l, c=c: O.atr(h, l, c, 14), L))
+        tasks.append((lambda h=h, l=l, c=c: O.adx(h, l, c, 14), L))
+        tasks.append((lambda h=h, l=l, c=c: O.supertrend(h, l, c, 10, 3.0), 2 * L))
+        tasks.append((lambda c=c: O.percentile_nearest_rank(c, 50, 50.0), L))
+    return tasks
 
 
 def e2e_bench(args, wl, inds, rows, out_per_step):
@@ -445,7 +590,7 @@ def main():
         if rank != 0:
             return
         threads = os.cpu_count() or 1
-        tasks = cpu_sample(wl)
+        tasks = cpu_sample_plan(wl) if wl.get("kind") == "plan" else cpu_sample(wl)
         run_cpu(tasks[: max(1, len(tasks) // 8)], threads)  # warm caches / page in
         vals = []
         for _ in range(max(1, args.warmup)):
@@ -458,8 +603,7 @@ def main():
         v = float(np.median(vals))
         line = dict(base, impl="reference", value=v, ms_per_step=wall * 1e3,
                     cpu_baseline={"value": v, "unit": "outputs/s", "cores": threads, "kind": "port",
-                                  "sample": f"{len(tasks)} rows of the workload's sweeps over the full series "
-                                            f"({outs:.3g} outputs per step), C oracle, {threads} threads"},
+                                  "sample": sample_desc(wl, tasks, outs, None, threads)},
                     e2e={"value": v, "unit": "outputs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
         print(json.dumps(line))
         return
@@ -471,7 +615,7 @@ def main():
         import torch
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    res = gpu_bench(args, wl)
+    res = gpu_bench_plan(args, wl) if wl.get("kind") == "plan" else gpu_bench(args, wl)
     if world > 1:
         import torch
         import torch.distributed as dist
@@ -485,14 +629,16 @@ def main():
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
-        tasks = cpu_sample(wl)
+        tasks = cpu_sample_plan(wl) if wl.get("kind") == "plan" else cpu_sample(wl)
         v, dt, outs = run_cpu(tasks, threads)
         cpu = {"value": v, "unit": "outputs/s", "cores": threads, "kind": "port",
-               "sample": f"{len(tasks)} rows of the workload's sweeps over the full series ({outs:.3g} outputs, "
-                         f"{dt:.1f} s), C oracle, {threads} threads"}
+               "sample": sample_desc(wl, tasks, outs, dt, threads)}
     line = dict(base, value=res["value"], ms_per_step=res["ms_per_step"], gpu_launches=res["gpu_launches"],
                 clocks=res["clocks"], roofline=res["roofline"], cpu_baseline=cpu, e2e=res["e2e"],
                 kernel_ms_per_call=res["kernel_ms_per_call"], outputs_per_step=res["outputs_per_step"])
+    for k in ("plan", "plain_per_request"):
+        if k in res:
+            line[k] = res[k]
     print(json.dumps(line))
 
 

@@ -57,6 +57,7 @@ __device__ __forceinline__ float true_range(float hi, float lo, float pc) {
 //   load(w, in, t0)              exact running state entering t0 from 8 words
 //   save(w)                      running state as 8 words
 //   step(in, t, o1) -> o0        process t (any phase), outputs for t
+//   stepv(t, h, l, c, o1) -> o0  the same with the inputs of t given
 //
 // ATR: atr_compute_into_scalar (atr.rs:329-460); TR(f) = h - l, seed = mean
 // of the first p TRs at s = f + p - 1, then rma = fma(-a, rma, rma) + a * tr.
@@ -84,9 +85,12 @@ struct PAtr {
         w[0] = rma;
         w[1] = w[2] = w[3] = w[4] = w[5] = w[6] = w[7] = 0.f;
     }
-    __device__ float step(const TmIn& in, int t, float&) {
+    __device__ float step(const TmIn& in, int t, float& o1) {
         if (t < f) return qnan();
-        const float hi = in.H(t), lo = in.L(t), cl = in.C(t);
+        return stepv(t, in.H(t), in.L(t), in.C(t), o1);
+    }
+    __device__ float stepv(int t, float hi, float lo, float cl, float&) {
+        if (t < f) return qnan();
         const float tr = (t == f) ? hi - lo : true_range(hi, lo, pc);
         pc = cl;
         const int s = f + p - 1;
@@ -152,9 +156,12 @@ struct PAdx {
         const float sdi = pdi + mdi;
         return sdi != 0.f ? (fabsf(pdi - mdi) / sdi) * 100.f : 0.f;
     }
-    __device__ float step(const TmIn& in, int t, float&) {
+    __device__ float step(const TmIn& in, int t, float& o1) {
         if (t < f) return qnan();
-        const float ch = in.H(t), cl = in.L(t), cc = in.C(t);
+        return stepv(t, in.H(t), in.L(t), in.C(t), o1);
+    }
+    __device__ float stepv(int t, float ch, float cl, float cc, float&) {
+        if (t < f) return qnan();
         const int r = t - f;
         float v = qnan();
         if (r > 0) {
@@ -230,7 +237,11 @@ struct PSuperTrend {
     __device__ float step(const TmIn& in, int t, float& v1) {
         v1 = qnan();
         if (t < f) return qnan();
-        const float hi = in.H(t), lo = in.L(t), cl = in.C(t);
+        return stepv(t, in.H(t), in.L(t), in.C(t), v1);
+    }
+    __device__ float stepv(int t, float hi, float lo, float cl, float& v1) {
+        v1 = qnan();
+        if (t < f) return qnan();
         float tr = hi - lo;
         if (t != f) {
             const float hc = fabsf(hi - pc);
@@ -284,62 +295,168 @@ __device__ __forceinline__ int pnr_rank(double pf, int wl) {
     const int k = raw <= 0 ? 0 : (int)raw;
     return k >= wl ? wl - 1 : k;
 }
+// Insert v (not NaN) into the ascending window, dropping the last (+inf)
+// slot: w'[i] = min(w[i], max(w[i-1], v)) -- two min/max per slot, no
+// predicates, every slot independent.
 template <int W>
 __device__ __forceinline__ void reg_insert(float (&w)[W], float v) {
 #pragma unroll
-    for (int i = W - 1; i > 0; --i) w[i] = (w[i] < v) ? w[i] : ((w[i - 1] < v) ? v : w[i - 1]);
-    w[0] = (w[0] < v) ? w[0] : v;
+    for (int i = W - 1; i > 0; --i) w[i] = fminf(w[i], fmaxf(w[i - 1], v));
+    w[0] = fminf(w[0], v);
 }
-// removes one element equal to v (v is in the window)
+// Remove one element equal to v (v is in the window): slots below v keep their
+// value, the others take their right neighbour.  "w[i] < v" is the sign of
+// w[i] - v (exact: a difference of distinct floats is never zero with
+// denormals kept, and equal values give +0), turned into a bit mask.
 template <int W>
 __device__ __forceinline__ void reg_remove(float (&w)[W], float v) {
+    constexpr unsigned kInf = 0x7f800000u;
 #pragma unroll
-    for (int i = 0; i < W - 1; ++i) w[i] = (w[i] < v) ? w[i] : w[i + 1];
-    w[W - 1] = (w[W - 1] < v) ? w[W - 1] : __int_as_float(0x7f800000);
+    for (int i = 0; i < W; ++i) {
+        const unsigned m = (unsigned)((int)__float_as_uint(__fsub_rn(w[i], v)) >> 31);
+        const unsigned nxt = i + 1 < W ? __float_as_uint(w[i + 1]) : kInf;
+        w[i] = __uint_as_float((__float_as_uint(w[i]) & m) | (nxt & ~m));
+    }
 }
+// w[k] for a runtime k by a select tree on the bits of k (depth log2 W
+// instead of a W-long chain of dependent selects)
 template <int W>
-__device__ void pnr_chunk(const TmIn& in, int f, int len, double pf, int c0, int c1, float* out,
-                          size_t cols, size_t s) {
+__device__ __forceinline__ float pick_tree(const float (&w)[W], int k) {
+    constexpr int P = W <= 16 ? 16 : (W <= 32 ? 32 : 64);
+    float v[P];
+#pragma unroll
+    for (int i = 0; i < P; ++i) v[i] = i < W ? w[i] : 0.f;
+#pragma unroll
+    for (int step = 1; step < P; step <<= 1) {
+        const bool hi = (k & step) != 0;
+#pragma unroll
+        for (int i = 0; i + step < P; i += 2 * step) v[i] = hi ? v[i + step] : v[i];
+    }
+    return v[0];
+}
+
+template <int W>
+__device__ __forceinline__ float pnr_pick(const float (&w)[W], int wl, int len, int kfull, double pf) {
+    const int k = wl == len ? kfull : (wl > 0 ? pnr_rank(pf, wl) : 0);
+    const float r = pick_tree(w, k);
+    return wl > 0 ? r : qnan();
+}
+
+// ------------------------------------------------ chunk runners -------------
+// Inputs are staged per warp in shared memory: a double buffer of kPB steps
+// x {high, low, close} x 32 lanes, filled with cp.async (4 bytes per lane and
+// value, so each step of a warp is one 128-byte row segment).  Each lane
+// copies and reads only its own column, so no cross-lane synchronisation is
+// needed; while a block is computed the next one is in flight, so a warp
+// waits for memory about once per kPB steps instead of once per step.
+constexpr int kPB = 16;
+constexpr int kStageFloats = 2 * 3 * kPB * 32;  // per warp
+constexpr size_t kPlanSmem = (size_t)kPlanWarps * kStageFloats * sizeof(float);
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+struct Stage {
+    float* base;  // this warp's [2][3][kPB][32]
+    int lane;
+    __device__ float* at(int buf, int arr, int j) const { return base + ((buf * 3 + arr) * kPB + j) * 32 + lane; }
+    // copies of steps [tb, min(tb + kPB, tend)) of the given arrays into `buf`
+    __device__ void load(int buf, const float* a0, const float* a1, const float* a2, size_t cols, size_t s,
+                         int tb, int tend) const {
+        for (int j = 0; j < kPB && tb + j < tend; ++j) {
+            const size_t g = (size_t)(tb + j) * cols + s;
+            if (a0) cp_async4(at(buf, 0, j), a0 + g);
+            if (a1) cp_async4(at(buf, 1, j), a1 + g);
+            if (a2) cp_async4(at(buf, 2, j), a2 + g);
+        }
+        cp_async_commit();
+    }
+};
+
+// Steps t in [t, tend); with `emit` writes the outputs of each step.
+template <class Op>
+__device__ void run_span(Op& op, const TmIn& in, const Stage& sg, int t, int tend, bool emit, float* out0,
+                         float* out1) {
+    if (t >= tend) return;
+    sg.load(0, in.h, in.l, in.c, in.cols, in.s, t, tend);
+    int buf = 0;
+    for (int tb = t; tb < tend; tb += kPB, buf ^= 1) {
+        // next block in flight (an empty group at the end keeps the count)
+        sg.load(buf ^ 1, in.h, in.l, in.c, in.cols, in.s, tb + kPB, tend);
+        cp_async_wait1();
+        const int te = min(tb + kPB, tend);
+        for (int tt = tb; tt < te; ++tt) {
+            const int j = tt - tb;
+            float o1;
+            const float o0 = op.stepv(tt, *sg.at(buf, 0, j), *sg.at(buf, 1, j), *sg.at(buf, 2, j), o1);
+            if (emit) {
+                out0[(size_t)tt * in.cols + in.s] = o0;
+                if (Op::kTwo) out1[(size_t)tt * in.cols + in.s] = o1;
+            }
+        }
+    }
+}
+
+// Percentile chunk [c0, c1) of each lane.  All lanes of the warp run one
+// time loop over [c0 - len + 1, max c1) in step: each step removes the value
+// leaving the window and inserts the one entering (NaN values are never in
+// the window, which also covers the NaN lead), and writes its output when
+// the step is inside the lane's own chunk.  A lane whose series has ended
+// follows along without inserting or writing.  Keeping the lanes on one
+// loop (instead of each running its own window build and loop) keeps the
+// warp converged.
+template <int W>
+__device__ void pnr_chunk(const TmIn& in, const Stage& sg, unsigned mask, int f, int L, int len, double pf, int c0,
+                          int c1, float* out) {
+    const int tend = __reduce_max_sync(mask, c1);
+    if (tend <= c0) return;  // warp-uniform
+    const int tbeg = max(0, c0 - len + 1);
     const int start = f + len - 1;
-    int t = c0;
-    for (; t < c1 && t < start; ++t) out[(size_t)t * cols + s] = qnan();
-    if (t >= c1) return;
+    const int kfull = pnr_rank(pf, len);
     float w[W];
 #pragma unroll
     for (int i = 0; i < W; ++i) w[i] = __int_as_float(0x7f800000);
     int wl = 0;
-    for (int j = t - len + 1; j <= t; ++j) {
-        const float v = in.C(j);
-        if (!isnan(v)) {
-            reg_insert(w, v);
-            ++wl;
+    // staged arrays: 0 = entering x[u], 1 = leaving x[u - len]
+    auto load = [&](int buf, int ub) {
+        for (int j = 0; j < kPB && ub + j < tend; ++j) {
+            const int u = ub + j, uo = u - len;
+            if (u < L) cp_async4(sg.at(buf, 0, j), in.c + (size_t)u * in.cols + in.s);
+            if (uo >= tbeg && uo < L) cp_async4(sg.at(buf, 1, j), in.c + (size_t)uo * in.cols + in.s);
         }
-    }
-    const int kfull = pnr_rank(pf, len);
-    for (;;) {
-        const int k = wl == len ? kfull : (wl > 0 ? pnr_rank(pf, wl) : 0);
-        float r = w[0];
-#pragma unroll
-        for (int i = 1; i < W; ++i) r = (i == k) ? w[i] : r;
-        out[(size_t)t * cols + s] = wl > 0 ? r : qnan();
-        if (t + 1 >= c1) break;
-        const float vo = in.C(t + 1 - len);
-        if (!isnan(vo)) {
-            reg_remove(w, vo);
-            --wl;
+        cp_async_commit();
+    };
+    load(0, tbeg);
+    int buf = 0;
+    for (int ub = tbeg; ub < tend; ub += kPB, buf ^= 1) {
+        load(buf ^ 1, ub + kPB);
+        cp_async_wait1();
+        const int ue = min(ub + kPB, tend);
+        for (int u = ub; u < ue; ++u) {
+            const int j = u - ub, uo = u - len;
+            const float vo = (uo >= tbeg && uo < L) ? *sg.at(buf, 1, j) : qnan();
+            const float vi = u < L ? *sg.at(buf, 0, j) : qnan();
+            if (!isnan(vo)) {
+                reg_remove(w, vo);
+                --wl;
+            }
+            if (!isnan(vi)) {
+                reg_insert(w, vi);
+                ++wl;
+            }
+            if (u >= c0 && u < c1)
+                out[(size_t)u * in.cols + in.s] = u < start ? qnan() : pnr_pick(w, wl, len, kfull, pf);
         }
-        const float vi = in.C(t + 1);
-        if (!isnan(vi)) {
-            reg_insert(w, vi);
-            ++wl;
-        }
-        ++t;
     }
 }
 
-// ------------------------------------------------ chunk runners -------------
 template <class Op>
-__device__ void run_chunk(const PlanArgs& a, const PlanJob& J, int s, int k) {
+__device__ void run_chunk(const PlanArgs& a, const PlanJob& J, int s, int k, const Stage& sg) {
     const int L = a.len[s];
     const int c0 = k * J.chunk;
     if (c0 >= L) return;
@@ -359,8 +476,7 @@ __device__ void run_chunk(const PlanArgs& a, const PlanJob& J, int s, int k) {
         t = min(f, c0);
         op.start_exact();
     }
-    float o1;
-    for (; t < c0; ++t) op.step(in, t, o1);
+    run_span(op, in, sg, t, c0, false, J.out0, J.out1);
     float w[8];
     if (k > 0) {
         op.save(w);
@@ -369,32 +485,37 @@ __device__ void run_chunk(const PlanArgs& a, const PlanJob& J, int s, int k) {
         d[1] = make_float4(w[4], w[5], w[6], w[7]);
         J.exact[sidx] = exact ? 1 : 0;
     }
-    for (; t < c1; ++t) {
-        const float o0 = op.step(in, t, o1);
-        J.out0[(size_t)t * a.cols + s] = o0;
-        if (Op::kTwo) J.out1[(size_t)t * a.cols + s] = o1;
-    }
+    run_span(op, in, sg, c0, c1, true, J.out0, J.out1);
     op.save(w);
     float4* d = reinterpret_cast<float4*>(J.st_end + sidx * 8);
     d[0] = make_float4(w[0], w[1], w[2], w[3]);
     d[1] = make_float4(w[4], w[5], w[6], w[7]);
 }
 
-__device__ void run_pnr(const PlanArgs& a, const PlanJob& J, int s, int k) {
+// `mask`: the lanes of the warp working on this item (all of them call).
+__device__ void run_pnr(const PlanArgs& a, const PlanJob& J, int s, int k, const Stage& sg, unsigned mask) {
     const int L = a.len[s];
     const int c0 = k * J.chunk;
-    if (c0 >= L) return;
-    const int c1 = min(c0 + J.chunk, L);
+    const int c1 = max(c0, min(c0 + J.chunk, L));
     const TmIn in{a.h, a.l, a.c, (size_t)a.cols, (size_t)s};
     const int f = a.first_c[s];
-    if (J.period <= 16) pnr_chunk<16>(in, f, J.period, J.pfrac, c0, c1, J.out0, a.cols, s);
-    else if (J.period <= 32) pnr_chunk<32>(in, f, J.period, J.pfrac, c0, c1, J.out0, a.cols, s);
-    else pnr_chunk<64>(in, f, J.period, J.pfrac, c0, c1, J.out0, a.cols, s);
+    // window registers: the length rounded up to a multiple of 8
+    switch ((J.period + 7) >> 3) {
+        case 1: case 2: pnr_chunk<16>(in, sg, mask, f, L, J.period, J.pfrac, c0, c1, J.out0); break;
+        case 3: pnr_chunk<24>(in, sg, mask, f, L, J.period, J.pfrac, c0, c1, J.out0); break;
+        case 4: pnr_chunk<32>(in, sg, mask, f, L, J.period, J.pfrac, c0, c1, J.out0); break;
+        case 5: pnr_chunk<40>(in, sg, mask, f, L, J.period, J.pfrac, c0, c1, J.out0); break;
+        case 6: pnr_chunk<48>(in, sg, mask, f, L, J.period, J.pfrac, c0, c1, J.out0); break;
+        case 7: pnr_chunk<56>(in, sg, mask, f, L, J.period, J.pfrac, c0, c1, J.out0); break;
+        default: pnr_chunk<64>(in, sg, mask, f, L, J.period, J.pfrac, c0, c1, J.out0); break;
+    }
 }
 
 // Persistent work-list kernel: each warp takes items until the list is done.
 __global__ void __launch_bounds__(kPlanWarps * 32) k_tm_plan(PlanArgs a) {
+    extern __shared__ float plan_smem[];
     const int lane = threadIdx.x & 31;
+    const Stage sg{plan_smem + (threadIdx.x >> 5) * kStageFloats, lane};
     for (;;) {
         int it = 0;
         if (lane == 0) it = atomicAdd(a.counter, 1);
@@ -402,13 +523,14 @@ __global__ void __launch_bounds__(kPlanWarps * 32) k_tm_plan(PlanArgs a) {
         if (it >= a.n_items) break;
         const int4 w = a.items[it];
         const int s = w.y * 32 + lane;
+        const unsigned mask = __ballot_sync(0xffffffffu, s < a.cols);
         if (s >= a.cols) continue;
         const PlanJob& J = a.jobs[w.x];
         switch (J.kind) {
-            case PJ_ATR: run_chunk<PAtr>(a, J, s, w.z); break;
-            case PJ_ADX: run_chunk<PAdx>(a, J, s, w.z); break;
-            case PJ_SUPERTREND: run_chunk<PSuperTrend>(a, J, s, w.z); break;
-            default: run_pnr(a, J, s, w.z); break;
+            case PJ_ATR: run_chunk<PAtr>(a, J, s, w.z, sg); break;
+            case PJ_ADX: run_chunk<PAdx>(a, J, s, w.z, sg); break;
+            case PJ_SUPERTREND: run_chunk<PSuperTrend>(a, J, s, w.z, sg); break;
+            default: run_pnr(a, J, s, w.z, sg, mask); break;
         }
     }
 }
@@ -495,7 +617,7 @@ vta_status launch_plan_first(const PlanArgs& a, int* first_hlc, int* first_c, cu
 
 int tm_plan_blocks(int num_sms) {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tm_plan, kPlanWarps * 32, 0) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tm_plan, kPlanWarps * 32, kPlanSmem) != cudaSuccess ||
         per_sm < 1) {
         cudaGetLastError();
         per_sm = 1;
@@ -504,7 +626,7 @@ int tm_plan_blocks(int num_sms) {
 }
 
 vta_status launch_tm_plan(const PlanArgs& a, int blocks, cudaStream_t st) {
-    k_tm_plan<<<blocks, kPlanWarps * 32, 0, st>>>(a);
+    k_tm_plan<<<blocks, kPlanWarps * 32, kPlanSmem, st>>>(a);
     return check_launch("k_tm_plan");
 }
 

@@ -202,7 +202,7 @@ void tune_store_locked(const TuneKey& key, int chunk) {
 // and returns the fastest.
 vta_status tune_job(vta_tm_plan* P, int j, int* best) {
     static const int kRec[] = {1024, 2048, 4096, 8192, 16384};
-    static const int kPnr[] = {512, 1024, 2048, 4096};
+    static const int kPnr[] = {128, 256, 512, 1024};
     const bool rec = plan_job_recurrent(P->jobs[j].kind);
     const int* cand = rec ? kRec : kPnr;
     const int nc = rec ? 5 : 4;

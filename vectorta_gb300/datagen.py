@@ -70,17 +70,33 @@ def ohlcv(n: int, seed: int, nan_lead: int = 0, sigma: float = 0.01, hl_sigma: f
 
 
 def ragged_many_series(n_series: int, seed: int, min_len: int = 1000, max_len: int = 50000,
-                       max_nan_lead: int = 500):
+                       max_nan_lead: int = 500, fields=("open", "high", "low", "close", "volume"),
+                       threads: int | None = None):
     """Many OHLCV series of uneven length and NaN lead, stacked time-major
-    [max_len][n_series] as float32 with a NaN tail past each series' end."""
+    [max_len][n_series] as float32 with a NaN tail past each series' end.
+    Series s is ohlcv(len_s, seed * 100003 + s, lead_s); series are generated
+    on `threads` threads (numpy releases the GIL), each writing its column."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+
     u_len = uniform(seed, 10, n_series)
     u_lead = uniform(seed, 11, n_series)
     lens = (min_len + np.floor(u_len * (max_len - min_len + 1))).astype(np.int64)
     leads = np.floor(u_lead * (max_nan_lead + 1)).astype(np.int64)
     rows = int(lens.max())
-    out = {k: np.full((rows, n_series), np.nan, dtype=np.float32) for k in ("open", "high", "low", "close", "volume")}
-    for s in range(n_series):
+    out = {k: np.full((rows, n_series), np.nan, dtype=np.float32) for k in fields}
+
+    def one(s):
         d = ohlcv(int(lens[s]), seed * 100003 + s, nan_lead=int(leads[s]))
-        for k in out:
+        for k in fields:
             out[k][: lens[s], s] = d[k]
+
+    # many small numpy calls hold the GIL often: scaling stops at ~4 threads
+    workers = threads or min(4, os.cpu_count() or 1)
+    if workers <= 1:
+        for s in range(n_series):
+            one(s)
+    else:
+        with ThreadPoolExecutor(workers) as ex:
+            list(ex.map(one, range(n_series)))
     return out, lens, leads
