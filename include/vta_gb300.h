@@ -574,6 +574,63 @@ vta_status vta_tm_plan_run(vta_tm_plan* plan);
 vta_status vta_tm_plan_info_get(const vta_tm_plan* plan, vta_tm_plan_info* info);
 vta_status vta_tm_plan_destroy(vta_tm_plan* plan);
 
+/* ==== request server (continuous batching over a device-resident store) ====
+ * No counterpart in the crate.  A server owns a store of series resident on
+ * one device and a pool of slots (each a stream with its own workspace).
+ * Requests -- one single-series parameter sweep of any batch indicator above
+ * over one stored series -- are queued by vta_server_submit and admitted in
+ * arrival order by a server thread as soon as a slot is free and their output
+ * fits the memory budget; admitted requests run concurrently, each on its
+ * slot's stream, with the same kernels and results as the corresponding
+ * vta_X_batch_device call.  Completed requests are collected with
+ * vta_server_poll; their device outputs stay valid until vta_server_release.
+ * Times are seconds since the server was created. */
+typedef struct vta_sweep {      /* generic sweep: the fields each indicator reads */
+    vta_range_usize period;     /* period / length */
+    vta_range_f64 p1;           /* alma offset, stddev/zscore nbdev, bb devup, supertrend factor, percentile % */
+    vta_range_f64 p2;           /* alma sigma, bb devdn */
+} vta_sweep;
+typedef struct vta_server_config {
+    int slots;                  /* concurrent requests (streams); 0 = 8 */
+    size_t memory_budget;       /* bytes of request outputs held at once; 0 = half the free memory */
+} vta_server_config;
+typedef struct vta_request {
+    const char* indicator;      /* "alma", "ema", "rsi", "adx", "bollinger_bands", ... */
+    uint32_t series;            /* id from vta_server_add_series */
+    vta_sweep sweep;
+} vta_request;
+typedef struct vta_completion {
+    uint64_t ticket;
+    int status;                 /* vta_status of the request */
+    size_t rows, cols;          /* combos x series length */
+    int n_out;
+    float* d_out[3];            /* device [rows][cols] outputs (valid until released) */
+    double t_submit, t_start, t_done;
+} vta_completion;
+typedef struct vta_server_stats {
+    uint64_t submitted, admitted, deferred, completed, failed;
+    size_t queued, running, bytes_in_use, memory_budget;
+} vta_server_stats;
+typedef struct vta_server vta_server;
+vta_status vta_server_create(int device_id, const vta_server_config* config, vta_server** out);
+/* Copies a host series into the store (high/low may be NULL: close-only). */
+vta_status vta_server_add_series(vta_server* s, const float* high, const float* low, const float* close,
+    size_t len, uint32_t* id);
+/* Same from device buffers (copied; the caller keeps its buffers). */
+vta_status vta_server_add_series_device(vta_server* s, const float* d_high, const float* d_low,
+    const float* d_close, size_t len, uint32_t* id);
+/* Validates and queues a request; never waits for the device. */
+vta_status vta_server_submit(vta_server* s, const vta_request* req, uint64_t* ticket);
+/* Up to cap completed requests (waits up to wait_ms for at least one). */
+vta_status vta_server_poll(vta_server* s, vta_completion* out, size_t cap, size_t* n, int wait_ms);
+/* Copies output k of a completed, unreleased request to host memory. */
+vta_status vta_server_copy_out(vta_server* s, uint64_t ticket, int k, float* host, size_t n_floats);
+/* Frees a completed request's outputs (returns their bytes to the budget). */
+vta_status vta_server_release(vta_server* s, uint64_t ticket);
+vta_status vta_server_get_stats(vta_server* s, vta_server_stats* st);
+/* Waits for running requests, then frees everything. */
+vta_status vta_server_destroy(vta_server* s);
+
 /* ==== sma without device allocation ====
  * No counterpart in the crate: its wrappers allocate device memory on every
  * call (sma_batch_dev_from_device, sma_wrapper.rs:830-841, allocates the

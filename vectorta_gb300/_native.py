@@ -107,6 +107,31 @@ class TmPlanInfoC(C.Structure):
 
 TM_KINDS = {"atr": 0, "adx": 1, "supertrend": 2, "percentile_nearest_rank": 3}
 
+
+# request server (vta_sweep / vta_request / vta_completion / ...)
+class SweepC(C.Structure):
+    _fields_ = [("period", RangeUsize), ("p1", RangeF64), ("p2", RangeF64)]
+
+
+class ServerConfigC(C.Structure):
+    _fields_ = [("slots", C.c_int), ("memory_budget", C.c_size_t)]
+
+
+class RequestC(C.Structure):
+    _fields_ = [("indicator", C.c_char_p), ("series", C.c_uint32), ("sweep", SweepC)]
+
+
+class CompletionC(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("status", C.c_int), ("rows", C.c_size_t), ("cols", C.c_size_t),
+                ("n_out", C.c_int), ("d_out", C.c_void_p * 3), ("t_submit", C.c_double), ("t_start", C.c_double),
+                ("t_done", C.c_double)]
+
+
+class ServerStatsC(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("admitted", C.c_uint64), ("deferred", C.c_uint64),
+                ("completed", C.c_uint64), ("failed", C.c_uint64), ("queued", C.c_size_t), ("running", C.c_size_t),
+                ("bytes_in_use", C.c_size_t), ("memory_budget", C.c_size_t)]
+
 _lib = None
 
 
@@ -173,6 +198,19 @@ def lib() -> C.CDLL:
     L.vta_tm_plan_info_get.argtypes = [vp, C.POINTER(TmPlanInfoC)]
     L.vta_tm_plan_destroy.argtypes = [vp]
     for fn in ("vta_tm_plan_create", "vta_tm_plan_run", "vta_tm_plan_info_get", "vta_tm_plan_destroy"):
+        getattr(L, fn).restype = st
+    L.vta_server_create.argtypes = [C.c_int, C.POINTER(ServerConfigC), C.POINTER(vp)]
+    L.vta_server_add_series.argtypes = [vp, vp, vp, vp, sz, C.POINTER(C.c_uint32)]
+    L.vta_server_add_series_device.argtypes = [vp, vp, vp, vp, sz, C.POINTER(C.c_uint32)]
+    L.vta_server_submit.argtypes = [vp, C.POINTER(RequestC), C.POINTER(C.c_uint64)]
+    L.vta_server_poll.argtypes = [vp, C.POINTER(CompletionC), sz, C.POINTER(sz), C.c_int]
+    L.vta_server_copy_out.argtypes = [vp, C.c_uint64, C.c_int, vp, sz]
+    L.vta_server_release.argtypes = [vp, C.c_uint64]
+    L.vta_server_get_stats.argtypes = [vp, C.POINTER(ServerStatsC)]
+    L.vta_server_destroy.argtypes = [vp]
+    for fn in ("vta_server_create", "vta_server_add_series", "vta_server_add_series_device", "vta_server_submit",
+               "vta_server_poll", "vta_server_copy_out", "vta_server_release", "vta_server_get_stats",
+               "vta_server_destroy"):
         getattr(L, fn).restype = st
     L.vta_sma_batch_device_noalloc.argtypes = [vp, vp, sz, sz, C.POINTER(SWEEPS["period"]), vp]
     L.vta_sma_batch_device_noalloc.restype = st

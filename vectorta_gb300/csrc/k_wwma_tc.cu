@@ -801,6 +801,11 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
     kern<<<grid, kThreads, smem, st>>>(t, tmap);
     ktimer_end(st);
     VTA_TRY(check_launch("k_wwma_tc"));
+    if (ctx->async_alloc && !d_trace) {
+        // server slot: the error word is read when the request completes
+        VTA_CUDA_TRY(cudaMemcpyAsync(ctx->err_host, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        return VTA_OK;
+    }
     int err = 0;
     VTA_CUDA_TRY(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     VTA_CUDA_TRY(cudaStreamSynchronize(st));

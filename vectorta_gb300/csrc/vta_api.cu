@@ -54,14 +54,24 @@ vta_status check_launch(const char* kernel) {
 
 vta_status Arena::commit() {
     if (total_ <= ctx_->scratch_bytes) return VTA_OK;
+    size_t want = std::max(total_, size_t(1) << 20);
+    want = (want + (size_t(1) << 20) - 1) & ~((size_t(1) << 20) - 1);
+    if (ctx_->async_alloc) {
+        // server slots: stream-ordered, so growing never waits for other streams
+        if (ctx_->scratch) VTA_CUDA_TRY(cudaFreeAsync(ctx_->scratch, ctx_->stream));
+        ctx_->scratch = nullptr;
+        ctx_->scratch_bytes = 0;
+        VTA_CUDA_TRY(ctx_->pool ? cudaMallocFromPoolAsync(&ctx_->scratch, want, ctx_->pool, ctx_->stream)
+                                : cudaMallocAsync(&ctx_->scratch, want, ctx_->stream));
+        ctx_->scratch_bytes = want;
+        return VTA_OK;
+    }
     if (ctx_->scratch) {
         VTA_CUDA_TRY(cudaStreamSynchronize(ctx_->stream));
         cudaFree(ctx_->scratch);
         ctx_->scratch = nullptr;
         ctx_->scratch_bytes = 0;
     }
-    size_t want = std::max(total_, size_t(1) << 20);
-    want = (want + (size_t(1) << 20) - 1) & ~((size_t(1) << 20) - 1);
     VTA_TRY(vram_check(want));
     VTA_CUDA_TRY(cudaMalloc(&ctx_->scratch, want));
     ctx_->scratch_bytes = want;
@@ -290,6 +300,14 @@ vta_status upload_async(vta_ctx* ctx, void* dst, const void* src, size_t bytes, 
 }
 
 vta_status ctx_aux(vta_ctx* ctx, size_t bytes, void** out) {
+    if (bytes > ctx->aux_bytes && ctx->async_alloc) {
+        if (ctx->aux) VTA_CUDA_TRY(cudaFreeAsync(ctx->aux, ctx->stream));
+        ctx->aux = nullptr;
+        ctx->aux_bytes = 0;
+        VTA_CUDA_TRY(ctx->pool ? cudaMallocFromPoolAsync(&ctx->aux, bytes, ctx->pool, ctx->stream)
+                               : cudaMallocAsync(&ctx->aux, bytes, ctx->stream));
+        ctx->aux_bytes = bytes;
+    }
     if (bytes > ctx->aux_bytes) {
         if (ctx->aux) {
             VTA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -899,6 +917,56 @@ static vta_status expand(Ind ind, const R* r, P* out, size_t cap, size_t* n) {
     return cs.empty() ? fail(VTA_ERR_INVALID_INPUT, "empty range") : VTA_OK;
 }
 
+// ---- hooks for the request server (vta_server.cu) -------------------------
+int ind_by_name(const char* name) {
+    if (!name) return -1;
+    for (int i = 0; i < (int)(sizeof(kInfo) / sizeof(kInfo[0])); ++i)
+        if (std::strcmp(kInfo[i].name, name) == 0) return i;
+    return -1;
+}
+int ind_inputs(int ind) { return kInfo[ind].in; }
+int ind_outputs(int ind) { return kInfo[ind].n_out; }
+
+// first valid index from the per-field firsts of a stored series, as
+// host_first defines it per indicator
+size_t ind_first(int ind, size_t fh, size_t fl, size_t fc, size_t fall) {
+    if (kInfo[ind].in == IN_X) return fc;
+    if (ind == I_DONCHIAN) return std::max(fh, fl);
+    if (ind == I_ADX) return std::max(fh, std::max(fl, fc));
+    return fall;
+}
+
+static std::vector<Combo> grid_generic(Ind ind, const vta_sweep* sw) {
+    switch (ind) {
+        case I_ALMA: { const vta_alma_batch_range r{sw->period, sw->p1, sw->p2}; return grid_of(ind, &r); }
+        case I_STDDEV: { const vta_stddev_batch_range r{sw->period, sw->p1}; return grid_of(ind, &r); }
+        case I_ZSCORE: { const vta_zscore_batch_range r{sw->period, sw->p1}; return grid_of(ind, &r); }
+        case I_BB: { const vta_bollinger_batch_range r{sw->period, sw->p1, sw->p2}; return grid_of(ind, &r); }
+        case I_SUPERTREND: { const vta_supertrend_batch_range r{sw->period, sw->p1}; return grid_of(ind, &r); }
+        case I_PNR: { const vta_percentile_batch_range r{sw->period, sw->p1}; return grid_of(ind, &r); }
+        default: { const vta_period_batch_range r{sw->period}; return grid_of(ind, &r); }
+    }
+}
+
+vta_status batch_check(int ind, const vta_sweep* sw, size_t len, size_t first, size_t* rows) {
+    const std::vector<Combo> cs = grid_generic((Ind)ind, sw);
+    VTA_TRY(validate_combos((Ind)ind, cs, len, first));
+    if (cs.size() > SIZE_MAX / len) return fail(VTA_ERR_INVALID_INPUT, "rows*cols overflow");
+    *rows = cs.size();
+    return VTA_OK;
+}
+
+vta_status batch_enqueue(vta_ctx* ctx, int ind, const float* const* d_in, size_t len, size_t first,
+                         const vta_sweep* sw, float* const* d_out) {
+    VTA_CUDA_TRY(cudaSetDevice(ctx->device));
+    ctx->host_stage_off = 0;  // the slot's previous request has completed
+    const std::vector<Combo> cs = grid_generic((Ind)ind, sw);
+    VTA_TRY(validate_combos((Ind)ind, cs, len, first));
+    DevIn din{};
+    for (int k = 0; k < kInfo[ind].in; ++k) din.p[k] = d_in[k];
+    return run_batch(ctx, (Ind)ind, din, len, first, cs, d_out);
+}
+
 // ---- hooks for the no-allocation SMA entry point (vta_noalloc.cu) --------
 vta_status enter_call(vta_ctx* ctx) { return check_ctx(ctx); }
 
@@ -980,8 +1048,10 @@ vta_status vta_ctx_destroy(vta_ctx* ctx) {
     if (!ctx) return VTA_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    if (ctx->scratch) cudaFree(ctx->scratch);
-    if (ctx->aux) cudaFree(ctx->aux);
+    if (ctx->scratch) ctx->async_alloc ? (void)cudaFreeAsync(ctx->scratch, ctx->stream) : (void)cudaFree(ctx->scratch);
+    if (ctx->aux) ctx->async_alloc ? (void)cudaFreeAsync(ctx->aux, ctx->stream) : (void)cudaFree(ctx->aux);
+    if (ctx->async_alloc) cudaStreamSynchronize(ctx->stream);
+    if (ctx->err_host) cudaFreeHost(ctx->err_host);
     if (ctx->host_stage) cudaFreeHost(ctx->host_stage);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);

@@ -78,6 +78,11 @@ struct vta_ctx {
     std::string last_kernel;
     bool timing = false;
     bool timed = false;  // the last call recorded both events
+    // server slots: workspaces grow stream-ordered and calls never wait for
+    // the device; the tensor-core path leaves its error word in err_host
+    bool async_alloc = false;
+    int* err_host = nullptr;         // pinned
+    cudaMemPool_t pool = nullptr;    // stream-ordered allocations of async slots
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -298,6 +303,17 @@ struct PnrArgs {
     size_t scratch_floats;
 };
 vta_status launch_percentile(const PnrArgs& a, cudaStream_t st);
+
+// ------------------------------------------------- request server ---------
+int ind_by_name(const char* name);  // -1 if unknown
+int ind_inputs(int ind);            // 1: close, 2: high, low, 3: high, low, close
+int ind_outputs(int ind);
+size_t ind_first(int ind, size_t fh, size_t fl, size_t fc, size_t fall);
+// grid expansion + the crate's checks for a series of len with first valid `first`
+vta_status batch_check(int ind, const vta_sweep* sw, size_t len, size_t first, size_t* rows);
+// the same plus the kernels of the sweep enqueued on ctx's stream (no wait)
+vta_status batch_enqueue(vta_ctx* ctx, int ind, const float* const* d_in, size_t len, size_t first,
+                         const vta_sweep* sw, float* const* d_out);
 
 // ------------------------------------------------- no-allocation SMA -------
 // Binds a call to `ctx` (device current, timing events), as every entry does.

@@ -26,7 +26,7 @@ import numpy as np
 
 from . import _native as N
 
-__all__ = ["DeviceArrayF32", "Context", "VtaError", "TmPlan"]
+__all__ = ["DeviceArrayF32", "Context", "VtaError", "TmPlan", "Server"]
 VtaError = N.VtaError
 
 
@@ -424,6 +424,90 @@ class TmPlan:
     def close(self):
         if getattr(self, "handle", None) is not None and self.handle.value:
             N.lib().vta_tm_plan_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _sweep_c(sweep: dict) -> "N.SweepC":
+    """dict with "period" (start, end, step) and optionally p1 / p2 (start, end, step);
+    the indicator's own names (offset/sigma, nbdev, devup/devdn, factor, percentage) map to p1/p2."""
+    alias = {"offset": "p1", "sigma": "p2", "nbdev": "p1", "devup": "p1", "devdn": "p2", "factor": "p1",
+             "percentage": "p1", "length": "period"}
+    d = {alias.get(k, k): v for k, v in sweep.items()}
+    s = N.SweepC()
+    p = d["period"]
+    s.period = N.RangeUsize(int(p[0]), int(p[1]), int(p[2]))
+    for f in ("p1", "p2"):
+        v = d.get(f, (0.0, 0.0, 0.0))
+        setattr(s, f, N.RangeF64(float(v[0]), float(v[1]), float(v[2])))
+    return s
+
+
+class Server:
+    """Request server (vta_server_*): a device-resident series store and
+    continuously batched single-series sweeps of any batch indicator."""
+
+    def __init__(self, device_id: int = 0, slots: int = 0, memory_budget: int = 0):
+        cfg = N.ServerConfigC(int(slots), int(memory_budget))
+        h = C.c_void_p()
+        N.check(N.lib().vta_server_create(int(device_id), C.byref(cfg), C.byref(h)))
+        self.handle = h
+
+    def add_series(self, close, high=None, low=None) -> int:
+        c = _f32(close)
+        hi = None if high is None else _f32(high)
+        lo = None if low is None else _f32(low)
+        i = C.c_uint32()
+        N.check(N.lib().vta_server_add_series(self.handle, None if hi is None else hi.ctypes.data,
+                                              None if lo is None else lo.ctypes.data, c.ctypes.data, c.size,
+                                              C.byref(i)))
+        return i.value
+
+    def add_series_device(self, close, length: int, high=None, low=None) -> int:
+        i = C.c_uint32()
+        N.check(N.lib().vta_server_add_series_device(self.handle, None if high is None else _dptr(high),
+                                                     None if low is None else _dptr(low), _dptr(close),
+                                                     int(length), C.byref(i)))
+        return i.value
+
+    def submit(self, indicator: str, series: int, sweep: dict) -> int:
+        r = N.RequestC(indicator.encode(), int(series), _sweep_c(sweep))
+        t = C.c_uint64()
+        N.check(N.lib().vta_server_submit(self.handle, C.byref(r), C.byref(t)))
+        return t.value
+
+    def poll(self, cap: int = 64, wait_ms: int = 0) -> list:
+        arr = (N.CompletionC * cap)()
+        n = C.c_size_t()
+        N.check(N.lib().vta_server_poll(self.handle, arr, cap, C.byref(n), int(wait_ms)))
+        out = []
+        for c in arr[: n.value]:
+            out.append({"ticket": c.ticket, "status": c.status, "rows": c.rows, "cols": c.cols, "n_out": c.n_out,
+                        "d_out": [c.d_out[k] for k in range(c.n_out)], "t_submit": c.t_submit,
+                        "t_start": c.t_start, "t_done": c.t_done})
+        return out
+
+    def copy_out(self, ticket: int, k: int, rows: int, cols: int) -> np.ndarray:
+        h = np.empty((rows, cols), dtype=np.float32)
+        N.check(N.lib().vta_server_copy_out(self.handle, int(ticket), int(k), h.ctypes.data, h.size))
+        return h
+
+    def release(self, ticket: int):
+        N.check(N.lib().vta_server_release(self.handle, int(ticket)))
+
+    def stats(self) -> dict:
+        st = N.ServerStatsC()
+        N.check(N.lib().vta_server_get_stats(self.handle, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in N.ServerStatsC._fields_}
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            N.lib().vta_server_destroy(self.handle)
             self.handle = C.c_void_p()
 
     def __del__(self):
