@@ -123,7 +123,20 @@ def workload_ragged_tm():
                        "layout": "time-major f32, NaN tail past each series (not read, not written)"}}
 
 
-WORKLOADS = {"sweeps": workload_sweeps, "ragged_tm": workload_ragged_tm, "alma_grid": workload_alma_grid, "ema_small": workload_ema_small,
+def workload_served_stream():
+    """10,000 OHLC series (lengths log-uniform 1e3..1e6, NaN lead U[0, 500])
+    resident on the device; requests arrive as a Poisson stream (2,000/s), each
+    an indicator from {ALMA, EMA, RSI, ADX, Bollinger(20-style grid, 2.0)} over
+    a random stored series with a sweep of log-uniform 1..4,096 combos drawn
+    from the grids of the other workloads (capped at each grid's size)."""
+    return {"name": "served_stream", "kind": "server",
+            "config": {"workload": "served_mixed_stream", "series": 10000, "lengths": "log-uniform 1e3..1e6",
+                       "nan_lead": "U[0, 500]", "arrivals": "Poisson 2000 req/s", "seed": 5,
+                       "indicators": "alma, ema, rsi, adx, bollinger_bands (uniform)",
+                       "sweep_size": "log-uniform 1..4096 combos, capped at the grid"}}
+
+
+WORKLOADS = {"sweeps": workload_sweeps, "ragged_tm": workload_ragged_tm, "served_stream": workload_served_stream, "alma_grid": workload_alma_grid, "ema_small": workload_ema_small,
              "alma_small": workload_alma_small}
 
 
@@ -277,8 +290,10 @@ def cpu_sample(wl, budget_rows=None):
 
 
 def sample_desc(wl, tasks, outs, dt, threads):
-    what = (f"{len(tasks) // 4} of the workload's series (every 64th) x its 4 indicators"
-            if wl.get("kind") == "plan" else f"{len(tasks)} rows of the workload's sweeps over the full series")
+    kind = wl.get("kind")
+    what = (f"{len(tasks) // 4} of the workload's series (every 64th) x its 4 indicators" if kind == "plan" else
+            f"the first {len(tasks)} requests of the stream, first combo of each sweep" if kind == "server" else
+            f"{len(tasks)} rows of the workload's sweeps over the full series")
     took = f", {dt:.1f} s" if dt is not None else " per step"
     return f"{what} ({outs:.3g} outputs{took}), C oracle, {threads} threads"
 
@@ -479,6 +494,223 @@ def gpu_bench_plan(args, wl):
     }
 
 
+SERVED_INDS = ["alma", "ema", "rsi", "adx", "bollinger_bands"]
+N_OUT = {"alma": 1, "ema": 1, "rsi": 1, "adx": 1, "bollinger_bands": 3}
+
+
+def stream_store(n_series=10000, seed=5):
+    """Lengths (log-uniform 1e3..1e6), NaN leads (U[0, 500]) and generator
+    seeds of the served stream's store."""
+    from vectorta_gb300 import datagen
+
+    lens = np.floor(1000.0 * 1000.0 ** datagen.uniform(seed, 20, n_series)).astype(np.int64)
+    leads = np.floor(datagen.uniform(seed, 21, n_series) * 501).astype(np.int64)
+    seeds = [seed * 100003 + i for i in range(n_series)]
+    return lens, leads, seeds
+
+
+def served_sweep(name, n, valid):
+    """Sweep of about n combos of indicator `name` from the other workloads' grids,
+    capped at the grid size and at what a series with `valid` bars allows."""
+    if name == "alma":
+        npd = max(1, min(256, n))
+        rem = -(-n // npd)
+        no = min(10, rem)
+        ns = min(7, -(-rem // no))
+        return {"period": (5, 5 + npd - 1, 1), "offset": (0.5, 0.5 + 0.05 * (no - 1), 0.05),
+                "sigma": (3.0, 3.0 + (ns - 1), 1.0)}, npd * no * ns
+    if name in ("ema", "rsi"):
+        m = max(1, min(n, 999, valid - 2))
+        return {"period": (2, 1 + m, 1)}, m
+    if name == "adx":
+        m = max(1, min(n, valid // 2 - 2))
+        return {"period": (2, 1 + m, 1)}, m
+    m = max(1, min(n, 100, valid // 5))
+    return {"period": (5, 5 * m, 5), "devup": (2.0, 2.0, 0.0), "devdn": (2.0, 2.0, 0.0)}, m
+
+
+def served_requests(duration, rate=2000.0, seed=5, n_series=10000, lens=None, leads=None):
+    rng = np.random.default_rng(seed)
+    n = int(rate * duration)
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    ind = rng.integers(0, len(SERVED_INDS), n)
+    ser = rng.integers(0, n_series, n)
+    size = np.floor(np.exp(rng.uniform(0.0, np.log(4096.0), n))).astype(np.int64)
+    reqs = []
+    for i in range(n):
+        name = SERVED_INDS[ind[i]]
+        valid = int(lens[ser[i]] - leads[ser[i]])
+        sw, rows = served_sweep(name, int(size[i]), valid)
+        reqs.append({"t": float(t[i]), "name": name, "series": int(ser[i]), "sweep": sw, "rows": rows,
+                     "outputs": rows * int(lens[ser[i]]) * N_OUT[name]})
+    return reqs
+
+
+def gpu_bench_server(args, wl):
+    """Three runs over one request mix: Poisson-paced (latency), backlogged
+    (capacity) and the plain per-request kernels one at a time."""
+    import threading
+
+    import torch
+
+    from vectorta_gb300 import cuda as V
+    from vectorta_gb300 import datagen
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    lens, leads, seeds = stream_store()
+    srv = V.Server(0, slots=args.slots)
+    kept = []  # the generated device series (also used by the plain run)
+    t0 = time.perf_counter()
+    i = 0
+    while i < len(lens):
+        j, tot = i, 0
+        while j < len(lens) and tot + lens[j] <= 200_000_000:
+            tot += int(lens[j])
+            j += 1
+        j = max(j, i + 1)
+        h, l, c, offs = datagen.ohlc_many_torch(lens[i:j], seeds[i:j], leads[i:j], device=dev)
+        for q in range(j - i):
+            o = int(offs[q]) * 4
+            srv.add_series_device(c.data_ptr() + o, int(lens[i + q]), h.data_ptr() + o, l.data_ptr() + o)
+        kept.append((i, j, h, l, c, offs))
+        i = j
+    store_s = time.perf_counter() - t0
+    reqs = served_requests(args.duration, lens=lens, leads=leads)
+    n_req = len(reqs)
+
+    def run(batch, paced):
+        lat, outs, times = [], 0, []
+        pending = {}
+        lock = threading.Lock()
+        finished = threading.Event()
+
+        failed = []
+
+        def poller():
+            got = 0
+            while got < len(batch):
+                for cpl in srv.poll(256, wait_ms=2):
+                    with lock:
+                        pending.pop(cpl["ticket"], None)
+                    if cpl["status"] != 0:
+                        failed.append(cpl["ticket"])
+                    lat.append(cpl["t_done"] - cpl["t_submit"])
+                    times.append((cpl["t_submit"], cpl["t_done"]))
+                    srv.release(cpl["ticket"])
+                    got += 1
+            finished.set()
+
+        th = threading.Thread(target=poller, daemon=True)
+        th.start()
+        base = time.perf_counter()
+        for r in batch:
+            if paced:
+                delay = base + r["t"] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+            with lock:
+                tk = srv.submit(r["name"], r["series"], r["sweep"])
+                pending[tk] = r
+            outs += r["outputs"]
+        if not finished.wait(timeout=900):
+            raise RuntimeError("served stream: requests did not complete")
+        if failed:
+            raise RuntimeError(f"served stream: {len(failed)} requests failed")
+        span = max(t for _, t in times) - min(t for t, _ in times)
+        lat = np.array(lat)
+        return {"requests": len(batch), "outputs": outs, "seconds": span, "outputs_per_s": outs / span,
+                "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                "max_ms": float(lat.max() * 1e3)}
+
+    # warm-up: a few requests of every indicator (workspaces, module loading)
+    run(reqs[: min(50, n_req)], paced=False)
+    launches0 = V.launch_count()
+    st0 = srv.stats()
+    with ClockSampler(0) as clk:
+        cap = run(reqs[: min(n_req, 4000)], paced=False)
+    launches = V.launch_count() - launches0
+    served = run(reqs, paced=True)
+    st1 = srv.stats()
+
+    # plain per-request kernels, one request at a time, on the same requests
+    ctx = V.Context(0)
+    ctx.set_policy("wma_batch", "plain")
+    ctx.set_policy("recur_chunk", "sequential")
+    inds = {k: V.CLASSES[k](0, ctx=ctx) for k in SERVED_INDS}
+
+    def series_views(sid):
+        for a, b, h, l, c, offs in kept:
+            if a <= sid < b:
+                o, n = int(offs[sid - a]), int(lens[sid])
+                return h[o:o + n], l[o:o + n], c[o:o + n]
+
+    sample = reqs[: min(n_req, 400)]
+    p_out, p_t = 0, 0.0
+    for r in sample:
+        h, l, c = series_views(r["series"])
+        ins = [h, l, c] if r["name"] == "adx" else [c]
+        n = int(lens[r["series"]])
+        outs_t = [torch.empty(r["rows"], n, device=dev) for _ in range(N_OUT[r["name"]])]
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        inds[r["name"]].batch_device(ins, n, int(leads[r["series"]]), r["sweep"], outs_t)
+        p_t += time.perf_counter() - t1
+        p_out += r["outputs"]
+        del outs_t
+    plain = {"requests": len(sample), "outputs_per_s": p_out / p_t, "seconds": p_t,
+             "note": "the same requests one at a time through the plain FP32 kernels (wma_batch=plain, "
+                     "recur_chunk=sequential)"}
+    cap_bytes = cap["outputs"] * 4
+    hbm, src = peaks()
+    srv.close()
+    return {
+        "value": cap["outputs_per_s"], "ms_per_step": cap["seconds"] * 1e3 / cap["requests"],
+        "gpu_launches": int(launches), "clocks": clk.summary(),
+        "roofline": {"bound": "hbm", "achieved": cap_bytes / cap["seconds"] / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": cap_bytes / cap["seconds"] / 1e9 / hbm, "traffic": None,
+                     "kernel": "all kernels of the backlogged run (output bytes / makespan)", "peak_source": src,
+                     "bytes_per_launch": None, "ms_per_launch": None},
+        "kernel_ms_per_call": {}, "outputs_per_step": cap["outputs"] / cap["requests"], "e2e": None,
+        "served": dict(served, rate_req_s=2000.0, duration_s=args.duration,
+                       admitted=st1["admitted"] - st0["admitted"], deferred=st1["deferred"] - st0["deferred"]),
+        "capacity": cap, "plain_per_request": dict(plain, speedup=cap["outputs_per_s"] / plain["outputs_per_s"]),
+        "store": {"series": int(len(lens)), "bars": int(lens.sum()), "build_s": store_s},
+    }
+
+
+def cpu_sample_server(wl, n=40):
+    """The first n requests of the served stream, each reduced to the first
+    combo of its sweep over its whole series, through the oracle."""
+    from oracle import oracle as O
+    from vectorta_gb300 import datagen
+
+    lens, leads, seeds = stream_store()
+    tasks = []
+    for r in served_requests(1.0, lens=lens, leads=leads)[:n]:
+        sid = r["series"]
+        d = datagen.ohlcv(int(lens[sid]), seeds[sid], nan_lead=int(leads[sid]))
+        h, l, c = d["high"], d["low"], d["close"]
+        p = int(r["sweep"]["period"][0])
+        L = int(lens[sid])
+        if r["name"] == "alma":
+            tasks.append((lambda c=c, p=p, o=r["sweep"]["offset"][0], sg=r["sweep"]["sigma"][0]: O.alma(c, p, o, sg), L))
+        elif r["name"] == "ema":
+            tasks.append((lambda c=c, p=p: O.ema(c, p), L))
+        elif r["name"] == "rsi":
+            tasks.append((lambda c=c, p=p: O.rsi_batch(c, [p]), L))
+        elif r["name"] == "adx":
+            tasks.append((lambda h=h, l=l, c=c, p=p: O.adx(h, l, c, p), L))
+        else:
+            tasks.append((lambda c=c, p=p: O.bollinger(c, p, 2.0, 2.0), 3 * L))
+    return tasks
+
+
+def cpu_tasks(wl):
+    kind = wl.get("kind")
+    return cpu_sample_plan(wl) if kind == "plan" else cpu_sample_server(wl) if kind == "server" else cpu_sample(wl)
+
+
 def cpu_sample_plan(wl, every=64):
     """Every `every`-th series of the plan workload through the oracle."""
     from oracle import oracle as O
@@ -574,6 +806,8 @@ def main():
     ap.add_argument("--workload", default="sweeps", choices=sorted(WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--duration", type=float, default=10.0, help="served_stream: seconds of Poisson arrivals")
+    ap.add_argument("--slots", type=int, default=8, help="served_stream: concurrent server slots")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -590,7 +824,7 @@ def main():
         if rank != 0:
             return
         threads = os.cpu_count() or 1
-        tasks = cpu_sample_plan(wl) if wl.get("kind") == "plan" else cpu_sample(wl)
+        tasks = cpu_tasks(wl)
         run_cpu(tasks[: max(1, len(tasks) // 8)], threads)  # warm caches / page in
         vals = []
         for _ in range(max(1, args.warmup)):
@@ -615,7 +849,9 @@ def main():
         import torch
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    res = gpu_bench_plan(args, wl) if wl.get("kind") == "plan" else gpu_bench(args, wl)
+    kind = wl.get("kind")
+    res = (gpu_bench_plan(args, wl) if kind == "plan" else
+           gpu_bench_server(args, wl) if kind == "server" else gpu_bench(args, wl))
     if world > 1:
         import torch
         import torch.distributed as dist
@@ -629,14 +865,14 @@ def main():
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
-        tasks = cpu_sample_plan(wl) if wl.get("kind") == "plan" else cpu_sample(wl)
+        tasks = cpu_tasks(wl)
         v, dt, outs = run_cpu(tasks, threads)
         cpu = {"value": v, "unit": "outputs/s", "cores": threads, "kind": "port",
                "sample": sample_desc(wl, tasks, outs, dt, threads)}
     line = dict(base, value=res["value"], ms_per_step=res["ms_per_step"], gpu_launches=res["gpu_launches"],
                 clocks=res["clocks"], roofline=res["roofline"], cpu_baseline=cpu, e2e=res["e2e"],
                 kernel_ms_per_call=res["kernel_ms_per_call"], outputs_per_step=res["outputs_per_step"])
-    for k in ("plan", "plain_per_request"):
+    for k in ("plan", "plain_per_request", "served", "capacity", "store"):
         if k in res:
             line[k] = res[k]
     print(json.dumps(line))

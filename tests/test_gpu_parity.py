@@ -316,3 +316,28 @@ def test_golden_fixture_through_gpu(candles, golden):
         exp = np.array(g["last5"])
         # f32 input and arithmetic: relative 2e-5 plus the crate's own tolerance
         assert np.all(np.abs(out - exp) <= g["tol"] + 2e-5 * np.abs(exp)), (name, out, exp)
+
+
+@pytest.mark.parametrize("name,sweep", [
+    ("adx", {"period": (5, 60, 5)}),
+    ("supertrend", {"period": (7, 21, 7), "factor": (2.0, 3.0, 0.5)}),
+])
+def test_chunked_hlc_sweeps_equal_sequential(name, sweep):
+    """ADX / SuperTrend sweeps cut into time chunks (verified warm restarts,
+    also with a warm length too short to converge so the fix-up pass repairs
+    chunks) are bit-identical to the sequential per-combo kernel."""
+    d = datagen.ohlcv(30000, seed=31, nan_lead=17)
+    h, l, c = (f32(d[k]) for k in ("high", "low", "close"))
+    seq = V.CLASSES[name](0)
+    seq.set_policy("recur_chunk", "sequential")
+    ref = seq.batch_dev(h, l, c, sweep=sweep)
+    ref = [r.to_host() for r in (ref if isinstance(ref, tuple) else (ref,))]
+    for warm in (None, "32"):
+        ind = V.CLASSES[name](0)
+        if warm:
+            ind.set_policy("tm_warm", warm)
+        got = ind.batch_dev(h, l, c, sweep=sweep)
+        assert ind.last_kernel.endswith("_chunked")
+        got = [g.to_host() for g in (got if isinstance(got, tuple) else (got,))]
+        for k, (g, r) in enumerate(zip(got, ref)):
+            assert np.array_equal(g, r, equal_nan=True), f"{name}[{k}] warm={warm}"

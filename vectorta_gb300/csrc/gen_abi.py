@@ -119,7 +119,7 @@ void* vta_ctx_get_stream(vta_ctx* ctx);
  *   "wma_batch"   = "auto" | "plain" | "tc_fp16x3" | "tc_bf16x3"
  *   "recur_chunk" = "auto" | "sequential" | <positive multiple of 32>
  *   "tm_chunk"    = "auto" | "sequential" | <steps>   (many-series plans)
- *   "tm_warm"     = "auto" | <steps>                  (many-series plans)
+ *   "tm_warm"     = "auto" | <steps>   (plans; chunked ADX/SuperTrend sweeps)
  *   "timing"      = "on" | "off"                                         */
 vta_status vta_ctx_set_policy(vta_ctx* ctx, const char* key, const char* value);
 /* selected_batch_kernel() (alma_wrapper.rs:239-245): name of the last kernel

@@ -1,0 +1,173 @@
+// Time-chunked single-series sweeps of ADX and SuperTrend (batch layout:
+// one series, lane = parameter combo).
+//
+// The sequential kernels (k_hlc.cu) run one lane per combo over the whole
+// series, so a sweep of a few hundred combos keeps a few warps busy for the
+// series' full length.  Here the combos of a 32-combo group are also cut into
+// time chunks with the verified warm restart of the many-series plans: a
+// chunk that starts past the seeding phase first runs `warm` steps from a
+// guessed state (the state decays by (1 - 1/p) per step), records the state
+// it reaches at its start and at its end, and k_hlc_chunk_fixup recomputes,
+// per combo and in chunk order, every chunk whose recorded start state differs
+// (bit for bit) from its predecessor's end state.  Results are therefore
+// bit-identical to the sequential kernels.
+//
+// A warp owns one (group, chunk) item.  The shared inputs of each 32-step tile
+// are loaded once per warp (lane j loads step tb + j, one coalesced 128-byte
+// row per array) and broadcast step by step with shuffles; outputs are staged
+// per warp in shared memory and written as 32 rows x 128 bytes.
+#include "hlc_ops.cuh"
+#include "vta_internal.h"
+
+namespace vta {
+namespace {
+
+constexpr int kCW = 4;  // warps per block
+
+struct In1 {
+    const float *h, *l, *c;
+    __device__ float H(int t) const { return __ldg(h + t); }
+    __device__ float L(int t) const { return __ldg(l + t); }
+    __device__ float C(int t) const { return __ldg(c + t); }
+};
+
+__device__ __forceinline__ void store_state(float* dst, const float (&w)[8]) {
+    float4* d = reinterpret_cast<float4*>(dst);
+    d[0] = make_float4(w[0], w[1], w[2], w[3]);
+    d[1] = make_float4(w[4], w[5], w[6], w[7]);
+}
+
+template <class Op>
+__global__ void __launch_bounds__(kCW * 32) k_hlc_chunk(HlcChunkArgs a) {
+    __shared__ float stage0[kCW][32][33];
+    __shared__ float stage1[kCW][Op::kTwo ? 32 : 1][33];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int item = blockIdx.x * kCW + warp;
+    if (item >= a.n_items) return;
+    const int2 it = a.items[item];
+    const int g = it.x, k = it.y;
+    const int chunk = a.group_chunk[g];
+    const int c0 = k * chunk;
+    const int c1 = min(c0 + chunk, a.n);
+    const int li = g * 32 + lane;
+    const bool valid = li < a.n_combos;
+    const int lc = valid ? li : g * 32;  // idle lanes shadow the group's first combo (nothing written)
+    Op op;
+    op.init(a.periods[lc], a.factors ? a.factors[lc] : 0.f, a.first);
+    const In1 in{a.h, a.l, a.c};
+    const int W = a.group_warm[g];  // multiple of 32
+    const bool warm = k > 0 && __all_sync(0xffffffffu, c0 - W >= op.run_from());
+    int t0;
+    if (warm) {
+        t0 = c0 - W;
+        op.start_warm(in, t0);
+    } else {
+        t0 = min(a.first, c0) & ~31;
+        op.start_exact();
+    }
+    // tiles of 32 steps over [tb0, tend); with `emit` the outputs go to the rows
+    auto tiles = [&](int tb0, int tend, bool emit) {
+        for (int tb = tb0; tb < tend; tb += 32) {
+            const int nt = min(32, tend - tb);
+            const int tj = tb + lane;
+            float xh = 0.f, xl = 0.f, xc = 0.f;
+            if (lane < nt) {
+                xh = __ldg(a.h + tj);
+                xl = __ldg(a.l + tj);
+                xc = __ldg(a.c + tj);
+            }
+            for (int j = 0; j < nt; ++j) {
+                const float hv = __shfl_sync(0xffffffffu, xh, j);
+                const float lv = __shfl_sync(0xffffffffu, xl, j);
+                const float cv = __shfl_sync(0xffffffffu, xc, j);
+                float o1;
+                const float o0 = op.stepv(tb + j, hv, lv, cv, o1);
+                if (emit) {
+                    stage0[warp][lane][j] = o0;
+                    if (Op::kTwo) stage1[warp][lane][j] = o1;
+                }
+            }
+            if (emit) {
+                __syncwarp();
+                if (lane < nt) {
+                    for (int r = 0; r < 32; ++r) {
+                        const int row = g * 32 + r;
+                        if (row >= a.n_combos) break;
+                        a.out0[(size_t)row * a.n + tj] = stage0[warp][r][lane];
+                        if (Op::kTwo) a.out1[(size_t)row * a.n + tj] = stage1[warp][r][lane];
+                    }
+                }
+                __syncwarp();
+            }
+        }
+    };
+    tiles(t0, c0, false);
+    float w[8];
+    const size_t sidx = (size_t)k * a.n_combos + li;
+    if (k > 0 && valid) {
+        op.save(w);
+        store_state(a.st_start + sidx * 8, w);
+        a.exact[sidx] = warm ? 0 : 1;
+    }
+    tiles(c0, c1, true);
+    if (valid) {
+        op.save(w);
+        store_state(a.st_end + sidx * 8, w);
+    }
+}
+
+// Per combo, chunks in order: a warm-restarted chunk whose start state is not
+// its predecessor's end state is recomputed from that end state.
+template <class Op>
+__global__ void k_hlc_chunk_fixup(HlcChunkArgs a) {
+    const int li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= a.n_combos) return;
+    const int chunk = a.group_chunk[li >> 5];
+    const In1 in{a.h, a.l, a.c};
+    for (int k = 1; (long long)k * chunk < a.n; ++k) {
+        const size_t sidx = (size_t)k * a.n_combos + li, pidx = sidx - a.n_combos;
+        if (a.exact[sidx]) continue;
+        const uint4* ps = reinterpret_cast<const uint4*>(a.st_start + sidx * 8);
+        const uint4* pe = reinterpret_cast<const uint4*>(a.st_end + pidx * 8);
+        const uint4 s0 = ps[0], s1 = ps[1], e0 = pe[0], e1 = pe[1];
+        if (s0.x == e0.x && s0.y == e0.y && s0.z == e0.z && s0.w == e0.w && s1.x == e1.x && s1.y == e1.y &&
+            s1.z == e1.z && s1.w == e1.w)
+            continue;
+        const int c0 = k * chunk, c1 = min(c0 + chunk, a.n);
+        Op op;
+        op.init(a.periods[li], a.factors ? a.factors[li] : 0.f, a.first);
+        float w[8];
+        for (int i = 0; i < 8; ++i) w[i] = a.st_end[pidx * 8 + i];
+        op.load(w, in, c0);
+        for (int t = c0; t < c1; ++t) {
+            float o1;
+            const float o0 = op.step(in, t, o1);
+            a.out0[(size_t)li * a.n + t] = o0;
+            if (Op::kTwo) a.out1[(size_t)li * a.n + t] = o1;
+        }
+        op.save(w);
+        store_state(a.st_end + sidx * 8, w);
+        atomicAdd(a.fixups, 1);
+    }
+}
+
+}  // namespace
+
+vta_status launch_hlc_chunk(const HlcChunkArgs& a, cudaStream_t st) {
+    const unsigned blocks = ceil_div(a.n_items, kCW);
+    const unsigned fix_blocks = ceil_div(a.n_combos, 128);
+    ktimer_begin(st);
+    if (a.kind == 0) {
+        k_hlc_chunk<hlc::PAdx><<<blocks, kCW * 32, 0, st>>>(a);
+        VTA_TRY(check_launch("k_hlc_chunk<adx>"));
+        k_hlc_chunk_fixup<hlc::PAdx><<<fix_blocks, 128, 0, st>>>(a);
+    } else {
+        k_hlc_chunk<hlc::PSuperTrend><<<blocks, kCW * 32, 0, st>>>(a);
+        VTA_TRY(check_launch("k_hlc_chunk<supertrend>"));
+        k_hlc_chunk_fixup<hlc::PSuperTrend><<<fix_blocks, 128, 0, st>>>(a);
+    }
+    ktimer_end(st);
+    return check_launch("k_hlc_chunk_fixup");
+}
+
+}  // namespace vta

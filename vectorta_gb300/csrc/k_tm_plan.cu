@@ -23,6 +23,7 @@
 
 #include "vta_internal.h"
 #include "vta_plan.h"
+#include "hlc_ops.cuh"
 
 namespace vta {
 namespace {
@@ -38,252 +39,9 @@ struct TmIn {
     __device__ float C(int t) const { return __ldg(c + (size_t)t * cols + s); }
 };
 
-// True range with the crate's NaN-skipping comparisons (atr.rs:352-366).
-__device__ __forceinline__ float true_range(float hi, float lo, float pc) {
-    float tr = hi - lo;
-    const float hc = fabsf(hi - pc);
-    if (hc > tr) tr = hc;
-    const float lc = fabsf(lo - pc);
-    if (lc > tr) tr = lc;
-    return tr;
-}
-
-// Op interface (lane-level, one series):
-//   init(job, f)                 constants; f = first valid index
-//   run_from() -> int            first t whose entering state is a running
-//                                state (everything before is seeding)
-//   start_exact()                state entering t = f
-//   start_warm(in, t0)           guessed running state entering t0 > run_from()
-//   load(w, in, t0)              exact running state entering t0 from 8 words
-//   save(w)                      running state as 8 words
-//   step(in, t, o1) -> o0        process t (any phase), outputs for t
-//   stepv(t, h, l, c, o1) -> o0  the same with the inputs of t given
-//
-// ATR: atr_compute_into_scalar (atr.rs:329-460); TR(f) = h - l, seed = mean
-// of the first p TRs at s = f + p - 1, then rma = fma(-a, rma, rma) + a * tr.
-struct PAtr {
-    static constexpr bool kTwo = false;
-    int p, f;
-    float alpha, rma, pc;
-    double tr_sum;
-    __device__ void init(const PlanJob& j, int first) {
-        p = j.period;
-        f = first;
-        alpha = (float)(1.0 / (double)p);
-    }
-    __device__ int run_from() const { return f + p; }
-    __device__ void start_exact() { tr_sum = 0.0; rma = 0.f; pc = 0.f; }
-    __device__ void start_warm(const TmIn& in, int t0) {
-        pc = in.C(t0 - 1);
-        rma = in.H(t0 - 1) - in.L(t0 - 1);
-    }
-    __device__ void load(const float* w, const TmIn& in, int t0) {
-        rma = w[0];
-        pc = in.C(t0 - 1);
-    }
-    __device__ void save(float* w) const {
-        w[0] = rma;
-        w[1] = w[2] = w[3] = w[4] = w[5] = w[6] = w[7] = 0.f;
-    }
-    __device__ float step(const TmIn& in, int t, float& o1) {
-        if (t < f) return qnan();
-        return stepv(t, in.H(t), in.L(t), in.C(t), o1);
-    }
-    __device__ float stepv(int t, float hi, float lo, float cl, float&) {
-        if (t < f) return qnan();
-        const float tr = (t == f) ? hi - lo : true_range(hi, lo, pc);
-        pc = cl;
-        const int s = f + p - 1;
-        if (t < s) {
-            tr_sum += (double)tr;
-            return qnan();
-        }
-        if (t == s) {
-            tr_sum += (double)tr;
-            rma = (float)(tr_sum / (double)p);
-            return rma;
-        }
-        rma = fmaf(-alpha, rma, rma) + alpha * tr;
-        return rma;
-    }
-};
-
-// ADX: adx_scalar on the slice from f (adx.rs:299-421): Wilder sums over
-// relative indices 1..=p, DX from the smoothed DM/TR, ADX = mean of the
-// first p DX, then (adx * (p - 1) + dx) / p; first output at f + 2p - 1.
-// The arithmetic is the sequential time-major kernel's (k_adx).
-struct PAdx {
-    static constexpr bool kTwo = false;
-    int p, f, dx_count;
-    float rp, omr, pm1;
-    float atr, pdm, mdm, dx_sum, adx, ph, pl, pc;
-    __device__ void init(const PlanJob& j, int first) {
-        p = j.period;
-        f = first;
-        rp = (float)(1.0 / (double)p);
-        omr = (float)(1.0 - 1.0 / (double)p);
-        pm1 = (float)p - 1.f;
-    }
-    __device__ int run_from() const { return f + 2 * p; }
-    __device__ void start_exact() {
-        atr = pdm = mdm = dx_sum = adx = ph = pl = pc = 0.f;
-        dx_count = 0;
-    }
-    __device__ void prev_inputs(const TmIn& in, int t0) {
-        ph = in.H(t0 - 1);
-        pl = in.L(t0 - 1);
-        pc = in.C(t0 - 1);
-    }
-    __device__ void start_warm(const TmIn& in, int t0) {
-        prev_inputs(in, t0);
-        atr = (float)p * (ph - pl);
-        pdm = mdm = 0.f;
-        adx = 0.f;
-        dx_count = p;
-    }
-    __device__ void load(const float* w, const TmIn& in, int t0) {
-        atr = w[0]; pdm = w[1]; mdm = w[2]; adx = w[3];
-        dx_count = p;
-        prev_inputs(in, t0);
-    }
-    __device__ void save(float* w) const {
-        w[0] = atr; w[1] = pdm; w[2] = mdm; w[3] = adx;
-        w[4] = w[5] = w[6] = w[7] = 0.f;
-    }
-    __device__ float dx_now() const {
-        float pdi = 0.f, mdi = 0.f;
-        if (atr != 0.f) { pdi = (pdm / atr) * 100.f; mdi = (mdm / atr) * 100.f; }
-        const float sdi = pdi + mdi;
-        return sdi != 0.f ? (fabsf(pdi - mdi) / sdi) * 100.f : 0.f;
-    }
-    __device__ float step(const TmIn& in, int t, float& o1) {
-        if (t < f) return qnan();
-        return stepv(t, in.H(t), in.L(t), in.C(t), o1);
-    }
-    __device__ float stepv(int t, float ch, float cl, float cc, float&) {
-        if (t < f) return qnan();
-        const int r = t - f;
-        float v = qnan();
-        if (r > 0) {
-            const float tr = fmaxf(fmaxf(ch - cl, fabsf(ch - pc)), fabsf(cl - pc));
-            const float up = ch - ph, down = pl - cl;
-            const float dp = (up > down && up > 0.f) ? up : 0.f;
-            const float dm = (down > up && down > 0.f) ? down : 0.f;
-            if (r <= p) {
-                atr += tr; pdm += dp; mdm += dm;
-                if (r == p) {
-                    dx_sum = dx_now();
-                    dx_count = 1;
-                }
-            } else {
-                atr = atr * omr + tr;
-                pdm = pdm * omr + dp;
-                mdm = mdm * omr + dm;
-                const float dx = dx_now();
-                if (dx_count < p) {
-                    dx_sum += dx;
-                    dx_count += 1;
-                    if (dx_count == p) { adx = dx_sum * rp; v = adx; }
-                } else {
-                    adx = (adx * pm1 + dx) * rp;
-                    v = adx;
-                }
-            }
-        }
-        ph = ch; pl = cl; pc = cc;
-        return v;
-    }
-};
-
-// SuperTrend: supertrend_scalar (supertrend.rs:457-550) with the ATR of the
-// slice from f computed inline; outputs trend and changed, first at f + p - 1.
-// The arithmetic is the sequential time-major kernel's (k_supertrend).
-struct PSuperTrend {
-    static constexpr bool kTwo = true;
-    int p, f;
-    float alpha, fac, atr, pub, plb, last_close, pc;
-    bool upper;
-    double tr_sum;
-    __device__ void init(const PlanJob& j, int first) {
-        p = j.period;
-        f = first;
-        alpha = (float)(1.0 / (double)p);
-        fac = j.param;
-    }
-    __device__ int run_from() const { return f + p; }
-    __device__ void start_exact() {
-        tr_sum = 0.0;
-        atr = pub = plb = last_close = pc = 0.f;
-        upper = false;
-    }
-    __device__ void start_warm(const TmIn& in, int t0) {
-        const float hi = in.H(t0 - 1), lo = in.L(t0 - 1), cl = in.C(t0 - 1);
-        atr = hi - lo;
-        const float hl2 = (hi + lo) * 0.5f;
-        pub = hl2 + fac * atr;
-        plb = hl2 - fac * atr;
-        last_close = pc = cl;
-        upper = cl <= pub;
-    }
-    __device__ void load(const float* w, const TmIn& in, int t0) {
-        atr = w[0]; pub = w[1]; plb = w[2];
-        upper = w[3] != 0.f;
-        last_close = pc = in.C(t0 - 1);
-    }
-    __device__ void save(float* w) const {
-        w[0] = atr; w[1] = pub; w[2] = plb; w[3] = upper ? 1.f : 0.f;
-        w[4] = w[5] = w[6] = w[7] = 0.f;
-    }
-    __device__ float step(const TmIn& in, int t, float& v1) {
-        v1 = qnan();
-        if (t < f) return qnan();
-        return stepv(t, in.H(t), in.L(t), in.C(t), v1);
-    }
-    __device__ float stepv(int t, float hi, float lo, float cl, float& v1) {
-        v1 = qnan();
-        if (t < f) return qnan();
-        float tr = hi - lo;
-        if (t != f) {
-            const float hc = fabsf(hi - pc);
-            if (hc > tr) tr = hc;
-            const float lc = fabsf(lo - pc);
-            if (lc > tr) tr = lc;
-        }
-        pc = cl;
-        const int warm = f + p - 1;
-        float v0 = qnan();
-        if (t < warm) {
-            tr_sum += (double)tr;
-        } else if (t == warm) {
-            tr_sum += (double)tr;
-            atr = (float)(tr_sum / (double)p);
-            const float hl2 = (hi + lo) * 0.5f;
-            pub = hl2 + fac * atr;
-            plb = hl2 - fac * atr;
-            last_close = cl;
-            if (cl <= pub) { v0 = pub; upper = true; }
-            else { v0 = plb; upper = false; }
-            v1 = 0.f;
-        } else {
-            atr = fmaf(-alpha, atr, atr) + alpha * tr;
-            const float hl2 = (hi + lo) * 0.5f;
-            const float ub = fmaf(fac, atr, hl2);
-            const float lb = fmaf(-fac, atr, hl2);
-            float cub = ub, clb = lb;
-            if (last_close <= pub) cub = fminf(cub, pub);
-            if (last_close >= plb) clb = fmaxf(clb, plb);
-            if (upper) {
-                if (cl <= cub) { v0 = cub; v1 = 0.f; }
-                else { v0 = clb; v1 = 1.f; upper = false; }
-            } else {
-                if (cl >= clb) { v0 = clb; v1 = 0.f; }
-                else { v0 = cub; v1 = 1.f; upper = true; }
-            }
-            pub = cub; plb = clb; last_close = cl;
-        }
-        return v0;
-    }
-};
+using hlc::PAtr;
+using hlc::PAdx;
+using hlc::PSuperTrend;
 
 // ------------------------------------------------ nearest-rank percentile ---
 // percentile_nearest_rank over a window of `len` values (NaN excluded),
@@ -463,7 +221,7 @@ __device__ void run_chunk(const PlanArgs& a, const PlanJob& J, int s, int k, con
     const int c1 = min(c0 + J.chunk, L);
     const int f = a.first_hlc[s];
     Op op;
-    op.init(J, f);
+    op.init(J.period, J.param, f);
     const TmIn in{a.h, a.l, a.c, (size_t)a.cols, (size_t)s};
     const size_t sidx = (size_t)k * a.cols + s;
     int t;
@@ -555,7 +313,7 @@ __device__ void fixup_series(const PlanArgs& a, const PlanJob& J, int s) {
         const int c0 = k * J.chunk;
         const int c1 = min(c0 + J.chunk, L);
         Op op;
-        op.init(J, a.first_hlc[s]);
+        op.init(J.period, J.param, a.first_hlc[s]);
         const float* we = J.st_end + pidx * 8;
         float w[8];
         for (int i = 0; i < 8; ++i) w[i] = we[i];

@@ -446,6 +446,45 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             return launch_recurrence(a, st);
         }
         case I_ADX: case I_SUPERTREND: {
+            // time-chunked with verified warm restarts unless the policy asks
+            // for the sequential kernel; per 32-combo group a chunk of at least
+            // 2x the warm length (else the group runs as one chunk)
+            const int G = (nc + 31) / 32;
+            std::vector<int> gchunk(G), gwarm(G);
+            std::vector<int2> items;
+            int max_nch = 1;
+            bool chunked = false;
+            if (ctx->policy.recur_chunk != 1) {
+                for (int g = 0; g < G; ++g) {
+                    int pm = 1;
+                    for (int i = g * 32; i < std::min(nc, g * 32 + 32); ++i) pm = std::max(pm, periods[i]);
+                    // 32 p steps shrink the guessed state's error by (1 - 1/p)^(32 p) < e^-32,
+                    // far below an f32 ulp, so the warm run (almost always) lands on the
+                    // exact state; the fix-up pass covers the rest
+                    long long w = ((32LL * pm + 64) + 31) & ~31LL;
+                    if (ctx->policy.tm_warm > 0) w = ((long long)ctx->policy.tm_warm + 31) & ~31LL;
+                    long long c = std::max<long long>(2048, 2 * w);
+                    if (ctx->policy.recur_chunk > 1) c = std::max<long long>(ctx->policy.recur_chunk, 2 * w);
+                    c = (c + 31) & ~31LL;
+                    if (2 * c > n) c = ((long long)n + 31) & ~31LL;  // one chunk: the sequential run
+                    gchunk[g] = (int)c;
+                    gwarm[g] = (int)std::min<long long>(w, INT32_MAX / 2);
+                    const int nch = (int)((n + c - 1) / c);
+                    max_nch = std::max(max_nch, nch);
+                    chunked = chunked || nch > 1;
+                    for (int k = 0; k < nch; ++k) items.push_back(make_int2(g, k));
+                }
+            }
+            if (chunked) {
+                const size_t states = (size_t)max_nch * nc;
+                ar.need(G * sizeof(int));
+                ar.need(G * sizeof(int));
+                ar.need(items.size() * sizeof(int2));
+                ar.need(states * 8 * sizeof(float));
+                ar.need(states * 8 * sizeof(float));
+                ar.need(states);
+                ar.need(sizeof(int));
+            }
             VTA_TRY(ar.commit());
             int* d_per = ar.take<int>(nc);
             ar.take<double>(nc);
@@ -454,6 +493,36 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             ar.take<float>(nc);
             VTA_TRY(upload(ctx, d_per, periods.data(), nc * sizeof(int)));
             VTA_TRY(upload(ctx, d_fa, fa.data(), nc * sizeof(float)));
+            if (chunked) {
+                const size_t states = (size_t)max_nch * nc;
+                HlcChunkArgs c{};
+                c.kind = ind == I_ADX ? 0 : 1;
+                c.h = in.p[0]; c.l = in.p[1]; c.c = in.p[2];
+                c.n = n;
+                c.first = (int)first;
+                c.periods = d_per;
+                c.factors = ind == I_SUPERTREND ? d_fa : nullptr;
+                c.n_combos = nc;
+                int* d_gc = ar.take<int>(G);
+                int* d_gw = ar.take<int>(G);
+                int2* d_items = ar.take<int2>(items.size());
+                c.st_start = ar.take<float>(states * 8);
+                c.st_end = ar.take<float>(states * 8);
+                c.exact = ar.take<unsigned char>(states);
+                c.fixups = ar.take<int>(1);
+                VTA_TRY(upload(ctx, d_gc, gchunk.data(), G * sizeof(int)));
+                VTA_TRY(upload(ctx, d_gw, gwarm.data(), G * sizeof(int)));
+                VTA_TRY(upload(ctx, d_items, items.data(), items.size() * sizeof(int2)));
+                VTA_CUDA_TRY(cudaMemsetAsync(c.fixups, 0, sizeof(int), st));
+                c.group_chunk = d_gc;
+                c.group_warm = d_gw;
+                c.items = d_items;
+                c.n_items = (int)items.size();
+                c.out0 = out[0];
+                c.out1 = ind == I_SUPERTREND ? out[1] : nullptr;
+                ctx->last_kernel = ind == I_ADX ? "adx_chunked" : "supertrend_chunked";
+                return launch_hlc_chunk(c, st);
+            }
             HlcArgs a{};
             a.layout = 0;
             a.h = in.p[0]; a.l = in.p[1]; a.c = in.p[2];

@@ -223,6 +223,29 @@ struct HlcArgs {
     float* out1;           // changed
 };
 vta_status launch_adx(const HlcArgs& a, cudaStream_t st);
+// Batch ADX (kind 0) / SuperTrend (kind 1) cut into time chunks with verified
+// warm restarts (k_hlc_chunk.cu); bit-identical to the sequential kernels.
+struct HlcChunkArgs {
+    int kind;
+    const float* h;
+    const float* l;
+    const float* c;
+    int n, first;
+    const int* periods;
+    const float* factors;   // supertrend
+    int n_combos;
+    const int2* items;      // {32-combo group, chunk}
+    int n_items;
+    const int* group_chunk; // chunk length per group (n: one chunk)
+    const int* group_warm;  // warm-restart steps per group (multiple of 32)
+    float* out0;
+    float* out1;
+    float* st_start;        // [max chunks][n_combos][8]
+    float* st_end;
+    unsigned char* exact;   // [max chunks][n_combos]
+    int* fixups;
+};
+vta_status launch_hlc_chunk(const HlcChunkArgs& a, cudaStream_t st);
 vta_status launch_supertrend(const HlcArgs& a, cudaStream_t st);
 
 // ------------------------------------------------- prefix-sum windows ------

@@ -300,6 +300,8 @@ vta_status plan_create(vta_ctx* ctx, const float* h, const float* l, const float
         J.pfrac = in.param * 0.01;
         J.out0 = in.d_out0;
         J.out1 = in.d_out1;
+        // (1 - 1/p)^(32 p) < e^-32: the guessed state's error decays far below an
+        // f32 ulp, with room for the last ulp of difference to round away
         J.warm = ctx->policy.tm_warm > 0 ? ctx->policy.tm_warm : 32 * J.period + 64;
         P->jobs.push_back(J);
     }

@@ -100,3 +100,77 @@ def ragged_many_series(n_series: int, seed: int, min_len: int = 1000, max_len: i
         with ThreadPoolExecutor(workers) as ex:
             list(ex.map(one, range(n_series)))
     return out, lens, leads
+
+
+# ------------------------------------------------------------ GPU version ----
+# The same generator evaluated with torch on a device, for many series at once
+# (int64 arithmetic wraps like the uint64 one; shifts are made logical).  The
+# float64 results equal the numpy ones up to the last bits of exp/log/cos, so
+# the float32 series agree with ohlcv() to rounding.
+def _i64(u: int) -> int:
+    u &= (1 << 64) - 1
+    return u - (1 << 64) if u >= (1 << 63) else u
+
+
+def _lsr(z, k: int):
+    return (z >> k) & ((1 << (64 - k)) - 1)
+
+
+def _splitmix64_t(x):
+    z = x + _i64(0x9E3779B97F4A7C15)
+    z = (z ^ _lsr(z, 30)) * _i64(0xBF58476D1CE4E5B9)
+    z = (z ^ _lsr(z, 27)) * _i64(0x94D049BB133111EB)
+    return z ^ _lsr(z, 31)
+
+
+def _base_t(torch, seeds, stream: int, device):
+    return torch.tensor([_i64(((s & 0xFFFFFF) << 40) | ((stream & 0xFF) << 32)) for s in seeds], dtype=torch.int64,
+                        device=device)
+
+
+def _uniform_t(torch, base_e, idx):
+    z = _splitmix64_t(base_e + idx)
+    return (_lsr(z, 11).to(torch.float64) + 0.5) * (1.0 / 9007199254740992.0)
+
+
+def _normal_t(torch, seeds, rep, stream: int, idx, device):
+    b1 = torch.repeat_interleave(_base_t(torch, seeds, 2 * stream, device), rep)
+    b2 = torch.repeat_interleave(_base_t(torch, seeds, 2 * stream + 1, device), rep)
+    u1 = _uniform_t(torch, b1, idx)
+    u2 = _uniform_t(torch, b2, idx)
+    return torch.sqrt(-2.0 * torch.log(u1)) * torch.cos(2.0 * np.pi * u2)
+
+
+def ohlc_many_torch(lens, seeds, leads, device="cuda", sigma: float = 0.01, hl_sigma: float = 0.004):
+    """high, low, close of series s = ohlcv(lens[s], seeds[s], leads[s]),
+    concatenated as float32 device tensors, plus the int64 segment offsets."""
+    import torch
+
+    lens = [int(v) for v in lens]
+    rep = torch.tensor(lens, dtype=torch.int64, device=device)
+    offs = torch.zeros(len(lens), dtype=torch.int64, device=device)
+    offs[1:] = torch.cumsum(rep, 0)[:-1]
+    total = int(sum(lens))
+    j = torch.arange(total, dtype=torch.int64, device=device) - torch.repeat_interleave(offs, rep)
+    # random walk: x[0] = 0, x[j] = sum of eps[0..j-1], eps = sigma * normal(seed, 0, .)
+    eps = sigma * _normal_t(torch, seeds, rep, 0, j - 1, device)
+    eps[j == 0] = 0.0
+    cs = torch.cumsum(eps, 0)
+    del eps
+    close = 100.0 * torch.exp(cs - torch.repeat_interleave(cs[offs], rep))
+    del cs
+    opn = torch.empty_like(close)
+    opn[1:] = close[:-1]
+    first = j == 0
+    opn[first] = close[first]
+    hi = torch.maximum(opn, close) * (1.0 + torch.abs(hl_sigma * _normal_t(torch, seeds, rep, 1, j, device)))
+    lo = torch.minimum(opn, close) * (1.0 - torch.abs(hl_sigma * _normal_t(torch, seeds, rep, 2, j, device)))
+    del opn
+    lead = torch.repeat_interleave(torch.tensor([int(v) for v in leads], dtype=torch.int64, device=device), rep)
+    nan = j < lead
+    out = []
+    for a in (hi, lo, close):
+        a = a.to(torch.float32)
+        a[nan] = float("nan")
+        out.append(a)
+    return out[0], out[1], out[2], offs
