@@ -95,6 +95,29 @@ def workload_ema_small():
             "config": {"workload": "ema_small", "bars": n, "seed": 1, "combos": 999}}
 
 
+def workload_adx_sweep():
+    """ADX sweep, periods 2..400 (399 combos) on 1,000,000 OHLC bars (seed 3,
+    NaN lead 100): the single-series ADX path (time-chunked, verified warm
+    restarts)."""
+    from vectorta_gb300 import datagen
+
+    n = 1_000_000
+    d = datagen.ohlcv(n, seed=3, nan_lead=100)
+    series = {k: d[k].astype(np.float32) for k in ("high", "low", "close")}
+    return {"name": "adx_sweep", "n": n, "series": series,
+            "jobs": [("adx", ["high", "low", "close"], {"period": (2, 400, 1)})], "dominant": "adx",
+            "config": {"workload": "adx_sweep", "bars": n, "seed": 3, "nan_lead": 100, "combos": 399}}
+
+
+def workload_ragged_small():
+    """Profiling case of the many-series plan: 1,024 series of length
+    U[1000, 20000] (seed 4), the four jobs of ragged_tm."""
+    wl = workload_ragged_tm(n_series=1024, max_len=20000)
+    wl["name"] = "ragged_small"
+    wl["config"] = dict(wl["config"], workload="ragged_small_plan", series=1024, lengths="U[1000, 20000]")
+    return wl
+
+
 def workload_alma_small():
     """Profiling case: the 17,920-combo ALMA grid on 20,000 bars (1.4 GB of
     outputs: larger than L2, a few GB on the device at most)."""
@@ -107,13 +130,13 @@ def workload_alma_small():
     return w
 
 
-def workload_ragged_tm():
+def workload_ragged_tm(n_series=4096, max_len=50000):
     """4,096 OHLCV series of uneven length (U[1000, 50000]) and NaN lead
     (U[0, 500]), time-major and padded with NaN, through one many-series plan
     running ATR(14), ADX(14), SuperTrend(10, 3.0) and percentile(50, 50%)."""
     from vectorta_gb300 import datagen
 
-    d, lens, leads = datagen.ragged_many_series(4096, seed=4, fields=("high", "low", "close"))
+    d, lens, leads = datagen.ragged_many_series(n_series, seed=4, max_len=max_len, fields=("high", "low", "close"))
     jobs = [("atr", 14, 0.0, 1), ("adx", 14, 0.0, 1), ("supertrend", 10, 3.0, 2),
             ("percentile_nearest_rank", 50, 50.0, 1)]
     return {"name": "ragged_tm", "kind": "plan", "tm": d, "lens": lens, "plan_jobs": jobs,
@@ -136,7 +159,8 @@ def workload_served_stream():
                        "sweep_size": "log-uniform 1..4096 combos, capped at the grid"}}
 
 
-WORKLOADS = {"sweeps": workload_sweeps, "ragged_tm": workload_ragged_tm, "served_stream": workload_served_stream, "alma_grid": workload_alma_grid, "ema_small": workload_ema_small,
+WORKLOADS = {"sweeps": workload_sweeps, "ragged_tm": workload_ragged_tm, "served_stream": workload_served_stream,
+             "adx_sweep": workload_adx_sweep, "ragged_small": workload_ragged_small, "alma_grid": workload_alma_grid, "ema_small": workload_ema_small,
              "alma_small": workload_alma_small}
 
 
@@ -286,6 +310,8 @@ def cpu_sample(wl, budget_rows=None):
                 tasks.append((lambda p=p: O.donchian(s["high"], s["low"], p, fast=True), 3 * wl["n"]))
             elif name == "willr":
                 tasks.append((lambda p=p: O.willr(s["high"], s["low"], s["close"], p, fast=True), wl["n"]))
+            elif name == "adx":
+                tasks.append((lambda p=p: O.adx(s["high"], s["low"], s["close"], p), wl["n"]))
     return tasks
 
 
@@ -438,8 +464,12 @@ def gpu_bench_plan(args, wl):
     alg = sum_len * sum(PLAN_BYTES[j[0]] for j in wl["plan_jobs"])
     hbm, src = peaks()
 
-    # plain per-request path: one many-series call per indicator, padded matrix
-    inds = {k: V.CLASSES[k](0, ctx=ctx) for k in PLAIN_PARAMS}
+    # plain per-request path: one many-series call per indicator, padded matrix,
+    # with the plain sequential kernels (policy recur_chunk=sequential)
+    pctx = V.Context(0)
+    pctx.set_stream(stream.cuda_stream)
+    pctx.set_policy("recur_chunk", "sequential")
+    inds = {k: V.CLASSES[k](0, ctx=pctx) for k in PLAIN_PARAMS}
     p_out = {k: [torch.empty(rows, cols, device=dev) for _ in range(2 if k == "supertrend" else 1)]
              for k in PLAIN_PARAMS}
 
@@ -490,7 +520,7 @@ def gpu_bench_plan(args, wl):
                  "n_items": info["n_items"], "fixups_last_run": info["fixups"]},
         "plain_per_request": {"ms_per_step": plain_ms, "value": out_per_step / (plain_ms / 1e3),
                               "note": "ATR/ADX/SuperTrend/percentile many-series entry points, one call each, "
-                                      "over the padded matrix"},
+                                      "over the padded matrix, plain sequential kernels"},
     }
 
 
@@ -794,7 +824,8 @@ TRAFFIC = {
     "alma_small": 15.215616e6 + 1382.070e6,
 }
 KERNEL_NAME = {"recurrence_window_sweeps": "k_recur<OpEma, batch, EMIT>", "alma_grid": "k_wwma_tc<fp16x3>",
-               "ema_small": "k_recur<OpEma, batch, EMIT>", "alma_small": "k_wwma_tc<fp16x3>"}
+               "ema_small": "k_recur<OpEma, batch, EMIT>", "alma_small": "k_wwma_tc<fp16x3>",
+               "adx_sweep": "k_hlc_chunk<adx> + fix-up"}
 
 
 def main():

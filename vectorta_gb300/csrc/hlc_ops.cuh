@@ -12,6 +12,7 @@
 //   save(w)                      running state as 8 words
 //   step(in, t, o1) -> o0        process t (any phase), outputs for t
 //   stepv(t, h, l, c, o1) -> o0  the same with the inputs of t given
+//   step_run(h, l, c, o1) -> o0  stepv for t >= run_from() without phase checks
 // `In` provides H(t), L(t), C(t).  The arithmetic of each op is that of the
 // sequential kernels in k_hlc.cu, so a run that starts at the series start is
 // bit-identical to them.
@@ -32,6 +33,17 @@ __device__ __forceinline__ float true_range(float hi, float lo, float pc) {
     const float lc = fabsf(lo - pc);
     if (lc > tr) tr = lc;
     return tr;
+}
+
+// DX from the smoothed DM and TR sums.  The crate forms +DI = 100 pdm / atr and
+// -DI = 100 mdm / atr, then DX = 100 |+DI - -DI| / (+DI + -DI); the common
+// factor 100 / atr cancels, leaving one division.  atr == 0 gives 0 (both DI
+// are 0) and a NaN atr gives NaN, as in the crate.
+__device__ __forceinline__ float adx_dx(float pdm, float mdm, float atr) {
+    if (atr == 0.f) return 0.f;
+    const float s = pdm + mdm;
+    const float d = s != 0.f ? (fabsf(pdm - mdm) / s) * 100.f : 0.f;
+    return atr == atr ? d : qnan();
 }
 
 // ATR: atr_compute_into_scalar (atr.rs:329-460); TR(f) = h - l, seed = mean
@@ -81,6 +93,13 @@ struct PAtr {
         rma = fmaf(-alpha, rma, rma) + alpha * tr;
         return rma;
     }
+    // stepv for t >= run_from(): the running update alone
+    __device__ __forceinline__ float step_run(float hi, float lo, float cl, float&) {
+        const float tr = true_range(hi, lo, pc);
+        pc = cl;
+        rma = fmaf(-alpha, rma, rma) + alpha * tr;
+        return rma;
+    }
 };
 
 // ADX: adx_scalar on the slice from f (adx.rs:299-421): Wilder sums over
@@ -126,10 +145,7 @@ struct PAdx {
         w[4] = w[5] = w[6] = w[7] = 0.f;
     }
     __device__ float dx_now() const {
-        float pdi = 0.f, mdi = 0.f;
-        if (atr != 0.f) { pdi = (pdm / atr) * 100.f; mdi = (mdm / atr) * 100.f; }
-        const float sdi = pdi + mdi;
-        return sdi != 0.f ? (fabsf(pdi - mdi) / sdi) * 100.f : 0.f;
+        return adx_dx(pdm, mdm, atr);
     }
     template <class In> __device__ float step(const In& in, int t, float& o1) {
         if (t < f) return qnan();
@@ -167,6 +183,19 @@ struct PAdx {
         }
         ph = ch; pl = cl; pc = cc;
         return v;
+    }
+    // stepv for t >= run_from(): the running update alone
+    __device__ __forceinline__ float step_run(float ch, float cl, float cc, float&) {
+        const float tr = fmaxf(fmaxf(ch - cl, fabsf(ch - pc)), fabsf(cl - pc));
+        const float up = ch - ph, down = pl - cl;
+        const float dp = (up > down && up > 0.f) ? up : 0.f;
+        const float dm = (down > up && down > 0.f) ? down : 0.f;
+        atr = atr * omr + tr;
+        pdm = pdm * omr + dp;
+        mdm = mdm * omr + dm;
+        adx = (adx * pm1 + adx_dx(pdm, mdm, atr)) * rp;
+        ph = ch; pl = cl; pc = cc;
+        return adx;
     }
 };
 
@@ -256,6 +285,30 @@ struct PSuperTrend {
             }
             pub = cub; plb = clb; last_close = cl;
         }
+        return v0;
+    }
+    // stepv for t >= run_from(): the running update alone
+    __device__ __forceinline__ float step_run(float hi, float lo, float cl, float& v1) {
+        float tr = hi - lo;
+        const float hc = fabsf(hi - pc);
+        if (hc > tr) tr = hc;
+        const float lc = fabsf(lo - pc);
+        if (lc > tr) tr = lc;
+        pc = cl;
+        atr = fmaf(-alpha, atr, atr) + alpha * tr;
+        const float hl2 = (hi + lo) * 0.5f;
+        float cub = fmaf(fac, atr, hl2), clb = fmaf(-fac, atr, hl2);
+        if (last_close <= pub) cub = fminf(cub, pub);
+        if (last_close >= plb) clb = fmaxf(clb, plb);
+        float v0;
+        if (upper) {
+            if (cl <= cub) { v0 = cub; v1 = 0.f; }
+            else { v0 = clb; v1 = 1.f; upper = false; }
+        } else {
+            if (cl >= clb) { v0 = clb; v1 = 0.f; }
+            else { v0 = cub; v1 = 1.f; upper = true; }
+        }
+        pub = cub; plb = clb; last_close = cl;
         return v0;
     }
 };

@@ -4,6 +4,7 @@
 // non-linear function (DX) of the first; SuperTrend is a band state machine.
 // Both run one lane per combo (batch, staged stores) or per series
 // (time-major, coalesced) over the full series.
+#include "hlc_ops.cuh"
 #include "vta_internal.h"
 
 namespace vta {
@@ -99,20 +100,14 @@ __global__ void __launch_bounds__(kWarps * 32) k_adx(HlcArgs a) {
                     if (r <= p) {
                         atr += tr; pdm += dp; mdm += dm;
                         if (r == p) {
-                            float pdi = 0.f, mdi = 0.f;
-                            if (atr != 0.f) { pdi = (pdm / atr) * 100.f; mdi = (mdm / atr) * 100.f; }
-                            const float sdi = pdi + mdi;
-                            dx_sum = sdi != 0.f ? (fabsf(pdi - mdi) / sdi) * 100.f : 0.f;
+                            dx_sum = hlc::adx_dx(pdm, mdm, atr);
                             dx_count = 1;
                         }
                     } else {
                         atr = atr * omr + tr;
                         pdm = pdm * omr + dp;
                         mdm = mdm * omr + dm;
-                        float pdi = 0.f, mdi = 0.f;
-                        if (atr != 0.f) { pdi = (pdm / atr) * 100.f; mdi = (mdm / atr) * 100.f; }
-                        const float sdi = pdi + mdi;
-                        const float dx = sdi != 0.f ? (fabsf(pdi - mdi) / sdi) * 100.f : 0.f;
+                        const float dx = hlc::adx_dx(pdm, mdm, atr);
                         if (dx_count < p) {
                             dx_sum += dx;
                             dx_count += 1;

@@ -16,6 +16,8 @@
 // are loaded once per warp (lane j loads step tb + j, one coalesced 128-byte
 // row per array) and broadcast step by step with shuffles; outputs are staged
 // per warp in shared memory and written as 32 rows x 128 bytes.
+#include <algorithm>
+
 #include "hlc_ops.cuh"
 #include "vta_internal.h"
 
@@ -65,6 +67,8 @@ __global__ void __launch_bounds__(kCW * 32) k_hlc_chunk(HlcChunkArgs a) {
         t0 = min(a.first, c0) & ~31;
         op.start_exact();
     }
+    // from rf on every lane of the warp is in its running phase
+    const int rf = __reduce_max_sync(0xffffffffu, op.run_from());
     // tiles of 32 steps over [tb0, tend); with `emit` the outputs go to the rows
     auto tiles = [&](int tb0, int tend, bool emit) {
         for (int tb = tb0; tb < tend; tb += 32) {
@@ -76,15 +80,30 @@ __global__ void __launch_bounds__(kCW * 32) k_hlc_chunk(HlcChunkArgs a) {
                 xl = __ldg(a.l + tj);
                 xc = __ldg(a.c + tj);
             }
-            for (int j = 0; j < nt; ++j) {
-                const float hv = __shfl_sync(0xffffffffu, xh, j);
-                const float lv = __shfl_sync(0xffffffffu, xl, j);
-                const float cv = __shfl_sync(0xffffffffu, xc, j);
-                float o1;
-                const float o0 = op.stepv(tb + j, hv, lv, cv, o1);
-                if (emit) {
-                    stage0[warp][lane][j] = o0;
-                    if (Op::kTwo) stage1[warp][lane][j] = o1;
+            if (tb >= rf && nt == 32) {
+#pragma unroll 8
+                for (int j = 0; j < 32; ++j) {
+                    const float hv = __shfl_sync(0xffffffffu, xh, j);
+                    const float lv = __shfl_sync(0xffffffffu, xl, j);
+                    const float cv = __shfl_sync(0xffffffffu, xc, j);
+                    float o1;
+                    const float o0 = op.step_run(hv, lv, cv, o1);
+                    if (emit) {
+                        stage0[warp][lane][j] = o0;
+                        if (Op::kTwo) stage1[warp][lane][j] = o1;
+                    }
+                }
+            } else {
+                for (int j = 0; j < nt; ++j) {
+                    const float hv = __shfl_sync(0xffffffffu, xh, j);
+                    const float lv = __shfl_sync(0xffffffffu, xl, j);
+                    const float cv = __shfl_sync(0xffffffffu, xc, j);
+                    float o1;
+                    const float o0 = op.stepv(tb + j, hv, lv, cv, o1);
+                    if (emit) {
+                        stage0[warp][lane][j] = o0;
+                        if (Op::kTwo) stage1[warp][lane][j] = o1;
+                    }
                 }
             }
             if (emit) {
@@ -116,23 +135,40 @@ __global__ void __launch_bounds__(kCW * 32) k_hlc_chunk(HlcChunkArgs a) {
     }
 }
 
-// Per combo, chunks in order: a warm-restarted chunk whose start state is not
-// its predecessor's end state is recomputed from that end state.
+__device__ __forceinline__ bool same_state(const float* x, const float* y) {
+    const uint4* p = reinterpret_cast<const uint4*>(x);
+    const uint4* q = reinterpret_cast<const uint4*>(y);
+    const uint4 a0 = p[0], a1 = p[1], b0 = q[0], b1 = q[1];
+    return a0.x == b0.x && a0.y == b0.y && a0.z == b0.z && a0.w == b0.w && a1.x == b1.x && a1.y == b1.y &&
+           a1.z == b1.z && a1.w == b1.w;
+}
+
+// All (chunk, combo) pairs in parallel: count, per combo, the warm-restarted
+// chunks whose start state differs from the end state the kernel left before
+// them.  Combos with none need no sequential pass.
+__global__ void k_hlc_mismatch(HlcChunkArgs a) {
+    const int li = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = blockIdx.y + 1;
+    if (li >= a.n_combos) return;
+    if ((long long)k * a.group_chunk[li >> 5] >= a.n) return;
+    const size_t sidx = (size_t)k * a.n_combos + li;
+    if (a.exact[sidx]) return;
+    if (!same_state(a.st_start + sidx * 8, a.st_end + (sidx - a.n_combos) * 8)) atomicAdd(&a.need[li], 1);
+}
+
+// Per combo with a mismatch, chunks in order: a warm-restarted chunk whose
+// start state is not its predecessor's end state is recomputed from that end
+// state (which may itself have been recomputed just before).
 template <class Op>
 __global__ void k_hlc_chunk_fixup(HlcChunkArgs a) {
     const int li = blockIdx.x * blockDim.x + threadIdx.x;
-    if (li >= a.n_combos) return;
+    if (li >= a.n_combos || a.need[li] == 0) return;
     const int chunk = a.group_chunk[li >> 5];
     const In1 in{a.h, a.l, a.c};
     for (int k = 1; (long long)k * chunk < a.n; ++k) {
         const size_t sidx = (size_t)k * a.n_combos + li, pidx = sidx - a.n_combos;
         if (a.exact[sidx]) continue;
-        const uint4* ps = reinterpret_cast<const uint4*>(a.st_start + sidx * 8);
-        const uint4* pe = reinterpret_cast<const uint4*>(a.st_end + pidx * 8);
-        const uint4 s0 = ps[0], s1 = ps[1], e0 = pe[0], e1 = pe[1];
-        if (s0.x == e0.x && s0.y == e0.y && s0.z == e0.z && s0.w == e0.w && s1.x == e1.x && s1.y == e1.y &&
-            s1.z == e1.z && s1.w == e1.w)
-            continue;
+        if (same_state(a.st_start + sidx * 8, a.st_end + pidx * 8)) continue;
         const int c0 = k * chunk, c1 = min(c0 + chunk, a.n);
         Op op;
         op.init(a.periods[li], a.factors ? a.factors[li] : 0.f, a.first);
@@ -156,16 +192,17 @@ __global__ void k_hlc_chunk_fixup(HlcChunkArgs a) {
 vta_status launch_hlc_chunk(const HlcChunkArgs& a, cudaStream_t st) {
     const unsigned blocks = ceil_div(a.n_items, kCW);
     const unsigned fix_blocks = ceil_div(a.n_combos, 128);
+    const dim3 mm_grid(fix_blocks, (unsigned)std::max(1, a.max_chunks - 1));
     ktimer_begin(st);
-    if (a.kind == 0) {
-        k_hlc_chunk<hlc::PAdx><<<blocks, kCW * 32, 0, st>>>(a);
-        VTA_TRY(check_launch("k_hlc_chunk<adx>"));
-        k_hlc_chunk_fixup<hlc::PAdx><<<fix_blocks, 128, 0, st>>>(a);
-    } else {
-        k_hlc_chunk<hlc::PSuperTrend><<<blocks, kCW * 32, 0, st>>>(a);
-        VTA_TRY(check_launch("k_hlc_chunk<supertrend>"));
-        k_hlc_chunk_fixup<hlc::PSuperTrend><<<fix_blocks, 128, 0, st>>>(a);
+    if (a.kind == 0) k_hlc_chunk<hlc::PAdx><<<blocks, kCW * 32, 0, st>>>(a);
+    else k_hlc_chunk<hlc::PSuperTrend><<<blocks, kCW * 32, 0, st>>>(a);
+    VTA_TRY(check_launch("k_hlc_chunk"));
+    if (a.max_chunks > 1) {
+        k_hlc_mismatch<<<mm_grid, 128, 0, st>>>(a);
+        VTA_TRY(check_launch("k_hlc_mismatch"));
     }
+    if (a.kind == 0) k_hlc_chunk_fixup<hlc::PAdx><<<fix_blocks, 128, 0, st>>>(a);
+    else k_hlc_chunk_fixup<hlc::PSuperTrend><<<fix_blocks, 128, 0, st>>>(a);
     ktimer_end(st);
     return check_launch("k_hlc_chunk_fixup");
 }

@@ -141,6 +141,7 @@ template <class Op>
 __device__ void run_span(Op& op, const TmIn& in, const Stage& sg, int t, int tend, bool emit, float* out0,
                          float* out1) {
     if (t >= tend) return;
+    const int rf = op.run_from();  // from here on the running update alone
     sg.load(0, in.h, in.l, in.c, in.cols, in.s, t, tend);
     int buf = 0;
     for (int tb = t; tb < tend; tb += kPB, buf ^= 1) {
@@ -151,7 +152,8 @@ __device__ void run_span(Op& op, const TmIn& in, const Stage& sg, int t, int ten
         for (int tt = tb; tt < te; ++tt) {
             const int j = tt - tb;
             float o1;
-            const float o0 = op.stepv(tt, *sg.at(buf, 0, j), *sg.at(buf, 1, j), *sg.at(buf, 2, j), o1);
+            const float hv = *sg.at(buf, 0, j), lv = *sg.at(buf, 1, j), cv = *sg.at(buf, 2, j);
+            const float o0 = tt >= rf ? op.step_run(hv, lv, cv, o1) : op.stepv(tt, hv, lv, cv, o1);
             if (emit) {
                 out0[(size_t)tt * in.cols + in.s] = o0;
                 if (Op::kTwo) out1[(size_t)tt * in.cols + in.s] = o1;

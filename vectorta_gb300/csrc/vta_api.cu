@@ -448,7 +448,7 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
         case I_ADX: case I_SUPERTREND: {
             // time-chunked with verified warm restarts unless the policy asks
             // for the sequential kernel; per 32-combo group a chunk of at least
-            // 2x the warm length (else the group runs as one chunk)
+            // the warm length (else the group runs as one chunk)
             const int G = (nc + 31) / 32;
             std::vector<int> gchunk(G), gwarm(G);
             std::vector<int2> items;
@@ -463,8 +463,8 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
                     // exact state; the fix-up pass covers the rest
                     long long w = ((32LL * pm + 64) + 31) & ~31LL;
                     if (ctx->policy.tm_warm > 0) w = ((long long)ctx->policy.tm_warm + 31) & ~31LL;
-                    long long c = std::max<long long>(2048, 2 * w);
-                    if (ctx->policy.recur_chunk > 1) c = std::max<long long>(ctx->policy.recur_chunk, 2 * w);
+                    long long c = std::max<long long>(1024, w);
+                    if (ctx->policy.recur_chunk > 1) c = std::max<long long>(ctx->policy.recur_chunk, w);
                     c = (c + 31) & ~31LL;
                     if (2 * c > n) c = ((long long)n + 31) & ~31LL;  // one chunk: the sequential run
                     gchunk[g] = (int)c;
@@ -474,6 +474,11 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
                     chunked = chunked || nch > 1;
                     for (int k = 0; k < nch; ++k) items.push_back(make_int2(g, k));
                 }
+                // longest items first (chunk + warm steps), so the long warm
+                // runs of large-period groups do not trail at the end
+                std::stable_sort(items.begin(), items.end(), [&](const int2& x, const int2& y) {
+                    return (long long)gchunk[x.x] + gwarm[x.x] > (long long)gchunk[y.x] + gwarm[y.x];
+                });
             }
             if (chunked) {
                 const size_t states = (size_t)max_nch * nc;
@@ -484,6 +489,7 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
                 ar.need(states * 8 * sizeof(float));
                 ar.need(states);
                 ar.need(sizeof(int));
+                ar.need(nc * sizeof(int));
             }
             VTA_TRY(ar.commit());
             int* d_per = ar.take<int>(nc);
@@ -510,6 +516,9 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
                 c.st_end = ar.take<float>(states * 8);
                 c.exact = ar.take<unsigned char>(states);
                 c.fixups = ar.take<int>(1);
+                c.need = ar.take<int>(nc);
+                c.max_chunks = max_nch;
+                VTA_CUDA_TRY(cudaMemsetAsync(c.need, 0, nc * sizeof(int), st));
                 VTA_TRY(upload(ctx, d_gc, gchunk.data(), G * sizeof(int)));
                 VTA_TRY(upload(ctx, d_gw, gwarm.data(), G * sizeof(int)));
                 VTA_TRY(upload(ctx, d_items, items.data(), items.size() * sizeof(int2)));
@@ -633,6 +642,19 @@ static vta_status run_tm(vta_ctx* ctx, Ind ind, const DevIn& in, size_t cols, si
         return fail(VTA_ERR_INVALID_INPUT, "matrix too large");
     const int C = (int)cols, R = (int)rows;
     const int p = (int)c.period;
+    // ADX, SuperTrend and the percentile (window <= 64) run on the many-series
+    // work-list kernels (time-chunked, bit-identical to the sequential kernels
+    // below, which the "sequential" policy keeps)
+    if (ctx->policy.recur_chunk != 1 &&
+        (ind == I_ADX || ind == I_SUPERTREND || (ind == I_PNR && c.period <= 64))) {
+        const int kind = ind == I_ADX ? 1 : ind == I_SUPERTREND ? 2 : 3;
+        ctx->last_kernel = ind == I_ADX ? "adx_tm_chunked" : ind == I_SUPERTREND ? "supertrend_tm_chunked"
+                                                                               : "percentile_tm_register";
+        if (ind == I_PNR)
+            return tm_job_enqueue(ctx, kind, p, c.a, nullptr, nullptr, in.p[0], C, R, out[0], nullptr, st);
+        return tm_job_enqueue(ctx, kind, p, c.a, in.p[0], in.p[1], in.p[2], C, R, out[0],
+                              ind == I_SUPERTREND ? out[1] : nullptr, st);
+    }
     Arena ar(ctx);
     ar.need(2 * cols * sizeof(int));  // first + first_nan
     const bool recur = ind == I_EMA || ind == I_DEMA || ind == I_TEMA || ind == I_RSI || ind == I_WILDERS ||

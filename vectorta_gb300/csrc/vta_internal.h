@@ -244,6 +244,8 @@ struct HlcChunkArgs {
     float* st_end;
     unsigned char* exact;   // [max chunks][n_combos]
     int* fixups;
+    int* need;              // [n_combos] mismatches found (zeroed before the launch)
+    int max_chunks;
 };
 vta_status launch_hlc_chunk(const HlcChunkArgs& a, cudaStream_t st);
 vta_status launch_supertrend(const HlcArgs& a, cudaStream_t st);
@@ -326,6 +328,11 @@ struct PnrArgs {
     size_t scratch_floats;
 };
 vta_status launch_percentile(const PnrArgs& a, cudaStream_t st);
+
+// One ATR (0) / ADX (1) / SuperTrend (2) / percentile (3) job of the plan
+// kernels over a rectangular time-major matrix, enqueued on st (vta_plan.cu).
+vta_status tm_job_enqueue(vta_ctx* ctx, int kind, int period, double param, const float* h, const float* l,
+                          const float* c, int cols, int rows, float* out0, float* out1, cudaStream_t st);
 
 // ------------------------------------------------- request server ---------
 int ind_by_name(const char* name);  // -1 if unknown

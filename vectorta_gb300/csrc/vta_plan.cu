@@ -421,3 +421,83 @@ vta_status vta_tm_plan_destroy(vta_tm_plan* plan) {
 }
 
 }  // extern "C"
+
+namespace vta {
+
+// One job of the plan kernels over a rectangular time-major matrix (every
+// series `rows` long): the many-series entry points of ATR, ADX, SuperTrend
+// and percentile use it.  Workspace from the context arena, chunk length
+// fixed (1,024 steps; 512 for the percentile) unless the policy sets it.
+vta_status tm_job_enqueue(vta_ctx* ctx, int kind, int period, double param, const float* h, const float* l,
+                          const float* c, int cols, int rows, float* out0, float* out1, cudaStream_t st) {
+    const bool rec = plan_job_recurrent(kind);
+    int chunk = rec ? 1024 : 512;
+    if (ctx->policy.tm_chunk > 0) chunk = ctx->policy.tm_chunk;
+    if (ctx->policy.tm_chunk < 0 || 2LL * chunk > rows) chunk = rows;  // one chunk per series
+    const int tiles = (cols + 31) / 32;
+    const int nch = (rows + chunk - 1) / chunk;
+    const size_t n_items = (size_t)tiles * nch;
+    if (n_items > (size_t)INT32_MAX) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "too many work items");
+    const size_t states = rec ? (size_t)nch * cols : 0;
+    Arena ar(ctx);
+    ar.need(cols * sizeof(int));
+    ar.need(cols * sizeof(int));
+    ar.need(cols * sizeof(int));
+    ar.need(sizeof(PlanJob));
+    ar.need(n_items * sizeof(int4));
+    ar.need(2 * sizeof(int));
+    ar.need(states * 8 * sizeof(float));
+    ar.need(states * 8 * sizeof(float));
+    ar.need(states);
+    VTA_TRY(ar.commit());
+    int* d_len = ar.take<int>(cols);
+    int* d_fh = ar.take<int>(cols);
+    int* d_fc = ar.take<int>(cols);
+    PlanJob* d_job = ar.take<PlanJob>(1);
+    int4* d_items = ar.take<int4>(n_items);
+    int* d_ctr = ar.take<int>(2);
+    PlanJob J{};
+    J.kind = kind;
+    J.period = period;
+    J.param = (float)param;
+    J.pfrac = param * 0.01;
+    J.chunk = chunk;
+    J.warm = ctx->policy.tm_warm > 0 ? ctx->policy.tm_warm : 32 * period + 64;
+    J.out0 = out0;
+    J.out1 = out1;
+    J.st_start = ar.take<float>(states * 8);
+    J.st_end = ar.take<float>(states * 8);
+    J.exact = ar.take<unsigned char>(states);
+    const std::vector<int> lens(cols, rows);
+    std::vector<int4> items;
+    items.reserve(n_items);
+    for (int k = 0; k < nch; ++k)
+        for (int g = 0; g < tiles; ++g) items.push_back(make_int4(0, g, k, 0));
+    VTA_TRY(upload_async(ctx, d_len, lens.data(), cols * sizeof(int), st));
+    VTA_TRY(upload_async(ctx, d_job, &J, sizeof(PlanJob), st));
+    VTA_TRY(upload_async(ctx, d_items, items.data(), n_items * sizeof(int4), st));
+    VTA_CUDA_TRY(cudaMemsetAsync(d_ctr, 0, 2 * sizeof(int), st));
+    PlanArgs a{};
+    a.h = h ? h : c;  // close-only jobs: the high/low scan sees close
+    a.l = l ? l : c;
+    a.c = c;
+    a.cols = cols;
+    a.rows = rows;
+    a.len = d_len;
+    a.first_hlc = d_fh;
+    a.first_c = d_fc;
+    a.jobs = d_job;
+    a.n_jobs = 1;
+    a.items = d_items;
+    a.n_items = (int)n_items;
+    a.counter = d_ctr;
+    a.stats = d_ctr + 1;
+    VTA_TRY(launch_plan_first(a, d_fh, d_fc, st));
+    ktimer_begin(st);
+    VTA_TRY(launch_tm_plan(a, tm_plan_blocks(ctx->num_sms), st));
+    VTA_TRY(launch_tm_fixup(a, st));
+    ktimer_end(st);
+    return VTA_OK;
+}
+
+}  // namespace vta
