@@ -15,25 +15,47 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kScanBlock = kScanThreads * kScanItems;  // elements per block
 
+// First valid row per series: one thread per series (coalesced across the
+// series of a row), rows examined kFvRows at a time with independent loads so
+// a NaN lead of a few hundred rows costs a few dozen memory round trips.
+constexpr int kFvRows = 16;
+
 __global__ void k_first_valid_tm(const float* __restrict__ x, int cols, int rows, int* first) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= cols) return;
-    int t = 0;
-    while (t < rows && isnan(x[(size_t)t * cols + s])) ++t;
-    first[s] = t;
+    int found = rows;
+    for (int t0 = 0; t0 < rows && found == rows; t0 += kFvRows) {
+        bool ok[kFvRows];
+#pragma unroll
+        for (int j = 0; j < kFvRows; ++j) {
+            const int t = t0 + j;
+            ok[j] = t < rows && !isnan(__ldg(x + (size_t)t * cols + s));
+        }
+#pragma unroll
+        for (int j = kFvRows - 1; j >= 0; --j)
+            if (ok[j]) found = t0 + j;
+    }
+    first[s] = found;
 }
 
 __global__ void k_first_valid_tm_hlc(const float* __restrict__ h, const float* __restrict__ l,
                                      const float* __restrict__ c, int cols, int rows, int* first) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= cols) return;
-    int t = 0;
-    while (t < rows) {
-        const size_t i = (size_t)t * cols + s;
-        if (!isnan(h[i]) && !isnan(l[i]) && !isnan(c[i])) break;
-        ++t;
+    int found = rows;
+    for (int t0 = 0; t0 < rows && found == rows; t0 += kFvRows) {
+        bool ok[kFvRows];
+#pragma unroll
+        for (int j = 0; j < kFvRows; ++j) {
+            const int t = t0 + j;
+            const size_t i = (size_t)t * cols + s;
+            ok[j] = t < rows && !isnan(__ldg(h + i)) && !isnan(__ldg(l + i)) && !isnan(__ldg(c + i));
+        }
+#pragma unroll
+        for (int j = kFvRows - 1; j >= 0; --j)
+            if (ok[j]) found = t0 + j;
     }
-    first[s] = t;
+    first[s] = found;
 }
 
 __device__ __forceinline__ double prefix_value(const float* x, int i, int first, int kind) {

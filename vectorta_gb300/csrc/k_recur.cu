@@ -25,6 +25,35 @@ namespace {
 constexpr int kWarps = 4;  // warps per block
 __device__ __forceinline__ float qnan() { return __int_as_float(0x7fc00000); }
 
+// Compensated running sum (float value + float error term, Neumaier): the
+// warm-up accumulators of the crate are f64, and GB300's FP64 rate is a
+// small fraction of FP32, so the per-step sums are kept in float pairs and
+// turned into f64 only once, at the seed.  Sums of up to a few thousand
+// terms stay within ~1e-14 relative of the f64 ones.
+struct Acc {
+    float hi, lo;
+    __device__ void zero() { hi = 0.f; lo = 0.f; }
+    // error terms of non-finite sums are dropped so that inf / NaN propagate
+    // through hi exactly as through an f64 sum
+    __device__ void add(float v) {
+        const float sum = hi + v;
+        const float bb = sum - hi;
+        const float e = (hi - (sum - bb)) + (v - bb);
+        lo += isfinite(e) ? e : 0.f;
+        hi = sum;
+    }
+    // adds the exact difference a - b
+    __device__ void add_diff(float a, float b) {
+        const float d = a - b;
+        const float bb = d - a;
+        const float e = (a - (d - bb)) - (b + bb);
+        add(d);
+        lo += isfinite(e) ? e : 0.f;
+    }
+    __device__ float f() const { return hi + lo; }
+    __device__ double d() const { return (double)hi + (double)lo; }
+};
+
 // ------------------------------------------------------------ inputs -------
 struct InBatch {
     const float *x, *h, *l, *c;
@@ -63,6 +92,18 @@ struct InTile {
     }
 };
 
+// The values of one step t of a single shared series (and of t - 1), for the
+// general path: X / C at t or t - 1, H / L at t.
+struct InStep {
+    int t;
+    float x0, x1;  // x[t], x[t-1]  (close for the high/low/close ops)
+    float h0, l0;  // h[t], l[t]
+    __device__ float X(int u) const { return u == t ? x0 : x1; }
+    __device__ float C(int u) const { return u == t ? x0 : x1; }
+    __device__ float H(int) const { return h0; }
+    __device__ float L(int) const { return l0; }
+};
+
 // ------------------------------------------------------------ ops ----------
 // Common op interface:
 //   init(p, f)            lane constants; sets f (first valid), s (seed index),
@@ -82,20 +123,20 @@ struct OpEma {
     static constexpr int NS = 1;
     float alpha, beta, y;
     int f, s, warm;
-    double wsum;
+    Acc wsum;
     int wcnt;
     __device__ void init(int p, int first) {
         double a = 2.0 / ((double)p + 1.0);
         alpha = (float)a;
         beta = (float)(1.0 - a);
         f = first; s = first + p - 1; warm = first;
-        wsum = 0.0; wcnt = 0;
+        wsum.zero(); wcnt = 0;
     }
     template <class In> __device__ void accum(const In& in, int t) {
         float v = in.X(t);
-        if (t == f || isfinite(v)) { wsum += (double)v; wcnt += 1; }
+        if (t == f || isfinite(v)) { wsum.add(v); wcnt += 1; }
     }
-    __device__ float cur_mean() const { return (float)wsum / (float)wcnt; }
+    __device__ float cur_mean() const { return wsum.f() / (float)wcnt; }
     __device__ void seed() { y = cur_mean(); }
     template <class In> __device__ int step(const In& in, int t) {
         float v = in.X(t);
@@ -178,8 +219,11 @@ struct OpTema {
     static constexpr bool kHlc = false;
     static constexpr int NS = 3;
     float per, per1, e1, e2, e3;
+    float z1, z2, z3;  // scaled state of the emit fast tiles (valid while zs)
+    bool zs;
     int f, s, warm, start2, p1;
     __device__ void init(int p, int first) {
+        zs = false;
         double pd = 2.0 / ((double)p + 1.0);
         per = (float)pd;
         per1 = (float)(1.0 - pd);
@@ -242,30 +286,31 @@ template <bool kBatchSem>
 struct OpRsi {
     static constexpr bool kHlc = false;
     static constexpr int NS = 2;
-    float inv_p, beta, ag, al, xprev;
+    float inv_p, beta, ag, al, xprev, pf;
     int f, s, warm;
-    double sg, sl;
+    Acc sg, sl;
     bool wnan;
     __device__ void init(int p, int first) {
         double ip = 1.0 / (double)p;
         inv_p = (float)ip;
+        pf = (float)p;
         beta = (float)(1.0 - ip);
         f = first; s = first + p; warm = s;
-        sg = 0.0; sl = 0.0; wnan = false;
+        sg.zero(); sl.zero(); wnan = false;
     }
     template <class In> __device__ void accum(const In& in, int t) {
         float v = in.X(t);
         if (t > f && !wnan) {
-            double d = (double)v - (double)xprev;
-            if (!isfinite(d)) wnan = true;
-            else if (d > 0.0) sg += d;
-            else if (d < 0.0) sl -= d;
+            // the f64 difference of two floats is exact; its sign is v vs xprev
+            if (!(isfinite(v) && isfinite(xprev))) wnan = true;
+            else if (v > xprev) sg.add_diff(v, xprev);
+            else if (v < xprev) sl.add_diff(xprev, v);
         }
         xprev = v;
     }
     __device__ void seed() {
         if (wnan) { ag = qnan(); al = qnan(); }
-        else { ag = (float)(sg * (double)inv_p); al = (float)(sl * (double)inv_p); }
+        else { ag = (float)(sg.d() * (double)inv_p); al = (float)(sl.d() * (double)inv_p); }
         // the crate multiplies by inv_p = 1/p in f64
     }
     template <class In> __device__ int step(const In& in, int t) {
@@ -312,15 +357,15 @@ struct OpWilders {
     static constexpr int NS = 1;
     float alpha, y;
     int f, s, warm, p;
-    double wsum;
+    Acc wsum;
     __device__ void init(int p_, int first) {
         p = p_;
         alpha = (float)(1.0 / (double)p);
         f = first; s = first + p - 1; warm = s;
-        wsum = 0.0;
+        wsum.zero();
     }
-    template <class In> __device__ void accum(const In& in, int t) { wsum += (double)in.X(t); }
-    __device__ void seed() { y = (float)(wsum * (1.0 / (double)p)); }
+    template <class In> __device__ void accum(const In& in, int t) { wsum.add(in.X(t)); }
+    __device__ void seed() { y = (float)(wsum.d() * (1.0 / (double)p)); }
     template <class In> __device__ int step(const In& in, int t) {
         float v = in.X(t);
         y = (p == 1) ? v : fmaf(v - y, alpha, y);
@@ -359,19 +404,19 @@ struct OpAtr {
     static constexpr bool kHlc = true;
     float alpha, y;
     int f, s, warm, p;
-    double wsum;
+    Acc wsum;
     __device__ void init(int p_, int first) {
         p = p_;
         alpha = (float)(1.0 / (double)p);
         f = first; s = first + p - 1; warm = s;
-        wsum = 0.0;
+        wsum.zero();
     }
     template <class In> __device__ void accum(const In& in, int t) {
         float hi = in.H(t), lo = in.L(t);
-        if (t == f) wsum += (double)hi - (double)lo;
-        else wsum += (double)true_range(hi, lo, in.C(t - 1));
+        if (t == f) wsum.add_diff(hi, lo);
+        else wsum.add(true_range(hi, lo, in.C(t - 1)));
     }
-    __device__ void seed() { y = (float)(wsum / (double)p); }
+    __device__ void seed() { y = (float)(wsum.d() / (double)p); }
     template <class In> __device__ int step(const In& in, int t) {
         float tr = true_range(in.H(t), in.L(t), in.C(t - 1));
         y = fmaf(-alpha, y, y) + alpha * tr;
@@ -418,6 +463,91 @@ __device__ __forceinline__ void run_tile(Op& op, const InTile& ti, float* row, i
     }
 }
 
+// RSI emit tile with finite inputs, in the scaled domain gs = ag p,
+// ls = al p: each lane forms its step's gain and loss once, then a step is two
+// shuffles and two FMAs; the output ratio gs / (gs + ls) is scale-free and the
+// state is scaled back at the end of the tile.
+template <bool FIN, int PASS, bool kB>
+__device__ __forceinline__ void run_tile(OpRsi<kB>& op, const InTile& ti, float* row, int& steps) {
+    if constexpr (!(FIN && PASS == PASS_EMIT)) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const float y = op.template fast<FIN>(ti, ti.tb + j, steps);
+            if (PASS == PASS_EMIT) row[j] = y;
+        }
+    } else {
+        float xp = __shfl_up_sync(0xffffffffu, ti.xv, 1);
+        if ((threadIdx.x & 31) == 0) xp = ti.xb;
+        const float d = ti.xv - xp;
+        const float gl = d > 0.f ? d : 0.f, ll = d < 0.f ? -d : 0.f;
+        float gs = op.ag * op.pf, ls = op.al * op.pf;
+        const float b = op.beta;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            gs = fmaf(b, gs, __shfl_sync(0xffffffffu, gl, j));
+            ls = fmaf(b, ls, __shfl_sync(0xffffffffu, ll, j));
+            const float den = gs + ls;
+            row[j] = den == 0.f ? 50.f : __fdividef(100.f * gs, den);
+        }
+        op.ag = gs * op.inv_p;
+        op.al = ls * op.inv_p;
+        steps += 32;
+    }
+}
+
+// TEMA emit tile with finite inputs, in the scaled domain zk = ek / a^k
+// (a = 2 / (p + 1)): a step is three FMAs and the output
+// 3 e1 - 3 e2 + e3 = (3a) z1 - (3a^2) z2 + (a^3) z3; p == 1 copies x.  The
+// scaled state stays in the op across consecutive tiles (op.zs) and is turned
+// back into e1..e3 only when another path takes over (leave_scaled), so no
+// rounding of the scale round trip accumulates.
+template <bool FIN, int PASS>
+__device__ __forceinline__ void run_tile(OpTema& op, const InTile& ti, float* row, int& steps) {
+    if constexpr (!(FIN && PASS == PASS_EMIT)) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const float y = op.template fast<FIN>(ti, ti.tb + j, steps);
+            if (PASS == PASS_EMIT) row[j] = y;
+        }
+    } else {
+        const float a = op.per, a2 = a * a, a3 = a2 * a, b = op.per1;
+        const float c1 = 3.f * a, c2 = -3.f * a2;
+        const bool copy = op.p1 == 0;
+        if (!op.zs) {
+            op.z1 = op.e1 / a;
+            op.z2 = op.e2 / a2;
+            op.z3 = op.e3 / a3;
+            op.zs = true;
+        }
+        float z1 = op.z1, z2 = op.z2, z3 = op.z3;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const float v = __shfl_sync(0xffffffffu, ti.xv, j);
+            z1 = fmaf(b, z1, v);
+            z2 = fmaf(b, z2, z1);
+            z3 = fmaf(b, z3, z2);
+            const float y = fmaf(a3, z3, fmaf(c2, z2, c1 * z1));
+            row[j] = copy ? v : y;
+        }
+        op.z1 = z1;
+        op.z2 = z2;
+        op.z3 = z3;
+        steps += 32;
+    }
+}
+
+// Ops without a scaled tile state have nothing to convert.
+template <class Op>
+__device__ __forceinline__ void leave_scaled(Op&) {}
+__device__ __forceinline__ void leave_scaled(OpTema& op) {
+    if (!op.zs) return;
+    const float a = op.per, a2 = a * a, a3 = a2 * a;
+    op.e1 = op.p1 == 0 ? op.z1 : op.z1 * a;
+    op.e2 = op.z2 * a2;
+    op.e3 = op.z3 * a3;
+    op.zs = false;
+}
+
 template <class Op, bool TM, int PASS>
 __global__ void __launch_bounds__(kWarps * 32)
 k_recur(RecurArgs a) {
@@ -427,9 +557,11 @@ k_recur(RecurArgs a) {
     const int li = group * 32 + lane;
     const bool valid = li < a.n_lanes;
     const int chunk = blockIdx.y;
-    const int c0 = chunk * a.chunk;
-    const int c1 = min(c0 + a.chunk, a.n);
+    int c0, c1;
+    recur_chunk_bounds(a, chunk, c0, c1);
     if (c0 >= a.n) return;
+    // aggregates of this chunk already came from k_agg_fast
+    if (PASS == PASS_AGG && a.agg_fallback && chunk >= a.fast_from && !a.agg_fallback[chunk]) return;
     // a warp with no valid lane has nothing to compute (whole warp leaves; the
     // kernel has no block-wide barrier)
     if (group * 32 >= a.n_lanes) return;
@@ -504,9 +636,14 @@ k_recur(RecurArgs a) {
                 } else {
                     fin = __all_sync(0xffffffffu, isfinite(ti.xv) && isfinite(ti.xb));
                 }
-                if (fin) run_tile<true, PASS>(op, ti, stage[warp][lane], steps);
-                else run_tile<false, PASS>(op, ti, stage[warp][lane], steps);
+                if (fin) {
+                    run_tile<true, PASS>(op, ti, stage[warp][lane], steps);
+                } else {
+                    leave_scaled(op);
+                    run_tile<false, PASS>(op, ti, stage[warp][lane], steps);
+                }
             } else if (PASS == PASS_EMIT && !TM) {
+                leave_scaled(op);
 #pragma unroll 8
                 for (int t = tb; t < te; ++t) stage[warp][lane][t - tb] = op.fast(in, t, steps);
             } else if (PASS == PASS_EMIT) {
@@ -520,33 +657,63 @@ k_recur(RecurArgs a) {
                 for (int t = tb; t < te; ++t) op.fast(in, t, steps);
             }
         } else {
-            // ---- general path
-            for (int t = tb; t < te; ++t) {
+            // ---- general path: per-step phase logic
+            auto gen_step = [&](const auto& in_, int t) -> float {
                 float v = qnan();
                 if (active && t >= op.f && seeded_ever) {
                     if (running) {
-                        steps += op.step(in, t);
-                        v = op.value(in, t);
+                        steps += op.step(in_, t);
+                        v = op.value(in_, t);
                     } else if (t <= op.s) {
-                        op.accum(in, t);
+                        op.accum(in_, t);
                         if (t == op.s) {
                             op.seed();
                             running = true;
-                            v = op.value(in, t);
+                            v = op.value(in_, t);
                         } else {
                             v = op.warm_value(t);
                         }
                     }
                 } else if (active && t >= op.f && !seeded_ever) {
-                    op.accum(in, t);  // never seeded (s >= n): warm-up style outputs only
+                    op.accum(in_, t);  // never seeded (s >= n): warm-up style outputs only
                     v = op.warm_value(t);
                 }
-                if (PASS == PASS_EMIT) {
-                    if (TM) {
-                        if (valid) a.out[(size_t)t * a.cols + li] = v;
-                    } else {
-                        stage[warp][lane][t - tb] = v;
+                return v;
+            };
+            if constexpr (!TM) {
+                // the tile's inputs in registers (one coalesced load per lane);
+                // each step's values are broadcast by shuffles at the top of
+                // the warp-uniform step loop, before any per-lane branch
+                const int nt = te - tb;
+                float xv = 0.f, hv = 0.f, lv = 0.f, pb = 0.f;
+                if constexpr (Op::kHlc) {
+                    if (lane < nt) {
+                        hv = __ldg(a.h + tb + lane);
+                        lv = __ldg(a.l + tb + lane);
+                        xv = __ldg(a.c + tb + lane);
                     }
+                    if (tb > 0) pb = __ldg(a.c + tb - 1);
+                } else {
+                    if (lane < nt) xv = __ldg(a.x + tb + lane);
+                    if (tb > 0) pb = __ldg(a.x + tb - 1);
+                }
+                for (int j = 0; j < nt; ++j) {
+                    InStep st;
+                    st.t = tb + j;
+                    st.x0 = __shfl_sync(0xffffffffu, xv, j);
+                    const float xm = __shfl_sync(0xffffffffu, xv, (j - 1) & 31);
+                    st.x1 = j > 0 ? xm : pb;
+                    if constexpr (Op::kHlc) {
+                        st.h0 = __shfl_sync(0xffffffffu, hv, j);
+                        st.l0 = __shfl_sync(0xffffffffu, lv, j);
+                    }
+                    const float v = gen_step(st, tb + j);
+                    if (PASS == PASS_EMIT) stage[warp][lane][j] = v;
+                }
+            } else {
+                for (int t = tb; t < te; ++t) {
+                    const float v = gen_step(in, t);
+                    if (PASS == PASS_EMIT && valid) a.out[(size_t)t * a.cols + li] = v;
                 }
             }
         }
@@ -580,121 +747,265 @@ k_recur(RecurArgs a) {
 // the affine chunk maps S -> M_k S + b_k (f64).  One warp per lane: each
 // thread composes a contiguous run of chunks, a Kogge-Stone scan across the
 // warp combines the runs, then each thread re-walks its run writing carries.
+// The maps are N x N with N the op's state size (GB300's FP64 rate is a small
+// fraction of FP32, so the scan does no f64 work for absent components).
+template <int N>
 struct Aff {
-    double m[3][3];
-    double b[3];
+    double m[N][N];
+    double b[N];
 };
 
-__device__ __forceinline__ void aff_identity(Aff& a) {
+template <int N>
+__device__ __forceinline__ void aff_identity(Aff<N>& a) {
 #pragma unroll
-    for (int r = 0; r < 3; ++r) {
+    for (int r = 0; r < N; ++r) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) a.m[r][c] = r == c ? 1.0 : 0.0;
+        for (int c = 0; c < N; ++c) a.m[r][c] = r == c ? 1.0 : 0.0;
         a.b[r] = 0.0;
     }
 }
 // returns second o first (apply `first`, then `second`)
-__device__ __forceinline__ Aff aff_then(const Aff& first, const Aff& second) {
-    Aff o;
+template <int N>
+__device__ __forceinline__ Aff<N> aff_then(const Aff<N>& first, const Aff<N>& second) {
+    Aff<N> o;
 #pragma unroll
-    for (int r = 0; r < 3; ++r) {
+    for (int r = 0; r < N; ++r) {
+        double br = second.b[r];
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
-            o.m[r][c] = second.m[r][0] * first.m[0][c] + second.m[r][1] * first.m[1][c] + second.m[r][2] * first.m[2][c];
-        o.b[r] = second.m[r][0] * first.b[0] + second.m[r][1] * first.b[1] + second.m[r][2] * first.b[2] + second.b[r];
+        for (int c = 0; c < N; ++c) {
+            double mrc = 0.0;
+#pragma unroll
+            for (int q = 0; q < N; ++q) mrc = fma(second.m[r][q], first.m[q][c], mrc);
+            o.m[r][c] = mrc;
+            br = fma(second.m[r][c], first.b[c], br);
+        }
+        o.b[r] = br;
     }
     return o;
 }
-__device__ __forceinline__ Aff aff_shfl_up(const Aff& a, int d) {
-    Aff o;
+template <int N>
+__device__ __forceinline__ Aff<N> aff_shfl_up(const Aff<N>& a, int d) {
+    Aff<N> o;
 #pragma unroll
-    for (int r = 0; r < 3; ++r) {
+    for (int r = 0; r < N; ++r) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) o.m[r][c] = __shfl_up_sync(0xffffffffu, a.m[r][c], d);
+        for (int c = 0; c < N; ++c) o.m[r][c] = __shfl_up_sync(0xffffffffu, a.m[r][c], d);
         o.b[r] = __shfl_up_sync(0xffffffffu, a.b[r], d);
     }
     return o;
 }
 
+// M^n of the op's transition, column by column from propagate.
 template <class Op>
-__device__ void chunk_map(const float4 g, int p, int chunk, const double (&ml)[3][3], Aff& a) {
+__device__ void trans_pow(double n, int p, double (&m)[Op::NS][Op::NS]) {
+    constexpr int N = Op::NS;
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+        double e[3] = {0.0, 0.0, 0.0};
+        e[c] = 1.0;
+        Op::propagate(e, n, p);
+#pragma unroll
+        for (int r = 0; r < N; ++r) m[r][c] = e[r];
+    }
+}
+
+template <class Op>
+__device__ void chunk_map(const float4 g, int p, int chunk, const double (&ml)[Op::NS][Op::NS],
+                          Aff<Op::NS>& a) {
+    constexpr int N = Op::NS;
     if (g.w == kBeforeSeed) {
         aff_identity(a);
         return;
     }
     if (g.w == kAbsolute) {
 #pragma unroll
-        for (int r = 0; r < 3; ++r)
+        for (int r = 0; r < N; ++r)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) a.m[r][c] = 0.0;
+            for (int c = 0; c < N; ++c) a.m[r][c] = 0.0;
     } else if (g.w == (float)chunk) {
 #pragma unroll
-        for (int r = 0; r < 3; ++r)
+        for (int r = 0; r < N; ++r)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) a.m[r][c] = ml[r][c];
+            for (int c = 0; c < N; ++c) a.m[r][c] = ml[r][c];
     } else {
-        for (int c = 0; c < 3; ++c) {
-            double e[3] = {0.0, 0.0, 0.0};
-            e[c] = 1.0;
-            Op::propagate(e, (double)g.w, p);
-            for (int r = 0; r < 3; ++r) a.m[r][c] = e[r];
-        }
+        trans_pow<Op>((double)g.w, p, a.m);
     }
-    a.b[0] = g.x;
-    a.b[1] = g.y;
-    a.b[2] = g.z;
+    const float gb[3] = {g.x, g.y, g.z};
+#pragma unroll
+    for (int r = 0; r < N; ++r) a.b[r] = gb[r];
 }
 
 template <class Op>
 __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
+    constexpr int N = Op::NS;
     const int lane = threadIdx.x & 31;
     const int li = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // one warp per lane of the scan
     if (li >= a.n_lanes) return;
     const int p = a.layout ? a.period : a.periods[li];
-    double ml[3][3];  // transition of a full chunk
-    for (int c = 0; c < 3; ++c) {
-        double e[3] = {0.0, 0.0, 0.0};
-        e[c] = 1.0;
-        Op::propagate(e, (double)a.chunk, p);
-        for (int r = 0; r < 3; ++r) ml[r][c] = e[r];
-    }
+    double ml[N][N];  // transition of a full chunk
+    trans_pow<Op>((double)a.chunk, p, ml);
     const float4* agg = reinterpret_cast<const float4*>(a.agg);
     float4* carry = reinterpret_cast<float4*>(a.carry);
     const int per = (n_chunks + 31) / 32;
     const int k0 = min(lane * per, n_chunks), k1 = min(k0 + per, n_chunks);
-    Aff run;
+    Aff<N> run;
     aff_identity(run);
     for (int k = k0; k < k1; ++k) {
-        Aff ak;
+        Aff<N> ak;
         chunk_map<Op>(agg[(size_t)k * a.n_lanes + li], p, a.chunk, ml, ak);
         run = aff_then(run, ak);
     }
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-        const Aff up = aff_shfl_up(run, d);
+        const Aff<N> up = aff_shfl_up(run, d);
         if (lane >= d) run = aff_then(up, run);
     }
-    Aff ex = aff_shfl_up(run, 1);
+    Aff<N> ex = aff_shfl_up(run, 1);
     if (lane == 0) aff_identity(ex);
-    double S[3] = {ex.b[0], ex.b[1], ex.b[2]};  // state at the start of chunk k0
-    for (int k = k0; k < k1; ++k) {
-        carry[(size_t)k * a.n_lanes + li] = make_float4((float)S[0], (float)S[1], (float)S[2], 0.f);
-        Aff ak;
-        chunk_map<Op>(agg[(size_t)k * a.n_lanes + li], p, a.chunk, ml, ak);
-        double t[3];
+    double S[N];  // state at the start of chunk k0
 #pragma unroll
-        for (int r = 0; r < 3; ++r) t[r] = ak.m[r][0] * S[0] + ak.m[r][1] * S[1] + ak.m[r][2] * S[2] + ak.b[r];
-        S[0] = t[0]; S[1] = t[1]; S[2] = t[2];
+    for (int r = 0; r < N; ++r) S[r] = ex.b[r];
+    for (int k = k0; k < k1; ++k) {
+        float4 cv = make_float4(0.f, 0.f, 0.f, 0.f);
+        cv.x = (float)S[0];
+        if (N > 1) cv.y = (float)S[N > 1 ? 1 : 0];
+        if (N > 2) cv.z = (float)S[N > 2 ? 2 : 0];
+        carry[(size_t)k * a.n_lanes + li] = cv;
+        Aff<N> ak;
+        chunk_map<Op>(agg[(size_t)k * a.n_lanes + li], p, a.chunk, ml, ak);
+        double t[N];
+#pragma unroll
+        for (int r = 0; r < N; ++r) {
+            double v = ak.b[r];
+#pragma unroll
+            for (int c = 0; c < N; ++c) v = fma(ak.m[r][c], S[c], v);
+            t[r] = v;
+        }
+#pragma unroll
+        for (int r = 0; r < N; ++r) S[r] = t[r];
     }
+}
+
+// ------------------------------------------------------- fast aggregates ---
+// Aggregate pass of the chunks in which every combo of a batch sweep is
+// already running (EMA, DEMA, TEMA, RSI).  A block stages the chunk's inputs
+// in shared memory, kAggTile steps at a time, and reads them back four steps
+// per 16-byte broadcast load; each thread advances kAggPer combos from a zero
+// state in a scaled state domain where a step costs one FMA per component:
+//   EMA   z = y / a                    z <- b z + x
+//   DEMA  z1 = e1 / a, z2 = e2 / a^2   z1 <- b z1 + x,  z2 <- b z2 + z1
+//   TEMA  zk = ek / a^k                z1 <- b z1 + x,  z2 <- b z2 + z1,  z3 <- b z3 + z2
+//   RSI   zg = ag p, zl = al p         zg <- b zg + gain,  zl <- b zl + loss
+// (a = 2 / (p + 1), b = 1 - a for the EMAs; b = 1 - 1/p for RSI).  The
+// chunk-end state is scaled back once.  A chunk holding a non-finite input
+// (RSI: a non-finite difference) is flagged in agg_fallback[] and left to the
+// general aggregate pass, which applies the skip / NaN rules.
+enum FastKind { FK_EMA = 0, FK_DEMA = 1, FK_TEMA = 2, FK_RSI = 3 };
+constexpr int kAggThreads = 128, kAggPer = 4, kAggTile = 1024;
+
+template <int K>
+__global__ void __launch_bounds__(kAggThreads) k_agg_fast(RecurArgs a) {
+    constexpr int NZ = K == FK_EMA ? 1 : (K == FK_TEMA ? 3 : 2);
+    __shared__ __align__(16) float s0[kAggTile];
+    __shared__ __align__(16) float s1[K == FK_RSI ? kAggTile : 4];
+    const int chunk = a.fast_from + blockIdx.y;
+    int c0, c1;
+    recur_chunk_bounds(a, chunk, c0, c1);
+    const int base = blockIdx.x * kAggThreads * kAggPer + threadIdx.x;
+    float b[kAggPer], z[kAggPer][NZ];
+#pragma unroll
+    for (int j = 0; j < kAggPer; ++j) {
+        const int li = base + j * kAggThreads;
+        const double p = li < a.n_lanes ? (double)a.periods[li] : 1.0;
+        b[j] = K == FK_RSI ? (float)(1.0 - 1.0 / p) : (float)(1.0 - 2.0 / (p + 1.0));
+#pragma unroll
+        for (int q = 0; q < NZ; ++q) z[j][q] = 0.f;
+    }
+    auto step = [&](float v, float w) {
+#pragma unroll
+        for (int j = 0; j < kAggPer; ++j) {
+            z[j][0] = fmaf(b[j], z[j][0], v);
+            if constexpr (K == FK_RSI) {
+                z[j][1] = fmaf(b[j], z[j][1], w);
+            } else {
+                if constexpr (NZ > 1) z[j][1] = fmaf(b[j], z[j][1], z[j][0]);
+                if constexpr (NZ > 2) z[j][2] = fmaf(b[j], z[j][2], z[j][1]);
+            }
+        }
+    };
+    for (int t0 = c0; t0 < c1; t0 += kAggTile) {
+        const int m = min(kAggTile, c1 - t0);
+        int bad = 0;
+        for (int i = threadIdx.x; i < m; i += kAggThreads) {
+            const float v = __ldg(a.x + t0 + i);
+            if (K == FK_RSI) {
+                const float d = v - __ldg(a.x + t0 + i - 1);  // t0 + i >= c0 > 0
+                bad |= !isfinite(d);
+                s0[i] = d > 0.f ? d : 0.f;
+                s1[i] = d < 0.f ? -d : 0.f;
+            } else {
+                bad |= !isfinite(v);
+                s0[i] = v;
+            }
+        }
+        if (__syncthreads_or(bad)) {
+            if (threadIdx.x == 0) a.agg_fallback[chunk] = 1;
+            return;
+        }
+        const int m4 = m & ~3;
+        for (int i = 0; i < m4; i += 4) {
+            const float4 v = *reinterpret_cast<const float4*>(s0 + i);
+            float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (K == FK_RSI) w = *reinterpret_cast<const float4*>(s1 + i);
+            step(v.x, w.x);
+            step(v.y, w.y);
+            step(v.z, w.z);
+            step(v.w, w.w);
+        }
+        for (int i = m4; i < m; ++i) step(s0[i], K == FK_RSI ? s1[i] : 0.f);
+        __syncthreads();
+    }
+    float4* agg = reinterpret_cast<float4*>(a.agg);
+#pragma unroll
+    for (int j = 0; j < kAggPer; ++j) {
+        const int li = base + j * kAggThreads;
+        if (li >= a.n_lanes) continue;
+        const double p = (double)a.periods[li];
+        float4 g = make_float4(0.f, 0.f, 0.f, (float)(c1 - c0));
+        if constexpr (K == FK_RSI) {
+            const float ip = (float)(1.0 / p);
+            g.x = z[j][0] * ip;
+            g.y = z[j][1] * ip;
+        } else {
+            const double al = 2.0 / (p + 1.0);
+            g.x = (float)((double)z[j][0] * al);
+            if constexpr (NZ > 1) g.y = (float)((double)z[j][1] * al * al);
+            if constexpr (NZ > 2) g.z = (float)((double)z[j][2] * al * al * al);
+        }
+        agg[(size_t)chunk * a.n_lanes + li] = g;
+    }
+}
+
+vta_status launch_agg_fast(const RecurArgs& a, int n_chunks, cudaStream_t st) {
+    const dim3 grid(ceil_div(a.n_lanes, kAggThreads * kAggPer), n_chunks - a.fast_from);
+    switch (a.kind) {
+        case RK_EMA: k_agg_fast<FK_EMA><<<grid, kAggThreads, 0, st>>>(a); break;
+        case RK_DEMA: k_agg_fast<FK_DEMA><<<grid, kAggThreads, 0, st>>>(a); break;
+        case RK_TEMA: k_agg_fast<FK_TEMA><<<grid, kAggThreads, 0, st>>>(a); break;
+        case RK_RSI: k_agg_fast<FK_RSI><<<grid, kAggThreads, 0, st>>>(a); break;
+        default: return fail(VTA_ERR_INVALID_INPUT, "fast aggregate pass: unsupported recurrence");
+    }
+    return check_launch("k_agg_fast");
 }
 
 template <class Op, bool TM>
 vta_status run(const RecurArgs& a, cudaStream_t st) {
-    const int n_chunks = (int)ceil_div(a.n, a.chunk);
+    const int n_chunks = recur_n_chunks(a.n, a.chunk, a.chunk0);
     const int groups = (int)ceil_div(a.n_lanes, 32);
     dim3 grid(ceil_div(groups, kWarps), n_chunks);
     if (n_chunks > 65535) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "recurrence: too many time chunks");
     if (n_chunks > 1) {
+        if (!TM && a.agg_fallback && a.fast_from < n_chunks) VTA_TRY(launch_agg_fast(a, n_chunks, st));
         k_recur<Op, TM, PASS_AGG><<<grid, kWarps * 32, 0, st>>>(a);
         VTA_TRY(check_launch("k_recur_agg"));
         k_recur_carry<Op><<<ceil_div((size_t)a.n_lanes * 32, 128), 128, 0, st>>>(a, n_chunks);

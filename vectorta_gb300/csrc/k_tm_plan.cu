@@ -349,20 +349,37 @@ __global__ void k_tm_fixup(PlanArgs a) {
 
 // First valid index per series within its own length: close alone and
 // high, low and close together (len[s] when there is none).
+// First valid row of each series: close alone (percentile) and high, low and
+// close together (the high/low/close jobs).  Rows are examined kFirstRows at a
+// time with independent loads (the NaN lead costs few memory round trips).
+constexpr int kFirstRows = 16;
+
 __global__ void k_plan_first(PlanArgs a, int* first_hlc, int* first_c) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= a.cols) return;
     const int L = a.len[s];
     const TmIn in{a.h, a.l, a.c, (size_t)a.cols, (size_t)s};
     int fc = L, fh = L;
-    for (int t = 0; t < L; ++t) {
-        const float cl = in.C(t);
-        if (isnan(cl)) continue;
-        if (fc == L) fc = t;
-        if (!isnan(in.H(t)) && !isnan(in.L(t))) {
-            fh = t;
-            break;
+    for (int t0 = 0; t0 < L && fh == L; t0 += kFirstRows) {
+        bool okc[kFirstRows], okh[kFirstRows];
+#pragma unroll
+        for (int j = 0; j < kFirstRows; ++j) {
+            const int t = t0 + j;
+            const bool in_len = t < L;
+            const float cv = in_len ? in.C(t) : 0.f;
+            const float hv = in_len ? in.H(t) : 0.f;
+            const float lv = in_len ? in.L(t) : 0.f;
+            okc[j] = in_len && !isnan(cv);
+            okh[j] = okc[j] && !isnan(hv) && !isnan(lv);
         }
+        int bc = L, bh = L;  // first hit of this block
+#pragma unroll
+        for (int j = kFirstRows - 1; j >= 0; --j) {
+            if (okc[j]) bc = t0 + j;
+            if (okh[j]) bh = t0 + j;
+        }
+        if (fc == L) fc = bc;
+        fh = bh;
     }
     first_c[s] = fc;
     first_hlc[s] = fh;

@@ -62,28 +62,27 @@ __device__ __forceinline__ float ds_f(DS a) { return a.hi + a.lo; }
 struct WinOut {
     float o0, o1, o2;
 };
-__device__ __forceinline__ WinOut window_eval(int kind, DS s1, DS s2, float pf, float xt,
-                                              float k1, float k2) {
+// inv_p = 1/p and inv_p2 = 1/p^2 are per-combo constants (no division per
+// output).
+__device__ __forceinline__ WinOut window_eval(int kind, DS s1, DS s2, float pf, float inv_p, float inv_p2,
+                                              float xt, float k1, float k2) {
     WinOut r;
-    const float mean = ds_f(s1) / pf;
+    const float mean = ds_f(s1) * inv_p;
     if (kind == WK_SMA) {
         r.o0 = mean;
         return r;
     }
     // p*S2 - S1^2 = p^2 * var
     const DS num = ds_sub(ds_mul_f(s2, pf), ds_sqr(s1));
-    const float var = ds_f(num) / (pf * pf);
+    const float var = ds_f(num) * inv_p2;
     if (kind == WK_STDDEV) {
         r.o0 = var <= 0.f ? 0.f : sqrtf(var) * k1;
         return r;
     }
     if (kind == WK_ZSCORE) {
         const float sd = var <= 0.f ? 0.f : sqrtf(var) * k1;
-        // (x - mean) with the mean kept in double-single
-        const DS m = {ds_f(s1), 0.f};
-        (void)m;
         const float dev = xt - mean;
-        r.o0 = (sd == 0.f || isnan(sd)) ? qnan() : dev / sd;
+        r.o0 = (sd == 0.f || isnan(sd)) ? qnan() : __fdividef(dev, sd);
         return r;
     }
     // Bollinger (population std, devtype 0)
@@ -135,6 +134,7 @@ k_prefix_window_batch(PrefixWinArgs a, int pmax) {
         const float k1 = a.k1 ? a.k1[c] : 1.f;
         const float k2 = a.k2 ? a.k2[c] : 1.f;
         const float pf = (float)p;
+        const float inv_p = 1.f / pf, inv_p2 = inv_p * inv_p;
 #pragma unroll
         for (int k = 0; k < kPwPer; ++k) {
             const int t = t0 + threadIdx.x + k * kPwThreads;
@@ -148,7 +148,7 @@ k_prefix_window_batch(PrefixWinArgs a, int pmax) {
             const int lb = pmax + threadIdx.x + k * kPwThreads - p;  // local index of t - p
             const DS w1 = ds_sub2(p1t[k], s1[lb]);
             const DS w2 = two ? ds_sub2(p2t[k], s2[lb]) : DS{0.f, 0.f};
-            const WinOut r = window_eval(a.kind, w1, w2, pf, xt[k], k1, k2);
+            const WinOut r = window_eval(a.kind, w1, w2, pf, inv_p, inv_p2, xt[k], k1, k2);
             a.out0[o] = r.o0;
             if (a.kind == WK_BB) { a.out1[o] = r.o1; a.out2[o] = r.o2; }
         }
@@ -169,6 +169,7 @@ __global__ void k_prefix_window_tm(PrefixWinTmArgs a, const int* first_nan) {
     const int warm = f + p - 1;
     const size_t S = a.cols;
     const float pf = (float)p;
+    const float inv_p = 1.f / pf, inv_p2 = inv_p * inv_p;
     auto X = [&](int t) { return __ldg(a.x_tm + (size_t)t * S + s); };
     int t = c0;
     for (; t < c1 && t < warm; ++t) {
@@ -197,7 +198,7 @@ __global__ void k_prefix_window_tm(PrefixWinTmArgs a, const int* first_nan) {
             if (a.kind == WK_BB) { a.out1[o] = qnan(); a.out2[o] = qnan(); }
             continue;
         }
-        const WinOut r = window_eval(a.kind, s1, s2, pf, a.kind == WK_ZSCORE ? X(t) : 0.f, a.k1, a.k2);
+        const WinOut r = window_eval(a.kind, s1, s2, pf, inv_p, inv_p2, a.kind == WK_ZSCORE ? X(t) : 0.f, a.k1, a.k2);
         a.out0[o] = r.o0;
         if (a.kind == WK_BB) { a.out1[o] = r.o1; a.out2[o] = r.o2; }
     }

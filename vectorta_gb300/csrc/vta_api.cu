@@ -416,9 +416,41 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
     switch (ind) {
         case I_EMA: case I_DEMA: case I_TEMA: case I_RSI: case I_WILDERS: case I_ATR: {
             const int chunk = pick_chunk(ctx, n, nc);
-            const int nch = (n + chunk - 1) / chunk;
+            // EMA/DEMA/TEMA/RSI: the last seed index of the sweep; chunks that
+            // start past it run the fast aggregate pass.  With the automatic
+            // policy chunk 0 ends just past it, so that only one short chunk
+            // takes the general seeding path.
+            const bool fast_kind = ind == I_EMA || ind == I_DEMA || ind == I_TEMA || ind == I_RSI;
+            long long s_max = 0;
+            for (int i = 0; i < nc; ++i) {
+                const long long p = periods[i];
+                const long long s = ind == I_EMA ? (long long)first + p - 1
+                                    : ind == I_DEMA ? (long long)first
+                                    : ind == I_TEMA ? (long long)first + 2 * (p - 1)
+                                    : (long long)first + p;
+                s_max = std::max(s_max, s);
+            }
+            int chunk0 = chunk;
+            if (fast_kind && ctx->policy.recur_chunk == 0 && s_max + 1 < n)
+                chunk0 = (int)std::max<long long>(32, ((s_max + 1 + 31) / 32) * 32);
+            const int nch = recur_n_chunks(n, chunk, chunk0);
+            int fast_from = nch;
+            for (int k = 1; k < nch; ++k) {
+                int c0 = 0, c1 = 0;
+                RecurArgs tmp{};
+                tmp.n = n;
+                tmp.chunk = chunk;
+                tmp.chunk0 = chunk0;
+                recur_chunk_bounds(tmp, k, c0, c1);
+                if (c0 > s_max) {
+                    fast_from = k;
+                    break;
+                }
+            }
+            const bool use_fast = fast_kind && nch > 1 && fast_from < nch;
             ar.need((size_t)nch * nc * 16);
             ar.need((size_t)nch * nc * 16);
+            ar.need((size_t)nch * sizeof(int));
             VTA_TRY(ar.commit());
             int* d_per = ar.take<int>(nc);
             ar.take<double>(nc);
@@ -427,7 +459,9 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             ar.take<float>(nc);
             float* d_agg = ar.take<float>((size_t)nch * nc * 4);
             float* d_carry = ar.take<float>((size_t)nch * nc * 4);
+            int* d_fallback = ar.take<int>(nch);
             VTA_TRY(upload(ctx, d_per, periods.data(), nc * sizeof(int)));
+            if (use_fast) VTA_CUDA_TRY(cudaMemsetAsync(d_fallback, 0, (size_t)nch * sizeof(int), st));
             RecurArgs a{};
             a.kind = ind == I_EMA ? RK_EMA : ind == I_DEMA ? RK_DEMA : ind == I_TEMA ? RK_TEMA
                    : ind == I_RSI ? RK_RSI : ind == I_WILDERS ? RK_WILDERS : RK_ATR;
@@ -439,6 +473,9 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             a.periods = d_per;
             a.n_lanes = nc;
             a.chunk = chunk;
+            a.chunk0 = chunk0;
+            a.fast_from = fast_from;
+            a.agg_fallback = use_fast ? d_fallback : nullptr;
             a.out = out[0];
             a.agg = d_agg;
             a.carry = d_carry;

@@ -198,6 +198,12 @@ struct RecurArgs {
     const double* p0;
     const double* p1;
     int chunk;             // time chunk length (multiple of 32)
+    int chunk0;            // length of chunk 0 (multiple of 32; 0 = chunk); later chunks are `chunk` long
+    // batch EMA/DEMA/TEMA/RSI: chunks >= fast_from start with every lane past
+    // its seed; their aggregates come from k_agg_fast unless it flags the chunk
+    // in agg_fallback[] (a non-finite input).  agg_fallback == null: off.
+    int fast_from;
+    int* agg_fallback;     // [n_chunks], zeroed before the launch
     float* out;            // batch [n_combos][n]; tm [n][cols]
     // scratch
     float* agg;            // [n_chunks][n_lanes] float4 (state, applied steps)
@@ -205,6 +211,17 @@ struct RecurArgs {
 };
 vta_status launch_recurrence(const RecurArgs& a, cudaStream_t st);
 int recur_state_dim(int kind);
+// Time range [c0, c1) of chunk k (chunk 0 is chunk0 long, the rest chunk).
+__host__ __device__ inline void recur_chunk_bounds(const RecurArgs& a, int k, int& c0, int& c1) {
+    const int f0 = a.chunk0 > 0 ? a.chunk0 : a.chunk;
+    c0 = k == 0 ? 0 : f0 + (k - 1) * a.chunk;
+    const int e = k == 0 ? f0 : c0 + a.chunk;
+    c1 = e < a.n ? e : a.n;
+}
+inline int recur_n_chunks(int n, int chunk, int chunk0) {
+    const int f0 = chunk0 > 0 ? chunk0 : chunk;
+    return f0 >= n ? 1 : 1 + (n - f0 + chunk - 1) / chunk;
+}
 
 // ADX (two-level recurrence) and SuperTrend (state machine).
 struct HlcArgs {
