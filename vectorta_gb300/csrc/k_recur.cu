@@ -548,10 +548,103 @@ __device__ __forceinline__ void leave_scaled(OpTema& op) {
     op.zs = false;
 }
 
+// ------------------------------------------------------- fast aggregates ---
+// AGG blocks of the chunks in which every combo of a batch sweep is already
+// running (EMA, DEMA, TEMA, RSI; chunk >= fast_from).  They share the launch
+// with the seed chunk's general-path blocks, so the long per-step seeding run
+// of chunk 0 overlaps with this work.  The block stages the chunk's inputs in
+// shared memory, kAggTile steps at a time, and reads them back four steps per
+// 16-byte broadcast load; each thread advances its combo from a zero state in
+// a scaled state domain where a step costs one FMA per component:
+//   EMA   z = y / a                    z <- b z + x
+//   DEMA  z1 = e1 / a, z2 = e2 / a^2   z1 <- b z1 + x,  z2 <- b z2 + z1
+//   TEMA  zk = ek / a^k                z1 <- b z1 + x,  z2 <- b z2 + z1,  z3 <- b z3 + z2
+//   RSI   zg = ag p, zl = al p         zg <- b zg + gain,  zl <- b zl + loss
+// (a = 2 / (p + 1), b = 1 - a for the EMAs; b = 1 - 1/p for RSI), and the
+// chunk-end state is scaled back once.  A chunk holding a non-finite input
+// (RSI: a non-finite difference) returns false and the block runs the general
+// pass, which applies the skip / NaN rules.
+enum FastKind { FK_NONE = -1, FK_EMA = 0, FK_DEMA = 1, FK_TEMA = 2, FK_RSI = 3 };
+constexpr int kAggTile = 1024;  // steps staged per round (x, or gains + losses)
+
+template <class Op> struct FastKindOf { static constexpr int k = FK_NONE; };
+template <> struct FastKindOf<OpEma> { static constexpr int k = FK_EMA; };
+template <> struct FastKindOf<OpDema> { static constexpr int k = FK_DEMA; };
+template <> struct FastKindOf<OpTema> { static constexpr int k = FK_TEMA; };
+template <> struct FastKindOf<OpRsi<true>> { static constexpr int k = FK_RSI; };
+
+// smem: 2 * kAggTile floats, 16-byte aligned.  Called by the whole block.
+template <int K>
+__device__ bool agg_fast_block(const RecurArgs& a, int chunk, int c0, int c1, float* smem) {
+    constexpr int NZ = K == FK_EMA ? 1 : (K == FK_TEMA ? 3 : 2);
+    float* s0 = smem;
+    float* s1 = smem + kAggTile;
+    const int li = blockIdx.x * blockDim.x + threadIdx.x;
+    const double p = li < a.n_lanes ? (double)a.periods[li] : 1.0;
+    const float b = K == FK_RSI ? (float)(1.0 - 1.0 / p) : (float)(1.0 - 2.0 / (p + 1.0));
+    float z[NZ];
+#pragma unroll
+    for (int q = 0; q < NZ; ++q) z[q] = 0.f;
+    auto step = [&](float v, float w) {
+        z[0] = fmaf(b, z[0], v);
+        if constexpr (K == FK_RSI) {
+            z[1] = fmaf(b, z[1], w);
+        } else {
+            if constexpr (NZ > 1) z[1] = fmaf(b, z[1], z[0]);
+            if constexpr (NZ > 2) z[2] = fmaf(b, z[2], z[1]);
+        }
+    };
+    for (int t0 = c0; t0 < c1; t0 += kAggTile) {
+        const int m = min(kAggTile, c1 - t0);
+        int bad = 0;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const float v = __ldg(a.x + t0 + i);
+            if (K == FK_RSI) {
+                const float d = v - __ldg(a.x + t0 + i - 1);  // t0 + i >= c0 > 0
+                bad |= !isfinite(d);
+                s0[i] = d > 0.f ? d : 0.f;
+                s1[i] = d < 0.f ? -d : 0.f;
+            } else {
+                bad |= !isfinite(v);
+                s0[i] = v;
+            }
+        }
+        if (__syncthreads_or(bad)) return false;
+        const int m4 = m & ~3;
+#pragma unroll 2
+        for (int i = 0; i < m4; i += 4) {
+            const float4 v = *reinterpret_cast<const float4*>(s0 + i);
+            float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (K == FK_RSI) w = *reinterpret_cast<const float4*>(s1 + i);
+            step(v.x, w.x);
+            step(v.y, w.y);
+            step(v.z, w.z);
+            step(v.w, w.w);
+        }
+        for (int i = m4; i < m; ++i) step(s0[i], K == FK_RSI ? s1[i] : 0.f);
+        __syncthreads();
+    }
+    if (li < a.n_lanes) {
+        float4 g = make_float4(0.f, 0.f, 0.f, (float)(c1 - c0));
+        if constexpr (K == FK_RSI) {
+            const float ip = (float)(1.0 / p);
+            g.x = z[0] * ip;
+            g.y = z[1] * ip;
+        } else {
+            const double al = 2.0 / (p + 1.0);
+            g.x = (float)((double)z[0] * al);
+            if constexpr (NZ > 1) g.y = (float)((double)z[1] * al * al);
+            if constexpr (NZ > 2) g.z = (float)((double)z[2] * al * al * al);
+        }
+        reinterpret_cast<float4*>(a.agg)[(size_t)chunk * a.n_lanes + li] = g;
+    }
+    return true;
+}
+
 template <class Op, bool TM, int PASS>
 __global__ void __launch_bounds__(kWarps * 32)
 k_recur(RecurArgs a) {
-    __shared__ float stage[kWarps][32][33];
+    __shared__ __align__(16) float stage[kWarps][32][33];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int group = blockIdx.x * kWarps + warp;
     const int li = group * 32 + lane;
@@ -560,8 +653,13 @@ k_recur(RecurArgs a) {
     int c0, c1;
     recur_chunk_bounds(a, chunk, c0, c1);
     if (c0 >= a.n) return;
-    // aggregates of this chunk already came from k_agg_fast
-    if (PASS == PASS_AGG && a.agg_fallback && chunk >= a.fast_from && !a.agg_fallback[chunk]) return;
+    if constexpr (PASS == PASS_AGG && !TM && FastKindOf<Op>::k != FK_NONE) {
+        static_assert(sizeof(stage) >= 2 * kAggTile * sizeof(float), "fast AGG staging");
+        if (a.fast_agg && chunk >= a.fast_from &&
+            agg_fast_block<FastKindOf<Op>::k>(a, chunk, c0, c1, &stage[0][0][0]))
+            return;
+        __syncthreads();  // the general pass below reuses `stage`
+    }
     // a warp with no valid lane has nothing to compute (whole warp leaves; the
     // kernel has no block-wide barrier)
     if (group * 32 >= a.n_lanes) return;
@@ -886,118 +984,6 @@ __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
     }
 }
 
-// ------------------------------------------------------- fast aggregates ---
-// Aggregate pass of the chunks in which every combo of a batch sweep is
-// already running (EMA, DEMA, TEMA, RSI).  A block stages the chunk's inputs
-// in shared memory, kAggTile steps at a time, and reads them back four steps
-// per 16-byte broadcast load; each thread advances kAggPer combos from a zero
-// state in a scaled state domain where a step costs one FMA per component:
-//   EMA   z = y / a                    z <- b z + x
-//   DEMA  z1 = e1 / a, z2 = e2 / a^2   z1 <- b z1 + x,  z2 <- b z2 + z1
-//   TEMA  zk = ek / a^k                z1 <- b z1 + x,  z2 <- b z2 + z1,  z3 <- b z3 + z2
-//   RSI   zg = ag p, zl = al p         zg <- b zg + gain,  zl <- b zl + loss
-// (a = 2 / (p + 1), b = 1 - a for the EMAs; b = 1 - 1/p for RSI).  The
-// chunk-end state is scaled back once.  A chunk holding a non-finite input
-// (RSI: a non-finite difference) is flagged in agg_fallback[] and left to the
-// general aggregate pass, which applies the skip / NaN rules.
-enum FastKind { FK_EMA = 0, FK_DEMA = 1, FK_TEMA = 2, FK_RSI = 3 };
-constexpr int kAggThreads = 128, kAggPer = 4, kAggTile = 1024;
-
-template <int K>
-__global__ void __launch_bounds__(kAggThreads) k_agg_fast(RecurArgs a) {
-    constexpr int NZ = K == FK_EMA ? 1 : (K == FK_TEMA ? 3 : 2);
-    __shared__ __align__(16) float s0[kAggTile];
-    __shared__ __align__(16) float s1[K == FK_RSI ? kAggTile : 4];
-    const int chunk = a.fast_from + blockIdx.y;
-    int c0, c1;
-    recur_chunk_bounds(a, chunk, c0, c1);
-    const int base = blockIdx.x * kAggThreads * kAggPer + threadIdx.x;
-    float b[kAggPer], z[kAggPer][NZ];
-#pragma unroll
-    for (int j = 0; j < kAggPer; ++j) {
-        const int li = base + j * kAggThreads;
-        const double p = li < a.n_lanes ? (double)a.periods[li] : 1.0;
-        b[j] = K == FK_RSI ? (float)(1.0 - 1.0 / p) : (float)(1.0 - 2.0 / (p + 1.0));
-#pragma unroll
-        for (int q = 0; q < NZ; ++q) z[j][q] = 0.f;
-    }
-    auto step = [&](float v, float w) {
-#pragma unroll
-        for (int j = 0; j < kAggPer; ++j) {
-            z[j][0] = fmaf(b[j], z[j][0], v);
-            if constexpr (K == FK_RSI) {
-                z[j][1] = fmaf(b[j], z[j][1], w);
-            } else {
-                if constexpr (NZ > 1) z[j][1] = fmaf(b[j], z[j][1], z[j][0]);
-                if constexpr (NZ > 2) z[j][2] = fmaf(b[j], z[j][2], z[j][1]);
-            }
-        }
-    };
-    for (int t0 = c0; t0 < c1; t0 += kAggTile) {
-        const int m = min(kAggTile, c1 - t0);
-        int bad = 0;
-        for (int i = threadIdx.x; i < m; i += kAggThreads) {
-            const float v = __ldg(a.x + t0 + i);
-            if (K == FK_RSI) {
-                const float d = v - __ldg(a.x + t0 + i - 1);  // t0 + i >= c0 > 0
-                bad |= !isfinite(d);
-                s0[i] = d > 0.f ? d : 0.f;
-                s1[i] = d < 0.f ? -d : 0.f;
-            } else {
-                bad |= !isfinite(v);
-                s0[i] = v;
-            }
-        }
-        if (__syncthreads_or(bad)) {
-            if (threadIdx.x == 0) a.agg_fallback[chunk] = 1;
-            return;
-        }
-        const int m4 = m & ~3;
-        for (int i = 0; i < m4; i += 4) {
-            const float4 v = *reinterpret_cast<const float4*>(s0 + i);
-            float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (K == FK_RSI) w = *reinterpret_cast<const float4*>(s1 + i);
-            step(v.x, w.x);
-            step(v.y, w.y);
-            step(v.z, w.z);
-            step(v.w, w.w);
-        }
-        for (int i = m4; i < m; ++i) step(s0[i], K == FK_RSI ? s1[i] : 0.f);
-        __syncthreads();
-    }
-    float4* agg = reinterpret_cast<float4*>(a.agg);
-#pragma unroll
-    for (int j = 0; j < kAggPer; ++j) {
-        const int li = base + j * kAggThreads;
-        if (li >= a.n_lanes) continue;
-        const double p = (double)a.periods[li];
-        float4 g = make_float4(0.f, 0.f, 0.f, (float)(c1 - c0));
-        if constexpr (K == FK_RSI) {
-            const float ip = (float)(1.0 / p);
-            g.x = z[j][0] * ip;
-            g.y = z[j][1] * ip;
-        } else {
-            const double al = 2.0 / (p + 1.0);
-            g.x = (float)((double)z[j][0] * al);
-            if constexpr (NZ > 1) g.y = (float)((double)z[j][1] * al * al);
-            if constexpr (NZ > 2) g.z = (float)((double)z[j][2] * al * al * al);
-        }
-        agg[(size_t)chunk * a.n_lanes + li] = g;
-    }
-}
-
-vta_status launch_agg_fast(const RecurArgs& a, int n_chunks, cudaStream_t st) {
-    const dim3 grid(ceil_div(a.n_lanes, kAggThreads * kAggPer), n_chunks - a.fast_from);
-    switch (a.kind) {
-        case RK_EMA: k_agg_fast<FK_EMA><<<grid, kAggThreads, 0, st>>>(a); break;
-        case RK_DEMA: k_agg_fast<FK_DEMA><<<grid, kAggThreads, 0, st>>>(a); break;
-        case RK_TEMA: k_agg_fast<FK_TEMA><<<grid, kAggThreads, 0, st>>>(a); break;
-        case RK_RSI: k_agg_fast<FK_RSI><<<grid, kAggThreads, 0, st>>>(a); break;
-        default: return fail(VTA_ERR_INVALID_INPUT, "fast aggregate pass: unsupported recurrence");
-    }
-    return check_launch("k_agg_fast");
-}
-
 template <class Op, bool TM>
 vta_status run(const RecurArgs& a, cudaStream_t st) {
     const int n_chunks = recur_n_chunks(a.n, a.chunk, a.chunk0);
@@ -1005,7 +991,6 @@ vta_status run(const RecurArgs& a, cudaStream_t st) {
     dim3 grid(ceil_div(groups, kWarps), n_chunks);
     if (n_chunks > 65535) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "recurrence: too many time chunks");
     if (n_chunks > 1) {
-        if (!TM && a.agg_fallback && a.fast_from < n_chunks) VTA_TRY(launch_agg_fast(a, n_chunks, st));
         k_recur<Op, TM, PASS_AGG><<<grid, kWarps * 32, 0, st>>>(a);
         VTA_TRY(check_launch("k_recur_agg"));
         k_recur_carry<Op><<<ceil_div((size_t)a.n_lanes * 32, 128), 128, 0, st>>>(a, n_chunks);

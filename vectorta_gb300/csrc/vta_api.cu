@@ -450,7 +450,6 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             const bool use_fast = fast_kind && nch > 1 && fast_from < nch;
             ar.need((size_t)nch * nc * 16);
             ar.need((size_t)nch * nc * 16);
-            ar.need((size_t)nch * sizeof(int));
             VTA_TRY(ar.commit());
             int* d_per = ar.take<int>(nc);
             ar.take<double>(nc);
@@ -459,9 +458,7 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             ar.take<float>(nc);
             float* d_agg = ar.take<float>((size_t)nch * nc * 4);
             float* d_carry = ar.take<float>((size_t)nch * nc * 4);
-            int* d_fallback = ar.take<int>(nch);
             VTA_TRY(upload(ctx, d_per, periods.data(), nc * sizeof(int)));
-            if (use_fast) VTA_CUDA_TRY(cudaMemsetAsync(d_fallback, 0, (size_t)nch * sizeof(int), st));
             RecurArgs a{};
             a.kind = ind == I_EMA ? RK_EMA : ind == I_DEMA ? RK_DEMA : ind == I_TEMA ? RK_TEMA
                    : ind == I_RSI ? RK_RSI : ind == I_WILDERS ? RK_WILDERS : RK_ATR;
@@ -475,7 +472,7 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             a.chunk = chunk;
             a.chunk0 = chunk0;
             a.fast_from = fast_from;
-            a.agg_fallback = use_fast ? d_fallback : nullptr;
+            a.fast_agg = use_fast ? 1 : 0;
             a.out = out[0];
             a.agg = d_agg;
             a.carry = d_carry;
@@ -492,15 +489,26 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             int max_nch = 1;
             bool chunked = false;
             if (ctx->policy.recur_chunk != 1) {
-                for (int g = 0; g < G; ++g) {
+                // warm length per group: 32 p steps shrink the guessed state's
+                // error by (1 - 1/p)^(32 p) < e^-32, far below an f32 ulp, so the
+                // warm run (almost always) lands on the exact state; the fix-up
+                // pass covers the rest
+                auto warm_of = [&](int g) {
                     int pm = 1;
                     for (int i = g * 32; i < std::min(nc, g * 32 + 32); ++i) pm = std::max(pm, periods[i]);
-                    // 32 p steps shrink the guessed state's error by (1 - 1/p)^(32 p) < e^-32,
-                    // far below an f32 ulp, so the warm run (almost always) lands on the
-                    // exact state; the fix-up pass covers the rest
                     long long w = ((32LL * pm + 64) + 31) & ~31LL;
                     if (ctx->policy.tm_warm > 0) w = ((long long)ctx->policy.tm_warm + 31) & ~31LL;
-                    long long c = std::max<long long>(1024, w);
+                    return w;
+                };
+                long long w_max = 0;
+                for (int g = 0; g < G; ++g) w_max = std::max(w_max, warm_of(g));
+                // an item runs warm + chunk steps; the items of every group are
+                // made about equally long (1.5 x the longest warm), so the
+                // large-period groups' items do not form the critical path
+                const long long item_len = w_max + w_max / 2;
+                for (int g = 0; g < G; ++g) {
+                    const long long w = warm_of(g);
+                    long long c = std::max<long long>(1024, item_len - w);
                     if (ctx->policy.recur_chunk > 1) c = std::max<long long>(ctx->policy.recur_chunk, w);
                     c = (c + 31) & ~31LL;
                     if (2 * c > n) c = ((long long)n + 31) & ~31LL;  // one chunk: the sequential run

@@ -199,11 +199,11 @@ struct RecurArgs {
     const double* p1;
     int chunk;             // time chunk length (multiple of 32)
     int chunk0;            // length of chunk 0 (multiple of 32; 0 = chunk); later chunks are `chunk` long
-    // batch EMA/DEMA/TEMA/RSI: chunks >= fast_from start with every lane past
-    // its seed; their aggregates come from k_agg_fast unless it flags the chunk
-    // in agg_fallback[] (a non-finite input).  agg_fallback == null: off.
+    // batch EMA/DEMA/TEMA/RSI with fast_agg != 0: chunks >= fast_from start
+    // with every lane past its seed, and their AGG blocks take the scaled
+    // one-FMA-per-component path unless the chunk holds a non-finite input
     int fast_from;
-    int* agg_fallback;     // [n_chunks], zeroed before the launch
+    int fast_agg;
     float* out;            // batch [n_combos][n]; tm [n][cols]
     // scratch
     float* agg;            // [n_chunks][n_lanes] float4 (state, applied steps)
