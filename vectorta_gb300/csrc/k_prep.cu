@@ -16,8 +16,10 @@ constexpr int kScanItems = 8;
 constexpr int kScanBlock = kScanThreads * kScanItems;  // elements per block
 
 // First valid row per series: one thread per series (coalesced across the
-// series of a row), rows examined kFvRows at a time with independent loads so
-// a NaN lead of a few hundred rows costs a few dozen memory round trips.
+// series of a row), rows examined kFvRows at a time.  The block's loads are
+// all issued before any is tested (row indices clamped into the matrix, no
+// short-circuit), so a NaN lead of a few hundred rows costs a few dozen
+// memory round trips instead of one per row.
 constexpr int kFvRows = 16;
 
 __global__ void k_first_valid_tm(const float* __restrict__ x, int cols, int rows, int* first) {
@@ -25,15 +27,12 @@ __global__ void k_first_valid_tm(const float* __restrict__ x, int cols, int rows
     if (s >= cols) return;
     int found = rows;
     for (int t0 = 0; t0 < rows && found == rows; t0 += kFvRows) {
-        bool ok[kFvRows];
+        float v[kFvRows];
 #pragma unroll
-        for (int j = 0; j < kFvRows; ++j) {
-            const int t = t0 + j;
-            ok[j] = t < rows && !isnan(__ldg(x + (size_t)t * cols + s));
-        }
+        for (int j = 0; j < kFvRows; ++j) v[j] = __ldg(x + (size_t)min(t0 + j, rows - 1) * cols + s);
 #pragma unroll
         for (int j = kFvRows - 1; j >= 0; --j)
-            if (ok[j]) found = t0 + j;
+            if ((t0 + j < rows) & !isnan(v[j])) found = t0 + j;
     }
     first[s] = found;
 }
@@ -44,16 +43,17 @@ __global__ void k_first_valid_tm_hlc(const float* __restrict__ h, const float* _
     if (s >= cols) return;
     int found = rows;
     for (int t0 = 0; t0 < rows && found == rows; t0 += kFvRows) {
-        bool ok[kFvRows];
+        float hv[kFvRows], lv[kFvRows], cv[kFvRows];
 #pragma unroll
         for (int j = 0; j < kFvRows; ++j) {
-            const int t = t0 + j;
-            const size_t i = (size_t)t * cols + s;
-            ok[j] = t < rows && !isnan(__ldg(h + i)) && !isnan(__ldg(l + i)) && !isnan(__ldg(c + i));
+            const size_t i = (size_t)min(t0 + j, rows - 1) * cols + s;
+            hv[j] = __ldg(h + i);
+            lv[j] = __ldg(l + i);
+            cv[j] = __ldg(c + i);
         }
 #pragma unroll
         for (int j = kFvRows - 1; j >= 0; --j)
-            if (ok[j]) found = t0 + j;
+            if ((t0 + j < rows) & !isnan(hv[j]) & !isnan(lv[j]) & !isnan(cv[j])) found = t0 + j;
     }
     first[s] = found;
 }

@@ -351,7 +351,9 @@ __global__ void k_tm_fixup(PlanArgs a) {
 // high, low and close together (len[s] when there is none).
 // First valid row of each series: close alone (percentile) and high, low and
 // close together (the high/low/close jobs).  Rows are examined kFirstRows at a
-// time with independent loads (the NaN lead costs few memory round trips).
+// time; the block's loads are all issued before any is tested (rows clamped
+// into the series, no short-circuit), so the NaN lead costs few memory round
+// trips.
 constexpr int kFirstRows = 16;
 
 __global__ void k_plan_first(PlanArgs a, int* first_hlc, int* first_c) {
@@ -361,22 +363,20 @@ __global__ void k_plan_first(PlanArgs a, int* first_hlc, int* first_c) {
     const TmIn in{a.h, a.l, a.c, (size_t)a.cols, (size_t)s};
     int fc = L, fh = L;
     for (int t0 = 0; t0 < L && fh == L; t0 += kFirstRows) {
-        bool okc[kFirstRows], okh[kFirstRows];
+        float hv[kFirstRows], lv[kFirstRows], cv[kFirstRows];
 #pragma unroll
         for (int j = 0; j < kFirstRows; ++j) {
-            const int t = t0 + j;
-            const bool in_len = t < L;
-            const float cv = in_len ? in.C(t) : 0.f;
-            const float hv = in_len ? in.H(t) : 0.f;
-            const float lv = in_len ? in.L(t) : 0.f;
-            okc[j] = in_len && !isnan(cv);
-            okh[j] = okc[j] && !isnan(hv) && !isnan(lv);
+            const int t = min(t0 + j, L - 1);
+            cv[j] = in.C(t);
+            hv[j] = in.H(t);
+            lv[j] = in.L(t);
         }
         int bc = L, bh = L;  // first hit of this block
 #pragma unroll
         for (int j = kFirstRows - 1; j >= 0; --j) {
-            if (okc[j]) bc = t0 + j;
-            if (okh[j]) bh = t0 + j;
+            const bool okc = (t0 + j < L) & !isnan(cv[j]);
+            if (okc) bc = t0 + j;
+            if (okc & !isnan(hv[j]) & !isnan(lv[j])) bh = t0 + j;
         }
         if (fc == L) fc = bc;
         fh = bh;
