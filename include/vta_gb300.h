@@ -69,7 +69,10 @@ void* vta_ctx_get_stream(vta_ctx* ctx);
  *   "recur_chunk" = "auto" | "sequential" | <positive multiple of 32>
  *   "tm_chunk"    = "auto" | "sequential" | <steps>   (many-series plans)
  *   "tm_warm"     = "auto" | <steps>   (plans; chunked ADX/SuperTrend sweeps)
- *   "timing"      = "on" | "off"                                         */
+ *   "timing"      = "on" | "off"
+ *   "host_io"     = "cached" | "per_call": *_batch_into_host_f32 keeps its
+ *                   device input/output buffer in the context between calls
+ *                   (cached, the default; freed by per_call or ctx destroy) */
 vta_status vta_ctx_set_policy(vta_ctx* ctx, const char* key, const char* value);
 /* selected_batch_kernel() (alma_wrapper.rs:239-245): name of the last kernel
  * path used by this context. */

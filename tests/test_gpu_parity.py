@@ -166,6 +166,27 @@ def test_batch_entry_points_agree(name, data):
         assert np.array_equal(ah, d_out[k].cpu().numpy(), equal_nan=True)
 
 
+def test_into_host_buffer_policies(data):
+    """batch_into_host_f32 with the context-cached device buffer (default,
+    grown across calls of different sizes) equals the per-call allocation."""
+    x = data["close"]
+    for name, sweeps in (("ema", ({"period": (2, 30, 1)}, {"period": (2, 200, 1)}, {"period": (5, 9, 2)})),
+                         ("donchian", ({"period": (5, 50, 5)}, {"period": (2, 100, 1)}))):
+        ind = V.CLASSES[name](0)
+        ins = inputs_of(name, data)
+        for sw in sweeps:
+            ind.set_policy("host_io", "cached")
+            a, r, c = ind.batch_into_host_f32(*ins, sweep=sw)
+            ind.set_policy("host_io", "per_call")
+            b, r2, c2 = ind.batch_into_host_f32(*ins, sweep=sw)
+            a = a if isinstance(a, tuple) else (a,)
+            b = b if isinstance(b, tuple) else (b,)
+            assert (r, c) == (r2, c2) == (a[0].shape[0], x.size)
+            for u, v in zip(a, b):
+                assert np.array_equal(u, v, equal_nan=True), (name, sw)
+        ind.set_policy("host_io", "cached")
+
+
 def tm_matrix(seed, cols=7, rows=1500):
     """cols series, series j with a NaN lead of j*3 bars (tests/alma_cuda.rs:107-113)."""
     c = np.full((rows, cols), np.nan)

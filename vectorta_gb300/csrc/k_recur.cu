@@ -266,6 +266,24 @@ struct OpTema {
     }
     __device__ float get(int i) const { return i == 0 ? e1 : (i == 1 ? e2 : e3); }
     __device__ void set(int i, float v) { if (i == 0) e1 = v; else if (i == 1) e2 = v; else e3 = v; }
+    // One general-path step for any t >= f: the arithmetic of accum / step
+    // with the phase tests (t == f, start2, s) as selects instead of branches,
+    // so the lanes of a warp in different warm-up phases do not diverge.
+    static constexpr bool kUni = true;
+    template <class In> __device__ float uni(const In& in, int t, int& steps) {
+        const float v = in.X(t);
+        steps += t > s;
+        if (p1 == 0) { e1 = v; return v; }
+        const float a1 = t == f ? v : e1;
+        e1 = a1 * per1 + v * per;
+        const float a2 = t == start2 ? e1 : e2;
+        const float n2 = a2 * per1 + e1 * per;
+        e2 = t >= start2 ? n2 : e2;
+        const float a3 = t == s ? e2 : e3;
+        const float n3 = a3 * per1 + e2 * per;
+        e3 = t >= s ? n3 : e3;
+        return t < warm ? qnan() : 3.f * e1 - 3.f * e2 + e3;
+    }
     static __device__ void propagate(double* S, double n, int p) {
         if (p == 1) { S[0] = 0.0; return; }  // p==1 carries nothing (out = x)
         double al = 2.0 / ((double)p + 1.0);
@@ -536,6 +554,10 @@ __device__ __forceinline__ void run_tile(OpTema& op, const InTile& ti, float* ro
     }
 }
 
+// Ops with a branch-free general-path step (Op::kUni) use it for t >= f.
+template <class Op, class = void> struct HasUni : std::false_type {};
+template <class Op> struct HasUni<Op, std::void_t<decltype(Op::kUni)>> : std::true_type {};
+
 // Ops without a scaled tile state have nothing to convert.
 template <class Op>
 __device__ __forceinline__ void leave_scaled(Op&) {}
@@ -758,6 +780,10 @@ k_recur(RecurArgs a) {
             // ---- general path: per-step phase logic
             auto gen_step = [&](const auto& in_, int t) -> float {
                 float v = qnan();
+                if constexpr (HasUni<Op>::value) {
+                    if (active && t >= op.f) v = op.uni(in_, t, steps);
+                    return v;
+                }
                 if (active && t >= op.f && seeded_ever) {
                     if (running) {
                         steps += op.step(in_, t);

@@ -864,23 +864,48 @@ static vta_status batch_host(vta_ctx* ctx, Ind ind, const float* const* hin, siz
     if (nc > SIZE_MAX / len) return fail(VTA_ERR_INVALID_INPUT, "rows*cols overflow");
     const size_t out_elems = nc * len;
     if (out_host && out_len < out_elems) return fail(VTA_ERR_INVALID_INPUT, "output buffer too small");
-    VTA_TRY(vram_check(out_elems * sizeof(float) * nout + len * sizeof(float) * nin));
-    // inputs -> device
+    const size_t in_bytes = len * sizeof(float) * nin;
+    const size_t out_bytes = out_elems * sizeof(float);
+    // into-host calls with the cached policy keep one device buffer for the
+    // inputs and outputs in the context (grown when too small), so repeated
+    // calls do not pay a cudaMalloc / cudaFree of their outputs each time
+    const bool cached = out_host && ctx->policy.host_io == 0;
     float* d_in = nullptr;
-    VTA_CUDA_TRY(cudaMalloc((void**)&d_in, len * sizeof(float) * nin));
-    std::unique_ptr<void, void (*)(void*)> in_guard(d_in, [](void* p) { cudaFree(p); });
+    float* d_out[3] = {nullptr, nullptr, nullptr};
+    std::unique_ptr<void, void (*)(void*)> in_guard(nullptr, [](void* p) { cudaFree(p); });
+    if (cached) {
+        const size_t in_al = (in_bytes + 255) & ~size_t(255);
+        const size_t out_al = (out_bytes + 255) & ~size_t(255);
+        const size_t need = in_al + out_al * nout;
+        if (need > ctx->io_bytes) {
+            VTA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+            if (ctx->io) cudaFree(ctx->io);
+            ctx->io = nullptr;
+            ctx->io_bytes = 0;
+            VTA_TRY(vram_check(need));
+            VTA_CUDA_TRY(cudaMalloc(&ctx->io, need));
+            ctx->io_bytes = need;
+        }
+        char* base = static_cast<char*>(ctx->io);
+        d_in = reinterpret_cast<float*>(base);
+        for (int k = 0; k < nout; ++k) d_out[k] = reinterpret_cast<float*>(base + in_al + out_al * k);
+    } else {
+        VTA_TRY(vram_check(out_bytes * nout + in_bytes));
+        VTA_CUDA_TRY(cudaMalloc((void**)&d_in, in_bytes));
+        in_guard.reset(d_in);
+        for (int k = 0; k < nout; ++k) {
+            cudaError_t e = cudaMalloc((void**)&d_out[k], out_bytes);
+            if (e != cudaSuccess) {
+                for (int j = 0; j < k; ++j) cudaFree(d_out[j]);
+                return cuda_fail(e, "cudaMalloc(output)");
+            }
+        }
+    }
+    // inputs -> device
     DevIn din{};
     for (int k = 0; k < nin; ++k) {
         din.p[k] = d_in + (size_t)k * len;
         VTA_TRY(upload(ctx, d_in + (size_t)k * len, hin[k], len * sizeof(float)));
-    }
-    float* d_out[3] = {nullptr, nullptr, nullptr};
-    for (int k = 0; k < nout; ++k) {
-        cudaError_t e = cudaMalloc((void**)&d_out[k], out_elems * sizeof(float));
-        if (e != cudaSuccess) {
-            for (int j = 0; j < k; ++j) cudaFree(d_out[j]);
-            return cuda_fail(e, "cudaMalloc(output)");
-        }
     }
     vta_status s = run_batch(ctx, ind, din, len, first, cs, d_out);
     if (s == VTA_OK && out_host) {
@@ -893,7 +918,8 @@ static vta_status batch_host(vta_ctx* ctx, Ind ind, const float* const* hin, siz
     if (s == VTA_OK) s = sync(ctx);
     cudaStreamSynchronize(ctx->stream);
     if (s != VTA_OK || out_host) {
-        for (int k = 0; k < nout; ++k) cudaFree(d_out[k]);
+        if (!cached)
+            for (int k = 0; k < nout; ++k) cudaFree(d_out[k]);
         if (s != VTA_OK) return s;
     } else {
         for (int k = 0; k < nout; ++k) *out_arr[k] = vta_device_array{d_out[k], nc, len, ctx->device};
@@ -1186,6 +1212,7 @@ vta_status vta_ctx_destroy(vta_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     if (ctx->scratch) ctx->async_alloc ? (void)cudaFreeAsync(ctx->scratch, ctx->stream) : (void)cudaFree(ctx->scratch);
     if (ctx->aux) ctx->async_alloc ? (void)cudaFreeAsync(ctx->aux, ctx->stream) : (void)cudaFree(ctx->aux);
+    if (ctx->io) cudaFree(ctx->io);
     if (ctx->async_alloc) cudaStreamSynchronize(ctx->stream);
     if (ctx->err_host) cudaFreeHost(ctx->err_host);
     if (ctx->host_stage) cudaFreeHost(ctx->host_stage);
@@ -1254,6 +1281,23 @@ vta_status vta_ctx_set_policy(vta_ctx* ctx, const char* key, const char* value) 
             long x = std::strtol(v.c_str(), &end, 10);
             if (!end || *end || x < 32 || x % 32) return fail(VTA_ERR_INVALID_POLICY, "recur_chunk: multiple of 32");
             ctx->policy.recur_chunk = (int)x;
+        }
+        return VTA_OK;
+    }
+    if (k == "host_io") {
+        if (v == "cached") {
+            ctx->policy.host_io = 0;
+        } else if (v == "per_call") {
+            ctx->policy.host_io = 1;
+            if (ctx->io) {
+                VTA_CUDA_TRY(cudaSetDevice(ctx->device));
+                VTA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+                cudaFree(ctx->io);
+                ctx->io = nullptr;
+                ctx->io_bytes = 0;
+            }
+        } else {
+            return fail(VTA_ERR_INVALID_POLICY, "host_io: cached|per_call");
         }
         return VTA_OK;
     }

@@ -56,6 +56,9 @@ struct Policy {
     // -1 = one chunk per series) and warm-restart steps (0 = 32 p + 64)
     int tm_chunk = 0;
     int tm_warm = 0;
+    // *_batch_into_host_f32: 0 = keep the device input/output buffers in the
+    // context between calls ("cached"), 1 = allocate and free them per call
+    int host_io = 0;
 };
 
 }  // namespace vta
@@ -71,6 +74,8 @@ struct vta_ctx {
     size_t scratch_bytes = 0;
     void* aux = nullptr;      // second growing device workspace (operands a launcher
     size_t aux_bytes = 0;     // builds after the call's arena pieces are taken)
+    void* io = nullptr;       // device inputs + outputs of *_batch_into_host_f32 (host_io cached)
+    size_t io_bytes = 0;
     void* host_stage = nullptr;  // pinned staging of small uploads, reused per call
     size_t host_stage_bytes = 0;
     size_t host_stage_off = 0;
