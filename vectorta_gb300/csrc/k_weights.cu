@@ -93,45 +93,44 @@ __device__ DS raw_weight(int kind, int i, int p, const RowConst& rc) {
     return {0.f, 0.f};
 }
 
-// One block per combo: raw weights summed in double-single, block reduction,
-// then a second pass writes raw * (1 / sum).
+// One warp per combo (kWThreads / 32 combos per block): raw weights summed in
+// double-single across the lanes, then a second pass writes raw * (1 / sum).
+// The per-combo f64 constants and the reciprocal are formed by lane 0 only.
 __global__ void __launch_bounds__(kWThreads) k_weights(int kind, const int* periods, const double* pa,
-                                                       const double* pb, int kmax, float* w) {
-    __shared__ float red_hi[kWThreads / 32], red_lo[kWThreads / 32];
-    __shared__ float inv_sh[2];
-    const int c = blockIdx.x;
+                                                       const double* pb, int n_combos, int kmax, float* w) {
+    const int lane = threadIdx.x & 31;
+    const int c = blockIdx.x * (kWThreads / 32) + (threadIdx.x >> 5);
+    if (c >= n_combos) return;  // whole warp (no block-wide barrier below)
     const int p = periods[c];
     RowConst rc{};
     if (kind == WT_ALMA) {
-        const double a = pa[c], b = pb[c];
-        rc.m = split(a * (double)(p - 1));
-        rc.inv2s2 = split(b * b / (2.0 * (double)p * (double)p));
+        float m_hi = 0.f, m_lo = 0.f, q_hi = 0.f, q_lo = 0.f;
+        if (lane == 0) {
+            const double a = pa[c], b = pb[c];
+            const DS m = split(a * (double)(p - 1));
+            const DS q = split(b * b / (2.0 * (double)p * (double)p));
+            m_hi = m.hi; m_lo = m.lo; q_hi = q.hi; q_lo = q.lo;
+        }
+        rc.m = DS{__shfl_sync(0xffffffffu, m_hi, 0), __shfl_sync(0xffffffffu, m_lo, 0)};
+        rc.inv2s2 = DS{__shfl_sync(0xffffffffu, q_hi, 0), __shfl_sync(0xffffffffu, q_lo, 0)};
     }
     DS s{0.f, 0.f};
-    for (int i = threadIdx.x; i < p; i += kWThreads) s = ds_add(s, raw_weight(kind, i, p, rc));
+    for (int i = lane; i < p; i += 32) s = ds_add(s, raw_weight(kind, i, p, rc));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const DS t{__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)};
         s = ds_add(s, t);
     }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float i_hi = 0.f, i_lo = 0.f;
     if (lane == 0) {
-        red_hi[warp] = s.hi;
-        red_lo[warp] = s.lo;
+        const DS inv = split(1.0 / ((double)s.hi + (double)s.lo));
+        i_hi = inv.hi;
+        i_lo = inv.lo;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double tot = 0.0;
-        for (int k = 0; k < kWThreads / 32; ++k) tot += (double)red_hi[k] + (double)red_lo[k];
-        const DS inv = split(1.0 / tot);
-        inv_sh[0] = inv.hi;
-        inv_sh[1] = inv.lo;
-    }
-    __syncthreads();
-    const DS inv{inv_sh[0], inv_sh[1]};
+    const DS inv{__shfl_sync(0xffffffffu, i_hi, 0), __shfl_sync(0xffffffffu, i_lo, 0)};
     float* row = w + (size_t)c * kmax;
     const int lead = kmax - p;
-    for (int k = threadIdx.x; k < kmax; k += kWThreads) {
+    for (int k = lane; k < kmax; k += 32) {
         const int i = k - lead;
         float v = 0.f;
         if (i >= 0) {
@@ -146,7 +145,7 @@ __global__ void __launch_bounds__(kWThreads) k_weights(int kind, const int* peri
 
 vta_status launch_weights(int kind, const int* periods, const double* pa, const double* pb, int n_combos,
                           int kmax, float* w, cudaStream_t st) {
-    k_weights<<<n_combos, kWThreads, 0, st>>>(kind, periods, pa, pb, kmax, w);
+    k_weights<<<ceil_div(n_combos, kWThreads / 32), kWThreads, 0, st>>>(kind, periods, pa, pb, n_combos, kmax, w);
     return check_launch("k_weights");
 }
 

@@ -182,40 +182,69 @@ struct PackArgs {
     float* row_sum;             // [tiles*128] sum of the f32 weights
 };
 
+constexpr int kPackThreads = 512;
+
 template <int VARIANT>
-__global__ void k_pack_a(PackArgs a) {
+__global__ void __launch_bounds__(kPackThreads) k_pack_a(PackArgs a) {
+    __shared__ float sc_sh[kM];
     const int m = blockIdx.x;
     const int K = a.tile_k[m];
-    const int r = threadIdx.x;  // 128 threads: one row each
-    const int c = m * kM + r;
-    float mx = 0.f;
-    double sum = 0.0;
-    if (c < a.n_combos) {
-        const float* row = a.w + (size_t)c * a.kmax + (a.kmax - K);
-        for (int k = 0; k < K; ++k) {
-            const float v = (a.kmax - K + k) >= 0 ? row[k] : 0.f;
-            mx = fmaxf(mx, fabsf(v));
-            sum += (double)v;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int col0 = a.kmax - K;  // weight column of k = 0 (negative: zero padding)
+    // row statistics, one warp per row (coalesced along the row): maximum
+    // magnitude and the row sum as a compensated float pair (Neumaier; an f64
+    // running sum is a chain of slow FP64 adds on GB300)
+    for (int r = warp; r < kM; r += kPackThreads / 32) {
+        const int c = m * kM + r;
+        float mx = 0.f, sum = 0.f, comp = 0.f;
+        if (c < a.n_combos) {
+            const float* row = a.w + (size_t)c * a.kmax;
+            for (int k = lane; k < K; k += 32) {
+                const float v = col0 + k >= 0 ? row[col0 + k] : 0.f;
+                mx = fmaxf(mx, fabsf(v));
+                const float t = sum + v;
+                comp += fabsf(sum) >= fabsf(v) ? (sum - t) + v : (v - t) + sum;
+                sum = t;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            const float so = __shfl_xor_sync(0xffffffffu, sum, o);
+            const float co = __shfl_xor_sync(0xffffffffu, comp, o);
+            const float t = sum + so;
+            comp += co + (fabsf(sum) >= fabsf(so) ? (sum - t) + so : (so - t) + sum);
+            sum = t;
+        }
+        if (lane == 0) {
+            int e = 0;
+            if (mx > 0.f) {
+                int ex;
+                frexpf(mx, &ex);  // mx = f * 2^ex, f in [0.5, 1)
+                e = 14 - ex;
+            }
+            sc_sh[r] = ldexpf(1.f, e);
+            a.row_scale[(size_t)m * kM + r] = mx > 0.f ? ldexpf(1.f, -e) : 0.f;
+            a.row_sum[(size_t)m * kM + r] = sum + comp;
         }
     }
-    int e = 0;
-    if (mx > 0.f) {
-        int ex;
-        frexpf(mx, &ex);  // mx = f * 2^ex, f in [0.5, 1)
-        e = 14 - ex;
-    }
-    const float sc = ldexpf(1.f, e);
-    a.row_scale[(size_t)m * kM + r] = mx > 0.f ? ldexpf(1.f, -e) : 0.f;
-    a.row_sum[(size_t)m * kM + r] = (float)sum;
+    __syncthreads();
+    // packed element o = ((k / 8) * 16 + g) * 64 + rr * 8 + (k % 8) of row
+    // r = 8 g + rr: consecutive threads write consecutive elements and read 8
+    // consecutive weights of one row
     uint16_t* hi = a.packed + a.tile_off[m];
     uint16_t* lo = hi + (size_t)kM * K;
-    const int g = r >> 3, rr = r & 7;
-    for (int k = 0; k < K; ++k) {
+    const int total = kM * K;
+#pragma unroll 4
+    for (int o = threadIdx.x; o < total; o += kPackThreads) {
+        const int kb = o >> 10, rem = o & 1023;
+        const int r = ((rem >> 6) << 3) | ((rem >> 3) & 7);
+        const int k = (kb << 3) | (rem & 7);
+        const int c = m * kM + r;
         float v = 0.f;
-        if (c < a.n_combos && (a.kmax - K + k) >= 0) v = a.w[(size_t)c * a.kmax + (a.kmax - K + k)] * sc;
+        if (c < a.n_combos && col0 + k >= 0) v = a.w[(size_t)c * a.kmax + col0 + k] * sc_sh[r];
         uint16_t h, l;
         Split<VARIANT>::run(v, h, l);
-        const size_t o = ((size_t)(k >> 3) * 16 + g) * 64 + rr * 8 + (k & 7);
         hi[o] = h;
         lo[o] = l;
     }
@@ -725,8 +754,8 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
     VTA_TRY(upload_async(ctx, d_toff, toff.data(), n_tiles_m * sizeof(long long), st));
     VTA_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
     PackArgs pa{a.w, a.kmax, a.n_combos, d_tk, d_toff, d_packed, d_rs, d_rsum};
-    if (variant == 1) k_pack_a<1><<<n_tiles_m, kM, 0, st>>>(pa);
-    else k_pack_a<0><<<n_tiles_m, kM, 0, st>>>(pa);
+    if (variant == 1) k_pack_a<1><<<n_tiles_m, kPackThreads, 0, st>>>(pa);
+    else k_pack_a<0><<<n_tiles_m, kPackThreads, 0, st>>>(pa);
     VTA_TRY(check_launch("k_pack_a"));
     StripArgs sa{a.x, a.n, a.first, kbig, jmax, d_sh, d_sl, d_ref, d_xs};
     const int L = jmax * 8 + 8;
