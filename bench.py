@@ -83,6 +83,24 @@ def workload_alma_grid():
                        "sweep": "periods 5..260 x offsets 0.50..0.95/0.05 x sigmas 3..9"}}
 
 
+def workload_wwma_family():
+    """The remaining weighted-window moving averages on the tensor-core
+    contraction: CWMA, FWMA, SRWMA, SQWMA periods 5..260 (256 combos each) and
+    EPMA periods 16..260 x offset 4 (245 combos) on 1,000,000 bars (seed 6, 100
+    leading NaN): 1.27e9 outputs = 5.1 GB per step."""
+    from vectorta_gb300 import datagen
+
+    n = 1_000_000
+    close = datagen.random_walk(n, seed=6, nan_lead=100)
+    per = {"period": (5, 260, 1)}
+    jobs = [("cwma", ["close"], per), ("fwma", ["close"], per), ("srwma", ["close"], per),
+            ("sqwma", ["close"], per), ("epma", ["close"], {"period": (16, 260, 1), "offset": (4, 4, 0)})]
+    return {"name": "wwma_family", "n": n, "series": {"close": close.astype(np.float32)}, "jobs": jobs,
+            "dominant": "cwma",
+            "config": {"workload": "wwma_family", "bars": n, "seed": 6, "nan_lead": 100,
+                       "sweeps": "CWMA/FWMA/SRWMA/SQWMA periods 5..260; EPMA periods 16..260 x offset 4"}}
+
+
 def workload_ema_small():
     """Profiling case: one EMA sweep (periods 2..1000) on 200,000 bars
     (0.8 GB of outputs: larger than L2, a few GB on the device at most)."""
@@ -160,7 +178,7 @@ def workload_served_stream():
 
 
 WORKLOADS = {"sweeps": workload_sweeps, "ragged_tm": workload_ragged_tm, "served_stream": workload_served_stream,
-             "adx_sweep": workload_adx_sweep, "ragged_small": workload_ragged_small, "alma_grid": workload_alma_grid, "ema_small": workload_ema_small,
+             "adx_sweep": workload_adx_sweep, "wwma_family": workload_wwma_family, "ragged_small": workload_ragged_small, "alma_grid": workload_alma_grid, "ema_small": workload_ema_small,
              "alma_small": workload_alma_small}
 
 
@@ -291,6 +309,14 @@ def cpu_sample(wl, budget_rows=None):
             for p in ps:
                 tasks.append((lambda p=p: O.alma_batch(s["close"], (p, p, 0), sweep["offset"], sweep["sigma"]),
                               wl["n"] * len(O.axis_f64(sweep["offset"])) * len(O.axis_f64(sweep["sigma"]))))
+            continue
+        if name in ("cwma", "fwma", "srwma", "sqwma", "epma"):
+            fn = getattr(O, name)
+            offs = O.axis_usize(sweep["offset"], O.AX_SWAP) if name == "epma" else [None]
+            for p in O.periods_of(name, sweep["period"])[::16]:
+                for o in offs:
+                    args_ = (p,) if o is None else (p, o)
+                    tasks.append((lambda fn=fn, a=args_: fn(s["close"], *a), wl["n"]))
             continue
         ps = O.periods_of(name, sweep["period"])
         stride = 4 if len(ps) > 500 else 1
@@ -825,7 +851,7 @@ TRAFFIC = {
 }
 KERNEL_NAME = {"recurrence_window_sweeps": "k_recur<OpEma, batch, EMIT>", "alma_grid": "k_wwma_tc<fp16x3>",
                "ema_small": "k_recur<OpEma, batch, EMIT>", "alma_small": "k_wwma_tc<fp16x3>",
-               "adx_sweep": "k_hlc_chunk<adx> + fix-up"}
+               "adx_sweep": "k_hlc_chunk<adx> + fix-up", "wwma_family": "k_wwma_tc<fp16x3> (CWMA)"}
 
 
 def main():

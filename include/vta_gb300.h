@@ -115,7 +115,8 @@ typedef struct vta_range_f64 { double start, end, step; } vta_range_f64;
 typedef struct vta_alma_batch_range { vta_range_usize period; vta_range_f64 offset, sigma; } vta_alma_batch_range;
 typedef struct vta_alma_params { size_t period; double offset, sigma; } vta_alma_params;
 /* period-only sweeps: EMA, DEMA, TEMA, RSI, Wilders, SMA, WMA, SWMA, PWMA,
- * SINWMA, TRIMA, ATR (`length`), ADX, Donchian, WillR */
+ * SINWMA, TRIMA, ATR (`length`), ADX, Donchian, WillR, CWMA, FWMA, SRWMA,
+ * SQWMA */
 typedef struct vta_period_batch_range { vta_range_usize period; } vta_period_batch_range;
 typedef struct vta_period_params { size_t period; } vta_period_params;
 /* StdDevBatchRange (stddev.rs:573-585) */
@@ -133,6 +134,9 @@ typedef struct vta_supertrend_params { size_t period; double factor; } vta_super
 /* PercentileNearestRankBatchRange (percentile_nearest_rank.rs:815-827) */
 typedef struct vta_percentile_batch_range { vta_range_usize length; vta_range_f64 percentage; } vta_percentile_batch_range;
 typedef struct vta_percentile_params { size_t length; double percentage; } vta_percentile_params;
+/* EpmaBatchRange / EpmaParams (epma.rs:750-753; offset < period) */
+typedef struct vta_epma_batch_range { vta_range_usize period, offset; } vta_epma_batch_range;
+typedef struct vta_epma_params { size_t period, offset; } vta_epma_params;
 
 /* ==== alma (src/cuda/moving_averages/alma_wrapper.rs) ==== */
 /* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
@@ -533,6 +537,101 @@ vta_status vta_percentile_nearest_rank_many_series_one_param_time_major_dev(vta_
 vta_status vta_percentile_nearest_rank_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
     size_t cols, size_t rows, const vta_percentile_params* params, float* d_out);
 
+/* ==== cwma (src/cuda/moving_averages/cwma_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_cwma_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* cwma_batch_dev (cwma_wrapper.rs:767) */
+vta_status vta_cwma_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* cwma_batch_device / _from_device_prices (cwma_wrapper.rs:737); first_valid as in the crate. */
+vta_status vta_cwma_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* cwma_batch_into_host_f32 (cwma_wrapper.rs:850); each output holds out_len >= rows*cols floats. */
+vta_status vta_cwma_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* cwma_many_series_one_param_time_major_dev (cwma_wrapper.rs:1208) */
+vta_status vta_cwma_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* cwma_many_series_one_param_device (cwma_wrapper.rs:1180) */
+vta_status vta_cwma_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== fwma (src/cuda/moving_averages/fwma_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_fwma_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* fwma_batch_dev (fwma_wrapper.rs:491) */
+vta_status vta_fwma_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* fwma_batch_device / _from_device_prices (fwma_wrapper.rs:475); first_valid as in the crate. */
+vta_status vta_fwma_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* fwma_batch_into_host_f32 (host-output form of fwma_wrapper.rs:491); each output holds out_len >= rows*cols floats. */
+vta_status vta_fwma_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* fwma_many_series_one_param_time_major_dev (fwma_wrapper.rs:760) */
+vta_status vta_fwma_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* fwma_many_series_one_param_device (fwma_wrapper.rs:734) */
+vta_status vta_fwma_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== srwma (src/cuda/moving_averages/srwma_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_srwma_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* srwma_batch_dev (srwma_wrapper.rs:328) */
+vta_status vta_srwma_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* srwma_batch_device / _from_device_prices (srwma_wrapper.rs:420); first_valid as in the crate. */
+vta_status vta_srwma_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* srwma_batch_into_host_f32 (host-output form of srwma_wrapper.rs:328); each output holds out_len >= rows*cols floats. */
+vta_status vta_srwma_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* srwma_many_series_one_param_time_major_dev (srwma_wrapper.rs:485) */
+vta_status vta_srwma_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* srwma_many_series_one_param_device (srwma_wrapper.rs:572) */
+vta_status vta_srwma_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== sqwma (src/cuda/moving_averages/sqwma_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_sqwma_expand_grid(const vta_period_batch_range* sweep, vta_period_params* out, size_t cap, size_t* n_combos);
+/* sqwma_batch_dev (sqwma_wrapper.rs:157) */
+vta_status vta_sqwma_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, vta_device_array* out);
+/* sqwma_batch_device / _from_device_prices (sqwma_wrapper.rs:190); first_valid as in the crate. */
+vta_status vta_sqwma_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
+/* sqwma_batch_into_host_f32 (sqwma_wrapper.rs:166); each output holds out_len >= rows*cols floats. */
+vta_status vta_sqwma_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_period_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* sqwma_many_series_one_param_time_major_dev (sqwma_wrapper.rs:255) */
+vta_status vta_sqwma_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, vta_device_array* out);
+/* sqwma_many_series_one_param_device (sqwma_wrapper.rs:222) */
+vta_status vta_sqwma_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_period_params* params, float* d_out);
+
+/* ==== epma (src/cuda/moving_averages/epma_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_epma_expand_grid(const vta_epma_batch_range* sweep, vta_epma_params* out, size_t cap, size_t* n_combos);
+/* epma_batch_dev (epma_wrapper.rs:485) */
+vta_status vta_epma_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_epma_batch_range* sweep, vta_device_array* out);
+/* epma_batch_device / _from_device_prices (epma_wrapper.rs:574); first_valid as in the crate. */
+vta_status vta_epma_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_epma_batch_range* sweep, float* d_out);
+/* epma_batch_into_host_f32 (epma_wrapper.rs:495); each output holds out_len >= rows*cols floats. */
+vta_status vta_epma_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_epma_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* epma_many_series_one_param_time_major_dev (epma_wrapper.rs:773) */
+vta_status vta_epma_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_epma_params* params, vta_device_array* out);
+/* epma_many_series_one_param_device (epma_wrapper.rs:805) */
+vta_status vta_epma_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_epma_params* params, float* d_out);
+
 /* ==== many-series work-list plans ====
  * No counterpart in the crate, whose many-series entry points run one
  * indicator per call over a rectangular time-major matrix.  A plan runs
@@ -590,7 +689,7 @@ vta_status vta_tm_plan_destroy(vta_tm_plan* plan);
  * Times are seconds since the server was created. */
 typedef struct vta_sweep {      /* generic sweep: the fields each indicator reads */
     vta_range_usize period;     /* period / length */
-    vta_range_f64 p1;           /* alma offset, stddev/zscore nbdev, bb devup, supertrend factor, percentile % */
+    vta_range_f64 p1;           /* alma offset, stddev/zscore nbdev, bb devup, supertrend factor, percentile %, epma offset */
     vta_range_f64 p2;           /* alma sigma, bb devdn */
 } vta_sweep;
 typedef struct vta_server_config {

@@ -31,6 +31,7 @@ AXIS_MODE = {
     "bollinger": AX_DESC, "bollinger_bands": AX_DESC, "donchian": AX_DESC, "willr": AX_DESC,
     "percentile_nearest_rank": AX_DESC, "wma": AX_DESC_PLUS_END, "swma": AX_DESC,
     "pwma": AX_DESC, "sinwma": AX_DESC, "trima": AX_SWAP,
+    "cwma": AX_SWAP, "fwma": AX_SWAP, "srwma": AX_DESC, "sqwma": AX_DESC, "epma": AX_SWAP,
 }
 
 
@@ -90,6 +91,11 @@ def lib():
             "vto_trima": ([dp, sz, sz, dp], ip),
             "vto_donchian_fast": ([dp, dp, sz, sz, dp, dp, dp], ip),
             "vto_willr_fast": ([dp, dp, dp, sz, sz, dp], ip),
+            "vto_cwma": ([dp, sz, sz, dp], ip),
+            "vto_fwma": ([dp, sz, sz, dp], ip),
+            "vto_srwma": ([dp, sz, sz, dp], ip),
+            "vto_sqwma": ([dp, sz, sz, dp], ip),
+            "vto_epma": ([dp, sz, sz, sz, dp], ip),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -199,6 +205,26 @@ def pwma(x, period=5, batch=False):
 
 def sinwma(x, period=14):
     return _single("vto_sinwma", x, period)
+
+
+def cwma(x, period=14):
+    return _single("vto_cwma", x, period)
+
+
+def fwma(x, period=5):
+    return _single("vto_fwma", x, period)
+
+
+def srwma(x, period=14):
+    return _single("vto_srwma", x, period)
+
+
+def sqwma(x, period=14):
+    return _single("vto_sqwma", x, period)
+
+
+def epma(x, period=11, offset=4):
+    return _single("vto_epma", x, period, offset)
 
 
 def trima(x, period=30):

@@ -1320,3 +1320,181 @@ int vto_willr_fast(const double *h, const double *l, const double *c, size_t n, 
     free(dqx); free(dqn);
     return VTO_OK;
 }
+
+/* ------------------------------------------------------------------------ */
+/* The remaining weighted-window moving averages.                             */
+/* ------------------------------------------------------------------------ */
+
+/* cwma_prepare (cwma.rs:205-263): weights (p - i)^3, i < p - 1 (newest
+ * first), inv_norm = 1 / sum; cwma_scalar x86 form (cwma.rs:331-451): eight
+ * mul_add accumulators over blocks of 8, summed pairwise, then a sequential
+ * mul_add tail; first output first + p - 1. */
+int vto_cwma(const double *x, size_t n, size_t period, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || period > n || period == 1) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    const size_t wlen = period - 1;
+    double *w = (double *)malloc(sizeof(double) * wlen);
+    double norm = 0.0;
+    for (size_t i = 0; i < wlen; i++) {
+        double v = (double)(period - i);
+        w[i] = v * v * v;
+        norm += w[i];
+    }
+    double inv = 1.0 / norm;
+    fill_nan(out, first + wlen);
+    for (size_t i = first + wlen; i < n; i++) {
+        const double *d = x + i;
+        double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        size_t k = 0;
+        while (k + 7 < wlen) {
+            for (int j = 0; j < 8; j++) {
+                s[j] = fma(*d, w[k + j], s[j]);
+                d--;
+            }
+            k += 8;
+        }
+        double sum = (s[0] + s[1]) + (s[2] + s[3]) + (s[4] + s[5]) + (s[6] + s[7]);
+        for (; k < wlen; k++) {
+            sum = fma(*d, w[k], sum);
+            d--;
+        }
+        out[i] = sum * inv;
+    }
+    free(w);
+    return VTO_OK;
+}
+
+/* fwma_prepare (fwma.rs:293-339): Fibonacci weights fib[0] = fib[1] = 1
+ * (oldest first), each divided by their sum; fwma_scalar (fwma.rs:428-454):
+ * per group of 4 `sum += d0 w0 + d1 w1 + d2 w2 + d3 w3`, then the tail;
+ * first output first + p - 1. */
+int vto_fwma(const double *x, size_t n, size_t period, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    double *w = (double *)malloc(sizeof(double) * period);
+    for (size_t i = 0; i < period; i++) w[i] = 1.0;
+    for (size_t i = 2; i < period; i++) w[i] = w[i - 1] + w[i - 2];
+    double sum_w = 0.0;
+    for (size_t i = 0; i < period; i++) sum_w += w[i];
+    for (size_t i = 0; i < period; i++) w[i] /= sum_w;
+    fill_nan(out, first + period - 1);
+    const size_t p4 = period & ~(size_t)3;
+    for (size_t i = first + period - 1; i < n; i++) {
+        const double *d = x + i + 1 - period;
+        double sum = 0.0;
+        for (size_t k = 0; k < p4; k += 4)
+            sum += d[k] * w[k] + d[k + 1] * w[k + 1] + d[k + 2] * w[k + 2] + d[k + 3] * w[k + 3];
+        for (size_t k = p4; k < period; k++) sum += d[k] * w[k];
+        out[i] = sum;
+    }
+    free(w);
+    return VTO_OK;
+}
+
+/* srwma_with_kernel (srwma.rs:174-246): weights sqrt(p - i), i < p - 1
+ * (newest first), inv_norm = 1 / sum, first output first + p + 1; needs
+ * len - first >= p + 1.  srwma_scalar (srwma.rs:275-379): eight mul_add
+ * accumulators over blocks of 8, then four over blocks of 4, then s0; the
+ * accumulators summed as ((s0+s1)+(s2+s3)) + ((s4+s5)+(s6+s7)).  Periods
+ * below 2 are rejected here (the crate's p = 1 has an empty weight row). */
+int vto_srwma(const double *x, size_t n, size_t period, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period < 2 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period + 1) return VTO_E_NOT_ENOUGH_VALID;
+    const size_t wlen = period - 1;
+    double *w = (double *)malloc(sizeof(double) * wlen);
+    double norm = 0.0;
+    for (size_t i = 0; i < wlen; i++) {
+        w[i] = sqrt((double)(period - i));
+        norm += w[i];
+    }
+    double inv = 1.0 / norm;
+    const size_t start = first + period + 1;
+    fill_nan(out, start < n ? start : n);
+    for (size_t i = start; i < n; i++) {
+        const double *dp = x + i;
+        double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        size_t k = 0;
+        while (k + 8 <= wlen) {
+            for (int j = 0; j < 8; j++) s[j] = fma(*(dp - (k + j)), w[k + j], s[j]);
+            k += 8;
+        }
+        while (k + 4 <= wlen) {
+            for (int j = 0; j < 4; j++) s[j] = fma(*(dp - (k + j)), w[k + j], s[j]);
+            k += 4;
+        }
+        while (k < wlen) {
+            s[0] = fma(*(dp - k), w[k], s[0]);
+            k++;
+        }
+        double sum = ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
+        out[i] = sum * inv;
+    }
+    free(w);
+    return VTO_OK;
+}
+
+/* sqwma_with_kernel (sqwma.rs:195-251): weights (p - i)^2, i < p - 1 (newest
+ * first), first output first + p + 1; sqwma_scalar (sqwma.rs:254-300): one
+ * sequential mul_add chain, times 1 / weight_sum. */
+int vto_sqwma(const double *x, size_t n, size_t period, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period < 2 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    const size_t wlen = period - 1;
+    double *w = (double *)malloc(sizeof(double) * wlen);
+    double ws = 0.0;
+    for (size_t i = 0; i < wlen; i++) {
+        double v = (double)period - (double)i;
+        w[i] = v * v;
+        ws += w[i];
+    }
+    double inv = 1.0 / ws;
+    const size_t start = first + period + 1;
+    fill_nan(out, start < n ? start : n);
+    for (size_t j = start; j < n; j++) {
+        double sum = 0.0;
+        for (size_t k = 0; k < wlen; k++) sum = fma(x[j - k], w[k], sum);
+        out[j] = sum * inv;
+    }
+    free(w);
+    return VTO_OK;
+}
+
+/* epma_prepare (epma.rs:205-250) and epma_scalar (epma.rs:333-366): window
+ * of p - 1 values x[j-p+2 .. j] with weights c0, c0 + 1, ... (oldest first),
+ * c0 = 2 - offset; weight_sum = mul_add(p1, c0, 0.5 (p1 - 1) p1); one
+ * sequential mul_add chain times 1 / weight_sum; first output
+ * first + p + offset + 1; needs offset < p, p >= 2 and len - first >= p + offset + 1. */
+int vto_epma(const double *x, size_t n, size_t period, size_t offset, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (offset >= period) return VTO_E_INVALID_PARAM;
+    if (period < 2 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period + offset + 1) return VTO_E_NOT_ENOUGH_VALID;
+    const size_t p1 = period - 1;
+    const double c0 = 2.0 - (double)offset;
+    const double p1f = (double)p1;
+    const double weight_sum = fma(p1f, c0, 0.5 * (p1f - 1.0) * p1f);
+    const double inv = 1.0 / weight_sum;
+    const size_t start = first + period + offset + 1;
+    fill_nan(out, start < n ? start : n);
+    for (size_t j = start; j < n; j++) {
+        const size_t s0 = j + 1 - p1;
+        double sum = 0.0, wi = c0;
+        for (size_t i = 0; i < p1; i++, wi += 1.0) sum = fma(x[s0 + i], wi, sum);
+        out[j] = sum * inv;
+    }
+    return VTO_OK;
+}

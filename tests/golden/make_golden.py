@@ -82,6 +82,10 @@ def main(ref: str):
                              "source": "tests/python/test_utils.py trima.reinput_last_5; "
                                        "periods 30 then 10 as in tests/python/test_trima.py:118-137"}
     from_py("sma", "sma", {"period": 9}, 1e-1, "sma.rs:1628")
+    from_py("cwma", "cwma", {"period": 14}, 1e-9, "cwma.rs:2147-2160")
+    from_py("srwma", "srwma", {"period": 14}, 1e-8, "srwma.rs:1476-1490")
+    from_py("sqwma", "sqwma", {"period": 14}, 1e-5, "sqwma.rs:1066-1090")
+    from_py("epma", "epma", {"period": 11, "offset": 4}, 1e-1, "epma.rs:1217-1225")
     from_py("wilders", "wilders", {"period": 5}, 1e-8, "wilders.rs:1229-1235")
     from_py("atr", "atr", {"length": 14}, 1e-2, "atr.rs:1422")
     from_py("adx", "adx", {"period": 14}, 1e-1, "adx.rs:2163")
@@ -99,6 +103,8 @@ def main(ref: str):
             {"period": 5, "nbdev": 1.0}, 1e-1, "src/indicators/stddev.rs")
     from_rs("willr", os.path.join(ind, "willr.rs"), "expected_last_five", 1985, {"period": 14},
             1e-8, "src/indicators/willr.rs")
+    from_rs("fwma", os.path.join(ind, "moving_averages", "fwma.rs"), "expected_last_five", 1266,
+            {"period": 5}, 1e-8, "src/indicators/moving_averages/fwma.rs")
     st, line = rust_array(os.path.join(ind, "supertrend.rs"), "expected_last_five_trend", 2419)
     ch, _ = rust_array(os.path.join(ind, "supertrend.rs"), "expected_last_five_changed", 2419)
     gold["supertrend"] = {"params": {"period": 10, "factor": 3.0}, "last5_trend": st,

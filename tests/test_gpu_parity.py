@@ -20,6 +20,7 @@ TOL = {
     "adx": 1e-1, "supertrend": 7e-4, "sma": 1e-5, "stddev": 5e-4, "zscore": 5e-4,
     "bollinger_bands": 1e-3, "donchian": 5e-4, "willr": 5e-5, "percentile_nearest_rank": 1e-4,
     "wma": 1e-5, "swma": 2e-4, "pwma": 5e-4, "sinwma": 1e-5, "trima": 1e-4,
+    "cwma": 5e-5, "fwma": 5e-4, "srwma": 2e-5, "sqwma": 1e-5, "epma": 2e-5,
 }
 TOL_TM = dict(TOL, alma=3e-4, adx=3e-2)
 
@@ -73,7 +74,11 @@ def oracle_batch(name, d, sweep):
     if name == "pwma":
         return [O.rows_of(O.pwma, c, ps, batch=True)]
     simple = {"ema": O.ema, "dema": O.dema, "tema": O.tema, "wma": O.wma, "swma": O.swma,
-              "sinwma": O.sinwma, "trima": O.trima}
+              "sinwma": O.sinwma, "trima": O.trima, "cwma": O.cwma, "fwma": O.fwma, "srwma": O.srwma,
+              "sqwma": O.sqwma}
+    if name == "epma":
+        offs = O.axis_usize(sweep["offset"], O.AX_SWAP)
+        return [np.stack([O.epma(c, p, o) for p in ps for o in offs])]
     if name in simple:
         return [O.rows_of(simple[name], c, ps)]
     if name in ("stddev", "zscore"):
@@ -124,6 +129,10 @@ SWEEPS = {
     "supertrend": {"period": (5, 30, 5), "factor": (2.0, 3.0, 1.0)},
     "donchian": {"period": (1, 500, 13)}, "willr": {"period": (1, 500, 13)},
     "percentile_nearest_rank": {"length": (3, 120, 9), "percentage": (25.0, 75.0, 25.0)},
+    "cwma": {"period": (2, 120, 3)}, "fwma": {"period": (1, 60, 3)}, "srwma": {"period": (2, 120, 3)},
+    "sqwma": {"period": (2, 120, 3)},
+    # offsets even, so no combo has a zero weight sum (p - 1 odd, offset 2 + (p - 2) / 2)
+    "epma": {"period": (8, 60, 4), "offset": (0, 6, 2)},
 }
 
 
@@ -208,6 +217,8 @@ PARAMS = {
     "bollinger_bands": {"period": 20, "devup": 2.0, "devdn": 2.0}, "atr": {"period": 14},
     "adx": {"period": 14}, "supertrend": {"period": 10, "factor": 3.0}, "donchian": {"period": 20},
     "willr": {"period": 14}, "percentile_nearest_rank": {"length": 50, "percentage": 50.0},
+    "cwma": {"period": 14}, "fwma": {"period": 10}, "srwma": {"period": 14}, "sqwma": {"period": 14},
+    "epma": {"period": 11, "offset": 4},
 }
 
 
@@ -225,6 +236,8 @@ def oracle_series(name, c, h, l, prm):
         "supertrend": lambda: list(O.supertrend(h, l, c, p, prm["factor"])),
         "donchian": lambda: list(O.donchian(h, l, p)), "willr": lambda: [O.willr(h, l, c, p)],
         "percentile_nearest_rank": lambda: [O.percentile_nearest_rank(c, p, prm["percentage"])],
+        "cwma": lambda: [O.cwma(c, p)], "fwma": lambda: [O.fwma(c, p)], "srwma": lambda: [O.srwma(c, p)],
+        "sqwma": lambda: [O.sqwma(c, p)], "epma": lambda: [O.epma(c, p, prm["offset"])],
     }[name]
     return fn()
 
@@ -285,6 +298,20 @@ def test_interior_nan_semantics():
         assert_close(g, fn(xd, p), TOL[name], f"{name} interior NaN")
     g = V.CudaRsi(0).batch_dev(x, sweep={"period": (14, 14, 0)}).to_host()[0]
     assert_close(g, O.rsi_batch(xd, [14])[0], TOL["rsi"], "rsi batch interior NaN")
+
+
+def test_weighted_window_family_interior_nan_and_warmup():
+    """CWMA / FWMA / SRWMA / SQWMA / EPMA: a NaN inside a window gives NaN
+    there and only there, and each row starts at the crate's own warm-up."""
+    x = f32(datagen.random_walk(700, seed=5, nan_lead=9))
+    x[300] = np.nan
+    xd = x.astype(np.float64)
+    for name, fn, sweep in (("cwma", O.cwma, {"period": (7, 7, 0)}), ("fwma", O.fwma, {"period": (9, 9, 0)}),
+                            ("srwma", O.srwma, {"period": (6, 6, 0)}), ("sqwma", O.sqwma, {"period": (10, 10, 0)})):
+        g = V.CLASSES[name](0).batch_dev(x, sweep=sweep).to_host()[0]
+        assert_close(g, fn(xd, sweep["period"][0]), TOL[name], f"{name} interior NaN")
+    g = V.CudaEpma(0).batch_dev(x, sweep={"period": (11, 11, 0), "offset": (4, 4, 0)}).to_host()[0]
+    assert_close(g, O.epma(xd, 11, 4), TOL["epma"], "epma interior NaN")
 
 
 def test_small_series_and_periods():

@@ -35,6 +35,11 @@ SINGLE = {
     "atr": lambda c, p: O.atr(c["high"], c["low"], c["close"], **p),
     "adx": lambda c, p: O.adx(c["high"], c["low"], c["close"], **p),
     "willr": lambda c, p: O.willr(c["high"], c["low"], c["close"], **p),
+    "cwma": lambda c, p: O.cwma(c["close"], **p),
+    "fwma": lambda c, p: O.fwma(c["close"], **p),
+    "srwma": lambda c, p: O.srwma(c["close"], **p),
+    "sqwma": lambda c, p: O.sqwma(c["close"], **p),
+    "epma": lambda c, p: O.epma(c["close"], **p),
 }
 
 
@@ -164,3 +169,18 @@ def test_oracle_fast_minmax_equals_direct_scan():
         for x, y in zip(a, b):
             assert np.array_equal(x, y, equal_nan=True), p
         assert np.array_equal(O.willr(h, l, c, p), O.willr(h, l, c, p, fast=True), equal_nan=True), p
+
+
+def test_oracle_weighted_window_warmups(candles):
+    """First output index of each weighted-window MA on the fixture (the
+    crate's warm-up: cwma.rs:253, fwma.rs:442, srwma.rs:214, sqwma.rs:228,
+    epma.rs:247) and EPMA's documented warm-up of 16 at (11, 4)
+    (tests/python/test_utils.py EXPECTED_OUTPUTS['epma'])."""
+    c = candles["close"]
+    first = int(np.argmax(~np.isnan(c)))
+    cases = {"cwma": (O.cwma(c, 14), first + 13), "fwma": (O.fwma(c, 5), first + 4),
+             "srwma": (O.srwma(c, 14), first + 15), "sqwma": (O.sqwma(c, 14), first + 15),
+             "epma": (O.epma(c, 11, 4), first + 16)}
+    for name, (out, warm) in cases.items():
+        assert np.all(np.isnan(out[:warm])), name
+        assert not np.isnan(out[warm]), name

@@ -56,6 +56,7 @@ SWEEPS = {
                          [("period", RangeUsize), ("devup", RangeF64), ("devdn", RangeF64)]),
     "supertrend": _struct("vta_supertrend_batch_range", [("period", RangeUsize), ("factor", RangeF64)]),
     "percentile": _struct("vta_percentile_batch_range", [("length", RangeUsize), ("percentage", RangeF64)]),
+    "epma": _struct("vta_epma_batch_range", [("period", RangeUsize), ("offset", RangeUsize)]),
 }
 PARAMS = {
     "alma": _struct("vta_alma_params", [("period", C.c_size_t), ("offset", C.c_double), ("sigma", C.c_double)]),
@@ -66,6 +67,7 @@ PARAMS = {
                          [("period", C.c_size_t), ("devup", C.c_double), ("devdn", C.c_double)]),
     "supertrend": _struct("vta_supertrend_params", [("period", C.c_size_t), ("factor", C.c_double)]),
     "percentile": _struct("vta_percentile_params", [("length", C.c_size_t), ("percentage", C.c_double)]),
+    "epma": _struct("vta_epma_params", [("period", C.c_size_t), ("offset", C.c_size_t)]),
 }
 
 # name -> (input kind, outputs, sweep/params family)
@@ -91,6 +93,11 @@ INDICATORS = {
     "donchian": ("hl", ["upper", "middle", "lower"], "period"),
     "willr": ("hlc", ["out"], "period"),
     "percentile_nearest_rank": ("x", ["out"], "percentile"),
+    "cwma": ("x", ["out"], "period"),
+    "fwma": ("x", ["out"], "period"),
+    "srwma": ("x", ["out"], "period"),
+    "sqwma": ("x", ["out"], "period"),
+    "epma": ("x", ["out"], "epma"),
 }
 N_IN = {"x": 1, "hl": 2, "hlc": 3}
 

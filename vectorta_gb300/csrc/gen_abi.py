@@ -30,6 +30,11 @@ IND = [
  ("donchian","src/cuda/donchian_wrapper.rs","hl",["out_upper","out_middle","out_lower"],"period","period",(128,344,None,None,593,None)),
  ("willr","src/cuda/willr_wrapper.rs","hlc",["out"],"period","period",(75,132,236,None,583,642)),
  ("percentile_nearest_rank","src/cuda/percentile_nearest_rank_wrapper.rs","x",["out"],"percentile","percentile",(99,365,None,None,623,None)),
+ ("cwma","src/cuda/moving_averages/cwma_wrapper.rs","x",["out"],"period","period",(118,767,737,850,1208,1180)),
+ ("fwma","src/cuda/moving_averages/fwma_wrapper.rs","x",["out"],"period","period",(132,491,475,None,760,734)),
+ ("srwma","src/cuda/moving_averages/srwma_wrapper.rs","x",["out"],"period","period",(176,328,420,None,485,572)),
+ ("sqwma","src/cuda/moving_averages/sqwma_wrapper.rs","x",["out"],"period","period",(62,157,190,166,255,222)),
+ ("epma","src/cuda/moving_averages/epma_wrapper.rs","x",["out"],"epma","epma",(110,485,574,495,773,805)),
 ]
 RANGES = {
  "alma": ("vta_alma_batch_range", "vta_alma_params"),
@@ -39,6 +44,7 @@ RANGES = {
  "bollinger": ("vta_bollinger_batch_range", "vta_bollinger_params"),
  "supertrend": ("vta_supertrend_batch_range", "vta_supertrend_params"),
  "percentile": ("vta_percentile_batch_range", "vta_percentile_params"),
+ "epma": ("vta_epma_batch_range", "vta_epma_params"),
 }
 def inputs(kind, dev, tm):
     pre = "d_" if dev else ""
@@ -166,7 +172,8 @@ typedef struct vta_range_f64 { double start, end, step; } vta_range_f64;
 typedef struct vta_alma_batch_range { vta_range_usize period; vta_range_f64 offset, sigma; } vta_alma_batch_range;
 typedef struct vta_alma_params { size_t period; double offset, sigma; } vta_alma_params;
 /* period-only sweeps: EMA, DEMA, TEMA, RSI, Wilders, SMA, WMA, SWMA, PWMA,
- * SINWMA, TRIMA, ATR (`length`), ADX, Donchian, WillR */
+ * SINWMA, TRIMA, ATR (`length`), ADX, Donchian, WillR, CWMA, FWMA, SRWMA,
+ * SQWMA */
 typedef struct vta_period_batch_range { vta_range_usize period; } vta_period_batch_range;
 typedef struct vta_period_params { size_t period; } vta_period_params;
 /* StdDevBatchRange (stddev.rs:573-585) */
@@ -184,6 +191,9 @@ typedef struct vta_supertrend_params { size_t period; double factor; } vta_super
 /* PercentileNearestRankBatchRange (percentile_nearest_rank.rs:815-827) */
 typedef struct vta_percentile_batch_range { vta_range_usize length; vta_range_f64 percentage; } vta_percentile_batch_range;
 typedef struct vta_percentile_params { size_t length; double percentage; } vta_percentile_params;
+/* EpmaBatchRange / EpmaParams (epma.rs:750-753; offset < period) */
+typedef struct vta_epma_batch_range { vta_range_usize period, offset; } vta_epma_batch_range;
+typedef struct vta_epma_params { size_t period, offset; } vta_epma_params;
 """)
 for (name, wf, kind, outs, rng, prm, cites) in IND:
     R, P = RANGES[rng]
@@ -266,7 +276,7 @@ w("""/* ==== request server (continuous batching over a device-resident store) =
  * Times are seconds since the server was created. */
 typedef struct vta_sweep {      /* generic sweep: the fields each indicator reads */
     vta_range_usize period;     /* period / length */
-    vta_range_f64 p1;           /* alma offset, stddev/zscore nbdev, bb devup, supertrend factor, percentile % */
+    vta_range_f64 p1;           /* alma offset, stddev/zscore nbdev, bb devup, supertrend factor, percentile %, epma offset */
     vta_range_f64 p2;           /* alma sigma, bb devdn */
 } vta_sweep;
 typedef struct vta_server_config {
@@ -355,7 +365,8 @@ ENUM = {"alma":"I_ALMA","ema":"I_EMA","dema":"I_DEMA","tema":"I_TEMA","rsi":"I_R
         "sma":"I_SMA","wma":"I_WMA","swma":"I_SWMA","pwma":"I_PWMA","sinwma":"I_SINWMA","trima":"I_TRIMA",
         "stddev":"I_STDDEV","zscore":"I_ZSCORE","bollinger_bands":"I_BB","atr":"I_ATR","adx":"I_ADX",
         "supertrend":"I_SUPERTREND","donchian":"I_DONCHIAN","willr":"I_WILLR",
-        "percentile_nearest_rank":"I_PNR"}
+        "percentile_nearest_rank":"I_PNR","cwma":"I_CWMA","fwma":"I_FWMA","srwma":"I_SRWMA",
+        "sqwma":"I_SQWMA","epma":"I_EPMA"}
 def names(kind, dev, tm):
     return [a.split()[-1] for a in inputs(kind, dev, tm)]
 inc = ["// Generated by gen_abi.py: extern \"C\" entry points forwarding to the drivers of",

@@ -89,6 +89,38 @@ __device__ DS raw_weight(int kind, int i, int p, const RowConst& rc) {
             const int m1 = (p + 1) / 2, m2 = p - m1 + 1;
             return {(float)min(min(i + 1, p - i), min(m1, m2)), 0.f};
         }
+        // the next four have window L = p (FWMA) or L = period - 1 (the
+        // others), oldest first; p here is L
+        case WT_CWMA: {  // (k + 2)^3, cwma.rs:246-252
+            const double v = (double)(i + 2);
+            return split(v * v * v);
+        }
+        case WT_SQWMA: {  // (k + 2)^2, sqwma.rs:222-225
+            const double v = (double)(i + 2);
+            return split(v * v);
+        }
+        case WT_SRWMA: {  // sqrt(k + 2), srwma.rs:207-211; residual by FMA
+            const float v = (float)(i + 2);
+            const float r = sqrtf(v);
+            return {r, fmaf(-r, r, v) / (2.f * r)};
+        }
+        case WT_FWMA: {
+            // Fibonacci F(k+1) (fwma.rs:321-331) relative to F(L): by Binet,
+            // phi^(k+1-L) * (1 - (-1)^(k+1) phi^(-2(k+1))); the exponent is
+            // formed as a double-single product so the ratio of weights keeps
+            // f32 precision for windows of any length
+            const DS l2phi = rc.m;  // log2(phi) as double-single
+            const float e = (float)(i + 1 - p);
+            const DS ex = ds_mul(DS{e, 0.f}, l2phi);
+            float w = exp2f(ex.hi);
+            w = fmaf(w, ex.lo * 0.69314718f, w);
+            const DS ey = ds_mul(DS{-2.f * (float)(i + 1), 0.f}, l2phi);
+            const float alt = exp2f(ey.hi) * (((i + 1) & 1) ? -1.f : 1.f);
+            return {w * (1.f - alt), 0.f};
+        }
+        case WT_EPMA: {  // c0 + k with c0 = 2 - offset, epma.rs:346-366
+            return {(float)(i + 2) - rc.inv2s2.hi, 0.f};
+        }
     }
     return {0.f, 0.f};
 }
@@ -103,7 +135,11 @@ __global__ void __launch_bounds__(kWThreads) k_weights(int kind, const int* peri
     if (c >= n_combos) return;  // whole warp (no block-wide barrier below)
     const int p = periods[c];
     RowConst rc{};
-    if (kind == WT_ALMA) {
+    if (kind == WT_FWMA) {
+        rc.m = split(0.69424191363061730173879026);  // log2 of the golden ratio
+    } else if (kind == WT_EPMA) {
+        rc.inv2s2 = DS{(float)pa[c], 0.f};  // the offset (an integer)
+    } else if (kind == WT_ALMA) {
         float m_hi = 0.f, m_lo = 0.f, q_hi = 0.f, q_lo = 0.f;
         if (lane == 0) {
             const double a = pa[c], b = pb[c];

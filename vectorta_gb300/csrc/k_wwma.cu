@@ -83,7 +83,7 @@ k_wwma_batch_plain(WwmaBatchArgs a) {
         const int c = cb + cw + i;
         if (c >= a.n_combos) break;
         const int p = a.periods[c];
-        const int warm = a.first + p - 1;
+        const int warm = a.first + p - 1 + (a.warm_extra ? a.warm_extra[c] : 0);
         float v[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
@@ -151,7 +151,7 @@ __global__ void k_wwma_tm(WwmaTmArgs a, const int* first_nan) {
             const int t = t0 + j;
             if (t >= a.rows) break;
             float r = acc[j];
-            if (t < f + p - 1 || (a.nan_mode == 1 && t >= fn)) r = qnan();
+            if (t < f + p - 1 + a.warm_extra || (a.nan_mode == 1 && t >= fn)) r = qnan();
             a.out_tm[(size_t)t * S + s] = r;
         }
     }

@@ -58,6 +58,7 @@ constexpr int kN = 256;          // times per tile (MMA N)
 constexpr int kThreads = 288;     // warp 0: TMA + MMA issue; warps 1-8: epilogue
 constexpr int kEpiThreads = 256;
 constexpr int kMaxK = 272;       // largest tile K (period) the shared memory holds
+constexpr int kStripBufs = 3;    // strip buffers: copies for items i+1 and i+2 in flight during item i
 constexpr int kStageLd = 36;     // epilogue staging row stride (floats) of the st.global path
 constexpr int kStageTma = 32 * 32 * 4;  // epilogue staging per warp for a TMA store (bytes)
 constexpr uint32_t kTmemCols = 512;
@@ -145,6 +146,18 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
           "=r"(r[29]), "=r"(r[30]), "=r"(r[31])                                                              \
         : "r"(taddr))
 
+// Waits for this thread's tcgen05.ld to complete; the 32 destination registers
+// are operands, so no use of them can be scheduled before the wait.
+#define TC_WAIT_LD32(r)                                                                                   \
+    asm volatile("tcgen05.wait::ld.sync.aligned;"                                                         \
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]),     \
+                   "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), \
+                   "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]),          \
+                   "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]),          \
+                   "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31])           \
+                 :                                                                                        \
+                 : "memory")
+
 // ------------------------------------------------------------ splitting ---
 template <int VARIANT>
 struct Split;
@@ -194,16 +207,24 @@ __global__ void __launch_bounds__(kPackThreads) k_pack_a(PackArgs a) {
     // row statistics, one warp per row (coalesced along the row): maximum
     // magnitude and the row sum as a compensated float pair (Neumaier; an f64
     // running sum is a chain of slow FP64 adds on GB300)
+    constexpr int kSlots = (kMaxK + 31) / 32;  // row elements per lane
     for (int r = warp; r < kM; r += kPackThreads / 32) {
         const int c = m * kM + r;
         float mx = 0.f, sum = 0.f, comp = 0.f;
         if (c < a.n_combos) {
             const float* row = a.w + (size_t)c * a.kmax;
-            for (int k = lane; k < K; k += 32) {
-                const float v = col0 + k >= 0 ? row[col0 + k] : 0.f;
-                mx = fmaxf(mx, fabsf(v));
-                const float t = sum + v;
-                comp += fabsf(sum) >= fabsf(v) ? (sum - t) + v : (v - t) + sum;
+            // all of the lane's loads first (independent), then the sums
+            float v[kSlots];
+#pragma unroll
+            for (int j = 0; j < kSlots; ++j) {
+                const int k = lane + 32 * j;
+                v[j] = (k < K && col0 + k >= 0) ? row[col0 + k] : 0.f;
+            }
+#pragma unroll
+            for (int j = 0; j < kSlots; ++j) {
+                mx = fmaxf(mx, fabsf(v[j]));
+                const float t = sum + v[j];
+                comp += fabsf(sum) >= fabsf(v[j]) ? (sum - t) + v[j] : (v[j] - t) + sum;
                 sum = t;
             }
         }
@@ -373,6 +394,7 @@ struct TcArgs {
     const float* xscale;
     int nan_mode;
     const double* nanp;
+    const int* warm_extra;  // [n_combos] extra warm-up steps (null: 0)
     float* out;
     int n_time_tiles;     // time tiles per combo tile
     int items;            // combo tiles x time tiles, combo-tile major
@@ -386,7 +408,7 @@ constexpr int kTraceTiles = 64;
 
 struct __align__(16) SmemCtl {
     uint64_t a_full;
-    uint64_t strip_full[2];
+    uint64_t strip_full[kStripBufs];
     uint64_t mma_done[2];
     uint64_t acc_empty[2];
     uint32_t tmem_base;
@@ -431,18 +453,20 @@ struct ItemIter {
 template <int VARIANT, bool TMA_STORE>
 __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_constant__ CUtensorMap tmap_out) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
-    // layout (capacities for the largest tile K): A hi | A lo | strip[2] hi |
-    // strip[2] lo | staging (1024-aligned) | ctl
+    // layout (capacities for the largest tile K): A hi | A lo | strip[kStripBufs] hi |
+    // strip[kStripBufs] lo | staging (1024-aligned) | ctl
     const uint32_t strip_cap = (uint32_t)a.jmax * 128;
     uint8_t* p = smem_raw;
     uint16_t* a_hi = reinterpret_cast<uint16_t*>(p);
     p += (size_t)kM * a.kmax * 2;
     uint16_t* a_lo = reinterpret_cast<uint16_t*>(p);
     p += (size_t)kM * a.kmax * 2;
-    uint8_t* strip_hi[2] = {p, p + strip_cap};
-    p += 2 * (size_t)strip_cap;
-    uint8_t* strip_lo[2] = {p, p + strip_cap};
-    p += 2 * (size_t)strip_cap;
+    uint8_t* strip_hi[kStripBufs];
+    uint8_t* strip_lo[kStripBufs];
+    for (int j = 0; j < kStripBufs; ++j) strip_hi[j] = p + (size_t)j * strip_cap;
+    p += kStripBufs * (size_t)strip_cap;
+    for (int j = 0; j < kStripBufs; ++j) strip_lo[j] = p + (size_t)j * strip_cap;
+    p += kStripBufs * (size_t)strip_cap;
     p = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
     float* stage = reinterpret_cast<float*>(p);  // [8 epilogue warps][32][kStageLd] or [8][4 KB swizzled]
     p += (size_t)8 * 32 * kStageLd * sizeof(float);
@@ -458,8 +482,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
 
     if (tid == 0) {
         mbar_init(&ctl->a_full, 1);
+        for (int b = 0; b < kStripBufs; ++b) mbar_init(&ctl->strip_full[b], 1);
         for (int b = 0; b < 2; ++b) {
-            mbar_init(&ctl->strip_full[b], 1);
             mbar_init(&ctl->mma_done[b], 1);
             mbar_init(&ctl->acc_empty[b], kEpiThreads);
         }
@@ -484,7 +508,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
         const uint32_t idesc = instr_desc(VARIANT);
         // strip of item i: the Kmax strip of its time tile, entered 16 (Kmax - K) bytes in
         auto copy_strip = [&](int i, const ItemIter& itm) {
-            const int bb = i & 1;
+            const int bb = i % kStripBufs;
             const int Ki = a.tile_k[itm.tile(a)];
             const uint32_t sb = (uint32_t)(Ki / 8 + kN / 8 - 1) * 128;
             const size_t g = (size_t)itm.time_tile(a) * a.jmax * 128 + (size_t)(a.kmax - Ki) * 16;
@@ -503,18 +527,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
             a_mt = mt;
         };
         bool ok = true;
-        ItemIter cur;
+        ItemIter cur, nxt;  // nxt: the item whose strip is copied next
         cur.start(a, blockIdx.x);
+        nxt = cur;
+        int copies = 0;  // strips requested (items 0 .. copies-1)
         if (ntiles > 0) {
             load_a(cur.tile(a));
-            copy_strip(0, cur);
+            for (; copies < 2 && copies < ntiles; ++copies, nxt.advance(a)) copy_strip(copies, nxt);
             ok = mbar_wait(&ctl->a_full, 0, abort_flag);
             a_loads = 1;
         }
+        int consumed = 0;
         for (int i = 0; ok && i < ntiles; ++i) {
             const int b = i & 1;
+            const int sbuf = i % kStripBufs;
             const int mt = cur.tile(a);
-            ok = mbar_wait(&ctl->strip_full[b], (i >> 1) & 1, abort_flag);
+            ok = mbar_wait(&ctl->strip_full[sbuf], (i / kStripBufs) & 1, abort_flag);
+            if (ok) consumed = i + 1;
             if (tracing && i < kTraceTiles) a.trace[i * TR_N + TR_P_STRIP] = now_ns();
             if (ok && i >= 2) ok = mbar_wait(&ctl->acc_empty[b], ((i >> 1) - 1) & 1, abort_flag);
             if (ok && mt != a_mt) {
@@ -533,7 +562,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
             tc_fence_after();
             const uint32_t d = tmem + (uint32_t)(b * kN);
             const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
-            const uint32_t bh = smem_u32(strip_hi[b]), bl = smem_u32(strip_lo[b]);
+            const uint32_t bh = smem_u32(strip_hi[sbuf]), bl = smem_u32(strip_lo[sbuf]);
             for (int ks = 0; ks < (K >> 4); ++ks) {
                 // A: next 2 K-chunks (16 row groups * 128 B each); B: next 2 strip blocks
                 const uint32_t ao = (uint32_t)ks * 2 * 16 * 128, bo = (uint32_t)ks * 256;
@@ -548,14 +577,26 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
             tc_commit(&ctl->mma_done[b]);
             ctl->issued = i + 1;
             if (tracing && i < kTraceTiles) a.trace[i * TR_N + TR_P_ISSUED] = now_ns();
-            // next strip into the other buffer once the MMAs of tile i-1 (its last reader) are done
+            // strip of item i + 2 into the buffer of item i - 1, once the MMAs
+            // of item i - 1 (its last reader) are done
             cur.advance(a);
-            if (i + 1 < ntiles) {
+            if (copies < ntiles) {
                 if (i >= 1) ok = mbar_wait(&ctl->mma_done[b ^ 1], ((i - 1) >> 1) & 1, abort_flag);
-                if (ok) copy_strip(i + 1, cur);
+                if (ok) {
+                    copy_strip(copies, nxt);
+                    ++copies;
+                    nxt.advance(a);
+                }
             }
         }
-        if (!ok) ctl->abort_flag = 1;
+        if (!ok) {
+            ctl->abort_flag = 1;
+            // strip copies still in flight land in this CTA's shared memory:
+            // wait for them (bounded) before the CTA may exit
+            volatile int no_abort = 0;
+            for (int j = consumed; j < copies; ++j)
+                mbar_wait(&ctl->strip_full[j % kStripBufs], (j / kStripBufs) & 1, &no_abort);
+        }
     } else if (warp >= 1) {
         // ================= epilogue: warps 1-8 ================================
         // warp w reads TMEM lane quarter w % 4 (its 32 combo rows) and column
@@ -580,7 +621,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
                 cur_mt = mt;
                 const int c = mt * kM + r;
                 p = c < a.n_combos ? a.periods[c] : 1;
-                warm = a.first + p - 1;
+                warm = a.first + p - 1 + (a.warm_extra && c < a.n_combos ? a.warm_extra[c] : 0);
                 rscale = a.row_scale[(size_t)mt * kM + r];
                 rsum = a.row_sum[(size_t)mt * kM + r];
                 rbase = mt * kM + q4 * 32;  // first combo of this warp's rows
@@ -603,16 +644,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
             // tiles past every row's warm-up with a NaN-free series need no masks
             const bool plain = !has_nan && __all_sync(0xffffffffu, t0 >= warm);
             const uint32_t tbase = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * kN + half * 128);
+            // the TMEM load of block k + 1 is issued before block k is staged, so
+            // it overlaps the wait for the previous block's TMA store
+            uint32_t v[32];
+            TC_LD32(tbase, v);
 #pragma unroll 1
             for (int k = 0; k < 4; ++k) {
-                uint32_t v[32];
-                TC_LD32(tbase + (uint32_t)(k * 32), v);
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                TC_WAIT_LD32(v);
                 const int cb = half * 128 + k * 32;
                 float y[32];
 #pragma unroll
                 for (int j = 0; j < 32; ++j) y[j] = fmaf(__uint_as_float(v[j]), scale, off);
+                if (k < 3) TC_LD32(tbase + (uint32_t)((k + 1) * 32), v);
                 if constexpr (TMA_STORE) {
+                    // the staging block is rewritten: wait until the previous
+                    // block's store has read it
+                    if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                    __syncwarp();
                     // 128-byte swizzle: 16-byte chunk j4 of row `lane` goes to chunk j4 ^ (lane & 7)
                     uint8_t* row8 = reinterpret_cast<uint8_t*>(st) + lane * 128;
 #pragma unroll
@@ -632,8 +680,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
                             "r"(t0 + cb), "r"(rbase), "r"(smem_u32(st))
                             : "memory");
                         asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-                        // the staging block is rewritten for the next chunk: wait until read
-                        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
                     }
                     __syncwarp();
                 } else {
@@ -697,7 +743,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
 
 size_t smem_bytes_for(int K) {
     const int J = K / 8 + kN / 8 - 1;
-    return (size_t)kM * K * 2 * 2 + 4 * (size_t)J * 128 + 1024 + (size_t)8 * 32 * kStageLd * sizeof(float) +
+    return (size_t)kM * K * 2 * 2 + 2 * kStripBufs * (size_t)J * 128 + 1024 + (size_t)8 * 32 * kStageLd * sizeof(float) +
            sizeof(SmemCtl) + 128;
 }
 
@@ -782,6 +828,7 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
     t.xscale = d_xs;
     t.nan_mode = a.nan_mode;
     t.nanp = a.nanp;
+    t.warm_extra = a.warm_extra;
     t.out = a.out;
     t.err = d_err;
     unsigned long long* d_trace = nullptr;
@@ -800,7 +847,12 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
     const long long items = (long long)n_tiles_m * n_time_tiles;
     if (items > INT32_MAX / 2) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "tcgen05 path: too many tiles");
     const int G = (int)std::min<long long>(items, ctx->num_sms);
-    const int k = std::max(1, (int)std::llround((double)items / ((double)G * kItemsPerChunk)));
+    int k = std::max(1, (int)std::llround((double)items / ((double)G * kItemsPerChunk)));
+    // with few combo tiles every CTA should see each of them (large and small
+    // K tiles cost very different MMA time): at least two chunks per tile
+    if (n_tiles_m <= 4) k = std::max(k, 2 * n_tiles_m);
+    // every chunk must hold at least one item (the CTAs' item walk assumes it)
+    k = std::min<long long>(k, std::max<long long>(1, items / G));
     t.n_time_tiles = n_time_tiles;
     t.items = (int)items;
     t.nchunks = G * k;

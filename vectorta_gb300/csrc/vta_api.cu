@@ -150,7 +150,8 @@ static std::vector<double> axis_f64(vta_range_f64 r) {
 // ============================================================ indicators ===
 enum Ind {
     I_ALMA, I_EMA, I_DEMA, I_TEMA, I_RSI, I_WILDERS, I_SMA, I_WMA, I_SWMA, I_PWMA, I_SINWMA, I_TRIMA,
-    I_STDDEV, I_ZSCORE, I_BB, I_ATR, I_ADX, I_SUPERTREND, I_DONCHIAN, I_WILLR, I_PNR
+    I_STDDEV, I_ZSCORE, I_BB, I_ATR, I_ADX, I_SUPERTREND, I_DONCHIAN, I_WILLR, I_PNR,
+    I_CWMA, I_FWMA, I_SRWMA, I_SQWMA, I_EPMA
 };
 enum InKind { IN_X = 1, IN_HL = 2, IN_HLC = 3 };
 
@@ -168,25 +169,63 @@ static const IndInfo kInfo[] = {
     {"stddev", IN_X, 1, AX_DESC},      {"zscore", IN_X, 1, AX_DESC},      {"bollinger_bands", IN_X, 3, AX_DESC},
     {"atr", IN_HLC, 1, AX_REV_FROM_END}, {"adx", IN_HLC, 1, AX_DESC},     {"supertrend", IN_HLC, 2, AX_DESC},
     {"donchian", IN_HL, 3, AX_DESC},   {"willr", IN_HLC, 1, AX_DESC},     {"percentile_nearest_rank", IN_X, 1, AX_DESC},
+    {"cwma", IN_X, 1, AX_SWAP},        {"fwma", IN_X, 1, AX_SWAP},        {"srwma", IN_X, 1, AX_DESC},
+    {"sqwma", IN_X, 1, AX_DESC},       {"epma", IN_X, 1, AX_SWAP},
 };
 
 // One parameter set: period plus up to two f64 parameters
 // (alma: offset, sigma; stddev/zscore: nbdev; bb: devup, devdn;
-//  supertrend: factor; percentile: percentage).
+//  supertrend: factor; percentile: percentage; epma: offset).
 struct Combo {
     size_t period;
     double a, b;
 };
 
 static bool is_wwma(Ind i) {
-    return i == I_ALMA || i == I_WMA || i == I_SWMA || i == I_PWMA || i == I_SINWMA || i == I_TRIMA;
+    return i == I_ALMA || i == I_WMA || i == I_SWMA || i == I_PWMA || i == I_SINWMA || i == I_TRIMA ||
+           i == I_CWMA || i == I_FWMA || i == I_SRWMA || i == I_SQWMA || i == I_EPMA;
+}
+
+// Weighted-window geometry of a combo: window length L (the weight row) and
+// the extra warm-up past first + L - 1 of its first output.
+//   CWMA  L = p - 1, first output first + p - 1   (cwma.rs:243-253, 453-466)
+//   SRWMA L = p - 1, first output first + p + 1   (srwma.rs:204-215, 288-292)
+//   SQWMA L = p - 1, first output first + p + 1   (sqwma.rs:222-228, 270-272)
+//   EPMA  L = p - 1, first output first + p + o + 1 (epma.rs:247, 341-352)
+//   others L = p, first output first + p - 1
+static int wwma_len(Ind i, const Combo& c) {
+    return (i == I_CWMA || i == I_SRWMA || i == I_SQWMA || i == I_EPMA) ? (int)c.period - 1 : (int)c.period;
+}
+static int wwma_warm_extra(Ind i, const Combo& c) {
+    switch (i) {
+        case I_CWMA: return 1;
+        case I_SRWMA: case I_SQWMA: return 3;
+        case I_EPMA: return (int)c.a + 3;
+        default: return 0;
+    }
+}
+static int wwma_weight_kind(Ind i) {
+    switch (i) {
+        case I_WMA: return WT_WMA;
+        case I_SWMA: return WT_SWMA;
+        case I_PWMA: return WT_PWMA;
+        case I_SINWMA: return WT_SINWMA;
+        case I_TRIMA: return WT_TRIMA;
+        case I_CWMA: return WT_CWMA;
+        case I_FWMA: return WT_FWMA;
+        case I_SRWMA: return WT_SRWMA;
+        case I_SQWMA: return WT_SQWMA;
+        case I_EPMA: return WT_EPMA;
+        default: return WT_ALMA;
+    }
 }
 
 // minimum valid length after `first` a combo needs (the crate's checks)
-static size_t needed_len(Ind ind, size_t p) {
+static size_t needed_len(Ind ind, size_t p, double a = 0.0) {
     switch (ind) {
         case I_DEMA: return p > 0 ? 2 * (p - 1) : 0;
         case I_ADX: return p + 1;
+        case I_EPMA: return p + (size_t)a + 1;  // epma.rs:235
         default: return p;
     }
 }
@@ -207,8 +246,12 @@ static vta_status validate_combo(Ind ind, const Combo& c, size_t len) {
             if (!(c.b > 0.0)) return bad("sigma must be > 0");
             if (!(c.a >= 0.0 && c.a <= 1.0)) return bad("offset must be in [0, 1]");
             break;
-        case I_WMA:
+        case I_WMA: case I_CWMA: case I_SRWMA: case I_SQWMA:
             if (c.period < 2) return bad("period must be >= 2");
+            break;
+        case I_EPMA:
+            if (c.period < 2) return bad("period must be >= 2");
+            if (!(c.a < (double)c.period)) return bad("offset must be < period");
             break;
         case I_TRIMA:
             if (c.period <= 3) return bad("period must be > 3");
@@ -230,7 +273,7 @@ static vta_status validate_combos(Ind ind, const std::vector<Combo>& cs, size_t 
     size_t need = 0;
     for (const Combo& c : cs) {
         VTA_TRY(validate_combo(ind, c, len));
-        need = std::max(need, needed_len(ind, c.period));
+        need = std::max(need, needed_len(ind, c.period, c.a));
     }
     if (first >= len) return fail(VTA_ERR_INVALID_INPUT, std::string(kInfo[ind].name) + ": all values are NaN");
     if (len - first < need) {
@@ -353,12 +396,22 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
     ar.need(nc * sizeof(float));
 
     if (is_wwma(ind)) {
-        const int kmax = pmax;
+        // rows are window lengths from here on (the weight rows' length)
+        std::vector<int> wextra(nc);
+        bool any_extra = false;
+        int kmax = 1;
+        for (int i = 0; i < nc; ++i) {
+            periods[i] = wwma_len(ind, cs[i]);
+            wextra[i] = wwma_warm_extra(ind, cs[i]);
+            any_extra = any_extra || wextra[i] != 0;
+            kmax = std::max(kmax, periods[i]);
+        }
         const int ntile = (nc + 15) / 16;
         ar.need((size_t)nc * kmax * sizeof(float));
         ar.need(ntile * sizeof(int));
         ar.need(len * sizeof(double));
         ar.need(prefix_tmp_doubles(n) * sizeof(double));
+        ar.need(nc * sizeof(int));
         VTA_TRY(ar.commit());
         int* d_per = ar.take<int>(nc);
         double* d_pa = ar.take<double>(nc);
@@ -369,22 +422,15 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
         int* d_tk = ar.take<int>(ntile);
         double* d_nanp = ar.take<double>(len);
         double* d_tmp = ar.take<double>(prefix_tmp_doubles(n));
+        int* d_wx = ar.take<int>(nc);
         std::vector<int> tk(ntile, 0);
         for (int i = 0; i < nc; ++i) tk[i / 16] = std::max(tk[i / 16], periods[i]);
         VTA_TRY(upload(ctx, d_per, periods.data(), nc * sizeof(int)));
         VTA_TRY(upload(ctx, d_pa, pa.data(), nc * sizeof(double)));
         VTA_TRY(upload(ctx, d_pb, pb.data(), nc * sizeof(double)));
         VTA_TRY(upload(ctx, d_tk, tk.data(), ntile * sizeof(int)));
-        int wk = WT_ALMA;
-        switch (ind) {
-            case I_WMA: wk = WT_WMA; break;
-            case I_SWMA: wk = WT_SWMA; break;
-            case I_PWMA: wk = WT_PWMA; break;
-            case I_SINWMA: wk = WT_SINWMA; break;
-            case I_TRIMA: wk = WT_TRIMA; break;
-            default: break;
-        }
-        VTA_TRY(launch_weights(wk, d_per, d_pa, d_pb, nc, kmax, d_w, st));
+        if (any_extra) VTA_TRY(upload(ctx, d_wx, wextra.data(), nc * sizeof(int)));
+        VTA_TRY(launch_weights(wwma_weight_kind(ind), d_per, d_pa, d_pb, nc, kmax, d_w, st));
         VTA_TRY(launch_prefix_f64(in.p[0], n, (int)first, PK_NAN, d_nanp, nullptr, d_tmp, st));
         WwmaBatchArgs a{};
         a.x = in.p[0];
@@ -399,6 +445,7 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
         // running-sum indicators (WMA, SWMA, TRIMA) keep a NaN forever
         a.nan_mode = (ind == I_WMA || ind == I_SWMA || ind == I_TRIMA) ? 1 : 0;
         a.nanp = d_nanp;
+        a.warm_extra = any_extra ? d_wx : nullptr;
         a.out = out[0];
         const int pol = ctx->policy.wma_batch;
         if (pol == 0 || pol >= 2) {
@@ -711,7 +758,7 @@ static vta_status run_tm(vta_ctx* ctx, Ind ind, const DevIn& in, size_t cols, si
         ar.need((size_t)nch * cols * 16);
         ar.need((size_t)nch * cols * 16);
     }
-    const int pw = is_wwma(ind) ? p : 0;
+    const int pw = is_wwma(ind) ? wwma_len(ind, c) : 0;
     ar.need(pw * sizeof(float));
     ar.need(sizeof(int));
     ar.need(2 * sizeof(double));
@@ -731,19 +778,18 @@ static vta_status run_tm(vta_ctx* ctx, Ind ind, const DevIn& in, size_t cols, si
     else VTA_TRY(launch_first_valid_tm_hlc(in.p[0], in.p[1], in.p[2], C, R, d_first, st));
 
     if (is_wwma(ind)) {
-        int wk = ind == I_ALMA ? WT_ALMA : ind == I_WMA ? WT_WMA : ind == I_SWMA ? WT_SWMA
-               : ind == I_PWMA ? WT_PWMA : ind == I_SINWMA ? WT_SINWMA : WT_TRIMA;
         const double ab[2] = {c.a, c.b};
-        VTA_TRY(upload(ctx, d_p1, &p, sizeof(int)));
+        VTA_TRY(upload(ctx, d_p1, &pw, sizeof(int)));
         VTA_TRY(upload(ctx, d_ab, ab, sizeof ab));
-        VTA_TRY(launch_weights(wk, d_p1, d_ab, d_ab + 1, 1, p, d_w, st));
+        VTA_TRY(launch_weights(wwma_weight_kind(ind), d_p1, d_ab, d_ab + 1, 1, pw, d_w, st));
         WwmaTmArgs a{};
         a.x_tm = in.p[0];
         a.cols = C;
         a.rows = R;
         a.first = d_first;
         a.w = d_w;
-        a.period = p;
+        a.period = pw;
+        a.warm_extra = wwma_warm_extra(ind, c);
         a.nan_mode = (ind == I_WMA || ind == I_SWMA || ind == I_TRIMA) ? 1 : 0;
         a.out_tm = out[0];
         ctx->last_kernel = "wwma_tm_f32";
@@ -954,7 +1000,7 @@ static vta_status tm_validate_host(Ind ind, const float* const* hin, size_t cols
             std::snprintf(buf, sizeof buf, "%s: series %zu all NaN", kInfo[ind].name, s);
             return fail(VTA_ERR_INVALID_INPUT, buf);
         }
-        const size_t need = needed_len(ind, c.period);
+        const size_t need = needed_len(ind, c.period, c.a);
         if (rows - f < need) {
             std::snprintf(buf, sizeof buf, "%s: series %zu not enough valid data (needed >= %zu, valid = %zu)",
                           kInfo[ind].name, s, need, rows - f);
@@ -1052,6 +1098,14 @@ static std::vector<Combo> grid_of(Ind ind, const vta_zscore_batch_range* r) { re
 static std::vector<Combo> grid_of(Ind, const vta_bollinger_batch_range* r) { return grid_bb(r); }
 static std::vector<Combo> grid_of(Ind ind, const vta_supertrend_batch_range* r) { return grid_p1(ind, r->period, r->factor); }
 static std::vector<Combo> grid_of(Ind ind, const vta_percentile_batch_range* r) { return grid_p1(ind, r->length, r->percentage); }
+// EpmaBatchRange: period outer, offset inner, both axes ascending after a swap
+// (epma.rs:835-859)
+static std::vector<Combo> grid_of(Ind, const vta_epma_batch_range* r) {
+    std::vector<Combo> cs;
+    for (size_t p : axis_usize(r->period, AX_SWAP))
+        for (size_t o : axis_usize(r->offset, AX_SWAP)) cs.push_back({p, (double)o, 0.0});
+    return cs;
+}
 
 static Combo combo_of(const vta_alma_params* p) { return {p->period, p->offset, p->sigma}; }
 static Combo combo_of(const vta_period_params* p) { return {p->period, 0.0, 0.0}; }
@@ -1060,6 +1114,7 @@ static Combo combo_of(const vta_zscore_params* p) { return {p->period, p->nbdev,
 static Combo combo_of(const vta_bollinger_params* p) { return {p->period, p->devup, p->devdn}; }
 static Combo combo_of(const vta_supertrend_params* p) { return {p->period, p->factor, 0.0}; }
 static Combo combo_of(const vta_percentile_params* p) { return {p->length, p->percentage, 0.0}; }
+static Combo combo_of(const vta_epma_params* p) { return {p->period, (double)p->offset, 0.0}; }
 
 static void params_of(const Combo& c, vta_alma_params* p) { *p = {c.period, c.a, c.b}; }
 static void params_of(const Combo& c, vta_period_params* p) { *p = {c.period}; }
@@ -1068,6 +1123,7 @@ static void params_of(const Combo& c, vta_zscore_params* p) { *p = {c.period, c.
 static void params_of(const Combo& c, vta_bollinger_params* p) { *p = {c.period, c.a, c.b}; }
 static void params_of(const Combo& c, vta_supertrend_params* p) { *p = {c.period, c.a}; }
 static void params_of(const Combo& c, vta_percentile_params* p) { *p = {c.period, c.a}; }
+static void params_of(const Combo& c, vta_epma_params* p) { *p = {c.period, (size_t)c.a}; }
 
 template <class R, class P>
 static vta_status expand(Ind ind, const R* r, P* out, size_t cap, size_t* n) {
@@ -1106,6 +1162,12 @@ static std::vector<Combo> grid_generic(Ind ind, const vta_sweep* sw) {
         case I_BB: { const vta_bollinger_batch_range r{sw->period, sw->p1, sw->p2}; return grid_of(ind, &r); }
         case I_SUPERTREND: { const vta_supertrend_batch_range r{sw->period, sw->p1}; return grid_of(ind, &r); }
         case I_PNR: { const vta_percentile_batch_range r{sw->period, sw->p1}; return grid_of(ind, &r); }
+        case I_EPMA: {  // offsets from p1 (rounded to integers)
+            const vta_range_usize o{(size_t)std::llround(sw->p1.start), (size_t)std::llround(sw->p1.end),
+                                    (size_t)std::llround(sw->p1.step)};
+            const vta_epma_batch_range r{sw->period, o};
+            return grid_of(ind, &r);
+        }
         default: { const vta_period_batch_range r{sw->period}; return grid_of(ind, &r); }
     }
 }

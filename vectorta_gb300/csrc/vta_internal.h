@@ -145,8 +145,11 @@ vta_status launch_prefix_f64(const float* x, int n, int first, int kind, double*
                              float2* out_ds, double* block_tmp, cudaStream_t st);
 size_t prefix_tmp_doubles(int n);
 
-// --- weighted-window moving averages (ALMA/WMA/SWMA/PWMA/SINWMA/TRIMA) ----
-// Row weights are right-aligned into a [n_combos][kmax] f32 matrix.
+// --- weighted-window moving averages (ALMA/WMA/SWMA/PWMA/SINWMA/TRIMA,
+// CWMA/FWMA/SRWMA/SQWMA/EPMA) ----------------------------------------------
+// Row weights are right-aligned into a [n_combos][kmax] f32 matrix.  A row's
+// "period" here is its window length L; its first output is at
+// first + L - 1 + warm_extra (the crate's warm-up of each indicator).
 struct WwmaBatchArgs {
     const float* x;        // series (device)
     int n;                 // series length
@@ -159,9 +162,13 @@ struct WwmaBatchArgs {
     int n_combos;
     int nan_mode;          // 0: window NaN -> NaN; 1: NaN poisons all later outputs
     const double* nanp;    // [n] count of NaN in x[first..i] (null: series has none)
+    const int* warm_extra; // [n_combos] extra warm-up steps (device; null: 0)
     float* out;            // [n_combos][n]
 };
-enum WeightKind { WT_ALMA = 0, WT_WMA = 1, WT_SWMA = 2, WT_PWMA = 3, WT_SINWMA = 4, WT_TRIMA = 5 };
+enum WeightKind {
+    WT_ALMA = 0, WT_WMA = 1, WT_SWMA = 2, WT_PWMA = 3, WT_SINWMA = 4, WT_TRIMA = 5,
+    WT_CWMA = 6, WT_FWMA = 7, WT_SRWMA = 8, WT_SQWMA = 9, WT_EPMA = 10
+};
 vta_status launch_weights(int kind, const int* periods, const double* pa, const double* pb, int n_combos,
                           int kmax, float* w, cudaStream_t st);
 vta_status launch_wwma_batch_plain(const WwmaBatchArgs& a, cudaStream_t st);
@@ -175,7 +182,8 @@ struct WwmaTmArgs {
     int cols, rows;
     const int* first;      // per-series first valid
     const float* w;        // [period] normalised weights
-    int period;
+    int period;            // window length
+    int warm_extra;        // first output of series s at first[s] + period - 1 + warm_extra
     int nan_mode;
     float* out_tm;
 };

@@ -75,6 +75,12 @@ class PercentileNearestRankBatchRange:
 
 
 @dataclass
+class EpmaBatchRange:
+    period: tuple = (11, 260, 1)      # epma.rs:754-760
+    offset: tuple = (4, 4, 0)
+
+
+@dataclass
 class AlmaParams:
     period: int = 9
     offset: float = 0.85
@@ -117,12 +123,20 @@ class PercentileNearestRankParams:
     percentage: float = 50.0
 
 
+@dataclass
+class EpmaParams:
+    period: int = 11
+    offset: int = 4
+
+
 _RANGE_CLS = {"alma": AlmaBatchRange, "period": PeriodBatchRange, "stddev": StdDevBatchRange,
               "zscore": ZscoreBatchRange, "bollinger": BollingerBandsBatchRange,
-              "supertrend": SuperTrendBatchRange, "percentile": PercentileNearestRankBatchRange}
+              "supertrend": SuperTrendBatchRange, "percentile": PercentileNearestRankBatchRange,
+              "epma": EpmaBatchRange}
 _PARAM_CLS = {"alma": AlmaParams, "period": PeriodParams, "stddev": StdDevParams,
               "zscore": ZscoreParams, "bollinger": BollingerBandsParams,
-              "supertrend": SuperTrendParams, "percentile": PercentileNearestRankParams}
+              "supertrend": SuperTrendParams, "percentile": PercentileNearestRankParams,
+              "epma": EpmaParams}
 
 
 def _to_sweep(fam: str, sweep) -> Any:
@@ -374,12 +388,14 @@ _CLASS_NAMES = {
     "bollinger_bands": "CudaBollingerBands", "atr": "CudaAtr", "adx": "CudaAdx",
     "supertrend": "CudaSupertrend", "donchian": "CudaDonchian", "willr": "CudaWillr",
     "percentile_nearest_rank": "CudaPercentileNearestRank",
+    "cwma": "CudaCwma", "fwma": "CudaFwma", "srwma": "CudaSrwma", "sqwma": "CudaSqwma", "epma": "CudaEpma",
 }
 CLASSES = {name: _make(name, cls) for name, cls in _CLASS_NAMES.items()}
 __all__ += ["AlmaBatchRange", "PeriodBatchRange", "StdDevBatchRange", "ZscoreBatchRange",
             "BollingerBandsBatchRange", "SuperTrendBatchRange", "PercentileNearestRankBatchRange",
             "AlmaParams", "PeriodParams", "StdDevParams", "ZscoreParams", "BollingerBandsParams",
-            "SuperTrendParams", "PercentileNearestRankParams", "CLASSES", "device_count", "launch_count"]
+            "SuperTrendParams", "PercentileNearestRankParams", "EpmaBatchRange", "EpmaParams", "CLASSES",
+            "device_count", "launch_count"]
 
 
 class TmPlan:
