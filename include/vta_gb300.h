@@ -96,6 +96,14 @@ typedef struct vta_device_array {
 vta_status vta_device_array_free(vta_device_array* arr);
 vta_status vta_device_array_copy_to_host(vta_ctx* ctx, const vta_device_array* arr,
                                          float* host, size_t n);
+/* DeviceArrayF32Py::__dlpack__ (src/utilities/dlpack_cuda.rs:265-374): moves
+ * arr's buffer into a new DLPack managed tensor (2-D f32, kDLCUDA, row-major
+ * strides in elements) and empties arr.  versioned != 0 gives a
+ * DLManagedTensorVersioned (DLPack 1.0, for a "dltensor_versioned" capsule),
+ * else a DLManagedTensor ("dltensor").  Its deleter frees the buffer on the
+ * array's device; vta_dlpack_delete calls it for a tensor nobody consumed. */
+vta_status vta_device_array_to_dlpack(vta_device_array* arr, int versioned, void** out_managed);
+vta_status vta_dlpack_delete(void* managed, int versioned);
 
 /* Page-locked host buffers for fast copies (the crate's LockedBuffer,
  * alma_wrapper.rs:810-815). */

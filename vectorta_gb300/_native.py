@@ -177,6 +177,8 @@ def lib() -> C.CDLL:
     L.vta_launch_count.restype = C.c_uint64
     L.vta_device_array_free.argtypes = [C.POINTER(DeviceArrayC)]
     L.vta_device_array_copy_to_host.argtypes = [vp, C.POINTER(DeviceArrayC), fp, sz]
+    L.vta_device_array_to_dlpack.argtypes = [C.POINTER(DeviceArrayC), C.c_int, C.POINTER(vp)]
+    L.vta_dlpack_delete.argtypes = [vp, C.c_int]
     L.vta_pinned_alloc.argtypes = [sz, C.POINTER(vp)]
     L.vta_pinned_free.argtypes = [vp]
     L.vta_device_alloc.argtypes = [vp, sz, C.POINTER(vp)]

@@ -230,10 +230,39 @@ class Context:
             pass
 
 
+# DLPack capsules (the Python side of vta_device_array_to_dlpack).  A
+# consumer renames the capsule to "used_dltensor[_versioned]" and takes over
+# the managed tensor; a capsule that is dropped unconsumed still carries its
+# original name, and its destructor then frees the tensor.
+# private prototypes: the shared C.pythonapi function objects can have their
+# argtypes changed by other code in the process
+_capsule_new = C.PYFUNCTYPE(C.py_object, C.c_void_p, C.c_char_p, C.c_void_p)(("PyCapsule_New", C.pythonapi))
+_capsule_valid = C.PYFUNCTYPE(C.c_int, C.c_void_p, C.c_char_p)(("PyCapsule_IsValid", C.pythonapi))
+_capsule_ptr = C.PYFUNCTYPE(C.c_void_p, C.c_void_p, C.c_char_p)(("PyCapsule_GetPointer", C.pythonapi))
+_DL_NAMES = {0: b"dltensor", 1: b"dltensor_versioned"}
+
+
+def _make_capsule_dtor(versioned: int):
+    name = _DL_NAMES[versioned]
+
+    @C.CFUNCTYPE(None, C.c_void_p)
+    def dtor(cap):
+        if _capsule_valid(cap, name):
+            N.lib().vta_dlpack_delete(_capsule_ptr(cap, name), versioned)
+
+    return dtor
+
+
+_CAPSULE_DTORS = {v: _make_capsule_dtor(v) for v in (0, 1)}  # kept alive for the process
+
+
 class DeviceArrayF32:
     """Owned device array (alma_wrapper.rs:103-117) with zero-copy export via
-    ``__cuda_array_interface__`` (torch.as_tensor / cupy.asarray work on it),
-    as the crate's DeviceArrayF32Py does (dlpack_cuda.rs:267-374)."""
+    ``__cuda_array_interface__`` (torch.as_tensor / cupy.asarray work on it)
+    and ``__dlpack__`` / ``__dlpack_device__`` (torch.from_dlpack), as the
+    crate's DeviceArrayF32Py does (dlpack_cuda.rs:267-374).  ``__dlpack__``
+    hands the buffer over to the capsule, as the crate does: the array is
+    empty afterwards."""
 
     def __init__(self, c: N.DeviceArrayC, ctx: Context):
         self._c = c
@@ -262,6 +291,21 @@ class DeviceArrayF32:
     def __cuda_array_interface__(self):
         return {"shape": (self.rows, self.cols), "typestr": "<f4", "data": (self.ptr, False),
                 "version": 3, "strides": None}
+
+    def __dlpack_device__(self):
+        return (2, int(self._c.device))  # kDLCUDA
+
+    def __dlpack__(self, stream=None, max_version=None, dl_device=None, copy=None):
+        if dl_device is not None and tuple(dl_device) != self.__dlpack_device__():
+            raise ValueError("dl_device mismatch for __dlpack__" if not copy else
+                             "device copy not implemented for __dlpack__")
+        # every entry point returns after its work has finished, so the data
+        # is complete on any consumer stream
+        versioned = 1 if (max_version is not None and tuple(max_version)[0] >= 1) else 0
+        out = C.c_void_p()
+        N.check(N.lib().vta_device_array_to_dlpack(C.byref(self._c), versioned, C.byref(out)))
+        dtor = _CAPSULE_DTORS[versioned]
+        return _capsule_new(out.value, _DL_NAMES[versioned], C.cast(dtor, C.c_void_p).value)
 
     def to_host(self) -> np.ndarray:
         out = np.empty((self.rows, self.cols), dtype=np.float32)
