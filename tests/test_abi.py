@@ -98,3 +98,15 @@ def test_datagen_deterministic_and_shaped():
         assert np.isnan(col[: leads[s]]).all() and np.isfinite(col[leads[s]: lens[s]]).all()
         assert np.isnan(col[lens[s]:]).all()
         assert (d["high"][leads[s]:lens[s], s] >= d["low"][leads[s]:lens[s], s]).all()
+
+
+def test_ma_computer_names_without_gpu():
+    """vta_ma_supported mirrors supports_vram_kernel_ma (vram_ma.rs:68-76) for
+    the MAs this library has kernels for (trimmed, case-insensitive)."""
+    L = N.lib()
+    for name in ("sma", " EMA ", "wma", "alma", "dema", "tema", "swma", "trima", "sinwma", "epma", "wilders",
+                 "cwma", "fwma", "pwma", "srwma", "sqwma"):
+        assert L.vta_ma_supported(name.encode()) == 1, name
+    for name in ("hma", "jma", "vwma", "frama", "nosuch", ""):
+        assert L.vta_ma_supported(name.encode()) == 0, name
+

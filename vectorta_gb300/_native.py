@@ -179,6 +179,10 @@ def lib() -> C.CDLL:
     L.vta_device_array_copy_to_host.argtypes = [vp, C.POINTER(DeviceArrayC), fp, sz]
     L.vta_device_array_to_dlpack.argtypes = [C.POINTER(DeviceArrayC), C.c_int, C.POINTER(vp)]
     L.vta_dlpack_delete.argtypes = [vp, C.c_int]
+    L.vta_ma_supported.argtypes = [C.c_char_p]
+    L.vta_ma_supported.restype = C.c_int
+    L.vta_ma_periods_device.argtypes = [vp, C.c_char_p, C.POINTER(C.c_char_p), C.POINTER(C.c_double), sz, vp, sz,
+                                        sz, C.POINTER(C.c_int), sz, C.c_int, vp]
     L.vta_pinned_alloc.argtypes = [sz, C.POINTER(vp)]
     L.vta_pinned_free.argtypes = [vp]
     L.vta_device_alloc.argtypes = [vp, sz, C.POINTER(vp)]

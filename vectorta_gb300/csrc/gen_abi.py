@@ -162,6 +162,22 @@ vta_status vta_device_array_copy_to_host(vta_ctx* ctx, const vta_device_array* a
 vta_status vta_device_array_to_dlpack(vta_device_array* arr, int versioned, void** out_managed);
 vta_status vta_dlpack_delete(void* managed, int versioned);
 
+/* ---- MA computer: VramMaComputer (src/cuda/moving_averages/vram_ma.rs) -- */
+/* supports_vram_kernel_ma (vram_ma.rs:68-76), for the MAs this library has
+ * kernels for: sma ema wma alma dema tema swma trima sinwma epma wilders cwma
+ * fwma pwma srwma sqwma (trimmed, case-insensitive); 1 if supported. */
+int vta_ma_supported(const char* ma_type);
+/* compute_period_ma_into (vram_ma.rs:574) / compute_period_ma_tm_into (:2153):
+ * one MA over a device-resident series for an arbitrary list of periods.
+ * Optional parameters as key/value pairs like the crate's HashMap (ALMA
+ * "offset" (0.85) and "sigma" (6.0); EPMA "offset" (0, rounded); missing or
+ * non-finite values take the default).  d_out holds n_periods x len floats:
+ * [period][t] when time_major == 0, else [t][period].  The other names the
+ * crate's computer serves (jsa, smma, hma, ...) give VTA_ERR_NOT_IMPLEMENTED. */
+vta_status vta_ma_periods_device(vta_ctx* ctx, const char* ma_type, const char* const* param_keys,
+    const double* param_values, size_t n_params, const float* d_prices, size_t len, size_t first_valid,
+    const int* periods, size_t n_periods, int time_major, float* d_out);
+
 /* Page-locked host buffers for fast copies (the crate's LockedBuffer,
  * alma_wrapper.rs:810-815). */
 vta_status vta_pinned_alloc(size_t bytes, void** out);

@@ -196,4 +196,30 @@ vta_status launch_prefix_f64(const float* x, int n, int first, int kind, double*
     return check_launch("k_prefix_apply");
 }
 
+// Row-major [rows][cols] -> [cols][rows] through 32 x 33 shared tiles (one
+// coalesced read and one coalesced write per element).
+namespace {
+__global__ void k_transpose(const float* __restrict__ in, int rows, int cols, float* __restrict__ out) {
+    __shared__ float tile[32][33];
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int r = r0 + j, c = c0 + threadIdx.x;
+        if (r < rows && c < cols) tile[j][threadIdx.x] = in[(size_t)r * cols + c];
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int c = c0 + j, r = r0 + threadIdx.x;
+        if (r < rows && c < cols) out[(size_t)c * rows + r] = tile[threadIdx.x][j];
+    }
+}
+}  // namespace
+
+vta_status launch_transpose(const float* in, int rows, int cols, float* out, cudaStream_t st) {
+    if (rows <= 0 || cols <= 0) return VTA_OK;
+    const dim3 grid(ceil_div(cols, 32), ceil_div(rows, 32));
+    if (grid.y > 65535) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "transpose: too many rows");
+    k_transpose<<<grid, dim3(32, 8), 0, st>>>(in, rows, cols, out);
+    return check_launch("k_transpose");
+}
+
 }  // namespace vta

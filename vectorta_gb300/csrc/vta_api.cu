@@ -8,6 +8,7 @@
 // / *_many_series_*_dev forms add the crate's host-side validation, the
 // host->device copies and the output allocation around them.
 #include <algorithm>
+#include <cctype>
 #include <atomic>
 #include <cstdio>
 #include <cstdlib>
@@ -926,6 +927,7 @@ static vta_status batch_host(vta_ctx* ctx, Ind ind, const float* const* hin, siz
         if (need > ctx->io_bytes) {
             VTA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
             if (ctx->io) cudaFree(ctx->io);
+    if (ctx->tmp) cudaFree(ctx->tmp);
             ctx->io = nullptr;
             ctx->io_bytes = 0;
             VTA_TRY(vram_check(need));
@@ -1133,6 +1135,93 @@ static vta_status expand(Ind ind, const R* r, P* out, size_t cap, size_t* n) {
     if (out)
         for (size_t i = 0; i < cs.size() && i < cap; ++i) params_of(cs[i], &out[i]);
     return cs.empty() ? fail(VTA_ERR_INVALID_INPUT, "empty range") : VTA_OK;
+}
+
+// ---- MA computer over a device-resident series (VramMaComputer) ----------
+// The crate's VramMaComputer (vram_ma.rs:87-160) dispatches an MA name and an
+// arbitrary period list to the batch kernels (compute_period_ma_into,
+// vram_ma.rs:574; time-major output: compute_period_ma_tm_into, :2153).
+static int ma_ind(const char* name) {
+    if (!name) return -1;
+    std::string s(name);
+    while (!s.empty() && std::isspace((unsigned char)s.back())) s.pop_back();
+    size_t b = 0;
+    while (b < s.size() && std::isspace((unsigned char)s[b])) ++b;
+    s = s.substr(b);
+    for (char& ch : s) ch = (char)std::tolower((unsigned char)ch);
+    static const struct { const char* n; Ind i; } kMa[] = {
+        {"sma", I_SMA},     {"ema", I_EMA},       {"wma", I_WMA},     {"alma", I_ALMA},   {"dema", I_DEMA},
+        {"tema", I_TEMA},   {"swma", I_SWMA},     {"trima", I_TRIMA}, {"sinwma", I_SINWMA}, {"epma", I_EPMA},
+        {"wilders", I_WILDERS}, {"cwma", I_CWMA}, {"fwma", I_FWMA},   {"pwma", I_PWMA},   {"srwma", I_SRWMA},
+        {"sqwma", I_SQWMA},
+    };
+    for (const auto& m : kMa)
+        if (s == m.n) return m.i;
+    // names the crate's computer also serves (supports_vram_kernel_ma,
+    // vram_ma.rs:68-76) whose kernels are not part of this library
+    static const char* kOther[] = {"jsa", "smma", "highpass", "maaq", "mwdx", "supersmoother",
+                                   "supersmoother_3_pole", "zlema", "nma", "hma", "jma", "edcf",
+                                   "ehlers_itrend", "cora_wave", "vwma", "vpwma", "frama"};
+    for (const char* o : kOther)
+        if (s == o) return -2;
+    return -1;
+}
+
+static double ma_param(const char* const* keys, const double* vals, size_t n, const char* key, double dflt) {
+    for (size_t i = 0; i < n; ++i)
+        if (keys && keys[i] && vals && std::strcmp(keys[i], key) == 0 && std::isfinite(vals[i])) return vals[i];
+    return dflt;  // vram_ma.rs:521-523: missing or non-finite -> default
+}
+
+static vta_status ma_periods_device(vta_ctx* ctx, const char* ma_type, const char* const* keys, const double* vals,
+                                    size_t n_params, const float* d_prices, size_t len, size_t first_valid,
+                                    const int* periods, size_t n_periods, int time_major, float* d_out) {
+    VTA_TRY(check_ctx(ctx));
+    const int mi = ma_ind(ma_type);
+    if (mi == -2) return fail(VTA_ERR_NOT_IMPLEMENTED, std::string("ma computer: no kernel for ") + ma_type);
+    if (mi < 0) return fail(VTA_ERR_INVALID_INPUT, std::string("ma computer: unknown ma_type ") +
+                                                       (ma_type ? ma_type : "(null)"));
+    const Ind ind = (Ind)mi;
+    if (!d_prices || !d_out) return fail(VTA_ERR_INVALID_INPUT, "ma computer: null device pointer");
+    if (!periods || n_periods == 0) return fail(VTA_ERR_INVALID_INPUT, "ma computer: empty period list");
+    if (len == 0) return fail(VTA_ERR_INVALID_INPUT, "ma computer: empty series");
+    if (len > (size_t)INT32_MAX) return fail(VTA_ERR_INVALID_INPUT, "series longer than 2^31-1");
+    const double offset = ma_param(keys, vals, n_params, "offset", ind == I_ALMA ? 0.85 : 0.0);
+    const double sigma = ma_param(keys, vals, n_params, "sigma", 6.0);
+    std::vector<Combo> cs;
+    cs.reserve(n_periods);
+    for (size_t i = 0; i < n_periods; ++i) {
+        if (periods[i] <= 0) return fail(VTA_ERR_INVALID_INPUT, "ma computer: periods must be > 0");
+        const size_t p = (size_t)periods[i];
+        if (ind == I_ALMA) cs.push_back({p, offset, sigma});
+        else if (ind == I_EPMA) cs.push_back({p, std::max(0.0, std::round(offset)), 0.0});
+        else cs.push_back({p, 0.0, 0.0});
+    }
+    VTA_TRY(validate_combos(ind, cs, len, first_valid));
+    DevIn din{};
+    din.p[0] = d_prices;
+    if (!time_major) {
+        float* outs[1] = {d_out};
+        VTA_TRY(run_batch(ctx, ind, din, len, first_valid, cs, outs));
+        return sync(ctx);
+    }
+    // rows are produced row-major into the context's staging buffer, then
+    // transposed into d_out[t][combo]
+    const size_t bytes = n_periods * len * sizeof(float);
+    if (bytes > ctx->tmp_bytes) {
+        VTA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        if (ctx->tmp) cudaFree(ctx->tmp);
+        ctx->tmp = nullptr;
+        ctx->tmp_bytes = 0;
+        VTA_TRY(vram_check(bytes));
+        VTA_CUDA_TRY(cudaMalloc(&ctx->tmp, bytes));
+        ctx->tmp_bytes = bytes;
+    }
+    float* rowmajor = static_cast<float*>(ctx->tmp);
+    float* outs[1] = {rowmajor};
+    VTA_TRY(run_batch(ctx, ind, din, len, first_valid, cs, outs));
+    VTA_TRY(launch_transpose(rowmajor, (int)n_periods, (int)len, d_out, ctx->stream));
+    return sync(ctx);
 }
 
 // ---- hooks for the request server (vta_server.cu) -------------------------
@@ -1455,6 +1544,16 @@ vta_status vta_memcpy_d2h(vta_ctx* ctx, void* dst, const void* src, size_t bytes
 }
 
 // ---------------------------------------------------- per-indicator ABI ----
+int vta_ma_supported(const char* ma_type) { return ma_ind(ma_type) >= 0 ? 1 : 0; }
+
+vta_status vta_ma_periods_device(vta_ctx* ctx, const char* ma_type, const char* const* param_keys,
+                                 const double* param_values, size_t n_params, const float* d_prices, size_t len,
+                                 size_t first_valid, const int* periods, size_t n_periods, int time_major,
+                                 float* d_out) {
+    return ma_periods_device(ctx, ma_type, param_keys, param_values, n_params, d_prices, len, first_valid,
+                             periods, n_periods, time_major, d_out);
+}
+
 #include "vta_abi_gen.inc"
 
 }  // extern "C"

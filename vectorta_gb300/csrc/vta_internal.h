@@ -76,6 +76,8 @@ struct vta_ctx {
     size_t aux_bytes = 0;     // builds after the call's arena pieces are taken)
     void* io = nullptr;       // device inputs + outputs of *_batch_into_host_f32 (host_io cached)
     size_t io_bytes = 0;
+    void* tmp = nullptr;      // row-major staging of time-major MA-computer outputs
+    size_t tmp_bytes = 0;
     void* host_stage = nullptr;  // pinned staging of small uploads, reused per call
     size_t host_stage_bytes = 0;
     size_t host_stage_off = 0;
@@ -144,6 +146,8 @@ enum PrefixKind { PK_X = 0, PK_X2 = 1, PK_GAIN = 2, PK_LOSS = 3, PK_NAN = 4 };
 vta_status launch_prefix_f64(const float* x, int n, int first, int kind, double* out_f64,
                              float2* out_ds, double* block_tmp, cudaStream_t st);
 size_t prefix_tmp_doubles(int n);
+// out[c][r] = in[r][c] for a [rows][cols] f32 matrix.
+vta_status launch_transpose(const float* in, int rows, int cols, float* out, cudaStream_t st);
 
 // --- weighted-window moving averages (ALMA/WMA/SWMA/PWMA/SINWMA/TRIMA,
 // CWMA/FWMA/SRWMA/SQWMA/EPMA) ----------------------------------------------

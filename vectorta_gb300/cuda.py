@@ -408,6 +408,31 @@ class _CudaIndicator:
             C.byref(_to_params(self._fam, params)), *[_dptr(o) for o in d_outs]))
 
 
+class VramMaComputer:
+    """One MA by name over a device-resident series for an arbitrary period
+    list, like the crate's VramMaComputer (vram_ma.rs:87-160, 574, 2153);
+    outputs go to a caller-provided device buffer, [period][t] or, with
+    time_major=True, [t][period]."""
+
+    def __init__(self, device_id: int = 0, ctx: "Context | None" = None):
+        self.ctx = ctx if ctx is not None else Context(device_id)
+
+    @staticmethod
+    def supports(ma_type: str) -> bool:
+        """supports_vram_kernel_ma (vram_ma.rs:68-76) for this library's kernels."""
+        return bool(N.lib().vta_ma_supported(ma_type.encode()))
+
+    def compute_period_ma_into(self, ma_type: str, params, d_prices, series_len: int, first_valid: int,
+                               periods, d_out, time_major: bool = False):
+        params = params or {}
+        keys = (C.c_char_p * max(len(params), 1))(*[k.encode() for k in params])
+        vals = (C.c_double * max(len(params), 1))(*[float(v) for v in params.values()])
+        per = (C.c_int * len(periods))(*[int(p) for p in periods])
+        N.check(N.lib().vta_ma_periods_device(self.ctx.handle, ma_type.encode(), keys, vals, len(params),
+                                              _dptr(d_prices), int(series_len), int(first_valid), per,
+                                              len(periods), 1 if time_major else 0, _dptr(d_out)))
+
+
 def _make(name: str, cls_name: str):
     def method(suffix):
         def f(self, *a, **k):
@@ -438,7 +463,8 @@ CLASSES = {name: _make(name, cls) for name, cls in _CLASS_NAMES.items()}
 __all__ += ["AlmaBatchRange", "PeriodBatchRange", "StdDevBatchRange", "ZscoreBatchRange",
             "BollingerBandsBatchRange", "SuperTrendBatchRange", "PercentileNearestRankBatchRange",
             "AlmaParams", "PeriodParams", "StdDevParams", "ZscoreParams", "BollingerBandsParams",
-            "SuperTrendParams", "PercentileNearestRankParams", "EpmaBatchRange", "EpmaParams", "CLASSES",
+            "SuperTrendParams", "PercentileNearestRankParams", "EpmaBatchRange", "EpmaParams", "VramMaComputer",
+            "CLASSES",
             "device_count", "launch_count"]
 
 
