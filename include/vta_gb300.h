@@ -120,6 +120,18 @@ int vta_ma_supported(const char* ma_type);
 vta_status vta_ma_periods_device(vta_ctx* ctx, const char* ma_type, const char* const* param_keys,
     const double* param_values, size_t n_params, const float* d_prices, size_t len, size_t first_valid,
     const int* periods, size_t n_periods, int time_major, float* d_out);
+/* CudaMaSelector (src/cuda/moving_averages/ma_selector.rs): the same dispatch
+ * from host prices.  ma_to_device / ma_sweep_to_device (ma_selector.rs:935,
+ * 1712): period_start == period_end (or step 0) is the single-period call;
+ * otherwise the selector's own range rule (ma_selector.rs:1037-1061).  out:
+ * rows = periods, cols = len, owned by the caller (vta_device_array_free). */
+vta_status vta_ma_select_dev(vta_ctx* ctx, const char* ma_type, const char* const* param_keys,
+    const double* param_values, size_t n_params, const float* prices, size_t len, size_t period_start,
+    size_t period_end, size_t period_step, vta_device_array* out);
+/* ma_to_host_f32 / ma_sweep_to_host_f32 (ma_selector.rs:954, 1735). */
+vta_status vta_ma_select_into_host_f32(vta_ctx* ctx, const char* ma_type, const char* const* param_keys,
+    const double* param_values, size_t n_params, const float* prices, size_t len, size_t period_start,
+    size_t period_end, size_t period_step, float* out, size_t out_len, size_t* rows, size_t* cols);
 
 /* Page-locked host buffers for fast copies (the crate's LockedBuffer,
  * alma_wrapper.rs:810-815). */

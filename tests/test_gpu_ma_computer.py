@@ -67,3 +67,22 @@ def test_ma_computer_errors(series):
         mc.compute_period_ma_into("nosuchma", None, dx, x.size, 11, [5, 9], out)
     with pytest.raises(RuntimeError):
         mc.compute_period_ma_into("ema", None, dx, x.size, 11, [0, 9], out)
+
+
+def test_ma_selector_single_and_sweep(series):
+    """CudaMaSelector: one period and a descending sweep (the selector's range
+    rule) from host prices, to device and to host, against the oracle."""
+    x, _ = series
+    xd = x.astype(np.float64)
+    sel = V.CudaMaSelector(0)
+    one = sel.ma_to_device("sinwma", x, 14).to_host()
+    assert one.shape == (1, x.size)
+    assert_close(one[0], O.sinwma(xd, 14), TOL["sinwma"], "selector single")
+    h, rows, cols = sel.ma_sweep_to_host_f32("alma", x, 30, 10, 7, {"offset": 0.8, "sigma": 4.0})
+    assert (rows, cols) == (3, x.size)  # 30, 23, 16 (next 9 < 10)
+    exp = np.stack([O.alma(xd, p, 0.8, 4.0) for p in (30, 23, 16)])
+    assert_close(h, exp, TOL["alma"], "selector sweep")
+    d = sel.ma_sweep_to_device("epma", x, 12, 20, 4, {"offset": 3}).to_host()
+    assert_close(d, np.stack([O.epma(xd, p, 3) for p in (12, 16, 20)]), TOL["epma"], "selector epma")
+    h1 = sel.ma_to_host_f32("ema", x, 21)
+    assert_close(h1, O.ema(xd, 21), TOL["ema"], "selector to host")

@@ -183,6 +183,10 @@ def lib() -> C.CDLL:
     L.vta_ma_supported.restype = C.c_int
     L.vta_ma_periods_device.argtypes = [vp, C.c_char_p, C.POINTER(C.c_char_p), C.POINTER(C.c_double), sz, vp, sz,
                                         sz, C.POINTER(C.c_int), sz, C.c_int, vp]
+    L.vta_ma_select_dev.argtypes = [vp, C.c_char_p, C.POINTER(C.c_char_p), C.POINTER(C.c_double), sz, vp, sz, sz,
+                                    sz, sz, C.POINTER(DeviceArrayC)]
+    L.vta_ma_select_into_host_f32.argtypes = [vp, C.c_char_p, C.POINTER(C.c_char_p), C.POINTER(C.c_double), sz,
+                                              vp, sz, sz, sz, sz, vp, sz, C.POINTER(sz), C.POINTER(sz)]
     L.vta_pinned_alloc.argtypes = [sz, C.POINTER(vp)]
     L.vta_pinned_free.argtypes = [vp]
     L.vta_device_alloc.argtypes = [vp, sz, C.POINTER(vp)]

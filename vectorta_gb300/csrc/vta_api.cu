@@ -1224,6 +1224,59 @@ static vta_status ma_periods_device(vta_ctx* ctx, const char* ma_type, const cha
     return sync(ctx);
 }
 
+// The crate's CudaMaSelector (ma_selector.rs:194-1820): the same by-name
+// dispatch from host prices, one period (ma_to_device, :935) or a period
+// range (ma_sweep_to_device, :1712; its own range rule, :1037-1061).
+static std::vector<size_t> selector_periods(size_t start, size_t end, size_t step) {
+    std::vector<size_t> v;
+    if (step == 0 || start == end) return {start};
+    if (start < end) {
+        for (size_t x = start; x <= end; x += step) {
+            v.push_back(x);
+            if (x > SIZE_MAX - step) break;
+        }
+        return v;
+    }
+    size_t cur = start;
+    while (cur >= end) {
+        v.push_back(cur);
+        if (cur == 0) break;
+        const size_t next = cur >= step ? cur - step : 0;
+        if (next == cur) break;
+        cur = next;
+        if (cur < end) break;
+    }
+    return v;
+}
+
+static vta_status ma_select(vta_ctx* ctx, const char* ma_type, const char* const* keys, const double* vals,
+                            size_t n_params, const float* prices, size_t len, size_t start, size_t end, size_t step,
+                            vta_device_array* out_arr, float* out_host, size_t out_len, size_t* rows, size_t* cols) {
+    const int mi = ma_ind(ma_type);
+    if (mi == -2) return fail(VTA_ERR_NOT_IMPLEMENTED, std::string("ma selector: no kernel for ") + ma_type);
+    if (mi < 0) return fail(VTA_ERR_INVALID_INPUT, std::string("ma selector: unknown ma_type ") +
+                                                       (ma_type ? ma_type : "(null)"));
+    const Ind ind = (Ind)mi;
+    if (len == 0) return fail(VTA_ERR_INVALID_INPUT, "ma selector: empty price input");
+    const double offset = ma_param(keys, vals, n_params, "offset", ind == I_ALMA ? 0.85 : 0.0);
+    const double sigma = ma_param(keys, vals, n_params, "sigma", 6.0);
+    std::vector<Combo> cs;
+    for (size_t p : selector_periods(start, end, step)) {
+        if (p == 0 || p > len) {
+            char buf[120];
+            std::snprintf(buf, sizeof buf, "ma selector: invalid period: %zu for length %zu", p, len);
+            return fail(VTA_ERR_INVALID_INPUT, buf);
+        }
+        if (ind == I_ALMA) cs.push_back({p, offset, sigma});
+        else if (ind == I_EPMA) cs.push_back({p, std::max(0.0, std::round(offset)), 0.0});
+        else cs.push_back({p, 0.0, 0.0});
+    }
+    const float* in[1] = {prices};
+    vta_device_array* oa[1] = {out_arr};
+    float* oh[1] = {out_host};
+    return batch_host(ctx, ind, in, len, cs, out_arr ? oa : nullptr, out_host ? oh : nullptr, out_len, rows, cols);
+}
+
 // ---- hooks for the request server (vta_server.cu) -------------------------
 int ind_by_name(const char* name) {
     if (!name) return -1;
@@ -1552,6 +1605,23 @@ vta_status vta_ma_periods_device(vta_ctx* ctx, const char* ma_type, const char* 
                                  float* d_out) {
     return ma_periods_device(ctx, ma_type, param_keys, param_values, n_params, d_prices, len, first_valid,
                              periods, n_periods, time_major, d_out);
+}
+
+vta_status vta_ma_select_dev(vta_ctx* ctx, const char* ma_type, const char* const* param_keys,
+                             const double* param_values, size_t n_params, const float* prices, size_t len,
+                             size_t period_start, size_t period_end, size_t period_step, vta_device_array* out) {
+    if (!prices || !out) return fail(VTA_ERR_INVALID_INPUT, "ma selector: null pointer");
+    return ma_select(ctx, ma_type, param_keys, param_values, n_params, prices, len, period_start, period_end,
+                     period_step, out, nullptr, 0, nullptr, nullptr);
+}
+
+vta_status vta_ma_select_into_host_f32(vta_ctx* ctx, const char* ma_type, const char* const* param_keys,
+                                       const double* param_values, size_t n_params, const float* prices, size_t len,
+                                       size_t period_start, size_t period_end, size_t period_step, float* out,
+                                       size_t out_len, size_t* rows, size_t* cols) {
+    if (!prices || !out) return fail(VTA_ERR_INVALID_INPUT, "ma selector: null pointer");
+    return ma_select(ctx, ma_type, param_keys, param_values, n_params, prices, len, period_start, period_end,
+                     period_step, nullptr, out, out_len, rows, cols);
 }
 
 #include "vta_abi_gen.inc"

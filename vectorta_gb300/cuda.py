@@ -424,13 +424,73 @@ class VramMaComputer:
 
     def compute_period_ma_into(self, ma_type: str, params, d_prices, series_len: int, first_valid: int,
                                periods, d_out, time_major: bool = False):
-        params = params or {}
-        keys = (C.c_char_p * max(len(params), 1))(*[k.encode() for k in params])
-        vals = (C.c_double * max(len(params), 1))(*[float(v) for v in params.values()])
+        keys, vals, n = _kv(params)
         per = (C.c_int * len(periods))(*[int(p) for p in periods])
-        N.check(N.lib().vta_ma_periods_device(self.ctx.handle, ma_type.encode(), keys, vals, len(params),
+        N.check(N.lib().vta_ma_periods_device(self.ctx.handle, ma_type.encode(), keys, vals, n,
                                               _dptr(d_prices), int(series_len), int(first_valid), per,
                                               len(periods), 1 if time_major else 0, _dptr(d_out)))
+
+
+def _kv(params):
+    params = params or {}
+    keys = (C.c_char_p * max(len(params), 1))(*[k.encode() for k in params])
+    vals = (C.c_double * max(len(params), 1))(*[float(v) for v in params.values()])
+    return keys, vals, len(params)
+
+
+class CudaMaSelector:
+    """MA by name from host prices (the crate's CudaMaSelector,
+    ma_selector.rs:194-1820): one period or a period sweep, to a device array
+    or to host f32."""
+
+    def __init__(self, device_id: int = 0, ctx: "Context | None" = None):
+        self.ctx = ctx if ctx is not None else Context(device_id)
+
+    def ma_sweep_to_device(self, ma_type: str, data, start: int, end: int, step: int, params=None):
+        x = _f32(data)
+        keys, vals, n = _kv(params)
+        out = N.DeviceArrayC()
+        N.check(N.lib().vta_ma_select_dev(self.ctx.handle, ma_type.encode(), keys, vals, n, x.ctypes.data, x.size,
+                                          int(start), int(end), int(step), C.byref(out)))
+        return DeviceArrayF32(out, self.ctx)
+
+    def ma_to_device(self, ma_type: str, data, period: int, params=None):
+        return self.ma_sweep_to_device(ma_type, data, period, period, 0, params)
+
+    def ma_sweep_to_host_f32(self, ma_type: str, data, start: int, end: int, step: int, params=None):
+        x = _f32(data)
+        keys, vals, n = _kv(params)
+        r, c = C.c_size_t(), C.c_size_t()
+        rows = len(_selector_periods(int(start), int(end), int(step)))
+        out = np.empty((rows, x.size), dtype=np.float32)
+        N.check(N.lib().vta_ma_select_into_host_f32(self.ctx.handle, ma_type.encode(), keys, vals, n, x.ctypes.data,
+                                                    x.size, int(start), int(end), int(step), out.ctypes.data,
+                                                    out.size, C.byref(r), C.byref(c)))
+        return out, r.value, c.value
+
+    def ma_to_host_f32(self, ma_type: str, data, period: int, params=None):
+        out, _, _ = self.ma_sweep_to_host_f32(ma_type, data, period, period, 0, params)
+        return out[0]
+
+
+def _selector_periods(start: int, end: int, step: int) -> list:
+    """The selector's period range rule (ma_selector.rs:1037-1061)."""
+    if step == 0 or start == end:
+        return [start]
+    if start < end:
+        return list(range(start, end + 1, step))
+    v, cur = [], start
+    while cur >= end:
+        v.append(cur)
+        if cur == 0:
+            break
+        nxt = max(cur - step, 0)
+        if nxt == cur:
+            break
+        cur = nxt
+        if cur < end:
+            break
+    return v
 
 
 def _make(name: str, cls_name: str):
@@ -464,6 +524,7 @@ __all__ += ["AlmaBatchRange", "PeriodBatchRange", "StdDevBatchRange", "ZscoreBat
             "BollingerBandsBatchRange", "SuperTrendBatchRange", "PercentileNearestRankBatchRange",
             "AlmaParams", "PeriodParams", "StdDevParams", "ZscoreParams", "BollingerBandsParams",
             "SuperTrendParams", "PercentileNearestRankParams", "EpmaBatchRange", "EpmaParams", "VramMaComputer",
+            "CudaMaSelector",
             "CLASSES",
             "device_count", "launch_count"]
 
