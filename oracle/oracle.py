@@ -96,6 +96,12 @@ def lib():
             "vto_srwma": ([dp, sz, sz, dp], ip),
             "vto_sqwma": ([dp, sz, sz, dp], ip),
             "vto_epma": ([dp, sz, sz, sz, dp], ip),
+            "vto_ema_stream": ([dp, sz, sz, dp], ip),
+            "vto_sma_stream": ([dp, sz, sz, dp], ip),
+            "vto_alma_stream": ([dp, sz, sz, db, db, dp], ip),
+            "vto_rsi_stream": ([dp, sz, sz, dp], ip),
+            "vto_atr_stream": ([dp, dp, dp, sz, sz, dp], ip),
+            "vto_wilders_stream": ([dp, sz, sz, dp], ip),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -225,6 +231,24 @@ def sqwma(x, period=14):
 
 def epma(x, period=11, offset=4):
     return _single("vto_epma", x, period, offset)
+
+
+def stream(name, inputs, **prm):
+    """The crate's XStream for `name` fed the inputs bar by bar (NaN where
+    update() returns None)."""
+    xs = [_f64(a) for a in inputs]
+    out = np.empty_like(xs[0])
+    L = lib()
+    p = int(prm.get("period", prm.get("length", 14 if name in ("rsi", "atr") else 5 if name == "wilders" else 9)))
+    if name == "alma":
+        code = L.vto_alma_stream(_p(xs[0]), xs[0].size, p, float(prm.get("offset", 0.85)),
+                                 float(prm.get("sigma", 6.0)), _p(out))
+    elif name == "atr":
+        code = L.vto_atr_stream(_p(xs[0]), _p(xs[1]), _p(xs[2]), xs[0].size, p, _p(out))
+    else:
+        code = getattr(L, f"vto_{name}_stream")(_p(xs[0]), xs[0].size, p, _p(out))
+    _check(code, f"{name} stream")
+    return out
 
 
 def trima(x, period=30):

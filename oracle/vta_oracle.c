@@ -1498,3 +1498,219 @@ int vto_epma(const double *x, size_t n, size_t period, size_t offset, double *ou
     }
     return VTO_OK;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Streaming updates (the crate's XStream structs): x[t] is fed to update()   */
+/* in order; out[t] is the returned value, NaN where update() returns None.   */
+/* ------------------------------------------------------------------------ */
+
+/* EmaStream (ema.rs:519-585): running mean over the first `period` finite
+ * values (mean += (x - mean) / c by mul_add), then beta*mean + alpha*x by
+ * mul_add; non-finite x leaves the state alone and returns the mean once
+ * filled. */
+int vto_ema_stream(const double *x, size_t n, size_t period, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    const double alpha = 2.0 / ((double)period + 1.0), beta = 1.0 - alpha;
+    size_t count = 0;
+    double mean = QNAN;
+    int filled = 0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        if (!isfinite(v)) {
+            out[t] = filled ? mean : QNAN;
+            continue;
+        }
+        count++;
+        if (count == 1) mean = v;
+        else if (count <= period) mean = fma(v - mean, 1.0 / (double)count, mean);
+        else mean = fma(beta, mean, alpha * v);
+        if (!filled && count >= period) filled = 1;
+        out[t] = filled ? mean : QNAN;
+    }
+    return VTO_OK;
+}
+
+/* SmaStream (sma.rs: SmaStream::update): ring buffer and running sum,
+ * sum += value - old once full; period 1 copies the value. */
+int vto_sma_stream(const double *x, size_t n, size_t period, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    double *buf = (double *)calloc(period, sizeof(double));
+    size_t head = 0, count = 0;
+    double sum = 0.0, inv = 1.0 / (double)period;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        if (period == 1) { out[t] = v; continue; }
+        if (count < period) {
+            sum += v;
+            buf[head] = v;
+            head = head + 1 == period ? 0 : head + 1;
+            count++;
+            out[t] = count == period ? sum * inv : QNAN;
+            continue;
+        }
+        double old = buf[head];
+        sum += v - old;
+        buf[head] = v;
+        head = head + 1 == period ? 0 : head + 1;
+        out[t] = sum * inv;
+    }
+    free(buf);
+    return VTO_OK;
+}
+
+/* AlmaStream (alma.rs:865-964): weights exp(-(i-m)^2 / (2 s^2)) with
+ * m = offset (p-1), s = p / sigma (no FMA); every value (NaN included) enters
+ * the ring; once `period` values were seen, the window oldest first is
+ * dotted with 4 accumulators (dot_scalar_unrolled_safe) times 1 / norm. */
+void vto_alma_stream_weights(size_t period, double offset, double sigma, double *w, double *inv_norm) {
+    const double m = offset * (double)(period - 1);
+    const double s = (double)period / sigma;
+    const double s2 = 2.0 * s * s;
+    double norm = 0.0;
+    for (size_t i = 0; i < period; i++) {
+        double diff = (double)i - m;
+        w[i] = exp(-(diff * diff) / s2);
+        norm += w[i];
+    }
+    *inv_norm = 1.0 / norm;
+}
+
+int vto_alma_stream(const double *x, size_t n, size_t period, double offset, double sigma, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    if (!(offset >= 0.0 && offset <= 1.0)) return VTO_E_INVALID_PARAM;
+    if (!(sigma > 0.0)) return VTO_E_INVALID_PARAM;
+    double *w = (double *)malloc(sizeof(double) * period);
+    double inv_norm;
+    vto_alma_stream_weights(period, offset, sigma, w, &inv_norm);
+    double *ring = (double *)malloc(sizeof(double) * period);
+    double *win = (double *)malloc(sizeof(double) * period);
+    size_t head = 0, filled = 0;
+    for (size_t t = 0; t < n; t++) {
+        ring[head] = x[t];
+        head = head + 1 == period ? 0 : head + 1;
+        if (filled < period) {
+            filled++;
+            if (filled < period) { out[t] = QNAN; continue; }
+        }
+        for (size_t i = 0; i < period; i++) win[i] = ring[(head + i) % period];
+        size_t n4 = period & ~(size_t)3, i = 0;
+        double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+        for (; i < n4; i += 4) {
+            s0 += win[i] * w[i];
+            s1 += win[i + 1] * w[i + 1];
+            s2 += win[i + 2] * w[i + 2];
+            s3 += win[i + 3] * w[i + 3];
+        }
+        double sum = (s0 + s1) + (s2 + s3);
+        for (; i < period; i++) sum += win[i] * w[i];
+        out[t] = sum * inv_norm;
+    }
+    free(w);
+    free(ring);
+    free(win);
+    return VTO_OK;
+}
+
+/* RsiStream (rsi.rs: RsiStream::update): the first value only primes prev;
+ * gains / losses (f64::max against 0) summed over `period` deltas, a
+ * non-finite delta there poisons the seed (NaN); then Wilder mul_add. */
+int vto_rsi_stream(const double *x, size_t n, size_t period, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    const double inv_p = 1.0 / (double)period, beta = 1.0 - inv_p;
+    int has_prev = 0, poisoned = 0, seeded = 0;
+    size_t seed_count = 0;
+    double prev = QNAN, sg = 0.0, sl = 0.0, ag = 0.0, al = 0.0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        if (!has_prev) { prev = v; has_prev = 1; out[t] = QNAN; continue; }
+        double d = v - prev;
+        prev = v;
+        if (!seeded) {
+            if (!isfinite(d)) poisoned = 1;
+            sg += fmax(d, 0.0);
+            sl += fmax(-d, 0.0);
+            seed_count++;
+            if (seed_count == period) {
+                seeded = 1;
+                if (poisoned) { ag = al = QNAN; out[t] = QNAN; }
+                else {
+                    ag = sg * inv_p;
+                    al = sl * inv_p;
+                    double den = ag + al;
+                    out[t] = den == 0.0 ? 50.0 : 100.0 * ag / den;
+                }
+            } else {
+                out[t] = QNAN;
+            }
+            continue;
+        }
+        ag = fma(ag, beta, inv_p * fmax(d, 0.0));
+        al = fma(al, beta, inv_p * fmax(-d, 0.0));
+        double den = ag + al;
+        out[t] = den == 0.0 ? 50.0 : 100.0 * ag / den;
+    }
+    return VTO_OK;
+}
+
+/* AtrStream (atr.rs: AtrStream::update): TR = h - l while prev_close is NaN,
+ * else max(h, pc) - min(l, pc) by comparisons; seed = sum of the first
+ * `length` TRs times 1/length; then rma = mul_add(alpha, tr - rma, rma). */
+int vto_atr_stream(const double *h, const double *l, const double *c, size_t n, size_t length, double *out) {
+    if (length == 0) return VTO_E_INVALID_PERIOD;
+    const double alpha = 1.0 / (double)length;
+    double pc = QNAN, rma = QNAN, warm_sum = 0.0;
+    size_t warm_count = 0;
+    int seeded = 0;
+    for (size_t t = 0; t < n; t++) {
+        double tr;
+        if (isnan(pc)) tr = h[t] - l[t];
+        else {
+            double up = h[t] > pc ? h[t] : pc;
+            double dn = l[t] < pc ? l[t] : pc;
+            tr = up - dn;
+        }
+        pc = c[t];
+        if (!seeded) {
+            warm_sum += tr;
+            warm_count++;
+            if (warm_count == length) {
+                rma = warm_sum * alpha;
+                seeded = 1;
+                out[t] = rma;
+            } else {
+                out[t] = QNAN;
+            }
+            continue;
+        }
+        rma = fma(alpha, tr - rma, rma);
+        out[t] = rma;
+    }
+    return VTO_OK;
+}
+
+/* WildersStream (wilders.rs: WildersStream::update): a non-finite value
+ * during warm-up restarts it; seed = sum / period; then
+ * mul_add(value - last, alpha, last). */
+int vto_wilders_stream(const double *x, size_t n, size_t period, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    const double alpha = 1.0 / (double)period;
+    double warm_sum = 0.0, last = QNAN;
+    size_t warm_count = 0;
+    int started = 0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        if (!started) {
+            if (!isfinite(v)) { warm_sum = 0.0; warm_count = 0; out[t] = QNAN; continue; }
+            warm_sum += v;
+            warm_count++;
+            if (warm_count < period) { out[t] = QNAN; continue; }
+            last = warm_sum / (double)period;
+            started = 1;
+            out[t] = last;
+            continue;
+        }
+        last = fma(v - last, alpha, last);
+        out[t] = last;
+    }
+    return VTO_OK;
+}

@@ -184,3 +184,21 @@ def test_oracle_weighted_window_warmups(candles):
     for name, (out, warm) in cases.items():
         assert np.all(np.isnan(out[:warm])), name
         assert not np.isnan(out[warm]), name
+
+
+@pytest.mark.parametrize("name", ["ema", "sma", "alma", "rsi", "atr", "wilders"])
+def test_oracle_streams_match_batch(name, candles):
+    """The oracle's XStream restatements agree with the single-series paths
+    after the warm-up, as the crate's own check_X_streaming tests require
+    (e.g. ema.rs:1127-1190: skip 240 bars, |diff| < 1e-9)."""
+    c = candles["close"]
+    p = {"ema": 9, "sma": 9, "alma": 9, "rsi": 14, "atr": 14, "wilders": 5}[name]
+    if name == "atr":
+        s = O.stream("atr", [candles["high"], candles["low"], c], length=p)
+        b = O.atr(candles["high"], candles["low"], c, p)
+    else:
+        s = O.stream(name, [c], period=p)
+        b = {"ema": O.ema, "sma": O.sma, "alma": O.alma, "rsi": O.rsi, "wilders": O.wilders}[name](c, p)
+    s, b = s[240:], b[240:]
+    m = ~(np.isnan(s) & np.isnan(b))
+    assert np.all(np.abs(s[m] - b[m]) < 1e-9 * np.maximum(1.0, np.abs(b[m]))), name

@@ -185,6 +185,12 @@ def lib() -> C.CDLL:
                                         sz, C.POINTER(C.c_int), sz, C.c_int, vp]
     L.vta_ma_select_dev.argtypes = [vp, C.c_char_p, C.POINTER(C.c_char_p), C.POINTER(C.c_double), sz, vp, sz, sz,
                                     sz, sz, C.POINTER(DeviceArrayC)]
+    L.vta_streams_create.argtypes = [vp, C.c_char_p, C.POINTER(C.c_char_p), C.POINTER(C.c_double), sz, sz,
+                                     C.POINTER(vp)]
+    L.vta_streams_update_device.argtypes = [vp, vp, vp, vp, vp]
+    L.vta_streams_update_host.argtypes = [vp, vp, vp, vp, vp]
+    L.vta_streams_reset.argtypes = [vp]
+    L.vta_streams_destroy.argtypes = [vp]
     L.vta_ma_select_into_host_f32.argtypes = [vp, C.c_char_p, C.POINTER(C.c_char_p), C.POINTER(C.c_double), sz,
                                               vp, sz, sz, sz, sz, vp, sz, C.POINTER(sz), C.POINTER(sz)]
     L.vta_pinned_alloc.argtypes = [sz, C.POINTER(vp)]

@@ -190,6 +190,25 @@ vta_status vta_ma_select_into_host_f32(vta_ctx* ctx, const char* ma_type, const 
     const double* param_values, size_t n_params, const float* prices, size_t len, size_t period_start,
     size_t period_end, size_t period_step, float* out, size_t out_len, size_t* rows, size_t* cols);
 
+/* ---- streaming: banks of the crate's XStream structs ----------------- */
+/* n_streams independent streams of one indicator and parameter set on the
+ * device, advanced together by one bar per update, each bar for bar as the
+ * crate's XStream::update (EmaStream ema.rs:519-585, SmaStream sma.rs,
+ * AlmaStream alma.rs:865-964, RsiStream rsi.rs, AtrStream atr.rs,
+ * WildersStream wilders.rs), f64 state, f32 in and out; out is NaN where
+ * update() returns None.  indicator: "ema" "sma" "alma" "rsi" "atr"
+ * "wilders"; parameters as key/value pairs ("period", ATR also "length",
+ * ALMA "offset" / "sigma"; the crate's defaults when absent).  ATR takes
+ * (high, low, close), the others one series in a (b, c NULL). */
+typedef struct vta_streams vta_streams;
+vta_status vta_streams_create(vta_ctx* ctx, const char* indicator, const char* const* param_keys,
+    const double* param_values, size_t n_params, size_t n_streams, vta_streams** out);
+vta_status vta_streams_update_device(vta_streams* s, const float* d_a, const float* d_b, const float* d_c,
+    float* d_out);
+vta_status vta_streams_update_host(vta_streams* s, const float* a, const float* b, const float* c, float* out);
+vta_status vta_streams_reset(vta_streams* s);
+vta_status vta_streams_destroy(vta_streams* s);
+
 /* Page-locked host buffers for fast copies (the crate's LockedBuffer,
  * alma_wrapper.rs:810-815). */
 vta_status vta_pinned_alloc(size_t bytes, void** out);

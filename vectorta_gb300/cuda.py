@@ -473,6 +473,48 @@ class CudaMaSelector:
         return out[0]
 
 
+class StreamBank:
+    """n_streams streams of one indicator on the device, advanced together one
+    bar per update, each as the crate's XStream (EmaStream, SmaStream,
+    AlmaStream, RsiStream, AtrStream, WildersStream).  update() returns the
+    n_streams new values, NaN where the crate's update() returns None."""
+
+    def __init__(self, indicator: str, n_streams: int, params=None, device_id: int = 0,
+                 ctx: "Context | None" = None):
+        self.ctx = ctx if ctx is not None else Context(device_id)
+        self.indicator, self.n = indicator, int(n_streams)
+        keys, vals, n = _kv(params)
+        h = C.c_void_p()
+        N.check(N.lib().vta_streams_create(self.ctx.handle, indicator.encode(), keys, vals, n, self.n, C.byref(h)))
+        self._h = h
+
+    def update(self, *bars) -> np.ndarray:
+        xs = [_f32(b) for b in bars]
+        assert all(x.size == self.n for x in xs)
+        out = np.empty(self.n, dtype=np.float32)
+        ptrs = [x.ctypes.data for x in xs] + [None] * (3 - len(xs))
+        N.check(N.lib().vta_streams_update_host(self._h, *ptrs, out.ctypes.data))
+        return out
+
+    def update_device(self, *d_bars, d_out):
+        ptrs = [_dptr(b) for b in d_bars] + [None] * (3 - len(d_bars))
+        N.check(N.lib().vta_streams_update_device(self._h, *ptrs, _dptr(d_out)))
+
+    def reset(self):
+        N.check(N.lib().vta_streams_reset(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            N.lib().vta_streams_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _selector_periods(start: int, end: int, step: int) -> list:
     """The selector's period range rule (ma_selector.rs:1037-1061)."""
     if step == 0 or start == end:
@@ -524,7 +566,7 @@ __all__ += ["AlmaBatchRange", "PeriodBatchRange", "StdDevBatchRange", "ZscoreBat
             "BollingerBandsBatchRange", "SuperTrendBatchRange", "PercentileNearestRankBatchRange",
             "AlmaParams", "PeriodParams", "StdDevParams", "ZscoreParams", "BollingerBandsParams",
             "SuperTrendParams", "PercentileNearestRankParams", "EpmaBatchRange", "EpmaParams", "VramMaComputer",
-            "CudaMaSelector",
+            "CudaMaSelector", "StreamBank",
             "CLASSES",
             "device_count", "launch_count"]
 
