@@ -38,11 +38,15 @@ __device__ __forceinline__ float true_range(float hi, float lo, float pc) {
 // DX from the smoothed DM and TR sums.  The crate forms +DI = 100 pdm / atr and
 // -DI = 100 mdm / atr, then DX = 100 |+DI - -DI| / (+DI + -DI); the common
 // factor 100 / atr cancels, leaving one division.  atr == 0 gives 0 (both DI
-// are 0) and a NaN atr gives NaN, as in the crate.
+// are 0) and a NaN atr gives NaN, as in the crate.  The ratio |a - b| / (a + b)
+// lies in [0, 1] and is taken with the fast reciprocal-multiply divide (2 ulp;
+// the ADX sweeps and plans are issue-bound and the IEEE divide was a third of
+// a step); every ADX kernel shares this function, so the chunked and the
+// sequential kernels stay bit-identical.
 __device__ __forceinline__ float adx_dx(float pdm, float mdm, float atr) {
     if (atr == 0.f) return 0.f;
     const float s = pdm + mdm;
-    const float d = s != 0.f ? (fabsf(pdm - mdm) / s) * 100.f : 0.f;
+    const float d = s != 0.f ? __fdividef(fabsf(pdm - mdm), s) * 100.f : 0.f;
     return atr == atr ? d : qnan();
 }
 
