@@ -108,13 +108,13 @@ vta_status vta_dlpack_delete(void* managed, int versioned);
 /* ---- MA computer: VramMaComputer (src/cuda/moving_averages/vram_ma.rs) -- */
 /* supports_vram_kernel_ma (vram_ma.rs:68-76), for the MAs this library has
  * kernels for: sma ema wma alma dema tema swma trima sinwma epma wilders cwma
- * fwma pwma srwma sqwma (trimmed, case-insensitive); 1 if supported. */
+ * fwma pwma srwma sqwma vpwma (trimmed, case-insensitive); 1 if supported. */
 int vta_ma_supported(const char* ma_type);
 /* compute_period_ma_into (vram_ma.rs:574) / compute_period_ma_tm_into (:2153):
  * one MA over a device-resident series for an arbitrary list of periods.
  * Optional parameters as key/value pairs like the crate's HashMap (ALMA
- * "offset" (0.85) and "sigma" (6.0); EPMA "offset" (0, rounded); missing or
- * non-finite values take the default).  d_out holds n_periods x len floats:
+ * "offset" (0.85) and "sigma" (6.0); EPMA "offset" (0, rounded); VPWMA
+ * "power" (0.382); missing or non-finite values take the default).  d_out holds n_periods x len floats:
  * [period][t] when time_major == 0, else [t][period].  The other names the
  * crate's computer serves (jsa, smma, hma, ...) give VTA_ERR_NOT_IMPLEMENTED. */
 vta_status vta_ma_periods_device(vta_ctx* ctx, const char* ma_type, const char* const* param_keys,
@@ -192,6 +192,9 @@ typedef struct vta_percentile_params { size_t length; double percentage; } vta_p
 /* EpmaBatchRange / EpmaParams (epma.rs:750-753; offset < period) */
 typedef struct vta_epma_batch_range { vta_range_usize period, offset; } vta_epma_batch_range;
 typedef struct vta_epma_params { size_t period, offset; } vta_epma_params;
+/* VpwmaBatchRange / VpwmaParams (vpwma.rs:887-899; power finite) */
+typedef struct vta_vpwma_batch_range { vta_range_usize period; vta_range_f64 power; } vta_vpwma_batch_range;
+typedef struct vta_vpwma_params { size_t period; double power; } vta_vpwma_params;
 
 /* ==== alma (src/cuda/moving_averages/alma_wrapper.rs) ==== */
 /* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
@@ -687,6 +690,25 @@ vta_status vta_epma_many_series_one_param_time_major_dev(vta_ctx* ctx, const flo
 vta_status vta_epma_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
     size_t cols, size_t rows, const vta_epma_params* params, float* d_out);
 
+/* ==== vpwma (src/cuda/moving_averages/vpwma_wrapper.rs) ==== */
+/* expand_grid: the crate's combo order; n_combos always set; out may be NULL. */
+vta_status vta_vpwma_expand_grid(const vta_vpwma_batch_range* sweep, vta_vpwma_params* out, size_t cap, size_t* n_combos);
+/* vpwma_batch_dev (vpwma_wrapper.rs:720) */
+vta_status vta_vpwma_batch_dev(vta_ctx* ctx, const float* data, size_t len,
+    const vta_vpwma_batch_range* sweep, vta_device_array* out);
+/* vpwma_batch_device / _from_device_prices (vpwma_wrapper.rs:751); first_valid as in the crate. */
+vta_status vta_vpwma_batch_device(vta_ctx* ctx, const float* d_data, size_t len,
+    size_t first_valid, const vta_vpwma_batch_range* sweep, float* d_out);
+/* vpwma_batch_into_host_f32 (vpwma_wrapper.rs:730); each output holds out_len >= rows*cols floats. */
+vta_status vta_vpwma_batch_into_host_f32(vta_ctx* ctx, const float* data, size_t len,
+    const vta_vpwma_batch_range* sweep, float* out, size_t out_len, size_t* rows, size_t* cols);
+/* vpwma_many_series_one_param_time_major_dev (vpwma_wrapper.rs:851) */
+vta_status vta_vpwma_many_series_one_param_time_major_dev(vta_ctx* ctx, const float* data_tm,
+    size_t cols, size_t rows, const vta_vpwma_params* params, vta_device_array* out);
+/* vpwma_many_series_one_param_device (vpwma_wrapper.rs:823) */
+vta_status vta_vpwma_many_series_one_param_device(vta_ctx* ctx, const float* d_data_tm,
+    size_t cols, size_t rows, const vta_vpwma_params* params, float* d_out);
+
 /* ==== many-series work-list plans ====
  * No counterpart in the crate, whose many-series entry points run one
  * indicator per call over a rectangular time-major matrix.  A plan runs
@@ -744,7 +766,7 @@ vta_status vta_tm_plan_destroy(vta_tm_plan* plan);
  * Times are seconds since the server was created. */
 typedef struct vta_sweep {      /* generic sweep: the fields each indicator reads */
     vta_range_usize period;     /* period / length */
-    vta_range_f64 p1;           /* alma offset, stddev/zscore nbdev, bb devup, supertrend factor, percentile %, epma offset */
+    vta_range_f64 p1;           /* alma offset, stddev/zscore nbdev, bb devup, supertrend factor, percentile %, epma offset, vpwma power */
     vta_range_f64 p2;           /* alma sigma, bb devdn */
 } vta_sweep;
 typedef struct vta_server_config {

@@ -32,6 +32,7 @@ AXIS_MODE = {
     "percentile_nearest_rank": AX_DESC, "wma": AX_DESC_PLUS_END, "swma": AX_DESC,
     "pwma": AX_DESC, "sinwma": AX_DESC, "trima": AX_SWAP,
     "cwma": AX_SWAP, "fwma": AX_SWAP, "srwma": AX_DESC, "sqwma": AX_DESC, "epma": AX_SWAP,
+    "vpwma": AX_DESC,
 }
 
 
@@ -96,6 +97,7 @@ def lib():
             "vto_srwma": ([dp, sz, sz, dp], ip),
             "vto_sqwma": ([dp, sz, sz, dp], ip),
             "vto_epma": ([dp, sz, sz, sz, dp], ip),
+            "vto_vpwma": ([dp, sz, sz, db, dp], ip),
             "vto_ema_stream": ([dp, sz, sz, dp], ip),
             "vto_sma_stream": ([dp, sz, sz, dp], ip),
             "vto_alma_stream": ([dp, sz, sz, db, db, dp], ip),
@@ -227,6 +229,10 @@ def srwma(x, period=14):
 
 def sqwma(x, period=14):
     return _single("vto_sqwma", x, period)
+
+
+def vpwma(x, period=14, power=0.382):
+    return _single("vto_vpwma", x, period, power)
 
 
 def epma(x, period=11, offset=4):

@@ -1714,3 +1714,39 @@ int vto_wilders_stream(const double *x, size_t n, size_t period, double *out) {
     }
     return VTO_OK;
 }
+
+/* vpwma_with_kernel (vpwma.rs:215-290): weights (p - k)^power, k < p - 1
+ * (newest first), inv_norm = 1 / sum, first output first + p - 1;
+ * vpwma_scalar (vpwma.rs:296-360): four mul_add accumulators, two rounds per
+ * block of 8, then a block of 4, then up to three more (one per
+ * accumulator), summed as (s0 + s1) + (s2 + s3). */
+int vto_vpwma(const double *x, size_t n, size_t period, double power, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period < 2 || period > n) return VTO_E_INVALID_PERIOD;
+    if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    if (!isfinite(power)) return VTO_E_INVALID_PARAM;
+    const size_t wl = period - 1;
+    double *w = (double *)malloc(sizeof(double) * wl);
+    double norm = 0.0;
+    for (size_t k = 0; k < wl; k++) {
+        w[k] = pow((double)period - (double)k, power);
+        norm += w[k];
+    }
+    const double inv = 1.0 / norm;
+    fill_nan(out, first + wl < n ? first + wl : n);
+    const size_t p8 = wl & ~(size_t)7, p4 = wl & ~(size_t)3;
+    for (size_t i = first + wl; i < n; i++) {
+        double s[4] = {0, 0, 0, 0};
+        size_t k = 0;
+        for (; k < p8; k += 8)
+            for (int j = 0; j < 8; j++) s[j & 3] = fma(x[i - (k + j)], w[k + j], s[j & 3]);
+        for (; k < p4; k += 4)
+            for (int j = 0; j < 4; j++) s[j] = fma(x[i - (k + j)], w[k + j], s[j]);
+        for (int j = 0; k + j < wl; j++) s[j] = fma(x[i - (k + j)], w[k + j], s[j]);
+        out[i] = ((s[0] + s[1]) + (s[2] + s[3])) * inv;
+    }
+    free(w);
+    return VTO_OK;
+}

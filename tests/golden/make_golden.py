@@ -86,6 +86,7 @@ def main(ref: str):
     from_py("srwma", "srwma", {"period": 14}, 1e-8, "srwma.rs:1476-1490")
     from_py("sqwma", "sqwma", {"period": 14}, 1e-5, "sqwma.rs:1066-1090")
     from_py("epma", "epma", {"period": 11, "offset": 4}, 1e-1, "epma.rs:1217-1225")
+    from_py("vpwma", "vpwma", {"period": 14, "power": 0.382}, 1e-2, "vpwma.rs:1690-1707")
     from_py("wilders", "wilders", {"period": 5}, 1e-8, "wilders.rs:1229-1235")
     from_py("atr", "atr", {"length": 14}, 1e-2, "atr.rs:1422")
     from_py("adx", "adx", {"period": 14}, 1e-1, "adx.rs:2163")

@@ -105,7 +105,7 @@ def test_ma_computer_names_without_gpu():
     the MAs this library has kernels for (trimmed, case-insensitive)."""
     L = N.lib()
     for name in ("sma", " EMA ", "wma", "alma", "dema", "tema", "swma", "trima", "sinwma", "epma", "wilders",
-                 "cwma", "fwma", "pwma", "srwma", "sqwma"):
+                 "cwma", "fwma", "pwma", "srwma", "sqwma", "vpwma"):
         assert L.vta_ma_supported(name.encode()) == 1, name
     for name in ("hma", "jma", "vwma", "frama", "nosuch", ""):
         assert L.vta_ma_supported(name.encode()) == 0, name

@@ -23,8 +23,9 @@ CASES = {
     "srwma": lambda x, p, prm: O.srwma(x, p), "sqwma": lambda x, p, prm: O.sqwma(x, p),
     "alma": lambda x, p, prm: O.alma(x, p, prm.get("offset", 0.85), prm.get("sigma", 6.0)),
     "epma": lambda x, p, prm: O.epma(x, p, int(round(prm.get("offset", 0.0)))),
+    "vpwma": lambda x, p, prm: O.vpwma(x, p, prm.get("power", 0.382)),
 }
-PARAMS = {"alma": {"offset": 0.9, "sigma": 5.0}, "epma": {"offset": 2.0}}
+PARAMS = {"alma": {"offset": 0.9, "sigma": 5.0}, "epma": {"offset": 2.0}, "vpwma": {"power": 0.5}}
 
 
 @pytest.fixture(scope="module")

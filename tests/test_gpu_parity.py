@@ -20,7 +20,7 @@ TOL = {
     "adx": 1e-1, "supertrend": 7e-4, "sma": 1e-5, "stddev": 5e-4, "zscore": 5e-4,
     "bollinger_bands": 1e-3, "donchian": 5e-4, "willr": 5e-5, "percentile_nearest_rank": 1e-4,
     "wma": 1e-5, "swma": 2e-4, "pwma": 5e-4, "sinwma": 1e-5, "trima": 1e-4,
-    "cwma": 5e-5, "fwma": 5e-4, "srwma": 2e-5, "sqwma": 1e-5, "epma": 2e-5,
+    "cwma": 5e-5, "fwma": 5e-4, "srwma": 2e-5, "sqwma": 1e-5, "epma": 2e-5, "vpwma": 5e-4,
 }
 TOL_TM = dict(TOL, alma=3e-4, adx=3e-2)
 
@@ -76,6 +76,9 @@ def oracle_batch(name, d, sweep):
     simple = {"ema": O.ema, "dema": O.dema, "tema": O.tema, "wma": O.wma, "swma": O.swma,
               "sinwma": O.sinwma, "trima": O.trima, "cwma": O.cwma, "fwma": O.fwma, "srwma": O.srwma,
               "sqwma": O.sqwma}
+    if name == "vpwma":
+        pws = O.axis_f64(sweep["power"])
+        return [np.stack([O.vpwma(c, p, w) for p in ps for w in pws])]
     if name == "epma":
         offs = O.axis_usize(sweep["offset"], O.AX_SWAP)
         return [np.stack([O.epma(c, p, o) for p in ps for o in offs])]
@@ -133,6 +136,7 @@ SWEEPS = {
     "sqwma": {"period": (2, 120, 3)},
     # offsets even, so no combo has a zero weight sum (p - 1 odd, offset 2 + (p - 2) / 2)
     "epma": {"period": (8, 60, 4), "offset": (0, 6, 2)},
+    "vpwma": {"period": (2, 120, 3), "power": (0.2, 0.8, 0.3)},
 }
 
 
@@ -218,7 +222,7 @@ PARAMS = {
     "adx": {"period": 14}, "supertrend": {"period": 10, "factor": 3.0}, "donchian": {"period": 20},
     "willr": {"period": 14}, "percentile_nearest_rank": {"length": 50, "percentage": 50.0},
     "cwma": {"period": 14}, "fwma": {"period": 10}, "srwma": {"period": 14}, "sqwma": {"period": 14},
-    "epma": {"period": 11, "offset": 4},
+    "epma": {"period": 11, "offset": 4}, "vpwma": {"period": 14, "power": 0.382},
 }
 
 
@@ -238,6 +242,7 @@ def oracle_series(name, c, h, l, prm):
         "percentile_nearest_rank": lambda: [O.percentile_nearest_rank(c, p, prm["percentage"])],
         "cwma": lambda: [O.cwma(c, p)], "fwma": lambda: [O.fwma(c, p)], "srwma": lambda: [O.srwma(c, p)],
         "sqwma": lambda: [O.sqwma(c, p)], "epma": lambda: [O.epma(c, p, prm["offset"])],
+        "vpwma": lambda: [O.vpwma(c, p, prm["power"])],
     }[name]
     return fn()
 

@@ -40,6 +40,7 @@ SINGLE = {
     "srwma": lambda c, p: O.srwma(c["close"], **p),
     "sqwma": lambda c, p: O.sqwma(c["close"], **p),
     "epma": lambda c, p: O.epma(c["close"], **p),
+    "vpwma": lambda c, p: O.vpwma(c["close"], **p),
 }
 
 

@@ -57,6 +57,7 @@ SWEEPS = {
     "supertrend": _struct("vta_supertrend_batch_range", [("period", RangeUsize), ("factor", RangeF64)]),
     "percentile": _struct("vta_percentile_batch_range", [("length", RangeUsize), ("percentage", RangeF64)]),
     "epma": _struct("vta_epma_batch_range", [("period", RangeUsize), ("offset", RangeUsize)]),
+    "vpwma": _struct("vta_vpwma_batch_range", [("period", RangeUsize), ("power", RangeF64)]),
 }
 PARAMS = {
     "alma": _struct("vta_alma_params", [("period", C.c_size_t), ("offset", C.c_double), ("sigma", C.c_double)]),
@@ -68,6 +69,7 @@ PARAMS = {
     "supertrend": _struct("vta_supertrend_params", [("period", C.c_size_t), ("factor", C.c_double)]),
     "percentile": _struct("vta_percentile_params", [("length", C.c_size_t), ("percentage", C.c_double)]),
     "epma": _struct("vta_epma_params", [("period", C.c_size_t), ("offset", C.c_size_t)]),
+    "vpwma": _struct("vta_vpwma_params", [("period", C.c_size_t), ("power", C.c_double)]),
 }
 
 # name -> (input kind, outputs, sweep/params family)
@@ -98,6 +100,7 @@ INDICATORS = {
     "srwma": ("x", ["out"], "period"),
     "sqwma": ("x", ["out"], "period"),
     "epma": ("x", ["out"], "epma"),
+    "vpwma": ("x", ["out"], "vpwma"),
 }
 N_IN = {"x": 1, "hl": 2, "hlc": 3}
 

@@ -35,6 +35,7 @@ IND = [
  ("srwma","src/cuda/moving_averages/srwma_wrapper.rs","x",["out"],"period","period",(176,328,420,None,485,572)),
  ("sqwma","src/cuda/moving_averages/sqwma_wrapper.rs","x",["out"],"period","period",(62,157,190,166,255,222)),
  ("epma","src/cuda/moving_averages/epma_wrapper.rs","x",["out"],"epma","epma",(110,485,574,495,773,805)),
+ ("vpwma","src/cuda/moving_averages/vpwma_wrapper.rs","x",["out"],"vpwma","vpwma",(126,720,751,730,851,823)),
 ]
 RANGES = {
  "alma": ("vta_alma_batch_range", "vta_alma_params"),
@@ -45,6 +46,7 @@ RANGES = {
  "supertrend": ("vta_supertrend_batch_range", "vta_supertrend_params"),
  "percentile": ("vta_percentile_batch_range", "vta_percentile_params"),
  "epma": ("vta_epma_batch_range", "vta_epma_params"),
+ "vpwma": ("vta_vpwma_batch_range", "vta_vpwma_params"),
 }
 def inputs(kind, dev, tm):
     pre = "d_" if dev else ""
@@ -165,13 +167,13 @@ vta_status vta_dlpack_delete(void* managed, int versioned);
 /* ---- MA computer: VramMaComputer (src/cuda/moving_averages/vram_ma.rs) -- */
 /* supports_vram_kernel_ma (vram_ma.rs:68-76), for the MAs this library has
  * kernels for: sma ema wma alma dema tema swma trima sinwma epma wilders cwma
- * fwma pwma srwma sqwma (trimmed, case-insensitive); 1 if supported. */
+ * fwma pwma srwma sqwma vpwma (trimmed, case-insensitive); 1 if supported. */
 int vta_ma_supported(const char* ma_type);
 /* compute_period_ma_into (vram_ma.rs:574) / compute_period_ma_tm_into (:2153):
  * one MA over a device-resident series for an arbitrary list of periods.
  * Optional parameters as key/value pairs like the crate's HashMap (ALMA
- * "offset" (0.85) and "sigma" (6.0); EPMA "offset" (0, rounded); missing or
- * non-finite values take the default).  d_out holds n_periods x len floats:
+ * "offset" (0.85) and "sigma" (6.0); EPMA "offset" (0, rounded); VPWMA
+ * "power" (0.382); missing or non-finite values take the default).  d_out holds n_periods x len floats:
  * [period][t] when time_major == 0, else [t][period].  The other names the
  * crate's computer serves (jsa, smma, hma, ...) give VTA_ERR_NOT_IMPLEMENTED. */
 vta_status vta_ma_periods_device(vta_ctx* ctx, const char* ma_type, const char* const* param_keys,
@@ -249,6 +251,9 @@ typedef struct vta_percentile_params { size_t length; double percentage; } vta_p
 /* EpmaBatchRange / EpmaParams (epma.rs:750-753; offset < period) */
 typedef struct vta_epma_batch_range { vta_range_usize period, offset; } vta_epma_batch_range;
 typedef struct vta_epma_params { size_t period, offset; } vta_epma_params;
+/* VpwmaBatchRange / VpwmaParams (vpwma.rs:887-899; power finite) */
+typedef struct vta_vpwma_batch_range { vta_range_usize period; vta_range_f64 power; } vta_vpwma_batch_range;
+typedef struct vta_vpwma_params { size_t period; double power; } vta_vpwma_params;
 """)
 for (name, wf, kind, outs, rng, prm, cites) in IND:
     R, P = RANGES[rng]
@@ -331,7 +336,7 @@ w("""/* ==== request server (continuous batching over a device-resident store) =
  * Times are seconds since the server was created. */
 typedef struct vta_sweep {      /* generic sweep: the fields each indicator reads */
     vta_range_usize period;     /* period / length */
-    vta_range_f64 p1;           /* alma offset, stddev/zscore nbdev, bb devup, supertrend factor, percentile %, epma offset */
+    vta_range_f64 p1;           /* alma offset, stddev/zscore nbdev, bb devup, supertrend factor, percentile %, epma offset, vpwma power */
     vta_range_f64 p2;           /* alma sigma, bb devdn */
 } vta_sweep;
 typedef struct vta_server_config {
@@ -421,7 +426,7 @@ ENUM = {"alma":"I_ALMA","ema":"I_EMA","dema":"I_DEMA","tema":"I_TEMA","rsi":"I_R
         "stddev":"I_STDDEV","zscore":"I_ZSCORE","bollinger_bands":"I_BB","atr":"I_ATR","adx":"I_ADX",
         "supertrend":"I_SUPERTREND","donchian":"I_DONCHIAN","willr":"I_WILLR",
         "percentile_nearest_rank":"I_PNR","cwma":"I_CWMA","fwma":"I_FWMA","srwma":"I_SRWMA",
-        "sqwma":"I_SQWMA","epma":"I_EPMA"}
+        "sqwma":"I_SQWMA","epma":"I_EPMA","vpwma":"I_VPWMA"}
 def names(kind, dev, tm):
     return [a.split()[-1] for a in inputs(kind, dev, tm)]
 inc = ["// Generated by gen_abi.py: extern \"C\" entry points forwarding to the drivers of",

@@ -56,6 +56,7 @@ __device__ __forceinline__ DS split(double v) {
 struct RowConst {
     DS m;        // ALMA centre offset (p - 1)
     DS inv2s2;   // ALMA 1 / (2 s^2) = sigma^2 / (2 p^2)
+    double pw;   // VPWMA power
 };
 
 __device__ DS raw_weight(int kind, int i, int p, const RowConst& rc) {
@@ -89,8 +90,8 @@ __device__ DS raw_weight(int kind, int i, int p, const RowConst& rc) {
             const int m1 = (p + 1) / 2, m2 = p - m1 + 1;
             return {(float)min(min(i + 1, p - i), min(m1, m2)), 0.f};
         }
-        // the next four have window L = p (FWMA) or L = period - 1 (the
-        // others), oldest first; p here is L
+        // the rest have window L = p (FWMA) or L = period - 1 (the others),
+        // oldest first; p here is L
         case WT_CWMA: {  // (k + 2)^3, cwma.rs:246-252
             const double v = (double)(i + 2);
             return split(v * v * v);
@@ -121,6 +122,9 @@ __device__ DS raw_weight(int kind, int i, int p, const RowConst& rc) {
         case WT_EPMA: {  // c0 + k with c0 = 2 - offset, epma.rs:346-366
             return {(float)(i + 2) - rc.inv2s2.hi, 0.f};
         }
+        case WT_VPWMA: {  // (k + 2)^power, vpwma.rs:247-256 (f64 pow, once per weight)
+            return split(pow((double)(i + 2), rc.pw));
+        }
     }
     return {0.f, 0.f};
 }
@@ -139,6 +143,8 @@ __global__ void __launch_bounds__(kWThreads) k_weights(int kind, const int* peri
         rc.m = split(0.69424191363061730173879026);  // log2 of the golden ratio
     } else if (kind == WT_EPMA) {
         rc.inv2s2 = DS{(float)pa[c], 0.f};  // the offset (an integer)
+    } else if (kind == WT_VPWMA) {
+        rc.pw = pa[c];
     } else if (kind == WT_ALMA) {
         float m_hi = 0.f, m_lo = 0.f, q_hi = 0.f, q_lo = 0.f;
         if (lane == 0) {

@@ -152,7 +152,7 @@ static std::vector<double> axis_f64(vta_range_f64 r) {
 enum Ind {
     I_ALMA, I_EMA, I_DEMA, I_TEMA, I_RSI, I_WILDERS, I_SMA, I_WMA, I_SWMA, I_PWMA, I_SINWMA, I_TRIMA,
     I_STDDEV, I_ZSCORE, I_BB, I_ATR, I_ADX, I_SUPERTREND, I_DONCHIAN, I_WILLR, I_PNR,
-    I_CWMA, I_FWMA, I_SRWMA, I_SQWMA, I_EPMA
+    I_CWMA, I_FWMA, I_SRWMA, I_SQWMA, I_EPMA, I_VPWMA
 };
 enum InKind { IN_X = 1, IN_HL = 2, IN_HLC = 3 };
 
@@ -171,12 +171,12 @@ static const IndInfo kInfo[] = {
     {"atr", IN_HLC, 1, AX_REV_FROM_END}, {"adx", IN_HLC, 1, AX_DESC},     {"supertrend", IN_HLC, 2, AX_DESC},
     {"donchian", IN_HL, 3, AX_DESC},   {"willr", IN_HLC, 1, AX_DESC},     {"percentile_nearest_rank", IN_X, 1, AX_DESC},
     {"cwma", IN_X, 1, AX_SWAP},        {"fwma", IN_X, 1, AX_SWAP},        {"srwma", IN_X, 1, AX_DESC},
-    {"sqwma", IN_X, 1, AX_DESC},       {"epma", IN_X, 1, AX_SWAP},
+    {"sqwma", IN_X, 1, AX_DESC},       {"epma", IN_X, 1, AX_SWAP},        {"vpwma", IN_X, 1, AX_DESC},
 };
 
 // One parameter set: period plus up to two f64 parameters
 // (alma: offset, sigma; stddev/zscore: nbdev; bb: devup, devdn;
-//  supertrend: factor; percentile: percentage; epma: offset).
+//  supertrend: factor; percentile: percentage; epma: offset; vpwma: power).
 struct Combo {
     size_t period;
     double a, b;
@@ -184,7 +184,7 @@ struct Combo {
 
 static bool is_wwma(Ind i) {
     return i == I_ALMA || i == I_WMA || i == I_SWMA || i == I_PWMA || i == I_SINWMA || i == I_TRIMA ||
-           i == I_CWMA || i == I_FWMA || i == I_SRWMA || i == I_SQWMA || i == I_EPMA;
+           i == I_CWMA || i == I_FWMA || i == I_SRWMA || i == I_SQWMA || i == I_EPMA || i == I_VPWMA;
 }
 
 // Weighted-window geometry of a combo: window length L (the weight row) and
@@ -193,13 +193,15 @@ static bool is_wwma(Ind i) {
 //   SRWMA L = p - 1, first output first + p + 1   (srwma.rs:204-215, 288-292)
 //   SQWMA L = p - 1, first output first + p + 1   (sqwma.rs:222-228, 270-272)
 //   EPMA  L = p - 1, first output first + p + o + 1 (epma.rs:247, 341-352)
+//   VPWMA L = p - 1, first output first + p - 1   (vpwma.rs:246-262, 296-312)
 //   others L = p, first output first + p - 1
 static int wwma_len(Ind i, const Combo& c) {
-    return (i == I_CWMA || i == I_SRWMA || i == I_SQWMA || i == I_EPMA) ? (int)c.period - 1 : (int)c.period;
+    return (i == I_CWMA || i == I_SRWMA || i == I_SQWMA || i == I_EPMA || i == I_VPWMA) ? (int)c.period - 1
+                                                                                        : (int)c.period;
 }
 static int wwma_warm_extra(Ind i, const Combo& c) {
     switch (i) {
-        case I_CWMA: return 1;
+        case I_CWMA: case I_VPWMA: return 1;
         case I_SRWMA: case I_SQWMA: return 3;
         case I_EPMA: return (int)c.a + 3;
         default: return 0;
@@ -217,6 +219,7 @@ static int wwma_weight_kind(Ind i) {
         case I_SRWMA: return WT_SRWMA;
         case I_SQWMA: return WT_SQWMA;
         case I_EPMA: return WT_EPMA;
+        case I_VPWMA: return WT_VPWMA;
         default: return WT_ALMA;
     }
 }
@@ -249,6 +252,10 @@ static vta_status validate_combo(Ind ind, const Combo& c, size_t len) {
             break;
         case I_WMA: case I_CWMA: case I_SRWMA: case I_SQWMA:
             if (c.period < 2) return bad("period must be >= 2");
+            break;
+        case I_VPWMA:
+            if (c.period < 2) return bad("period must be >= 2");
+            if (!std::isfinite(c.a)) return bad("power must be finite");
             break;
         case I_EPMA:
             if (c.period < 2) return bad("period must be >= 2");
@@ -1102,6 +1109,7 @@ static std::vector<Combo> grid_of(Ind ind, const vta_supertrend_batch_range* r) 
 static std::vector<Combo> grid_of(Ind ind, const vta_percentile_batch_range* r) { return grid_p1(ind, r->length, r->percentage); }
 // EpmaBatchRange: period outer, offset inner, both axes ascending after a swap
 // (epma.rs:835-859)
+static std::vector<Combo> grid_of(Ind ind, const vta_vpwma_batch_range* r) { return grid_p1(ind, r->period, r->power); }
 static std::vector<Combo> grid_of(Ind, const vta_epma_batch_range* r) {
     std::vector<Combo> cs;
     for (size_t p : axis_usize(r->period, AX_SWAP))
@@ -1117,6 +1125,7 @@ static Combo combo_of(const vta_bollinger_params* p) { return {p->period, p->dev
 static Combo combo_of(const vta_supertrend_params* p) { return {p->period, p->factor, 0.0}; }
 static Combo combo_of(const vta_percentile_params* p) { return {p->length, p->percentage, 0.0}; }
 static Combo combo_of(const vta_epma_params* p) { return {p->period, (double)p->offset, 0.0}; }
+static Combo combo_of(const vta_vpwma_params* p) { return {p->period, p->power, 0.0}; }
 
 static void params_of(const Combo& c, vta_alma_params* p) { *p = {c.period, c.a, c.b}; }
 static void params_of(const Combo& c, vta_period_params* p) { *p = {c.period}; }
@@ -1126,6 +1135,7 @@ static void params_of(const Combo& c, vta_bollinger_params* p) { *p = {c.period,
 static void params_of(const Combo& c, vta_supertrend_params* p) { *p = {c.period, c.a}; }
 static void params_of(const Combo& c, vta_percentile_params* p) { *p = {c.period, c.a}; }
 static void params_of(const Combo& c, vta_epma_params* p) { *p = {c.period, (size_t)c.a}; }
+static void params_of(const Combo& c, vta_vpwma_params* p) { *p = {c.period, c.a}; }
 
 template <class R, class P>
 static vta_status expand(Ind ind, const R* r, P* out, size_t cap, size_t* n) {
@@ -1153,7 +1163,7 @@ static int ma_ind(const char* name) {
         {"sma", I_SMA},     {"ema", I_EMA},       {"wma", I_WMA},     {"alma", I_ALMA},   {"dema", I_DEMA},
         {"tema", I_TEMA},   {"swma", I_SWMA},     {"trima", I_TRIMA}, {"sinwma", I_SINWMA}, {"epma", I_EPMA},
         {"wilders", I_WILDERS}, {"cwma", I_CWMA}, {"fwma", I_FWMA},   {"pwma", I_PWMA},   {"srwma", I_SRWMA},
-        {"sqwma", I_SQWMA},
+        {"sqwma", I_SQWMA}, {"vpwma", I_VPWMA},
     };
     for (const auto& m : kMa)
         if (s == m.n) return m.i;
@@ -1161,7 +1171,7 @@ static int ma_ind(const char* name) {
     // vram_ma.rs:68-76) whose kernels are not part of this library
     static const char* kOther[] = {"jsa", "smma", "highpass", "maaq", "mwdx", "supersmoother",
                                    "supersmoother_3_pole", "zlema", "nma", "hma", "jma", "edcf",
-                                   "ehlers_itrend", "cora_wave", "vwma", "vpwma", "frama"};
+                                   "ehlers_itrend", "cora_wave", "vwma", "frama"};
     for (const char* o : kOther)
         if (s == o) return -2;
     return -1;
@@ -1188,6 +1198,7 @@ static vta_status ma_periods_device(vta_ctx* ctx, const char* ma_type, const cha
     if (len > (size_t)INT32_MAX) return fail(VTA_ERR_INVALID_INPUT, "series longer than 2^31-1");
     const double offset = ma_param(keys, vals, n_params, "offset", ind == I_ALMA ? 0.85 : 0.0);
     const double sigma = ma_param(keys, vals, n_params, "sigma", 6.0);
+    const double power = ma_param(keys, vals, n_params, "power", 0.382);
     std::vector<Combo> cs;
     cs.reserve(n_periods);
     for (size_t i = 0; i < n_periods; ++i) {
@@ -1195,6 +1206,7 @@ static vta_status ma_periods_device(vta_ctx* ctx, const char* ma_type, const cha
         const size_t p = (size_t)periods[i];
         if (ind == I_ALMA) cs.push_back({p, offset, sigma});
         else if (ind == I_EPMA) cs.push_back({p, std::max(0.0, std::round(offset)), 0.0});
+        else if (ind == I_VPWMA) cs.push_back({p, power, 0.0});
         else cs.push_back({p, 0.0, 0.0});
     }
     VTA_TRY(validate_combos(ind, cs, len, first_valid));
@@ -1260,6 +1272,7 @@ static vta_status ma_select(vta_ctx* ctx, const char* ma_type, const char* const
     if (len == 0) return fail(VTA_ERR_INVALID_INPUT, "ma selector: empty price input");
     const double offset = ma_param(keys, vals, n_params, "offset", ind == I_ALMA ? 0.85 : 0.0);
     const double sigma = ma_param(keys, vals, n_params, "sigma", 6.0);
+    const double power = ma_param(keys, vals, n_params, "power", 0.382);
     std::vector<Combo> cs;
     for (size_t p : selector_periods(start, end, step)) {
         if (p == 0 || p > len) {
@@ -1269,6 +1282,7 @@ static vta_status ma_select(vta_ctx* ctx, const char* ma_type, const char* const
         }
         if (ind == I_ALMA) cs.push_back({p, offset, sigma});
         else if (ind == I_EPMA) cs.push_back({p, std::max(0.0, std::round(offset)), 0.0});
+        else if (ind == I_VPWMA) cs.push_back({p, power, 0.0});
         else cs.push_back({p, 0.0, 0.0});
     }
     const float* in[1] = {prices};
@@ -1304,6 +1318,7 @@ static std::vector<Combo> grid_generic(Ind ind, const vta_sweep* sw) {
         case I_BB: { const vta_bollinger_batch_range r{sw->period, sw->p1, sw->p2}; return grid_of(ind, &r); }
         case I_SUPERTREND: { const vta_supertrend_batch_range r{sw->period, sw->p1}; return grid_of(ind, &r); }
         case I_PNR: { const vta_percentile_batch_range r{sw->period, sw->p1}; return grid_of(ind, &r); }
+        case I_VPWMA: { const vta_vpwma_batch_range r{sw->period, sw->p1}; return grid_of(ind, &r); }
         case I_EPMA: {  // offsets from p1 (rounded to integers)
             const vta_range_usize o{(size_t)std::llround(sw->p1.start), (size_t)std::llround(sw->p1.end),
                                     (size_t)std::llround(sw->p1.step)};

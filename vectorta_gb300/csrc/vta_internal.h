@@ -150,7 +150,7 @@ size_t prefix_tmp_doubles(int n);
 vta_status launch_transpose(const float* in, int rows, int cols, float* out, cudaStream_t st);
 
 // --- weighted-window moving averages (ALMA/WMA/SWMA/PWMA/SINWMA/TRIMA,
-// CWMA/FWMA/SRWMA/SQWMA/EPMA) ----------------------------------------------
+// CWMA/FWMA/SRWMA/SQWMA/EPMA/VPWMA) ----------------------------------------
 // Row weights are right-aligned into a [n_combos][kmax] f32 matrix.  A row's
 // "period" here is its window length L; its first output is at
 // first + L - 1 + warm_extra (the crate's warm-up of each indicator).
@@ -171,7 +171,7 @@ struct WwmaBatchArgs {
 };
 enum WeightKind {
     WT_ALMA = 0, WT_WMA = 1, WT_SWMA = 2, WT_PWMA = 3, WT_SINWMA = 4, WT_TRIMA = 5,
-    WT_CWMA = 6, WT_FWMA = 7, WT_SRWMA = 8, WT_SQWMA = 9, WT_EPMA = 10
+    WT_CWMA = 6, WT_FWMA = 7, WT_SRWMA = 8, WT_SQWMA = 9, WT_EPMA = 10, WT_VPWMA = 11
 };
 vta_status launch_weights(int kind, const int* periods, const double* pa, const double* pb, int n_combos,
                           int kmax, float* w, cudaStream_t st);

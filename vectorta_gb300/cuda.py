@@ -124,6 +124,18 @@ class PercentileNearestRankParams:
 
 
 @dataclass
+class VpwmaBatchRange:
+    period: tuple = (14, 263, 1)      # vpwma.rs:892-899
+    power: tuple = (0.382, 0.382, 0.0)
+
+
+@dataclass
+class VpwmaParams:
+    period: int = 14
+    power: float = 0.382
+
+
+@dataclass
 class EpmaParams:
     period: int = 11
     offset: int = 4
@@ -132,11 +144,11 @@ class EpmaParams:
 _RANGE_CLS = {"alma": AlmaBatchRange, "period": PeriodBatchRange, "stddev": StdDevBatchRange,
               "zscore": ZscoreBatchRange, "bollinger": BollingerBandsBatchRange,
               "supertrend": SuperTrendBatchRange, "percentile": PercentileNearestRankBatchRange,
-              "epma": EpmaBatchRange}
+              "epma": EpmaBatchRange, "vpwma": VpwmaBatchRange}
 _PARAM_CLS = {"alma": AlmaParams, "period": PeriodParams, "stddev": StdDevParams,
               "zscore": ZscoreParams, "bollinger": BollingerBandsParams,
               "supertrend": SuperTrendParams, "percentile": PercentileNearestRankParams,
-              "epma": EpmaParams}
+              "epma": EpmaParams, "vpwma": VpwmaParams}
 
 
 def _to_sweep(fam: str, sweep) -> Any:
@@ -560,12 +572,14 @@ _CLASS_NAMES = {
     "supertrend": "CudaSupertrend", "donchian": "CudaDonchian", "willr": "CudaWillr",
     "percentile_nearest_rank": "CudaPercentileNearestRank",
     "cwma": "CudaCwma", "fwma": "CudaFwma", "srwma": "CudaSrwma", "sqwma": "CudaSqwma", "epma": "CudaEpma",
+    "vpwma": "CudaVpwma",
 }
 CLASSES = {name: _make(name, cls) for name, cls in _CLASS_NAMES.items()}
 __all__ += ["AlmaBatchRange", "PeriodBatchRange", "StdDevBatchRange", "ZscoreBatchRange",
             "BollingerBandsBatchRange", "SuperTrendBatchRange", "PercentileNearestRankBatchRange",
             "AlmaParams", "PeriodParams", "StdDevParams", "ZscoreParams", "BollingerBandsParams",
-            "SuperTrendParams", "PercentileNearestRankParams", "EpmaBatchRange", "EpmaParams", "VramMaComputer",
+            "SuperTrendParams", "PercentileNearestRankParams", "EpmaBatchRange", "EpmaParams", "VpwmaBatchRange",
+            "VpwmaParams", "VramMaComputer",
             "CudaMaSelector", "StreamBank",
             "CLASSES",
             "device_count", "launch_count"]
