@@ -85,20 +85,22 @@ def workload_alma_grid():
 
 def workload_wwma_family():
     """The remaining weighted-window moving averages on the tensor-core
-    contraction: CWMA, FWMA, SRWMA, SQWMA periods 5..260 (256 combos each) and
-    EPMA periods 16..260 x offset 4 (245 combos) on 1,000,000 bars (seed 6, 100
-    leading NaN): 1.27e9 outputs = 5.1 GB per step."""
+    contraction: CWMA, FWMA, SRWMA, SQWMA, VPWMA (power 0.382) periods 5..260
+    (256 combos each) and EPMA periods 16..260 x offset 4 (245 combos) on
+    1,000,000 bars (seed 6, 100 leading NaN): 1.525e9 outputs = 6.1 GB per
+    step."""
     from vectorta_gb300 import datagen
 
     n = 1_000_000
     close = datagen.random_walk(n, seed=6, nan_lead=100)
     per = {"period": (5, 260, 1)}
     jobs = [("cwma", ["close"], per), ("fwma", ["close"], per), ("srwma", ["close"], per),
-            ("sqwma", ["close"], per), ("epma", ["close"], {"period": (16, 260, 1), "offset": (4, 4, 0)})]
+            ("sqwma", ["close"], per), ("vpwma", ["close"], {"period": (5, 260, 1), "power": (0.382, 0.382, 0.0)}),
+            ("epma", ["close"], {"period": (16, 260, 1), "offset": (4, 4, 0)})]
     return {"name": "wwma_family", "n": n, "series": {"close": close.astype(np.float32)}, "jobs": jobs,
             "dominant": "cwma",
             "config": {"workload": "wwma_family", "bars": n, "seed": 6, "nan_lead": 100,
-                       "sweeps": "CWMA/FWMA/SRWMA/SQWMA periods 5..260; EPMA periods 16..260 x offset 4"}}
+                       "sweeps": "CWMA/FWMA/SRWMA/SQWMA/VPWMA periods 5..260; EPMA periods 16..260 x offset 4"}}
 
 
 def workload_ema_small():
@@ -310,9 +312,10 @@ def cpu_sample(wl, budget_rows=None):
                 tasks.append((lambda p=p: O.alma_batch(s["close"], (p, p, 0), sweep["offset"], sweep["sigma"]),
                               wl["n"] * len(O.axis_f64(sweep["offset"])) * len(O.axis_f64(sweep["sigma"]))))
             continue
-        if name in ("cwma", "fwma", "srwma", "sqwma", "epma"):
+        if name in ("cwma", "fwma", "srwma", "sqwma", "epma", "vpwma"):
             fn = getattr(O, name)
-            offs = O.axis_usize(sweep["offset"], O.AX_SWAP) if name == "epma" else [None]
+            offs = (O.axis_usize(sweep["offset"], O.AX_SWAP) if name == "epma" else
+                    O.axis_f64(sweep["power"]) if name == "vpwma" else [None])
             for p in O.periods_of(name, sweep["period"])[::16]:
                 for o in offs:
                     args_ = (p,) if o is None else (p, o)
