@@ -847,10 +847,10 @@ def e2e_bench(args, wl, inds, rows, out_per_step):
 # output count to the full workloads (x5 and x10): these kernels' traffic is
 # linear in the outputs they write.
 TRAFFIC = {
-    "recurrence_window_sweeps": (5.709056e6 + 738.209024e6) * 5,
-    "ema_small": 5.709056e6 + 738.209024e6,
-    "alma_grid": (15.215616e6 + 1382.070e6) * 10,
-    "alma_small": 15.215616e6 + 1382.070e6,
+    "recurrence_window_sweeps": (5.870592e6 + 737.837568e6) * 5,
+    "ema_small": 5.870592e6 + 737.837568e6,
+    "alma_grid": (24.602112e6 + 1374.316e6) * 10,
+    "alma_small": 24.602112e6 + 1374.316e6,
 }
 KERNEL_NAME = {"recurrence_window_sweeps": "k_recur<OpEma, batch, EMIT>", "alma_grid": "k_wwma_tc<fp16x3>",
                "ema_small": "k_recur<OpEma, batch, EMIT>", "alma_small": "k_wwma_tc<fp16x3>",
