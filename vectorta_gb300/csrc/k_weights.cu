@@ -11,9 +11,9 @@
 //   SINWMA w_k = sin((k+1) pi / (p+1)) / sum             (sinwma.rs:271-289)
 //   TRIMA  box(m1) * box(m2), m1 = (p+1)/2, m2 = p - m1 + 1 (trima.rs:277-364)
 //
-// Arithmetic: GB300's FP64 rate is a small fraction of its FP32 rate, so only
-// the per-combo constants (ALMA's centre m and 1/(2 s^2), the row sum's
-// reciprocal) are formed in f64, once per block.  Each weight is evaluated in
+// Arithmetic: GB300's FP64 rate is a small fraction of its FP32 rate, so the
+// per-combo constants (ALMA's centre m and 1/(2 s^2)) come in f64 from the
+// host and the rest is FP32.  Each weight is evaluated in
 // double-single FP32 (error-free products through FMA): the ALMA exponent
 // e = (i - m)^2 / (2 s^2) is carried as e_hi + e_lo and exponentiated as
 // expf(-e_hi) * (1 - e_lo), and the row sum is accumulated as a double-single
@@ -146,11 +146,13 @@ __global__ void __launch_bounds__(kWThreads) k_weights(int kind, const int* peri
     } else if (kind == WT_VPWMA) {
         rc.pw = pa[c];
     } else if (kind == WT_ALMA) {
+        // pa = m = offset (p - 1) and pb = 1 / (2 s^2) = sigma^2 / (2 p^2),
+        // formed in f64 on the host (an f64 divide per combo on the device
+        // cost more than the whole weight row)
         float m_hi = 0.f, m_lo = 0.f, q_hi = 0.f, q_lo = 0.f;
         if (lane == 0) {
-            const double a = pa[c], b = pb[c];
-            const DS m = split(a * (double)(p - 1));
-            const DS q = split(b * b / (2.0 * (double)p * (double)p));
+            const DS m = split(pa[c]);
+            const DS q = split(pb[c]);
             m_hi = m.hi; m_lo = m.lo; q_hi = q.hi; q_lo = q.lo;
         }
         rc.m = DS{__shfl_sync(0xffffffffu, m_hi, 0), __shfl_sync(0xffffffffu, m_lo, 0)};
@@ -163,13 +165,11 @@ __global__ void __launch_bounds__(kWThreads) k_weights(int kind, const int* peri
         const DS t{__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)};
         s = ds_add(s, t);
     }
-    float i_hi = 0.f, i_lo = 0.f;
-    if (lane == 0) {
-        const DS inv = split(1.0 / ((double)s.hi + (double)s.lo));
-        i_hi = inv.hi;
-        i_lo = inv.lo;
-    }
-    const DS inv{__shfl_sync(0xffffffffu, i_hi, 0), __shfl_sync(0xffffffffu, i_lo, 0)};
+    // 1 / sum in double-single: r0 = 1 / hi, one Newton step on the residual
+    // 1 - sum r0 (formed exactly with FMA), so inv = r0 + r0 e to ~1e-14
+    const float r0 = 1.f / s.hi;
+    const float e = fmaf(-s.lo, r0, fmaf(-s.hi, r0, 1.f));
+    const DS inv = quick_two_sum(r0, r0 * e);
     float* row = w + (size_t)c * kmax;
     const int lead = kmax - p;
     for (int k = lane; k < kmax; k += 32) {

@@ -431,6 +431,12 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
         double* d_nanp = ar.take<double>(len);
         double* d_tmp = ar.take<double>(prefix_tmp_doubles(n));
         int* d_wx = ar.take<int>(nc);
+        if (ind == I_ALMA)  // the weight kernel takes m = offset (p - 1) and 1 / (2 s^2) = sigma^2 / (2 p^2)
+            for (int i = 0; i < nc; ++i) {
+                const double pd = (double)periods[i];
+                pa[i] = pa[i] * (pd - 1.0);
+                pb[i] = pb[i] * pb[i] / (2.0 * pd * pd);
+            }
         std::vector<int> tk(ntile, 0);
         for (int i = 0; i < nc; ++i) tk[i / 16] = std::max(tk[i / 16], periods[i]);
         VTA_TRY(upload(ctx, d_per, periods.data(), nc * sizeof(int)));
@@ -786,7 +792,11 @@ static vta_status run_tm(vta_ctx* ctx, Ind ind, const DevIn& in, size_t cols, si
     else VTA_TRY(launch_first_valid_tm_hlc(in.p[0], in.p[1], in.p[2], C, R, d_first, st));
 
     if (is_wwma(ind)) {
-        const double ab[2] = {c.a, c.b};
+        double ab[2] = {c.a, c.b};
+        if (ind == I_ALMA) {  // m and 1 / (2 s^2), as in the batch path
+            ab[0] = c.a * ((double)pw - 1.0);
+            ab[1] = c.b * c.b / (2.0 * (double)pw * (double)pw);
+        }
         VTA_TRY(upload(ctx, d_p1, &pw, sizeof(int)));
         VTA_TRY(upload(ctx, d_ab, ab, sizeof ab));
         VTA_TRY(launch_weights(wwma_weight_kind(ind), d_p1, d_ab, d_ab + 1, 1, pw, d_w, st));
