@@ -663,6 +663,54 @@ __device__ bool agg_fast_block(const RecurArgs& a, int chunk, int c0, int c1, fl
     return true;
 }
 
+// One step of the general (per-step phase) path of one lane: warm-up
+// accumulation until the seed index, the seed, then running steps.
+template <class Op, class In>
+__device__ __forceinline__ float general_step(Op& op, bool active, bool seeded_ever, bool& running, int& steps,
+                                              const In& in, int t) {
+    float v = qnan();
+    if constexpr (HasUni<Op>::value) {
+        if (active && t >= op.f) v = op.uni(in, t, steps);
+        return v;
+    }
+    if (active && t >= op.f && seeded_ever) {
+        if (running) {
+            steps += op.step(in, t);
+            v = op.value(in, t);
+        } else if (t <= op.s) {
+            op.accum(in, t);
+            if (t == op.s) {
+                op.seed();
+                running = true;
+                v = op.value(in, t);
+            } else {
+                v = op.warm_value(t);
+            }
+        }
+    } else if (active && t >= op.f && !seeded_ever) {
+        op.accum(in, t);  // never seeded (s >= n): warm-up style outputs only
+        v = op.warm_value(t);
+    }
+    return v;
+}
+
+// AGG record of one (lane, chunk): state, and applied steps or a marker for
+// a chunk before the seed / holding the seed.
+template <class Op>
+__device__ __forceinline__ void write_agg(const RecurArgs& a, const Op& op, bool active, bool seeded_ever, int steps,
+                                          int chunk, int c0, int c1, int li) {
+    float4 g;
+    const bool abs_chunk = active && seeded_ever && c0 <= op.s && op.s < c1;
+    const bool before = !active || !seeded_ever || c1 <= op.s;
+    g.x = Op::NS > 0 ? op.get(0) : 0.f;
+    g.y = Op::NS > 1 ? op.get(1) : 0.f;
+    g.z = Op::NS > 2 ? op.get(2) : 0.f;
+    g.w = before ? kBeforeSeed : (abs_chunk ? kAbsolute : (float)steps);
+    if (before) g.x = g.y = g.z = 0.f;
+    reinterpret_cast<float4*>(a.agg)[(size_t)chunk * a.n_lanes + li] = g;
+}
+
+
 template <class Op, bool TM, int PASS>
 __global__ void __launch_bounds__(kWarps * 32)
 k_recur(RecurArgs a) {
@@ -681,6 +729,34 @@ k_recur(RecurArgs a) {
             agg_fast_block<FastKindOf<Op>::k>(a, chunk, c0, c1, &stage[0][0][0]))
             return;
         __syncthreads();  // the general pass below reuses `stage`
+        // the seed chunk: each thread replays its combo's warm-up and seed
+        // from the chunk's inputs staged in shared memory (no per-step
+        // shuffles or warp-wide tiles: the lanes run independently)
+        if (a.fast_agg && chunk == 0 && c1 <= (int)(sizeof(stage) / sizeof(float))) {
+            float* xs = &stage[0][0][0];
+            for (int i = threadIdx.x; i < c1; i += blockDim.x) xs[i] = __ldg(a.x + i);
+            __syncthreads();
+            const int l0 = blockIdx.x * blockDim.x + threadIdx.x;
+            if (l0 < a.n_lanes) {
+                const int p0 = a.periods[l0];
+                Op op0;
+                op0.init(p0 > 0 ? p0 : 1, a.first);
+                const bool act0 = a.first < a.n && p0 > 0;
+                const bool seeded0 = act0 && op0.s < a.n;
+                bool run0 = false;
+                int st0 = 0;
+                for (int t = min(a.first, c1); t < c1; ++t) {
+                    InStep st;  // x[t] and x[t - 1] from shared memory
+                    st.t = t;
+                    st.x0 = xs[t];
+                    st.x1 = t > 0 ? xs[t - 1] : 0.f;
+                    st.h0 = st.l0 = 0.f;
+                    general_step(op0, act0, seeded0, run0, st0, st, t);
+                }
+                write_agg(a, op0, act0, seeded0, st0, 0, 0, c1, l0);
+            }
+            return;
+        }
     }
     // a warp with no valid lane has nothing to compute (whole warp leaves; the
     // kernel has no block-wide barrier)
@@ -779,30 +855,7 @@ k_recur(RecurArgs a) {
         } else {
             // ---- general path: per-step phase logic
             auto gen_step = [&](const auto& in_, int t) -> float {
-                float v = qnan();
-                if constexpr (HasUni<Op>::value) {
-                    if (active && t >= op.f) v = op.uni(in_, t, steps);
-                    return v;
-                }
-                if (active && t >= op.f && seeded_ever) {
-                    if (running) {
-                        steps += op.step(in_, t);
-                        v = op.value(in_, t);
-                    } else if (t <= op.s) {
-                        op.accum(in_, t);
-                        if (t == op.s) {
-                            op.seed();
-                            running = true;
-                            v = op.value(in_, t);
-                        } else {
-                            v = op.warm_value(t);
-                        }
-                    }
-                } else if (active && t >= op.f && !seeded_ever) {
-                    op.accum(in_, t);  // never seeded (s >= n): warm-up style outputs only
-                    v = op.warm_value(t);
-                }
-                return v;
+                return general_step(op, active, seeded_ever, running, steps, in_, t);
             };
             if constexpr (!TM) {
                 // the tile's inputs in registers (one coalesced load per lane);
@@ -854,17 +907,7 @@ k_recur(RecurArgs a) {
             __syncwarp();
         }
     }
-    if (PASS == PASS_AGG && valid) {
-        float4 g;
-        const bool abs_chunk = active && seeded_ever && c0 <= op.s && op.s < c1;
-        const bool before = !active || !seeded_ever || c1 <= op.s;
-        g.x = Op::NS > 0 ? op.get(0) : 0.f;
-        g.y = Op::NS > 1 ? op.get(1) : 0.f;
-        g.z = Op::NS > 2 ? op.get(2) : 0.f;
-        g.w = before ? kBeforeSeed : (abs_chunk ? kAbsolute : (float)steps);
-        if (before) g.x = g.y = g.z = 0.f;
-        reinterpret_cast<float4*>(a.agg)[(size_t)chunk * a.n_lanes + li] = g;
-    }
+    if (PASS == PASS_AGG && valid) write_agg(a, op, active, seeded_ever, steps, chunk, c0, c1, li);
 }
 
 // Carry-in of every chunk: an exclusive scan, over the chunks of one lane, of
