@@ -104,6 +104,18 @@ def lib():
             "vto_rsi_stream": ([dp, sz, sz, dp], ip),
             "vto_atr_stream": ([dp, dp, dp, sz, sz, dp], ip),
             "vto_wilders_stream": ([dp, sz, sz, dp], ip),
+            "vto_dema_stream": ([dp, sz, sz, dp], ip),
+            "vto_tema_stream": ([dp, sz, sz, dp], ip),
+            "vto_wma_stream": ([dp, sz, sz, dp], ip),
+            "vto_swma_stream": ([dp, sz, sz, dp], ip),
+            "vto_pwma_stream": ([dp, sz, sz, dp], ip),
+            "vto_stddev_stream": ([dp, sz, sz, db, dp], ip),
+            "vto_zscore_stream": ([dp, sz, sz, db, dp], ip),
+            "vto_bollinger_stream": ([dp, sz, sz, db, db, ip, dp, dp, dp], ip),
+            "vto_donchian_stream": ([dp, dp, sz, sz, dp, dp, dp], ip),
+            "vto_willr_stream": ([dp, dp, dp, sz, sz, dp], ip),
+            "vto_adx_stream": ([dp, dp, dp, sz, sz, dp], ip),
+            "vto_supertrend_stream": ([dp, dp, dp, sz, sz, db, dp, dp], ip),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -239,22 +251,63 @@ def epma(x, period=11, offset=4):
     return _single("vto_epma", x, period, offset)
 
 
+# The crate's XStream parameter defaults (XParams::default / try_new) and
+# each stream's inputs and outputs.
+STREAMS = {
+    "ema": (1, 1, {"period": 9}),
+    "sma": (1, 1, {"period": 9}),
+    "alma": (1, 1, {"period": 9, "offset": 0.85, "sigma": 6.0}),
+    "rsi": (1, 1, {"period": 14}),
+    "atr": (3, 1, {"length": 14}),
+    "wilders": (1, 1, {"period": 5}),
+    "dema": (1, 1, {"period": 30}),
+    "tema": (1, 1, {"period": 9}),
+    "wma": (1, 1, {"period": 30}),
+    "swma": (1, 1, {"period": 5}),
+    "pwma": (1, 1, {"period": 5}),
+    "stddev": (1, 1, {"period": 5, "nbdev": 1.0}),
+    "zscore": (1, 1, {"period": 14, "nbdev": 1.0}),
+    "bollinger_bands": (1, 3, {"period": 20, "devup": 2.0, "devdn": 2.0, "matype": "sma"}),
+    "donchian": (2, 3, {"period": 20}),
+    "willr": (3, 1, {"period": 14}),
+    "adx": (3, 1, {"period": 14}),
+    "supertrend": (3, 2, {"period": 10, "factor": 3.0}),
+}
+
+
 def stream(name, inputs, **prm):
     """The crate's XStream for `name` fed the inputs bar by bar (NaN where
-    update() returns None)."""
+    update() returns None).  One output: an array; several (Bollinger,
+    Donchian: upper / middle / lower; SuperTrend: trend / changed): a tuple."""
     xs = [_f64(a) for a in inputs]
-    out = np.empty_like(xs[0])
+    n_in, n_out, dflt = STREAMS[name]
+    assert len(xs) == n_in, (name, len(xs))
+    q = dict(dflt)
+    q.update(prm)
+    outs = [np.empty_like(xs[0]) for _ in range(n_out)]
+    n = xs[0].size
     L = lib()
-    p = int(prm.get("period", prm.get("length", 14 if name in ("rsi", "atr") else 5 if name == "wilders" else 9)))
+    P = [_p(a) for a in xs]
+    O_ = [_p(o) for o in outs]
     if name == "alma":
-        code = L.vto_alma_stream(_p(xs[0]), xs[0].size, p, float(prm.get("offset", 0.85)),
-                                 float(prm.get("sigma", 6.0)), _p(out))
+        code = L.vto_alma_stream(P[0], n, int(q["period"]), float(q["offset"]), float(q["sigma"]), O_[0])
     elif name == "atr":
-        code = L.vto_atr_stream(_p(xs[0]), _p(xs[1]), _p(xs[2]), xs[0].size, p, _p(out))
+        code = L.vto_atr_stream(*P, n, int(q["length"]), O_[0])
+    elif name in ("stddev", "zscore"):
+        code = getattr(L, f"vto_{name}_stream")(P[0], n, int(q["period"]), float(q["nbdev"]), O_[0])
+    elif name == "bollinger_bands":
+        mt = {"sma": 0, "ema": 1}[str(q["matype"]).lower()]
+        code = L.vto_bollinger_stream(P[0], n, int(q["period"]), float(q["devup"]), float(q["devdn"]), mt, *O_)
+    elif name == "donchian":
+        code = L.vto_donchian_stream(*P, n, int(q["period"]), *O_)
+    elif name == "supertrend":
+        code = L.vto_supertrend_stream(*P, n, int(q["period"]), float(q["factor"]), *O_)
+    elif n_in == 3:
+        code = getattr(L, f"vto_{name}_stream")(*P, n, int(q["period"]), O_[0])
     else:
-        code = getattr(L, f"vto_{name}_stream")(_p(xs[0]), xs[0].size, p, _p(out))
+        code = getattr(L, f"vto_{name}_stream")(P[0], n, int(q["period"]), O_[0])
     _check(code, f"{name} stream")
-    return out
+    return outs[0] if n_out == 1 else tuple(outs)
 
 
 def trima(x, period=30):

@@ -1715,6 +1715,446 @@ int vto_wilders_stream(const double *x, size_t n, size_t period, double *out) {
     return VTO_OK;
 }
 
+/* DemaStream (dema.rs:615-690): the first value seeds both EMAs (output if
+ * period 1); then ema = fmadd(ema, 1 - a, x a), ema2 = fmadd(ema2, 1 - a,
+ * ema a), y = fmadd(ema, 2, -ema2), output once more than period - 1 values
+ * were seen.  fmadd is mul_add on x86 targets (separate operations elsewhere);
+ * this follows x86. */
+int vto_dema_stream(const double *x, size_t n, size_t period, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    const double a = 2.0 / ((double)period + 1.0), a1 = 1.0 - 2.0 / ((double)period + 1.0);
+    double e1 = QNAN, e2 = QNAN;
+    size_t filled = 0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        if (filled == 0) {
+            e1 = e2 = v;
+            filled = 1;
+            out[t] = period == 1 ? v : QNAN;
+            continue;
+        }
+        e1 = fma(e1, a1, v * a);
+        e2 = fma(e2, a1, e1 * a);
+        double y = fma(e1, 2.0, -e2);
+        filled++;
+        out[t] = filled > period - 1 ? y : QNAN;
+    }
+    return VTO_OK;
+}
+
+/* TemaStream (tema.rs:324-425): NaN before the first value is skipped; the
+ * first value seeds ema1; ema2 starts at count == period (copy of ema1),
+ * ema3 at count == 2 period - 1; output once count > 3 (period - 1); all
+ * updates e = e (1 - a) + v a without FMA; y = 3 e1 - 3 e2 + e3. */
+int vto_tema_stream(const double *x, size_t n, size_t period, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    const double a = 2.0 / ((double)period + 1.0), om = 1.0 - a;
+    const size_t start2 = period, start3 = 2 * period - 1, lookback = 3 * (period - 1);
+    double e1 = QNAN, e2 = 0.0, e3 = 0.0;
+    size_t count = 0;
+    int ready = 0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        if (ready) {
+            e1 = e1 * om + v * a;
+            e2 = e2 * om + e1 * a;
+            e3 = e3 * om + e2 * a;
+            out[t] = 3.0 * e1 - 3.0 * e2 + e3;
+            continue;
+        }
+        if (count == 0) {
+            out[t] = QNAN;
+            if (isnan(v)) continue;
+            e1 = v;
+            count = 1;
+            if (period == 1) { e2 = e1; e3 = e2; ready = 1; out[t] = e1; }
+            continue;
+        }
+        e1 = e1 * om + v * a;
+        count++;
+        if (count == start2) e2 = e1;
+        else if (count > start2) e2 = e2 * om + e1 * a;
+        if (count == start3) e3 = e2;
+        else if (count > start3) e3 = e3 * om + e2 * a;
+        if (count > lookback) { ready = 1; out[t] = 3.0 * e1 - 3.0 * e2 + e3; }
+        else out[t] = QNAN;
+    }
+    return VTO_OK;
+}
+
+/* WmaStream (wma.rs:384-460): ring of `period` values; when it first fills,
+ * weighted and plain sums are formed oldest first (weights 1..p) and the
+ * output is wsum / (p (p + 1) / 2); then the sums are updated in O(1):
+ * wsum += p v, ssum += v, out, wsum -= ssum, ssum -= oldest. */
+int vto_wma_stream(const double *x, size_t n, size_t period, double *out) {
+    if (period < 2) return VTO_E_INVALID_PERIOD;
+    double *buf = (double *)malloc(sizeof(double) * period);
+    for (size_t i = 0; i < period; i++) buf[i] = QNAN;
+    const double inv_div = 1.0 / ((double)(period * (period + 1)) * 0.5), pf = (double)period;
+    size_t head = 0;
+    int filled = 0;
+    double plain = 0.0, wsum = 0.0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        buf[head] = v;
+        head = head + 1 == period ? 0 : head + 1;
+        if (!filled) {
+            if (head != 0) { out[t] = QNAN; continue; }
+            double ws = 0.0, ss = 0.0;
+            size_t idx = head;
+            for (size_t w = 1; w <= period; w++) {
+                double b = buf[idx];
+                ss += b;
+                ws += (double)w * b;
+                idx = idx + 1 == period ? 0 : idx + 1;
+            }
+            out[t] = ws * inv_div;
+            wsum = ws - ss;
+            plain = ss - buf[head];
+            filled = 1;
+            continue;
+        }
+        double oldest = buf[head];
+        wsum += pf * v;
+        plain += v;
+        out[t] = wsum * inv_div;
+        wsum -= plain;
+        plain -= oldest;
+    }
+    free(buf);
+    return VTO_OK;
+}
+
+/* SwmaStream (swma.rs:536-630): the triangle as two box sums, a = b = (p+1)/2
+ * for odd p, a = p/2, b = a + 1 for even p: s1 = sum of the last a values,
+ * s2 = sum of the last b values of s1, output s2 / (a b). */
+int vto_swma_stream(const double *x, size_t n, size_t period, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    size_t a, b;
+    if (period & 1) { a = b = (period + 1) >> 1; }
+    else { a = period >> 1; b = a + 1; }
+    double *ra = (double *)calloc(a, sizeof(double)), *rb = (double *)calloc(b, sizeof(double));
+    const double inv_ab = 1.0 / ((double)a * (double)b);
+    size_t ia = 0, ca = 0, ib = 0, cb = 0;
+    double s1 = 0.0, s2 = 0.0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        out[t] = QNAN;
+        double old_a = ra[ia];
+        if (ca == a) s1 -= old_a; else ca++;
+        ra[ia] = v;
+        s1 += v;
+        ia = ia + 1 == a ? 0 : ia + 1;
+        if (ca == a) {
+            double old_b = rb[ib];
+            if (cb == b) s2 -= old_b; else cb++;
+            rb[ib] = s1;
+            s2 += s1;
+            ib = ib + 1 == b ? 0 : ib + 1;
+            if (cb == b) out[t] = s2 * inv_ab;
+        }
+    }
+    free(ra);
+    free(rb);
+    return VTO_OK;
+}
+
+/* PwmaStream (pwma.rs:675-720): Pascal weights as a cascade of p - 1 running
+ * pairwise sums (prev starts NaN), output times 2^-(p-1) once p values were
+ * seen; period 1 returns the value. */
+int vto_pwma_stream(const double *x, size_t n, size_t period, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    const size_t m = period - 1;
+    double *prev = (double *)malloc(sizeof(double) * (m ? m : 1));
+    for (size_t i = 0; i < m; i++) prev[i] = QNAN;
+    const double norm = ldexp(1.0, -(int)(m > 2000 ? 2000 : m));
+    size_t seen = 0;
+    for (size_t t = 0; t < n; t++) {
+        if (m == 0) { out[t] = x[t]; continue; }
+        double acc = x[t];
+        for (size_t k = 0; k < m; k++) {
+            double o = acc + prev[k];
+            prev[k] = acc;
+            acc = o;
+        }
+        if (seen < m) { seen++; out[t] = QNAN; continue; }
+        out[t] = acc * norm;
+    }
+    free(prev);
+    return VTO_OK;
+}
+
+/* StdDevStream (stddev.rs:451-570): ring with NaN count; sums skip NaN
+ * values; while the window holds a NaN the output is NaN; else
+ * var = sum_sq / p - mean^2, sqrt(var) * nbdev (0 if var <= 0). */
+int vto_stddev_stream(const double *x, size_t n, size_t period, double nbdev, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    if (!isfinite(nbdev) || nbdev < 0.0) return VTO_E_INVALID_PARAM;
+    double *buf = (double *)malloc(sizeof(double) * period);
+    for (size_t i = 0; i < period; i++) buf[i] = QNAN;
+    const double inv = 1.0 / (double)period;
+    size_t head = 0, nanc = 0;
+    int filled = 0;
+    double sum = 0.0, sq = 0.0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        if (!filled) {
+            if (isnan(v)) nanc++;
+            else { sum += v; sq += v * v; }
+            buf[head] = v;
+            if (head + 1 != period) { head++; out[t] = QNAN; continue; }
+            head = 0;
+            filled = 1;
+        } else {
+            double old = buf[head];
+            int on = isnan(old), nn = isnan(v);
+            if (!on && !nn) { sum += v - old; sq += (v * v) - (old * old); }
+            else if (!on && nn) { sum -= old; sq -= old * old; nanc++; }
+            else if (on && !nn) { if (nanc > 0) nanc--; sum += v; sq += v * v; }
+            else { if (nanc > 0) nanc--; nanc++; }
+            buf[head] = v;
+            head = head + 1 == period ? 0 : head + 1;
+        }
+        if (nanc > 0) { out[t] = QNAN; continue; }
+        double mean = sum * inv;
+        double var = (sq * inv) - (mean * mean);
+        out[t] = var <= 0.0 ? 0.0 : sqrt(var) * nbdev;
+    }
+    free(buf);
+    return VTO_OK;
+}
+
+/* ZscoreStream (zscore.rs:567-735) with ma_type "sma", devtype 0: NaN-zeroed
+ * running sums; once filled and with no NaN in the window and nbdev != 0,
+ * z = (last - mean) / (sqrt(max(ex2 - mean^2, 0)) nbdev), NaN when the
+ * deviation is 0 or not finite.  A window holding a NaN, or nbdev == 0, goes
+ * through the crate's slow path, whose result is NaN for this MA. */
+int vto_zscore_stream(const double *x, size_t n, size_t period, double nbdev, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    double *buf = (double *)malloc(sizeof(double) * period);
+    for (size_t i = 0; i < period; i++) buf[i] = QNAN;
+    const double inv = 1.0 / (double)period;
+    size_t head = 0, nanc = period;
+    int filled = 0;
+    double sum = 0.0, sum2 = 0.0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        double old = buf[head];
+        buf[head] = v;
+        head = (head + 1) % period;
+        if (!filled && head == 0) filled = 1;
+        if (isnan(old) && nanc > 0) nanc--;
+        if (isnan(v)) nanc++;
+        double oc = isnan(old) ? 0.0 : old, nc = isnan(v) ? 0.0 : v;
+        sum = sum + nc - oc;
+        sum2 = sum2 + nc * nc - oc * oc;
+        if (!filled) { out[t] = QNAN; continue; }
+        if (nbdev == 0.0 || nanc != 0) { out[t] = QNAN; continue; }
+        double mean = sum * inv, ex2 = sum2 * inv;
+        double var = ex2 - mean * mean;
+        if (var < 0.0) var = 0.0;
+        double sd = sqrt(var);
+        if (sd == 0.0 || !isfinite(sd)) { out[t] = QNAN; continue; }
+        double last = buf[head == 0 ? period - 1 : head - 1];
+        out[t] = (last - mean) / (sd * nbdev);
+    }
+    free(buf);
+    return VTO_OK;
+}
+
+/* BollingerBandsStream (bollinger_bands.rs:884-1075), devtype 0 with ma "sma"
+ * (ema = 0) or "ema" (ema = 1): a non-finite value resets the stream; the
+ * ring keeps sum and sum of squares (x mul_add x); sd = sqrt(max(sq/p -
+ * mean^2, 0)); the EMA middle is seeded with the window mean, then
+ * mul_add(a, x, (1 - a) ema); bands mul_add(+-dev, sd, middle). */
+int vto_bollinger_stream(const double *x, size_t n, size_t period, double devup, double devdn, int ema,
+                         double *up, double *mid, double *lo) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    double *buf = (double *)calloc(period, sizeof(double));
+    const double inv = 1.0 / (double)period, alpha = 2.0 / ((double)period + 1.0);
+    size_t idx = 0, len = 0;
+    double sum = 0.0, sq = 0.0, e = 0.0;
+    int seeded = 0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        up[t] = mid[t] = lo[t] = QNAN;
+        if (!isfinite(v)) { idx = len = 0; sum = sq = e = 0.0; seeded = 0; continue; }
+        if (len < period) {
+            buf[idx] = v;
+            idx = idx + 1 == period ? 0 : idx + 1;
+            len++;
+            sum += v;
+            sq = fma(v, v, sq);
+        } else {
+            double old = buf[idx];
+            buf[idx] = v;
+            idx = idx + 1 == period ? 0 : idx + 1;
+            sum += v - old;
+            double tmp = sq - old * old;
+            sq = fma(v, v, tmp);
+        }
+        if (len < period) continue;
+        double mean = sum * inv;
+        double var = (sq * inv) - mean * mean;
+        double sd = sqrt(var > 0.0 ? var : 0.0);
+        double m = mean;
+        if (ema) {
+            if (!seeded) { e = sum * inv; seeded = 1; }
+            else e = fma(alpha, v, (1.0 - alpha) * e);
+            m = e;
+        }
+        up[t] = fma(devup, sd, m);
+        mid[t] = m;
+        lo[t] = fma(-devdn, sd, m);
+    }
+    free(buf);
+    return VTO_OK;
+}
+
+/* DonchianStream (donchian.rs:1251-1340): once `period` bars were seen, NaN
+ * bands while any bar of the window has a non-finite high or low; else the
+ * window's highest high and lowest low (the monotone deques' fronts) and
+ * middle mul_add(max - min, 0.5, min). */
+int vto_donchian_stream(const double *h, const double *l, size_t n, size_t period, double *up, double *mid,
+                        double *lo) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    for (size_t t = 0; t < n; t++) {
+        up[t] = mid[t] = lo[t] = QNAN;
+        if (t + 1 < period) continue;
+        int ok = 1;
+        double mx = -INFINITY, mn = INFINITY;
+        for (size_t k = t + 1 - period; k <= t; k++) {
+            if (!isfinite(h[k]) || !isfinite(l[k])) { ok = 0; break; }
+            if (h[k] > mx) mx = h[k];
+            if (l[k] < mn) mn = l[k];
+        }
+        if (!ok) continue;
+        up[t] = mx;
+        lo[t] = mn;
+        mid[t] = fma(mx - mn, 0.5, mn);
+    }
+    return VTO_OK;
+}
+
+/* WillrStream (willr.rs:1657-1820): once `period` bars were seen, NaN when
+ * the close is NaN or any bar of the window has a NaN high or low, or the
+ * window extremes are not finite; else 0 for a flat window and
+ * mul_add(-100, (hh - close) / (hh - ll), 0). */
+int vto_willr_stream(const double *h, const double *l, const double *c, size_t n, size_t period, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    for (size_t t = 0; t < n; t++) {
+        out[t] = QNAN;
+        if (t + 1 < period) continue;
+        int ok = !isnan(c[t]);
+        double hh = -INFINITY, ll = INFINITY;
+        for (size_t k = t + 1 - period; ok && k <= t; k++) {
+            if (isnan(h[k]) || isnan(l[k])) { ok = 0; break; }
+            if (h[k] > hh) hh = h[k];
+            if (l[k] < ll) ll = l[k];
+        }
+        if (!ok || !(isfinite(hh) && isfinite(ll))) continue;
+        double den = hh - ll;
+        out[t] = den == 0.0 ? 0.0 : fma(-100.0, (hh - c[t]) / den, 0.0);
+    }
+    return VTO_OK;
+}
+
+/* AdxStream (adx.rs:1949-2085): TR = max(h, pc) - min(l, pc) (f64::max /
+ * min, NaN-ignoring), +DM / -DM; the first `period` moves are summed and give
+ * the first DX; then Wilder smoothing s (1 - 1/p) + m, DX from
+ * 100 / ATR; ADX = mean of the first `period` DX values, then
+ * (adx (p - 1) + dx) / p. */
+int vto_adx_stream(const double *h, const double *l, const double *c, size_t n, size_t period, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    double atr = 0.0, pdm_s = 0.0, mdm_s = 0.0, dx_sum = 0.0, last = 0.0, ph = QNAN, pl = QNAN, pc = QNAN;
+    size_t count = 0, dx_count = 0;
+    const double rp = 1.0 / (double)period, omr = 1.0 - rp, pm1 = (double)period - 1.0;
+    for (size_t t = 0; t < n; t++) {
+        out[t] = QNAN;
+        if (count == 0) { ph = h[t]; pl = l[t]; pc = c[t]; count = 1; continue; }
+        double tr = fmax(h[t], pc) - fmin(l[t], pc);
+        double upm = h[t] - ph, dnm = pl - l[t];
+        double pdm = (upm > dnm && upm > 0.0) ? upm : 0.0;
+        double mdm = (dnm > upm && dnm > 0.0) ? dnm : 0.0;
+        count++;
+        if (count <= period + 1) {
+            atr += tr;
+            pdm_s += pdm;
+            mdm_s += mdm;
+            if (count == period + 1) {
+                double inv = atr != 0.0 ? 100.0 / atr : 0.0;
+                double pdi = pdm_s * inv, mdi = mdm_s * inv, sdi = pdi + mdi;
+                dx_sum = sdi != 0.0 ? (fabs(pdi - mdi) / sdi) * 100.0 : 0.0;
+                dx_count = 1;
+            }
+            ph = h[t]; pl = l[t]; pc = c[t];
+            continue;
+        }
+        atr = atr * omr + tr;
+        pdm_s = pdm_s * omr + pdm;
+        mdm_s = mdm_s * omr + mdm;
+        double inv = atr != 0.0 ? 100.0 / atr : 0.0;
+        double pdi = pdm_s * inv, mdi = mdm_s * inv, sdi = pdi + mdi;
+        double dx = sdi != 0.0 ? (fabs(pdi - mdi) / sdi) * 100.0 : 0.0;
+        if (dx_count < period) {
+            dx_sum += dx;
+            dx_count++;
+            if (dx_count == period) { last = dx_sum * rp; out[t] = last; }
+        } else {
+            last = (last * pm1 + dx) * rp;
+            out[t] = last;
+        }
+        ph = h[t]; pl = l[t]; pc = c[t];
+    }
+    return VTO_OK;
+}
+
+/* SuperTrendStream (supertrend.rs:798-885): AtrStream(length = period), then
+ * basic bands mul_add(+-factor, atr, (h + l) / 2); the first ATR bar picks
+ * the side (close <= upper) with changed 0; later bands ratchet with
+ * f64::min / max against the previous bands while the previous close was
+ * inside, and the side flips when the close crosses (changed 1). */
+int vto_supertrend_stream(const double *h, const double *l, const double *c, size_t n, size_t period,
+                          double factor, double *trend, double *changed) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    double *atr = (double *)malloc(sizeof(double) * (n ? n : 1));
+    int code = vto_atr_stream(h, l, c, n, period, atr);
+    if (code != VTO_OK) { free(atr); return code; }
+    double pu = QNAN, pl = QNAN, pc = QNAN;
+    int upper = 0, warmed = 0;
+    for (size_t t = 0; t < n; t++) {
+        trend[t] = changed[t] = QNAN;
+        if (t + 1 < period) continue; /* AtrStream::update returned None */
+        double hl2 = (h[t] + l[t]) * 0.5;
+        double ub = fma(factor, atr[t], hl2), lb = fma(-factor, atr[t], hl2);
+        if (!warmed) {
+            pu = ub; pl = lb;
+            upper = c[t] <= pu;
+            trend[t] = upper ? pu : pl;
+            changed[t] = 0.0;
+            pc = c[t];
+            warmed = 1;
+            continue;
+        }
+        double cu = ub, cl = lb;
+        if (pc <= pu) cu = fmin(cu, pu);
+        if (pc >= pl) cl = fmax(cl, pl);
+        double ch = 0.0, tv;
+        if (upper) {
+            if (c[t] <= cu) tv = cu;
+            else { ch = 1.0; upper = 0; tv = cl; }
+        } else {
+            if (c[t] >= cl) tv = cl;
+            else { ch = 1.0; upper = 1; tv = cu; }
+        }
+        pu = cu; pl = cl; pc = c[t];
+        trend[t] = tv;
+        changed[t] = ch;
+    }
+    free(atr);
+    return VTO_OK;
+}
+
 /* vpwma_with_kernel (vpwma.rs:215-290): weights (p - k)^power, k < p - 1
  * (newest first), inv_norm = 1 / sum, first output first + p - 1;
  * vpwma_scalar (vpwma.rs:296-360): four mul_add accumulators, two rounds per

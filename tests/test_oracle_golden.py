@@ -187,19 +187,42 @@ def test_oracle_weighted_window_warmups(candles):
         assert not np.isnan(out[warm]), name
 
 
-@pytest.mark.parametrize("name", ["ema", "sma", "alma", "rsi", "atr", "wilders"])
+STREAM_VS_BATCH = {
+    # name: (stream params, batch call on the candles, relative tolerance)
+    "ema": ({"period": 9}, lambda d: O.ema(d["close"], 9), 1e-9),
+    "sma": ({"period": 9}, lambda d: O.sma(d["close"], 9), 1e-9),
+    "alma": ({"period": 9}, lambda d: O.alma(d["close"], 9), 1e-9),
+    "rsi": ({"period": 14}, lambda d: O.rsi(d["close"], 14), 1e-9),
+    "atr": ({"length": 14}, lambda d: O.atr(d["high"], d["low"], d["close"], 14), 1e-9),
+    "wilders": ({"period": 5}, lambda d: O.wilders(d["close"], 5), 1e-9),
+    "dema": ({"period": 30}, lambda d: O.dema(d["close"], 30), 1e-9),
+    "tema": ({"period": 9}, lambda d: O.tema(d["close"], 9), 1e-9),
+    "wma": ({"period": 30}, lambda d: O.wma(d["close"], 30), 1e-9),
+    "swma": ({"period": 5}, lambda d: O.swma(d["close"], 5), 1e-9),
+    "pwma": ({"period": 5}, lambda d: O.pwma(d["close"], 5), 1e-9),
+    "stddev": ({"period": 5}, lambda d: O.stddev(d["close"], 5, 1.0), 1e-9),
+    # running sums of squares over ~15k bars: no streaming test in the crate
+    "zscore": ({"period": 14}, lambda d: O.zscore(d["close"], 14, 1.0), 1e-7),
+    "bollinger_bands": ({"period": 20}, lambda d: O.bollinger(d["close"], 20, 2.0, 2.0), 1e-9),
+    "donchian": ({"period": 20}, lambda d: O.donchian(d["high"], d["low"], 20), 1e-9),
+    "willr": ({"period": 14}, lambda d: O.willr(d["high"], d["low"], d["close"], 14), 1e-9),
+    "adx": ({"period": 14}, lambda d: O.adx(d["high"], d["low"], d["close"], 14), 1e-9),
+    "supertrend": ({"period": 10}, lambda d: O.supertrend(d["high"], d["low"], d["close"], 10, 3.0), 1e-9),
+}
+
+
+@pytest.mark.parametrize("name", sorted(STREAM_VS_BATCH))
 def test_oracle_streams_match_batch(name, candles):
     """The oracle's XStream restatements agree with the single-series paths
     after the warm-up, as the crate's own check_X_streaming tests require
     (e.g. ema.rs:1127-1190: skip 240 bars, |diff| < 1e-9)."""
-    c = candles["close"]
-    p = {"ema": 9, "sma": 9, "alma": 9, "rsi": 14, "atr": 14, "wilders": 5}[name]
-    if name == "atr":
-        s = O.stream("atr", [candles["high"], candles["low"], c], length=p)
-        b = O.atr(candles["high"], candles["low"], c, p)
-    else:
-        s = O.stream(name, [c], period=p)
-        b = {"ema": O.ema, "sma": O.sma, "alma": O.alma, "rsi": O.rsi, "wilders": O.wilders}[name](c, p)
-    s, b = s[240:], b[240:]
-    m = ~(np.isnan(s) & np.isnan(b))
-    assert np.all(np.abs(s[m] - b[m]) < 1e-9 * np.maximum(1.0, np.abs(b[m]))), name
+    prm, batch, tol = STREAM_VS_BATCH[name]
+    n_in = O.STREAMS[name][0]
+    ins = [candles["close"]] if n_in == 1 else [candles["high"], candles["low"]] + ([candles["close"]] if n_in == 3 else [])
+    s, b = O.stream(name, ins, **prm), batch(candles)
+    if not isinstance(s, tuple):
+        s, b = (s,), (b,)
+    for k, (sk, bk) in enumerate(zip(s, b)):
+        sk, bk = sk[240:], bk[240:]
+        m = ~(np.isnan(sk) & np.isnan(bk))
+        assert np.all(np.abs(sk[m] - bk[m]) < tol * np.maximum(1.0, np.abs(bk[m]))), (name, k)

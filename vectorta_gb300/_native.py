@@ -190,6 +190,7 @@ def lib() -> C.CDLL:
                                     sz, sz, C.POINTER(DeviceArrayC)]
     L.vta_streams_create.argtypes = [vp, C.c_char_p, C.POINTER(C.c_char_p), C.POINTER(C.c_double), sz, sz,
                                      C.POINTER(vp)]
+    L.vta_streams_shape.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.vta_streams_update_device.argtypes = [vp, vp, vp, vp, vp]
     L.vta_streams_update_host.argtypes = [vp, vp, vp, vp, vp]
     L.vta_streams_reset.argtypes = [vp]

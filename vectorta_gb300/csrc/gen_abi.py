@@ -197,14 +197,28 @@ vta_status vta_ma_select_into_host_f32(vta_ctx* ctx, const char* ma_type, const 
  * device, advanced together by one bar per update, each bar for bar as the
  * crate's XStream::update (EmaStream ema.rs:519-585, SmaStream sma.rs,
  * AlmaStream alma.rs:865-964, RsiStream rsi.rs, AtrStream atr.rs,
- * WildersStream wilders.rs), f64 state, f32 in and out; out is NaN where
- * update() returns None.  indicator: "ema" "sma" "alma" "rsi" "atr"
- * "wilders"; parameters as key/value pairs ("period", ATR also "length",
- * ALMA "offset" / "sigma"; the crate's defaults when absent).  ATR takes
- * (high, low, close), the others one series in a (b, c NULL). */
+ * WildersStream wilders.rs, DemaStream dema.rs:615-690, TemaStream
+ * tema.rs:324-425, WmaStream wma.rs:384-460, SwmaStream swma.rs:536-630,
+ * PwmaStream pwma.rs:675-720, StdDevStream stddev.rs:451-570, ZscoreStream
+ * zscore.rs:567-780, BollingerBandsStream bollinger_bands.rs:884-1075,
+ * DonchianStream donchian.rs:1251-1340, WillrStream willr.rs:1657-1820,
+ * AdxStream adx.rs:1949-2085, SuperTrendStream supertrend.rs:798-885), f64
+ * state, f32 in and out; outputs are NaN where update() returns None.
+ * indicator: "ema" "sma" "alma" "rsi" "atr" "wilders" "dema" "tema" "wma"
+ * "swma" "pwma" "stddev" "zscore" "bollinger_bands" "donchian" "willr" "adx"
+ * "supertrend".  Parameters as key/value pairs, the crate's defaults when
+ * absent: "period" (ATR also "length"), ALMA "offset" / "sigma", StdDev and
+ * Z-score "nbdev", Bollinger "devup" / "devdn" / "matype" (0 sma, 1 ema),
+ * SuperTrend "factor"; Z-score takes ma_type sma, Bollinger and Z-score
+ * devtype 0 (others: VTA_ERR_NOT_IMPLEMENTED).
+ * Inputs: one series in a (b, c NULL); Donchian (high, low) in (a, b); ATR,
+ * WillR, ADX, SuperTrend (high, low, close).  Outputs: out holds n_outputs
+ * rows of n_streams values: Bollinger and Donchian upper / middle / lower,
+ * SuperTrend trend / changed. */
 typedef struct vta_streams vta_streams;
 vta_status vta_streams_create(vta_ctx* ctx, const char* indicator, const char* const* param_keys,
     const double* param_values, size_t n_params, size_t n_streams, vta_streams** out);
+vta_status vta_streams_shape(const vta_streams* s, int* n_inputs, int* n_outputs);
 vta_status vta_streams_update_device(vta_streams* s, const float* d_a, const float* d_b, const float* d_c,
     float* d_out);
 vta_status vta_streams_update_host(vta_streams* s, const float* a, const float* b, const float* c, float* out);

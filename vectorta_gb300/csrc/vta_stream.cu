@@ -7,33 +7,85 @@
 // calls mul_add.  The outputs are the f64 values rounded to f32, NaN where the
 // crate's update() returns None.  The step after the batch entry points for
 // live data: the state stays resident between calls.
+//
+// State is structure-of-arrays: eight f64 and four int slots per stream
+// ([slot][stream]) whose meaning depends on the kind, plus a ring of
+// ring_slots f64 values per stream ([slot][stream]) for the windowed kinds.
 #include <cctype>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "vta_internal.h"
 
 namespace {
 
-enum StreamKind { SK_EMA = 0, SK_SMA = 1, SK_ALMA = 2, SK_RSI = 3, SK_ATR = 4, SK_WILDERS = 5 };
+enum StreamKind {
+    SK_EMA = 0,
+    SK_SMA,
+    SK_ALMA,
+    SK_RSI,
+    SK_ATR,
+    SK_WILDERS,
+    SK_DEMA,
+    SK_TEMA,
+    SK_WMA,
+    SK_SWMA,
+    SK_PWMA,
+    SK_STDDEV,
+    SK_ZSCORE,
+    SK_BOLLINGER,
+    SK_DONCHIAN,
+    SK_WILLR,
+    SK_ADX,
+    SK_SUPERTREND,
+    SK_COUNT
+};
 
-// Per-stream state, structure of arrays ([slot][stream] for the rings).
+struct KindInfo {
+    const char* name;
+    int n_in, n_out;
+    double period;  // the crate's default period (XParams / XStream::try_new)
+};
+
+// inputs: 1 = value; 2 = (high, low); 3 = (high, low, close)
+constexpr KindInfo kKinds[SK_COUNT] = {
+    {"ema", 1, 1, 9},
+    {"sma", 1, 1, 9},
+    {"alma", 1, 1, 9},
+    {"rsi", 1, 1, 14},
+    {"atr", 3, 1, 14},
+    {"wilders", 1, 1, 5},
+    {"dema", 1, 1, 30},
+    {"tema", 1, 1, 9},
+    {"wma", 1, 1, 30},
+    {"swma", 1, 1, 5},
+    {"pwma", 1, 1, 5},
+    {"stddev", 1, 1, 5},
+    {"zscore", 1, 1, 14},
+    {"bollinger_bands", 1, 3, 20},
+    {"donchian", 2, 3, 20},
+    {"willr", 3, 1, 14},
+    {"adx", 3, 1, 14},
+    {"supertrend", 3, 2, 10},
+};
+
+constexpr int kD = 8, kI = 4;
+
 struct StreamState {
-    int kind, n, period;
+    int kind, n, period, n_out;
+    int ka, kb;   // SWMA box lengths
+    int ema_mid;  // Bollinger: EMA middle band (else SMA)
+    int ring_slots;
     double alpha, beta, inv_p, inv_norm;
+    double nbdev, devup, devdn, factor;
     const double* w;  // ALMA weights (device)
-    int* i0;          // count / head / seed_count / warm_count
-    int* i1;          // filled / has_prev / seeded / started / ring head
-    int* i2;          // poisoned
-    double* d0;       // mean / sum / prev / prev_close / warm_sum
-    double* d1;       // sum_gain / rma / last
-    double* d2;       // sum_loss
-    double* d3;       // avg_gain
-    double* d4;       // avg_loss
-    double* ring;     // [period][n] (SMA, ALMA)
+    double* d[kD];    // per-stream f64 state
+    int* iv[kI];      // per-stream int state
+    double* ring;     // [ring_slots][n]
 };
 
 __device__ __forceinline__ double dnan() { return __longlong_as_double(0x7ff8000000000000ll); }
@@ -41,22 +93,71 @@ __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double dsqrt(double a) { return __dsqrt_rn(a); }
 
 __global__ void k_stream_init(StreamState s) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= s.n) return;
-    s.i0[j] = 0;
-    s.i1[j] = 0;
-    s.i2[j] = 0;
     const double nan = dnan();
-    // EMA mean NaN, RSI prev NaN, ATR prev_close NaN, Wilders last NaN
-    s.d0[j] = (s.kind == SK_EMA || s.kind == SK_RSI || s.kind == SK_ATR) ? nan : 0.0;
-    s.d1[j] = (s.kind == SK_ATR || s.kind == SK_WILDERS) ? nan : 0.0;
-    s.d2[j] = 0.0;
-    s.d3[j] = 0.0;
-    s.d4[j] = 0.0;
-    if (s.ring)
-        for (int k = 0; k < s.period; ++k) s.ring[(size_t)k * s.n + j] = nan;
+    for (int k = 0; k < kI; ++k) s.iv[k][j] = 0;
+    for (int k = 0; k < kD; ++k) s.d[k][j] = 0.0;
+    switch (s.kind) {
+        case SK_EMA:  // mean
+        case SK_RSI:  // prev
+        case SK_TEMA:  // ema1
+            s.d[0][j] = nan;
+            break;
+        case SK_ATR:         // prev_close, rma
+        case SK_DEMA:        // ema, ema2
+        case SK_SUPERTREND:  // (ATR) prev_close, rma
+            s.d[0][j] = nan;
+            s.d[1][j] = nan;
+            if (s.kind == SK_SUPERTREND) s.d[3][j] = s.d[4][j] = s.d[5][j] = nan;  // previous bands, close
+            break;
+        case SK_WILDERS: s.d[1][j] = nan; break;                       // last
+        case SK_ADX: s.d[5][j] = s.d[6][j] = s.d[7][j] = nan; break;  // previous high, low, close
+        case SK_ZSCORE: s.iv[2][j] = s.period; break;                  // nan_count
+        default: break;
+    }
+    if (s.ring) {
+        const double fill = (s.kind == SK_SWMA || s.kind == SK_BOLLINGER) ? 0.0 : nan;
+        for (int k = 0; k < s.ring_slots; ++k) s.ring[(size_t)k * s.n + j] = fill;
+    }
+}
+
+// AtrStream::update (atr.rs): TR = h - l while prev_close is NaN, else
+// max(h, pc) - min(l, pc) by comparisons; seed = sum of the first `length`
+// TRs times 1/length; then mul_add(alpha, tr - rma, rma).  Slots d0
+// prev_close, d1 rma, d2 warm_sum, i0 warm_count, i1 seeded.  Returns false
+// while update() returns None.
+__device__ __forceinline__ bool atr_step(const StreamState& s, int j, double h, double l, double cl, double& y) {
+    const double pc = s.d[0][j];
+    double tr;
+    if (isnan(pc)) {
+        tr = dsub(h, l);
+    } else {
+        const double up = h > pc ? h : pc;
+        const double dn = l < pc ? l : pc;
+        tr = dsub(up, dn);
+    }
+    s.d[0][j] = cl;
+    if (!s.iv[1][j]) {
+        s.d[2][j] = dadd(s.d[2][j], tr);
+        const int cnt = s.iv[0][j] + 1;
+        s.iv[0][j] = cnt;
+        if (cnt == s.period) {
+            const double rma = dmul(s.d[2][j], s.alpha);
+            s.d[1][j] = rma;
+            s.iv[1][j] = 1;
+            y = rma;
+            return true;
+        }
+        return false;
+    }
+    const double rma = fma(s.alpha, dsub(tr, s.d[1][j]), s.d[1][j]);
+    s.d[1][j] = rma;
+    y = rma;
+    return true;
 }
 
 template <int K>
@@ -66,54 +167,57 @@ __global__ void k_stream_update(StreamState s, const float* __restrict__ a, cons
     if (j >= s.n) return;
     const int p = s.period;
     const double nan = dnan();
-    double y = nan;
+    double y = nan, y1 = nan, y2 = nan;  // outputs 0..2
+#define D(k) s.d[k][j]
+#define IV(k) s.iv[k][j]
+#define RING(k) s.ring[(size_t)(k) * s.n + j]
     if constexpr (K == SK_EMA) {  // EmaStream::update, ema.rs:560-585
         const double v = (double)a[j];
         if (!isfinite(v)) {
-            y = s.i1[j] ? s.d0[j] : nan;
+            y = IV(1) ? D(0) : nan;
         } else {
-            const int cnt = s.i0[j] + 1;
-            s.i0[j] = cnt;
-            double mean = s.d0[j];
+            const int cnt = IV(0) + 1;
+            IV(0) = cnt;
+            double mean = D(0);
             if (cnt == 1) mean = v;
             else if (cnt <= p) mean = fma(dsub(v, mean), ddiv(1.0, (double)cnt), mean);
             else mean = fma(s.beta, mean, dmul(s.alpha, v));
-            s.d0[j] = mean;
-            if (!s.i1[j] && cnt >= p) s.i1[j] = 1;
-            y = s.i1[j] ? mean : nan;
+            D(0) = mean;
+            if (!IV(1) && cnt >= p) IV(1) = 1;
+            y = IV(1) ? mean : nan;
         }
     } else if constexpr (K == SK_SMA) {  // SmaStream::update (sma.rs)
         const double v = (double)a[j];
         if (p == 1) {
             y = v;
         } else {
-            int head = s.i1[j];
-            const int cnt = s.i0[j];
-            double sum = s.d0[j];
+            int head = IV(1);
+            const int cnt = IV(0);
+            double sum = D(0);
             if (cnt < p) {
                 sum = dadd(sum, v);
-                s.ring[(size_t)head * s.n + j] = v;
+                RING(head) = v;
                 head = head + 1 == p ? 0 : head + 1;
-                s.i0[j] = cnt + 1;
+                IV(0) = cnt + 1;
                 y = cnt + 1 == p ? dmul(sum, s.inv_p) : nan;
             } else {
-                const double old = s.ring[(size_t)head * s.n + j];
+                const double old = RING(head);
                 sum = dadd(sum, dsub(v, old));
-                s.ring[(size_t)head * s.n + j] = v;
+                RING(head) = v;
                 head = head + 1 == p ? 0 : head + 1;
                 y = dmul(sum, s.inv_p);
             }
-            s.d0[j] = sum;
-            s.i1[j] = head;
+            D(0) = sum;
+            IV(1) = head;
         }
     } else if constexpr (K == SK_ALMA) {  // AlmaStream::update / dot_at_head, alma.rs:865-964
         const double v = (double)a[j];
-        int head = s.i1[j];
-        s.ring[(size_t)head * s.n + j] = v;
+        int head = IV(1);
+        RING(head) = v;
         head = head + 1 == p ? 0 : head + 1;
-        s.i1[j] = head;
-        int filled = s.i0[j];
-        if (filled < p) s.i0[j] = ++filled;
+        IV(1) = head;
+        int filled = IV(0);
+        if (filled < p) IV(0) = ++filled;
         if (filled >= p) {
             // window oldest first = ring[(head + i) % p]; four accumulators
             // over blocks of 4, then the tail (dot_scalar_unrolled_safe)
@@ -124,122 +228,497 @@ __global__ void k_stream_update(StreamState s, const float* __restrict__ a, cons
                 for (int q = 0; q < 4; ++q) {
                     int slot = head + i + q;
                     if (slot >= p) slot -= p;
-                    acc[q] = dadd(acc[q], dmul(s.ring[(size_t)slot * s.n + j], s.w[i + q]));
+                    acc[q] = dadd(acc[q], dmul(RING(slot), s.w[i + q]));
                 }
             double sum = dadd(dadd(acc[0], acc[1]), dadd(acc[2], acc[3]));
             for (; i < p; ++i) {
                 int slot = head + i;
                 if (slot >= p) slot -= p;
-                sum = dadd(sum, dmul(s.ring[(size_t)slot * s.n + j], s.w[i]));
+                sum = dadd(sum, dmul(RING(slot), s.w[i]));
             }
             y = dmul(sum, s.inv_norm);
         }
     } else if constexpr (K == SK_RSI) {  // RsiStream::update (rsi.rs)
         const double v = (double)a[j];
-        if (!s.i1[j]) {
-            s.d0[j] = v;
-            s.i1[j] = 1;
+        if (!IV(1)) {
+            D(0) = v;
+            IV(1) = 1;
         } else {
-            const double d = dsub(v, s.d0[j]);
-            s.d0[j] = v;
+            const double d = dsub(v, D(0));
+            D(0) = v;
             const double g = fmax(d, 0.0), l = fmax(-d, 0.0);  // f64::max ignores NaN
-            const bool seeded = (s.i2[j] & 2) != 0;                 // i2: bit 0 poisoned, bit 1 seeded
+            const bool seeded = (IV(2) & 2) != 0;                  // i2: bit 0 poisoned, bit 1 seeded
             if (!seeded) {
-                int poisoned = s.i2[j] & 1;
+                int poisoned = IV(2) & 1;
                 if (!isfinite(d)) poisoned = 1;
-                s.d1[j] = dadd(s.d1[j], g);
-                s.d2[j] = dadd(s.d2[j], l);
-                const int cnt = s.i0[j] + 1;
-                s.i0[j] = cnt;
+                D(1) = dadd(D(1), g);
+                D(2) = dadd(D(2), l);
+                const int cnt = IV(0) + 1;
+                IV(0) = cnt;
                 if (cnt == p) {
                     if (poisoned) {
-                        s.d3[j] = nan;
-                        s.d4[j] = nan;
+                        D(3) = nan;
+                        D(4) = nan;
                         y = nan;
                     } else {
-                        const double ag = dmul(s.d1[j], s.inv_p), al = dmul(s.d2[j], s.inv_p);
-                        s.d3[j] = ag;
-                        s.d4[j] = al;
+                        const double ag = dmul(D(1), s.inv_p), al = dmul(D(2), s.inv_p);
+                        D(3) = ag;
+                        D(4) = al;
                         const double den = dadd(ag, al);
                         y = den == 0.0 ? 50.0 : ddiv(dmul(100.0, ag), den);
                     }
-                    s.i2[j] = poisoned | 2;
+                    IV(2) = poisoned | 2;
                 } else {
-                    s.i2[j] = poisoned;
+                    IV(2) = poisoned;
                 }
             } else {
-                const double ag = fma(s.d3[j], s.beta, dmul(s.inv_p, g));
-                const double al = fma(s.d4[j], s.beta, dmul(s.inv_p, l));
-                s.d3[j] = ag;
-                s.d4[j] = al;
+                const double ag = fma(D(3), s.beta, dmul(s.inv_p, g));
+                const double al = fma(D(4), s.beta, dmul(s.inv_p, l));
+                D(3) = ag;
+                D(4) = al;
                 const double den = dadd(ag, al);
                 y = den == 0.0 ? 50.0 : ddiv(dmul(100.0, ag), den);
             }
         }
-    } else if constexpr (K == SK_ATR) {  // AtrStream::update (atr.rs)
-        const double h = (double)a[j], l = (double)b[j], cl = (double)c[j];
-        const double pc = s.d0[j];
-        double tr;
-        if (isnan(pc)) {
-            tr = dsub(h, l);
-        } else {
-            const double up = h > pc ? h : pc;
-            const double dn = l < pc ? l : pc;
-            tr = dsub(up, dn);
-        }
-        s.d0[j] = cl;
-        if (!s.i1[j]) {
-            s.d2[j] = dadd(s.d2[j], tr);
-            const int cnt = s.i0[j] + 1;
-            s.i0[j] = cnt;
-            if (cnt == p) {
-                const double rma = dmul(s.d2[j], s.alpha);
-                s.d1[j] = rma;
-                s.i1[j] = 1;
-                y = rma;
-            }
-        } else {
-            const double rma = fma(s.alpha, dsub(tr, s.d1[j]), s.d1[j]);
-            s.d1[j] = rma;
-            y = rma;
-        }
+    } else if constexpr (K == SK_ATR) {
+        atr_step(s, j, (double)a[j], (double)b[j], (double)c[j], y);
     } else if constexpr (K == SK_WILDERS) {  // WildersStream::update (wilders.rs)
         const double v = (double)a[j];
-        if (!s.i1[j]) {
+        if (!IV(1)) {
             if (!isfinite(v)) {
-                s.d0[j] = 0.0;
-                s.i0[j] = 0;
+                D(0) = 0.0;
+                IV(0) = 0;
             } else {
-                const double sum = dadd(s.d0[j], v);
-                s.d0[j] = sum;
-                const int cnt = s.i0[j] + 1;
-                s.i0[j] = cnt;
+                const double sum = dadd(D(0), v);
+                D(0) = sum;
+                const int cnt = IV(0) + 1;
+                IV(0) = cnt;
                 if (cnt >= p) {
                     const double y0 = ddiv(sum, (double)p);
-                    s.d1[j] = y0;
-                    s.i1[j] = 1;
+                    D(1) = y0;
+                    IV(1) = 1;
                     y = y0;
                 }
             }
         } else {
-            const double last = fma(dsub(v, s.d1[j]), s.alpha, s.d1[j]);
-            s.d1[j] = last;
+            const double last = fma(dsub(v, D(1)), s.alpha, D(1));
+            D(1) = last;
             y = last;
         }
+    } else if constexpr (K == SK_DEMA) {
+        // DemaStream::update (dema.rs:657-687), fmadd = mul_add (x86
+        // targets): d0 ema, d1 ema2, i0 filled
+        const double v = (double)a[j];
+        if (IV(0) == 0) {
+            D(0) = v;
+            D(1) = v;
+            IV(0) = 1;
+            y = p == 1 ? v : nan;
+        } else {
+            const double e1 = fma(D(0), s.beta, dmul(v, s.alpha));
+            const double e2 = fma(D(1), s.beta, dmul(e1, s.alpha));
+            D(0) = e1;
+            D(1) = e2;
+            const double yy = fma(e1, 2.0, -e2);
+            const int f = IV(0) < INT32_MAX ? IV(0) + 1 : IV(0);
+            IV(0) = f;
+            y = f > p - 1 ? yy : nan;
+        }
+    } else if constexpr (K == SK_TEMA) {
+        // TemaStream::update (tema.rs:378-424): d0..d2 ema1..ema3, i0 count,
+        // i1 ready; e = e (1 - a) + v a without FMA
+        const double v = (double)a[j];
+        double e1 = D(0), e2 = D(1), e3 = D(2);
+        if (IV(1)) {
+            e1 = dadd(dmul(e1, s.beta), dmul(v, s.alpha));
+            e2 = dadd(dmul(e2, s.beta), dmul(e1, s.alpha));
+            e3 = dadd(dmul(e3, s.beta), dmul(e2, s.alpha));
+            y = dadd(dsub(dmul(3.0, e1), dmul(3.0, e2)), e3);
+        } else if (IV(0) == 0) {
+            if (!isnan(v)) {
+                e1 = v;
+                IV(0) = 1;
+                if (p == 1) {
+                    e2 = e1;
+                    e3 = e2;
+                    IV(1) = 1;
+                    y = e1;
+                }
+            }
+        } else {
+            e1 = dadd(dmul(e1, s.beta), dmul(v, s.alpha));
+            const int cnt = IV(0) + 1;
+            IV(0) = cnt;
+            const int start2 = p, start3 = 2 * p - 1, lookback = 3 * (p - 1);
+            if (cnt == start2) e2 = e1;
+            else if (cnt > start2) e2 = dadd(dmul(e2, s.beta), dmul(e1, s.alpha));
+            if (cnt == start3) e3 = e2;
+            else if (cnt > start3) e3 = dadd(dmul(e3, s.beta), dmul(e2, s.alpha));
+            if (cnt > lookback) {
+                IV(1) = 1;
+                y = dadd(dsub(dmul(3.0, e1), dmul(3.0, e2)), e3);
+            }
+        }
+        D(0) = e1;
+        D(1) = e2;
+        D(2) = e3;
+    } else if constexpr (K == SK_WMA) {
+        // WmaStream::update (wma.rs:420-459): ring of p values, i0 head,
+        // i1 filled, d0 plain_sum, d1 weighted_sum
+        const double v = (double)a[j];
+        int head = IV(0);
+        RING(head) = v;
+        head = head + 1 == p ? 0 : head + 1;
+        IV(0) = head;
+        if (!IV(1)) {
+            if (head == 0) {
+                double ws = 0.0, ss = 0.0;
+                for (int w = 1; w <= p; ++w) {  // oldest first from slot 0
+                    const double bv = RING(w - 1);
+                    ss = dadd(ss, bv);
+                    ws = dadd(ws, dmul((double)w, bv));
+                }
+                y = dmul(ws, s.inv_norm);
+                D(1) = dsub(ws, ss);
+                D(0) = dsub(ss, RING(0));
+                IV(1) = 1;
+            }
+        } else {
+            const double oldest = RING(head);
+            const double ws = dadd(D(1), dmul((double)p, v));
+            const double ps = dadd(D(0), v);
+            y = dmul(ws, s.inv_norm);
+            D(1) = dsub(ws, ps);
+            D(0) = dsub(ps, oldest);
+        }
+    } else if constexpr (K == SK_SWMA) {
+        // SwmaStream::update (swma.rs:595-630): ring_a = ring slots [0, a),
+        // ring_b = [a, a + b); i0 idx_a, i1 cnt_a, i2 idx_b, i3 cnt_b,
+        // d0 s1_sum, d1 s2_sum
+        const double v = (double)a[j];
+        const int ka = s.ka, kb = s.kb;
+        const int ia = IV(0);
+        const double old_a = RING(ia);
+        double s1 = D(0);
+        int ca = IV(1);
+        if (ca == ka) s1 = dsub(s1, old_a);
+        else IV(1) = ++ca;
+        RING(ia) = v;
+        s1 = dadd(s1, v);
+        D(0) = s1;
+        IV(0) = ia + 1 == ka ? 0 : ia + 1;
+        if (ca == ka) {
+            const int ib = IV(2);
+            const double old_b = RING(ka + ib);
+            double s2 = D(1);
+            int cb = IV(3);
+            if (cb == kb) s2 = dsub(s2, old_b);
+            else IV(3) = ++cb;
+            RING(ka + ib) = s1;
+            s2 = dadd(s2, s1);
+            D(1) = s2;
+            IV(2) = ib + 1 == kb ? 0 : ib + 1;
+            if (cb == kb) y = dmul(s2, s.inv_norm);
+        }
+    } else if constexpr (K == SK_PWMA) {
+        // PwmaStream::update (pwma.rs:712-733): cascade of p - 1 pairwise
+        // running sums in the ring (prev, NaN at start), i0 seen
+        const double v = (double)a[j];
+        const int m = p - 1;
+        if (m == 0) {
+            y = v;
+        } else {
+            double acc = v;
+            for (int k = 0; k < m; ++k) {
+                const double o = dadd(acc, RING(k));
+                RING(k) = acc;
+                acc = o;
+            }
+            if (IV(0) < m) ++IV(0);
+            else y = dmul(acc, s.inv_norm);
+        }
+    } else if constexpr (K == SK_STDDEV) {
+        // StdDevStream::update (stddev.rs:490-569): ring, i0 head, i1 filled,
+        // i2 nan_count, d0 sum, d1 sum_sqr
+        const double v = (double)a[j];
+        const int head = IV(0);
+        bool emit = true;
+        if (!IV(1)) {
+            if (isnan(v)) {
+                ++IV(2);
+            } else {
+                D(0) = dadd(D(0), v);
+                D(1) = dadd(D(1), dmul(v, v));
+            }
+            RING(head) = v;
+            if (head + 1 == p) {
+                IV(0) = 0;
+                IV(1) = 1;
+            } else {
+                IV(0) = head + 1;
+                emit = false;
+            }
+        } else {
+            const double old = RING(head);
+            const bool nn = isnan(v), on = isnan(old);
+            if (!on && !nn) {
+                D(0) = dadd(D(0), dsub(v, old));
+                D(1) = dadd(D(1), dsub(dmul(v, v), dmul(old, old)));
+            } else if (!on && nn) {
+                D(0) = dsub(D(0), old);
+                D(1) = dsub(D(1), dmul(old, old));
+                ++IV(2);
+            } else if (on && !nn) {
+                if (IV(2) > 0) --IV(2);
+                D(0) = dadd(D(0), v);
+                D(1) = dadd(D(1), dmul(v, v));
+            } else {
+                if (IV(2) > 0) --IV(2);
+                ++IV(2);
+            }
+            RING(head) = v;
+            IV(0) = head + 1 == p ? 0 : head + 1;
+        }
+        if (emit) {
+            if (IV(2) > 0) {
+                y = nan;
+            } else {
+                const double mean = dmul(D(0), s.inv_p);
+                const double var = dsub(dmul(D(1), s.inv_p), dmul(mean, mean));
+                y = var <= 0.0 ? 0.0 : dmul(dsqrt(var), s.nbdev);
+            }
+        }
+    } else if constexpr (K == SK_ZSCORE) {
+        // ZscoreStream::update (zscore.rs:657-735), MA "sma", devtype 0:
+        // ring, i0 head, i1 filled, i2 nan_count (starts at p), d0 sum,
+        // d1 sum2.  A window holding a NaN, or nbdev == 0, takes the crate's
+        // slow path, whose result is NaN for this MA.
+        const double v = (double)a[j];
+        int head = IV(0);
+        const double old = RING(head);
+        RING(head) = v;
+        head = head + 1 == p ? 0 : head + 1;
+        IV(0) = head;
+        if (!IV(1) && head == 0) IV(1) = 1;
+        if (isnan(old) && IV(2) > 0) --IV(2);
+        if (isnan(v)) ++IV(2);
+        const double oc = isnan(old) ? 0.0 : old, nc = isnan(v) ? 0.0 : v;
+        D(0) = dsub(dadd(D(0), nc), oc);
+        D(1) = dsub(dadd(D(1), dmul(nc, nc)), dmul(oc, oc));
+        if (IV(1) && s.nbdev != 0.0 && IV(2) == 0) {
+            const double mean = dmul(D(0), s.inv_p), ex2 = dmul(D(1), s.inv_p);
+            double var = dsub(ex2, dmul(mean, mean));
+            if (var < 0.0) var = 0.0;
+            const double sd = dsqrt(var);
+            if (sd != 0.0 && isfinite(sd)) {
+                const double last = RING(head == 0 ? p - 1 : head - 1);
+                y = ddiv(dsub(last, mean), dmul(sd, s.nbdev));
+            }
+        }
+    } else if constexpr (K == SK_BOLLINGER) {
+        // BollingerBandsStream::update (bollinger_bands.rs:1022-1060), devtype
+        // 0, SMA or EMA middle: ring, i0 idx, i1 len, i2 ema_seeded, d0 sum,
+        // d1 sum_sq, d2 ema.  A non-finite value resets the stream.
+        const double v = (double)a[j];
+        if (!isfinite(v)) {
+            IV(0) = IV(1) = IV(2) = 0;
+            D(0) = D(1) = D(2) = 0.0;
+        } else {
+            const int idx = IV(0);
+            const int len = IV(1);
+            if (len < p) {
+                RING(idx) = v;
+                IV(1) = len + 1;
+                D(0) = dadd(D(0), v);
+                D(1) = fma(v, v, D(1));
+            } else {
+                const double old = RING(idx);
+                RING(idx) = v;
+                D(0) = dadd(D(0), dsub(v, old));
+                const double tmp = dsub(D(1), dmul(old, old));
+                D(1) = fma(v, v, tmp);
+            }
+            IV(0) = idx + 1 == p ? 0 : idx + 1;
+            if (IV(1) >= p) {
+                const double mean = dmul(D(0), s.inv_p);
+                const double var = dsub(dmul(D(1), s.inv_p), dmul(mean, mean));
+                const double sd = dsqrt(var > 0.0 ? var : 0.0);
+                double mid = mean;
+                if (s.ema_mid) {
+                    if (!IV(2)) {
+                        D(2) = dmul(D(0), s.inv_p);
+                        IV(2) = 1;
+                    } else {
+                        D(2) = fma(s.alpha, v, dmul(s.beta, D(2)));
+                    }
+                    mid = D(2);
+                }
+                y = fma(s.devup, sd, mid);
+                y1 = mid;
+                y2 = fma(-s.devdn, sd, mid);
+            }
+        }
+    } else if constexpr (K == SK_DONCHIAN) {
+        // DonchianStream::update (donchian.rs:1302-1340): once p bars were
+        // seen, NaN while the window holds a non-finite high or low, else the
+        // window's highest high / lowest low (the monotone deques' fronts).
+        // Ring slots [0, p) highs, [p, 2p) lows; i0 head, i1 seen (capped).
+        const double h = (double)a[j], l = (double)b[j];
+        const int head = IV(0);
+        RING(head) = h;
+        RING(p + head) = l;
+        IV(0) = head + 1 == p ? 0 : head + 1;
+        if (IV(1) < p) ++IV(1);
+        if (IV(1) >= p) {
+            bool ok = true;
+            double mx = -INFINITY, mn = INFINITY;
+            for (int k = 0; k < p; ++k) {
+                const double hk = RING(k), lk = RING(p + k);
+                ok = ok && isfinite(hk) && isfinite(lk);
+                mx = hk > mx ? hk : mx;
+                mn = lk < mn ? lk : mn;
+            }
+            if (ok) {
+                y = mx;
+                y1 = fma(dsub(mx, mn), 0.5, mn);
+                y2 = mn;
+            }
+        }
+    } else if constexpr (K == SK_WILLR) {
+        // WillrStream::update (willr.rs:1709-1820): once p bars were seen,
+        // NaN when the close is NaN or the window holds a NaN high or low or
+        // its extremes are not finite; 0 for a flat window; else
+        // mul_add(-100, (hh - close) / (hh - ll), 0).  Ring slots as Donchian.
+        const double h = (double)a[j], l = (double)b[j], cl = (double)c[j];
+        const int head = IV(0);
+        RING(head) = h;
+        RING(p + head) = l;
+        IV(0) = head + 1 == p ? 0 : head + 1;
+        if (IV(1) < p) ++IV(1);
+        if (IV(1) >= p) {
+            bool ok = !isnan(cl);
+            double hh = -INFINITY, ll = INFINITY;
+            for (int k = 0; k < p; ++k) {
+                const double hk = RING(k), lk = RING(p + k);
+                ok = ok && !isnan(hk) && !isnan(lk);
+                hh = hk > hh ? hk : hh;
+                ll = lk < ll ? lk : ll;
+            }
+            if (ok && isfinite(hh) && isfinite(ll)) {
+                const double den = dsub(hh, ll);
+                y = den == 0.0 ? 0.0 : fma(-100.0, ddiv(dsub(hh, cl), den), 0.0);
+            }
+        }
+    } else if constexpr (K == SK_ADX) {
+        // AdxStream::update (adx.rs:1988-2084): d0 atr, d1 +DM, d2 -DM
+        // (smoothed), d3 dx_sum, d4 last_adx, d5..d7 previous high / low /
+        // close; i0 count (capped at p + 2), i1 dx_count
+        const double h = (double)a[j], l = (double)b[j], cl = (double)c[j];
+        if (IV(0) == 0) {
+            IV(0) = 1;
+        } else {
+            const double tr = dsub(fmax(h, D(7)), fmin(l, D(7)));
+            const double upm = dsub(h, D(5)), dnm = dsub(D(6), l);
+            const double pdm = (upm > dnm && upm > 0.0) ? upm : 0.0;
+            const double mdm = (dnm > upm && dnm > 0.0) ? dnm : 0.0;
+            const int cnt = IV(0) + 1;
+            IV(0) = cnt < p + 2 ? cnt : p + 2;
+            if (cnt <= p + 1) {
+                D(0) = dadd(D(0), tr);
+                D(1) = dadd(D(1), pdm);
+                D(2) = dadd(D(2), mdm);
+                if (cnt == p + 1) {
+                    const double inv = D(0) != 0.0 ? ddiv(100.0, D(0)) : 0.0;
+                    const double pdi = dmul(D(1), inv), mdi = dmul(D(2), inv), sdi = dadd(pdi, mdi);
+                    D(3) = sdi != 0.0 ? dmul(ddiv(fabs(dsub(pdi, mdi)), sdi), 100.0) : 0.0;
+                    IV(1) = 1;
+                }
+            } else {
+                D(0) = dadd(dmul(D(0), s.beta), tr);
+                D(1) = dadd(dmul(D(1), s.beta), pdm);
+                D(2) = dadd(dmul(D(2), s.beta), mdm);
+                const double inv = D(0) != 0.0 ? ddiv(100.0, D(0)) : 0.0;
+                const double pdi = dmul(D(1), inv), mdi = dmul(D(2), inv), sdi = dadd(pdi, mdi);
+                const double dx = sdi != 0.0 ? dmul(ddiv(fabs(dsub(pdi, mdi)), sdi), 100.0) : 0.0;
+                if (IV(1) < p) {
+                    D(3) = dadd(D(3), dx);
+                    const int dc = IV(1) + 1;
+                    IV(1) = dc;
+                    if (dc == p) {
+                        D(4) = dmul(D(3), s.inv_p);
+                        y = D(4);
+                    }
+                } else {
+                    D(4) = dmul(dadd(dmul(D(4), (double)p - 1.0), dx), s.inv_p);
+                    y = D(4);
+                }
+            }
+        }
+        D(5) = h;
+        D(6) = l;
+        D(7) = cl;
+    } else if constexpr (K == SK_SUPERTREND) {
+        // SuperTrendStream::update (supertrend.rs:831-884) over the AtrStream
+        // slots (d0..d2, i0, i1): d3 / d4 previous upper / lower band, d5
+        // previous close, i2 upper_state, i3 warmed.  Outputs trend, changed.
+        const double h = (double)a[j], l = (double)b[j], cl = (double)c[j];
+        double atr;
+        if (atr_step(s, j, h, l, cl, atr)) {
+            const double hl2 = dmul(dadd(h, l), 0.5);
+            const double ub = fma(s.factor, atr, hl2), lb = fma(-s.factor, atr, hl2);
+            if (!IV(3)) {
+                D(3) = ub;
+                D(4) = lb;
+                IV(2) = cl <= ub;
+                y = IV(2) ? ub : lb;
+                y1 = 0.0;
+                D(5) = cl;
+                IV(3) = 1;
+            } else {
+                double cu = ub, cb = lb;
+                if (D(5) <= D(3)) cu = fmin(cu, D(3));
+                if (D(5) >= D(4)) cb = fmax(cb, D(4));
+                double ch = 0.0, tv;
+                if (IV(2)) {
+                    if (cl <= cu) {
+                        tv = cu;
+                    } else {
+                        ch = 1.0;
+                        IV(2) = 0;
+                        tv = cb;
+                    }
+                } else {
+                    if (cl >= cb) {
+                        tv = cb;
+                    } else {
+                        ch = 1.0;
+                        IV(2) = 1;
+                        tv = cu;
+                    }
+                }
+                D(3) = cu;
+                D(4) = cb;
+                D(5) = cl;
+                y = tv;
+                y1 = ch;
+            }
+        }
     }
+#undef D
+#undef IV
+#undef RING
     out[j] = (float)y;
+    if (s.n_out > 1) out[(size_t)s.n + j] = (float)y1;
+    if (s.n_out > 2) out[2 * (size_t)s.n + j] = (float)y2;
 }
 
 int kind_of(const char* name) {
     if (!name) return -1;
     std::string s(name);
     for (char& ch : s) ch = (char)std::tolower((unsigned char)ch);
-    if (s == "ema") return SK_EMA;
-    if (s == "sma") return SK_SMA;
-    if (s == "alma") return SK_ALMA;
-    if (s == "rsi") return SK_RSI;
-    if (s == "atr") return SK_ATR;
-    if (s == "wilders") return SK_WILDERS;
+    if (s == "bollinger" || s == "bb") s = "bollinger_bands";
+    for (int k = 0; k < SK_COUNT; ++k)
+        if (s == kKinds[k].name) return k;
     return -1;
 }
 
@@ -249,13 +728,25 @@ double param(const char* const* keys, const double* vals, size_t n, const char* 
     return dflt;
 }
 
+template <int K>
+void launch_update(const StreamState& s, cudaStream_t st, const float* a, const float* b, const float* c,
+                   float* out) {
+    k_stream_update<K><<<vta::ceil_div(s.n, 256), 256, 0, st>>>(s, a, b, c, out);
+}
+
+template <int... Ks>
+void dispatch_update(std::integer_sequence<int, Ks...>, const StreamState& s, cudaStream_t st, const float* a,
+                     const float* b, const float* c, float* out) {
+    ((s.kind == Ks ? launch_update<Ks>(s, st, a, b, c, out) : void()), ...);
+}
+
 }  // namespace
 
 struct vta_streams {
     vta_ctx* ctx = nullptr;
     StreamState s{};
     void* block = nullptr;  // one device allocation for all state
-    float* d_io = nullptr;  // staging of the host-buffer update: inputs (3 n) + output (n)
+    float* d_io = nullptr;  // staging of the host-buffer update: inputs (3 n) + outputs (n_out n)
 };
 
 using namespace vta;
@@ -263,17 +754,13 @@ using namespace vta;
 namespace {
 
 vta_status enqueue_update(vta_streams* S, const float* a, const float* b, const float* c, float* out) {
-    cudaStream_t st = S->ctx->stream;
-    const unsigned blocks = ceil_div(S->s.n, 256);
-    switch (S->s.kind) {
-        case SK_EMA: k_stream_update<SK_EMA><<<blocks, 256, 0, st>>>(S->s, a, b, c, out); break;
-        case SK_SMA: k_stream_update<SK_SMA><<<blocks, 256, 0, st>>>(S->s, a, b, c, out); break;
-        case SK_ALMA: k_stream_update<SK_ALMA><<<blocks, 256, 0, st>>>(S->s, a, b, c, out); break;
-        case SK_RSI: k_stream_update<SK_RSI><<<blocks, 256, 0, st>>>(S->s, a, b, c, out); break;
-        case SK_ATR: k_stream_update<SK_ATR><<<blocks, 256, 0, st>>>(S->s, a, b, c, out); break;
-        default: k_stream_update<SK_WILDERS><<<blocks, 256, 0, st>>>(S->s, a, b, c, out); break;
-    }
+    dispatch_update(std::make_integer_sequence<int, SK_COUNT>{}, S->s, S->ctx->stream, a, b, c, out);
     return check_launch("k_stream_update");
+}
+
+bool inputs_ok(const vta_streams* S, const float* a, const float* b, const float* c) {
+    const int n_in = kKinds[S->s.kind].n_in;
+    return a && (n_in < 2 || b) && (n_in < 3 || c);
 }
 
 }  // namespace
@@ -289,56 +776,135 @@ vta_status vta_streams_create(vta_ctx* ctx, const char* indicator, const char* c
     if (kind < 0) return fail(VTA_ERR_NOT_IMPLEMENTED, std::string("streams: no streaming kernel for ") +
                                                            (indicator ? indicator : "(null)"));
     if (n_streams == 0 || n_streams > (size_t)INT32_MAX) return fail(VTA_ERR_INVALID_INPUT, "streams: bad count");
-    // the crate's defaults (EmaParams 9, SmaParams 9, AlmaParams 9 / 0.85 /
-    // 6.0, RsiParams 14, AtrParams 14, WildersParams 5)
-    const double dflt = kind == SK_RSI || kind == SK_ATR ? 14.0 : kind == SK_WILDERS ? 5.0 : 9.0;
-    double pd = param(param_keys, param_values, n_params, "period", dflt);
-    if (kind == SK_ATR) pd = param(param_keys, param_values, n_params, "length", pd);
-    if (!(pd >= 1.0) || pd != std::floor(pd) || pd > 1e7)
+    const KindInfo& info = kKinds[kind];
+    auto P = [&](const char* key, double dflt) { return param(param_keys, param_values, n_params, key, dflt); };
+    double pd = P("period", info.period);
+    if (kind == SK_ATR) pd = P("length", pd);
+    if (!(pd >= 1.0) || pd != std::floor(pd) || pd > 1e6)
         return fail(VTA_ERR_INVALID_INPUT, "streams: invalid period (must be a positive integer)");
     const int p = (int)pd;
-    const double offset = param(param_keys, param_values, n_params, "offset", 0.85);
-    const double sigma = param(param_keys, param_values, n_params, "sigma", 6.0);
-    if (kind == SK_ALMA && !(offset >= 0.0 && offset <= 1.0)) return fail(VTA_ERR_INVALID_INPUT, "streams: alma offset");
-    if (kind == SK_ALMA && !(sigma > 0.0)) return fail(VTA_ERR_INVALID_INPUT, "streams: alma sigma");
+    if (kind == SK_WMA && p < 2) return fail(VTA_ERR_INVALID_INPUT, "streams: wma period must be >= 2");
 
-    auto* S = new vta_streams();
-    S->ctx = ctx;
-    StreamState& s = S->s;
+    StreamState s{};
     s.kind = kind;
     s.n = (int)n_streams;
     s.period = p;
-    if (kind == SK_EMA) {
-        s.alpha = 2.0 / ((double)p + 1.0);
-        s.beta = 1.0 - s.alpha;
-    } else if (kind == SK_RSI) {
-        s.inv_p = 1.0 / (double)p;
-        s.beta = 1.0 - s.inv_p;
-    } else if (kind == SK_SMA) {
-        s.inv_p = 1.0 / (double)p;
-    } else {
-        s.alpha = 1.0 / (double)p;
-    }
-    // ALMA weights on the host with the C library's exp, as the crate's
-    // AlmaStream::try_new forms them (alma.rs:883-899)
+    s.n_out = info.n_out;
     std::vector<double> w;
-    if (kind == SK_ALMA) {
-        const double m = offset * (double)(p - 1);
-        const double sg = (double)p / sigma;
-        const double s2 = 2.0 * sg * sg;
-        double norm = 0.0;
-        w.resize(p);
-        for (int i = 0; i < p; ++i) {
-            const double diff = (double)i - m;
-            w[i] = std::exp(-(diff * diff) / s2);
-            norm += w[i];
+    int ring_slots = 0;
+    switch (kind) {
+        case SK_EMA:
+            s.alpha = 2.0 / ((double)p + 1.0);
+            s.beta = 1.0 - s.alpha;
+            break;
+        case SK_RSI:
+            s.inv_p = 1.0 / (double)p;
+            s.beta = 1.0 - s.inv_p;
+            break;
+        case SK_SMA:
+            s.inv_p = 1.0 / (double)p;
+            ring_slots = p;
+            break;
+        case SK_ALMA: {
+            const double offset = P("offset", 0.85), sigma = P("sigma", 6.0);
+            if (!(offset >= 0.0 && offset <= 1.0)) return fail(VTA_ERR_INVALID_INPUT, "streams: alma offset");
+            if (!(sigma > 0.0)) return fail(VTA_ERR_INVALID_INPUT, "streams: alma sigma");
+            // weights on the host with the C library's exp, as the crate's
+            // AlmaStream::try_new forms them (alma.rs:883-899)
+            const double m = offset * (double)(p - 1);
+            const double sg = (double)p / sigma;
+            const double s2 = 2.0 * sg * sg;
+            double norm = 0.0;
+            w.resize(p);
+            for (int i = 0; i < p; ++i) {
+                const double diff = (double)i - m;
+                w[i] = std::exp(-(diff * diff) / s2);
+                norm += w[i];
+            }
+            s.inv_norm = 1.0 / norm;
+            ring_slots = p;
+            break;
         }
-        s.inv_norm = 1.0 / norm;
+        case SK_ATR:
+        case SK_WILDERS:
+            s.alpha = 1.0 / (double)p;
+            break;
+        case SK_SUPERTREND:
+            // AtrStream(length = period) inside (supertrend.rs:810-818)
+            s.alpha = 1.0 / (double)p;
+            s.factor = P("factor", 3.0);
+            break;
+        case SK_DEMA:
+            // DemaStream::try_new (dema.rs:625-640)
+            s.alpha = 2.0 / ((double)p + 1.0);
+            s.beta = 1.0 - 2.0 / ((double)p + 1.0);
+            break;
+        case SK_TEMA:
+            s.alpha = 2.0 / ((double)p + 1.0);
+            s.beta = 1.0 - s.alpha;
+            break;
+        case SK_WMA:
+            // 1 / (p (p + 1) / 2), the product formed in integers (wma.rs:406)
+            s.inv_norm = 1.0 / ((double)((long long)p * (p + 1)) * 0.5);
+            ring_slots = p;
+            break;
+        case SK_SWMA:
+            if (p & 1) {
+                s.ka = s.kb = (p + 1) >> 1;
+            } else {
+                s.ka = p >> 1;
+                s.kb = s.ka + 1;
+            }
+            s.inv_norm = 1.0 / ((double)s.ka * (double)s.kb);
+            ring_slots = s.ka + s.kb;
+            break;
+        case SK_PWMA:
+            // 2^-(p-1) exactly (fast_pow2_neg_i32, pwma.rs:738-750); 0 below
+            // the subnormal range
+            s.inv_norm = std::ldexp(1.0, -(p - 1 > 2000 ? 2000 : p - 1));
+            ring_slots = p - 1;
+            break;
+        case SK_STDDEV:
+        case SK_ZSCORE:
+            s.nbdev = P("nbdev", 1.0);
+            if (kind == SK_STDDEV && !(std::isfinite(s.nbdev) && s.nbdev >= 0.0))
+                return fail(VTA_ERR_INVALID_INPUT, "streams: stddev nbdev must be finite and >= 0");
+            if (kind == SK_ZSCORE && (P("ma_type", 0.0) != 0.0 || P("devtype", 0.0) != 0.0))
+                return fail(VTA_ERR_NOT_IMPLEMENTED, "streams: zscore supports ma_type sma (0), devtype 0");
+            s.inv_p = 1.0 / (double)p;
+            ring_slots = p;
+            break;
+        case SK_BOLLINGER: {
+            s.devup = P("devup", 2.0);
+            s.devdn = P("devdn", 2.0);
+            const double mt = P("matype", 0.0);
+            if ((mt != 0.0 && mt != 1.0) || P("devtype", 0.0) != 0.0)
+                return fail(VTA_ERR_NOT_IMPLEMENTED,
+                            "streams: bollinger_bands supports matype sma (0) / ema (1), devtype 0");
+            s.ema_mid = mt == 1.0;
+            s.inv_p = 1.0 / (double)p;
+            s.alpha = 2.0 / ((double)p + 1.0);
+            s.beta = 1.0 - s.alpha;
+            ring_slots = p;
+            break;
+        }
+        case SK_DONCHIAN:
+        case SK_WILLR:
+            ring_slots = 2 * p;
+            break;
+        case SK_ADX:
+            s.inv_p = 1.0 / (double)p;
+            s.beta = 1.0 - s.inv_p;
+            break;
+        default: break;
     }
+    s.ring_slots = ring_slots;
+
+    auto* S = new vta_streams();
+    S->ctx = ctx;
     const size_t n = n_streams;
-    const bool ring = kind == SK_SMA || kind == SK_ALMA;
-    const size_t bytes = 3 * n * sizeof(int) + 5 * n * sizeof(double) + (ring ? (size_t)p * n * sizeof(double) : 0) +
-                         w.size() * sizeof(double) + 4 * n * sizeof(float) + 64 * 8;
+    const size_t bytes = kI * n * sizeof(int) + kD * n * sizeof(double) + (size_t)ring_slots * n * sizeof(double) +
+                         w.size() * sizeof(double) + (3 + (size_t)info.n_out) * n * sizeof(float) + 64 * 24;
     vta_status st = vram_check(bytes);
     if (st == VTA_OK) {
         const cudaError_t e = cudaMalloc(&S->block, bytes);
@@ -354,22 +920,17 @@ vta_status vta_streams_create(vta_ctx* ctx, const char* indicator, const char* c
         q += (b + 63) & ~size_t(63);
         return r;
     };
-    s.d0 = reinterpret_cast<double*>(take(n * sizeof(double)));
-    s.d1 = reinterpret_cast<double*>(take(n * sizeof(double)));
-    s.d2 = reinterpret_cast<double*>(take(n * sizeof(double)));
-    s.d3 = reinterpret_cast<double*>(take(n * sizeof(double)));
-    s.d4 = reinterpret_cast<double*>(take(n * sizeof(double)));
-    s.ring = ring ? reinterpret_cast<double*>(take((size_t)p * n * sizeof(double))) : nullptr;
+    for (int k = 0; k < kD; ++k) s.d[k] = reinterpret_cast<double*>(take(n * sizeof(double)));
+    s.ring = ring_slots ? reinterpret_cast<double*>(take((size_t)ring_slots * n * sizeof(double))) : nullptr;
     double* dw = w.empty() ? nullptr : reinterpret_cast<double*>(take(w.size() * sizeof(double)));
     s.w = dw;
-    s.i0 = reinterpret_cast<int*>(take(n * sizeof(int)));
-    s.i1 = reinterpret_cast<int*>(take(n * sizeof(int)));
-    s.i2 = reinterpret_cast<int*>(take(n * sizeof(int)));
-    S->d_io = reinterpret_cast<float*>(take(4 * n * sizeof(float)));
+    for (int k = 0; k < kI; ++k) s.iv[k] = reinterpret_cast<int*>(take(n * sizeof(int)));
+    S->d_io = reinterpret_cast<float*>(take((3 + (size_t)info.n_out) * n * sizeof(float)));
+    S->s = s;
     cudaStream_t cs = ctx->stream;
     if (dw) st = upload_async(ctx, dw, w.data(), w.size() * sizeof(double), cs);
     if (st == VTA_OK) {
-        k_stream_init<<<ceil_div(n, 256), 256, 0, cs>>>(s);
+        k_stream_init<<<ceil_div(n, 256), 256, 0, cs>>>(S->s);
         st = check_launch("k_stream_init");
     }
     if (st == VTA_OK) {
@@ -385,11 +946,18 @@ vta_status vta_streams_create(vta_ctx* ctx, const char* indicator, const char* c
     return VTA_OK;
 }
 
+vta_status vta_streams_shape(const vta_streams* S, int* n_inputs, int* n_outputs) {
+    if (!S) return fail(VTA_ERR_INVALID_INPUT, "streams: null handle");
+    if (n_inputs) *n_inputs = kKinds[S->s.kind].n_in;
+    if (n_outputs) *n_outputs = S->s.n_out;
+    return VTA_OK;
+}
+
 vta_status vta_streams_update_device(vta_streams* S, const float* d_a, const float* d_b, const float* d_c,
                                      float* d_out) {
     if (!S) return fail(VTA_ERR_INVALID_INPUT, "streams: null handle");
     VTA_TRY(enter_call(S->ctx));
-    if (!d_a || !d_out || (S->s.kind == SK_ATR && (!d_b || !d_c)))
+    if (!inputs_ok(S, d_a, d_b, d_c) || !d_out)
         return fail(VTA_ERR_INVALID_INPUT, "streams: null input/output pointer");
     VTA_TRY(enqueue_update(S, d_a, d_b, d_c, d_out));
     VTA_CUDA_TRY(cudaStreamSynchronize(S->ctx->stream));
@@ -399,21 +967,19 @@ vta_status vta_streams_update_device(vta_streams* S, const float* d_a, const flo
 vta_status vta_streams_update_host(vta_streams* S, const float* a, const float* b, const float* c, float* out) {
     if (!S) return fail(VTA_ERR_INVALID_INPUT, "streams: null handle");
     VTA_TRY(enter_call(S->ctx));
-    if (!a || !out || (S->s.kind == SK_ATR && (!b || !c)))
-        return fail(VTA_ERR_INVALID_INPUT, "streams: null input/output pointer");
+    if (!inputs_ok(S, a, b, c) || !out) return fail(VTA_ERR_INVALID_INPUT, "streams: null input/output pointer");
     const size_t n = (size_t)S->s.n;
+    const int n_in = kKinds[S->s.kind].n_in;
     cudaStream_t cs = S->ctx->stream;
     float* da = S->d_io;
     float* db = da + n;
     float* dc = db + n;
     float* dout = dc + n;
     VTA_TRY(upload_async(S->ctx, da, a, n * sizeof(float), cs));
-    if (S->s.kind == SK_ATR) {
-        VTA_TRY(upload_async(S->ctx, db, b, n * sizeof(float), cs));
-        VTA_TRY(upload_async(S->ctx, dc, c, n * sizeof(float), cs));
-    }
+    if (n_in >= 2) VTA_TRY(upload_async(S->ctx, db, b, n * sizeof(float), cs));
+    if (n_in >= 3) VTA_TRY(upload_async(S->ctx, dc, c, n * sizeof(float), cs));
     VTA_TRY(enqueue_update(S, da, db, dc, dout));
-    VTA_CUDA_TRY(cudaMemcpyAsync(out, dout, n * sizeof(float), cudaMemcpyDeviceToHost, cs));
+    VTA_CUDA_TRY(cudaMemcpyAsync(out, dout, (size_t)S->s.n_out * n * sizeof(float), cudaMemcpyDeviceToHost, cs));
     VTA_CUDA_TRY(cudaStreamSynchronize(cs));
     return check_launch("stream");
 }

@@ -488,27 +488,51 @@ class CudaMaSelector:
 class StreamBank:
     """n_streams streams of one indicator on the device, advanced together one
     bar per update, each as the crate's XStream (EmaStream, SmaStream,
-    AlmaStream, RsiStream, AtrStream, WildersStream).  update() returns the
-    n_streams new values, NaN where the crate's update() returns None."""
+    AlmaStream, RsiStream, AtrStream, WildersStream, DemaStream, TemaStream,
+    WmaStream, SwmaStream, PwmaStream, StdDevStream, ZscoreStream,
+    BollingerBandsStream, DonchianStream, WillrStream, AdxStream,
+    SuperTrendStream).  update() takes one array of n_streams values per input
+    (value; Donchian high, low; ATR / WillR / ADX / SuperTrend high, low,
+    close) and returns the n_streams new values, NaN where the crate's
+    update() returns None; several outputs (Bollinger and Donchian upper /
+    middle / lower, SuperTrend trend / changed) come as an
+    [n_outputs][n_streams] array.  String parameters take the crate's names:
+    Bollinger matype "sma" / "ema", Z-score ma_type "sma"."""
+
+    _CODES = {"matype": {"sma": 0.0, "ema": 1.0}, "ma_type": {"sma": 0.0}}
 
     def __init__(self, indicator: str, n_streams: int, params=None, device_id: int = 0,
                  ctx: "Context | None" = None):
         self.ctx = ctx if ctx is not None else Context(device_id)
         self.indicator, self.n = indicator, int(n_streams)
-        keys, vals, n = _kv(params)
+        prm = {}
+        for k, v in dict(params or {}).items():
+            if isinstance(v, str):
+                codes = self._CODES.get(k, {})
+                if v.lower() not in codes:
+                    raise RuntimeError(f"streams: {k}={v!r} has no streaming kernel")
+                v = codes[v.lower()]
+            prm[k] = v
+        keys, vals, n = _kv(prm)
         h = C.c_void_p()
         N.check(N.lib().vta_streams_create(self.ctx.handle, indicator.encode(), keys, vals, n, self.n, C.byref(h)))
         self._h = h
+        ni, no = C.c_int(), C.c_int()
+        N.check(N.lib().vta_streams_shape(self._h, C.byref(ni), C.byref(no)))
+        self.n_inputs, self.n_outputs = ni.value, no.value
 
     def update(self, *bars) -> np.ndarray:
+        assert len(bars) == self.n_inputs, (self.indicator, len(bars))
         xs = [_f32(b) for b in bars]
         assert all(x.size == self.n for x in xs)
-        out = np.empty(self.n, dtype=np.float32)
+        out = np.empty((self.n_outputs, self.n), dtype=np.float32)
         ptrs = [x.ctypes.data for x in xs] + [None] * (3 - len(xs))
         N.check(N.lib().vta_streams_update_host(self._h, *ptrs, out.ctypes.data))
-        return out
+        return out[0] if self.n_outputs == 1 else out
 
     def update_device(self, *d_bars, d_out):
+        """d_out: n_outputs x n_streams f32 on the device."""
+        assert len(d_bars) == self.n_inputs, (self.indicator, len(d_bars))
         ptrs = [_dptr(b) for b in d_bars] + [None] * (3 - len(d_bars))
         N.check(N.lib().vta_streams_update_device(self._h, *ptrs, _dptr(d_out)))
 
