@@ -116,6 +116,15 @@ def lib():
             "vto_willr_stream": ([dp, dp, dp, sz, sz, dp], ip),
             "vto_adx_stream": ([dp, dp, dp, sz, sz, dp], ip),
             "vto_supertrend_stream": ([dp, dp, dp, sz, sz, db, dp, dp], ip),
+            "vto_sinwma_stream": ([dp, sz, sz, dp], ip),
+            "vto_trima_stream": ([dp, sz, sz, dp], ip),
+            "vto_cwma_stream": ([dp, sz, sz, dp], ip),
+            "vto_fwma_stream": ([dp, sz, sz, dp], ip),
+            "vto_srwma_stream": ([dp, sz, sz, dp], ip),
+            "vto_sqwma_stream": ([dp, sz, sz, dp], ip),
+            "vto_epma_stream": ([dp, sz, sz, sz, dp], ip),
+            "vto_vpwma_stream": ([dp, sz, sz, db, dp], ip),
+            "vto_percentile_nearest_rank_stream": ([dp, sz, sz, db, dp], ip),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -272,6 +281,15 @@ STREAMS = {
     "willr": (3, 1, {"period": 14}),
     "adx": (3, 1, {"period": 14}),
     "supertrend": (3, 2, {"period": 10, "factor": 3.0}),
+    "sinwma": (1, 1, {"period": 14}),
+    "trima": (1, 1, {"period": 30}),
+    "cwma": (1, 1, {"period": 14}),
+    "fwma": (1, 1, {"period": 5}),
+    "srwma": (1, 1, {"period": 14}),
+    "sqwma": (1, 1, {"period": 14}),
+    "epma": (1, 1, {"period": 11, "offset": 4}),
+    "vpwma": (1, 1, {"period": 14, "power": 0.382}),
+    "percentile_nearest_rank": (1, 1, {"length": 15, "percentage": 50.0}),
 }
 
 
@@ -300,6 +318,12 @@ def stream(name, inputs, **prm):
         code = L.vto_bollinger_stream(P[0], n, int(q["period"]), float(q["devup"]), float(q["devdn"]), mt, *O_)
     elif name == "donchian":
         code = L.vto_donchian_stream(*P, n, int(q["period"]), *O_)
+    elif name == "epma":
+        code = L.vto_epma_stream(P[0], n, int(q["period"]), int(q["offset"]), O_[0])
+    elif name == "vpwma":
+        code = L.vto_vpwma_stream(P[0], n, int(q["period"]), float(q["power"]), O_[0])
+    elif name == "percentile_nearest_rank":
+        code = L.vto_percentile_nearest_rank_stream(P[0], n, int(q["length"]), float(q["percentage"]), O_[0])
     elif name == "supertrend":
         code = L.vto_supertrend_stream(*P, n, int(q["period"]), float(q["factor"]), *O_)
     elif n_in == 3:

@@ -2155,6 +2155,479 @@ int vto_supertrend_stream(const double *h, const double *l, const double *c, siz
     return VTO_OK;
 }
 
+/* SinWmaStream (sinwma.rs:586-750): sine weights through the rotation
+ * z = sum_j r^j x_(newest - j), r = e^(i alpha), alpha = pi / (p + 1):
+ * rebuilt from the ring (mul_add chain) when the window becomes NaN-free,
+ * then advanced in O(1): z' = r z + x_new - r^p x_old; output
+ * mul_add(sin(p alpha), Re z, -cos(p alpha) Im z) / sum of sines.
+ * Constants with the C library's sin / cos, as the crate's try_new. */
+static void sinwma_rebuild(const double *buf, size_t p, size_t head, double r_re, double r_im, double *zr,
+                           double *zi) {
+    size_t newest = (head + p - 1) % p;
+    double rj_re = 1.0, rj_im = 0.0, a = 0.0, b = 0.0;
+    for (size_t j = 0; j < p; j++) {
+        double xv = buf[(newest + p - j) % p];
+        a = fma(rj_re, xv, a);
+        b = fma(rj_im, xv, b);
+        double nr = fma(rj_re, r_re, -rj_im * r_im);
+        double ni = fma(rj_re, r_im, rj_im * r_re);
+        rj_re = nr;
+        rj_im = ni;
+    }
+    *zr = a;
+    *zi = b;
+}
+
+int vto_sinwma_stream(const double *x, size_t n, size_t period, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    const double pi = 3.14159265358979323846;
+    const double alpha = pi / ((double)period + 1.0);
+    const double sina = sin(alpha), cosa = cos(alpha);
+    const double sinp = sin(alpha * (double)period), cosp = cos(alpha * (double)period);
+    const double denom = sin(0.5 * alpha);
+    if (fabs(denom) < 2.220446049250313e-16) return VTO_E_INVALID_PARAM;
+    const double sum_sines = sin(0.5 * alpha * (double)period) / denom;
+    if (fabs(sum_sines) < 2.220446049250313e-16) return VTO_E_INVALID_PARAM;
+    const double inv_sum = 1.0 / sum_sines;
+    double *buf = (double *)malloc(sizeof(double) * period);
+    for (size_t i = 0; i < period; i++) buf[i] = QNAN;
+    size_t head = 0, nanc = period;
+    int filled = 0, zvalid = 0;
+    double zr = 0.0, zi = 0.0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        out[t] = QNAN;
+        double old = buf[head];
+        buf[head] = v;
+        head = (head + 1) % period;
+        if (isnan(old) && nanc > 0) nanc--;
+        if (isnan(v)) nanc++;
+        if (!filled) {
+            if (head != 0) continue;
+            filled = 1;
+            if (nanc != 0) { zvalid = 0; continue; }
+            sinwma_rebuild(buf, period, head, cosa, sina, &zr, &zi);
+            zvalid = 1;
+        } else {
+            if (nanc != 0) { zvalid = 0; continue; }
+            if (!zvalid) {
+                sinwma_rebuild(buf, period, head, cosa, sina, &zr, &zi);
+                zvalid = 1;
+            } else {
+                double rr = fma(cosa, zr, -sina * zi);
+                double ri = fma(cosa, zi, sina * zr);
+                zr = rr + v - cosp * old;
+                zi = ri - sinp * old;
+            }
+        }
+        out[t] = fma(sinp, zr, -cosp * zi) * inv_sum;
+    }
+    free(buf);
+    return VTO_OK;
+}
+
+/* TrimaStream (trima.rs:826-905): SMA(m1) of the values (NaN values left out
+ * of the running sum), then SMA(m2) of those means, m1 = (p + 1) / 2,
+ * m2 = p - m1 + 1; period > 3. */
+int vto_trima_stream(const double *x, size_t n, size_t period, double *out) {
+    if (period <= 3) return VTO_E_INVALID_PERIOD;
+    const size_t m1 = (period + 1) / 2, m2 = period - m1 + 1;
+    const double inv1 = 1.0 / (double)m1, inv2 = 1.0 / (double)m2;
+    double *b1 = (double *)malloc(sizeof(double) * m1), *b2 = (double *)malloc(sizeof(double) * m2);
+    for (size_t i = 0; i < m1; i++) b1[i] = QNAN;
+    for (size_t i = 0; i < m2; i++) b2[i] = QNAN;
+    size_t h1 = 0, h2 = 0;
+    int f1 = 0, f2 = 0;
+    double s1 = 0.0, s2 = 0.0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        out[t] = QNAN;
+        double o1 = b1[h1];
+        b1[h1] = v;
+        if (++h1 == m1) { h1 = 0; f1 = 1; }
+        if (!isnan(o1)) s1 -= o1;
+        if (!isnan(v)) s1 += v;
+        if (!f1) continue;
+        double mean1 = s1 * inv1;
+        double o2 = b2[h2];
+        b2[h2] = mean1;
+        if (++h2 == m2) { h2 = 0; f2 = 1; }
+        if (!isnan(o2)) s2 -= o2;
+        s2 += mean1;
+        if (f2) out[t] = s2 * inv2;
+    }
+    free(b1);
+    free(b2);
+    return VTO_OK;
+}
+
+/* CwmaStream (cwma.rs:792-1040): leading NaNs are skipped; a ring of the last
+ * n = p - 1 values; the first n values give None, then NaN while the window
+ * holds a NaN, else the direct sum (sum_weighted: mul_add chain newest
+ * first, weights (p + 1 - r)^3, r = 1..n) over sum_{j=2..p} j^3.  The
+ * crate's running moments do not enter the output. */
+int vto_cwma_stream(const double *x, size_t n, size_t period, double *out) {
+    if (period <= 1) return VTO_E_INVALID_PERIOD;
+    const size_t m = period - 1;
+    double norm = 0.0;
+    for (size_t j = 2; j <= period; j++) {
+        double jf = (double)j;
+        norm += jf * jf * jf;
+    }
+    const double inv_norm = 1.0 / norm, a = (double)(m + 2);
+    double *ring = (double *)malloc(sizeof(double) * m);
+    for (size_t i = 0; i < m; i++) ring[i] = QNAN;
+    size_t head = 0, filled = 0, nanc = 0;
+    int found = 0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        out[t] = QNAN;
+        if (!found) {
+            if (isnan(v)) continue;
+            found = 1;
+        }
+        double old = filled >= m ? ring[head] : QNAN;
+        size_t new_nan = isnan(v) ? 1 : 0, old_nan = (filled >= m && isnan(old)) ? 1 : 0;
+        ring[head] = v;
+        head = (head + 1) % m;
+        if (filled <= m) {
+            filled++;
+            nanc += new_nan;
+            if (filled == m + 1) nanc -= old_nan;
+            if (filled <= m) continue;
+        } else {
+            nanc = nanc + new_nan - old_nan;
+        }
+        if (nanc > 0) continue;
+        double s = 0.0;
+        for (size_t r = 1; r <= m; r++) {
+            double tv = a - (double)r;
+            s = fma(ring[(head + m - r) % m], tv * tv * tv, s);
+        }
+        out[t] = s * inv_norm;
+    }
+    free(ring);
+    return VTO_OK;
+}
+
+/* FwmaStream (fwma.rs:750-890): Fibonacci weights 1, 1, 2, 3, ... divided
+ * by their sum; once `period` values were seen, NaN while the window holds
+ * a NaN, else the dot of the window (oldest first) with the weights. */
+int vto_fwma_stream(const double *x, size_t n, size_t period, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    double *w = (double *)malloc(sizeof(double) * period), *buf = (double *)malloc(sizeof(double) * period);
+    for (size_t i = 0; i < period; i++) { w[i] = 1.0; buf[i] = QNAN; }
+    for (size_t i = 2; i < period; i++) w[i] = w[i - 1] + w[i - 2];
+    double sum = 0.0;
+    for (size_t i = 0; i < period; i++) sum += w[i];
+    for (size_t i = 0; i < period; i++) w[i] /= sum;
+    size_t head = 0, nanc = 0;
+    int filled = 0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        out[t] = QNAN;
+        double old = buf[head];
+        if (filled && isnan(old) && nanc > 0) nanc--;
+        buf[head] = v;
+        if (isnan(v)) nanc++;
+        head = head + 1 == period ? 0 : head + 1;
+        if (!filled) {
+            if (head != 0) continue;
+            filled = 1;
+        }
+        if (nanc != 0) continue;
+        double s = 0.0;
+        size_t idx = head;
+        for (size_t j = 0; j < period; j++) {
+            s += w[j] * buf[idx];
+            idx = idx + 1 == period ? 0 : idx + 1;
+        }
+        out[t] = s;
+    }
+    free(w);
+    free(buf);
+    return VTO_OK;
+}
+
+/* SrwmaStream (srwma.rs:1183-1290): weights sqrt(p - k), k = 0..p-2, newest
+ * first; output once more than p + 1 values were seen: four mul_add
+ * accumulators over blocks of 4, the tail into the first, times 1 / sum of
+ * weights.  Period 1 passes the value through after two bars. */
+int vto_srwma_stream(const double *x, size_t n, size_t period, double *out) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    const size_t m = period - 1;
+    double *w = (double *)malloc(sizeof(double) * (m ? m : 1)), *ring = (double *)calloc(m ? m : 1, sizeof(double));
+    double sumw = 0.0;
+    for (size_t k = 0; k < m; k++) { w[k] = sqrt((double)(period - k)); sumw += w[k]; }
+    const double inv = sumw == 0.0 ? 0.0 : 1.0 / sumw;
+    size_t head = 0, count = 0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        out[t] = QNAN;
+        count++;
+        if (m == 0) { if (count > period + 1) out[t] = v; continue; }
+        ring[head] = v;
+        head = head + 1 == m ? 0 : head + 1;
+        if (count <= period + 1) continue;
+        double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+        size_t k = 0;
+        /* newest first: ring[(head - 1 - k) mod m] */
+        for (; k + 4 <= m; k += 4) {
+            s0 = fma(ring[(head + 2 * m - 1 - k) % m], w[k], s0);
+            s1 = fma(ring[(head + 2 * m - 2 - k) % m], w[k + 1], s1);
+            s2 = fma(ring[(head + 2 * m - 3 - k) % m], w[k + 2], s2);
+            s3 = fma(ring[(head + 2 * m - 4 - k) % m], w[k + 3], s3);
+        }
+        for (; k < m; k++) s0 = fma(ring[(head + 2 * m - 1 - k) % m], w[k], s0);
+        out[t] = ((s0 + s1) + (s2 + s3)) * inv;
+    }
+    free(w);
+    free(ring);
+    return VTO_OK;
+}
+
+/* SqwmaStream (sqwma.rs:360-545): weights (p - i)^2, i = 0..p-2, newest
+ * first; output once p + 2 values were seen; REBASE_MASK = 0 rebuilds the
+ * sum from the ring on every bar (one mul_add chain), so that sum is the
+ * output, times 1 / sum of weights. */
+int vto_sqwma_stream(const double *x, size_t n, size_t period, double *out) {
+    if (period < 2) return VTO_E_INVALID_PERIOD;
+    const size_t m = period - 1;
+    double *w = (double *)malloc(sizeof(double) * m), *ring = (double *)calloc(period, sizeof(double));
+    double ws = 0.0;
+    for (size_t i = 0; i < m; i++) { double d = (double)period - (double)i; w[i] = d * d; ws += w[i]; }
+    const double inv = 1.0 / ws;
+    size_t head = 0, count = 0;
+    for (size_t t = 0; t < n; t++) {
+        out[t] = QNAN;
+        ring[head] = x[t];
+        head = head + 1 == period ? 0 : head + 1;
+        count++;
+        if (count < period + 2) continue;
+        double r = 0.0;
+        for (size_t i = 0; i < m; i++) r = fma(ring[(head + period - 1 - i) % period], w[i], r);
+        out[t] = r * inv;
+    }
+    free(w);
+    free(ring);
+    return VTO_OK;
+}
+
+/* EpmaStream (epma.rs:635-735): Kahan-compensated running sum and ramp of
+ * the last p - 1 values; during the first p + offset + 1 bars update()
+ * returns the value itself; then mul_add(c0, sum, ramp) / wsum with
+ * c0 = 2 - offset, wsum = mul_add(p - 1, c0, (p - 2)(p - 1) / 2). */
+static void kahan(double *s, double *c, double v) {
+    double y = v - *c;
+    double t = *s + y;
+    *c = (t - *s) - y;
+    *s = t;
+}
+
+int vto_epma_stream(const double *x, size_t n, size_t period, size_t offset, double *out) {
+    if (period < 2) return VTO_E_INVALID_PERIOD;
+    if (offset >= period) return VTO_E_INVALID_PARAM;
+    const size_t p1 = period - 1;
+    const double c0 = 2.0 - (double)offset, p1f = (double)p1, p1m1 = (double)(p1 - 1);
+    const double inv_wsum = 1.0 / fma(p1f, c0, 0.5 * (p1f - 1.0) * p1f);
+    double *buf = (double *)calloc(period, sizeof(double));
+    size_t head = 0, seen = 0, inc = 0;
+    double sum = 0.0, sc = 0.0, ramp = 0.0, rc = 0.0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        double xo = inc == p1 ? buf[(head + 1) % period] : 0.0;
+        buf[head] = v;
+        head = (head + 1) % period;
+        seen++;
+        if (inc < p1) {
+            double mm = (double)inc;
+            kahan(&sum, &sc, v);
+            kahan(&ramp, &rc, mm * v);
+            inc++;
+        } else {
+            double s_old = sum;
+            kahan(&sum, &sc, v - xo);
+            kahan(&ramp, &rc, fma(p1m1, v, xo - s_old));
+        }
+        out[t] = seen <= period + offset + 1 ? v : fma(c0, sum, ramp) * inv_wsum;
+    }
+    free(buf);
+    return VTO_OK;
+}
+
+/* VpwmaStream (vpwma.rs:583-884): weights (p - k)^power, k = 0..p-2, newest
+ * first, over 1 / their sum; output once p values were seen.  A power within
+ * 1e-12 of an integer deg in 0..8 runs the crate's PolyInt mode: moments
+ * m_j = sum k^j x (k = age, 0 newest) built from the ring on the first
+ * output, then shifted each bar by binomial sums, output dot(coeff, m) with
+ * coeff_j = (-1)^j C(deg, j) p^(deg - j); any other power the ExactDot mode:
+ * the window oldest first against the reversed weights as two ring segments,
+ * each with four mul_add accumulators.  Integer powers of p by binary
+ * exponentiation (the LLVM runtime's powi). */
+static double powi_bin(double a, int b) {
+    double r = 1.0;
+    for (;;) {
+        if (b & 1) r *= a;
+        b /= 2;
+        if (b == 0) break;
+        a *= a;
+    }
+    return r;
+}
+
+static double binom_f(size_t n, size_t k) {
+    if (k == 0 || k == n) return 1.0;
+    if (k > n - k) k = n - k;
+    unsigned long long num = 1, den = 1;
+    for (size_t i = 1; i <= k; i++) { num *= (unsigned long long)(n + 1 - i); den *= (unsigned long long)i; }
+    return (double)num / (double)den;
+}
+
+static double dot4(const double *a, const double *b, size_t n) {
+    double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    size_t i = 0, p4 = n & ~(size_t)3;
+    for (; i < p4; i += 4) {
+        s0 = fma(a[i], b[i], s0);
+        s1 = fma(a[i + 1], b[i + 1], s1);
+        s2 = fma(a[i + 2], b[i + 2], s2);
+        s3 = fma(a[i + 3], b[i + 3], s3);
+    }
+    for (; i < n; i++) s0 = fma(a[i], b[i], s0);
+    return (s0 + s1) + (s2 + s3);
+}
+
+int vto_vpwma_stream(const double *x, size_t n, size_t period, double power, double *out) {
+    if (period < 2) return VTO_E_INVALID_PERIOD;
+    if (isnan(power) || isinf(power)) return VTO_E_INVALID_PARAM;
+    const size_t m = period - 1;
+    double *w = (double *)malloc(sizeof(double) * m), *buf = (double *)malloc(sizeof(double) * period);
+    double norm = 0.0;
+    for (size_t k = 0; k < m; k++) { w[k] = pow((double)period - (double)k, power); norm += w[k]; }
+    const double inv_norm = 1.0 / norm;
+    for (size_t i = 0; i < period; i++) buf[i] = QNAN;
+    const double pr = round(power);
+    const int poly = fabs(power - pr) <= 1e-12 && pr >= 0.0 && pr <= 8.0;
+    const size_t deg = poly ? (size_t)pr : 0;
+    double coeff[9], bv[45], pm1[9], mom[9], nxt[9];
+    size_t rs[10];
+    if (poly) {
+        for (size_t j = 0; j <= deg; j++)
+            coeff[j] = ((j & 1) ? -1.0 : 1.0) * binom_f(deg, j) * powi_bin((double)period, (int)(deg - j));
+        size_t c = 0;
+        for (size_t j = 0; j <= deg; j++) {
+            rs[j] = c;
+            for (size_t q = 0; q <= j; q++) bv[c++] = binom_f(j, q);
+        }
+        double pp = 1.0, mm1 = (double)(m - 1);
+        for (size_t q = 0; q <= deg; q++) { pm1[q] = pp; pp *= mm1; }
+    }
+    size_t head = 0;
+    int filled = 0, ready = 0;
+    for (size_t t = 0; t < n; t++) {
+        double v = x[t];
+        out[t] = QNAN;
+        buf[head] = v;
+        head = (head + 1) % period;
+        if (!filled && head == 0) filled = 1;
+        if (!filled) continue;
+        const size_t oldest = (head + 1) % period;
+        const size_t left = period - oldest < m ? period - oldest : m, right = m - left;
+        if (poly) {
+            double xo = buf[head];
+            if (!ready) {
+                for (size_t j = 0; j <= deg; j++) mom[j] = 0.0;
+                for (size_t pos = 0; pos < left; pos++) {
+                    double xv = buf[oldest + pos], kk = (double)(m - 1 - pos), kp = 1.0;
+                    for (size_t j = 0; j <= deg; j++) { mom[j] += kp * xv; kp *= kk; }
+                }
+                for (size_t pos = 0; pos < right; pos++) {
+                    double xv = buf[pos], kk = (double)(right - 1 - pos), kp = 1.0;
+                    for (size_t j = 0; j <= deg; j++) { mom[j] += kp * xv; kp *= kk; }
+                }
+                ready = 1;
+            } else {
+                nxt[0] = mom[0] + v - xo;
+                for (size_t j = 1; j <= deg; j++) {
+                    double s = 0.0;
+                    for (size_t q = 0; q <= j; q++) s += bv[rs[j] + q] * (mom[q] - pm1[q] * xo);
+                    nxt[j] = s;
+                }
+                for (size_t j = 0; j <= deg; j++) mom[j] = nxt[j];
+            }
+            out[t] = dot4(coeff, mom, deg + 1) * inv_norm;
+        } else {
+            /* weights_rev[i] = w[m - 1 - i] */
+            double s0 = 0, s1 = 0, s2 = 0, s3 = 0, sum;
+            size_t k = 0, p4 = left & ~(size_t)3;
+            for (; k < p4; k += 4) {
+                s0 = fma(buf[oldest + k], w[m - 1 - k], s0);
+                s1 = fma(buf[oldest + k + 1], w[m - 2 - k], s1);
+                s2 = fma(buf[oldest + k + 2], w[m - 3 - k], s2);
+                s3 = fma(buf[oldest + k + 3], w[m - 4 - k], s3);
+            }
+            for (; k < left; k++) s0 = fma(buf[oldest + k], w[m - 1 - k], s0);
+            sum = (s0 + s1) + (s2 + s3);
+            if (right) {
+                s0 = s1 = s2 = s3 = 0;
+                k = 0;
+                p4 = right & ~(size_t)3;
+                for (; k < p4; k += 4) {
+                    s0 = fma(buf[k], w[m - 1 - (left + k)], s0);
+                    s1 = fma(buf[k + 1], w[m - 2 - (left + k)], s1);
+                    s2 = fma(buf[k + 2], w[m - 3 - (left + k)], s2);
+                    s3 = fma(buf[k + 3], w[m - 4 - (left + k)], s3);
+                }
+                for (; k < right; k++) s0 = fma(buf[k], w[m - 1 - (left + k)], s0);
+                sum += (s0 + s1) + (s2 + s3);
+            }
+            out[t] = sum * inv_norm;
+        }
+    }
+    free(w);
+    free(buf);
+    return VTO_OK;
+}
+
+/* PercentileNearestRankStream (percentile_nearest_rank.rs:468-665): two
+ * heaps with lazy deletion keep the window's valid (non-NaN) values split at
+ * the target rank; the output is the left heap's top, i.e. the k-th smallest
+ * valid value, k = nearest_rank(p / 100, valid) + 1 with
+ * nearest_rank(f, n) = clamp(trunc(mul_add(f, n, 0.5)) - 1, 0, n - 1);
+ * NaN when the window has no valid value.  Restated here by sorting. */
+static int cmp_d(const void *a, const void *b) {
+    double x = *(const double *)a, y = *(const double *)b;
+    return x < y ? -1 : x > y ? 1 : 0;
+}
+
+int vto_percentile_nearest_rank_stream(const double *x, size_t n, size_t length, double percentage, double *out) {
+    if (length == 0) return VTO_E_INVALID_PERIOD;
+    if (!(percentage >= 0.0 && percentage <= 100.0)) return VTO_E_INVALID_PARAM;
+    const double pf = percentage * 0.01;
+    double *buf = (double *)malloc(sizeof(double) * length), *tmp = (double *)malloc(sizeof(double) * length);
+    for (size_t i = 0; i < length; i++) buf[i] = QNAN;
+    size_t head = 0;
+    int filled = 0;
+    for (size_t t = 0; t < n; t++) {
+        out[t] = QNAN;
+        buf[head] = x[t];
+        head = (head + 1) % length;
+        if (!filled && head == 0) filled = 1;
+        if (!filled) continue;
+        size_t valid = 0;
+        for (size_t i = 0; i < length; i++)
+            if (!isnan(buf[i])) tmp[valid++] = buf[i];
+        if (valid == 0) continue;
+        double kf = fma(pf, (double)valid, 0.5);
+        size_t k = kf > 0.0 ? (size_t)kf : 0;
+        k = k == 0 ? 0 : (k - 1 >= valid ? valid - 1 : k - 1);
+        qsort(tmp, valid, sizeof(double), cmp_d);
+        out[t] = tmp[k];
+    }
+    free(buf);
+    free(tmp);
+    return VTO_OK;
+}
+
 /* vpwma_with_kernel (vpwma.rs:215-290): weights (p - k)^power, k < p - 1
  * (newest first), inv_norm = 1 / sum, first output first + p - 1;
  * vpwma_scalar (vpwma.rs:296-360): four mul_add accumulators, two rounds per

@@ -44,6 +44,13 @@ CASES = [
     ("bollinger_bands", {"period": 12, "matype": "ema"}),
     ("donchian", {"period": 20}), ("willr", {"period": 14}), ("adx", {"period": 14}),
     ("supertrend", {"period": 10, "factor": 3.0}),
+    ("sinwma", {"period": 14}), ("trima", {"period": 30}), ("trima", {"period": 9}),
+    ("cwma", {"period": 14}), ("fwma", {"period": 5}), ("srwma", {"period": 14}), ("srwma", {"period": 1}),
+    ("sqwma", {"period": 14}), ("epma", {"period": 11, "offset": 4}), ("epma", {"period": 20, "offset": 0}),
+    ("vpwma", {"period": 14, "power": 0.382}), ("vpwma", {"period": 10, "power": 2.0}),
+    ("vpwma", {"period": 9, "power": 0.0}), ("vpwma", {"period": 30, "power": 5.0}),
+    ("percentile_nearest_rank", {"length": 15, "percentage": 50.0}),
+    ("percentile_nearest_rank", {"length": 20, "percentage": 90.0}),
 ]
 
 
@@ -101,3 +108,9 @@ def test_stream_bank_rejects_unknown_and_bad_params():
         V.StreamBank("bollinger_bands", 4, {"matype": "wma"})
     with pytest.raises(RuntimeError):
         V.StreamBank("zscore", 4, {"devtype": 1})
+    with pytest.raises(RuntimeError):
+        V.StreamBank("trima", 4, {"period": 3})
+    with pytest.raises(RuntimeError):
+        V.StreamBank("epma", 4, {"period": 5, "offset": 5})
+    with pytest.raises(RuntimeError):
+        V.StreamBank("percentile_nearest_rank", 4, {"percentage": 101.0})

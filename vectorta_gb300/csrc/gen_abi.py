@@ -202,15 +202,22 @@ vta_status vta_ma_select_into_host_f32(vta_ctx* ctx, const char* ma_type, const 
  * PwmaStream pwma.rs:675-720, StdDevStream stddev.rs:451-570, ZscoreStream
  * zscore.rs:567-780, BollingerBandsStream bollinger_bands.rs:884-1075,
  * DonchianStream donchian.rs:1251-1340, WillrStream willr.rs:1657-1820,
- * AdxStream adx.rs:1949-2085, SuperTrendStream supertrend.rs:798-885), f64
+ * AdxStream adx.rs:1949-2085, SuperTrendStream supertrend.rs:798-885,
+ * SinWmaStream sinwma.rs:586-750, TrimaStream trima.rs:826-905, CwmaStream
+ * cwma.rs:792-1040, FwmaStream fwma.rs:750-890, SrwmaStream
+ * srwma.rs:1183-1290, SqwmaStream sqwma.rs:360-545, EpmaStream
+ * epma.rs:635-735, VpwmaStream vpwma.rs:583-884,
+ * PercentileNearestRankStream percentile_nearest_rank.rs:468-700), f64
  * state, f32 in and out; outputs are NaN where update() returns None.
  * indicator: "ema" "sma" "alma" "rsi" "atr" "wilders" "dema" "tema" "wma"
  * "swma" "pwma" "stddev" "zscore" "bollinger_bands" "donchian" "willr" "adx"
- * "supertrend".  Parameters as key/value pairs, the crate's defaults when
- * absent: "period" (ATR also "length"), ALMA "offset" / "sigma", StdDev and
- * Z-score "nbdev", Bollinger "devup" / "devdn" / "matype" (0 sma, 1 ema),
- * SuperTrend "factor"; Z-score takes ma_type sma, Bollinger and Z-score
- * devtype 0 (others: VTA_ERR_NOT_IMPLEMENTED).
+ * "supertrend" "sinwma" "trima" "cwma" "fwma" "srwma" "sqwma" "epma" "vpwma"
+ * "percentile_nearest_rank".  Parameters as key/value pairs, the crate's
+ * defaults when absent: "period" (ATR and percentile also "length"), ALMA
+ * "offset" / "sigma", StdDev and Z-score "nbdev", Bollinger "devup" /
+ * "devdn" / "matype" (0 sma, 1 ema), SuperTrend "factor", EPMA "offset",
+ * VPWMA "power", percentile "percentage"; Z-score takes ma_type sma,
+ * Bollinger and Z-score devtype 0 (others: VTA_ERR_NOT_IMPLEMENTED).
  * Inputs: one series in a (b, c NULL); Donchian (high, low) in (a, b); ATR,
  * WillR, ADX, SuperTrend (high, low, close).  Outputs: out holds n_outputs
  * rows of n_streams values: Bollinger and Donchian upper / middle / lower,

@@ -42,6 +42,15 @@ enum StreamKind {
     SK_WILLR,
     SK_ADX,
     SK_SUPERTREND,
+    SK_SINWMA,
+    SK_TRIMA,
+    SK_CWMA,
+    SK_FWMA,
+    SK_SRWMA,
+    SK_SQWMA,
+    SK_EPMA,
+    SK_VPWMA,
+    SK_PERCENTILE,
     SK_COUNT
 };
 
@@ -71,17 +80,34 @@ constexpr KindInfo kKinds[SK_COUNT] = {
     {"willr", 3, 1, 14},
     {"adx", 3, 1, 14},
     {"supertrend", 3, 2, 10},
+    {"sinwma", 1, 1, 14},
+    {"trima", 1, 1, 30},
+    {"cwma", 1, 1, 14},
+    {"fwma", 1, 1, 5},
+    {"srwma", 1, 1, 14},
+    {"sqwma", 1, 1, 14},
+    {"epma", 1, 1, 11},
+    {"vpwma", 1, 1, 14},
+    {"percentile_nearest_rank", 1, 1, 15},
 };
 
-constexpr int kD = 8, kI = 4;
+constexpr int kD = 10, kI = 4;
+
+// VPWMA integer-power constants in the weight array: coeff at 0, (m - 1)^q at
+// kVpPow, binomial row j at kVpBinom + j (j + 1) / 2
+constexpr int kVpPow = 9, kVpBinom = 18, kVpConsts = kVpBinom + 45;
 
 struct StreamState {
     int kind, n, period, n_out;
-    int ka, kb;   // SWMA box lengths
+    int ka, kb;   // SWMA box lengths; TRIMA m1, m2
+    int offset;   // EPMA offset
+    int deg;      // VPWMA: integer power (moment mode), -1 = exact dot
     int ema_mid;  // Bollinger: EMA middle band (else SMA)
     int ring_slots;
     double alpha, beta, inv_p, inv_norm;
     double nbdev, devup, devdn, factor;
+    double k[5];  // SINWMA cos a, sin a, cos pa, sin pa, 1 / sum of sines; EPMA c0, 1 / wsum,
+                  // p - 2; percentile p / 100
     const double* w;  // ALMA weights (device)
     double* d[kD];    // per-stream f64 state
     int* iv[kI];      // per-stream int state
@@ -116,11 +142,16 @@ __global__ void k_stream_init(StreamState s) {
             break;
         case SK_WILDERS: s.d[1][j] = nan; break;                       // last
         case SK_ADX: s.d[5][j] = s.d[6][j] = s.d[7][j] = nan; break;  // previous high, low, close
-        case SK_ZSCORE: s.iv[2][j] = s.period; break;                  // nan_count
+        case SK_ZSCORE:  // nan_count
+        case SK_SINWMA:
+            s.iv[2][j] = s.period;
+            break;
         default: break;
     }
     if (s.ring) {
-        const double fill = (s.kind == SK_SWMA || s.kind == SK_BOLLINGER) ? 0.0 : nan;
+        const bool zero = s.kind == SK_SWMA || s.kind == SK_BOLLINGER || s.kind == SK_SRWMA || s.kind == SK_SQWMA ||
+                          s.kind == SK_EPMA;
+        const double fill = zero ? 0.0 : nan;
         for (int k = 0; k < s.ring_slots; ++k) s.ring[(size_t)k * s.n + j] = fill;
     }
 }
@@ -703,6 +734,349 @@ __global__ void k_stream_update(StreamState s, const float* __restrict__ a, cons
                 y1 = ch;
             }
         }
+    } else if constexpr (K == SK_SINWMA) {
+        // SinWmaStream::update (sinwma.rs:654-718): z = sum_j r^j x(newest - j)
+        // with r = e^(i alpha); ring, i0 head, i1 filled, i2 nan_count (starts
+        // at p), i3 z_valid, d0 / d1 z.  Rebuilt from the ring when the window
+        // becomes NaN-free, else z' = r z + x_new - r^p x_old.
+        const double v = (double)a[j];
+        const double cosa = s.k[0], sina = s.k[1], cosp = s.k[2], sinp = s.k[3];
+        int head = IV(0);
+        const double old = RING(head);
+        RING(head) = v;
+        head = head + 1 == p ? 0 : head + 1;
+        IV(0) = head;
+        if (isnan(old) && IV(2) > 0) --IV(2);
+        if (isnan(v)) ++IV(2);
+        bool rebuild = false, emit = false;
+        if (!IV(1)) {
+            if (head == 0) {
+                IV(1) = 1;
+                if (IV(2) != 0) IV(3) = 0;
+                else rebuild = emit = true;
+            }
+        } else if (IV(2) != 0) {
+            IV(3) = 0;
+        } else if (!IV(3)) {
+            rebuild = emit = true;
+        } else {
+            const double zr = D(0), zi = D(1);
+            const double rr = fma(cosa, zr, dmul(-sina, zi));
+            const double ri = fma(cosa, zi, dmul(sina, zr));
+            D(0) = dsub(dadd(rr, v), dmul(cosp, old));
+            D(1) = dsub(ri, dmul(sinp, old));
+            emit = true;
+        }
+        if (rebuild) {
+            const int newest = head == 0 ? p - 1 : head - 1;
+            double rj_re = 1.0, rj_im = 0.0, zr = 0.0, zi = 0.0;
+            for (int q = 0; q < p; ++q) {
+                int idx = newest - q;
+                if (idx < 0) idx += p;
+                const double xv = RING(idx);
+                zr = fma(rj_re, xv, zr);
+                zi = fma(rj_im, xv, zi);
+                const double nr = fma(rj_re, cosa, dmul(-rj_im, sina));
+                const double ni = fma(rj_re, sina, dmul(rj_im, cosa));
+                rj_re = nr;
+                rj_im = ni;
+            }
+            D(0) = zr;
+            D(1) = zi;
+            IV(3) = 1;
+        }
+        if (emit) y = dmul(fma(sinp, D(0), dmul(-cosp, D(1))), s.k[4]);
+    } else if constexpr (K == SK_TRIMA) {
+        // TrimaStream::update (trima.rs:876-905): SMA(m1) of the values (NaN
+        // left out of the sum) in ring slots [0, m1), SMA(m2) of those means
+        // in [m1, m1 + m2); i0 / i1 head1 / filled1, i2 / i3 head2 / filled2,
+        // d0 / d1 sum1 / sum2
+        const double v = (double)a[j];
+        const int m1 = s.ka, m2 = s.kb;
+        int h1 = IV(0);
+        const double o1 = RING(h1);
+        RING(h1) = v;
+        if (++h1 == m1) {
+            h1 = 0;
+            IV(1) = 1;
+        }
+        IV(0) = h1;
+        double s1 = D(0);
+        if (!isnan(o1)) s1 = dsub(s1, o1);
+        if (!isnan(v)) s1 = dadd(s1, v);
+        D(0) = s1;
+        if (IV(1)) {
+            const double mean1 = dmul(s1, s.inv_p);
+            int h2 = IV(2);
+            const double o2 = RING(m1 + h2);
+            RING(m1 + h2) = mean1;
+            if (++h2 == m2) {
+                h2 = 0;
+                IV(3) = 1;
+            }
+            IV(2) = h2;
+            double s2 = D(1);
+            if (!isnan(o2)) s2 = dsub(s2, o2);
+            s2 = dadd(s2, mean1);
+            D(1) = s2;
+            if (IV(3)) y = dmul(s2, s.inv_norm);
+        }
+    } else if constexpr (K == SK_CWMA) {
+        // CwmaStream::update (cwma.rs:893-980): leading NaNs skipped; ring of
+        // the last m = p - 1 values; i0 head, i1 filled (to m + 1), i2
+        // nan_count, i3 found_first.  Output: NaN while the window holds a NaN,
+        // else sum_weighted (mul_add chain newest first, weights (p + 1 - r)^3
+        // in w) / sum of j^3; the crate's moments do not enter it.
+        const double v = (double)a[j];
+        const int m = p - 1;
+        bool go = true;
+        if (!IV(3)) {
+            if (isnan(v)) go = false;
+            else IV(3) = 1;
+        }
+        if (go) {
+            int filled = IV(1), head = IV(0);
+            const double old = filled >= m ? RING(head) : nan;
+            const int new_nan = isnan(v) ? 1 : 0, old_nan = (filled >= m && isnan(old)) ? 1 : 0;
+            RING(head) = v;
+            head = head + 1 == m ? 0 : head + 1;
+            IV(0) = head;
+            bool emit = true;
+            if (filled <= m) {
+                IV(1) = ++filled;
+                int nc = IV(2) + new_nan;
+                if (filled == m + 1) nc -= old_nan;
+                IV(2) = nc;
+                emit = filled > m;
+            } else {
+                IV(2) = IV(2) + new_nan - old_nan;
+            }
+            if (emit && IV(2) == 0) {
+                double acc = 0.0;
+                int idx = head;
+                for (int r = 1; r <= m; ++r) {  // newest first
+                    idx = idx == 0 ? m - 1 : idx - 1;
+                    acc = fma(RING(idx), s.w[r - 1], acc);
+                }
+                y = dmul(acc, s.inv_norm);
+            }
+        }
+    } else if constexpr (K == SK_FWMA) {
+        // FwmaStream::update (fwma.rs:814-875): ring, i0 head, i1 filled,
+        // i2 nan_count; output the dot of the window (oldest first) with the
+        // normalised Fibonacci weights in w, NaN while it holds a NaN
+        const double v = (double)a[j];
+        int head = IV(0);
+        const double old = RING(head);
+        if (IV(1) && isnan(old) && IV(2) > 0) --IV(2);
+        RING(head) = v;
+        if (isnan(v)) ++IV(2);
+        head = head + 1 == p ? 0 : head + 1;
+        IV(0) = head;
+        bool emit = true;
+        if (!IV(1)) {
+            if (head != 0) emit = false;
+            else IV(1) = 1;
+        }
+        if (emit && IV(2) == 0) {
+            double acc = 0.0;
+            int idx = head;
+            for (int q = 0; q < p; ++q) {
+                acc = dadd(acc, dmul(s.w[q], RING(idx)));
+                idx = idx + 1 == p ? 0 : idx + 1;
+            }
+            y = acc;
+        }
+    } else if constexpr (K == SK_SRWMA) {
+        // SrwmaStream::update (srwma.rs:1242-1290): ring of m = p - 1 values,
+        // i0 head, i1 count (capped at p + 2); output once count > p + 1:
+        // four mul_add accumulators newest first over blocks of 4, the tail in
+        // the first; weights sqrt(p - k) in w
+        const double v = (double)a[j];
+        const int m = p - 1;
+        const int cnt = IV(1) < p + 2 ? IV(1) + 1 : p + 2;
+        IV(1) = cnt;
+        if (m == 0) {
+            if (cnt > p + 1) y = v;
+        } else {
+            int head = IV(0);
+            RING(head) = v;
+            head = head + 1 == m ? 0 : head + 1;
+            IV(0) = head;
+            if (cnt > p + 1) {
+                double acc[4] = {0.0, 0.0, 0.0, 0.0};
+                int idx = head, k = 0;  // idx walks newest first
+                for (; k + 4 <= m; k += 4)
+                    for (int q = 0; q < 4; ++q) {
+                        idx = idx == 0 ? m - 1 : idx - 1;
+                        acc[q] = fma(RING(idx), s.w[k + q], acc[q]);
+                    }
+                for (; k < m; ++k) {
+                    idx = idx == 0 ? m - 1 : idx - 1;
+                    acc[0] = fma(RING(idx), s.w[k], acc[0]);
+                }
+                y = dmul(dadd(dadd(acc[0], acc[1]), dadd(acc[2], acc[3])), s.inv_norm);
+            }
+        }
+    } else if constexpr (K == SK_SQWMA) {
+        // SqwmaStream::update (sqwma.rs:495-530) with REBASE_MASK = 0: every
+        // output is the ring's mul_add chain newest first over the p - 1 most
+        // recent values, weights (p - i)^2 in w; ring of p, i0 head, i1 count
+        // (capped at p + 2), output once count >= p + 2
+        const double v = (double)a[j];
+        int head = IV(0);
+        RING(head) = v;
+        head = head + 1 == p ? 0 : head + 1;
+        IV(0) = head;
+        const int cnt = IV(1) < p + 2 ? IV(1) + 1 : p + 2;
+        IV(1) = cnt;
+        if (cnt >= p + 2) {
+            double r = 0.0;
+            int idx = head;
+            for (int i = 0; i < p - 1; ++i) {
+                idx = idx == 0 ? p - 1 : idx - 1;
+                r = fma(RING(idx), s.w[i], r);
+            }
+            y = dmul(r, s.inv_norm);
+        }
+    } else if constexpr (K == SK_EPMA) {
+        // EpmaStream::update (epma.rs:707-735): Kahan-compensated sum (d0, d1)
+        // and ramp (d2, d3) of the last p - 1 values; ring of p, i0 head, i1
+        // seen (capped), i2 included; the value itself during the first
+        // p + offset + 1 bars, then mul_add(c0, sum, ramp) / wsum
+        const double v = (double)a[j];
+        const int p1 = p - 1;
+        const int head = IV(0), inc = IV(2);
+        int nx = head + 1 == p ? 0 : head + 1;
+        const double xo = inc == p1 ? RING(nx) : 0.0;
+        RING(head) = v;
+        IV(0) = nx;
+        const int cap = p + s.offset + 2;
+        const int seen = IV(1) < cap ? IV(1) + 1 : cap;
+        IV(1) = seen;
+        auto kahan = [&](int si, int ci, double x) {
+            const double yk = dsub(x, D(ci));
+            const double tk = dadd(D(si), yk);
+            D(ci) = dsub(dsub(tk, D(si)), yk);
+            D(si) = tk;
+        };
+        if (inc < p1) {
+            kahan(0, 1, v);
+            kahan(2, 3, dmul((double)inc, v));
+            IV(2) = inc + 1;
+        } else {
+            const double s_old = D(0);
+            kahan(0, 1, dsub(v, xo));
+            kahan(2, 3, fma(s.k[2], v, dsub(xo, s_old)));
+        }
+        y = seen <= p + s.offset + 1 ? v : dmul(fma(s.k[0], D(0), D(2)), s.k[1]);
+    } else if constexpr (K == SK_VPWMA) {
+        // VpwmaStream::update (vpwma.rs:684-750): ring of p (NaN at start), i0
+        // head, i1 filled, i2 moments_ready; output once p values were seen.
+        // deg >= 0: PolyInt moments d0..d_deg (age powers), shifted by
+        // binomial sums; else ExactDot: the window oldest first against the
+        // reversed weights as two ring segments of four accumulators each.
+        const double v = (double)a[j];
+        int head = IV(0);
+        RING(head) = v;
+        head = head + 1 == p ? 0 : head + 1;
+        IV(0) = head;
+        if (!IV(1) && head == 0) IV(1) = 1;
+        if (IV(1)) {
+            const int m = p - 1;
+            const int oldest = head + 1 == p ? 0 : head + 1;
+            const int left = min(p - oldest, m), right = m - left;
+            if (s.deg >= 0) {
+                const int dg = s.deg;
+                double mo[9];
+                if (!IV(2)) {
+                    for (int q = 0; q <= dg; ++q) mo[q] = 0.0;
+                    for (int pos = 0; pos < m; ++pos) {
+                        const double xv = pos < left ? RING(oldest + pos) : RING(pos - left);
+                        const double kk = pos < left ? (double)(m - 1 - pos) : (double)(right - 1 - (pos - left));
+                        double kp = 1.0;
+                        for (int q = 0; q <= dg; ++q) {
+                            mo[q] = dadd(mo[q], dmul(kp, xv));
+                            kp = dmul(kp, kk);
+                        }
+                    }
+                    IV(2) = 1;
+                } else {
+                    const double xo = RING(head);
+                    double nx[9];
+                    for (int q = 0; q <= dg; ++q) mo[q] = D(q);
+                    nx[0] = dsub(dadd(mo[0], v), xo);
+                    for (int jj = 1; jj <= dg; ++jj) {
+                        double acc = 0.0;
+                        for (int q = 0; q <= jj; ++q)
+                            acc = dadd(acc, dmul(s.w[kVpBinom + jj * (jj + 1) / 2 + q],
+                                                 dsub(mo[q], dmul(s.w[kVpPow + q], xo))));
+                        nx[jj] = acc;
+                    }
+                    for (int q = 0; q <= dg; ++q) mo[q] = nx[q];
+                }
+                for (int q = 0; q <= dg; ++q) D(q) = mo[q];
+                double acc[4] = {0.0, 0.0, 0.0, 0.0};
+                const int n4 = (dg + 1) & ~3;
+                int i = 0;
+                for (; i < n4; i += 4)
+                    for (int q = 0; q < 4; ++q) acc[q] = fma(s.w[i + q], mo[i + q], acc[q]);
+                for (; i <= dg; ++i) acc[0] = fma(s.w[i], mo[i], acc[0]);
+                y = dmul(dadd(dadd(acc[0], acc[1]), dadd(acc[2], acc[3])), s.inv_norm);
+            } else {
+                // weights_rev[i] = w[m - 1 - i]
+                double sum = 0.0;
+                for (int seg = 0; seg < 2; ++seg) {
+                    const int len = seg == 0 ? left : right, base = seg == 0 ? oldest : 0, wo = seg == 0 ? 0 : left;
+                    if (seg == 1 && len == 0) break;
+                    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+                    const int n4 = len & ~3;
+                    int k = 0;
+                    for (; k < n4; k += 4)
+                        for (int q = 0; q < 4; ++q)
+                            acc[q] = fma(RING(base + k + q), s.w[m - 1 - (wo + k + q)], acc[q]);
+                    for (; k < len; ++k) acc[0] = fma(RING(base + k), s.w[m - 1 - (wo + k)], acc[0]);
+                    const double part = dadd(dadd(acc[0], acc[1]), dadd(acc[2], acc[3]));
+                    sum = seg == 0 ? part : dadd(sum, part);
+                }
+                y = dmul(sum, s.inv_norm);
+            }
+        }
+    } else if constexpr (K == SK_PERCENTILE) {
+        // PercentileNearestRankStream::update (percentile_nearest_rank.rs:
+        // 665-700): once `length` values were seen, the k-th smallest valid
+        // (non-NaN) value of the window, k = nearest_rank(p / 100, valid) + 1,
+        // NaN with no valid value.  The crate's two heaps hold exactly that
+        // value on top; here it is selected by counting (O(length^2)).
+        const double v = (double)a[j];
+        int head = IV(0);
+        RING(head) = v;
+        head = head + 1 == p ? 0 : head + 1;
+        IV(0) = head;
+        if (!IV(1) && head == 0) IV(1) = 1;
+        if (IV(1)) {
+            int valid = 0;
+            for (int q = 0; q < p; ++q) valid += isnan(RING(q)) ? 0 : 1;
+            if (valid > 0) {
+                const double kf = fma(s.k[0], (double)valid, 0.5);
+                long long k = kf > 0.0 ? (long long)kf : 0;  // kf <= valid + 0.5
+                k = k == 0 ? 0 : (k - 1 >= valid ? valid - 1 : k - 1);
+                for (int q = 0; q < p; ++q) {
+                    const double xq = RING(q);
+                    if (isnan(xq)) continue;
+                    int less = 0, eq = 0;
+                    for (int r = 0; r < p; ++r) {
+                        const double xr = RING(r);
+                        less += xr < xq ? 1 : 0;
+                        eq += xr == xq ? 1 : 0;
+                    }
+                    if (less <= k && k < less + eq) {
+                        y = xq;
+                        break;
+                    }
+                }
+            }
+        }
     }
 #undef D
 #undef IV
@@ -779,7 +1153,7 @@ vta_status vta_streams_create(vta_ctx* ctx, const char* indicator, const char* c
     const KindInfo& info = kKinds[kind];
     auto P = [&](const char* key, double dflt) { return param(param_keys, param_values, n_params, key, dflt); };
     double pd = P("period", info.period);
-    if (kind == SK_ATR) pd = P("length", pd);
+    if (kind == SK_ATR || kind == SK_PERCENTILE) pd = P("length", pd);
     if (!(pd >= 1.0) || pd != std::floor(pd) || pd > 1e6)
         return fail(VTA_ERR_INVALID_INPUT, "streams: invalid period (must be a positive integer)");
     const int p = (int)pd;
@@ -896,6 +1270,164 @@ vta_status vta_streams_create(vta_ctx* ctx, const char* indicator, const char* c
             s.inv_p = 1.0 / (double)p;
             s.beta = 1.0 - s.inv_p;
             break;
+        case SK_SINWMA: {
+            // SinWmaStream::try_new (sinwma.rs:610-650), the C library's sin / cos
+            const double pi = 3.14159265358979323846;
+            const double al = pi / ((double)p + 1.0);
+            s.k[0] = std::cos(al);
+            s.k[1] = std::sin(al);
+            s.k[2] = std::cos(al * (double)p);
+            s.k[3] = std::sin(al * (double)p);
+            const double den = std::sin(0.5 * al);
+            const double eps = 2.220446049250313e-16;
+            if (std::fabs(den) < eps) return fail(VTA_ERR_INVALID_INPUT, "streams: sinwma zero sum of sines");
+            const double sum_sines = std::sin(0.5 * al * (double)p) / den;
+            if (std::fabs(sum_sines) < eps) return fail(VTA_ERR_INVALID_INPUT, "streams: sinwma zero sum of sines");
+            s.k[4] = 1.0 / sum_sines;
+            ring_slots = p;
+            break;
+        }
+        case SK_TRIMA:
+            if (p <= 3) return fail(VTA_ERR_INVALID_INPUT, "streams: trima period must be > 3");
+            s.ka = (p + 1) / 2;
+            s.kb = p - s.ka + 1;
+            s.inv_p = 1.0 / (double)s.ka;
+            s.inv_norm = 1.0 / (double)s.kb;
+            ring_slots = s.ka + s.kb;
+            break;
+        case SK_CWMA: {
+            // CwmaStream::try_new (cwma.rs:832-870): weights (p + 1 - r)^3,
+            // r = 1..p-1 (newest first), norm = sum_{j=2..p} j^3
+            if (p <= 1) return fail(VTA_ERR_INVALID_INPUT, "streams: cwma period must be > 1");
+            double norm = 0.0;
+            for (int jj = 2; jj <= p; ++jj) {
+                const double jf = (double)jj;
+                norm += jf * jf * jf;
+            }
+            s.inv_norm = 1.0 / norm;
+            const double av = (double)(p + 1);
+            w.resize(p - 1);
+            for (int r = 1; r <= p - 1; ++r) {
+                const double t = av - (double)r;
+                w[r - 1] = t * t * t;
+            }
+            ring_slots = p - 1;
+            break;
+        }
+        case SK_FWMA: {
+            // FwmaStream::try_new (fwma.rs:771-800): 1, 1, 2, 3, ... / sum
+            w.assign(p, 1.0);
+            for (int i = 2; i < p; ++i) w[i] = w[i - 1] + w[i - 2];
+            double sum = 0.0;
+            for (int i = 0; i < p; ++i) sum += w[i];
+            for (int i = 0; i < p; ++i) w[i] /= sum;
+            ring_slots = p;
+            break;
+        }
+        case SK_SRWMA: {
+            // SrwmaStream::try_new (srwma.rs:1208-1235): sqrt(p - k), k < p - 1
+            double sumw = 0.0;
+            w.resize(p > 1 ? p - 1 : 0);
+            for (int k = 0; k < p - 1; ++k) {
+                w[k] = std::sqrt((double)(p - k));
+                sumw += w[k];
+            }
+            s.inv_norm = sumw == 0.0 ? 0.0 : 1.0 / sumw;
+            ring_slots = p > 1 ? p - 1 : 0;
+            break;
+        }
+        case SK_SQWMA: {
+            // SqwmaStream::try_new (sqwma.rs:383-420): (p - i)^2, i < p - 1
+            if (p < 2) return fail(VTA_ERR_INVALID_INPUT, "streams: sqwma period must be >= 2");
+            double ws = 0.0;
+            w.resize(p - 1);
+            for (int i = 0; i < p - 1; ++i) {
+                const double d = (double)p - (double)i;
+                w[i] = d * d;
+                ws += w[i];
+            }
+            s.inv_norm = 1.0 / ws;
+            ring_slots = p;
+            break;
+        }
+        case SK_EPMA: {
+            // EpmaStream::try_new (epma.rs:667-700)
+            const double off = P("offset", 4.0);
+            if (p < 2) return fail(VTA_ERR_INVALID_INPUT, "streams: epma period must be >= 2");
+            if (!(off >= 0.0) || off != std::floor(off) || off >= (double)p)
+                return fail(VTA_ERR_INVALID_INPUT, "streams: epma offset must be an integer in [0, period)");
+            s.offset = (int)off;
+            const double p1f = (double)(p - 1);
+            s.k[0] = 2.0 - off;
+            s.k[1] = 1.0 / std::fma(p1f, s.k[0], 0.5 * (p1f - 1.0) * p1f);
+            s.k[2] = (double)(p - 2);
+            ring_slots = p;
+            break;
+        }
+        case SK_VPWMA: {
+            // VpwmaStream::try_new (vpwma.rs:595-680)
+            const double power = P("power", 0.382);
+            if (p < 2) return fail(VTA_ERR_INVALID_INPUT, "streams: vpwma period must be >= 2");
+            if (!std::isfinite(power)) return fail(VTA_ERR_INVALID_INPUT, "streams: vpwma power must be finite");
+            const int m = p - 1;
+            std::vector<double> wt(m);
+            double norm = 0.0;
+            for (int k = 0; k < m; ++k) {
+                wt[k] = std::pow((double)p - (double)k, power);
+                norm += wt[k];
+            }
+            s.inv_norm = 1.0 / norm;
+            const double pr = std::round(power);
+            if (std::fabs(power - pr) <= 1e-12 && pr >= 0.0 && pr <= 8.0) {
+                const int dg = (int)pr;
+                s.deg = dg;
+                w.assign(kVpConsts, 0.0);
+                // integer powers by binary exponentiation (the LLVM runtime's
+                // powi); binomials as exact integer ratios
+                auto powi = [](double base, int e) {
+                    double r = 1.0;
+                    for (;;) {
+                        if (e & 1) r *= base;
+                        e /= 2;
+                        if (e == 0) break;
+                        base *= base;
+                    }
+                    return r;
+                };
+                auto binom = [](int nn, int kk) {
+                    if (kk == 0 || kk == nn) return 1.0;
+                    if (kk > nn - kk) kk = nn - kk;
+                    unsigned long long num = 1, den = 1;
+                    for (int i = 1; i <= kk; ++i) {
+                        num *= (unsigned long long)(nn + 1 - i);
+                        den *= (unsigned long long)i;
+                    }
+                    return (double)num / (double)den;
+                };
+                for (int jj = 0; jj <= dg; ++jj)
+                    w[jj] = ((jj & 1) ? -1.0 : 1.0) * binom(dg, jj) * powi((double)p, dg - jj);
+                double pp = 1.0;
+                for (int q = 0; q <= dg; ++q) {
+                    w[kVpPow + q] = pp;
+                    pp *= (double)(m - 1);
+                }
+                for (int jj = 0; jj <= dg; ++jj)
+                    for (int q = 0; q <= jj; ++q) w[kVpBinom + jj * (jj + 1) / 2 + q] = binom(jj, q);
+            } else {
+                s.deg = -1;
+                w = wt;
+            }
+            ring_slots = p;
+            break;
+        }
+        case SK_PERCENTILE: {
+            const double pct = P("percentage", 50.0);
+            if (!(pct >= 0.0 && pct <= 100.0))
+                return fail(VTA_ERR_INVALID_INPUT, "streams: percentage must be in [0, 100]");
+            s.k[0] = pct * 0.01;
+            ring_slots = p;
+            break;
+        }
         default: break;
     }
     s.ring_slots = ring_slots;
