@@ -115,6 +115,35 @@ def workload_ema_small():
             "config": {"workload": "ema_small", "bars": n, "seed": 1, "combos": 999}}
 
 
+def workload_recur_small():
+    """Profiling case of the chunked recurrences: EMA and DEMA sweeps (periods
+    2..1000, 999 combos) on 400,000 bars (1.6 GB of outputs per call)."""
+    from vectorta_gb300 import datagen
+
+    n = 400_000
+    close = datagen.random_walk(n, seed=1, nan_lead=200)
+    rec = {"period": (2, 1000, 1)}
+    return {"name": "recur_small", "n": n, "series": {"close": close.astype(np.float32)},
+            "jobs": [("ema", ["close"], rec), ("dema", ["close"], rec)], "dominant": "ema",
+            "config": {"workload": "recur_small", "bars": n, "seed": 1, "combos": 999}}
+
+
+def workload_windows_small():
+    """Profiling case of the window kernels: StdDev and WillR sweeps (windows
+    5..500 step 5, 100 combos) on 400,000 bars (160 MB of outputs per call:
+    larger than L2)."""
+    from vectorta_gb300 import datagen
+
+    n = 400_000
+    close = datagen.random_walk(n, seed=1, nan_lead=200)
+    hi, lo = datagen.high_low(close, seed=1)
+    series = {"close": close.astype(np.float32), "high": hi.astype(np.float32), "low": lo.astype(np.float32)}
+    jobs = [("stddev", ["close"], {"period": (5, 500, 5), "nbdev": (1.0, 1.0, 0.0)}),
+            ("willr", ["high", "low", "close"], {"period": (5, 500, 5)})]
+    return {"name": "windows_small", "n": n, "series": series, "jobs": jobs, "dominant": "stddev",
+            "config": {"workload": "windows_small", "bars": n, "seed": 1, "combos": 100}}
+
+
 def workload_adx_sweep():
     """ADX sweep, periods 2..400 (399 combos) on 1,000,000 OHLC bars (seed 3,
     NaN lead 100): the single-series ADX path (time-chunked, verified warm
@@ -181,7 +210,8 @@ def workload_served_stream():
 
 WORKLOADS = {"sweeps": workload_sweeps, "ragged_tm": workload_ragged_tm, "served_stream": workload_served_stream,
              "adx_sweep": workload_adx_sweep, "wwma_family": workload_wwma_family, "ragged_small": workload_ragged_small, "alma_grid": workload_alma_grid, "ema_small": workload_ema_small,
-             "alma_small": workload_alma_small}
+             "alma_small": workload_alma_small, "windows_small": workload_windows_small,
+             "recur_small": workload_recur_small}
 
 
 # ------------------------------------------------------------- clocks -------
@@ -854,7 +884,8 @@ TRAFFIC = {
 }
 KERNEL_NAME = {"recurrence_window_sweeps": "k_recur<OpEma, batch, EMIT>", "alma_grid": "k_wwma_tc<fp16x3>",
                "ema_small": "k_recur<OpEma, batch, EMIT>", "alma_small": "k_wwma_tc<fp16x3>",
-               "adx_sweep": "k_hlc_chunk<adx> + fix-up", "wwma_family": "k_wwma_tc<fp16x3> (CWMA)"}
+               "adx_sweep": "k_hlc_chunk<adx> + fix-up", "wwma_family": "k_wwma_tc<fp16x3> (CWMA)",
+               "windows_small": "k_prefix_window_batch (StdDev)", "recur_small": "k_recur<OpEma, batch, EMIT>"}
 
 
 def main():

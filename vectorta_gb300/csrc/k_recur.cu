@@ -754,13 +754,27 @@ k_recur(RecurArgs a) {
                 const bool seeded0 = act0 && op0.s < a.n;
                 bool run0 = false;
                 int st0 = 0;
-                for (int t = min(a.first, c1); t < c1; ++t) {
+                int t = min(a.first, c1);
+                // warm-up and seed through the per-step phase logic ...
+                for (; t < c1 && !run0; ++t) {
                     InStep st;  // x[t] and x[t - 1] from shared memory
                     st.t = t;
                     st.x0 = xs[t];
                     st.x1 = t > 0 ? xs[t - 1] : 0.f;
                     st.h0 = st.l0 = 0.f;
                     general_step(op0, act0, seeded0, run0, st0, st, t);
+                }
+                // ... then the running steps without it (the same state update
+                // as the op's step(); t > s >= 0 here)
+                if constexpr (!HasUni<Op>::value) {
+                    float xprev = t > 0 && t <= c1 ? xs[t - 1] : 0.f;
+#pragma unroll 4
+                    for (; t < c1; ++t) {
+                        const float xv = xs[t];
+                        const InStep st{t, xv, xprev, 0.f, 0.f};
+                        op0.template fast<false>(st, t, st0);
+                        xprev = xv;
+                    }
                 }
                 write_agg(a, op0, act0, seeded0, st0, 0, 0, c1, l0);
             }
