@@ -36,25 +36,16 @@ __device__ __forceinline__ DS ds_sub2(float2 a, float2 b) {
     const DS s = two_sum(a.x, -b.x);
     return fast_two_sum(s.hi, s.lo + (a.y - b.y));
 }
-__device__ __forceinline__ DS ds_sub(DS a, DS b) {
-    const DS s = two_sum(a.hi, -b.hi);
-    return fast_two_sum(s.hi, s.lo + (a.lo - b.lo));
+// a - b for a.x >= b.x >= 0 (a prefix of squares: non-decreasing), where the
+// error of the leading difference is exact by Fast2Sum
+__device__ __forceinline__ DS ds_sub2_ge(float2 a, float2 b) {
+    const float d = a.x - b.x;
+    const float e = (a.x - d) - b.x;
+    return fast_two_sum(d, e + (a.y - b.y));
 }
 __device__ __forceinline__ DS ds_add_f(DS a, float b) {
     const DS s = two_sum(a.hi, b);
     return fast_two_sum(s.hi, s.lo + a.lo);
-}
-__device__ __forceinline__ DS ds_mul_f(DS a, float b) {
-    const float p = a.hi * b;
-    float e = fmaf(a.hi, b, -p);
-    e = fmaf(a.lo, b, e);
-    return fast_two_sum(p, e);
-}
-__device__ __forceinline__ DS ds_sqr(DS a) {
-    const float p = a.hi * a.hi;
-    float e = fmaf(a.hi, a.hi, -p);
-    e = fmaf(2.f * a.hi, a.lo, e);
-    return fast_two_sum(p, e);
 }
 __device__ __forceinline__ float ds_f(DS a) { return a.hi + a.lo; }
 
@@ -72,9 +63,14 @@ __device__ __forceinline__ WinOut window_eval(int kind, DS s1, DS s2, float pf, 
         r.o0 = mean;
         return r;
     }
-    // p*S2 - S1^2 = p^2 * var
-    const DS num = ds_sub(ds_mul_f(s2, pf), ds_sqr(s1));
-    const float var = ds_f(num) * inv_p2;
+    // p*S2 - S1^2 = p^2 * var, from the error-free products p*S2.hi and
+    // S1.hi^2 (their difference is exact where it cancels) plus the
+    // first-order low-part terms; the dropped S1.lo^2 is 2^-48 of S1^2
+    const float h = s1.hi * s1.hi, eh = fmaf(s1.hi, s1.hi, -h);
+    const float g = pf * s2.hi, eg = fmaf(pf, s2.hi, -g);
+    float corr = fmaf(pf, s2.lo, eg - eh);
+    corr = fmaf(-2.f * s1.hi, s1.lo, corr);
+    const float var = ((g - h) + corr) * inv_p2;
     if (kind == WK_STDDEV) {
         r.o0 = var <= 0.f ? 0.f : sqrtf(var) * k1;
         return r;
@@ -147,7 +143,7 @@ k_prefix_window_batch(PrefixWinArgs a, int pmax) {
             }
             const int lb = pmax + threadIdx.x + k * kPwThreads - p;  // local index of t - p
             const DS w1 = ds_sub2(p1t[k], s1[lb]);
-            const DS w2 = two ? ds_sub2(p2t[k], s2[lb]) : DS{0.f, 0.f};
+            const DS w2 = two ? ds_sub2_ge(p2t[k], s2[lb]) : DS{0.f, 0.f};
             const WinOut r = window_eval(a.kind, w1, w2, pf, inv_p, inv_p2, xt[k], k1, k2);
             a.out0[o] = r.o0;
             if (a.kind == WK_BB) { a.out1[o] = r.o1; a.out2[o] = r.o2; }
