@@ -229,6 +229,16 @@ k_minmax_batch(MinMaxArgs a, int tile, int levels) {
     float* mn = sm + (size_t)levels * nloc;  // [levels][nloc]
     int* bad_nan = reinterpret_cast<int*>(mn + (size_t)levels * nloc);  // [nloc+1]
     int* bad_fin = bad_nan + nloc + 1;                                   // [nloc+1]
+    // per combo: window start and first output index, and the two table
+    // offsets of the window's sparse-table lookups (level k, positions
+    // t - p + 1 and t - 2^k + 1 relative to the local index of t)
+    const size_t ctab_at = ((size_t)2 * levels * nloc + 2 * ((size_t)nloc + 1) + 3) & ~size_t(3);  // 16-byte aligned
+    int4* ctab = reinterpret_cast<int4*>(reinterpret_cast<int*>(sm) + ctab_at);
+    for (int c = threadIdx.x; c < a.n_combos; c += blockDim.x) {
+        const int p = a.periods[c];
+        const int k = 31 - __clz(p);
+        ctab[c] = make_int4(p, a.first + p - 1, k * nloc - p + 1, k * nloc - (1 << k) + 1);
+    }
     // level 0 + invalid flags
     for (int i = threadIdx.x; i < nloc; i += blockDim.x) {
         const int g = lo_i + i;
@@ -278,24 +288,27 @@ k_minmax_batch(MinMaxArgs a, int tile, int levels) {
         }
     }
     __syncthreads();
+    // a span without invalid inputs (the usual case) needs no window counts
+    const bool clean = bad_nan[nloc] == 0 && bad_fin[nloc] == 0;
     for (int tt = threadIdx.x; tt < tile; tt += blockDim.x) {
         const int t = t0 + tt;
         if (t >= a.n) break;
         const float cl = a.kind == MM_WILLR ? a.c[t] : 0.f;
         const int ie = t - lo_i;  // local index of t
-        for (int c = 0; c < a.n_combos; ++c) {
-            const int p = a.periods[c];
-            const size_t o = (size_t)c * a.n + t;
+        float* o0 = a.out0 + t;
+        float* o1 = a.out1 + t;
+        float* o2 = a.out2 + t;
+        for (int c = 0; c < a.n_combos; ++c, o0 += a.n, o1 += a.n, o2 += a.n) {
+            const int4 ct = ctab[c];
+            const int p = ct.x;
             float r0 = qnan(), r1 = qnan(), r2 = qnan();
-            if (t >= a.first + p - 1) {
+            if (t >= ct.y) {
                 const int ib = ie - p + 1;
-                const int k = 31 - __clz(p);
-                const int ib2 = ie - (1 << k) + 1;
-                const float hmax = fmaxf(mx[(size_t)k * nloc + ib], mx[(size_t)k * nloc + ib2]);
-                const float lmin = fminf(mn[(size_t)k * nloc + ib], mn[(size_t)k * nloc + ib2]);
-                const int nn = bad_nan[ie + 1] - bad_nan[ib];
+                const float hmax = fmaxf(mx[ie + ct.z], mx[ie + ct.w]);
+                const float lmin = fminf(mn[ie + ct.z], mn[ie + ct.w]);
+                const int nn = clean ? 0 : bad_nan[ie + 1] - bad_nan[ib];
                 if (a.kind == MM_DONCHIAN) {
-                    const int nb = p > 32 ? bad_fin[ie + 1] - bad_fin[ib] : nn;
+                    const int nb = clean ? 0 : (p > 32 ? bad_fin[ie + 1] - bad_fin[ib] : nn);
                     if (nb == 0) {
                         r0 = hmax;
                         r2 = lmin;
@@ -304,12 +317,17 @@ k_minmax_batch(MinMaxArgs a, int tile, int levels) {
                 } else {
                     if (!isnan(cl) && nn == 0 && isfinite(hmax) && isfinite(lmin)) {
                         const float den = hmax - lmin;
-                        r0 = den == 0.f ? 0.f : fmaf(-100.f, (hmax - cl) / den, 0.f);
+                        // hmax, lmin and cl are finite prices: the fast divide
+                        // is within 2 ulp
+                        r0 = den == 0.f ? 0.f : fmaf(-100.f, __fdividef(hmax - cl, den), 0.f);
                     }
                 }
             }
-            a.out0[o] = r0;
-            if (a.kind == MM_DONCHIAN) { a.out1[o] = r1; a.out2[o] = r2; }
+            *o0 = r0;
+            if (a.kind == MM_DONCHIAN) {
+                *o1 = r1;
+                *o2 = r2;
+            }
         }
     }
 }
@@ -496,7 +514,8 @@ vta_status launch_minmax_batch(const MinMaxArgs& a, size_t smem_optin, cudaStrea
     const int levels = 32 - __builtin_clz((unsigned)a.pmax);  // floor(log2 pmax) + 1
     for (int tile = 2048; tile >= 256; tile >>= 1) {
         const size_t nloc = (size_t)tile + a.pmax - 1;
-        const size_t bytes = nloc * levels * 2 * sizeof(float) + 2 * (nloc + 1) * sizeof(int);
+        const size_t bytes = nloc * levels * 2 * sizeof(float) + (2 * (nloc + 1) + 4) * sizeof(int) +
+                             (size_t)a.n_combos * sizeof(int4);
         if (bytes <= smem_optin && (tile <= 512 || (size_t)a.n >= (size_t)tile * 8 * kNumSMs)) {
             VTA_CUDA_TRY(cudaFuncSetAttribute(k_minmax_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)bytes));
