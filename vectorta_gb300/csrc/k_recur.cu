@@ -173,6 +173,7 @@ struct OpEma {
 struct OpDema {
     static constexpr bool kHlc = false;
     static constexpr int NS = 2;
+    static constexpr int kShape = 1;
     float alpha, a, e1, e2, xf;
     int f, s, warm;
     __device__ void init(int p, int first) {
@@ -218,6 +219,7 @@ struct OpDema {
 struct OpTema {
     static constexpr bool kHlc = false;
     static constexpr int NS = 3;
+    static constexpr int kShape = 1;
     float per, per1, e1, e2, e3;
     float z1, z2, z3;  // scaled state of the emit fast tiles (valid while zs)
     bool zs;
@@ -304,6 +306,7 @@ template <bool kBatchSem>
 struct OpRsi {
     static constexpr bool kHlc = false;
     static constexpr int NS = 2;
+    static constexpr int kShape = 2;
     float inv_p, beta, ag, al, xprev, pf;
     int f, s, warm;
     Acc sg, sl;
@@ -972,8 +975,16 @@ __device__ __forceinline__ void aff_identity(Aff<N>& a) {
         a.b[r] = 0.0;
     }
 }
+// Structure of an op's transition matrix: every product of such matrices
+// keeps it, so the f64 work skips the structural zeros (GB300's FP64 rate
+// makes them count).  0 = full, 1 = lower triangular (DEMA, TEMA cascades),
+// 2 = diagonal (RSI's independent gain / loss averages).
+template <class Op, class = void> struct ShapeOf { static constexpr int v = 0; };
+template <class Op> struct ShapeOf<Op, std::void_t<decltype(Op::kShape)>> { static constexpr int v = Op::kShape; };
+__host__ __device__ constexpr bool shape_nz(int sh, int r, int c) { return sh == 0 || (sh == 1 ? c <= r : c == r); }
+
 // returns second o first (apply `first`, then `second`)
-template <int N>
+template <int N, int SH = 0>
 __device__ __forceinline__ Aff<N> aff_then(const Aff<N>& first, const Aff<N>& second) {
     Aff<N> o;
 #pragma unroll
@@ -982,22 +993,25 @@ __device__ __forceinline__ Aff<N> aff_then(const Aff<N>& first, const Aff<N>& se
 #pragma unroll
         for (int c = 0; c < N; ++c) {
             double mrc = 0.0;
+            if (shape_nz(SH, r, c)) {
 #pragma unroll
-            for (int q = 0; q < N; ++q) mrc = fma(second.m[r][q], first.m[q][c], mrc);
+                for (int q = 0; q < N; ++q)
+                    if (shape_nz(SH, r, q) && shape_nz(SH, q, c)) mrc = fma(second.m[r][q], first.m[q][c], mrc);
+                br = fma(second.m[r][c], first.b[c], br);
+            }
             o.m[r][c] = mrc;
-            br = fma(second.m[r][c], first.b[c], br);
         }
         o.b[r] = br;
     }
     return o;
 }
-template <int N>
+template <int N, int SH = 0>
 __device__ __forceinline__ Aff<N> aff_shfl_up(const Aff<N>& a, int d) {
     Aff<N> o;
 #pragma unroll
     for (int r = 0; r < N; ++r) {
 #pragma unroll
-        for (int c = 0; c < N; ++c) o.m[r][c] = __shfl_up_sync(0xffffffffu, a.m[r][c], d);
+        for (int c = 0; c < N; ++c) o.m[r][c] = shape_nz(SH, r, c) ? __shfl_up_sync(0xffffffffu, a.m[r][c], d) : 0.0;
         o.b[r] = __shfl_up_sync(0xffffffffu, a.b[r], d);
     }
     return o;
@@ -1061,14 +1075,14 @@ __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
     for (int k = k0; k < k1; ++k) {
         Aff<N> ak;
         chunk_map<Op>(agg[(size_t)k * a.n_lanes + li], p, a.chunk, ml, ak);
-        run = aff_then(run, ak);
+        run = aff_then<N, ShapeOf<Op>::v>(run, ak);
     }
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-        const Aff<N> up = aff_shfl_up(run, d);
-        if (lane >= d) run = aff_then(up, run);
+        const Aff<N> up = aff_shfl_up<N, ShapeOf<Op>::v>(run, d);
+        if (lane >= d) run = aff_then<N, ShapeOf<Op>::v>(up, run);
     }
-    Aff<N> ex = aff_shfl_up(run, 1);
+    Aff<N> ex = aff_shfl_up<N, ShapeOf<Op>::v>(run, 1);
     if (lane == 0) aff_identity(ex);
     double S[N];  // state at the start of chunk k0
 #pragma unroll
@@ -1086,7 +1100,8 @@ __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
         for (int r = 0; r < N; ++r) {
             double v = ak.b[r];
 #pragma unroll
-            for (int c = 0; c < N; ++c) v = fma(ak.m[r][c], S[c], v);
+            for (int c = 0; c < N; ++c)
+                if (shape_nz(ShapeOf<Op>::v, r, c)) v = fma(ak.m[r][c], S[c], v);
             t[r] = v;
         }
 #pragma unroll

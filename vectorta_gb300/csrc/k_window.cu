@@ -130,14 +130,15 @@ k_prefix_window_batch(PrefixWinArgs a, int pmax) {
         const float k1 = a.k1 ? a.k1[c] : 1.f;
         const float k2 = a.k2 ? a.k2[c] : 1.f;
         const float pf = (float)p;
-        const float inv_p = 1.f / pf, inv_p2 = inv_p * inv_p;
+        const float inv_p = __frcp_rn(pf), inv_p2 = inv_p * inv_p;  // 1/p correctly rounded
+        float* row0 = a.out0 + (size_t)c * a.n;
 #pragma unroll
         for (int k = 0; k < kPwPer; ++k) {
             const int t = t0 + threadIdx.x + k * kPwThreads;
             if (t >= a.n) break;
             const size_t o = (size_t)c * a.n + t;
             if (t < warm) {
-                a.out0[o] = qnan();
+                row0[t] = qnan();
                 if (a.kind == WK_BB) { a.out1[o] = qnan(); a.out2[o] = qnan(); }
                 continue;
             }
@@ -145,7 +146,7 @@ k_prefix_window_batch(PrefixWinArgs a, int pmax) {
             const DS w1 = ds_sub2(p1t[k], s1[lb]);
             const DS w2 = two ? ds_sub2_ge(p2t[k], s2[lb]) : DS{0.f, 0.f};
             const WinOut r = window_eval(a.kind, w1, w2, pf, inv_p, inv_p2, xt[k], k1, k2);
-            a.out0[o] = r.o0;
+            row0[t] = r.o0;
             if (a.kind == WK_BB) { a.out1[o] = r.o1; a.out2[o] = r.o2; }
         }
     }
