@@ -838,7 +838,7 @@ vta_status vta_server_destroy(vta_server* s);
  * here.  vta_sma_batch_device_noalloc returns what vta_sma_batch_device
  * returns (same arguments, checks and errors) but never allocates device
  * memory: its working buffers live in one fixed scratch area of the library's
- * static device memory (VTA_NOALLOC_SCRATCH_BYTES, about 8 MiB per device,
+ * static device memory (VTA_NOALLOC_SCRATCH_BYTES, about 16 KiB per device,
  * reserved on a device when the function is first called there).
  * It is for callers that may not allocate once running: cudaMalloc and
  * cudaFree can synchronise the whole device and take unbounded time, which a
@@ -860,7 +860,7 @@ vta_status vta_server_destroy(vta_server* s);
  *     scratch cell it reads. */
 #define VTA_NOALLOC_MAX_LEN 1048576
 #define VTA_NOALLOC_MAX_COMBOS 4096
-#define VTA_NOALLOC_SCRATCH_BYTES 8437760
+#define VTA_NOALLOC_SCRATCH_BYTES 16640
 vta_status vta_sma_batch_device_noalloc(vta_ctx* ctx, const float* d_data, size_t len,
     size_t first_valid, const vta_period_batch_range* sweep, float* d_out);
 

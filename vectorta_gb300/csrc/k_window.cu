@@ -2,15 +2,19 @@
 // sliding min/max (Donchian, Williams %R) and nearest-rank percentile.
 //
 // Precision plan (GB300's FP64 rate is a small fraction of FP32):
-//   * batch: the series prefix sums are built once in FP64 and packed as
-//     double-single float2; every output is then a difference of two prefix
-//     entries evaluated in double-single FP32 arithmetic (error-free
-//     two-sum / FMA products), and the variance is formed as
-//     (p*S2 - S1^2) / p^2 so the cancellation happens in ~48-bit precision;
+//   * batch: each block builds a double-single (float pair) prefix of x and
+//     of x^2 over its own input span only, so every window sum is a
+//     difference of two local prefix entries whose magnitude is that of the
+//     span's data, not of the whole series (a global prefix loses the
+//     variance where a series falls far below its earlier levels); the
+//     variance is formed as (p*S2 - S1^2) / p^2 from error-free products;
 //   * time-major: each thread slides compensated (double-single) running sums
 //     over its time chunk, re-initialised exactly at the chunk start.
 // NaN semantics follow the crate's running-sum code: a NaN after the first
-// valid index poisons every later output of that series.
+// valid index poisons every later output of that series, an infinite input
+// every output from p steps after it (where it leaves the window: inf - inf).
+#include <algorithm>
+
 #include "vta_internal.h"
 
 namespace vta {
@@ -90,16 +94,43 @@ __device__ __forceinline__ WinOut window_eval(int kind, DS s1, DS s2, float pf, 
 }
 
 // ---------------------------------------------- prefix windows, batch ------
-// One block per time tile of kPwTile steps serves every combo: the tile's
-// prefix span [t0 - pmax, t0 + kPwTile) is staged in shared memory once, each
-// thread keeps P[t] for its kPwPer times in registers and loops over combos.
+// One block per time tile of kPwTile steps serves every combo: the block
+// builds the local double-single prefix of x and x^2 over the tile's input
+// span [t0 - pmax, t0 + kPwTile) in shared memory, each thread keeps the
+// prefix at its kPwPer times in registers and loops over combos.
 constexpr int kPwThreads = 256;
 constexpr int kPwPer = 4;
 constexpr int kPwTile = kPwThreads * kPwPer;
 
+__device__ __forceinline__ DS ds_add(DS a, DS b) {
+    const DS s = two_sum(a.hi, b.hi);
+    return fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+}
+
+// first NaN / first infinite input at or after `first`, stored as n - index
+// (bad[] starts at 0 = none, so a memset clears it)
+__global__ void k_first_bad(const float* __restrict__ x, int n, int first, int* bad) {
+    int fn = n, fi = n;
+    for (int i = first + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float v = x[i];
+        if (isnan(v)) fn = min(fn, i);
+        else if (isinf(v)) fi = min(fi, i);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        fn = min(fn, __shfl_xor_sync(0xffffffffu, fn, o));
+        fi = min(fi, __shfl_xor_sync(0xffffffffu, fi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (fn < n) atomicMax(bad, n - fn);
+        if (fi < n) atomicMax(bad + 1, n - fi);
+    }
+}
+
 __global__ void __launch_bounds__(kPwThreads)
 k_prefix_window_batch(PrefixWinArgs a, int pmax) {
     extern __shared__ float2 psm[];
+    __shared__ DS wsum1[kPwThreads / 32], wsum2[kPwThreads / 32];
     const int t0 = blockIdx.x * kPwTile;
     const int span = kPwTile + pmax;
     const int base = t0 - pmax;  // global index of slot 0
@@ -107,13 +138,62 @@ k_prefix_window_batch(PrefixWinArgs a, int pmax) {
     float2* s1 = psm;
     float2* s2 = psm + span;
     const float2 z = make_float2(0.f, 0.f);
-    for (int i = threadIdx.x; i < span; i += kPwThreads) {
+    // 1. local inclusive prefix: each thread sums a run of `per` slots, the
+    // run totals are scanned across the block, then added back
+    const int per = (span + kPwThreads - 1) / kPwThreads;
+    const int i0 = threadIdx.x * per, i1 = min(i0 + per, span);
+    DS a1 = {0.f, 0.f}, a2 = {0.f, 0.f};
+    for (int i = i0; i < i1; ++i) {
         const int g = base + i;
-        const bool in = g >= 0 && g < a.n;
-        s1[i] = in ? a.p1[g] : z;
-        if (two) s2[i] = in ? a.p2[g] : z;
+        const float v = (g >= a.first && g < a.n) ? __ldg(a.x + g) : 0.f;
+        a1 = ds_add_f(a1, v);
+        s1[i] = make_float2(a1.hi, a1.lo);
+        if (two) {
+            const float h = v * v;
+            a2 = ds_add_f(ds_add_f(a2, h), fmaf(v, v, -h));
+            s2[i] = make_float2(a2.hi, a2.lo);
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    DS e1 = a1, e2 = a2;  // inclusive scan of the run totals within the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const DS u1 = {__shfl_up_sync(0xffffffffu, e1.hi, o), __shfl_up_sync(0xffffffffu, e1.lo, o)};
+        const DS u2 = {__shfl_up_sync(0xffffffffu, e2.hi, o), __shfl_up_sync(0xffffffffu, e2.lo, o)};
+        if (lane >= o) {
+            e1 = ds_add(u1, e1);
+            e2 = ds_add(u2, e2);
+        }
+    }
+    if (lane == 31) {
+        wsum1[warp] = e1;
+        wsum2[warp] = e2;
+    }
+    // exclusive offset of this thread's run: the totals of the earlier warps,
+    // then the previous lanes' inclusive total
+    DS ex1 = {__shfl_up_sync(0xffffffffu, e1.hi, 1), __shfl_up_sync(0xffffffffu, e1.lo, 1)};
+    DS ex2 = {__shfl_up_sync(0xffffffffu, e2.hi, 1), __shfl_up_sync(0xffffffffu, e2.lo, 1)};
+    if (lane == 0) ex1 = ex2 = DS{0.f, 0.f};
+    __syncthreads();
+    DS off1 = {0.f, 0.f}, off2 = {0.f, 0.f};
+    for (int w = 0; w < warp; ++w) {
+        off1 = ds_add(off1, wsum1[w]);
+        off2 = ds_add(off2, wsum2[w]);
+    }
+    off1 = ds_add(off1, ex1);
+    off2 = ds_add(off2, ex2);
+    for (int i = i0; i < i1; ++i) {
+        const float2 v1 = s1[i];
+        const DS r1 = ds_add(off1, DS{v1.x, v1.y});
+        s1[i] = make_float2(r1.hi, r1.lo);
+        if (two) {
+            const float2 v2 = s2[i];
+            const DS r2 = ds_add(off2, DS{v2.x, v2.y});
+            s2[i] = make_float2(r2.hi, r2.lo);
+        }
     }
     __syncthreads();
+    const int first_nan = a.n - a.bad[0], first_inf = a.n - a.bad[1];
     float2 p1t[kPwPer], p2t[kPwPer];
     float xt[kPwPer];
 #pragma unroll
@@ -127,6 +207,7 @@ k_prefix_window_batch(PrefixWinArgs a, int pmax) {
     for (int c = 0; c < a.n_combos; ++c) {
         const int p = a.periods[c];
         const int warm = a.first + p - 1;
+        const int poison = min(first_nan, first_inf < a.n ? first_inf + p : a.n);
         const float k1 = a.k1 ? a.k1[c] : 1.f;
         const float k2 = a.k2 ? a.k2[c] : 1.f;
         const float pf = (float)p;
@@ -137,7 +218,7 @@ k_prefix_window_batch(PrefixWinArgs a, int pmax) {
             const int t = t0 + threadIdx.x + k * kPwThreads;
             if (t >= a.n) break;
             const size_t o = (size_t)c * a.n + t;
-            if (t < warm) {
+            if (t < warm || t >= poison) {
                 row0[t] = qnan();
                 if (a.kind == WK_BB) { a.out1[o] = qnan(); a.out2[o] = qnan(); }
                 continue;
@@ -491,7 +572,13 @@ __global__ void k_percentile(PnrArgs a) {
 
 vta_status launch_prefix_window_batch(const PrefixWinArgs& a, int pmax, size_t smem_optin, cudaStream_t st) {
     const size_t smem = (size_t)(kPwTile + pmax) * sizeof(float2) * (a.kind == WK_SMA ? 1 : 2);
-    if (smem > smem_optin) return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "prefix window: period too large");
+    if (smem + 2 * (kPwThreads / 32) * sizeof(DS) > smem_optin)
+        return fail(VTA_ERR_LAUNCH_CONFIG_TOO_LARGE, "prefix window: period too large");
+    VTA_CUDA_TRY(cudaMemsetAsync(a.bad, 0, 2 * sizeof(int), st));
+    if (a.first < a.n) {
+        k_first_bad<<<std::min<int>(ceil_div(a.n - a.first, 256), 4 * kNumSMs), 256, 0, st>>>(a.x, a.n, a.first, a.bad);
+        VTA_TRY(check_launch("k_first_bad"));
+    }
     VTA_CUDA_TRY(cudaFuncSetAttribute(k_prefix_window_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     ktimer_begin(st);
     k_prefix_window_batch<<<ceil_div(a.n, kPwTile), kPwThreads, smem, st>>>(a, pmax);

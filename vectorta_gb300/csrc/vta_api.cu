@@ -652,29 +652,21 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             return ind == I_ADX ? launch_adx(a, st) : launch_supertrend(a, st);
         }
         case I_SMA: case I_STDDEV: case I_ZSCORE: case I_BB: {
-            const bool need2 = ind != I_SMA;
-            ar.need(len * sizeof(float2));
-            ar.need(need2 ? len * sizeof(float2) : 0);
-            ar.need(prefix_tmp_doubles(n) * sizeof(double));
+            ar.need(2 * sizeof(int));
             VTA_TRY(ar.commit());
             int* d_per = ar.take<int>(nc);
             ar.take<double>(nc);
             ar.take<double>(nc);
             float* d_fa = ar.take<float>(nc);
             float* d_fb = ar.take<float>(nc);
-            float2* d_p1 = ar.take<float2>(len);
-            float2* d_p2 = need2 ? ar.take<float2>(len) : nullptr;
-            double* d_tmp = ar.take<double>(prefix_tmp_doubles(n));
+            int* d_bad = ar.take<int>(2);
             VTA_TRY(upload(ctx, d_per, periods.data(), nc * sizeof(int)));
             VTA_TRY(upload(ctx, d_fa, fa.data(), nc * sizeof(float)));
             VTA_TRY(upload(ctx, d_fb, fb.data(), nc * sizeof(float)));
-            VTA_TRY(launch_prefix_f64(in.p[0], n, (int)first, PK_X, nullptr, d_p1, d_tmp, st));
-            if (need2) VTA_TRY(launch_prefix_f64(in.p[0], n, (int)first, PK_X2, nullptr, d_p2, d_tmp, st));
             PrefixWinArgs a{};
             a.kind = ind == I_SMA ? WK_SMA : ind == I_STDDEV ? WK_STDDEV : ind == I_ZSCORE ? WK_ZSCORE : WK_BB;
             a.x = in.p[0];
-            a.p1 = d_p1;
-            a.p2 = d_p2;
+            a.bad = d_bad;
             a.n = n;
             a.first = (int)first;
             a.periods = d_per;

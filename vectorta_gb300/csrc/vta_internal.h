@@ -289,8 +289,9 @@ enum WinKind { WK_SMA = 0, WK_STDDEV = 1, WK_ZSCORE = 2, WK_BB = 3 };
 struct PrefixWinArgs {
     int kind;
     const float* x;
-    const float2* p1;      // double-single prefix of x  (index i -> sum x[first..i])
-    const float2* p2;      // double-single prefix of x^2
+    // int[2] scratch: the first NaN / infinite input at or after `first`,
+    // filled by launch_prefix_window_batch
+    int* bad;
     int n, first;
     const int* periods;
     const float* k1;       // stddev/zscore nbdev; bb devup

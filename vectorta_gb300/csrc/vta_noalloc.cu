@@ -8,11 +8,9 @@
 //
 // Scratch layout (256-byte aligned pieces):
 //   [0, kPeriodBytes)                  int periods[kMaxCombos]
-//   [kPrefixOff, + kPrefixBytes)       float2 double-single prefix of x, kMaxLen
-//   [kBlockOff, + kBlockBytes)         f64 block sums of the prefix scan
-// No piece has to start at zero: the prefix reduce writes every block sum
-// before the block scan reads it, the apply pass writes prefix[0, len) before
-// the window kernel reads it, and the period list is copied in before use.
+//   [kBadOff, + 256)                   int bad[2]: first NaN / infinite input
+// No piece has to start at zero: the period list is copied in before use and
+// the window launcher sets bad[] before its scan.
 #include <cstdio>
 #include <mutex>
 
@@ -23,14 +21,10 @@ namespace {
 
 constexpr size_t kMaxLen = VTA_NOALLOC_MAX_LEN;
 constexpr size_t kMaxCombos = VTA_NOALLOC_MAX_COMBOS;
-constexpr size_t kMaxBlockDoubles = 4096;  // >= prefix_tmp_doubles(kMaxLen) (513)
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 constexpr size_t kPeriodBytes = align256(kMaxCombos * sizeof(int));
-constexpr size_t kPrefixOff = kPeriodBytes;
-constexpr size_t kPrefixBytes = align256(kMaxLen * sizeof(float2));
-constexpr size_t kBlockOff = kPrefixOff + kPrefixBytes;
-constexpr size_t kBlockBytes = align256(kMaxBlockDoubles * sizeof(double));
-constexpr size_t kScratchBytes = kBlockOff + kBlockBytes;
+constexpr size_t kBadOff = kPeriodBytes;
+constexpr size_t kScratchBytes = kBadOff + 256;
 static_assert(kScratchBytes == VTA_NOALLOC_SCRATCH_BYTES, "header and layout disagree");
 
 // One copy per device (per CUDA context of the process).  Uninitialised, so it
@@ -75,7 +69,7 @@ extern "C" vta_status vta_sma_batch_device_noalloc(vta_ctx* ctx, const float* d_
     char buf[240];
     if (len > kMaxLen) {
         std::snprintf(buf, sizeof buf,
-                      "sma_batch_device_noalloc: len %zu exceeds the fixed scratch limit of %zu bars "
+                      "sma_batch_device_noalloc: len %zu exceeds this entry point's limit of %zu bars "
                       "(VTA_NOALLOC_MAX_LEN); use vta_sma_batch_device",
                       len, kMaxLen);
         return fail(VTA_ERR_INVALID_INPUT, buf);
@@ -93,8 +87,6 @@ extern "C" vta_status vta_sma_batch_device_noalloc(vta_ctx* ctx, const float* d_
     VTA_TRY(vta_sma_expand_grid(sweep, params, kMaxCombos, &nc));
     VTA_TRY(validate_sma_periods(params, nc, len, first_valid));
     const int n = (int)len;
-    if ((size_t)prefix_tmp_doubles(n) > kMaxBlockDoubles)
-        return fail(VTA_ERR_INVALID_INPUT, "sma_batch_device_noalloc: scan block table too small");
 
     int periods[kMaxCombos];
     int pmax = 0;
@@ -106,16 +98,14 @@ extern "C" vta_status vta_sma_batch_device_noalloc(vta_ctx* ctx, const float* d_
     unsigned char* base = nullptr;
     VTA_TRY(scratch_on(ctx->device, &base));
     int* d_per = reinterpret_cast<int*>(base);
-    float2* d_prefix = reinterpret_cast<float2*>(base + kPrefixOff);
-    double* d_blocks = reinterpret_cast<double*>(base + kBlockOff);
+    int* d_bad = reinterpret_cast<int*>(base + kBadOff);
 
     cudaStream_t st = ctx->stream;
     VTA_CUDA_TRY(cudaMemcpyAsync(d_per, periods, nc * sizeof(int), cudaMemcpyHostToDevice, st));
-    VTA_TRY(launch_prefix_f64(d_data, n, (int)first_valid, PK_X, nullptr, d_prefix, d_blocks, st));
     PrefixWinArgs a{};
     a.kind = WK_SMA;
     a.x = d_data;
-    a.p1 = d_prefix;
+    a.bad = d_bad;
     a.n = n;
     a.first = (int)first_valid;
     a.periods = d_per;
