@@ -48,6 +48,43 @@ def peaks():
 
 
 # ------------------------------------------------------------- workloads ----
+def _dist():
+    """torch.distributed when a process group is up (torchrun, N > 1), else None."""
+    try:
+        import torch.distributed as dist
+    except Exception:
+        return None
+    return dist if dist.is_available() and dist.is_initialized() else None
+
+
+def barrier():
+    """All ranks meet here (no-op on one rank)."""
+    d = _dist()
+    if d is not None:
+        d.barrier()
+
+
+def rank_max(x: float) -> float:
+    """Maximum of x over the ranks (x itself on one rank)."""
+    d = _dist()
+    if d is None:
+        return float(x)
+    import torch
+
+    dev = "cuda" if d.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    d.all_reduce(t, op=d.ReduceOp.MAX)
+    return float(t.item())
+
+
+def combine_ranks(res: dict, world: int) -> dict:
+    """Whole-job figures of N replicas: the slowest rank's step time, and the
+    outputs of all ranks over it."""
+    res["ms_per_step"] = rank_max(res["ms_per_step"])
+    res["value"] = res["outputs_per_step"] * world / (res["ms_per_step"] / 1e3)
+    return res
+
+
 def workload_sweeps():
     from vectorta_gb300 import datagen
 
@@ -440,11 +477,13 @@ def gpu_bench(args, wl):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(0) as clk:
         torch.cuda.synchronize()
+        barrier()
         e0.record(stream)
         for _ in range(args.steps):
             step(record=True)
         e1.record(stream)
         torch.cuda.synchronize()
+        barrier()
     launches = V.launch_count() - launches0
     ms = e0.elapsed_time(e1)
     ms_per_step = ms / args.steps
@@ -511,12 +550,14 @@ def gpu_bench_plan(args, wl):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     graph_ms = []
     with ClockSampler(0) as clk:
+        barrier()
         e0.record(stream)
         for _ in range(args.steps):
             plan.run()
             graph_ms.append(ctx.kernel_ms)
         e1.record(stream)
         torch.cuda.synchronize()
+        barrier()
     ms = e0.elapsed_time(e1) / args.steps
     info = plan.info()
     g_ms = float(np.median(graph_ms))
@@ -944,13 +985,7 @@ def main():
     res = (gpu_bench_plan(args, wl) if kind == "plan" else
            gpu_bench_server(args, wl) if kind == "server" else gpu_bench(args, wl))
     if world > 1:
-        import torch
-        import torch.distributed as dist
-
-        t = torch.tensor([res["ms_per_step"]], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        res["ms_per_step"] = float(t.item())
-        res["value"] = res["outputs_per_step"] * world / (res["ms_per_step"] / 1e3)
+        combine_ranks(res, world)
     if rank != 0:
         return
     cpu = None
