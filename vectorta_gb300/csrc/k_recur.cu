@@ -11,7 +11,7 @@
 //       and write the outputs.
 // A "lane" is one parameter combo of a single-series sweep (batch layout:
 // every lane reads the same x[t], outputs are staged through shared memory so
-// each store instruction writes one contiguous 128-byte row segment) or one
+// each store instruction writes one contiguous 256-byte row segment) or one
 // series of a time-major matrix (coalesced loads and stores directly).
 // The warm-up rules (seed index, NaN prefix, running-mean outputs) follow the
 // crate's scalar paths cited on each op.
