@@ -153,15 +153,16 @@ def workload_ema_small():
 
 
 def workload_recur_small():
-    """Profiling case of the chunked recurrences: EMA and DEMA sweeps (periods
-    2..1000, 999 combos) on 400,000 bars (1.6 GB of outputs per call)."""
+    """Profiling case of the chunked recurrences: EMA, DEMA and RSI sweeps
+    (periods 2..1000, 999 combos) on 400,000 bars (1.6 GB of outputs per
+    call)."""
     from vectorta_gb300 import datagen
 
     n = 400_000
     close = datagen.random_walk(n, seed=1, nan_lead=200)
     rec = {"period": (2, 1000, 1)}
     return {"name": "recur_small", "n": n, "series": {"close": close.astype(np.float32)},
-            "jobs": [("ema", ["close"], rec), ("dema", ["close"], rec)], "dominant": "ema",
+            "jobs": [("ema", ["close"], rec), ("dema", ["close"], rec), ("rsi", ["close"], rec)], "dominant": "ema",
             "config": {"workload": "recur_small", "bars": n, "seed": 1, "combos": 999}}
 
 

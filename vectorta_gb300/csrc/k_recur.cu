@@ -469,6 +469,13 @@ __device__ __forceinline__ int warp_max(int v) {
     return v;
 }
 
+// Staging row write at column j ^ sw (sw = 0 or 1) with no per-step address
+// arithmetic once j is a compile-time constant: even columns go to row + sw,
+// odd ones to row - sw.
+__device__ __forceinline__ void stage_put(float* row, int sw, int j, float v) {
+    (j & 1 ? row - sw : row + sw)[j] = v;
+}
+
 // One warp = 32 lanes x one time chunk.  Tiles of 32 steps where every lane
 // of the warp is past its seed and warm-up take the fast path (no phase
 // checks: 2-6 FP ops per step); the few tiles around warm-up take the general
@@ -480,7 +487,7 @@ __device__ __forceinline__ void run_tile(Op& op, const InTile& ti, float* row, i
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
         const float y = op.template fast<FIN>(ti, ti.tb + j, steps);
-        if (PASS == PASS_EMIT) row[j ^ sw] = y;
+        if (PASS == PASS_EMIT) stage_put(row, sw, j, y);
     }
 }
 
@@ -494,7 +501,7 @@ __device__ __forceinline__ void run_tile(OpRsi<kB>& op, const InTile& ti, float*
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
             const float y = op.template fast<FIN>(ti, ti.tb + j, steps);
-            if (PASS == PASS_EMIT) row[j ^ sw] = y;
+            if (PASS == PASS_EMIT) stage_put(row, sw, j, y);
         }
     } else {
         float xp = __shfl_up_sync(0xffffffffu, ti.xv, 1);
@@ -508,7 +515,7 @@ __device__ __forceinline__ void run_tile(OpRsi<kB>& op, const InTile& ti, float*
             gs = fmaf(b, gs, __shfl_sync(0xffffffffu, gl, j));
             ls = fmaf(b, ls, __shfl_sync(0xffffffffu, ll, j));
             const float den = gs + ls;
-            row[j ^ sw] = den == 0.f ? 50.f : __fdividef(100.f * gs, den);
+            stage_put(row, sw, j, den == 0.f ? 50.f : __fdividef(100.f * gs, den));
         }
         op.ag = gs * op.inv_p;
         op.al = ls * op.inv_p;
@@ -528,7 +535,7 @@ __device__ __forceinline__ void run_tile(OpTema& op, const InTile& ti, float* ro
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
             const float y = op.template fast<FIN>(ti, ti.tb + j, steps);
-            if (PASS == PASS_EMIT) row[j ^ sw] = y;
+            if (PASS == PASS_EMIT) stage_put(row, sw, j, y);
         }
     } else {
         const float a = op.per, a2 = a * a, a3 = a2 * a, b = op.per1;
@@ -548,7 +555,7 @@ __device__ __forceinline__ void run_tile(OpTema& op, const InTile& ti, float* ro
             z2 = fmaf(b, z2, z1);
             z3 = fmaf(b, z3, z2);
             const float y = fmaf(a3, z3, fmaf(c2, z2, c1 * z1));
-            row[j ^ sw] = copy ? v : y;
+            stage_put(row, sw, j, copy ? v : y);
         }
         op.z1 = z1;
         op.z2 = z2;
