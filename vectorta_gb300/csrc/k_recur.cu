@@ -943,11 +943,16 @@ k_recur(RecurArgs a) {
             const int len = te - seg0;
             float* ob = a.out + (size_t)row0 * a.n + seg0;
             if (vec2 && len == kSeg) {
+                // rows 0..15 as staged, rows 16..31 with each pair swapped back
+                const int r16 = min(rows, 16);
+                float* op = ob + 2 * lane;
 #pragma unroll 4
-                for (int r = 0; r < rows; ++r) {
-                    float2 v = *reinterpret_cast<const float2*>(&stage[warp][r][2 * lane]);
-                    if ((r >> 4) & 1) v = make_float2(v.y, v.x);
-                    *reinterpret_cast<float2*>(ob + (size_t)r * a.n + 2 * lane) = v;
+                for (int r = 0; r < r16; ++r, op += a.n)
+                    *reinterpret_cast<float2*>(op) = *reinterpret_cast<const float2*>(&stage[warp][r][2 * lane]);
+#pragma unroll 4
+                for (int r = 16; r < rows; ++r, op += a.n) {
+                    const float2 v = *reinterpret_cast<const float2*>(&stage[warp][r][2 * lane]);
+                    *reinterpret_cast<float2*>(op) = make_float2(v.y, v.x);
                 }
             } else {
                 for (int h = lane; h < len; h += 32) {
