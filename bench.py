@@ -16,6 +16,18 @@ Metric: indicator outputs per second (higher is better).
          the calls' stream around exactly K steps.
   e2e:   the *_batch_into_host_f32 C-ABI calls from pinned host inputs to
          pinned host outputs (H2D + kernels + D2H of every output).
+  calls: each indicator's whole call (every kernel and the gaps between
+         them) timed with CUDA events; roofline.call_frac is the dominant
+         indicator's algorithmic bytes over its whole call.
+  err:   outside every timed region, in the CPU-baseline leg: max abs / rel
+         error of the device outputs against the oracle over every bar of
+         sampled rows (every row of the 100-combo windows, every 10th of the
+         999-combo recurrences); StdDev / Z-score also against the exact
+         window statistics.
+The default run adds two more figures, each with its own clock record:
+`alma_grid` (the 17,920-combo ALMA grid, roofline and error) and
+`served_stream` (Poisson 2,000 req/s for --duration = 60 s over the
+10,000-series store: p50/p99 latency, capacity, plain per-request ratio).
 `--impl reference` times the CPU reference restatement (oracle, all host
 threads) on a bounded sample of the same workload.
 """
@@ -464,11 +476,17 @@ def gpu_bench(args, wl):
     out_per_step = sum(rows[nm] * n * len(outs[nm]) for nm in rows)
 
     kernel_ms = {nm: [] for nm in rows}
+    call_ev = {nm: [] for nm in rows}
 
     def step(record=False):
         for name, ins, sweep in wl["jobs"]:
+            if record:
+                ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                ev[0].record(stream)
             inds[name].batch_device([d_series[k] for k in ins], n, firsts[name], sweep, outs[name])
             if record:
+                ev[1].record(stream)
+                call_ev[name].append(ev)
                 kernel_ms[name].append(ctx.kernel_ms)
 
     for _ in range(args.warmup):
@@ -498,6 +516,14 @@ def gpu_bench(args, wl):
     hbm, src = peaks()
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
     share = {nm: float(np.mean(v)) for nm, v in kernel_ms.items()}
+    # whole calls (every kernel of the call and the gaps between them), CUDA
+    # events on the calls' stream around each call of the timed steps
+    call_ms = {nm: float(np.mean([a.elapsed_time(b) for a, b in v])) for nm, v in call_ev.items()}
+    calls = {}
+    for name, ins, _ in wl["jobs"]:
+        b = rows[name] * n * 4 * len(outs[name]) + sum(wl["series"][k].nbytes for k in ins)
+        calls[name] = {"call_ms": call_ms[name], "kernel_ms": share[name], "bytes": b,
+                       "call_frac": b / (call_ms[name] / 1e3) / 1e9 / hbm}
 
     # e2e through the host-in / host-out C-ABI calls, pinned host buffers
     e2e = None
@@ -508,8 +534,10 @@ def gpu_bench(args, wl):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": TRAFFIC.get(wl["name"]),
                      "kernel": KERNEL_NAME.get(wl["name"]), "peak_source": src,
-                     "bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
-        "kernel_ms_per_call": share, "outputs_per_step": out_per_step, "e2e": e2e,
+                     "bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms,
+                     "call_ms": call_ms[dom], "call_frac": calls[dom]["call_frac"]},
+        "kernel_ms_per_call": share, "calls": calls, "outputs_per_step": out_per_step, "e2e": e2e,
+        "_state": {"inds": inds, "outs": outs, "rows": rows},
     }
 
 
@@ -858,6 +886,40 @@ def cpu_sample_plan(wl, every=64):
     return tasks
 
 
+def err_rows(name, n_rows):
+    """Rows whose every bar is compared with the oracle: every row of the
+    100-combo window sweeps, every 10th row (and the last) of the 999-combo
+    recurrence sweeps, 64 rows spread over the ALMA grid."""
+    if name == "alma":
+        return sorted(set(np.linspace(0, n_rows - 1, 64).round().astype(int).tolist()))
+    if n_rows <= 128:
+        return list(range(n_rows))
+    return sorted(set(range(0, n_rows, 10)) | {n_rows - 1})
+
+
+def measure_err(wl, state):
+    """Error of this run's device outputs against the oracle (CPU-baseline
+    leg; outside every timed region).  Per indicator: max abs and rel error
+    over every bar of the sampled rows (oracle/parity.py gives the
+    definitions), and for StdDev / Z-score the same against the exact window
+    statistics plus the crate's own drift from them."""
+    from oracle import parity as P
+
+    inds, outs, rows = state["inds"], state["outs"], state["rows"]
+    res = {}
+    for name, ins, sweep in wl["jobs"]:
+        combos = [tuple(c.values()) for c in inds[name].expand_grid(sweep)]
+
+        def fetch(r, name=name):
+            return np.concatenate([o[r].cpu().numpy() for o in outs[name]])
+
+        series = {k: wl["series"][k] for k in set(ins) | {"close"} if k in wl["series"]}
+        t0 = time.perf_counter()
+        res[name] = P.sweep_err(name, series, combos, fetch, err_rows(name, rows[name]))
+        res[name]["seconds"] = time.perf_counter() - t0
+    return res
+
+
 def e2e_bench(args, wl, inds, rows, out_per_step):
     import ctypes as C
 
@@ -897,7 +959,7 @@ def e2e_bench(args, wl, inds, rows, out_per_step):
                 ind.ctx.handle, *[host_in[k][0].value for k in ins], n, C.byref(s),
                 *[host_out[i].value for i in range(nout)], rows[name] * n, C.byref(r), C.byref(c)))
 
-    steps = max(1, min(args.steps, 2))
+    steps = max(1, args.steps)
     step()  # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -939,7 +1001,10 @@ def main():
     ap.add_argument("--workload", default="sweeps", choices=sorted(WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--duration", type=float, default=10.0, help="served_stream: seconds of Poisson arrivals")
+    ap.add_argument("--duration", type=float, default=60.0, help="served_stream: seconds of Poisson arrivals")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload: skip the ALMA-grid and served-stream figures")
+    ap.add_argument("--no-err", action="store_true", help="skip the error measurement against the oracle")
     ap.add_argument("--slots", type=int, default=8, help="served_stream: concurrent server slots")
     args = ap.parse_args()
 
@@ -985,24 +1050,68 @@ def main():
     kind = wl.get("kind")
     res = (gpu_bench_plan(args, wl) if kind == "plan" else
            gpu_bench_server(args, wl) if kind == "server" else gpu_bench(args, wl))
+    state = res.pop("_state", None)
     if world > 1:
         combine_ranks(res, world)
     if rank != 0:
         return
     cpu = None
+    err = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
         tasks = cpu_tasks(wl)
         v, dt, outs = run_cpu(tasks, threads)
         cpu = {"value": v, "unit": "outputs/s", "cores": threads, "kind": "port",
                "sample": sample_desc(wl, tasks, outs, dt, threads)}
+        if state is not None and not args.no_err:
+            err = measure_err(wl, state)
+    state = None
     line = dict(base, value=res["value"], ms_per_step=res["ms_per_step"], gpu_launches=res["gpu_launches"],
                 clocks=res["clocks"], roofline=res["roofline"], cpu_baseline=cpu, e2e=res["e2e"],
                 kernel_ms_per_call=res["kernel_ms_per_call"], outputs_per_step=res["outputs_per_step"])
-    for k in ("plan", "plain_per_request", "served", "capacity", "store"):
+    if err is not None:
+        line["err"] = err
+    for k in ("calls", "plan", "plain_per_request", "served", "capacity", "store"):
         if k in res:
             line[k] = res[k]
+    if args.workload == "sweeps" and world == 1 and not args.no_extras:
+        line.update(extras(args))
     print(json.dumps(line))
+
+
+def extras(args):
+    """The two other headline figures of the default run, each measured as
+    its own workload with its own clock record: the ALMA grid (17,920 combos x
+    200,000 bars on the tensor-core contraction, with its error against the
+    oracle) and the served mixed request stream (Poisson 2,000 req/s for
+    --duration seconds, p50/p99 latency, against plain per-request kernels)."""
+    import gc
+
+    import torch
+
+    out = {}
+    gc.collect()
+    torch.cuda.empty_cache()
+    wl = workload_alma_grid()
+    r = gpu_bench(args, wl)
+    st = r.pop("_state")
+    e = None if (args.no_cpu or args.no_err) else measure_err(wl, st)["alma"]
+    st = None
+    out["alma_grid"] = {"config": wl["config"], "value": r["value"], "unit": "outputs/s",
+                        "ms_per_step": r["ms_per_step"], "roofline": r["roofline"], "clocks": r["clocks"],
+                        "err": e, "e2e": r["e2e"], "gpu_launches": r["gpu_launches"]}
+    r = None
+    gc.collect()
+    torch.cuda.empty_cache()
+    wl = workload_served_stream()
+    r = gpu_bench_server(args, wl)
+    out["served_stream"] = {"config": dict(wl["config"], duration_s=args.duration), "clocks": r["clocks"],
+                            "served": r["served"], "capacity": r["capacity"],
+                            "plain_per_request": r["plain_per_request"], "store": r["store"],
+                            "roofline": r["roofline"], "gpu_launches": r["gpu_launches"]}
+    gc.collect()
+    torch.cuda.empty_cache()
+    return out
 
 
 if __name__ == "__main__":

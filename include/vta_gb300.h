@@ -836,7 +836,7 @@ vta_status vta_server_destroy(vta_server* s);
  * call (sma_batch_dev_from_device, sma_wrapper.rs:830-841, allocates the
  * period list, the prefix and the output), and so do the other entry points
  * here.  vta_sma_batch_device_noalloc returns what vta_sma_batch_device
- * returns (same arguments, checks and errors) but never allocates device
+ * returns (same arguments and parameter checks) but never allocates device
  * memory: its working buffers live in one fixed scratch area of the library's
  * static device memory (VTA_NOALLOC_SCRATCH_BYTES, about 16 KiB per device,
  * reserved on a device when the function is first called there).
@@ -850,7 +850,12 @@ vta_status vta_server_destroy(vta_server* s);
  *     the limit (vta_sma_batch_device has no such limit).
  *   - The first call on each device does one-time setup (it looks up the
  *     scratch address, which loads the library's device code there); make
- *     that first call before any stream capture on that device.
+ *     that first call before any stream capture on that device.  No call can
+ *     be captured: each uploads its period list from host memory and waits
+ *     for its stream.
+ *   - The period count is taken from the range arithmetic before anything
+ *     is expanded, so an oversized sweep is refused at once; the periods
+ *     live on the caller's stack (16 KiB at the limit).
  *   - There is one scratch area per device per process.  Calls that overlap
  *     in time on the same device (from several host threads, whatever their
  *     contexts or streams) race on it and corrupt each other's results:

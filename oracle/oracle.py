@@ -79,6 +79,9 @@ def lib():
             "vto_stddev": ([dp, sz, sz, db, dp], ip),
             "vto_zscore": ([dp, sz, sz, db, dp], ip),
             "vto_zscore_batch_row": ([dp, sz, sz, db, dp], ip),
+            "vto_stddev_batch_prefix": ([dp, sz, sz, db, dp], ip),
+            "vto_window_exact": ([dp, sz, sz, szp, sz, dp, dp], ip),
+            "vto_alma_batch_row_at": ([dp, sz, sz, db, db, szp, sz, dp], ip),
             "vto_bollinger": ([dp, sz, sz, db, db, dp, dp, dp], ip),
             "vto_donchian": ([dp, dp, sz, sz, dp, dp, dp], ip),
             "vto_willr": ([dp, dp, dp, sz, sz, dp], ip),
@@ -214,6 +217,24 @@ def zscore(x, period=14, nbdev=1.0):
 
 def zscore_batch_row(x, period=14, nbdev=1.0):
     return _single("vto_zscore_batch_row", x, period, nbdev)
+
+
+def stddev_batch_prefix(x, period=5, nbdev=1.0):
+    """The crate's batch StdDev row: differences of whole-series f64 prefixes."""
+    return _single("vto_stddev_batch_prefix", x, period, nbdev)
+
+
+def window_exact(x, period, idx):
+    """Exact (corrected two-pass f64) mean and population standard deviation of
+    the windows [i-period+1, i] ending at each index in `idx`.  Not a crate
+    path: the yardstick that measures the crate's running-sum drift."""
+    x = _f64(x)
+    idx = np.ascontiguousarray(idx, dtype=np.uintp)
+    mean = np.empty(idx.size)
+    sd = np.empty(idx.size)
+    _check(lib().vto_window_exact(_p(x), x.size, period, idx.ctypes.data_as(C.POINTER(C.c_size_t)), idx.size,
+                                  _p(mean), _p(sd)), "window_exact")
+    return mean, sd
 
 
 def percentile_nearest_rank(x, length=15, percentage=50.0):
@@ -404,6 +425,17 @@ def alma_batch(x, period_rng, offset_rng, sigma_rng):
     _check(lib().vto_alma_batch(_p(x), x.size, rows, P.ctypes.data_as(C.POINTER(C.c_size_t)),
                                 _p(O), _p(S), _p(out)), "alma_batch")
     return out, combos
+
+
+def alma_batch_row_at(x, period, offset, sigma, idx):
+    """One alma_batch row (batch weights) evaluated at the end indices idx."""
+    x = _f64(x)
+    idx = np.ascontiguousarray(idx, dtype=np.uintp)
+    out = np.empty(idx.size)
+    _check(lib().vto_alma_batch_row_at(_p(x), x.size, period, offset, sigma,
+                                       idx.ctypes.data_as(C.POINTER(C.c_size_t)), idx.size, _p(out)),
+           "alma_batch_row_at")
+    return out
 
 
 def _period_batch(fname, x, periods):

@@ -233,6 +233,36 @@ int vto_alma_batch(const double *x, size_t n, size_t rows, const size_t *periods
     return VTO_OK;
 }
 
+/* One row of vto_alma_batch evaluated only at the end indices idx[0..nidx)
+ * (same batch weights, same 4-wide dot as alma_row; NaN before the row's
+ * warm-up end first + p - 1).  Lets a test check every row of a large grid
+ * on a time sample without computing the whole row. */
+int vto_alma_batch_row_at(const double *x, size_t n, size_t period, double offset, double sigma,
+                          const size_t *idx, size_t nidx, double *out) {
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    double *w = (double *)malloc(sizeof(double) * period);
+    double inv_n;
+    vto_alma_weights_batch(period, offset, sigma, w, &inv_n);
+    size_t p4 = period & ~(size_t)3;
+    for (size_t k = 0; k < nidx; k++) {
+        size_t i = idx[k];
+        if (i >= n) { free(w); return VTO_E_INVALID_RANGE; }
+        if (i < first + period - 1) { out[k] = QNAN; continue; }
+        size_t start = i + 1 - period;
+        double sum = 0.0;
+        for (size_t j = 0; j < p4; j += 4) {
+            const double *d = x + start + j;
+            sum += d[0] * w[j] + d[1] * w[j + 1] + d[2] * w[j + 2] + d[3] * w[j + 3];
+        }
+        for (size_t j = p4; j < period; j++) sum += x[start + j] * w[j];
+        out[k] = sum * inv_n;
+    }
+    free(w);
+    return VTO_OK;
+}
+
 /* ------------------------------------------------------------------------ */
 /* EMA / DEMA / TEMA                                                          */
 /* ------------------------------------------------------------------------ */
@@ -792,6 +822,89 @@ int vto_stddev(const double *x, size_t n, size_t period, double nbdev, double *o
     if (period == 0 || period > n) return VTO_E_INVALID_PERIOD;
     if (n - first < period) return VTO_E_NOT_ENOUGH_VALID;
     stddev_row(x, n, first, period, nbdev, out);
+    return VTO_OK;
+}
+
+/* The crate's batch StdDev row (stddev_batch_inner with Kernel::Scalar,
+ * stddev.rs:822-1060): f64 prefixes ps, ps2 of x and x^2 and a NaN-count
+ * prefix over the WHOLE series (build_std_prefixes, stddev.rs:878-897), then
+ * per output sum = ps[i+1] - ps[i+1-p], sum2 likewise and
+ * var = sum2.mul_add(1/p, -(sum*sum) * (1/p)^2) (stddev_from_prefix_scalar,
+ * stddev.rs:899-935, called per row at stddev.rs:1043-1050); a window holding
+ * a NaN gives NaN. */
+int vto_stddev_batch_prefix(const double *x, size_t n, size_t period, double nbdev, double *out) {
+    if (n == 0) return VTO_E_EMPTY;
+    size_t first = first_valid(x, n);
+    if (first >= n) return VTO_E_ALL_NAN;
+    if (period == 0 || n - first < period) return VTO_E_NOT_ENOUGH_VALID;
+    double *ps = (double *)malloc(sizeof(double) * (n + 1));
+    double *ps2 = (double *)malloc(sizeof(double) * (n + 1));
+    int *pn = (int *)malloc(sizeof(int) * (n + 1));
+    ps[0] = ps2[0] = 0.0;
+    pn[0] = 0;
+    for (size_t i = 0; i < n; i++) {
+        double v = x[i];
+        if (isnan(v)) {
+            ps[i + 1] = ps[i];
+            ps2[i + 1] = ps2[i];
+            pn[i + 1] = pn[i] + 1;
+        } else {
+            ps[i + 1] = ps[i] + v;
+            ps2[i + 1] = ps2[i] + v * v;
+            pn[i + 1] = pn[i];
+        }
+    }
+    size_t we = first + period - 1;
+    fill_nan(out, we < n ? we : n);
+    double inv = 1.0 / (double)period, inv2 = inv * inv;
+    for (size_t i = we; i < n; i++) {
+        if (pn[i + 1] - pn[i + 1 - period] > 0) {
+            out[i] = QNAN;
+            continue;
+        }
+        double s = ps[i + 1] - ps[i + 1 - period];
+        double s2 = ps2[i + 1] - ps2[i + 1 - period];
+        double var = fma(s2, inv, -(s * s) * inv2);
+        out[i] = var <= 0.0 ? 0.0 : sqrt(var) * nbdev;
+    }
+    free(ps);
+    free(ps2);
+    free(pn);
+    return VTO_OK;
+}
+
+/* NOT a restatement of the crate: the exact window statistics that the
+ * crate's StdDev / Z-score paths approximate, used to measure how far the
+ * crate's own running f64 sums drift on long series.  For each requested end
+ * index i (window [i-p+1, i], all values finite) it returns the mean and the
+ * population standard deviation by the corrected two-pass algorithm in f64
+ * (Chan, Golub and LeVeque 1983: mean by a compensated sum, then
+ * sum (x-m)^2 - (sum (x-m))^2 / p), whose relative error is a few f64 ulps
+ * for windows of up to thousands of values. */
+int vto_window_exact(const double *x, size_t n, size_t period, const size_t *idx, size_t nidx,
+                     double *mean, double *sd) {
+    if (period == 0) return VTO_E_INVALID_PERIOD;
+    for (size_t k = 0; k < nidx; k++) {
+        size_t i = idx[k];
+        if (i >= n || i + 1 < period) return VTO_E_INVALID_RANGE;
+        const double *w = x + (i + 1 - period);
+        double s = 0.0, c = 0.0; /* Neumaier compensated sum */
+        for (size_t j = 0; j < period; j++) {
+            double t = s + w[j];
+            c += fabs(s) >= fabs(w[j]) ? (s - t) + w[j] : (w[j] - t) + s;
+            s = t;
+        }
+        double m = (s + c) / (double)period;
+        double d1 = 0.0, d2 = 0.0;
+        for (size_t j = 0; j < period; j++) {
+            double d = w[j] - m;
+            d1 += d;
+            d2 += d * d;
+        }
+        double var = (d2 - d1 * d1 / (double)period) / (double)period;
+        mean[k] = m;
+        sd[k] = var > 0.0 ? sqrt(var) : 0.0;
+    }
     return VTO_OK;
 }
 

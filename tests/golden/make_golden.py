@@ -1,7 +1,11 @@
 """Regenerate the golden fixtures in this folder from the VectorTA sources.
 
-Run in a container where the reference checkout exists (default path below,
-or pass it as argv[1]).  Produces:
+Run where a checkout of the VectorTA project exists; its root is the
+required argument (or the VECTORTA_ROOT environment variable):
+
+    python tests/golden/make_golden.py <path to the VectorTA checkout>
+
+Produces:
 
 * ``bitfinex_4h.npz``  -- OHLCV columns (float64) of the crate's fixture
   ``src/data/2018-09-01-2024-Bitfinex_Spot-4h.csv``, loaded with the crate's
@@ -139,4 +143,7 @@ def main(ref: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("VECTORTA_ROOT")
+    if not root:
+        sys.exit("usage: make_golden.py <path to the VectorTA checkout> (or set VECTORTA_ROOT)")
+    main(root)

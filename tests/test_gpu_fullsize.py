@@ -1,40 +1,64 @@
-"""Parity at the benchmark workloads' full sizes, where the oracle cannot run
-every row in seconds: each row's NaN warm-up prefix is checked for every combo
-(size-independent: it depends only on the first valid index and the
-parameters), and evenly spaced sampled rows are checked value by value against
-the oracle at the crate's GPU-test tolerances.
+"""Parity at the benchmark workloads' full sizes, on every row.
+
+Each row's NaN warm-up prefix is checked for every combo, and every row is
+compared with the oracle on a time sample: every 997th bar from the row's
+warm-up end, plus the first 2p bars after it (where a recurrence is still
+close to its seed).  The measured error of each indicator, per period band, is
+printed and, with VTA_PARITY_REPORT=<file>, appended to that file as JSON.
 
 * recurrence and window sweeps: 1,000,000 bars (seed 1, NaN lead 200),
   EMA / DEMA / TEMA / RSI periods 2..1000, SMA / StdDev / Z-score / Donchian /
   WillR windows 5..500 step 5;
 * ALMA grid: 200,000 bars (seed 2), periods 5..260 x offsets 0.50..0.95 x
   sigmas 3..9 (17,920 combos, 14 GB of outputs).
+
+StdDev and Z-score are also compared with the exact window statistics.  The
+crate's scalar paths keep f64 running sums of x and x^2 over the whole series;
+where this series falls far below its earlier levels (it spans 0.02 to 33,000)
+those sums drift by more than the window's variance, and the crate's output
+there is off by up to 200% (or clamped to 0, or NaN for Z-score) against the
+exact statistic.  The device path differences block-local prefixes and has no
+such drift.  So every sampled cell is checked against the exact statistic, and
+against the crate wherever the crate itself is within a tenth of the
+tolerance of the exact statistic; the remaining cells (the crate's drift) are
+counted and their error against the crate is reported, not hidden.
 """
+import json
+import os
+from concurrent.futures import ThreadPoolExecutor
+
 import numpy as np
 import pytest
 
 from oracle import oracle as O
+from oracle import parity as P
 from vectorta_gb300 import cuda as V
 from vectorta_gb300 import datagen
 
 pytestmark = pytest.mark.gpu
 
 N_BARS, LEAD = 1_000_000, 200
-# The crate's GPU-test tolerances, except DEMA / TEMA: their f32 recurrences'
-# relative error grows with the period (measured on this workload: 2e-7 at
-# p = 2, 1e-6 at p = 100, up to 1.2e-5 at p = 1000), past the crate's 5e-6 /
-# 1e-5, which its tests apply to short periods.
-TOL = {"ema": 5e-5, "dema": 2e-5, "tema": 2e-5, "rsi": 5e-4, "sma": 1e-5, "stddev": 5e-4, "zscore": 5e-4,
-       "donchian": 5e-4, "willr": 5e-5, "alma": 1e-5}
+# Tolerances of the mixed test |gpu - ref| <= tol * (1 + max(|gpu|, |ref|)),
+# per period band (upper period bound, tol).  The crate's GPU-test
+# tolerances, except where an f32 recurrence's rounding noise, which grows
+# with the period's memory, passes them: DEMA keeps the crate's 5e-6
+# (dema_cuda.rs) up to period 400 and 1e-5 beyond (measured maximum relative
+# error 6.8e-6 at p = 700..1000), TEMA the crate's 1e-5 (tema_cuda.rs) up to
+# period 400 and 2e-5 beyond (measured 1.7e-5).  The measured maxima per band
+# are printed by the test.
+TOL = {"ema": [(1000, 5e-5)], "dema": [(400, 5e-6), (1000, 1e-5)], "tema": [(400, 1e-5), (1000, 2e-5)],
+       "rsi": [(1000, 5e-4)], "sma": [(500, 1e-5)], "stddev": [(500, 5e-4)], "zscore": [(500, 5e-4)],
+       "donchian": [(500, 5e-4)], "willr": [(500, 5e-5)], "alma": [(260, 1e-5)]}
+# against the exact window statistics (StdDev relative; Z-score mixed)
+TOL_EXACT = {"stddev": 2e-5, "zscore": 1e-4}
+BANDS = [(2, 10), (11, 100), (101, 200), (201, 1000)]
 
 
-def assert_close(gpu, cpu, tol, what):
-    gpu, cpu = np.asarray(gpu, np.float64), np.asarray(cpu, np.float64)
-    assert np.array_equal(np.isnan(gpu), np.isnan(cpu)), what
-    m = ~np.isnan(cpu)
-    d = np.abs(gpu[m] - cpu[m])
-    lim = tol + tol * np.maximum(np.abs(gpu[m]), np.abs(cpu[m]))
-    assert np.all(d <= lim), (what, float(np.max(d - lim)))
+def tol_for(name, p):
+    for pmax, t in TOL[name]:
+        if p <= pmax:
+            return t
+    raise AssertionError((name, p))
 
 
 @pytest.fixture(scope="module")
@@ -61,20 +85,27 @@ SWEEPS = {
 }
 
 
-def oracle_row(name, d, p):
-    c = d["close"].astype(np.float64)
-    h, l = d["high"].astype(np.float64), d["low"].astype(np.float64)
-    if name == "rsi":
-        return O.rsi_batch(c, [p])[0]
-    if name == "stddev":
-        return O.stddev(c, p, 1.0)
-    if name == "zscore":
-        return O.zscore_batch_row(c, p, 1.0)
-    if name == "donchian":
-        return O.donchian(h, l, p)[0]
-    if name == "willr":
-        return O.willr(h, l, c, p)
-    return {"ema": O.ema, "dema": O.dema, "tema": O.tema, "sma": O.sma}[name](c, p)
+def sample_idx(n, warm, p):
+    """Every 997th bar from the warm-up end, plus the first 2p bars after it."""
+    return np.union1d(np.arange(warm, n, 997), np.arange(warm, min(n, warm + 2 * p)))
+
+
+def mixed_excess(g, e, tol):
+    """max of |g - e| - tol * (1 + max(|g|, |e|)) over non-NaN cells (<= 0 passes)."""
+    m = ~np.isnan(e)
+    d = np.abs(g[m] - e[m])
+    return float(np.max(d - tol * (1.0 + np.maximum(np.abs(g[m]), np.abs(e[m]))))) if m.any() else -1.0
+
+
+def report(name, bands, extra=None):
+    line = {"indicator": name, "bands": bands}
+    if extra:
+        line.update(extra)
+    print(json.dumps(line))
+    path = os.environ.get("VTA_PARITY_REPORT")
+    if path:
+        with open(path, "a") as f:
+            f.write(json.dumps(line) + "\n")
 
 
 @pytest.mark.parametrize("name", sorted(SWEEPS))
@@ -82,30 +113,81 @@ def test_sweep_full_size(name, sweep_data):
     ind = V.CLASSES[name](0)
     ins = {"x": ["close"], "hl": ["high", "low"], "hlc": ["high", "low", "close"]}[V.N.INDICATORS[name][0]]
     out = ind.batch_dev(*[sweep_data[k] for k in ins], sweep=SWEEPS[name])
-    got = (out[0] if isinstance(out, tuple) else out).to_host()  # Donchian: the upper band
-    periods = O.periods_of(name, SWEEPS[name]["period"])
-    assert got.shape == (len(periods), N_BARS)
+    outs = [o.to_host() for o in (out if isinstance(out, tuple) else (out,))]  # Donchian: upper, middle, lower
+    combos = [tuple(c.values()) for c in ind.expand_grid(SWEEPS[name])]
+    periods = [int(c[0]) for c in combos]
+    assert outs[0].shape == (len(periods), N_BARS)
     # every row: NaN exactly before its warm-up end
-    finite = ~np.isnan(got)
+    finite = ~np.isnan(outs[0])
     first = np.where(finite.any(axis=1), finite.argmax(axis=1), N_BARS)
     exp_first = np.array([min(WARM[name](LEAD, p), N_BARS) for p in periods])
     assert np.array_equal(first, exp_first), (name, np.flatnonzero(first != exp_first)[:5])
-    # sampled rows against the oracle
-    keep = np.ones(N_BARS, dtype=bool)
-    if name in ("stddev", "zscore"):
-        # The crate's StdDev / Z-score keep f64 running sums of x and x^2 over
-        # the whole series; where the series has fallen far below its earlier
-        # levels their drift (~sqrt(t) ulp of the largest sum) swamps the
-        # variance, so the oracle is compared only where x(t) >= 1% of its
-        # running maximum (69% of this series).  The GPU path differences
-        # block-local prefixes and has no such drift.
-        c = sweep_data["close"].astype(np.float64)
-        keep = np.nan_to_num(c) >= 0.01 * np.fmax.accumulate(np.nan_to_num(c))
-    for r in np.linspace(0, len(periods) - 1, 6).round().astype(int):
-        exp = oracle_row(name, sweep_data, periods[r])
-        # (Z-score is NaN where its deviation is 0, which the drifting sums
-        # also decide: the NaN mask is compared on the same positions)
-        assert_close(got[r][keep], exp[keep], TOL[name], f"{name} p={periods[r]}")
+
+    s64 = {k: v.astype(np.float64) for k, v in sweep_data.items()}
+    drift = name in ("stddev", "zscore")
+    floor = P.rel_floor(name)
+
+    def row(r):
+        p = periods[r]
+        idx = sample_idx(N_BARS, exp_first[r], p)
+        ref = P.oracle_row(name, s64, combos[r])
+        nb = len(outs)
+        g = np.concatenate([o[r][idx] for o in outs])
+        e = np.concatenate([ref[k * N_BARS:(k + 1) * N_BARS][idx] for k in range(nb)])
+        res = {"r": r, "p": p, "g": g, "e": e}
+        if drift:
+            res["x"] = P.exact_window(name, s64["close"], combos[r], idx)
+        return res
+
+    with ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+        rows = list(ex.map(row, range(len(periods))))
+
+    # all figures first (reported even when an assertion below fails)
+    bands, fails = {}, []
+    drift_cells, drift_max = 0, 0.0
+    ex_acc = P.Acc(floor)
+    for res in rows:
+        p, g, e = res["p"], res["g"], res["e"]
+        band = next(f"{a}-{b}" for a, b in BANDS if a <= p <= b)
+        acc = bands.setdefault(band, P.Acc(floor))
+        tol = tol_for(name, p)
+        if not drift:
+            if not np.array_equal(np.isnan(g), np.isnan(e)):
+                fails.append((p, "NaN cells differ"))
+            ex = mixed_excess(g, e, tol)
+            if ex > 0.0:
+                fails.append((p, "vs crate", ex))
+            acc.add(g, e)
+            continue
+        x = res["x"]
+        ex_acc.add(g, x)
+        # against the exact window statistic: every sampled cell
+        if not np.array_equal(np.isnan(g), np.isnan(x)):
+            fails.append((p, "NaN cells differ from the exact statistic"))
+        if name == "stddev":
+            m = x > 0
+            if not np.all(np.abs(g[m] - x[m]) <= TOL_EXACT[name] * x[m]):
+                fails.append((p, "vs exact", float(np.max(np.abs(g[m] - x[m]) / x[m]))))
+        elif mixed_excess(g, x, TOL_EXACT[name]) > 0.0:
+            fails.append((p, "vs exact", mixed_excess(g, x, TOL_EXACT[name])))
+        # against the crate where its own running sums have not drifted
+        with np.errstate(invalid="ignore"):
+            crate_ok = np.abs(e - x) <= 0.1 * tol * (1.0 + np.abs(x))
+        if not np.all(np.isnan(e[crate_ok]) == np.isnan(g[crate_ok])):
+            fails.append((p, "NaN cells differ from the crate where it has not drifted"))
+        if mixed_excess(g[crate_ok], e[crate_ok], tol) > 0.0:
+            fails.append((p, "vs crate", mixed_excess(g[crate_ok], e[crate_ok], tol)))
+        acc.add(g[crate_ok], e[crate_ok])
+        drift_cells += int((~crate_ok).sum())
+        if (~crate_ok).any():
+            a, r_, _, _ = P.cell_err(g[~crate_ok], e[~crate_ok], floor)
+            drift_max = max(drift_max, r_)
+    extra = {"failures": fails[:10]} if fails else {}
+    if drift:
+        extra.update({"vs_exact": ex_acc.as_dict(), "crate_drift_cells": drift_cells,
+                      "vs_crate_on_drift_cells_rel": drift_max})
+    report(name, {b: a.as_dict() for b, a in bands.items()}, extra)
+    assert not fails, (name, len(fails), fails[:5])
 
 
 def test_alma_grid_full_size():
@@ -113,21 +195,32 @@ def test_alma_grid_full_size():
     sweep = {"period": (5, 260, 1), "offset": (0.50, 0.95, 0.05), "sigma": (3.0, 9.0, 1.0)}
     ind = V.CudaAlma(0)
     got = ind.alma_batch_dev(x, sweep=sweep).to_host()
+    combos = [(c["period"], c["offset"], c["sigma"]) for c in ind.expand_grid(sweep)]
+    assert got.shape == (len(combos), x.size) == (17920, 200_000)
+    # combo order: period-major, then offset, then sigma (the oracle's own
+    # restatement of the crate's expand_grid)
     periods = list(range(5, 261))
     offsets = O.axis_f64(sweep["offset"])
     sigmas = O.axis_f64(sweep["sigma"])
-    assert got.shape == (len(periods) * len(offsets) * len(sigmas), x.size) == (17920, 200_000)
-    # combo order: period-major, then offset, then sigma; NaN prefix p - 1
+    assert [c[0] for c in combos] == list(np.repeat(periods, len(offsets) * len(sigmas)))
+    assert [c[1] for c in combos[:len(offsets) * len(sigmas)]] == list(np.repeat(offsets, len(sigmas)))
+    assert [c[2] for c in combos[:len(sigmas)]] == sigmas
+    # every row: NaN prefix p - 1
     first = np.isnan(got).argmin(axis=1)
-    exp_first = np.repeat(np.array(periods) - 1, len(offsets) * len(sigmas))
-    assert np.array_equal(first, exp_first)
+    assert np.array_equal(first, np.array([c[0] - 1 for c in combos]))
     xd = x.astype(np.float64)
-    for r in np.linspace(0, got.shape[0] - 1, 12).round().astype(int):
-        p = periods[r // (len(offsets) * len(sigmas))]
-        o = offsets[(r // len(sigmas)) % len(offsets)]
-        s = sigmas[r % len(sigmas)]
-        exp = O.alma_batch(xd, (p, p, 0), (o, o, 0.0), (s, s, 0.0))[0][0]  # the batch rows' weights
-        m = ~np.isnan(exp)
-        assert np.array_equal(np.isnan(got[r]), ~m)
-        rel = np.max(np.abs(got[r][m] - exp[m]) / np.abs(exp[m]))
-        assert rel <= TOL["alma"], (p, o, s, rel)
+
+    def row(r):
+        p, o, s = combos[r]
+        idx = sample_idx(x.size, p - 1, p)
+        exp = O.alma_batch_row_at(xd, p, o, s, idx)
+        g = got[r][idx].astype(np.float64)
+        return p, float(np.max(np.abs(g - exp) / np.abs(exp))), bool(np.isnan(g).any())
+
+    with ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+        res = list(ex.map(row, range(len(combos))))
+    assert not any(nan for _, _, nan in res)
+    worst = max(res, key=lambda t: t[1])
+    assert worst[1] <= tol_for("alma", worst[0]), worst
+    acc = {f"{a}-{b}": max([r for p, r, _ in res if a <= p <= b], default=0.0) for a, b in [(5, 64), (65, 260)]}
+    report("alma_grid", {k: {"rel": v} for k, v in acc.items()}, {"rows": len(res)})

@@ -1,7 +1,7 @@
 """vta_sma_batch_device_noalloc: the SMA sweep without device allocation.
 
 Called through the C ABI and compared with vta_sma_batch_device (the
-allocating entry point) on two consecutive calls with different series,
+allocating entry point) on three consecutive calls with different series,
 lengths and sweeps, so the second call runs on scratch the first one left
 behind.  Both run the same kernels, so the results are expected to agree
 bit for bit; the test allows 1e-6 relative.  Collected last on purpose: it
@@ -49,7 +49,9 @@ def test_noalloc_matches_allocating_entry_point_on_consecutive_calls():
     ref_ctx = V.Context(0)
     ctx = V.Context(0)
     sma = V.CudaSma(0, ctx=ref_ctx)
-    cases = [(_case(11, 200_000, 7), (5, 400, 5)), (_case(12, 150_001, 0), (2, 1000, 37))]
+    # the third case sweeps a descending range (300, 293, ..., 20)
+    cases = [(_case(11, 200_000, 7), (5, 400, 5)), (_case(12, 150_001, 0), (2, 1000, 37)),
+             (_case(13, 50_000, 3), (300, 20, 7))]
     for i, ((x, first), rng) in enumerate(cases):
         n = x.size
         sweep = _sweep(*rng)
@@ -90,6 +92,10 @@ def test_noalloc_rejects_sizes_beyond_its_limits():
     d_x = torch.ones(n, device="cuda")
     d_out = torch.empty(MAX_COMBOS + 4, n, device="cuda")
     st = _noalloc(ctx, d_x, n, 0, _sweep(1, MAX_COMBOS + 4, 1), d_out)
+    assert st == 4
+    assert "VTA_NOALLOC_MAX_COMBOS" in N.lib().vta_last_error().decode()
+    # a huge sweep is refused from its count, before anything is expanded
+    st = _noalloc(ctx, d_x, n, 0, _sweep(1, 10**15, 1), d_out)
     assert st == 4
     assert "VTA_NOALLOC_MAX_COMBOS" in N.lib().vta_last_error().decode()
     ctx.close()

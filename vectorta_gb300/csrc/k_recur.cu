@@ -138,9 +138,13 @@ struct OpEma {
     }
     __device__ float cur_mean() const { return wsum.f() / (float)wcnt; }
     __device__ void seed() { y = cur_mean(); }
+    // y <- y + alpha (x - y): the fixed point is x itself whatever the f32
+    // rounding of alpha.  The crate's form beta y + alpha x, with alpha and
+    // beta = 1 - alpha rounded to f32 separately, has the steady-state gain
+    // alpha / (1 - beta) = 1 + O(2^-25 / alpha): a bias of 1.5e-5 at p = 1000.
     template <class In> __device__ int step(const In& in, int t) {
         float v = in.X(t);
-        if (isfinite(v)) { y = fmaf(beta, y, alpha * v); return 1; }
+        if (isfinite(v)) { y = fmaf(alpha, v - y, y); return 1; }
         return 0;
     }
     template <class In> __device__ float value(const In&, int) const { return y; }
@@ -153,12 +157,12 @@ struct OpEma {
     template <bool FIN = false, class In> __device__ float fast(const In& in, int t, int& applied) {
         const float v = in.X(t);
         if (FIN) {
-            y = fmaf(beta, y, alpha * v);
+            y = fmaf(alpha, v - y, y);
             ++applied;
             return y;
         }
         const bool ok = isfinite(v);
-        y = ok ? fmaf(beta, y, alpha * v) : y;
+        y = ok ? fmaf(alpha, v - y, y) : y;
         applied += ok;
         return y;
     }
@@ -184,10 +188,11 @@ struct OpDema {
     }
     template <class In> __device__ void accum(const In& in, int t) { xf = in.X(t); }
     __device__ void seed() { e1 = xf; e2 = xf; }
+    // gain-exact form of e <- a e + alpha x (see OpEma::step)
     template <class In> __device__ int step(const In& in, int t) {
         float v = in.X(t);
-        e1 = fmaf(e1, a, v * alpha);
-        e2 = fmaf(e2, a, e1 * alpha);
+        e1 = fmaf(alpha, v - e1, e1);
+        e2 = fmaf(alpha, e1 - e2, e2);
         return 1;
     }
     template <class In> __device__ float value(const In&, int t) const {
@@ -199,8 +204,8 @@ struct OpDema {
     __device__ void set(int i, float v) { if (i == 0) e1 = v; else e2 = v; }
     template <bool FIN = false, class In> __device__ float fast(const In& in, int t, int& applied) {
         const float v = in.X(t);
-        e1 = fmaf(e1, a, v * alpha);
-        e2 = fmaf(e2, a, e1 * alpha);
+        e1 = fmaf(alpha, v - e1, e1);
+        e2 = fmaf(alpha, e1 - e2, e2);
         ++applied;
         return fmaf(e1, 2.f, -e2);
     }
@@ -221,11 +226,8 @@ struct OpTema {
     static constexpr int NS = 3;
     static constexpr int kShape = 1;
     float per, per1, e1, e2, e3;
-    float z1, z2, z3;  // scaled state of the emit fast tiles (valid while zs)
-    bool zs;
     int f, s, warm, start2, p1;
     __device__ void init(int p, int first) {
-        zs = false;
         double pd = 2.0 / ((double)p + 1.0);
         per = (float)pd;
         per1 = (float)(1.0 - pd);
@@ -237,18 +239,19 @@ struct OpTema {
         float v = in.X(t);
         if (p1 == 0) { e1 = v; return; }
         if (t == f) e1 = v;  // ema1 = data[first]; the loop then re-applies it
-        e1 = e1 * per1 + v * per;
-        if (t == start2) { e2 = e1; e2 = e2 * per1 + e1 * per; }
-        else if (t > start2) e2 = e2 * per1 + e1 * per;
-        if (t == s) { e3 = e2; e3 = e3 * per1 + e2 * per; }
+        // gain-exact form of e <- per1 e + per x (see OpEma::step)
+        e1 = fmaf(per, v - e1, e1);
+        if (t == start2) { e2 = e1; e2 = fmaf(per, e1 - e2, e2); }
+        else if (t > start2) e2 = fmaf(per, e1 - e2, e2);
+        if (t == s) { e3 = e2; e3 = fmaf(per, e2 - e3, e3); }
     }
     __device__ void seed() {}
     template <class In> __device__ int step(const In& in, int t) {
         float v = in.X(t);
         if (p1 == 0) { e1 = v; return 1; }
-        e1 = e1 * per1 + v * per;
-        e2 = e2 * per1 + e1 * per;
-        e3 = e3 * per1 + e2 * per;
+        e1 = fmaf(per, v - e1, e1);
+        e2 = fmaf(per, e1 - e2, e2);
+        e3 = fmaf(per, e2 - e3, e3);
         return 1;
     }
     template <class In> __device__ float value(const In& in, int t) const {
@@ -261,9 +264,9 @@ struct OpTema {
         const float v = in.X(t);
         ++applied;
         if (p1 == 0) { e1 = v; return v; }
-        e1 = e1 * per1 + v * per;
-        e2 = e2 * per1 + e1 * per;
-        e3 = e3 * per1 + e2 * per;
+        e1 = fmaf(per, v - e1, e1);
+        e2 = fmaf(per, e1 - e2, e2);
+        e3 = fmaf(per, e2 - e3, e3);
         return 3.f * e1 - 3.f * e2 + e3;
     }
     __device__ float get(int i) const { return i == 0 ? e1 : (i == 1 ? e2 : e3); }
@@ -277,12 +280,12 @@ struct OpTema {
         steps += t > s;
         if (p1 == 0) { e1 = v; return v; }
         const float a1 = t == f ? v : e1;
-        e1 = a1 * per1 + v * per;
+        e1 = fmaf(per, v - a1, a1);
         const float a2 = t == start2 ? e1 : e2;
-        const float n2 = a2 * per1 + e1 * per;
+        const float n2 = fmaf(per, e1 - a2, a2);
         e2 = t >= start2 ? n2 : e2;
         const float a3 = t == s ? e2 : e3;
-        const float n3 = a3 * per1 + e2 * per;
+        const float n3 = fmaf(per, e2 - a3, a3);
         e3 = t >= s ? n3 : e3;
         return t < warm ? qnan() : 3.f * e1 - 3.f * e2 + e3;
     }
@@ -523,12 +526,8 @@ __device__ __forceinline__ void run_tile(OpRsi<kB>& op, const InTile& ti, float*
     }
 }
 
-// TEMA emit tile with finite inputs, in the scaled domain zk = ek / a^k
-// (a = 2 / (p + 1)): a step is three FMAs and the output
-// 3 e1 - 3 e2 + e3 = (3a) z1 - (3a^2) z2 + (a^3) z3; p == 1 copies x.  The
-// scaled state stays in the op across consecutive tiles (op.zs) and is turned
-// back into e1..e3 only when another path takes over (leave_scaled), so no
-// rounding of the scale round trip accumulates.
+// TEMA emit tile with finite inputs: the three cascaded gain-exact EMA steps
+// with shuffle-broadcast inputs and no phase checks; p == 1 copies x.
 template <bool FIN, int PASS>
 __device__ __forceinline__ void run_tile(OpTema& op, const InTile& ti, float* row, int sw, int& steps) {
     if constexpr (!(FIN && PASS == PASS_EMIT)) {
@@ -538,28 +537,20 @@ __device__ __forceinline__ void run_tile(OpTema& op, const InTile& ti, float* ro
             if (PASS == PASS_EMIT) stage_put(row, sw, j, y);
         }
     } else {
-        const float a = op.per, a2 = a * a, a3 = a2 * a, b = op.per1;
-        const float c1 = 3.f * a, c2 = -3.f * a2;
+        const float a = op.per;
         const bool copy = op.p1 == 0;
-        if (!op.zs) {
-            op.z1 = op.e1 / a;
-            op.z2 = op.e2 / a2;
-            op.z3 = op.e3 / a3;
-            op.zs = true;
-        }
-        float z1 = op.z1, z2 = op.z2, z3 = op.z3;
+        float e1 = op.e1, e2 = op.e2, e3 = op.e3;
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
             const float v = __shfl_sync(0xffffffffu, ti.xv, j);
-            z1 = fmaf(b, z1, v);
-            z2 = fmaf(b, z2, z1);
-            z3 = fmaf(b, z3, z2);
-            const float y = fmaf(a3, z3, fmaf(c2, z2, c1 * z1));
-            stage_put(row, sw, j, copy ? v : y);
+            e1 = fmaf(a, v - e1, e1);
+            e2 = fmaf(a, e1 - e2, e2);
+            e3 = fmaf(a, e2 - e3, e3);
+            stage_put(row, sw, j, copy ? v : fmaf(3.f, e1 - e2, e3));
         }
-        op.z1 = z1;
-        op.z2 = z2;
-        op.z3 = z3;
+        op.e1 = e1;  // (a p == 1 lane's state is never read: each step copies x)
+        op.e2 = e2;
+        op.e3 = e3;
         steps += 32;
     }
 }
@@ -568,32 +559,20 @@ __device__ __forceinline__ void run_tile(OpTema& op, const InTile& ti, float* ro
 template <class Op, class = void> struct HasUni : std::false_type {};
 template <class Op> struct HasUni<Op, std::void_t<decltype(Op::kUni)>> : std::true_type {};
 
-// Ops without a scaled tile state have nothing to convert.
-template <class Op>
-__device__ __forceinline__ void leave_scaled(Op&) {}
-__device__ __forceinline__ void leave_scaled(OpTema& op) {
-    if (!op.zs) return;
-    const float a = op.per, a2 = a * a, a3 = a2 * a;
-    op.e1 = op.p1 == 0 ? op.z1 : op.z1 * a;
-    op.e2 = op.z2 * a2;
-    op.e3 = op.z3 * a3;
-    op.zs = false;
-}
-
 // ------------------------------------------------------- fast aggregates ---
 // AGG blocks of the chunks in which every combo of a batch sweep is already
 // running (EMA, DEMA, TEMA, RSI; chunk >= fast_from).  They share the launch
 // with the seed chunk's general-path blocks, so the long per-step seeding run
 // of chunk 0 overlaps with this work.  The block stages the chunk's inputs in
 // shared memory, kAggTile steps at a time, and reads them back four steps per
-// 16-byte broadcast load; each thread advances its combo from a zero state in
-// a scaled state domain where a step costs one FMA per component:
-//   EMA   z = y / a                    z <- b z + x
-//   DEMA  z1 = e1 / a, z2 = e2 / a^2   z1 <- b z1 + x,  z2 <- b z2 + z1
-//   TEMA  zk = ek / a^k                z1 <- b z1 + x,  z2 <- b z2 + z1,  z3 <- b z3 + z2
-//   RSI   zg = ag p, zl = al p         zg <- b zg + gain,  zl <- b zl + loss
-// (a = 2 / (p + 1), b = 1 - a for the EMAs; b = 1 - 1/p for RSI), and the
-// chunk-end state is scaled back once.  A chunk holding a non-finite input
+// 16-byte broadcast load; each thread advances its combo from a zero state:
+//   EMA / DEMA / TEMA  the emit pass's gain-exact steps e <- e + a (in - e)
+//                      (a = 2 / (p + 1)), two FP ops per component;
+//   RSI                zg = ag p, zl = al p: zg <- b zg + gain, zl <- b zl + loss
+//                      (b = 1 - 1/p), one FMA each, scaled back at the chunk
+//                      end (the output ratio is insensitive to the rounding
+//                      of b, which scales gains and losses alike).
+// A chunk holding a non-finite input
 // (RSI: a non-finite difference) returns false and the block runs the general
 // pass, which applies the skip / NaN rules.
 enum FastKind { FK_NONE = -1, FK_EMA = 0, FK_DEMA = 1, FK_TEMA = 2, FK_RSI = 3 };
@@ -613,17 +592,20 @@ __device__ bool agg_fast_block(const RecurArgs& a, int chunk, int c0, int c1, fl
     float* s1 = smem + kAggTile;
     const int li = blockIdx.x * blockDim.x + threadIdx.x;
     const double p = li < a.n_lanes ? (double)a.periods[li] : 1.0;
-    const float b = K == FK_RSI ? (float)(1.0 - 1.0 / p) : (float)(1.0 - 2.0 / (p + 1.0));
+    const float b = (float)(1.0 - 1.0 / p);       // RSI
+    const float al = (float)(2.0 / (p + 1.0));   // the EMAs
     float z[NZ];
 #pragma unroll
     for (int q = 0; q < NZ; ++q) z[q] = 0.f;
     auto step = [&](float v, float w) {
-        z[0] = fmaf(b, z[0], v);
         if constexpr (K == FK_RSI) {
+            z[0] = fmaf(b, z[0], v);
             z[1] = fmaf(b, z[1], w);
         } else {
-            if constexpr (NZ > 1) z[1] = fmaf(b, z[1], z[0]);
-            if constexpr (NZ > 2) z[2] = fmaf(b, z[2], z[1]);
+            // the gain-exact EMA step of the emit pass (OpEma::step)
+            z[0] = fmaf(al, v - z[0], z[0]);
+            if constexpr (NZ > 1) z[1] = fmaf(al, z[0] - z[1], z[1]);
+            if constexpr (NZ > 2) z[2] = fmaf(al, z[1] - z[2], z[2]);
         }
     };
     for (int t0 = c0; t0 < c1; t0 += kAggTile) {
@@ -663,10 +645,9 @@ __device__ bool agg_fast_block(const RecurArgs& a, int chunk, int c0, int c1, fl
             g.x = z[0] * ip;
             g.y = z[1] * ip;
         } else {
-            const double al = 2.0 / (p + 1.0);
-            g.x = (float)((double)z[0] * al);
-            if constexpr (NZ > 1) g.y = (float)((double)z[1] * al * al);
-            if constexpr (NZ > 2) g.z = (float)((double)z[2] * al * al * al);
+            g.x = z[0];
+            if constexpr (NZ > 1) g.y = z[1];
+            if constexpr (NZ > 2) g.z = z[2];
         }
         reinterpret_cast<float4*>(a.agg)[(size_t)chunk * a.n_lanes + li] = g;
     }
@@ -876,11 +857,9 @@ k_recur(RecurArgs a) {
                 if (fin) {
                     run_tile<true, PASS>(op, ti, srow, sw, steps);
                 } else {
-                    leave_scaled(op);
                     run_tile<false, PASS>(op, ti, srow, sw, steps);
                 }
             } else if (PASS == PASS_EMIT && !TM) {
-                leave_scaled(op);
 #pragma unroll 8
                 for (int t = tb; t < te; ++t) srow[(t - tb) ^ sw] = op.fast(in, t, steps);
             } else if (PASS == PASS_EMIT) {

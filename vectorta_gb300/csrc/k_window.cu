@@ -61,7 +61,7 @@ struct WinOut {
 // output).
 __device__ __forceinline__ WinOut window_eval(int kind, DS s1, DS s2, float pf, float inv_p, float inv_p2,
                                               float xt, float k1, float k2) {
-    WinOut r;
+    WinOut r = {0.f, 0.f, 0.f};
     const float mean = ds_f(s1) * inv_p;
     if (kind == WK_SMA) {
         r.o0 = mean;
@@ -127,6 +127,154 @@ __global__ void k_first_bad(const float* __restrict__ x, int n, int first, int* 
     }
 }
 
+// ---- clean-tile fast path ---------------------------------------------
+// In a tile whose input span holds no NaN or infinite value (the usual case)
+// each local prefix entry P = (hi, lo) is re-split as P = A + a with A a
+// multiple of one quantum Q per span: Q = 2^(e-21) for a bound 2^(e+1) on
+// |P| over the span, so every |A| <= 2^22 Q and every difference A(t) -
+// A(t-p) is a multiple of Q of at most 2^23 Q: exact in f32.  A window sum is
+// then the exact f32 difference of the A parts plus the (small) difference of
+// the a parts, two subtractions instead of a double-single subtraction.
+// A = (hi + C) - C with C = 1.5 * 2^(e+2) rounds hi to the nearest multiple
+// of Q (|hi| <= 2^(e+1) keeps hi + C inside [2^(e+2), 2^(e+3))); hi - A is
+// exact and a = (hi - A) + lo rounds at Q * 2^-25, i.e. 2^-47 of the bound.
+struct Quant {
+    float c;
+};
+__device__ __forceinline__ Quant quant_of(float bound) {
+    int e = (int)((__float_as_uint(bound) >> 23) & 0xffu) - 127;  // bound < 2^(e+1)
+    e = max(e, -100);
+    return {__uint_as_float(((unsigned)(e + 2 + 127) << 23) | 0x400000u)};
+}
+__device__ __forceinline__ float2 quant_split(float2 v, Quant q) {
+    const float A = __fsub_rn(__fadd_rn(v.x, q.c), q.c);
+    return make_float2(A, __fadd_rn(__fsub_rn(v.x, A), v.y));
+}
+
+// p^2 * var = p * S2 - S1^2 from the split window sums S1 = d1h + d1l and
+// S2 = d2h + d2l (d1h, d2h exact): the error-free products p * d2h and d1h^2
+// (their difference is exact where it cancels) plus p * d2l - 2 d1h d1l -
+// d1l^2.  The last term matters: d1l is up to one quantum of the span's
+// bound, which for a short window is not negligible against S1.
+__device__ __forceinline__ float window_d(float d1h, float d1l, float d2h, float d2l, float pf) {
+    const float g = __fmul_rn(pf, d2h), eg = fmaf(pf, d2h, -g);
+    const float h = __fmul_rn(d1h, d1h), eh = fmaf(d1h, d1h, -h);
+    float t = fmaf(pf, d2l, __fsub_rn(eg, eh));
+    t = fmaf(-__fadd_rn(d1h, d1h), d1l, t);
+    t = fmaf(-d1l, d1l, t);
+    return __fadd_rn(__fsub_rn(g, h), t);
+}
+
+// Per-combo constants of the fast path, computed once per block into shared
+// memory: x = period (int bits), y = 1/p (correctly rounded), z = the output
+// scale (StdDev: nbdev / p; Z-score: p / nbdev, NaN for nbdev 0; BB: devup),
+// w = BB devdn.
+__device__ __forceinline__ float4 combo_consts(int K, int p, float k1, float k2) {
+    const float pf = (float)p;
+    const float inv_p = __frcp_rn(pf);
+    float z = k1;
+    if (K == WK_STDDEV) z = __fmul_rn(k1, inv_p);
+    if (K == WK_ZSCORE) z = (k1 == 0.f || isnan(k1)) ? qnan() : __fdiv_rn(pf, k1);
+    return make_float4(__int_as_float(p), inv_p, z, k2);
+}
+
+// 1/sqrt(v) for a normal positive v: the hardware approximation (max
+// relative error about 2^-22.9), one instruction.
+__device__ __forceinline__ float rsqrt_approx(float v) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+    return r;
+}
+
+// One combo's outputs at this thread's kPwPer times of a clean tile.
+// q1[k], q2[k]: split prefix at t; b1, b2: split prefix array shifted to t - p.
+template <int K, bool FULL>
+__device__ __forceinline__ void fast_outputs(const float2 (&q1)[4], const float2 (&q2)[4], const float (&xt)[4],
+                                             const float2* b1, const float2* b2, float4 cc, float ref, float* r0,
+                                             float* r1, float* r2, int t, int n, int warm) {
+    const float pf = (float)__float_as_int(cc.x);
+    const float inv_p = cc.y;
+    // stddev: sqrt(var) * k1 = sqrt(D) * (k1 / p); z-score: dev / (sqrt(var) k1)
+    // = dev * rsqrt(D) * (p / k1); BB: sqrt(max(var, 0)) = sqrt(max(D, 0)) / p
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int tk = t + k * kPwThreads;
+        if (!FULL && (tk >= n || tk < warm)) {
+            if (tk < n) {
+                r0[k * kPwThreads] = qnan();
+                if (K == WK_BB) { r1[k * kPwThreads] = qnan(); r2[k * kPwThreads] = qnan(); }
+            }
+            continue;
+        }
+        const float2 v1 = b1[k * kPwThreads];
+        const float d1h = __fsub_rn(q1[k].x, v1.x), d1l = __fsub_rn(q1[k].y, v1.y);
+        if (K == WK_SMA) {
+            r0[k * kPwThreads] = __fadd_rn(ref, __fmul_rn(__fadd_rn(d1h, d1l), inv_p));
+            continue;
+        }
+        const float2 v2 = b2[k * kPwThreads];
+        const float D = window_d(d1h, d1l, __fsub_rn(q2[k].x, v2.x), __fsub_rn(q2[k].y, v2.y), pf);
+        const float r = rsqrt_approx(fmaxf(D, 1.17549435e-38f));
+        if (K == WK_STDDEV) {
+            r0[k * kPwThreads] = D > 0.f ? __fmul_rn(__fmul_rn(D, r), cc.z) : 0.f;
+        } else if (K == WK_ZSCORE) {
+            const float dev = __fsub_rn(xt[k], __fmul_rn(__fadd_rn(d1h, d1l), inv_p));
+            r0[k * kPwThreads] = D > 0.f ? __fmul_rn(__fmul_rn(dev, r), cc.z) : qnan();
+        } else {
+            const float mean = __fadd_rn(ref, __fmul_rn(__fadd_rn(d1h, d1l), inv_p));
+            const float sd = __fmul_rn(__fmul_rn(fmaxf(D, 0.f), r), inv_p);
+            r1[k * kPwThreads] = mean;
+            r0[k * kPwThreads] = fmaf(cc.z, sd, mean);
+            r2[k * kPwThreads] = fmaf(-cc.w, sd, mean);
+        }
+    }
+}
+
+constexpr int kPwComboGroup = 256;  // combos whose constants share memory holds at a time
+static_assert(kPwComboGroup <= kPwThreads, "one thread per combo of a group");
+
+template <int K>
+__device__ void fast_tile(const PrefixWinArgs& a, const float2* s1, const float2* s2, int pmax, int t0,
+                          float r0) {
+    static_assert(kPwPer == 4, "fast_outputs is written for 4 outputs per thread");
+    __shared__ float4 cc[kPwComboGroup];
+    float2 q1[4], q2[4];
+    float xt[4];
+    const int tid = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int l = pmax + tid + k * kPwThreads;
+        const int t = t0 + tid + k * kPwThreads;
+        q1[k] = s1[l];
+        q2[k] = K == WK_SMA ? make_float2(0.f, 0.f) : s2[l];
+        xt[k] = (K == WK_ZSCORE && t < a.n) ? __fsub_rn(__ldg(a.x + t), r0) : 0.f;  // y(t)
+    }
+    const bool tail = t0 + kPwTile > a.n;
+    for (int g0 = 0; g0 < a.n_combos; g0 += kPwComboGroup) {
+        const int gn = min(kPwComboGroup, a.n_combos - g0);
+        __syncthreads();  // the previous group's constants are no longer read
+        if (tid < gn) {
+            const int c = g0 + tid;
+            cc[tid] = combo_consts(K, __ldg(a.periods + c), a.k1 ? __ldg(a.k1 + c) : 1.f,
+                                   a.k2 ? __ldg(a.k2 + c) : 1.f);
+        }
+        __syncthreads();
+        for (int j = 0; j < gn; ++j) {
+            const float4 k4 = cc[j];
+            const int p = __float_as_int(k4.x);
+            const int warm = a.first + p - 1;
+            const size_t o = (size_t)(g0 + j) * a.n + t0 + tid;
+            const int sh = pmax - p + tid;
+            float* o1 = a.out1 ? a.out1 + o : nullptr;
+            float* o2 = a.out2 ? a.out2 + o : nullptr;
+            if (!tail && t0 >= warm)  // the whole tile is past this combo's warm-up
+                fast_outputs<K, true>(q1, q2, xt, s1 + sh, s2 + sh, k4, r0, a.out0 + o, o1, o2, t0 + tid, a.n, warm);
+            else
+                fast_outputs<K, false>(q1, q2, xt, s1 + sh, s2 + sh, k4, r0, a.out0 + o, o1, o2, t0 + tid, a.n, warm);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kPwThreads)
 k_prefix_window_batch(PrefixWinArgs a, int pmax) {
     extern __shared__ float2 psm[];
@@ -142,10 +290,20 @@ k_prefix_window_batch(PrefixWinArgs a, int pmax) {
     // run totals are scanned across the block, then added back
     const int per = (span + kPwThreads - 1) / kPwThreads;
     const int i0 = threadIdx.x * per, i1 = min(i0 + per, span);
+    // no NaN / infinite input at or after `first` before the tile's end: no
+    // output of the tile is poisoned and the span's prefixes are finite
+    const bool clean = a.n - a.bad[0] >= t0 + kPwTile && a.n - a.bad[1] >= t0 + kPwTile;
+    // A clean tile's prefixes are of y = x - r0, centred on the tile's first
+    // valid value: window variances are shift-invariant, and the centred sums
+    // are smaller, so both the cancellation in p S2 - S1^2 and the quantum of
+    // the split below shrink with the span's spread instead of its level.
+    const float r0 = clean && a.first < a.n ? __ldg(a.x + max(t0, a.first)) : 0.f;
     DS a1 = {0.f, 0.f}, a2 = {0.f, 0.f};
+    float abs1 = 0.f;  // sum of |y| over this thread's run: bounds |prefix of y|
     for (int i = i0; i < i1; ++i) {
         const int g = base + i;
-        const float v = (g >= a.first && g < a.n) ? __ldg(a.x + g) : 0.f;
+        const float v = (g >= a.first && g < a.n) ? __fsub_rn(__ldg(a.x + g), r0) : 0.f;
+        abs1 += fabsf(v);
         a1 = ds_add_f(a1, v);
         s1[i] = make_float2(a1.hi, a1.lo);
         if (two) {
@@ -192,6 +350,37 @@ k_prefix_window_batch(PrefixWinArgs a, int pmax) {
             s2[i] = make_float2(r2.hi, r2.lo);
         }
     }
+    if (clean) {
+        // bounds of |prefix| over the span: sum |x| (the x^2 prefix is
+        // non-decreasing, so its last entry), rounded up by a factor 2^-20
+        __shared__ float red[kPwThreads / 32 + 1];
+        float b = abs1;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) b += __shfl_xor_sync(0xffffffffu, b, o);
+        if (lane == 0) red[warp] = b;
+        // the last prefix entry, read by its owner before anyone splits it
+        if (two && i0 <= span - 1 && span - 1 < i1) red[kPwThreads / 32] = s2[span - 1].x + s2[span - 1].y;
+        __syncthreads();
+        float bound1 = 0.f;
+        for (int w = 0; w < kPwThreads / 32; ++w) bound1 += red[w];
+        bound1 *= 1.f + 0x1p-20f;
+        const float bound2 = two ? red[kPwThreads / 32] * (1.f + 0x1p-20f) : 0.f;
+        if (bound1 < 0x1p120f && bound2 < 0x1p120f) {
+            const Quant q1 = quant_of(bound1), q2 = quant_of(bound2);
+            for (int i = i0; i < i1; ++i) {
+                s1[i] = quant_split(s1[i], q1);
+                if (two) s2[i] = quant_split(s2[i], q2);
+            }
+            __syncthreads();
+            switch (a.kind) {
+                case WK_SMA: fast_tile<WK_SMA>(a, s1, s2, pmax, t0, r0); break;
+                case WK_STDDEV: fast_tile<WK_STDDEV>(a, s1, s2, pmax, t0, r0); break;
+                case WK_ZSCORE: fast_tile<WK_ZSCORE>(a, s1, s2, pmax, t0, r0); break;
+                default: fast_tile<WK_BB>(a, s1, s2, pmax, t0, r0); break;
+            }
+            return;
+        }
+    }
     __syncthreads();
     const int first_nan = a.n - a.bad[0], first_inf = a.n - a.bad[1];
     float2 p1t[kPwPer], p2t[kPwPer];
@@ -202,7 +391,7 @@ k_prefix_window_batch(PrefixWinArgs a, int pmax) {
         const int t = t0 + threadIdx.x + k * kPwThreads;
         p1t[k] = s1[l];
         p2t[k] = two ? s2[l] : z;
-        xt[k] = (a.kind == WK_ZSCORE && t < a.n) ? a.x[t] : 0.f;
+        xt[k] = (a.kind == WK_ZSCORE && t < a.n) ? __fsub_rn(a.x[t], r0) : 0.f;
     }
     for (int c = 0; c < a.n_combos; ++c) {
         const int p = a.periods[c];
@@ -226,7 +415,14 @@ k_prefix_window_batch(PrefixWinArgs a, int pmax) {
             const int lb = pmax + threadIdx.x + k * kPwThreads - p;  // local index of t - p
             const DS w1 = ds_sub2(p1t[k], s1[lb]);
             const DS w2 = two ? ds_sub2_ge(p2t[k], s2[lb]) : DS{0.f, 0.f};
-            const WinOut r = window_eval(a.kind, w1, w2, pf, inv_p, inv_p2, xt[k], k1, k2);
+            WinOut r = window_eval(a.kind, w1, w2, pf, inv_p, inv_p2, xt[k], k1, k2);
+            // r0 is 0 unless a clean tile's bound check failed after its
+            // prefixes were built centred on r0 (values near the f32 range)
+            if (a.kind == WK_SMA || a.kind == WK_BB) {
+                r.o0 = __fadd_rn(r.o0, r0);
+                r.o1 = __fadd_rn(r.o1, r0);
+                r.o2 = __fadd_rn(r.o2, r0);
+            }
             row0[t] = r.o0;
             if (a.kind == WK_BB) { a.out1[o] = r.o1; a.out2[o] = r.o2; }
         }
@@ -301,6 +497,58 @@ __global__ void k_first_nan_after_tm(const float* __restrict__ x, int cols, int 
 // non-finite rule for Donchian p > 32, donchian.rs:327-346 / 413-480).
 constexpr int kMmThreads = 512;
 
+// Outputs of a clean tile (every window past its warm-up is valid): combo-
+// outer, so a combo's table offsets are read once for the thread's PER times
+// t = t0 + tid + k * kMmThreads; the closes are read once for all combos.
+template <int KIND, int PER>
+__device__ __forceinline__ void minmax_clean(const MinMaxArgs& a, const float* mx, const float* mn,
+                                             const int4* ctab, int t0, int tile) {
+    const int tid = threadIdx.x;
+    const bool full = t0 + tile <= a.n;
+    float cl[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int t = t0 + tid + k * kMmThreads;
+        cl[k] = (KIND == MM_WILLR && t < a.n) ? __ldg(a.c + t) : 0.f;
+    }
+    const int ie0 = tid + a.pmax - 1;  // local index of t0 + tid
+    for (int c = 0; c < a.n_combos; ++c) {
+        const int4 ct = ctab[c];
+        const size_t o = (size_t)c * a.n + t0 + tid;
+        float* r0 = a.out0 + o;
+        const float* mz = mx + ie0 + ct.z;
+        const float* mw = mx + ie0 + ct.w;
+        const float* nz = mn + ie0 + ct.z;
+        const float* nw = mn + ie0 + ct.w;
+        const bool all_valid = full && t0 >= ct.y;
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int t = t0 + tid + k * kMmThreads;
+            if (!all_valid && t >= a.n) break;
+            float v0 = qnan(), v1 = qnan(), v2 = qnan();
+            if (all_valid || t >= ct.y) {
+                const float hmax = fmaxf(mz[k * kMmThreads], mw[k * kMmThreads]);
+                const float lmin = fminf(nz[k * kMmThreads], nw[k * kMmThreads]);
+                if (KIND == MM_DONCHIAN) {
+                    v0 = hmax;
+                    v2 = lmin;
+                    v1 = fmaf(hmax - lmin, 0.5f, lmin);
+                } else {
+                    const float den = hmax - lmin;
+                    // hmax, lmin and the close are finite prices: the fast
+                    // divide is within 2 ulp
+                    v0 = den == 0.f ? 0.f : fmaf(-100.f, __fdividef(hmax - cl[k], den), 0.f);
+                }
+            }
+            r0[k * kMmThreads] = v0;
+            if (KIND == MM_DONCHIAN) {
+                a.out1[o + k * kMmThreads] = v1;
+                a.out2[o + k * kMmThreads] = v2;
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kMmThreads)
 k_minmax_batch(MinMaxArgs a, int tile, int levels) {
     extern __shared__ float sm[];
@@ -321,7 +569,10 @@ k_minmax_batch(MinMaxArgs a, int tile, int levels) {
         const int k = 31 - __clz(p);
         ctab[c] = make_int4(p, a.first + p - 1, k * nloc - p + 1, k * nloc - (1 << k) + 1);
     }
-    // level 0 + invalid flags
+    // level 0 + invalid flags; a span whose valid part holds only finite
+    // highs and lows (and closes at the tile's times) is clean: every window
+    // of the tile is then valid past its warm-up, and no counts are needed
+    int any_bad = 0;
     for (int i = threadIdx.x; i < nloc; i += blockDim.x) {
         const int g = lo_i + i;
         float hv = -INFINITY, lv = INFINITY;
@@ -331,6 +582,8 @@ k_minmax_batch(MinMaxArgs a, int tile, int levels) {
             fnan = (isnan(h) || isnan(l)) ? 1 : 0;
             ffin = (isfinite(h) && isfinite(l)) ? 0 : 1;
             if (!fnan) { hv = h; lv = l; }
+            if (g >= a.first) any_bad |= ffin;
+            if (a.kind == MM_WILLR && g >= a.first && i >= a.pmax - 1 && isnan(a.c[g])) any_bad = 1;
         }
         mx[i] = hv;
         mn[i] = lv;
@@ -338,9 +591,9 @@ k_minmax_batch(MinMaxArgs a, int tile, int levels) {
         bad_fin[i + 1] = ffin;
     }
     if (threadIdx.x == 0) { bad_nan[0] = 0; bad_fin[0] = 0; }
-    __syncthreads();
+    const bool clean = !__syncthreads_or(any_bad);
     // prefix counts (single warp, sequential per lane-strided segments)
-    if (threadIdx.x < 32) {
+    if (!clean && threadIdx.x < 32) {
         const int lane = threadIdx.x;
         const int seg = (nloc + 31) / 32;
         const int b = 1 + lane * seg, e = min(nloc + 1, b + seg);
@@ -370,8 +623,19 @@ k_minmax_batch(MinMaxArgs a, int tile, int levels) {
         }
     }
     __syncthreads();
-    // a span without invalid inputs (the usual case) needs no window counts
-    const bool clean = bad_nan[nloc] == 0 && bad_fin[nloc] == 0;
+    if (clean && tile >= kMmThreads) {
+        const int per = tile / kMmThreads;  // 1, 2 or 4: the launcher's tiles are 256..2048
+        if (a.kind == MM_DONCHIAN) {
+            if (per == 1) minmax_clean<MM_DONCHIAN, 1>(a, mx, mn, ctab, t0, tile);
+            else if (per == 2) minmax_clean<MM_DONCHIAN, 2>(a, mx, mn, ctab, t0, tile);
+            else minmax_clean<MM_DONCHIAN, 4>(a, mx, mn, ctab, t0, tile);
+        } else {
+            if (per == 1) minmax_clean<MM_WILLR, 1>(a, mx, mn, ctab, t0, tile);
+            else if (per == 2) minmax_clean<MM_WILLR, 2>(a, mx, mn, ctab, t0, tile);
+            else minmax_clean<MM_WILLR, 4>(a, mx, mn, ctab, t0, tile);
+        }
+        return;
+    }
     for (int tt = threadIdx.x; tt < tile; tt += blockDim.x) {
         const int t = t0 + tt;
         if (t >= a.n) break;

@@ -1367,12 +1367,30 @@ vta_status batch_enqueue(vta_ctx* ctx, int ind, const float* const* d_in, size_t
 // ---- hooks for the no-allocation SMA entry point (vta_noalloc.cu) --------
 vta_status enter_call(vta_ctx* ctx) { return check_ctx(ctx); }
 
-vta_status validate_sma_periods(const vta_period_params* p, size_t n, size_t len, size_t first) {
+// Number of periods of an SMA sweep, counted the way axis_usize expands it
+// (SMA's descending ranges run start, start - step, ... while >= end), so the
+// caller can reject an oversized sweep before expanding it.
+size_t sma_period_count(vta_range_usize r) {
+    if (r.step == 0 || r.start == r.end) return 1;
+    if (r.start < r.end) return (r.end - r.start) / r.step + 1;
+    return (r.start - r.end) / r.step + 1;  // kInfo[I_SMA].axis is AX_DESC
+}
+
+// Period k of an SMA sweep (k < sma_period_count(r)): the same values as
+// axis_usize(r, SMA's mode), without building a vector.
+size_t sma_period_at(vta_range_usize r, size_t k) {
+    if (r.step == 0 || r.start == r.end) return r.start;
+    return r.start < r.end ? r.start + k * r.step : r.start - k * r.step;
+}
+
+// The checks of validate_combos for the n periods of an SMA sweep.
+vta_status validate_sma_range(vta_range_usize r, size_t n, size_t len, size_t first) {
     if (n == 0) return fail(VTA_ERR_INVALID_INPUT, "sma: no parameter combinations");
     size_t need = 0;
     for (size_t i = 0; i < n; ++i) {
-        VTA_TRY(validate_combo(I_SMA, Combo{p[i].period, 0.0, 0.0}, len));
-        need = std::max(need, needed_len(I_SMA, p[i].period));
+        const size_t p = sma_period_at(r, i);
+        VTA_TRY(validate_combo(I_SMA, Combo{p, 0.0, 0.0}, len));
+        need = std::max(need, needed_len(I_SMA, p));
     }
     if (first >= len) return fail(VTA_ERR_INVALID_INPUT, "sma: all values are NaN");
     if (len - first < need) {

@@ -384,6 +384,8 @@ vta_status batch_enqueue(vta_ctx* ctx, int ind, const float* const* d_in, size_t
 // Binds a call to `ctx` (device current, timing events), as every entry does.
 vta_status enter_call(vta_ctx* ctx);
 // The allocating SMA entry points' parameter and length checks, same messages.
-vta_status validate_sma_periods(const vta_period_params* p, size_t n, size_t len, size_t first);
+size_t sma_period_count(vta_range_usize r);
+size_t sma_period_at(vta_range_usize r, size_t k);
+vta_status validate_sma_range(vta_range_usize r, size_t n, size_t len, size_t first);
 
 }  // namespace vta

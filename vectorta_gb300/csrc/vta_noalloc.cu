@@ -74,8 +74,10 @@ extern "C" vta_status vta_sma_batch_device_noalloc(vta_ctx* ctx, const float* d_
                       len, kMaxLen);
         return fail(VTA_ERR_INVALID_INPUT, buf);
     }
-    size_t nc = 0;
-    VTA_TRY(vta_sma_expand_grid(sweep, nullptr, 0, &nc));
+    // The period count comes from the range arithmetic, so an oversized sweep
+    // is rejected before anything is built; the periods are then written
+    // straight into a fixed array (no host or device allocation).
+    const size_t nc = sma_period_count(sweep->period);
     if (nc > kMaxCombos) {
         std::snprintf(buf, sizeof buf,
                       "sma_batch_device_noalloc: %zu periods exceed the fixed scratch limit of %zu "
@@ -83,15 +85,13 @@ extern "C" vta_status vta_sma_batch_device_noalloc(vta_ctx* ctx, const float* d_
                       nc, kMaxCombos);
         return fail(VTA_ERR_INVALID_INPUT, buf);
     }
-    vta_period_params params[kMaxCombos];
-    VTA_TRY(vta_sma_expand_grid(sweep, params, kMaxCombos, &nc));
-    VTA_TRY(validate_sma_periods(params, nc, len, first_valid));
+    VTA_TRY(validate_sma_range(sweep->period, nc, len, first_valid));
     const int n = (int)len;
 
-    int periods[kMaxCombos];
+    int periods[kMaxCombos];  // 16 KiB of the caller's stack
     int pmax = 0;
     for (size_t i = 0; i < nc; ++i) {
-        periods[i] = (int)params[i].period;
+        periods[i] = (int)sma_period_at(sweep->period, i);
         pmax = periods[i] > pmax ? periods[i] : pmax;
     }
 
