@@ -104,6 +104,20 @@ struct InStep {
     __device__ float L(int) const { return l0; }
 };
 
+// b^n for a whole step count n >= 0 by repeated squaring: about 2 log2(n)
+// f64 multiplies (a few ulp), instead of pow()'s log / exp evaluation, which
+// on GB300's FP64 rate made the carry scan latency-bound.
+__device__ __forceinline__ double ipow(double b, double n) {
+    unsigned long long e = (unsigned long long)n;
+    double r = 1.0;
+    while (e) {
+        if (e & 1ull) r *= b;
+        b *= b;
+        e >>= 1;
+    }
+    return r;
+}
+
 // ------------------------------------------------------------ ops ----------
 // Common op interface:
 //   init(p, f)            lane constants; sets f (first valid), s (seed index),
@@ -168,7 +182,7 @@ struct OpEma {
     }
     static __device__ void propagate(double* S, double n, int p) {
         double b = 1.0 - 2.0 / ((double)p + 1.0);
-        S[0] *= pow(b, n);
+        S[0] *= ipow(b, n);
     }
 };
 
@@ -211,7 +225,7 @@ struct OpDema {
     }
     static __device__ void propagate(double* S, double n, int p) {
         double al = 2.0 / ((double)p + 1.0);
-        double an = pow(1.0 - al, n);
+        double an = ipow(1.0 - al, n);
         double s1 = S[0];
         S[0] = an * s1;
         S[1] = an * (S[1] + n * al * s1);
@@ -292,7 +306,7 @@ struct OpTema {
     static __device__ void propagate(double* S, double n, int p) {
         if (p == 1) { S[0] = 0.0; return; }  // p==1 carries nothing (out = x)
         double al = 2.0 / ((double)p + 1.0);
-        double an = pow(1.0 - al, n);
+        double an = ipow(1.0 - al, n);
         double s1 = S[0], s2 = S[1], s3 = S[2];
         double c2 = n * (n - 1.0) * 0.5;
         S[0] = an * s1;
@@ -368,7 +382,7 @@ struct OpRsi {
     __device__ float get(int i) const { return i == 0 ? ag : al; }
     __device__ void set(int i, float v) { if (i == 0) ag = v; else al = v; }
     static __device__ void propagate(double* S, double n, int p) {
-        double bn = pow(1.0 - 1.0 / (double)p, n);
+        double bn = ipow(1.0 - 1.0 / (double)p, n);
         S[0] *= bn;
         S[1] *= bn;
     }
@@ -407,7 +421,7 @@ struct OpWilders {
         return y;
     }
     static __device__ void propagate(double* S, double n, int p) {
-        S[0] = (p == 1) ? 0.0 : S[0] * pow(1.0 - 1.0 / (double)p, n);
+        S[0] = (p == 1) ? 0.0 : S[0] * ipow(1.0 - 1.0 / (double)p, n);
     }
 };
 
@@ -458,7 +472,7 @@ struct OpAtr {
         return y;
     }
     static __device__ void propagate(double* S, double n, int p) {
-        S[0] *= pow(1.0 - 1.0 / (double)p, n);
+        S[0] *= ipow(1.0 - 1.0 / (double)p, n);
     }
 };
 
@@ -585,6 +599,79 @@ template <> struct FastKindOf<OpTema> { static constexpr int k = FK_TEMA; };
 template <> struct FastKindOf<OpRsi<true>> { static constexpr int k = FK_RSI; };
 
 // smem: 2 * kAggTile floats, 16-byte aligned.  Called by the whole block.
+// The EMA cascades advance kAggBlk steps at a time by their exact block
+// transition: after B steps from (e1, e2, e3) with inputs x_0..x_{B-1}
+// (a = 2/(p+1), b = 1 - a, j = 0 the oldest),
+//   e1' = b^B e1 + sum_j a b^(B-1-j) x_j
+//   e2' = b^B e2 + a B b^B e1 + sum_j a^2 (B-j) b^(B-1-j) x_j
+//   e3' = b^B e3 + a B b^B e2 + a^2 b^B B(B+1)/2 e1
+//         + sum_j a^3 (B-j)(B-j+1)/2 b^(B-1-j) x_j,
+// evaluated in the gain-exact form e' = e + sum_i c_i (e_i - e) + (dot - W e)
+// (W = the sum of the rounded x-weights; the coefficient of e is b^B in exact
+// arithmetic), so a constant input stays fixed whatever the weights'
+// rounding.  A block costs one FMA per input per component plus a few for
+// the update: about half the work of the per-step form, whose two dependent
+// FP ops per step also made each lane's chain latency-bound.
+constexpr int kAggBlk = 16;
+
+template <int NZ>
+struct CascadeBlock {
+    float w[NZ][kAggBlk];  // x-weights, j = 0 the oldest input of the block
+    float W[NZ];           // their sums
+    float c1, c2;          // a B b^B (e1 -> e2 and e2 -> e3), a^2 b^B B(B+1)/2 (e1 -> e3)
+    __device__ void init(float al) {
+        // b = 1 - a and its powers in f32: the weights carry relative errors
+        // near 1e-6, a perturbation of the filter's time constant (the gain
+        // stays exact by the update's form)
+        const float be = 1.f - al;
+        float pw = 1.f;  // b^(B-1-j), j from B-1 down to 0
+#pragma unroll
+        for (int q = 0; q < NZ; ++q) W[q] = 0.f;
+#pragma unroll
+        for (int j = kAggBlk - 1; j >= 0; --j) {
+            const float r = (float)(kAggBlk - j);  // B - j
+            w[0][j] = al * pw;
+            if constexpr (NZ > 1) w[1][j] = al * al * r * pw;
+            if constexpr (NZ > 2) w[2][j] = al * al * al * (r * (r + 1.f) * 0.5f) * pw;
+            pw *= be;
+        }
+        // the sums in the order the dots accumulate (oldest first)
+#pragma unroll
+        for (int j = 0; j < kAggBlk; ++j)
+#pragma unroll
+            for (int q = 0; q < NZ; ++q) W[q] += w[q][j];
+        c1 = al * (float)kAggBlk * pw;
+        c2 = al * al * pw * (float)(kAggBlk * (kAggBlk + 1) / 2);
+    }
+    // one block of inputs x[0..B) (shared-memory broadcast reads)
+    __device__ __forceinline__ void step(float (&z)[NZ], const float* x) const {
+        float d[NZ][2];
+#pragma unroll
+        for (int q = 0; q < NZ; ++q) d[q][0] = d[q][1] = 0.f;
+#pragma unroll
+        for (int j = 0; j < kAggBlk; j += 4) {
+            const float4 v = *reinterpret_cast<const float4*>(x + j);
+#pragma unroll
+            for (int q = 0; q < NZ; ++q) {
+                d[q][0] = fmaf(w[q][j], v.x, d[q][0]);
+                d[q][1] = fmaf(w[q][j + 1], v.y, d[q][1]);
+                d[q][0] = fmaf(w[q][j + 2], v.z, d[q][0]);
+                d[q][1] = fmaf(w[q][j + 3], v.w, d[q][1]);
+            }
+        }
+        const float e1 = z[0];
+        z[0] = e1 + fmaf(-W[0], e1, d[0][0] + d[0][1]);
+        if constexpr (NZ > 1) {
+            const float e2 = z[1];
+            z[1] = fmaf(c1, e1 - e2, e2) + fmaf(-W[1], e2, d[1][0] + d[1][1]);
+            if constexpr (NZ > 2) {
+                const float e3 = z[2];
+                z[2] = fmaf(c1, e2 - e3, fmaf(c2, e1 - e3, e3)) + fmaf(-W[2], e3, d[2][0] + d[2][1]);
+            }
+        }
+    }
+};
+
 template <int K>
 __device__ bool agg_fast_block(const RecurArgs& a, int chunk, int c0, int c1, float* smem) {
     constexpr int NZ = K == FK_EMA ? 1 : (K == FK_TEMA ? 3 : 2);
@@ -597,6 +684,8 @@ __device__ bool agg_fast_block(const RecurArgs& a, int chunk, int c0, int c1, fl
     float z[NZ];
 #pragma unroll
     for (int q = 0; q < NZ; ++q) z[q] = 0.f;
+    CascadeBlock<NZ> cb;
+    if constexpr (K != FK_RSI) cb.init(al);
     auto step = [&](float v, float w) {
         if constexpr (K == FK_RSI) {
             z[0] = fmaf(b, z[0], v);
@@ -624,6 +713,13 @@ __device__ bool agg_fast_block(const RecurArgs& a, int chunk, int c0, int c1, fl
             }
         }
         if (__syncthreads_or(bad)) return false;
+        if constexpr (K != FK_RSI) {
+            const int mb = m - m % kAggBlk;
+            for (int i = 0; i < mb; i += kAggBlk) cb.step(z, s0 + i);
+            for (int i = mb; i < m; ++i) step(s0[i], 0.f);
+            __syncthreads();
+            continue;
+        }
         const int m4 = m & ~3;
 #pragma unroll 2
         for (int i = 0; i < m4; i += 4) {
@@ -651,6 +747,106 @@ __device__ bool agg_fast_block(const RecurArgs& a, int chunk, int c0, int c1, fl
         }
         reinterpret_cast<float4*>(a.agg)[(size_t)chunk * a.n_lanes + li] = g;
     }
+    return true;
+}
+
+// ------------------------------------------------------ seed chunk, AGG ---
+// The AGG pass needs only the state at the end of the seed chunk [0, c1).
+// When every input in [first, c1) is finite and every lane's seed index lies
+// inside the chunk, a lane gets there by plain loops instead of the per-step
+// phase logic: the warm-up sum in four independent compensated partial sums
+// (a short dependency chain), then the running steps from the seed on.  The
+// per-step phase logic made each lane's 1,000-2,000-step walk the critical
+// path of the whole AGG launch.
+template <int K>
+__device__ bool agg_seed_fast(const RecurArgs& a, const float* xs, int c1) {
+    const int f = a.first;
+    const int li = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool lane_ok = li < a.n_lanes;
+    const int p = lane_ok ? a.periods[li] : 1;
+    // seed index of the lane (the op's s)
+    const int s = K == FK_EMA ? f + p - 1 : K == FK_RSI ? f + p : f + 2 * (p - 1);
+    int bad = lane_ok && (p <= 0 || s >= c1);
+    for (int t = max(f, 0) + threadIdx.x; t < c1; t += blockDim.x) bad |= !isfinite(xs[t]);
+    if (__syncthreads_or(bad)) return false;
+    if (!lane_ok) return true;
+    float4 g = make_float4(0.f, 0.f, 0.f, kAbsolute);
+    if constexpr (K == FK_EMA) {
+        // the op's warm-up mean of x[f..s] (every value finite: count p)
+        Acc acc[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[q].zero();
+        int t = f;
+        for (; t + 3 <= s; t += 4)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[q].add(xs[t + q]);
+        for (; t <= s; ++t) acc[0].add(xs[t]);
+        acc[0].add(acc[1].hi); acc[0].add(acc[1].lo);
+        acc[2].add(acc[3].hi); acc[2].add(acc[3].lo);
+        acc[0].add(acc[2].hi); acc[0].add(acc[2].lo);
+        const float al = (float)(2.0 / ((double)p + 1.0));
+        float y = acc[0].f() / (float)p;
+        for (t = s + 1; t < c1; ++t) y = fmaf(al, xs[t] - y, y);
+        g.x = y;
+    } else if constexpr (K == FK_RSI) {
+        // sums of the gains and losses of the p deltas in (f, s], then the
+        // Wilder steps (the op's seed() and step() arithmetic)
+        Acc sg[2], sl[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) { sg[q].zero(); sl[q].zero(); }
+        int t = f + 1;
+        for (; t + 1 <= s; t += 2)
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const float v = xs[t + q], xp = xs[t + q - 1];
+                if (v > xp) sg[q].add_diff(v, xp);
+                else if (v < xp) sl[q].add_diff(xp, v);
+            }
+        for (; t <= s; ++t) {
+            const float v = xs[t], xp = xs[t - 1];
+            if (v > xp) sg[0].add_diff(v, xp);
+            else if (v < xp) sl[0].add_diff(xp, v);
+        }
+        const double inv_p = (double)(float)(1.0 / (double)p);
+        const float beta = (float)(1.0 - 1.0 / (double)p), ip = (float)(1.0 / (double)p);
+        float ag = (float)((sg[0].d() + sg[1].d()) * inv_p);
+        float al = (float)((sl[0].d() + sl[1].d()) * inv_p);
+        for (t = s + 1; t < c1; ++t) {
+            const float d = xs[t] - xs[t - 1];
+            ag = fmaf(ag, beta, ip * (d > 0.f ? d : 0.f));
+            al = fmaf(al, beta, ip * (d < 0.f ? -d : 0.f));
+        }
+        g.x = ag;
+        g.y = al;
+    } else {
+        // TEMA: e1 from x[f]; e2 joins at f + p - 1 as a copy of e1, e3 at s
+        // as a copy of e2 (the op's accum), then all three run (p == 1:
+        // the op copies x into e1)
+        const float per = (float)(2.0 / ((double)p + 1.0));
+        if (p == 1) {
+            g.x = xs[c1 - 1];
+        } else {
+            const int start2 = f + p - 1;
+            float e1 = xs[f], e2, e3;
+            int t = f + 1;
+            for (; t <= start2; ++t) e1 = fmaf(per, xs[t] - e1, e1);
+            e2 = e1;
+            for (; t <= s; ++t) {
+                e1 = fmaf(per, xs[t] - e1, e1);
+                e2 = fmaf(per, e1 - e2, e2);
+            }
+            e3 = e2;
+            for (; t < c1; ++t) {
+                e1 = fmaf(per, xs[t] - e1, e1);
+                e2 = fmaf(per, e1 - e2, e2);
+                e3 = fmaf(per, e2 - e3, e3);
+            }
+            g.x = e1;
+            g.y = e2;
+            g.z = e3;
+        }
+    }
+    reinterpret_cast<float4*>(a.agg)[li] = g;  // chunk 0
     return true;
 }
 
@@ -736,6 +932,10 @@ k_recur(RecurArgs a) {
             float* xs = &stage[0][0][0];
             for (int i = threadIdx.x; i < c1; i += blockDim.x) xs[i] = __ldg(a.x + i);
             __syncthreads();
+            constexpr int FK = FastKindOf<Op>::k;
+            if constexpr (FK == FK_EMA || FK == FK_RSI || FK == FK_TEMA) {
+                if (a.first < a.n && agg_seed_fast<FK>(a, xs, c1)) return;
+            }
             const int l0 = blockIdx.x * blockDim.x + threadIdx.x;
             if (l0 < a.n_lanes) {
                 const int p0 = a.periods[l0];

@@ -350,6 +350,70 @@ vta_status upload_async(vta_ctx* ctx, void* dst, const void* src, size_t bytes, 
     return VTA_OK;
 }
 
+// Constant cache of a context (see vta_ctx::cc_*): a device buffer filled
+// front to back by uploads; an upload whose bytes match an earlier one (hash,
+// then a full compare with the host copy) reuses it.  When the buffer is full
+// it starts over: every earlier call has synchronised, so no kernel still
+// reads it.  Server slots (calls that do not wait) bypass it.
+static constexpr size_t kConstCacheBytes = size_t(4) << 20;
+static constexpr size_t kConstCacheMaxItem = size_t(256) << 10;
+
+static uint64_t bytes_hash(const void* src, size_t n) {
+    const unsigned char* b = static_cast<const unsigned char*>(src);
+    uint64_t h = 0x9E3779B97F4A7C15ull ^ n;
+    size_t i = 0;
+    for (; i + 8 <= n; i += 8) {
+        uint64_t w;
+        std::memcpy(&w, b + i, 8);
+        h = (h ^ w) * 0xff51afd7ed558ccdull;
+        h ^= h >> 32;
+    }
+    for (; i < n; ++i) h = (h ^ b[i]) * 0x100000001b3ull;
+    return h;
+}
+
+vta_status const_upload_bytes(vta_ctx* ctx, const void* src, size_t bytes, void* fallback, const void** out) {
+    if (bytes == 0) {
+        *out = fallback;
+        return VTA_OK;
+    }
+    if (ctx->async_alloc || bytes > kConstCacheMaxItem) {
+        VTA_TRY(upload_async(ctx, fallback, src, bytes, ctx->stream));
+        *out = fallback;
+        return VTA_OK;
+    }
+    const uint64_t h = bytes_hash(src, bytes);
+    for (const auto& e : ctx->cc)
+        if (e.hash == h && e.bytes == bytes && std::memcmp(ctx->cc_host.data() + e.off, src, bytes) == 0) {
+            *out = static_cast<const char*>(ctx->cc_dev) + e.off;
+            return VTA_OK;
+        }
+    if (!ctx->cc_dev) {
+        if (vram_check(kConstCacheBytes) != VTA_OK || cudaMalloc(&ctx->cc_dev, kConstCacheBytes) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->cc_dev = nullptr;
+            VTA_TRY(upload_async(ctx, fallback, src, bytes, ctx->stream));
+            *out = fallback;
+            return VTA_OK;
+        }
+        ctx->cc_cap = kConstCacheBytes;
+        ctx->cc_host.resize(kConstCacheBytes);
+    }
+    const size_t need = (bytes + 255) & ~size_t(255);
+    if (ctx->cc_used + need > ctx->cc_cap) {
+        ctx->cc_used = 0;
+        ctx->cc.clear();
+    }
+    const size_t off = ctx->cc_used;
+    std::memcpy(ctx->cc_host.data() + off, src, bytes);
+    char* dst = static_cast<char*>(ctx->cc_dev) + off;
+    VTA_TRY(upload_async(ctx, dst, src, bytes, ctx->stream));
+    ctx->cc.push_back({h, off, bytes});
+    ctx->cc_used = off + need;
+    *out = dst;
+    return VTA_OK;
+}
+
 vta_status ctx_aux(vta_ctx* ctx, size_t bytes, void** out) {
     if (bytes > ctx->aux_bytes && ctx->async_alloc) {
         if (ctx->aux) VTA_CUDA_TRY(cudaFreeAsync(ctx->aux, ctx->stream));
@@ -512,14 +576,14 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             ar.need((size_t)nch * nc * 16);
             ar.need((size_t)nch * nc * 16);
             VTA_TRY(ar.commit());
-            int* d_per = ar.take<int>(nc);
+            const int* d_per = nullptr;
+            VTA_TRY(const_upload(ctx, periods.data(), nc, ar.take<int>(nc), &d_per));
             ar.take<double>(nc);
             ar.take<double>(nc);
             ar.take<float>(nc);
             ar.take<float>(nc);
             float* d_agg = ar.take<float>((size_t)nch * nc * 4);
             float* d_carry = ar.take<float>((size_t)nch * nc * 4);
-            VTA_TRY(upload(ctx, d_per, periods.data(), nc * sizeof(int)));
             RecurArgs a{};
             a.kind = ind == I_EMA ? RK_EMA : ind == I_DEMA ? RK_DEMA : ind == I_TEMA ? RK_TEMA
                    : ind == I_RSI ? RK_RSI : ind == I_WILDERS ? RK_WILDERS : RK_ATR;
@@ -654,15 +718,19 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
         case I_SMA: case I_STDDEV: case I_ZSCORE: case I_BB: {
             ar.need(2 * sizeof(int));
             VTA_TRY(ar.commit());
-            int* d_per = ar.take<int>(nc);
+            const int* d_per = nullptr;
+            VTA_TRY(const_upload(ctx, periods.data(), nc, ar.take<int>(nc), &d_per));
             ar.take<double>(nc);
             ar.take<double>(nc);
-            float* d_fa = ar.take<float>(nc);
-            float* d_fb = ar.take<float>(nc);
+            float* fa_slot = ar.take<float>(nc);
+            float* fb_slot = ar.take<float>(nc);
             int* d_bad = ar.take<int>(2);
-            VTA_TRY(upload(ctx, d_per, periods.data(), nc * sizeof(int)));
-            VTA_TRY(upload(ctx, d_fa, fa.data(), nc * sizeof(float)));
-            VTA_TRY(upload(ctx, d_fb, fb.data(), nc * sizeof(float)));
+            // per-combo scales: nbdev (StdDev / Z-score), devup and devdn (BB);
+            // SMA has none
+            const float* d_fa = nullptr;
+            const float* d_fb = nullptr;
+            if (ind != I_SMA) VTA_TRY(const_upload(ctx, fa.data(), nc, fa_slot, &d_fa));
+            if (ind == I_BB) VTA_TRY(const_upload(ctx, fb.data(), nc, fb_slot, &d_fb));
             PrefixWinArgs a{};
             a.kind = ind == I_SMA ? WK_SMA : ind == I_STDDEV ? WK_STDDEV : ind == I_ZSCORE ? WK_ZSCORE : WK_BB;
             a.x = in.p[0];
@@ -680,8 +748,8 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
         }
         case I_DONCHIAN: case I_WILLR: {
             VTA_TRY(ar.commit());
-            int* d_per = ar.take<int>(nc);
-            VTA_TRY(upload(ctx, d_per, periods.data(), nc * sizeof(int)));
+            const int* d_per = nullptr;
+            VTA_TRY(const_upload(ctx, periods.data(), nc, ar.take<int>(nc), &d_per));
             MinMaxArgs a{};
             a.kind = ind == I_DONCHIAN ? MM_DONCHIAN : MM_WILLR;
             a.h = in.p[0]; a.l = in.p[1];
@@ -1466,6 +1534,7 @@ vta_status vta_ctx_destroy(vta_ctx* ctx) {
     if (ctx->scratch) ctx->async_alloc ? (void)cudaFreeAsync(ctx->scratch, ctx->stream) : (void)cudaFree(ctx->scratch);
     if (ctx->aux) ctx->async_alloc ? (void)cudaFreeAsync(ctx->aux, ctx->stream) : (void)cudaFree(ctx->aux);
     if (ctx->io) cudaFree(ctx->io);
+    if (ctx->cc_dev) cudaFree(ctx->cc_dev);
     if (ctx->async_alloc) cudaStreamSynchronize(ctx->stream);
     if (ctx->err_host) cudaFreeHost(ctx->err_host);
     if (ctx->host_stage) cudaFreeHost(ctx->host_stage);

@@ -91,6 +91,16 @@ struct vta_ctx {
     int* err_host = nullptr;         // pinned
     cudaMemPool_t pool = nullptr;    // stream-ordered allocations of async slots
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // constant cache: small per-sweep arrays (period lists, per-combo
+    // constants) uploaded once and reused by later calls with the same bytes
+    void* cc_dev = nullptr;
+    size_t cc_cap = 0, cc_used = 0;
+    std::vector<unsigned char> cc_host;  // host copy of cc_dev[0, cc_used)
+    struct CcEntry {
+        uint64_t hash;
+        size_t off, bytes;
+    };
+    std::vector<CcEntry> cc;
 };
 
 namespace vta {
@@ -124,6 +134,18 @@ vta_status ctx_aux(vta_ctx* ctx, size_t bytes, void** out);
 // Host -> device copy on `st`, staged through the context's pinned buffer when
 // it fits (the copy is then fully asynchronous), else a pageable copy.
 vta_status upload_async(vta_ctx* ctx, void* dst, const void* src, size_t bytes, cudaStream_t st);
+
+// Device copy of `bytes` constant bytes for this call: from the context's
+// constant cache when an earlier call uploaded the same bytes, else uploaded
+// into the cache (or, for server slots and large arrays, into `fallback`).
+vta_status const_upload_bytes(vta_ctx* ctx, const void* src, size_t bytes, void* fallback, const void** out);
+template <class T>
+inline vta_status const_upload(vta_ctx* ctx, const T* src, size_t count, T* fallback, const T** out) {
+    const void* p = nullptr;
+    const vta_status st = const_upload_bytes(ctx, src, count * sizeof(T), fallback, &p);
+    *out = static_cast<const T*>(p);
+    return st;
+}
 
 // VRAM admission check mirroring the crate's wrappers: required + 64 MiB
 // headroom must fit in free memory (disabled with VTA_MEM_CHECK=0).
