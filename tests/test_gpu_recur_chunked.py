@@ -60,7 +60,7 @@ def test_chunked_equals_sequential_and_oracle(name, gaps, chunk):
         ind.set_policy("recur_chunk", chunk if mode == "chunked" and chunk else
                        ("sequential" if mode == "sequential" else "auto"))
         out[mode] = ind.batch_dev(*ins, sweep=sweep).to_host()
-        assert ind.last_kernel == f"recurrence_{mode}"
+        assert ind.last_kernel.startswith(f"recurrence_{mode}")
     periods = list(range(2, 521, 3))
     exp = oracle_rows(name, h.astype(np.float64), l.astype(np.float64), c.astype(np.float64), periods)
     assert_close(out["chunked"], exp, TOL[name], f"{name} chunked vs oracle")

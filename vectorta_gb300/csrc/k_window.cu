@@ -862,13 +862,26 @@ vta_status launch_prefix_window_tm(const PrefixWinTmArgs& a, cudaStream_t st) {
     return check_launch("k_prefix_window_tm");
 }
 
+static size_t minmax_smem(const MinMaxArgs& a, int tile, int levels) {
+    const size_t nloc = (size_t)tile + a.pmax - 1;
+    return nloc * levels * 2 * sizeof(float) + (2 * (nloc + 1) + 4) * sizeof(int) + (size_t)a.n_combos * sizeof(int4);
+}
+
+std::vector<int> minmax_tile_candidates(const MinMaxArgs& a, size_t smem_optin) {
+    const int levels = 32 - __builtin_clz((unsigned)a.pmax);
+    std::vector<int> c;
+    for (int tile : {512, 1024})
+        if (minmax_smem(a, tile, levels) <= smem_optin && (size_t)a.n >= (size_t)tile * 2 * kNumSMs) c.push_back(tile);
+    return c.size() > 1 ? c : std::vector<int>{};
+}
+
 vta_status launch_minmax_batch(const MinMaxArgs& a, size_t smem_optin, cudaStream_t st) {
     const int levels = 32 - __builtin_clz((unsigned)a.pmax);  // floor(log2 pmax) + 1
     for (int tile = 2048; tile >= 256; tile >>= 1) {
-        const size_t nloc = (size_t)tile + a.pmax - 1;
-        const size_t bytes = nloc * levels * 2 * sizeof(float) + (2 * (nloc + 1) + 4) * sizeof(int) +
-                             (size_t)a.n_combos * sizeof(int4);
-        if (bytes <= smem_optin && (tile <= 512 || (size_t)a.n >= (size_t)tile * 8 * kNumSMs)) {
+        const size_t bytes = minmax_smem(a, tile, levels);
+        const bool pick = a.tile_hint > 0 ? tile == a.tile_hint
+                                          : (tile <= 512 || (size_t)a.n >= (size_t)tile * 8 * kNumSMs);
+        if (bytes <= smem_optin && pick) {
             VTA_CUDA_TRY(cudaFuncSetAttribute(k_minmax_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)bytes));
             ktimer_begin(st);

@@ -12,7 +12,11 @@
 #include <atomic>
 #include <cstdio>
 #include <cstdlib>
+#include <map>
 #include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
 
 #include "vta_internal.h"
 
@@ -321,18 +325,126 @@ struct DevIn {
     const float* p[3];
 };
 
-static int pick_chunk(vta_ctx* ctx, int n, int lanes) {
+// `warps_per_sm`: how many lane-warps x time chunks the chunked scan aims to
+// have in flight per SM (the autotuner's recurrence knob; 64 untuned).
+static int pick_chunk(vta_ctx* ctx, int n, int lanes, int warps_per_sm = 64) {
     const int pol = ctx->policy.recur_chunk;
     if (pol == 1) return ((n + 31) / 32) * 32;
     if (pol > 1) return pol;
     const long lane_warps = (lanes + 31) / 32;
-    const long target = (long)ctx->num_sms * 64;  // warps in flight we aim for
+    const long target = (long)ctx->num_sms * warps_per_sm;  // warps in flight we aim for
     long chunks = std::max(1L, target / std::max(1L, lane_warps));
     long len = (n + chunks - 1) / chunks;
     len = std::max<long>(len, kChunkMin);
     len = ((len + 31) / 32) * 32;
     while ((n + len - 1) / len > 65535) len *= 2;
     return (int)len;
+}
+
+// ------------------------------------------------------ sweep autotuner ---
+// The launch knobs of the batch sweeps are picked by timing: the first call
+// with a new (indicator, log2 length, log2 sweep size, knob) runs the sweep
+// once per candidate (CUDA events around the call's kernels), keeps the
+// fastest, and leaves the outputs of a run with that choice.  The choice is
+// cached for the process and, with VTA_TUNE_CACHE=<file>, in <file>.sweeps
+// ("indicator len_bucket combos_bucket knob value" per line).  Knobs:
+//   TK_RECUR   chunked scans: lane-warps x chunks in flight per SM (32, 64, 128)
+//   TK_MINMAX  sliding min/max: output tile (512, 1024 times per block)
+// Policy "tune" = on (default) | off (untuned defaults) | cached (use cached
+// choices, never time); server slots never time.
+enum TuneKnob { TK_RECUR = 1, TK_MINMAX = 2 };
+using SweepTuneKey = std::tuple<int, int, int, int>;
+static std::mutex g_stune_mu;
+static std::map<SweepTuneKey, int> g_stune;
+static bool g_stune_loaded = false;
+
+static int log2_bucket(long long v) {
+    int b = 0;
+    while ((1LL << b) < v) ++b;
+    return b;
+}
+
+static std::string stune_path() {
+    const char* p = std::getenv("VTA_TUNE_CACHE");
+    return p && *p ? std::string(p) + ".sweeps" : std::string();
+}
+
+static bool stune_lookup(const SweepTuneKey& k, int* v) {
+    std::lock_guard<std::mutex> lock(g_stune_mu);
+    if (!g_stune_loaded) {
+        g_stune_loaded = true;
+        const std::string path = stune_path();
+        if (!path.empty())
+            if (FILE* f = std::fopen(path.c_str(), "r")) {
+                int a, b, c, d, e;
+                while (std::fscanf(f, "%d %d %d %d %d", &a, &b, &c, &d, &e) == 5)
+                    if (e > 0) g_stune[SweepTuneKey{a, b, c, d}] = e;
+                std::fclose(f);
+            }
+    }
+    auto it = g_stune.find(k);
+    if (it == g_stune.end()) return false;
+    *v = it->second;
+    return true;
+}
+
+static void stune_store(const SweepTuneKey& k, int v) {
+    std::lock_guard<std::mutex> lock(g_stune_mu);
+    g_stune[k] = v;
+    const std::string path = stune_path();
+    if (!path.empty())
+        if (FILE* f = std::fopen(path.c_str(), "a")) {
+            std::fprintf(f, "%d %d %d %d %d\n", std::get<0>(k), std::get<1>(k), std::get<2>(k), std::get<3>(k), v);
+            std::fclose(f);
+        }
+}
+
+// Runs `launch(candidate)` for every candidate, keeps the fastest and makes
+// sure the outputs left behind are that candidate's.  `tag` gets the choice
+// and whether it was timed now ("tuned") or taken from the cache ("cached").
+template <class F>
+static vta_status tuned_launch(vta_ctx* ctx, int ind, long long n, long long combos, int knob,
+                               const std::vector<int>& cand, int dflt, F launch, int* chosen, const char** tag) {
+    const SweepTuneKey key{ind, log2_bucket(n), log2_bucket(combos), knob};
+    int v = 0;
+    if (ctx->policy.tune != 1 && cand.size() > 1 && stune_lookup(key, &v) &&
+        std::find(cand.begin(), cand.end(), v) != cand.end()) {
+        *chosen = v;
+        *tag = "cached";
+        return launch(v);
+    }
+    if (ctx->policy.tune != 0 || ctx->async_alloc || cand.size() < 2) {
+        *chosen = dflt;
+        *tag = "default";
+        return launch(dflt);
+    }
+    cudaStream_t st = ctx->stream;
+    cudaEvent_t e0, e1;
+    VTA_CUDA_TRY(cudaEventCreate(&e0));
+    VTA_CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_v = dflt;
+    vta_status s = VTA_OK;
+    for (size_t i = 0; i < cand.size() && s == VTA_OK; ++i) {
+        cudaEventRecord(e0, st);
+        s = launch(cand[i]);
+        cudaEventRecord(e1, st);
+        if (s == VTA_OK && cudaStreamSynchronize(st) != cudaSuccess) s = check_launch("sweep tuning");
+        float ms = 0.f;
+        if (s == VTA_OK) cudaEventElapsedTime(&ms, e0, e1);
+        if (s == VTA_OK && ms < best) {
+            best = ms;
+            best_v = cand[i];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s != VTA_OK) return s;
+    stune_store(key, best_v);
+    *chosen = best_v;
+    *tag = "tuned";
+    // the last run's outputs stand unless another candidate won
+    return best_v == cand.back() ? VTA_OK : launch(best_v);
 }
 
 vta_status upload_async(vta_ctx* ctx, void* dst, const void* src, size_t bytes, cudaStream_t st) {
@@ -540,7 +652,6 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
 
     switch (ind) {
         case I_EMA: case I_DEMA: case I_TEMA: case I_RSI: case I_WILDERS: case I_ATR: {
-            const int chunk = pick_chunk(ctx, n, nc);
             // EMA/DEMA/TEMA/RSI: the last seed index of the sweep; chunks that
             // start past it run the fast aggregate pass.  With the automatic
             // policy chunk 0 ends just past it, so that only one short chunk
@@ -555,26 +666,38 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
                                     : (long long)first + p;
                 s_max = std::max(s_max, s);
             }
-            int chunk0 = chunk;
-            if (fast_kind && ctx->policy.recur_chunk == 0 && s_max + 1 < n)
-                chunk0 = (int)std::max<long long>(32, ((s_max + 1 + 31) / 32) * 32);
-            const int nch = recur_n_chunks(n, chunk, chunk0);
-            int fast_from = nch;
-            for (int k = 1; k < nch; ++k) {
-                int c0 = 0, c1 = 0;
-                RecurArgs tmp{};
-                tmp.n = n;
-                tmp.chunk = chunk;
-                tmp.chunk0 = chunk0;
-                recur_chunk_bounds(tmp, k, c0, c1);
-                if (c0 > s_max) {
-                    fast_from = k;
-                    break;
+            // chunking for a target of `wps` lane-warps x chunks per SM
+            struct Chunking {
+                int chunk, chunk0, nch, fast_from;
+            };
+            auto chunking = [&](int wps) {
+                Chunking c{};
+                c.chunk = pick_chunk(ctx, n, nc, wps);
+                c.chunk0 = c.chunk;
+                if (fast_kind && ctx->policy.recur_chunk == 0 && s_max + 1 < n)
+                    c.chunk0 = (int)std::max<long long>(32, ((s_max + 1 + 31) / 32) * 32);
+                c.nch = recur_n_chunks(n, c.chunk, c.chunk0);
+                c.fast_from = c.nch;
+                for (int k = 1; k < c.nch; ++k) {
+                    int c0 = 0, c1 = 0;
+                    RecurArgs tmp{};
+                    tmp.n = n;
+                    tmp.chunk = c.chunk;
+                    tmp.chunk0 = c.chunk0;
+                    recur_chunk_bounds(tmp, k, c0, c1);
+                    if (c0 > s_max) {
+                        c.fast_from = k;
+                        break;
+                    }
                 }
-            }
-            const bool use_fast = fast_kind && nch > 1 && fast_from < nch;
-            ar.need((size_t)nch * nc * 16);
-            ar.need((size_t)nch * nc * 16);
+                return c;
+            };
+            const std::vector<int> cand = ctx->policy.recur_chunk == 0 ? std::vector<int>{32, 64, 128}
+                                                                       : std::vector<int>{64};
+            int max_nch = 1;
+            for (int w : cand) max_nch = std::max(max_nch, chunking(w).nch);
+            ar.need((size_t)max_nch * nc * 16);
+            ar.need((size_t)max_nch * nc * 16);
             VTA_TRY(ar.commit());
             const int* d_per = nullptr;
             VTA_TRY(const_upload(ctx, periods.data(), nc, ar.take<int>(nc), &d_per));
@@ -582,8 +705,8 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             ar.take<double>(nc);
             ar.take<float>(nc);
             ar.take<float>(nc);
-            float* d_agg = ar.take<float>((size_t)nch * nc * 4);
-            float* d_carry = ar.take<float>((size_t)nch * nc * 4);
+            float* d_agg = ar.take<float>((size_t)max_nch * nc * 4);
+            float* d_carry = ar.take<float>((size_t)max_nch * nc * 4);
             RecurArgs a{};
             a.kind = ind == I_EMA ? RK_EMA : ind == I_DEMA ? RK_DEMA : ind == I_TEMA ? RK_TEMA
                    : ind == I_RSI ? RK_RSI : ind == I_WILDERS ? RK_WILDERS : RK_ATR;
@@ -594,15 +717,27 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             a.first = (int)first;
             a.periods = d_per;
             a.n_lanes = nc;
-            a.chunk = chunk;
-            a.chunk0 = chunk0;
-            a.fast_from = fast_from;
-            a.fast_agg = use_fast ? 1 : 0;
             a.out = out[0];
             a.agg = d_agg;
             a.carry = d_carry;
-            ctx->last_kernel = nch > 1 ? "recurrence_chunked" : "recurrence_sequential";
-            return launch_recurrence(a, st);
+            int nch_used = 1;
+            auto launch = [&](int wps) {
+                const Chunking c = chunking(wps);
+                a.chunk = c.chunk;
+                a.chunk0 = c.chunk0;
+                a.fast_from = c.fast_from;
+                a.fast_agg = (fast_kind && c.nch > 1 && c.fast_from < c.nch) ? 1 : 0;
+                nch_used = c.nch;
+                return launch_recurrence(a, st);
+            };
+            int wps = 64;
+            const char* tag = "default";
+            VTA_TRY(tuned_launch(ctx, (int)ind, n, nc, TK_RECUR, cand, 64, launch, &wps, &tag));
+            ctx->last_kernel = nch_used > 1 ? "recurrence_chunked" : "recurrence_sequential";
+            if (nch_used > 1 && ctx->policy.recur_chunk == 0)
+                ctx->last_kernel += "(chunk=" + std::to_string(a.chunk) + ", " + std::to_string(wps) + " warps/SM, " +
+                                    tag + ")";
+            return VTA_OK;
         }
         case I_ADX: case I_SUPERTREND: {
             // time-chunked with verified warm restarts unless the policy asks
@@ -752,6 +887,7 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             VTA_TRY(const_upload(ctx, periods.data(), nc, ar.take<int>(nc), &d_per));
             MinMaxArgs a{};
             a.kind = ind == I_DONCHIAN ? MM_DONCHIAN : MM_WILLR;
+            a.tile_hint = 0;
             a.h = in.p[0]; a.l = in.p[1];
             a.c = ind == I_WILLR ? in.p[2] : nullptr;
             a.n = n;
@@ -761,8 +897,17 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             a.pmax = pmax;
             a.out0 = out[0];
             if (ind == I_DONCHIAN) { a.out1 = out[1]; a.out2 = out[2]; }
-            ctx->last_kernel = "minmax_sparse_table";
-            return launch_minmax_batch(a, ctx->smem_optin, st);
+            int tile = 0;
+            const char* tag = "default";
+            auto launch = [&](int t) {
+                a.tile_hint = t;
+                return launch_minmax_batch(a, ctx->smem_optin, st);
+            };
+            VTA_TRY(tuned_launch(ctx, (int)ind, n, nc, TK_MINMAX, minmax_tile_candidates(a, ctx->smem_optin), 0,
+                                 launch, &tile, &tag));
+            ctx->last_kernel = std::string("minmax_sparse_table(tile=") + (tile ? std::to_string(tile) : "auto") +
+                               ", " + tag + ")";
+            return VTA_OK;
         }
         case I_PNR: {
             const int nchunk = (n + 255) / 256;
@@ -1621,6 +1766,13 @@ vta_status vta_ctx_set_policy(vta_ctx* ctx, const char* key, const char* value) 
         } else {
             return fail(VTA_ERR_INVALID_POLICY, "host_io: cached|per_call");
         }
+        return VTA_OK;
+    }
+    if (k == "tune") {
+        if (v == "on") ctx->policy.tune = 0;
+        else if (v == "off") ctx->policy.tune = 1;
+        else if (v == "cached") ctx->policy.tune = 2;
+        else return fail(VTA_ERR_INVALID_POLICY, "tune: on|off|cached");
         return VTA_OK;
     }
     if (k == "tm_chunk" || k == "tm_warm") {

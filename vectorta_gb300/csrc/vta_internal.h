@@ -59,6 +59,9 @@ struct Policy {
     // *_batch_into_host_f32: 0 = keep the device input/output buffers in the
     // context between calls ("cached"), 1 = allocate and free them per call
     int host_io = 0;
+    // batch-sweep autotuner: 0 = on (time candidates on the first call per
+    // key), 1 = off (untuned defaults), 2 = cached choices only
+    int tune = 0;
 };
 
 }  // namespace vta
@@ -352,8 +355,12 @@ struct MinMaxArgs {
     float* out0;           // donchian upper / willr
     float* out1;           // donchian middle
     float* out2;           // donchian lower
+    int tile_hint;         // output times per block (0 = the launcher's choice)
 };
 vta_status launch_minmax_batch(const MinMaxArgs& a, size_t smem_optin, cudaStream_t st);
+// Tiles launch_minmax_batch can run for `a` (the autotuner's candidates;
+// empty when only the launcher's own choice applies).
+std::vector<int> minmax_tile_candidates(const MinMaxArgs& a, size_t smem_optin);
 
 struct MinMaxTmArgs {
     int kind;
