@@ -48,6 +48,12 @@ typedef enum vta_status {
 /* Message of the last failure on the calling thread (the Display text of the
  * crate's error enums). */
 const char* vta_last_error(void);
+/* The fields of CudaXError::OutOfMemory{required, free, headroom}
+ * (alma_wrapper.rs:72-101, raised at alma_wrapper.rs:300-310): when the last
+ * failure on the calling thread was VTA_ERR_OUT_OF_MEMORY, writes its byte
+ * counts (any pointer may be null) and returns VTA_OK; otherwise writes zeros
+ * and returns VTA_ERR_INVALID_INPUT. */
+vta_status vta_last_error_oom(size_t* required, size_t* free_bytes, size_t* headroom);
 const char* vta_version(void);
 
 /* Number of CUDA devices (crate: cuda_device_count, src/cuda/mod.rs:560-575);

@@ -33,6 +33,39 @@ def test_version_and_device_count_without_gpu():
     assert N.lib().vta_device_count() >= 0
 
 
+def test_oom_payload_is_empty_unless_the_last_failure_was_out_of_memory():
+    # (no GPU needed: nothing has failed with OutOfMemory on this thread)
+    r, f, h = C.c_size_t(7), C.c_size_t(7), C.c_size_t(7)
+    assert N.lib().vta_last_error_oom(C.byref(r), C.byref(f), C.byref(h)) == 4
+    assert (r.value, f.value, h.value) == (0, 0, 0)
+    assert N.lib().vta_last_error_oom(None, None, None) == 4
+
+
+def test_rust_binding_declares_every_entry_point():
+    """The generated Rust crate (not compiled here: no Rust toolchain) declares
+    each C entry point of the indicators and of the context, with as many
+    parameters as the header gives it."""
+    import os
+    import re
+
+    src = open(os.path.join(os.path.dirname(N.HEADER), "..", "vectorta_gb300", "rust", "vta_sys", "src",
+                            "lib.rs")).read()
+    hdr = open(N.HEADER).read()
+    rust = {m.group(1): m.group(2) for m in re.finditer(r"pub fn (vta_\w+)\(([^)]*)\)", src)}
+    want = [f"vta_{n}_{s}" for n in N.INDICATORS for s in (
+        "expand_grid", "batch_dev", "batch_device", "batch_into_host_f32",
+        "many_series_one_param_time_major_dev", "many_series_one_param_device")]
+    want += ["vta_ctx_create", "vta_ctx_destroy", "vta_ctx_synchronize", "vta_ctx_set_policy",
+             "vta_last_error", "vta_last_error_oom", "vta_device_array_free"]
+    for name in want:
+        assert name in rust, name
+        m = re.search(name + r"\(([^;]*)\);", hdr)
+        assert m, name
+        n_c = 0 if m.group(1).strip() in ("void", "") else m.group(1).count(",") + 1
+        n_r = 0 if not rust[name].strip() else rust[name].count(",") + 1
+        assert n_c == n_r, (name, n_c, n_r)
+
+
 def test_ctx_create_fails_loudly_without_gpu():
     if V.device_count() > 0:
         pytest.skip("a GPU is present")

@@ -355,6 +355,29 @@ def test_invalid_inputs_raise():
         V.CudaEma(0).ema_many_series_one_param_time_major_dev(c, params={"period": 5})
 
 
+def test_out_of_memory_carries_its_byte_counts():
+    """CudaXError::OutOfMemory{required, free, headroom}: a sweep whose outputs
+    exceed the free device memory is refused by the admission check before
+    anything that large is allocated, and the error carries the byte counts."""
+    import torch
+
+    free, _ = torch.cuda.mem_get_info()
+    n = 1 << 24  # 16.8M bars: 64 MB of input
+    rows = free // (n * 4) + 64  # outputs larger than all the free memory
+    x = datagen.random_walk(n, seed=3).astype(np.float32)
+    with pytest.raises(V.VtaError) as e:
+        V.CudaEma(0).ema_batch_dev(x, sweep={"period": (2, 1 + int(rows), 1)})
+    err = e.value
+    assert err.kind == "OutOfMemory"
+    assert err.required >= rows * n * 4
+    assert 0 < err.free < err.required
+    assert err.headroom == 64 << 20
+    # a later failure of another kind clears the payload
+    with pytest.raises(V.VtaError) as e2:
+        V.CudaEma(0).ema_batch_dev(np.zeros(0, dtype=np.float32), sweep={"period": (3, 3, 0)})
+    assert e2.value.kind == "InvalidInput" and e2.value.required == 0
+
+
 def test_golden_fixture_through_gpu(candles, golden):
     """The crate's golden vectors, reproduced by the GPU path on the f32 fixture."""
     c = f32(candles["close"])

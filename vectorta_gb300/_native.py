@@ -22,11 +22,14 @@ STATUS = {
 
 
 class VtaError(RuntimeError):
-    """Mirrors the crate's CudaXError enums: `kind` is the variant name."""
+    """Mirrors the crate's CudaXError enums: `kind` is the variant name.
+    OutOfMemory also carries the variant's fields `required`, `free` and
+    `headroom` (bytes)."""
 
-    def __init__(self, status: int, message: str):
+    def __init__(self, status: int, message: str, oom=None):
         self.status = status
         self.kind = STATUS.get(status, f"status{status}")
+        self.required, self.free, self.headroom = oom if oom else (0, 0, 0)
         super().__init__(f"{self.kind}: {message}")
 
 
@@ -162,6 +165,8 @@ def lib() -> C.CDLL:
     vp, sz, st = C.c_void_p, C.c_size_t, C.c_int
     fp = C.POINTER(C.c_float)
     L.vta_last_error.restype = C.c_char_p
+    L.vta_last_error_oom.argtypes = [C.POINTER(sz)] * 3
+    L.vta_last_error_oom.restype = st
     L.vta_version.restype = C.c_char_p
     L.vta_device_count.restype = C.c_int
     L.vta_ctx_create.argtypes = [C.c_int, C.POINTER(vp)]
@@ -252,5 +257,11 @@ def lib() -> C.CDLL:
 
 def check(status: int):
     if status != 0:
-        msg = lib().vta_last_error()
-        raise VtaError(status, msg.decode() if msg else "")
+        L = lib()
+        msg = L.vta_last_error()
+        oom = None
+        if status == 2:  # VTA_ERR_OUT_OF_MEMORY
+            r, f, h = C.c_size_t(), C.c_size_t(), C.c_size_t()
+            if L.vta_last_error_oom(C.byref(r), C.byref(f), C.byref(h)) == 0:
+                oom = (r.value, f.value, h.value)
+        raise VtaError(status, msg.decode() if msg else "", oom)

@@ -107,6 +107,12 @@ typedef enum vta_status {
 /* Message of the last failure on the calling thread (the Display text of the
  * crate's error enums). */
 const char* vta_last_error(void);
+/* The fields of CudaXError::OutOfMemory{required, free, headroom}
+ * (alma_wrapper.rs:72-101, raised at alma_wrapper.rs:300-310): when the last
+ * failure on the calling thread was VTA_ERR_OUT_OF_MEMORY, writes its byte
+ * counts (any pointer may be null) and returns VTA_OK; otherwise writes zeros
+ * and returns VTA_ERR_INVALID_INPUT. */
+vta_status vta_last_error_oom(size_t* required, size_t* free_bytes, size_t* headroom);
 const char* vta_version(void);
 
 /* Number of CUDA devices (crate: cuda_device_count, src/cuda/mod.rs:560-575);
@@ -406,7 +412,7 @@ w("""/* ==== sma without device allocation ====
  * call (sma_batch_dev_from_device, sma_wrapper.rs:830-841, allocates the
  * period list, the prefix and the output), and so do the other entry points
  * here.  vta_sma_batch_device_noalloc returns what vta_sma_batch_device
- * returns (same arguments, checks and errors) but never allocates device
+ * returns (same arguments and parameter checks) but never allocates device
  * memory: its working buffers live in one fixed scratch area of the library's
  * static device memory (VTA_NOALLOC_SCRATCH_BYTES, about 16 KiB per device,
  * reserved on a device when the function is first called there).
@@ -420,7 +426,12 @@ w("""/* ==== sma without device allocation ====
  *     the limit (vta_sma_batch_device has no such limit).
  *   - The first call on each device does one-time setup (it looks up the
  *     scratch address, which loads the library's device code there); make
- *     that first call before any stream capture on that device.
+ *     that first call before any stream capture on that device.  No call can
+ *     be captured: each uploads its period list from host memory and waits
+ *     for its stream.
+ *   - The period count is taken from the range arithmetic before anything
+ *     is expanded, so an oversized sweep is refused at once; the periods
+ *     live on the caller's stack (16 KiB at the limit).
  *   - There is one scratch area per device per process.  Calls that overlap
  *     in time on the same device (from several host threads, whatever their
  *     contexts or streams) race on it and corrupt each other's results:
@@ -491,3 +502,297 @@ for (name, wf, kind, outs, rng, prm, cites) in IND:
     inc.append("")
 open("vectorta_gb300/csrc/vta_abi_gen.inc","w").write("\n".join(inc)+"\n")
 print("ok")
+
+# ---------------------------------------------------------------- Rust ----
+# A thin Rust binding crate (vectorta_gb300/rust/vta_sys): the C ABI's
+# declarations plus CudaX-shaped safe wrappers with the crate's method names,
+# so the crate's src/cuda callers can switch their backend to the library.
+# No Rust toolchain exists in the environment that builds this repository, so
+# the generated crate is not compiled here.
+RFIELDS = {
+    "alma": ([("period", "VtaRangeUsize"), ("offset", "VtaRangeF64"), ("sigma", "VtaRangeF64")],
+             [("period", "usize"), ("offset", "f64"), ("sigma", "f64")]),
+    "period": ([("period", "VtaRangeUsize")], [("period", "usize")]),
+    "stddev": ([("period", "VtaRangeUsize"), ("nbdev", "VtaRangeF64")], [("period", "usize"), ("nbdev", "f64")]),
+    "zscore": ([("period", "VtaRangeUsize"), ("nbdev", "VtaRangeF64")], [("period", "usize"), ("nbdev", "f64")]),
+    "bollinger": ([("period", "VtaRangeUsize"), ("devup", "VtaRangeF64"), ("devdn", "VtaRangeF64")],
+                  [("period", "usize"), ("devup", "f64"), ("devdn", "f64")]),
+    "supertrend": ([("period", "VtaRangeUsize"), ("factor", "VtaRangeF64")], [("period", "usize"), ("factor", "f64")]),
+    "percentile": ([("length", "VtaRangeUsize"), ("percentage", "VtaRangeF64")],
+                   [("length", "usize"), ("percentage", "f64")]),
+    "epma": ([("period", "VtaRangeUsize"), ("offset", "VtaRangeUsize")], [("period", "usize"), ("offset", "usize")]),
+    "vpwma": ([("period", "VtaRangeUsize"), ("power", "VtaRangeF64")], [("period", "usize"), ("power", "f64")]),
+}
+
+
+def camel(s):
+    return "".join(p[:1].upper() + p[1:] for p in s.split("_"))
+
+
+def rtypes(rng):
+    R, P = RANGES[rng]
+    return camel(R), camel(P)
+
+
+def rin(kind, dev, tm):
+    """Rust parameters of the input series (slices, or raw device pointers)."""
+    nm = {"x": ["data"], "hl": ["high", "low"], "hlc": ["high", "low", "close"]}[kind]
+    suf = "_tm" if tm else ""
+    return [(f"{'d_' if dev else ''}{n}{suf}", "*const f32" if dev else "&[f32]") for n in nm]
+
+
+rs = []
+r = rs.append
+r("""//! vta_sys -- Rust binding of libvta_gb300.so (include/vta_gb300.h).
+//!
+//! Generated by vectorta_gb300/csrc/gen_abi.py; do not edit by hand.  NOT
+//! COMPILED in the environment that builds this repository (it has no Rust
+//! toolchain): the declarations follow the C header one to one and the safe
+//! layer mirrors the crate's src/cuda wrappers (`CudaX::new`,
+//! `x_batch_dev`, `x_batch_into_host_f32`, `x_many_series_one_param_time_major_dev`,
+//! `x_batch_device`, `DeviceArrayF32`, `CudaXError`), so a caller switches by
+//! replacing its `use crate::cuda::...` imports.  Link with
+//! `-L <repo>/vectorta_gb300/_lib -lvta_gb300` (see build.rs).
+#![allow(non_camel_case_types, clippy::too_many_arguments)]
+
+use std::ffi::{CStr, CString};
+use std::os::raw::{c_char, c_int, c_void};
+
+pub type VtaStatus = c_int;
+
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct VtaRangeUsize { pub start: usize, pub end: usize, pub step: usize }
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct VtaRangeF64 { pub start: f64, pub end: f64, pub step: f64 }
+#[repr(C)]
+#[derive(Clone, Copy, Debug)]
+pub struct VtaDeviceArray { pub ptr: *mut f32, pub rows: usize, pub cols: usize, pub device: c_int }
+impl Default for VtaDeviceArray {
+    fn default() -> Self { VtaDeviceArray { ptr: std::ptr::null_mut(), rows: 0, cols: 0, device: -1 } }
+}
+#[repr(C)]
+pub struct VtaCtx { _private: [u8; 0] }
+""")
+for rng, (rf, pf) in RFIELDS.items():
+    RT, PT = rtypes(rng)
+    r("#[repr(C)]\n#[derive(Clone, Copy, Debug, Default)]")
+    r(f"pub struct {RT} {{ " + ", ".join(f"pub {n}: {t}" for n, t in rf) + " }")
+    r("#[repr(C)]\n#[derive(Clone, Copy, Debug, Default)]")
+    r(f"pub struct {PT} {{ " + ", ".join(f"pub {n}: {t}" for n, t in pf) + " }")
+r("""
+#[link(name = "vta_gb300")]
+extern "C" {
+    pub fn vta_last_error() -> *const c_char;
+    pub fn vta_last_error_oom(required: *mut usize, free_bytes: *mut usize, headroom: *mut usize) -> VtaStatus;
+    pub fn vta_version() -> *const c_char;
+    pub fn vta_device_count() -> c_int;
+    pub fn vta_ctx_create(device_id: c_int, out: *mut *mut VtaCtx) -> VtaStatus;
+    pub fn vta_ctx_destroy(ctx: *mut VtaCtx) -> VtaStatus;
+    pub fn vta_ctx_synchronize(ctx: *mut VtaCtx) -> VtaStatus;
+    pub fn vta_ctx_set_stream(ctx: *mut VtaCtx, stream: *mut c_void) -> VtaStatus;
+    pub fn vta_ctx_set_policy(ctx: *mut VtaCtx, key: *const c_char, value: *const c_char) -> VtaStatus;
+    pub fn vta_ctx_last_kernel(ctx: *mut VtaCtx) -> *const c_char;
+    pub fn vta_device_array_free(a: *mut VtaDeviceArray) -> VtaStatus;
+    pub fn vta_device_array_copy_to_host(ctx: *mut VtaCtx, a: *const VtaDeviceArray, host: *mut f32, n: usize) -> VtaStatus;""")
+for (name, wf, kind, outs, rng, prm, cites) in IND:
+    RT, PT = rtypes(rng)
+    hin = ", ".join(f"{n.replace('&[f32]','')}: *const f32" for n, _ in rin(kind, False, False))
+    din = ", ".join(f"{n}: *const f32" for n, _ in rin(kind, True, False))
+    thin = ", ".join(f"{n}: *const f32" for n, _ in rin(kind, False, True))
+    tdin = ", ".join(f"{n}: *const f32" for n, _ in rin(kind, True, True))
+    oa = ", ".join(f"{o}: *mut VtaDeviceArray" for o in outs)
+    od = ", ".join(f"d_{o}: *mut f32" for o in outs)
+    oh = ", ".join(f"{o}: *mut f32" for o in outs)
+    r(f"    pub fn vta_{name}_expand_grid(sweep: *const {RT}, out: *mut {PT}, cap: usize, n_combos: *mut usize) -> VtaStatus;")
+    r(f"    pub fn vta_{name}_batch_dev(ctx: *mut VtaCtx, {hin}, len: usize, sweep: *const {RT}, {oa}) -> VtaStatus;")
+    r(f"    pub fn vta_{name}_batch_device(ctx: *mut VtaCtx, {din}, len: usize, first_valid: usize, sweep: *const {RT}, {od}) -> VtaStatus;")
+    r(f"    pub fn vta_{name}_batch_into_host_f32(ctx: *mut VtaCtx, {hin}, len: usize, sweep: *const {RT}, {oh}, out_len: usize, rows: *mut usize, cols: *mut usize) -> VtaStatus;")
+    r(f"    pub fn vta_{name}_many_series_one_param_time_major_dev(ctx: *mut VtaCtx, {thin}, cols: usize, rows: usize, params: *const {PT}, {oa}) -> VtaStatus;")
+    r(f"    pub fn vta_{name}_many_series_one_param_device(ctx: *mut VtaCtx, {tdin}, cols: usize, rows: usize, params: *const {PT}, {od}) -> VtaStatus;")
+r("}")
+r("""
+/// The crate's CudaXError variants (alma_wrapper.rs:72-101), one per status.
+#[derive(Debug, Clone)]
+pub enum CudaError {
+    Cuda(String),
+    OutOfMemory { required: usize, free: usize, headroom: usize },
+    MissingKernelSymbol(String),
+    InvalidInput(String),
+    InvalidPolicy(String),
+    LaunchConfigTooLarge(String),
+    DeviceMismatch(String),
+    NotImplemented(String),
+}
+
+impl std::fmt::Display for CudaError {
+    fn fmt(&self, f: &mut std::fmt::Formatter<'_>) -> std::fmt::Result { write!(f, "{:?}", self) }
+}
+impl std::error::Error for CudaError {}
+
+fn check(st: VtaStatus) -> Result<(), CudaError> {
+    if st == 0 {
+        return Ok(());
+    }
+    let msg = unsafe {
+        let p = vta_last_error();
+        if p.is_null() { String::new() } else { CStr::from_ptr(p).to_string_lossy().into_owned() }
+    };
+    Err(match st {
+        2 => {
+            let (mut r, mut f, mut h) = (0usize, 0usize, 0usize);
+            unsafe { vta_last_error_oom(&mut r, &mut f, &mut h) };
+            CudaError::OutOfMemory { required: r, free: f, headroom: h }
+        }
+        3 => CudaError::MissingKernelSymbol(msg),
+        4 => CudaError::InvalidInput(msg),
+        5 => CudaError::InvalidPolicy(msg),
+        6 => CudaError::LaunchConfigTooLarge(msg),
+        7 => CudaError::DeviceMismatch(msg),
+        8 => CudaError::NotImplemented(msg),
+        _ => CudaError::Cuda(msg),
+    })
+}
+
+/// One context: a device and a private non-blocking stream (CudaX::new).
+pub struct Context { raw: *mut VtaCtx }
+impl Context {
+    pub fn new(device_id: usize) -> Result<Self, CudaError> {
+        let mut raw = std::ptr::null_mut();
+        check(unsafe { vta_ctx_create(device_id as c_int, &mut raw) })?;
+        Ok(Context { raw })
+    }
+    pub fn raw(&self) -> *mut VtaCtx { self.raw }
+    pub fn synchronize(&self) -> Result<(), CudaError> { check(unsafe { vta_ctx_synchronize(self.raw) }) }
+    pub fn set_policy(&self, key: &str, value: &str) -> Result<(), CudaError> {
+        let (k, v) = (CString::new(key).unwrap(), CString::new(value).unwrap());
+        check(unsafe { vta_ctx_set_policy(self.raw, k.as_ptr(), v.as_ptr()) })
+    }
+    pub fn selected_kernel(&self) -> String {
+        unsafe { CStr::from_ptr(vta_ctx_last_kernel(self.raw)).to_string_lossy().into_owned() }
+    }
+}
+impl Drop for Context {
+    fn drop(&mut self) { unsafe { vta_ctx_destroy(self.raw); } }
+}
+
+/// A device-resident f32 matrix owned by the caller (the crate's DeviceArrayF32,
+/// alma_wrapper.rs:103-117): row-major rows x cols, freed on drop.
+pub struct DeviceArrayF32 { pub raw: VtaDeviceArray }
+impl DeviceArrayF32 {
+    pub fn rows(&self) -> usize { self.raw.rows }
+    pub fn cols(&self) -> usize { self.raw.cols }
+    pub fn len(&self) -> usize { self.raw.rows * self.raw.cols }
+    pub fn is_empty(&self) -> bool { self.len() == 0 }
+    pub fn device_ptr(&self) -> *mut f32 { self.raw.ptr }
+    pub fn copy_to_host(&self, ctx: &Context, out: &mut [f32]) -> Result<(), CudaError> {
+        check(unsafe { vta_device_array_copy_to_host(ctx.raw(), &self.raw, out.as_mut_ptr(), out.len()) })
+    }
+}
+impl Drop for DeviceArrayF32 {
+    fn drop(&mut self) { unsafe { vta_device_array_free(&mut self.raw); } }
+}
+""")
+for (name, wf, kind, outs, rng, prm, cites) in IND:
+    RT, PT = rtypes(rng)
+    cls = "Cuda" + camel(name)
+    ins = rin(kind, False, False)
+    ins_tm = rin(kind, False, True)
+    dins = rin(kind, True, False)
+    dins_tm = rin(kind, True, True)
+    no = len(outs)
+    ret = "DeviceArrayF32" if no == 1 else "(" + ", ".join(["DeviceArrayF32"] * no) + ")"
+    mk = ("DeviceArrayF32 { raw: o[0] }" if no == 1 else
+          "(" + ", ".join(f"DeviceArrayF32 {{ raw: o[{i}] }}" for i in range(no)) + ")")
+    optrs = ", ".join(f"&mut o[{i}]" for i in range(no))
+    r(f"/// {name}: replaces {wf} (CudaX::new at line {cites[0]}).")
+    r(f"pub struct {cls} {{ pub ctx: Context }}")
+    r(f"impl {cls} {{")
+    r(f"    pub fn new(device_id: usize) -> Result<Self, CudaError> {{ Ok({cls} {{ ctx: Context::new(device_id)? }}) }}")
+    r(f"    pub fn synchronize(&self) -> Result<(), CudaError> {{ self.ctx.synchronize() }}")
+    r(f"    pub fn set_policy(&self, key: &str, value: &str) -> Result<(), CudaError> {{ self.ctx.set_policy(key, value) }}")
+    r(f"    pub fn expand_grid(sweep: &{RT}) -> Result<Vec<{PT}>, CudaError> {{")
+    r(f"        let mut n = 0usize;")
+    r(f"        unsafe {{ vta_{name}_expand_grid(sweep, std::ptr::null_mut(), 0, &mut n) }};")
+    r(f"        let mut v = vec![{PT}::default(); n];")
+    r(f"        check(unsafe {{ vta_{name}_expand_grid(sweep, v.as_mut_ptr(), n, &mut n) }})?;")
+    r(f"        Ok(v)")
+    r(f"    }}")
+    a_in = ", ".join(f"{n}: {t}" for n, t in ins)
+    lens = ins[0][0]
+    checks = "".join(f"        if {n}.len() != {lens}.len() {{ return Err(CudaError::InvalidInput(\"inconsistent input lengths\".into())); }}\n"
+                     for n, _ in ins[1:])
+    p_in = ", ".join(f"{n}.as_ptr()" for n, _ in ins)
+    r(f"    pub fn {name}_batch_dev(&self, {a_in}, sweep: &{RT}) -> Result<{ret}, CudaError> {{")
+    if checks: r(checks.rstrip("\n"))
+    r(f"        let mut o = [VtaDeviceArray::default(); {no}];")
+    r(f"        check(unsafe {{ vta_{name}_batch_dev(self.ctx.raw(), {p_in}, {lens}.len(), sweep, {optrs}) }})?;")
+    r(f"        Ok({mk})")
+    r(f"    }}")
+    on_ = [o if o.startswith("out") else "out_" + o for o in outs]
+    o_mut = ", ".join(f"{o}: &mut [f32]" for o in on_)
+    o_ptr = ", ".join(f"{o}.as_mut_ptr()" for o in on_)
+    r(f"    /// Returns (rows, cols); every output slice holds at least rows * cols values.")
+    r(f"    pub fn {name}_batch_into_host_f32(&self, {a_in}, sweep: &{RT}, {o_mut}) -> Result<(usize, usize), CudaError> {{")
+    if checks: r(checks.rstrip("\n"))
+    r(f"        let out_len = {on_[0]}.len();")
+    for o in on_[1:]:
+        r(f"        if {o}.len() < out_len {{ return Err(CudaError::InvalidInput(\"output slices of different lengths\".into())); }}")
+    r(f"        let (mut rows, mut cols) = (0usize, 0usize);")
+    r(f"        check(unsafe {{ vta_{name}_batch_into_host_f32(self.ctx.raw(), {p_in}, {lens}.len(), sweep, {o_ptr}, out_len, &mut rows, &mut cols) }})?;")
+    r(f"        Ok((rows, cols))")
+    r(f"    }}")
+    a_tm = ", ".join(f"{n}: {t}" for n, t in ins_tm)
+    p_tm = ", ".join(f"{n}.as_ptr()" for n, _ in ins_tm)
+    r(f"    /// Time-major [rows][cols] input (element (t, s) at t * cols + s).")
+    r(f"    pub fn {name}_many_series_one_param_time_major_dev(&self, {a_tm}, cols: usize, rows: usize, params: &{PT}) -> Result<{ret}, CudaError> {{")
+    for n, _ in ins_tm:
+        r(f"        if {n}.len() < cols * rows {{ return Err(CudaError::InvalidInput(\"input shorter than cols * rows\".into())); }}")
+    r(f"        let mut o = [VtaDeviceArray::default(); {no}];")
+    r(f"        check(unsafe {{ vta_{name}_many_series_one_param_time_major_dev(self.ctx.raw(), {p_tm}, cols, rows, params, {optrs}) }})?;")
+    r(f"        Ok({mk})")
+    r(f"    }}")
+    a_d = ", ".join(f"{n}: {t}" for n, t in dins)
+    n_d = ", ".join(n for n, _ in dins)
+    od_a = ", ".join(f"d_{o}: *mut f32" for o in outs)
+    od_n = ", ".join(f"d_{o}" for o in outs)
+    r(f"    /// Device inputs and caller-provided device outputs (x_batch_device).")
+    r(f"    /// # Safety: the pointers address device buffers of len and n_combos * len floats.")
+    r(f"    pub unsafe fn {name}_batch_device(&self, {a_d}, len: usize, first_valid: usize, sweep: &{RT}, {od_a}) -> Result<(), CudaError> {{")
+    r(f"        check(vta_{name}_batch_device(self.ctx.raw(), {n_d}, len, first_valid, sweep, {od_n}))")
+    r(f"    }}")
+    a_dt = ", ".join(f"{n}: {t}" for n, t in dins_tm)
+    n_dt = ", ".join(n for n, _ in dins_tm)
+    r(f"    /// # Safety: the pointers address device buffers of cols * rows floats.")
+    r(f"    pub unsafe fn {name}_many_series_one_param_device(&self, {a_dt}, cols: usize, rows: usize, params: &{PT}, {od_a}) -> Result<(), CudaError> {{")
+    r(f"        check(vta_{name}_many_series_one_param_device(self.ctx.raw(), {n_dt}, cols, rows, params, {od_n}))")
+    r(f"    }}")
+    r("}")
+    r("")
+import os as _os
+_os.makedirs("vectorta_gb300/rust/vta_sys/src", exist_ok=True)
+open("vectorta_gb300/rust/vta_sys/src/lib.rs", "w").write("\n".join(rs) + "\n")
+open("vectorta_gb300/rust/vta_sys/Cargo.toml", "w").write("""[package]
+name = "vta_sys"
+version = "0.1.0"
+edition = "2021"
+description = "Rust binding of libvta_gb300 (GB300-native VectorTA indicator hot path); generated by gen_abi.py"
+publish = false
+
+[lib]
+path = "src/lib.rs"
+""")
+open("vectorta_gb300/rust/vta_sys/build.rs", "w").write("""// Links libvta_gb300.so from the repository's build folder, or from
+// VTA_GB300_LIB_DIR when set.  Generated by gen_abi.py.
+fn main() {
+    let dir = std::env::var("VTA_GB300_LIB_DIR").unwrap_or_else(|_| {
+        let here = std::env::var("CARGO_MANIFEST_DIR").unwrap();
+        format!("{}/../../_lib", here)
+    });
+    println!("cargo:rustc-link-search=native={}", dir);
+    println!("cargo:rustc-link-lib=dylib=vta_gb300");
+    println!("cargo:rerun-if-env-changed=VTA_GB300_LIB_DIR");
+}
+""")
+print("rust ok")

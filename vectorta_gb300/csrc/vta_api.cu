@@ -24,10 +24,15 @@
 namespace vta {
 
 static thread_local std::string g_err;
+// status of the last failure on this thread and, for VTA_ERR_OUT_OF_MEMORY,
+// its byte counts (required, free, headroom)
+static thread_local vta_status g_err_status = VTA_OK;
+static thread_local size_t g_oom[3] = {0, 0, 0};
 
 void set_error(const std::string& msg) { g_err = msg; }
 vta_status fail(vta_status st, const std::string& msg) {
     g_err = msg;
+    g_err_status = st;
     return st;
 }
 vta_status cuda_fail(cudaError_t e, const char* what) {
@@ -93,7 +98,11 @@ vta_status vram_check(size_t required) {
         char buf[160];
         std::snprintf(buf, sizeof buf, "out of memory: required=%zu free=%zu headroom=%zu", required, free_b,
                       headroom);
-        return fail(VTA_ERR_OUT_OF_MEMORY, buf);
+        const vta_status st = fail(VTA_ERR_OUT_OF_MEMORY, buf);
+        g_oom[0] = required;
+        g_oom[1] = free_b;
+        g_oom[2] = headroom;
+        return st;
     }
     return VTA_OK;
 }
@@ -1622,6 +1631,14 @@ using namespace vta;
 extern "C" {
 
 const char* vta_last_error(void) { return g_err.c_str(); }
+
+vta_status vta_last_error_oom(size_t* required, size_t* free_bytes, size_t* headroom) {
+    const bool oom = g_err_status == VTA_ERR_OUT_OF_MEMORY;
+    if (required) *required = oom ? g_oom[0] : 0;
+    if (free_bytes) *free_bytes = oom ? g_oom[1] : 0;
+    if (headroom) *headroom = oom ? g_oom[2] : 0;
+    return oom ? VTA_OK : VTA_ERR_INVALID_INPUT;
+}
 const char* vta_version(void) { return "vta_gb300 0.1.0 (sm_103a)"; }
 
 int vta_device_count(void) {
