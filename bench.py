@@ -152,6 +152,20 @@ def workload_wwma_family():
                        "sweeps": "CWMA/FWMA/SRWMA/SQWMA/VPWMA periods 5..260; EPMA periods 16..260 x offset 4"}}
 
 
+def workload_wma_long():
+    """Long weighted windows on the tensor cores: WMA periods 2..1000 (999
+    combos, tiles of K up to 1008, run as 256-wide K slices) on 1,000,000 bars
+    (seed 7): 4.0 GB of outputs per step."""
+    from vectorta_gb300 import datagen
+
+    n = 1_000_000
+    close = datagen.random_walk(n, seed=7, nan_lead=10)
+    return {"name": "wma_long", "n": n, "series": {"close": close.astype(np.float32)},
+            "jobs": [("wma", ["close"], {"period": (2, 1000, 1)})], "dominant": "wma",
+            "config": {"workload": "wma_long", "bars": n, "seed": 7, "nan_lead": 10, "combos": 999,
+                       "sweep": "WMA periods 2..1000"}}
+
+
 def workload_ema_small():
     """Profiling case: one EMA sweep (periods 2..1000) on 200,000 bars
     (0.8 GB of outputs: larger than L2, a few GB on the device at most)."""
@@ -261,7 +275,7 @@ def workload_served_stream():
 WORKLOADS = {"sweeps": workload_sweeps, "ragged_tm": workload_ragged_tm, "served_stream": workload_served_stream,
              "adx_sweep": workload_adx_sweep, "wwma_family": workload_wwma_family, "ragged_small": workload_ragged_small, "alma_grid": workload_alma_grid, "ema_small": workload_ema_small,
              "alma_small": workload_alma_small, "windows_small": workload_windows_small,
-             "recur_small": workload_recur_small}
+             "recur_small": workload_recur_small, "wma_long": workload_wma_long}
 
 
 # ------------------------------------------------------------- clocks -------
@@ -392,7 +406,7 @@ def cpu_sample(wl, budget_rows=None):
                 tasks.append((lambda p=p: O.alma_batch(s["close"], (p, p, 0), sweep["offset"], sweep["sigma"]),
                               wl["n"] * len(O.axis_f64(sweep["offset"])) * len(O.axis_f64(sweep["sigma"]))))
             continue
-        if name in ("cwma", "fwma", "srwma", "sqwma", "epma", "vpwma"):
+        if name in ("cwma", "fwma", "srwma", "sqwma", "epma", "vpwma", "wma"):
             fn = getattr(O, name)
             offs = (O.axis_usize(sweep["offset"], O.AX_SWAP) if name == "epma" else
                     O.axis_f64(sweep["power"]) if name == "vpwma" else [None])
@@ -989,7 +1003,8 @@ TRAFFIC = {
 KERNEL_NAME = {"recurrence_window_sweeps": "k_recur<OpEma, batch, EMIT>", "alma_grid": "k_wwma_tc<fp16x3>",
                "ema_small": "k_recur<OpEma, batch, EMIT>", "alma_small": "k_wwma_tc<fp16x3>",
                "adx_sweep": "k_hlc_chunk<adx> + fix-up", "wwma_family": "k_wwma_tc<fp16x3> (CWMA)",
-               "windows_small": "k_prefix_window_batch (StdDev)", "recur_small": "k_recur<OpEma, batch, EMIT>"}
+               "windows_small": "k_prefix_window_batch (StdDev)", "recur_small": "k_recur<OpEma, batch, EMIT>",
+               "wma_long": "k_wwma_tc<fp16x3> (K slices)"}
 
 
 def main():

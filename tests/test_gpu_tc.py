@@ -81,3 +81,58 @@ def test_tc_ragged_tail_and_nan(series):
     exp, _ = O.alma_batch(x.astype(np.float64), sweep["period"], sweep["offset"], sweep["sigma"])
     assert np.array_equal(np.isnan(got), np.isnan(exp))
     assert max_rel(got, exp) <= 1e-5
+
+
+@pytest.fixture(scope="module")
+def long_series():
+    return datagen.random_walk(100_000, seed=9, nan_lead=37).astype(np.float32)
+
+
+@pytest.mark.parametrize("variant,bound", [("auto", 1e-5), ("tc_bf16x3", 1e-4)])
+def test_long_windows_stay_on_tensor_cores(long_series, variant, bound):
+    """Windows longer than one shared-memory A tile (K > 272) run as K slices
+    accumulating in the same TMEM accumulator; the sweep mixes whole-tile and
+    sliced combo tiles.  WMA periods 2..1000 on 100,000 bars against the
+    oracle on every 7th row, every bar."""
+    ind = V.CudaWma(0)
+    ind.set_policy("wma_batch", variant)
+    rng = (2, 1000, 1)
+    got = ind.batch_dev(long_series, sweep={"period": rng}).to_host()
+    assert ind.last_kernel == ("wwma_tc_fp16x3" if variant == "auto" else f"wwma_{variant}")
+    ps = O.periods_of("wma", rng)
+    xd = long_series.astype(np.float64)
+    for r in range(0, len(ps), 7):
+        exp = O.wma(xd, ps[r])
+        assert np.array_equal(np.isnan(got[r]), np.isnan(exp)), ps[r]
+        assert max_rel(got[r], exp) <= bound, (ps[r], max_rel(got[r], exp))
+
+
+def test_long_alma_windows_every_row_sampled(long_series):
+    """ALMA periods 200..600 (401 combos, tiles of K up to 608) on 100,000
+    bars: every row against the oracle on a time sample (every 499th bar and
+    the first 2p bars after the warm-up)."""
+    ind = V.CudaAlma(0)
+    sweep = {"period": (200, 600, 1), "offset": (0.85, 0.85, 0.0), "sigma": (6.0, 6.0, 0.0)}
+    got = ind.alma_batch_dev(long_series, sweep=sweep).to_host()
+    assert ind.last_kernel == "wwma_tc_fp16x3"
+    xd = long_series.astype(np.float64)
+    first = int(np.argmax(~np.isnan(xd)))
+    for r, p in enumerate(range(200, 601)):
+        warm = first + p - 1
+        assert np.isnan(got[r][:warm]).all() and not np.isnan(got[r][warm:]).any(), p
+        idx = np.union1d(np.arange(warm, xd.size, 499), np.arange(warm, min(xd.size, warm + 2 * p)))
+        exp = O.alma_batch_row_at(xd, p, 0.85, 6.0, idx)
+        assert max_rel(got[r][idx], exp) <= 1e-5, (p, max_rel(got[r][idx], exp))
+
+
+def test_sliced_tiles_with_nan_and_ragged_tail(series):
+    x = series[:2999].copy()
+    x[:11] = np.nan
+    x[1500] = np.nan
+    sweep = {"period": (300, 420, 40), "offset": (0.85, 0.85, 0.0), "sigma": (6.0, 6.0, 0.0)}
+    ind = V.CudaAlma(0)
+    got = ind.alma_batch_dev(x, sweep=sweep).to_host()
+    assert ind.last_kernel == "wwma_tc_fp16x3"
+    exp, _ = O.alma_batch(x.astype(np.float64), sweep["period"], sweep["offset"], sweep["sigma"])
+    assert np.array_equal(np.isnan(got), np.isnan(exp))
+    assert max_rel(got, exp) <= 1e-5

@@ -57,7 +57,9 @@ constexpr int kM = 128;          // combos per tile (MMA M)
 constexpr int kN = 256;          // times per tile (MMA N)
 constexpr int kThreads = 288;     // warp 0: TMA + MMA issue; warps 1-8: epilogue
 constexpr int kEpiThreads = 256;
-constexpr int kMaxK = 272;       // largest tile K (period) the shared memory holds
+constexpr int kMaxK = 272;       // largest tile K whose whole A tile the shared memory holds
+constexpr int kSliceK = 256;     // K slice of a larger tile: its A slice and strip part are
+                                 // copied per (item, slice) and its MMAs accumulate in TMEM
 constexpr int kStripBufs = 3;    // strip buffers: copies for items i+1 and i+2 in flight during item i
 constexpr int kStageLd = 36;     // epilogue staging row stride (floats) of the st.global path
 constexpr int kStageTma = 32 * 32 * 4;  // epilogue staging per warp for a TMA store (bytes)
@@ -207,25 +209,27 @@ __global__ void __launch_bounds__(kPackThreads) k_pack_a(PackArgs a) {
     // row statistics, one warp per row (coalesced along the row): maximum
     // magnitude and the row sum as a compensated float pair (Neumaier; an f64
     // running sum is a chain of slow FP64 adds on GB300)
-    constexpr int kSlots = (kMaxK + 31) / 32;  // row elements per lane
+    constexpr int kSlots = (kMaxK + 31) / 32;  // row elements per lane per pass
     for (int r = warp; r < kM; r += kPackThreads / 32) {
         const int c = m * kM + r;
         float mx = 0.f, sum = 0.f, comp = 0.f;
         if (c < a.n_combos) {
             const float* row = a.w + (size_t)c * a.kmax;
-            // all of the lane's loads first (independent), then the sums
-            float v[kSlots];
+            for (int k0 = 0; k0 < K; k0 += 32 * kSlots) {
+                // all of the lane's loads first (independent), then the sums
+                float v[kSlots];
 #pragma unroll
-            for (int j = 0; j < kSlots; ++j) {
-                const int k = lane + 32 * j;
-                v[j] = (k < K && col0 + k >= 0) ? row[col0 + k] : 0.f;
-            }
+                for (int j = 0; j < kSlots; ++j) {
+                    const int k = k0 + lane + 32 * j;
+                    v[j] = (k < K && col0 + k >= 0) ? row[col0 + k] : 0.f;
+                }
 #pragma unroll
-            for (int j = 0; j < kSlots; ++j) {
-                mx = fmaxf(mx, fabsf(v[j]));
-                const float t = sum + v[j];
-                comp += fabsf(sum) >= fabsf(v[j]) ? (sum - t) + v[j] : (v[j] - t) + sum;
-                sum = t;
+                for (int j = 0; j < kSlots; ++j) {
+                    mx = fmaxf(mx, fabsf(v[j]));
+                    const float t = sum + v[j];
+                    comp += fabsf(sum) >= fabsf(v[j]) ? (sum - t) + v[j] : (v[j] - t) + sum;
+                    sum = t;
+                }
             }
         }
 #pragma unroll
@@ -387,7 +391,8 @@ struct TcArgs {
     const uint16_t* packed;
     const float* row_scale;
     const float* row_sum;
-    int kmax, jmax;
+    int kmax, jmax;       // the sweep's largest tile K and its strip blocks (global strips)
+    int ka, jcap;         // shared-memory capacities: A tile K and strip blocks per buffer
     const uint8_t* strips_hi;
     const uint8_t* strips_lo;
     const float* ref;
@@ -409,6 +414,7 @@ constexpr int kTraceTiles = 64;
 struct __align__(16) SmemCtl {
     uint64_t a_full;
     uint64_t strip_full[kStripBufs];
+    uint64_t unit_done[kStripBufs];  // MMAs of the (item, slice) unit using strip buffer u % kStripBufs
     uint64_t mma_done[2];
     uint64_t acc_empty[2];
     uint32_t tmem_base;
@@ -455,12 +461,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // layout (capacities for the largest tile K): A hi | A lo | strip[kStripBufs] hi |
     // strip[kStripBufs] lo | staging (1024-aligned) | ctl
-    const uint32_t strip_cap = (uint32_t)a.jmax * 128;
+    const uint32_t strip_cap = (uint32_t)a.jcap * 128;
     uint8_t* p = smem_raw;
     uint16_t* a_hi = reinterpret_cast<uint16_t*>(p);
-    p += (size_t)kM * a.kmax * 2;
+    p += (size_t)kM * a.ka * 2;
     uint16_t* a_lo = reinterpret_cast<uint16_t*>(p);
-    p += (size_t)kM * a.kmax * 2;
+    p += (size_t)kM * a.ka * 2;
     uint8_t* strip_hi[kStripBufs];
     uint8_t* strip_lo[kStripBufs];
     for (int j = 0; j < kStripBufs; ++j) strip_hi[j] = p + (size_t)j * strip_cap;
@@ -482,7 +488,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
 
     if (tid == 0) {
         mbar_init(&ctl->a_full, 1);
-        for (int b = 0; b < kStripBufs; ++b) mbar_init(&ctl->strip_full[b], 1);
+        for (int b = 0; b < kStripBufs; ++b) {
+            mbar_init(&ctl->strip_full[b], 1);
+            mbar_init(&ctl->unit_done[b], 1);
+        }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&ctl->mma_done[b], 1);
             mbar_init(&ctl->acc_empty[b], kEpiThreads);
@@ -505,97 +514,145 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
 
     if (tid == 0) {
         // ================= producer: TMA copies + MMA issue (one thread) ======
+        // The work of an item is one or more units (item, slice): a tile whose
+        // K fits the shared memory (K <= ka) is one unit and keeps its A tile
+        // resident across items; a larger tile is cut into K slices of
+        // kSliceK whose A slice and strip part are copied per unit and whose
+        // MMAs accumulate into the item's TMEM accumulator.  Strip buffers
+        // cycle per unit (copies for units u+1 and u+2 in flight during u).
         const uint32_t idesc = instr_desc(VARIANT);
-        // strip of item i: the Kmax strip of its time tile, entered 16 (Kmax - K) bytes in
-        auto copy_strip = [&](int i, const ItemIter& itm) {
-            const int bb = i % kStripBufs;
-            const int Ki = a.tile_k[itm.tile(a)];
-            const uint32_t sb = (uint32_t)(Ki / 8 + kN / 8 - 1) * 128;
-            const size_t g = (size_t)itm.time_tile(a) * a.jmax * 128 + (size_t)(a.kmax - Ki) * 16;
+        auto nslices = [&](int K) { return K <= a.ka ? 1 : (K + kSliceK - 1) / kSliceK; };
+        auto slice_k0 = [&](int K, int sl) { return K <= a.ka ? 0 : sl * kSliceK; };
+        auto slice_len = [&](int K, int sl) { return K <= a.ka ? K : min(kSliceK, K - sl * kSliceK); };
+        // a unit with its item's tile K and slice count read once per item
+        // (the producer is one thread: every global load sits on its path)
+        struct Unit {
+            ItemIter it;
+            int sl, mt, K, S;
+        };
+        auto unit_load = [&](Unit& un) {
+            if (un.it.q >= a.items) {  // past this CTA's last item: nothing to read
+                un.mt = -1;
+                un.K = 0;
+                un.S = 1;
+                return;
+            }
+            un.mt = un.it.tile(a);
+            un.K = a.tile_k[un.mt];
+            un.S = nslices(un.K);
+        };
+        auto unit_advance = [&](Unit& un) {
+            if (++un.sl >= un.S) {
+                un.sl = 0;
+                un.it.advance(a);
+                unit_load(un);
+            }
+        };
+        // strip part of unit u: the Kmax strip of its time tile, entered
+        // 16 (Kmax - K + k0) bytes in
+        auto copy_strip = [&](int u, const Unit& un) {
+            const int bb = u % kStripBufs;
+            const int Ki = un.K;
+            const int k0 = slice_k0(Ki, un.sl), ks = slice_len(Ki, un.sl);
+            const uint32_t sb = (uint32_t)(ks / 8 + kN / 8 - 1) * 128;
+            const size_t g = (size_t)un.it.time_tile(a) * a.jmax * 128 + (size_t)(a.kmax - Ki + k0) * 16;
             mbar_arrive_tx(&ctl->strip_full[bb], 2 * sb);
             bulk_g2s(strip_hi[bb], a.strips_hi + g, sb, &ctl->strip_full[bb]);
             bulk_g2s(strip_lo[bb], a.strips_lo + g, sb, &ctl->strip_full[bb]);
         };
         int a_mt = -1, a_loads = 0;
-        auto load_a = [&](int mt) {
+        bool a_pending = false;
+        // A of unit (tile mt, slice sl): the whole tile, or the slice's K range
+        auto load_a = [&](int mt, int sl) {
             const int Km = a.tile_k[mt];
-            const uint32_t abytes = (uint32_t)kM * Km * 2;
+            const int k0 = slice_k0(Km, sl), ks = slice_len(Km, sl);
+            const uint32_t abytes = (uint32_t)kM * ks * 2;
             const uint16_t* src = a.packed + a.tile_off[mt];
+            const size_t koff = (size_t)k0 * kM;  // core-matrix rows of k < k0 come first
             mbar_arrive_tx(&ctl->a_full, 2 * abytes);
-            bulk_g2s(a_hi, src, abytes, &ctl->a_full);
-            bulk_g2s(a_lo, src + (size_t)kM * Km, abytes, &ctl->a_full);
-            a_mt = mt;
+            bulk_g2s(a_hi, src + koff, abytes, &ctl->a_full);
+            bulk_g2s(a_lo, src + (size_t)kM * Km + koff, abytes, &ctl->a_full);
+            a_mt = nslices(Km) == 1 ? mt : -1;
+            a_pending = true;
         };
+        // (units are walked until the CTA's items run out: counting them up
+        // front cost the producer a serial pass over every item)
         bool ok = true;
-        ItemIter cur, nxt;  // nxt: the item whose strip is copied next
-        cur.start(a, blockIdx.x);
+        Unit cur, nxt;  // nxt: the unit whose strip is copied next
+        cur.it.start(a, blockIdx.x);
+        cur.sl = 0;
+        unit_load(cur);
         nxt = cur;
-        int copies = 0;  // strips requested (items 0 .. copies-1)
-        if (ntiles > 0) {
-            load_a(cur.tile(a));
-            for (; copies < 2 && copies < ntiles; ++copies, nxt.advance(a)) copy_strip(copies, nxt);
-            ok = mbar_wait(&ctl->a_full, 0, abort_flag);
-            a_loads = 1;
-        }
+        int copies = 0;  // strips requested (units 0 .. copies-1)
+        for (; copies < 2 && nxt.mt >= 0; ++copies, unit_advance(nxt)) copy_strip(copies, nxt);
         int consumed = 0;
-        for (int i = 0; ok && i < ntiles; ++i) {
+        int i = 0;  // item of the current unit
+        for (int u = 0; ok && cur.mt >= 0; ++u) {
             const int b = i & 1;
-            const int sbuf = i % kStripBufs;
-            const int mt = cur.tile(a);
-            ok = mbar_wait(&ctl->strip_full[sbuf], (i / kStripBufs) & 1, abort_flag);
-            if (ok) consumed = i + 1;
-            if (tracing && i < kTraceTiles) a.trace[i * TR_N + TR_P_STRIP] = now_ns();
-            if (ok && i >= 2) ok = mbar_wait(&ctl->acc_empty[b], ((i >> 1) - 1) & 1, abort_flag);
-            if (ok && mt != a_mt) {
-                // new combo tile: every MMA that reads the current A (tile i-1 and
-                // earlier) must have completed before A is overwritten
-                ok = mbar_wait(&ctl->mma_done[(i - 1) & 1], ((i - 1) >> 1) & 1, abort_flag);
+            const int sbuf = u % kStripBufs;
+            const int mt = cur.mt, K = cur.K, S = cur.S, sl = cur.sl;
+            ok = mbar_wait(&ctl->strip_full[sbuf], (u / kStripBufs) & 1, abort_flag);
+            if (ok) consumed = u + 1;
+            if (tracing && sl == 0 && i < kTraceTiles) a.trace[i * TR_N + TR_P_STRIP] = now_ns();
+            if (ok && sl == 0 && i >= 2) ok = mbar_wait(&ctl->acc_empty[b], ((i >> 1) - 1) & 1, abort_flag);
+            if (ok && (S > 1 || mt != a_mt)) {
+                // every MMA that reads the current A (unit u-1 and earlier)
+                // must have completed before A is overwritten
+                if (u >= 1)
+                    ok = mbar_wait(&ctl->unit_done[(u - 1) % kStripBufs], ((u - 1) / kStripBufs) & 1, abort_flag);
                 if (ok) {
-                    load_a(mt);
+                    load_a(mt, sl);
                     ok = mbar_wait(&ctl->a_full, a_loads & 1, abort_flag);
                     ++a_loads;
+                    if (ok) a_pending = false;
                 }
             }
             if (!ok) break;
-            if (tracing && i < kTraceTiles) a.trace[i * TR_N + TR_P_ACC] = now_ns();
-            const int K = a.tile_k[mt];
+            if (tracing && sl == 0 && i < kTraceTiles) a.trace[i * TR_N + TR_P_ACC] = now_ns();
+            const int ks = slice_len(K, sl);
             tc_fence_after();
             const uint32_t d = tmem + (uint32_t)(b * kN);
             const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
             const uint32_t bh = smem_u32(strip_hi[sbuf]), bl = smem_u32(strip_lo[sbuf]);
-            for (int ks = 0; ks < (K >> 4); ++ks) {
+            for (int kk = 0; kk < (ks >> 4); ++kk) {
                 // A: next 2 K-chunks (16 row groups * 128 B each); B: next 2 strip blocks
-                const uint32_t ao = (uint32_t)ks * 2 * 16 * 128, bo = (uint32_t)ks * 256;
+                const uint32_t ao = (uint32_t)kk * 2 * 16 * 128, bo = (uint32_t)kk * 256;
                 const uint64_t dah = smem_desc(ah + ao, 16 * 128, 128);
                 const uint64_t dal = smem_desc(al + ao, 16 * 128, 128);
                 const uint64_t dbh = smem_desc(bh + bo, 128, 128);
                 const uint64_t dbl = smem_desc(bl + bo, 128, 128);
-                tc_mma(d, dah, dbh, idesc, ks > 0 ? 1u : 0u);
+                tc_mma(d, dah, dbh, idesc, (sl > 0 || kk > 0) ? 1u : 0u);
                 tc_mma(d, dah, dbl, idesc, 1u);
                 tc_mma(d, dal, dbh, idesc, 1u);
             }
-            tc_commit(&ctl->mma_done[b]);
-            ctl->issued = i + 1;
-            if (tracing && i < kTraceTiles) a.trace[i * TR_N + TR_P_ISSUED] = now_ns();
-            // strip of item i + 2 into the buffer of item i - 1, once the MMAs
-            // of item i - 1 (its last reader) are done
-            cur.advance(a);
-            if (copies < ntiles) {
-                if (i >= 1) ok = mbar_wait(&ctl->mma_done[b ^ 1], ((i - 1) >> 1) & 1, abort_flag);
+            tc_commit(&ctl->unit_done[sbuf]);
+            if (sl == S - 1) {
+                tc_commit(&ctl->mma_done[b]);
+                ctl->issued = i + 1;
+                if (tracing && i < kTraceTiles) a.trace[i * TR_N + TR_P_ISSUED] = now_ns();
+                ++i;
+            }
+            unit_advance(cur);
+            // strip of unit u + 2 into the buffer of unit u - 1, once the MMAs
+            // of unit u - 1 (its last reader) are done
+            if (nxt.mt >= 0) {
+                if (u >= 1)
+                    ok = mbar_wait(&ctl->unit_done[(u - 1) % kStripBufs], ((u - 1) / kStripBufs) & 1, abort_flag);
                 if (ok) {
                     copy_strip(copies, nxt);
                     ++copies;
-                    nxt.advance(a);
+                    unit_advance(nxt);
                 }
             }
         }
         if (!ok) {
             ctl->abort_flag = 1;
-            // strip copies still in flight land in this CTA's shared memory:
-            // wait for them (bounded) before the CTA may exit
+            // copies still in flight land in this CTA's shared memory: wait
+            // for them (bounded) before the CTA may exit
             volatile int no_abort = 0;
             for (int j = consumed; j < copies; ++j)
                 mbar_wait(&ctl->strip_full[j % kStripBufs], (j / kStripBufs) & 1, &no_abort);
+            if (a_pending) mbar_wait(&ctl->a_full, a_loads & 1, &no_abort);
         }
     } else if (warp >= 1) {
         // ================= epilogue: warps 1-8 ================================
@@ -741,6 +798,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_wwma_tc(TcArgs a, const __grid_
     }
 }
 
+// Dynamic shared memory for an A capacity of K (whole tiles up to K; larger
+// tiles run in kSliceK slices).
 size_t smem_bytes_for(int K) {
     const int J = K / 8 + kN / 8 - 1;
     return (size_t)kM * K * 2 * 2 + 2 * kStripBufs * (size_t)J * 128 + 1024 + (size_t)8 * 32 * kStageLd * sizeof(float) +
@@ -760,13 +819,14 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
         int mx = 1;
         for (int r = 0; r < kM && mt * kM + r < a.n_combos; ++r) mx = std::max(mx, per[mt * kM + r]);
         const int K = (mx + 15) & ~15;
-        if (K > kMaxK) return fail(VTA_ERR_NOT_IMPLEMENTED, "tcgen05 path: period above the shared-memory limit");
         tk[mt] = K;
         toff[mt] = off;
         off += 2LL * kM * K;
         kbig = std::max(kbig, K);
     }
-    const size_t smem = std::max<size_t>(smem_bytes_for(kbig), 160 * 1024);
+    // A capacity: whole tiles up to kMaxK; larger tiles run in kSliceK slices
+    const int ka = std::min(kbig, kMaxK);
+    const size_t smem = std::max<size_t>(smem_bytes_for(ka), 160 * 1024);
     if (smem > ctx->smem_optin) return fail(VTA_ERR_NOT_IMPLEMENTED, "tcgen05 path: shared memory");
     const int n_time_tiles = (a.n + kN - 1) / kN;
     const int jmax = kbig / 8 + kN / 8 - 1;
@@ -806,8 +866,14 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
     StripArgs sa{a.x, a.n, a.first, kbig, jmax, d_sh, d_sl, d_ref, d_xs};
     const int L = jmax * 8 + 8;
     const size_t ssmem = (size_t)L * 4 + 2 * (size_t)((L + 7) & ~7) * 2 + 64;
-    if (variant == 1) k_hankel_strips<1><<<n_time_tiles, 128, ssmem, st>>>(sa);
-    else k_hankel_strips<0><<<n_time_tiles, 128, ssmem, st>>>(sa);
+    if (ssmem > ctx->smem_optin) return fail(VTA_ERR_NOT_IMPLEMENTED, "tcgen05 path: period above the strip limit");
+    if (variant == 1) {
+        VTA_CUDA_TRY(cudaFuncSetAttribute(k_hankel_strips<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssmem));
+        k_hankel_strips<1><<<n_time_tiles, 128, ssmem, st>>>(sa);
+    } else {
+        VTA_CUDA_TRY(cudaFuncSetAttribute(k_hankel_strips<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssmem));
+        k_hankel_strips<0><<<n_time_tiles, 128, ssmem, st>>>(sa);
+    }
     VTA_TRY(check_launch("k_hankel_strips"));
 
     TcArgs t{};
@@ -822,6 +888,8 @@ vta_status launch_wwma_batch_tc(const WwmaBatchArgs& a, int variant, vta_ctx* ct
     t.row_sum = d_rsum;
     t.kmax = kbig;
     t.jmax = jmax;
+    t.ka = ka;
+    t.jcap = ka / 8 + kN / 8 - 1;
     t.strips_hi = d_sh;
     t.strips_lo = d_sl;
     t.ref = d_ref;
