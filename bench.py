@@ -474,6 +474,7 @@ def gpu_bench(args, wl):
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)  # events below and the calls share one stream
     ctx.set_policy("timing", "on")
+    ctx.set_policy("tune", args.tune)
     inds = {name: V.CLASSES[name](0, ctx=ctx) for name, _, _ in wl["jobs"]}
     d_series = {k: torch.from_numpy(v).to(dev) for k, v in wl["series"].items()}
     firsts = {}
@@ -491,6 +492,7 @@ def gpu_bench(args, wl):
 
     kernel_ms = {nm: [] for nm in rows}
     call_ev = {nm: [] for nm in rows}
+    kernel_names = {}
 
     def step(record=False):
         for name, ins, sweep in wl["jobs"]:
@@ -498,6 +500,8 @@ def gpu_bench(args, wl):
                 ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                 ev[0].record(stream)
             inds[name].batch_device([d_series[k] for k in ins], n, firsts[name], sweep, outs[name])
+            if not record:  # (warm-up steps) the path each call took
+                kernel_names[name] = ctx.last_kernel
             if record:
                 ev[1].record(stream)
                 call_ev[name].append(ev)
@@ -537,7 +541,7 @@ def gpu_bench(args, wl):
     for name, ins, _ in wl["jobs"]:
         b = rows[name] * n * 4 * len(outs[name]) + sum(wl["series"][k].nbytes for k in ins)
         calls[name] = {"call_ms": call_ms[name], "kernel_ms": share[name], "bytes": b,
-                       "call_frac": b / (call_ms[name] / 1e3) / 1e9 / hbm}
+                       "call_frac": b / (call_ms[name] / 1e3) / 1e9 / hbm, "kernel": kernel_names.get(name)}
 
     # e2e through the host-in / host-out C-ABI calls, pinned host buffers
     e2e = None
@@ -1020,6 +1024,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="default workload: skip the ALMA-grid and served-stream figures")
     ap.add_argument("--no-err", action="store_true", help="skip the error measurement against the oracle")
+    ap.add_argument("--tune", default="on", choices=["on", "off", "cached"],
+                    help="batch-sweep autotuner policy (off: untuned defaults, e.g. for profiling)")
     ap.add_argument("--slots", type=int, default=8, help="served_stream: concurrent server slots")
     args = ap.parse_args()
 

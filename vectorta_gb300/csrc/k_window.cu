@@ -499,8 +499,8 @@ constexpr int kMmThreads = 512;
 
 // Outputs of a clean tile (every window past its warm-up is valid): combo-
 // outer, so a combo's table offsets are read once for the thread's PER times
-// t = t0 + tid + k * kMmThreads; the closes are read once for all combos.
-template <int KIND, int PER>
+// t = t0 + tid + k * THREADS; the closes are read once for all combos.
+template <int KIND, int PER, int THREADS>
 __device__ __forceinline__ void minmax_clean(const MinMaxArgs& a, const float* mx, const float* mn,
                                              const int4* ctab, int t0, int tile) {
     const int tid = threadIdx.x;
@@ -508,7 +508,7 @@ __device__ __forceinline__ void minmax_clean(const MinMaxArgs& a, const float* m
     float cl[PER];
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-        const int t = t0 + tid + k * kMmThreads;
+        const int t = t0 + tid + k * THREADS;
         cl[k] = (KIND == MM_WILLR && t < a.n) ? __ldg(a.c + t) : 0.f;
     }
     const int ie0 = tid + a.pmax - 1;  // local index of t0 + tid
@@ -523,12 +523,12 @@ __device__ __forceinline__ void minmax_clean(const MinMaxArgs& a, const float* m
         const bool all_valid = full && t0 >= ct.y;
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
-            const int t = t0 + tid + k * kMmThreads;
+            const int t = t0 + tid + k * THREADS;
             if (!all_valid && t >= a.n) break;
             float v0 = qnan(), v1 = qnan(), v2 = qnan();
             if (all_valid || t >= ct.y) {
-                const float hmax = fmaxf(mz[k * kMmThreads], mw[k * kMmThreads]);
-                const float lmin = fminf(nz[k * kMmThreads], nw[k * kMmThreads]);
+                const float hmax = fmaxf(mz[k * THREADS], mw[k * THREADS]);
+                const float lmin = fminf(nz[k * THREADS], nw[k * THREADS]);
                 if (KIND == MM_DONCHIAN) {
                     v0 = hmax;
                     v2 = lmin;
@@ -540,16 +540,20 @@ __device__ __forceinline__ void minmax_clean(const MinMaxArgs& a, const float* m
                     v0 = den == 0.f ? 0.f : fmaf(-100.f, __fdividef(hmax - cl[k], den), 0.f);
                 }
             }
-            r0[k * kMmThreads] = v0;
+            r0[k * THREADS] = v0;
             if (KIND == MM_DONCHIAN) {
-                a.out1[o + k * kMmThreads] = v1;
-                a.out2[o + k * kMmThreads] = v2;
+                a.out1[o + k * THREADS] = v1;
+                a.out2[o + k * THREADS] = v2;
             }
         }
     }
 }
 
-__global__ void __launch_bounds__(kMmThreads)
+// THREADS threads per block (the autotuner's choice with the tile): fewer
+// threads give each more times per combo, which spreads the combo's table and
+// pointer set-up over more outputs.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS)
 k_minmax_batch(MinMaxArgs a, int tile, int levels) {
     extern __shared__ float sm[];
     const int t0 = blockIdx.x * tile;
@@ -623,16 +627,18 @@ k_minmax_batch(MinMaxArgs a, int tile, int levels) {
         }
     }
     __syncthreads();
-    if (clean && tile >= kMmThreads) {
-        const int per = tile / kMmThreads;  // 1, 2 or 4: the launcher's tiles are 256..2048
+    if (clean && tile >= THREADS && tile <= 8 * THREADS) {
+        const int per = tile / THREADS;  // 1, 2, 4 or 8
         if (a.kind == MM_DONCHIAN) {
-            if (per == 1) minmax_clean<MM_DONCHIAN, 1>(a, mx, mn, ctab, t0, tile);
-            else if (per == 2) minmax_clean<MM_DONCHIAN, 2>(a, mx, mn, ctab, t0, tile);
-            else minmax_clean<MM_DONCHIAN, 4>(a, mx, mn, ctab, t0, tile);
+            if (per == 1) minmax_clean<MM_DONCHIAN, 1, THREADS>(a, mx, mn, ctab, t0, tile);
+            else if (per == 2) minmax_clean<MM_DONCHIAN, 2, THREADS>(a, mx, mn, ctab, t0, tile);
+            else if (per == 4) minmax_clean<MM_DONCHIAN, 4, THREADS>(a, mx, mn, ctab, t0, tile);
+            else minmax_clean<MM_DONCHIAN, 8, THREADS>(a, mx, mn, ctab, t0, tile);
         } else {
-            if (per == 1) minmax_clean<MM_WILLR, 1>(a, mx, mn, ctab, t0, tile);
-            else if (per == 2) minmax_clean<MM_WILLR, 2>(a, mx, mn, ctab, t0, tile);
-            else minmax_clean<MM_WILLR, 4>(a, mx, mn, ctab, t0, tile);
+            if (per == 1) minmax_clean<MM_WILLR, 1, THREADS>(a, mx, mn, ctab, t0, tile);
+            else if (per == 2) minmax_clean<MM_WILLR, 2, THREADS>(a, mx, mn, ctab, t0, tile);
+            else if (per == 4) minmax_clean<MM_WILLR, 4, THREADS>(a, mx, mn, ctab, t0, tile);
+            else minmax_clean<MM_WILLR, 8, THREADS>(a, mx, mn, ctab, t0, tile);
         }
         return;
     }
@@ -867,25 +873,31 @@ static size_t minmax_smem(const MinMaxArgs& a, int tile, int levels) {
     return nloc * levels * 2 * sizeof(float) + (2 * (nloc + 1) + 4) * sizeof(int) + (size_t)a.n_combos * sizeof(int4);
 }
 
+// Candidates encoded as tile | threads << 16.
 std::vector<int> minmax_tile_candidates(const MinMaxArgs& a, size_t smem_optin) {
     const int levels = 32 - __builtin_clz((unsigned)a.pmax);
     std::vector<int> c;
-    for (int tile : {512, 1024})
-        if (minmax_smem(a, tile, levels) <= smem_optin && (size_t)a.n >= (size_t)tile * 2 * kNumSMs) c.push_back(tile);
+    const int cfg[][2] = {{512, 512}, {512, 256}, {512, 128}, {1024, 512}, {1024, 256}};
+    for (const auto& tc : cfg)
+        if (minmax_smem(a, tc[0], levels) <= smem_optin && (size_t)a.n >= (size_t)tc[0] * 2 * kNumSMs)
+            c.push_back(tc[0] | (tc[1] << 16));
     return c.size() > 1 ? c : std::vector<int>{};
 }
 
 vta_status launch_minmax_batch(const MinMaxArgs& a, size_t smem_optin, cudaStream_t st) {
     const int levels = 32 - __builtin_clz((unsigned)a.pmax);  // floor(log2 pmax) + 1
+    const int hint_tile = a.tile_hint & 0xffff, hint_threads = a.tile_hint >> 16;
     for (int tile = 2048; tile >= 256; tile >>= 1) {
         const size_t bytes = minmax_smem(a, tile, levels);
-        const bool pick = a.tile_hint > 0 ? tile == a.tile_hint
-                                          : (tile <= 512 || (size_t)a.n >= (size_t)tile * 8 * kNumSMs);
+        const bool pick = hint_tile > 0 ? tile == hint_tile
+                                        : (tile <= 512 || (size_t)a.n >= (size_t)tile * 8 * kNumSMs);
         if (bytes <= smem_optin && pick) {
-            VTA_CUDA_TRY(cudaFuncSetAttribute(k_minmax_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)bytes));
+            const int threads = hint_threads == 128 ? 128 : hint_threads == 256 ? 256 : kMmThreads;
+            auto kern = threads == 128 ? k_minmax_batch<128> : threads == 256 ? k_minmax_batch<256>
+                                                                               : k_minmax_batch<kMmThreads>;
+            VTA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
             ktimer_begin(st);
-            k_minmax_batch<<<ceil_div(a.n, tile), kMmThreads, bytes, st>>>(a, tile, levels);
+            kern<<<ceil_div(a.n, tile), threads, bytes, st>>>(a, tile, levels);
             ktimer_end(st);
             return check_launch("k_minmax_batch");
         }

@@ -434,16 +434,20 @@ static vta_status tuned_launch(vta_ctx* ctx, int ind, long long n, long long com
     float best = 1e30f;
     int best_v = dflt;
     vta_status s = VTA_OK;
+    // each candidate runs twice and keeps its faster time (the first launch
+    // of a kernel variant pays one-time costs that say nothing of its speed)
     for (size_t i = 0; i < cand.size() && s == VTA_OK; ++i) {
-        cudaEventRecord(e0, st);
-        s = launch(cand[i]);
-        cudaEventRecord(e1, st);
-        if (s == VTA_OK && cudaStreamSynchronize(st) != cudaSuccess) s = check_launch("sweep tuning");
-        float ms = 0.f;
-        if (s == VTA_OK) cudaEventElapsedTime(&ms, e0, e1);
-        if (s == VTA_OK && ms < best) {
-            best = ms;
-            best_v = cand[i];
+        for (int rep = 0; rep < 2 && s == VTA_OK; ++rep) {
+            cudaEventRecord(e0, st);
+            s = launch(cand[i]);
+            cudaEventRecord(e1, st);
+            if (s == VTA_OK && cudaStreamSynchronize(st) != cudaSuccess) s = check_launch("sweep tuning");
+            float ms = 0.f;
+            if (s == VTA_OK) cudaEventElapsedTime(&ms, e0, e1);
+            if (s == VTA_OK && ms < best) {
+                best = ms;
+                best_v = cand[i];
+            }
         }
     }
     cudaEventDestroy(e0);
@@ -914,7 +918,10 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             };
             VTA_TRY(tuned_launch(ctx, (int)ind, n, nc, TK_MINMAX, minmax_tile_candidates(a, ctx->smem_optin), 0,
                                  launch, &tile, &tag));
-            ctx->last_kernel = std::string("minmax_sparse_table(tile=") + (tile ? std::to_string(tile) : "auto") +
+            ctx->last_kernel = std::string("minmax_sparse_table(") +
+                               (tile ? "tile=" + std::to_string(tile & 0xffff) + ", threads=" +
+                                           std::to_string(tile >> 16 ? tile >> 16 : 512)
+                                     : std::string("tile=auto")) +
                                ", " + tag + ")";
             return VTA_OK;
         }
