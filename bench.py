@@ -471,10 +471,15 @@ def gpu_bench(args, wl):
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     ctx = V.Context(0)
-    stream = torch.cuda.current_stream()
-    ctx.set_stream(stream.cuda_stream)  # events below and the calls share one stream
+    # one dedicated stream for torch's work, the library's calls and the
+    # events (torch's default stream is the legacy NULL stream, which a
+    # context given handle 0 would replace with a stream of its own)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
     ctx.set_policy("timing", "on")
     ctx.set_policy("tune", args.tune)
+    ctx.set_policy("recur_agg", args.recur_agg)
     inds = {name: V.CLASSES[name](0, ctx=ctx) for name, _, _ in wl["jobs"]}
     d_series = {k: torch.from_numpy(v).to(dev) for k, v in wl["series"].items()}
     firsts = {}
@@ -494,6 +499,9 @@ def gpu_bench(args, wl):
     call_ev = {nm: [] for nm in rows}
     kernel_names = {}
 
+    # The device entry points return once their work is queued (like the
+    # crate's x_batch_device), so the timed steps run back to back on the
+    # stream with no host wait between calls.
     def step(record=False):
         for name, ins, sweep in wl["jobs"]:
             if record:
@@ -505,7 +513,6 @@ def gpu_bench(args, wl):
             if record:
                 ev[1].record(stream)
                 call_ev[name].append(ev)
-                kernel_ms[name].append(ctx.kernel_ms)
 
     for _ in range(args.warmup):
         step()
@@ -525,6 +532,13 @@ def gpu_bench(args, wl):
     ms = e0.elapsed_time(e1)
     ms_per_step = ms / args.steps
     value = out_per_step / (ms_per_step / 1e3)
+    # the dominant kernel of each call (the library's events around it): one
+    # call at a time after the timed steps, each read once its call is done
+    for _ in range(min(args.steps, 5)):
+        for name, ins, sweep in wl["jobs"]:
+            inds[name].batch_device([d_series[k] for k in ins], n, firsts[name], sweep, outs[name])
+            ctx.synchronize()
+            kernel_ms[name].append(ctx.kernel_ms)
 
     # roofline of the dominant kernel: algorithmic bytes per launch / event-timed duration
     dom = wl["dominant"]
@@ -575,7 +589,8 @@ def gpu_bench_plan(args, wl):
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     ctx = V.Context(0)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream(device=dev)  # as in gpu_bench: one dedicated stream
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     ctx.set_policy("timing", "on")
     tm, lens = wl["tm"], wl["lens"]
@@ -832,6 +847,7 @@ def gpu_bench_server(args, wl):
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         inds[r["name"]].batch_device(ins, n, int(leads[r["series"]]), r["sweep"], outs_t)
+        inds[r["name"]].synchronize()
         p_t += time.perf_counter() - t1
         p_out += r["outputs"]
         del outs_t
@@ -1027,6 +1043,9 @@ def main():
     ap.add_argument("--tune", default="on", choices=["on", "off", "cached"],
                     help="batch-sweep autotuner policy (off: untuned defaults, e.g. for profiling)")
     ap.add_argument("--slots", type=int, default=8, help="served_stream: concurrent server slots")
+    ap.add_argument("--recur-agg", default="auto", choices=["auto", "cuda", "tc"],
+                    help="chunk aggregates of the EMA/DEMA/TEMA/RSI sweeps: tensor cores where eligible "
+                         "(auto), CUDA cores only, or tensor cores required")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))

@@ -17,8 +17,15 @@
  *     inputs and write into caller-provided device outputs (the crate's
  *     x_batch_device / x_many_series_one_param_device); *_into_host_f32
  *     writes host outputs (the crate's x_batch_into_host_f32);
- *   - every call is stream-ordered on the context's stream and synchronous on
- *     return, like the crate's wrappers (which end with stream.synchronize()).
+ *   - every call is stream-ordered on the context's stream.  Calls that take
+ *     host data or return host results wait for their work before returning,
+ *     like the crate's x_batch_dev / *_into_host_f32 (which end with
+ *     stream.synchronize()); the device-pointer entry points that write into
+ *     caller device buffers (*_batch_device, *_many_series_one_param_device)
+ *     return once their work is queued, like the crate's x_batch_device /
+ *     x_many_series_one_param_device: read their outputs after
+ *     vta_ctx_synchronize (CudaX::synchronize) or from work queued behind them
+ *     on the same stream.
  * Thread safety: a vta_ctx is used by one thread at a time (as a CudaX is).
  */
 #ifndef VTA_GB300_H

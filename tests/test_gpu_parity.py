@@ -173,6 +173,7 @@ def test_batch_entry_points_agree(name, data):
     first = V.N.INDICATORS[name][0]
     fv = int(np.argmax(~np.isnan(np.stack(ins)).any(axis=0))) if first != "x" else int(np.argmax(~np.isnan(ins[0])))
     ind.batch_device(d_in, cols, fv, sweep, d_out)
+    ind.synchronize()  # device entry points return once queued, like the crate's x_batch_device
     for k in range(len(a)):
         ah = a[k].to_host()
         assert np.array_equal(ah, h[k], equal_nan=True)
@@ -282,6 +283,7 @@ def test_many_series_device_entry_agrees(name):
     d_out = [torch.empty(c.shape, device="cuda") for _ in a]
     torch.cuda.synchronize()
     ind.many_series_one_param_device(d_in, c.shape[1], c.shape[0], PARAMS[name], d_out)
+    ind.synchronize()
     for k in range(len(a)):
         assert np.array_equal(a[k].to_host(), d_out[k].cpu().numpy(), equal_nan=True)
 

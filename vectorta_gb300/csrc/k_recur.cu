@@ -643,16 +643,20 @@ struct CascadeBlock {
         c1 = al * (float)kAggBlk * pw;
         c2 = al * al * pw * (float)(kAggBlk * (kAggBlk + 1) / 2);
     }
-    // one block of inputs x[0..B) (shared-memory broadcast reads)
+    // one block of inputs x[0..B) (shared-memory broadcast reads, x 16-byte
+    // aligned) advancing the first M components (the cascade's later stages
+    // not yet started stay as they are)
+    template <int M = NZ>
     __device__ __forceinline__ void step(float (&z)[NZ], const float* x) const {
-        float d[NZ][2];
+        static_assert(M >= 1 && M <= NZ, "components");
+        float d[M][2];
 #pragma unroll
-        for (int q = 0; q < NZ; ++q) d[q][0] = d[q][1] = 0.f;
+        for (int q = 0; q < M; ++q) d[q][0] = d[q][1] = 0.f;
 #pragma unroll
         for (int j = 0; j < kAggBlk; j += 4) {
             const float4 v = *reinterpret_cast<const float4*>(x + j);
 #pragma unroll
-            for (int q = 0; q < NZ; ++q) {
+            for (int q = 0; q < M; ++q) {
                 d[q][0] = fmaf(w[q][j], v.x, d[q][0]);
                 d[q][1] = fmaf(w[q][j + 1], v.y, d[q][1]);
                 d[q][0] = fmaf(w[q][j + 2], v.z, d[q][0]);
@@ -661,14 +665,28 @@ struct CascadeBlock {
         }
         const float e1 = z[0];
         z[0] = e1 + fmaf(-W[0], e1, d[0][0] + d[0][1]);
-        if constexpr (NZ > 1) {
+        if constexpr (M > 1) {
             const float e2 = z[1];
             z[1] = fmaf(c1, e1 - e2, e2) + fmaf(-W[1], e2, d[1][0] + d[1][1]);
-            if constexpr (NZ > 2) {
+            if constexpr (M > 2) {
                 const float e3 = z[2];
                 z[2] = fmaf(c1, e2 - e3, fmaf(c2, e1 - e3, e3)) + fmaf(-W[2], e3, d[2][0] + d[2][1]);
             }
         }
+    }
+    // steps t in [t0, t1) of the first M components: single gain-exact steps
+    // up to a 4-aligned index, blocks of kAggBlk, single steps for the rest
+    template <int M>
+    __device__ __forceinline__ void run(float (&z)[NZ], const float* xs, int t0, int t1, float al) const {
+        auto one = [&](float x) {
+            z[0] = fmaf(al, x - z[0], z[0]);
+            if constexpr (M > 1) z[1] = fmaf(al, z[0] - z[1], z[1]);
+            if constexpr (M > 2) z[2] = fmaf(al, z[1] - z[2], z[2]);
+        };
+        int t = t0;
+        for (; t < t1 && (t & 3); ++t) one(xs[t]);
+        for (; t + kAggBlk <= t1; t += kAggBlk) step<M>(z, xs + t);
+        for (; t < t1; ++t) one(xs[t]);
     }
 };
 
@@ -750,6 +768,29 @@ __device__ bool agg_fast_block(const RecurArgs& a, int chunk, int c0, int c1, fl
     return true;
 }
 
+// AGG record of a chunk from the tensor-core contraction's S partial sums
+// (k_recur_tc.cu): per component the sum of the partials, times the row and
+// column scales, plus the centring term.  One thread per lane.
+template <int K>
+__device__ void agg_from_partials(const RecurArgs& a, int chunk, int len) {
+    constexpr int NZ = K == FK_EMA ? 1 : (K == FK_TEMA ? 3 : 2);
+    const RecurTcView& v = a.tc;
+    const int li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= a.n_lanes) return;
+    const int j0 = chunk - v.g0;
+    float z[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < NZ; ++q) {
+        const int r = K == FK_RSI ? li : q * v.mpad + li;
+        const int j = K == FK_RSI ? j0 + q * v.nc : j0;
+        const float* p = v.part + (size_t)j * v.rows + r;
+        float acc = 0.f;
+        for (int s = 0; s < v.S; ++s) acc += __ldg(p + (size_t)s * v.npad * v.rows);
+        z[q] = fmaf(acc, __ldg(v.row_scale + r) * __ldg(v.col_scale + j), __ldg(v.col_ref + j) * __ldg(v.row_sum + r));
+    }
+    reinterpret_cast<float4*>(a.agg)[(size_t)chunk * a.n_lanes + li] = make_float4(z[0], z[1], z[2], (float)len);
+}
+
 // ------------------------------------------------------ seed chunk, AGG ---
 // The AGG pass needs only the state at the end of the seed chunk [0, c1).
 // When every input in [first, c1) is finite and every lane's seed index lies
@@ -758,8 +799,56 @@ __device__ bool agg_fast_block(const RecurArgs& a, int chunk, int c0, int c1, fl
 // (a short dependency chain), then the running steps from the seed on.  The
 // per-step phase logic made each lane's 1,000-2,000-step walk the critical
 // path of the whole AGG launch.
+// Pair sum of two (hi, lo) compensated values (TwoSum of the heads).
+__device__ __forceinline__ float2 pair_add(float2 a, float2 b) {
+    const float s = a.x + b.x;
+    const float bb = s - a.x;
+    const float e = (a.x - (s - bb)) + (b.x - bb);
+    const float lo = a.y + b.y + e;
+    const float hi = s + lo;
+    return make_float2(hi, lo - (hi - s));
+}
+
+// Block-wide sums of the seed chunk's warm-up terms in 32-step segments:
+// segment i covers [b0 + 32 i, b0 + 32 i + 32) ∩ [b0, c1) and holds, as
+// compensated (hi, lo) pairs, the sum of x (EMA: b0 = first) or of the
+// exact gains and losses (RSI: b0 = first + 1; the differences to the
+// previous bar).  A lane's warm-up sum over p terms from b0 is then p / 32
+// segment sums plus at most 31 single terms, instead of a p-step chain.
+// seg: float4 {sum hi, sum lo, loss hi, loss lo} per segment.  Called by the
+// whole block; every input in [b0 - 1, c1) is finite.
 template <int K>
-__device__ bool agg_seed_fast(const RecurArgs& a, const float* xs, int c1) {
+__device__ void seed_segments(const float* xs, int b0, int c1, float4* seg) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nseg = (c1 - b0 + 31) >> 5;
+    for (int i = warp; i < nseg; i += nw) {
+        const int t = b0 + 32 * i + lane;
+        float2 u = make_float2(0.f, 0.f), v = make_float2(0.f, 0.f);
+        if (t < c1) {
+            if constexpr (K == FK_RSI) {
+                const float x1 = xs[t], x0 = xs[t - 1];
+                const float d = x1 - x0;  // exact difference d + e (TwoDiff)
+                const float bb = d - x1;
+                const float e = (x1 - (d - bb)) - (x0 + bb);
+                if (d > 0.f) u = make_float2(d, e);
+                else if (d < 0.f) v = make_float2(-d, -e);
+            } else {
+                u = make_float2(xs[t], 0.f);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            u = pair_add(u, make_float2(__shfl_xor_sync(0xffffffffu, u.x, o), __shfl_xor_sync(0xffffffffu, u.y, o)));
+            if constexpr (K == FK_RSI)
+                v = pair_add(v, make_float2(__shfl_xor_sync(0xffffffffu, v.x, o),
+                                            __shfl_xor_sync(0xffffffffu, v.y, o)));
+        }
+        if (lane == 0) seg[i] = make_float4(u.x, u.y, v.x, v.y);
+    }
+}
+
+template <int K>
+__device__ bool agg_seed_fast(const RecurArgs& a, float* xs, int c1, int cap) {
     const int f = a.first;
     const int li = blockIdx.x * blockDim.x + threadIdx.x;
     const bool lane_ok = li < a.n_lanes;
@@ -769,6 +858,15 @@ __device__ bool agg_seed_fast(const RecurArgs& a, const float* xs, int c1) {
     int bad = lane_ok && (p <= 0 || s >= c1);
     for (int t = max(f, 0) + threadIdx.x; t < c1; t += blockDim.x) bad |= !isfinite(xs[t]);
     if (__syncthreads_or(bad)) return false;
+    // segment sums of the warm-up terms (EMA, RSI) when they fit beside xs
+    const int b0 = K == FK_RSI ? f + 1 : f;
+    const int seg_off = (c1 + 3) & ~3;
+    const bool use_seg = K != FK_TEMA && f >= 0 && seg_off + 4 * ((c1 - b0 + 31) >> 5) <= cap;
+    float4* seg = reinterpret_cast<float4*>(xs + seg_off);
+    if (use_seg) {
+        seed_segments<K>(xs, b0, c1, seg);
+        __syncthreads();
+    }
     if (!lane_ok) return true;
     float4 g = make_float4(0.f, 0.f, 0.f, kAbsolute);
     if constexpr (K == FK_EMA) {
@@ -777,6 +875,15 @@ __device__ bool agg_seed_fast(const RecurArgs& a, const float* xs, int c1) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[q].zero();
         int t = f;
+        if (use_seg) {
+            const int full = p >> 5;
+            for (int i = 0; i < full; ++i) {
+                const float4 sv = seg[i];
+                acc[i & 1].add(sv.x);
+                acc[i & 1].lo += sv.y;
+            }
+            t = f + 32 * full;
+        }
         for (; t + 3 <= s; t += 4)
 #pragma unroll
             for (int q = 0; q < 4; ++q) acc[q].add(xs[t + q]);
@@ -785,9 +892,11 @@ __device__ bool agg_seed_fast(const RecurArgs& a, const float* xs, int c1) {
         acc[2].add(acc[3].hi); acc[2].add(acc[3].lo);
         acc[0].add(acc[2].hi); acc[0].add(acc[2].lo);
         const float al = (float)(2.0 / ((double)p + 1.0));
-        float y = acc[0].f() / (float)p;
-        for (t = s + 1; t < c1; ++t) y = fmaf(al, xs[t] - y, y);
-        g.x = y;
+        CascadeBlock<1> cb;
+        cb.init(al);
+        float y[1] = {acc[0].f() / (float)p};
+        cb.run<1>(y, xs, s + 1, c1, al);  // the running steps, kAggBlk at a time
+        g.x = y[0];
     } else if constexpr (K == FK_RSI) {
         // sums of the gains and losses of the p deltas in (f, s], then the
         // Wilder steps (the op's seed() and step() arithmetic)
@@ -795,6 +904,17 @@ __device__ bool agg_seed_fast(const RecurArgs& a, const float* xs, int c1) {
 #pragma unroll
         for (int q = 0; q < 2; ++q) { sg[q].zero(); sl[q].zero(); }
         int t = f + 1;
+        if (use_seg) {
+            const int full = p >> 5;
+            for (int i = 0; i < full; ++i) {
+                const float4 sv = seg[i];
+                sg[i & 1].add(sv.x);
+                sg[i & 1].lo += sv.y;
+                sl[i & 1].add(sv.z);
+                sl[i & 1].lo += sv.w;
+            }
+            t = f + 1 + 32 * full;
+        }
         for (; t + 1 <= s; t += 2)
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
@@ -826,24 +946,19 @@ __device__ bool agg_seed_fast(const RecurArgs& a, const float* xs, int c1) {
         if (p == 1) {
             g.x = xs[c1 - 1];
         } else {
+            // the three phases kAggBlk steps at a time (CascadeBlock)
             const int start2 = f + p - 1;
-            float e1 = xs[f], e2, e3;
-            int t = f + 1;
-            for (; t <= start2; ++t) e1 = fmaf(per, xs[t] - e1, e1);
-            e2 = e1;
-            for (; t <= s; ++t) {
-                e1 = fmaf(per, xs[t] - e1, e1);
-                e2 = fmaf(per, e1 - e2, e2);
-            }
-            e3 = e2;
-            for (; t < c1; ++t) {
-                e1 = fmaf(per, xs[t] - e1, e1);
-                e2 = fmaf(per, e1 - e2, e2);
-                e3 = fmaf(per, e2 - e3, e3);
-            }
-            g.x = e1;
-            g.y = e2;
-            g.z = e3;
+            CascadeBlock<3> cb;
+            cb.init(per);
+            float z[3] = {xs[f], 0.f, 0.f};
+            cb.run<1>(z, xs, f + 1, start2 + 1, per);
+            z[1] = z[0];
+            cb.run<2>(z, xs, start2 + 1, s + 1, per);
+            z[2] = z[1];
+            cb.run<3>(z, xs, s + 1, c1, per);
+            g.x = z[0];
+            g.y = z[1];
+            g.z = z[2];
         }
     }
     reinterpret_cast<float4*>(a.agg)[li] = g;  // chunk 0
@@ -920,6 +1035,12 @@ k_recur(RecurArgs a) {
     recur_chunk_bounds(a, chunk, c0, c1);
     if (c0 >= a.n) return;
     if constexpr (PASS == PASS_AGG && !TM && FastKindOf<Op>::k != FK_NONE) {
+        // chunks the tensor-core contraction covered: sum its partials
+        const RecurTcView& v = a.tc;
+        if (v.done && chunk >= v.g0 && chunk < v.g0 + v.nc && v.done[chunk] && *v.err == 0) {
+            agg_from_partials<FastKindOf<Op>::k>(a, chunk, c1 - c0);
+            return;
+        }
         static_assert(sizeof(stage) >= 2 * kAggTile * sizeof(float), "fast AGG staging");
         if (a.fast_agg && chunk >= a.fast_from &&
             agg_fast_block<FastKindOf<Op>::k>(a, chunk, c0, c1, &stage[0][0][0]))
@@ -934,7 +1055,7 @@ k_recur(RecurArgs a) {
             __syncthreads();
             constexpr int FK = FastKindOf<Op>::k;
             if constexpr (FK == FK_EMA || FK == FK_RSI || FK == FK_TEMA) {
-                if (a.first < a.n && agg_seed_fast<FK>(a, xs, c1)) return;
+                if (a.first < a.n && agg_seed_fast<FK>(a, xs, c1, (int)(sizeof(stage) / sizeof(float)))) return;
             }
             const int l0 = blockIdx.x * blockDim.x + threadIdx.x;
             if (l0 < a.n_lanes) {
@@ -1248,55 +1369,162 @@ __device__ void chunk_map(const float4 g, int p, int chunk, const double (&ml)[O
     for (int r = 0; r < N; ++r) a.b[r] = gb[r];
 }
 
+// Carry-in state of every (lane, chunk): one warp per lane, each thread a
+// contiguous run of chunks.  Pass 1 composes the thread's chunk maps, a warp
+// scan of the compositions gives each thread its entry state, pass 2 applies
+// the maps chunk by chunk and writes the carries.  Full chunks share one
+// linear part M (the transition of `chunk` steps), so a run of them only
+// updates the offset (b <- M b + agg) and its power M^cnt is applied once
+// (trans_pow of cnt * chunk steps) when another map follows or the run ends:
+// the f64 work per chunk is a matrix-vector product, not a matrix product.
+// The chunk records are read eight at a time, ahead of the dependent math.
 template <class Op>
 __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
     constexpr int N = Op::NS;
+    constexpr int SH = ShapeOf<Op>::v;
+    constexpr int kB = 8;
     const int lane = threadIdx.x & 31;
     const int li = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // one warp per lane of the scan
     if (li >= a.n_lanes) return;
     const int p = a.layout ? a.period : a.periods[li];
-    double ml[N][N];  // transition of a full chunk
-    trans_pow<Op>((double)a.chunk, p, ml);
     const float4* agg = reinterpret_cast<const float4*>(a.agg);
     float4* carry = reinterpret_cast<float4*>(a.carry);
     const int per = (n_chunks + 31) / 32;
     const int k0 = min(lane * per, n_chunks), k1 = min(k0 + per, n_chunks);
+    const float full = (float)a.chunk;
+    // transitions of one full chunk (ml) and of `per` full chunks (mper):
+    // lanes 0 and 1 compute them (the f64 powers are costly at GB300's FP64
+    // rate), the warp shares them
+    double ml[N][N], mper[N][N];
+    {
+        double t[N][N];
+#pragma unroll
+        for (int r = 0; r < N; ++r)
+#pragma unroll
+            for (int c = 0; c < N; ++c) t[r][c] = 0.0;
+        if (lane < 2) trans_pow<Op>(lane == 0 ? (double)a.chunk : (double)per * a.chunk, p, t);
+#pragma unroll
+        for (int r = 0; r < N; ++r)
+#pragma unroll
+            for (int c = 0; c < N; ++c) {
+                ml[r][c] = shape_nz(SH, r, c) ? __shfl_sync(0xffffffffu, t[r][c], 0) : 0.0;
+                mper[r][c] = shape_nz(SH, r, c) ? __shfl_sync(0xffffffffu, t[r][c], 1) : 0.0;
+            }
+    }
+    // v <- M v + g (the map of a full chunk applied to a vector)
+    auto full_step = [&](double (&v)[N], const float4 g) {
+        const float gb[3] = {g.x, g.y, g.z};
+        double t[N];
+#pragma unroll
+        for (int r = 0; r < N; ++r) {
+            double x = gb[r];
+#pragma unroll
+            for (int c = 0; c < N; ++c)
+                if (shape_nz(SH, r, c)) x = fma(ml[r][c], v[c], x);
+            t[r] = x;
+        }
+#pragma unroll
+        for (int r = 0; r < N; ++r) v[r] = t[r];
+    };
     Aff<N> run;
     aff_identity(run);
-    for (int k = k0; k < k1; ++k) {
-        Aff<N> ak;
-        chunk_map<Op>(agg[(size_t)k * a.n_lanes + li], p, a.chunk, ml, ak);
-        run = aff_then<N, ShapeOf<Op>::v>(run, ak);
+    int cnt = 0;          // full chunks whose linear part is not yet in run.m
+    bool m_zero = false;  // run.m == 0 (after an absolute chunk): powers leave it 0
+    auto flush = [&]() {
+        if (cnt == 0 || m_zero) {
+            cnt = 0;
+            return;
+        }
+        double pw[N][N];
+        if (cnt == per) {
+#pragma unroll
+            for (int r = 0; r < N; ++r)
+#pragma unroll
+                for (int c = 0; c < N; ++c) pw[r][c] = mper[r][c];
+        } else {
+            trans_pow<Op>((double)cnt * a.chunk, p, pw);
+        }
+        double m2[N][N];  // run.m <- M^cnt run.m (the offset is already current)
+#pragma unroll
+        for (int r = 0; r < N; ++r)
+#pragma unroll
+            for (int c = 0; c < N; ++c) {
+                double v = 0.0;
+                if (shape_nz(SH, r, c))
+#pragma unroll
+                    for (int q = 0; q < N; ++q)
+                        if (shape_nz(SH, r, q) && shape_nz(SH, q, c)) v = fma(pw[r][q], run.m[q][c], v);
+                m2[r][c] = v;
+            }
+#pragma unroll
+        for (int r = 0; r < N; ++r)
+#pragma unroll
+            for (int c = 0; c < N; ++c) run.m[r][c] = m2[r][c];
+        cnt = 0;
+    };
+    for (int kb = k0; kb < k1; kb += kB) {
+        float4 gv[kB];
+#pragma unroll
+        for (int u = 0; u < kB; ++u)
+            if (kb + u < k1) gv[u] = __ldg(agg + (size_t)(kb + u) * a.n_lanes + li);
+#pragma unroll
+        for (int u = 0; u < kB; ++u) {
+            if (kb + u >= k1) break;
+            if (gv[u].w == full) {
+                full_step(run.b, gv[u]);
+                ++cnt;
+            } else {
+                flush();
+                Aff<N> ak;
+                chunk_map<Op>(gv[u], p, a.chunk, ml, ak);
+                run = aff_then<N, SH>(run, ak);
+                if (gv[u].w == kAbsolute) m_zero = true;
+            }
+        }
     }
+    flush();
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-        const Aff<N> up = aff_shfl_up<N, ShapeOf<Op>::v>(run, d);
-        if (lane >= d) run = aff_then<N, ShapeOf<Op>::v>(up, run);
+        const Aff<N> up = aff_shfl_up<N, SH>(run, d);
+        if (lane >= d) run = aff_then<N, SH>(up, run);
     }
-    Aff<N> ex = aff_shfl_up<N, ShapeOf<Op>::v>(run, 1);
+    Aff<N> ex = aff_shfl_up<N, SH>(run, 1);
     if (lane == 0) aff_identity(ex);
     double S[N];  // state at the start of chunk k0
 #pragma unroll
     for (int r = 0; r < N; ++r) S[r] = ex.b[r];
-    for (int k = k0; k < k1; ++k) {
-        float4 cv = make_float4(0.f, 0.f, 0.f, 0.f);
-        cv.x = (float)S[0];
-        if (N > 1) cv.y = (float)S[N > 1 ? 1 : 0];
-        if (N > 2) cv.z = (float)S[N > 2 ? 2 : 0];
-        carry[(size_t)k * a.n_lanes + li] = cv;
-        Aff<N> ak;
-        chunk_map<Op>(agg[(size_t)k * a.n_lanes + li], p, a.chunk, ml, ak);
-        double t[N];
+    for (int kb = k0; kb < k1; kb += kB) {
+        float4 gv[kB];
 #pragma unroll
-        for (int r = 0; r < N; ++r) {
-            double v = ak.b[r];
+        for (int u = 0; u < kB; ++u)
+            if (kb + u < k1) gv[u] = __ldg(agg + (size_t)(kb + u) * a.n_lanes + li);
 #pragma unroll
-            for (int c = 0; c < N; ++c)
-                if (shape_nz(ShapeOf<Op>::v, r, c)) v = fma(ak.m[r][c], S[c], v);
-            t[r] = v;
+        for (int u = 0; u < kB; ++u) {
+            const int k = kb + u;
+            if (k >= k1) break;
+            float4 cv = make_float4(0.f, 0.f, 0.f, 0.f);
+            cv.x = (float)S[0];
+            if (N > 1) cv.y = (float)S[N > 1 ? 1 : 0];
+            if (N > 2) cv.z = (float)S[N > 2 ? 2 : 0];
+            carry[(size_t)k * a.n_lanes + li] = cv;
+            if (gv[u].w == full) {
+                full_step(S, gv[u]);
+            } else {
+                Aff<N> ak;
+                chunk_map<Op>(gv[u], p, a.chunk, ml, ak);
+                double t[N];
+#pragma unroll
+                for (int r = 0; r < N; ++r) {
+                    double v = ak.b[r];
+#pragma unroll
+                    for (int c = 0; c < N; ++c)
+                        if (shape_nz(SH, r, c)) v = fma(ak.m[r][c], S[c], v);
+                    t[r] = v;
+                }
+#pragma unroll
+                for (int r = 0; r < N; ++r) S[r] = t[r];
+            }
         }
-#pragma unroll
-        for (int r = 0; r < N; ++r) S[r] = t[r];
     }
 }
 

@@ -61,6 +61,11 @@ vta_status check_launch(const char* kernel) {
     if (e != cudaSuccess) return cuda_fail(e, kernel);
     return VTA_OK;
 }
+vta_status check_async(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    return VTA_OK;
+}
 
 vta_status Arena::commit() {
     if (total_ <= ctx_->scratch_bytes) return VTA_OK;
@@ -359,9 +364,10 @@ static int pick_chunk(vta_ctx* ctx, int n, int lanes, int warps_per_sm = 64) {
 // ("indicator len_bucket combos_bucket knob value" per line).  Knobs:
 //   TK_RECUR   chunked scans: lane-warps x chunks in flight per SM (32, 64, 128)
 //   TK_MINMAX  sliding min/max: output tile (512, 1024 times per block)
+//   TK_RECUR_TC  TK_RECUR where the chunk aggregates may take the tensor cores
 // Policy "tune" = on (default) | off (untuned defaults) | cached (use cached
 // choices, never time); server slots never time.
-enum TuneKnob { TK_RECUR = 1, TK_MINMAX = 2 };
+enum TuneKnob { TK_RECUR = 1, TK_MINMAX = 2, TK_RECUR_TC = 3 };
 using SweepTuneKey = std::tuple<int, int, int, int>;
 static std::mutex g_stune_mu;
 static std::map<SweepTuneKey, int> g_stune;
@@ -408,6 +414,40 @@ static void stune_store(const SweepTuneKey& k, int v) {
         }
 }
 
+// Weights of the tensor-core recurrence aggregates for (kind, L, periods):
+// the context keeps up to kRwCap bytes of them across calls.  *build = 1 when
+// the buffer does not hold them yet (the caller launches the weights kernel
+// and then marks the entry valid).
+constexpr size_t kRwCap = size_t(256) << 20;
+static vta_status rw_get(vta_ctx* ctx, int kind, int L, const std::vector<int>& periods, size_t bytes,
+                         vta_ctx::RwEntry** out, int* build) {
+    for (auto& e : ctx->rw)
+        if (e.kind == kind && e.L == L && e.bytes >= bytes && e.periods == periods) {
+            e.tick = ++ctx->rw_tick;
+            *out = &e;
+            *build = e.valid ? 0 : 1;
+            return VTA_OK;
+        }
+    size_t total = bytes;
+    for (auto& e : ctx->rw) total += e.bytes;
+    if (total > kRwCap) VTA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));  // buffers may be in use
+    while (total > kRwCap && !ctx->rw.empty()) {
+        size_t lru = 0;
+        for (size_t i = 1; i < ctx->rw.size(); ++i)
+            if (ctx->rw[i].tick < ctx->rw[lru].tick) lru = i;
+        total -= ctx->rw[lru].bytes;
+        cudaFree(ctx->rw[lru].dev);
+        ctx->rw.erase(ctx->rw.begin() + (long)lru);
+    }
+    VTA_TRY(vram_check(bytes));
+    void* dev = nullptr;
+    VTA_CUDA_TRY(cudaMalloc(&dev, bytes));
+    ctx->rw.push_back(vta_ctx::RwEntry{kind, L, periods, dev, bytes, ++ctx->rw_tick, false});
+    *out = &ctx->rw.back();
+    *build = 1;
+    return VTA_OK;
+}
+
 // Runs `launch(candidate)` for every candidate, keeps the fastest and makes
 // sure the outputs left behind are that candidate's.  `tag` gets the choice
 // and whether it was timed now ("tuned") or taken from the cache ("cached").
@@ -441,7 +481,7 @@ static vta_status tuned_launch(vta_ctx* ctx, int ind, long long n, long long com
             cudaEventRecord(e0, st);
             s = launch(cand[i]);
             cudaEventRecord(e1, st);
-            if (s == VTA_OK && cudaStreamSynchronize(st) != cudaSuccess) s = check_launch("sweep tuning");
+            if (s == VTA_OK && cudaStreamSynchronize(st) != cudaSuccess) s = check_async("sweep tuning");
             float ms = 0.f;
             if (s == VTA_OK) cudaEventElapsedTime(&ms, e0, e1);
             if (s == VTA_OK && ms < best) {
@@ -464,11 +504,15 @@ vta_status upload_async(vta_ctx* ctx, void* dst, const void* src, size_t bytes, 
     if (!bytes) return VTA_OK;
     const size_t off = (ctx->host_stage_off + 255) & ~size_t(255);
     if (ctx->host_stage && off + bytes <= ctx->host_stage_bytes) {
-        // the staging region is not reused before this call's final synchronize
+        // the staging region is reused by the next call only after the event
+        // recorded behind this copy (check_ctx)
         char* h = static_cast<char*>(ctx->host_stage) + off;
         std::memcpy(h, src, bytes);
         ctx->host_stage_off = off + bytes;
         VTA_CUDA_TRY(cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, st));
+        if (!ctx->stage_ev) VTA_CUDA_TRY(cudaEventCreateWithFlags(&ctx->stage_ev, cudaEventDisableTiming));
+        VTA_CUDA_TRY(cudaEventRecord(ctx->stage_ev, st));
+        ctx->stage_pending = true;
         return VTA_OK;
     }
     VTA_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
@@ -478,8 +522,9 @@ vta_status upload_async(vta_ctx* ctx, void* dst, const void* src, size_t bytes, 
 // Constant cache of a context (see vta_ctx::cc_*): a device buffer filled
 // front to back by uploads; an upload whose bytes match an earlier one (hash,
 // then a full compare with the host copy) reuses it.  When the buffer is full
-// it starts over: every earlier call has synchronised, so no kernel still
-// reads it.  Server slots (calls that do not wait) bypass it.
+// it starts over: the uploads are stream-ordered copies on the context's
+// stream, behind every kernel of the earlier calls that reads the buffer
+// (a stream switch waits for the old stream).  Server slots bypass it.
 static constexpr size_t kConstCacheBytes = size_t(4) << 20;
 static constexpr size_t kConstCacheMaxItem = size_t(256) << 10;
 
@@ -682,6 +727,7 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             // chunking for a target of `wps` lane-warps x chunks per SM
             struct Chunking {
                 int chunk, chunk0, nch, fast_from;
+                int tc_nc;  // full-length chunks from fast_from on (tensor-core aggregates)
             };
             auto chunking = [&](int wps) {
                 Chunking c{};
@@ -703,14 +749,58 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
                         break;
                     }
                 }
+                c.tc_nc = 0;
+                if (c.fast_from < c.nch) {
+                    int c0 = 0, c1 = 0;
+                    RecurArgs tmp{};
+                    tmp.n = n;
+                    tmp.chunk = c.chunk;
+                    tmp.chunk0 = c.chunk0;
+                    recur_chunk_bounds(tmp, c.nch - 1, c0, c1);
+                    c.tc_nc = c.nch - c.fast_from - (c1 - c0 < c.chunk ? 1 : 0);
+                }
                 return c;
+            };
+            // tensor-core chunk aggregates: EMA / DEMA / TEMA / RSI with at
+            // least a few full chunks past every seed and a workspace (the
+            // packed weights and inputs) of at most 1 GiB
+            const int tc_kind = ind == I_EMA ? RK_EMA : ind == I_DEMA ? RK_DEMA : ind == I_TEMA ? RK_TEMA : RK_RSI;
+            constexpr size_t kTcWsCap = size_t(1) << 30;
+            auto tc_geo = [&](const Chunking& c) { return recur_agg_tc_geo(tc_kind, nc, c.chunk, c.tc_nc, ctx->num_sms); };
+            auto tc_ok = [&](const Chunking& c) {
+                if (!(fast_kind && ctx->policy.recur_agg != 1 && c.nch > 1 && c.tc_nc >= 2 && c.chunk % 32 == 0 &&
+                      ctx->smem_optin >= recur_agg_tc_smem()))
+                    return false;
+                const RecurTcGeo g = tc_geo(c);
+                return g.ws_bytes + g.w_bytes <= kTcWsCap && g.w_bytes <= kRwCap;
             };
             const std::vector<int> cand = ctx->policy.recur_chunk == 0 ? std::vector<int>{32, 64, 128}
                                                                        : std::vector<int>{64};
             int max_nch = 1;
-            for (int w : cand) max_nch = std::max(max_nch, chunking(w).nch);
+            size_t tc_ws = 0, tc_w = 0;
+            bool tc_any = false;
+            for (int w : cand) {
+                const Chunking c = chunking(w);
+                max_nch = std::max(max_nch, c.nch);
+                if (tc_ok(c)) {
+                    tc_any = true;
+                    const RecurTcGeo g = tc_geo(c);
+                    tc_ws = std::max(tc_ws, g.ws_bytes);
+                    tc_w = std::max(tc_w, g.w_bytes);
+                }
+            }
+            // server slots (stream-ordered workspaces) rebuild the weights per call
+            const bool tc_cache = !ctx->async_alloc;
+            if (ctx->policy.recur_agg == 2 && !tc_any)
+                return fail(VTA_ERR_NOT_IMPLEMENTED, "recur_agg=tc: this sweep has no tensor-core chunk aggregates");
             ar.need((size_t)max_nch * nc * 16);
             ar.need((size_t)max_nch * nc * 16);
+            if (tc_any) {
+                ar.need(tc_ws);
+                if (!tc_cache) ar.need(tc_w);
+                ar.need((size_t)max_nch * sizeof(int));
+                ar.need(sizeof(int));
+            }
             VTA_TRY(ar.commit());
             const int* d_per = nullptr;
             VTA_TRY(const_upload(ctx, periods.data(), nc, ar.take<int>(nc), &d_per));
@@ -720,6 +810,10 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             ar.take<float>(nc);
             float* d_agg = ar.take<float>((size_t)max_nch * nc * 4);
             float* d_carry = ar.take<float>((size_t)max_nch * nc * 4);
+            void* d_tc_ws = tc_any ? ar.take<char>(tc_ws) : nullptr;
+            void* d_tc_w = tc_any && !tc_cache ? ar.take<char>(tc_w) : nullptr;
+            int* d_tc_done = tc_any ? ar.take<int>(max_nch) : nullptr;
+            int* d_tc_err = tc_any ? ar.take<int>(1) : nullptr;
             RecurArgs a{};
             a.kind = ind == I_EMA ? RK_EMA : ind == I_DEMA ? RK_DEMA : ind == I_TEMA ? RK_TEMA
                    : ind == I_RSI ? RK_RSI : ind == I_WILDERS ? RK_WILDERS : RK_ATR;
@@ -734,6 +828,7 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             a.agg = d_agg;
             a.carry = d_carry;
             int nch_used = 1;
+            bool tc_used = false;
             auto launch = [&](int wps) {
                 const Chunking c = chunking(wps);
                 a.chunk = c.chunk;
@@ -741,15 +836,62 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
                 a.fast_from = c.fast_from;
                 a.fast_agg = (fast_kind && c.nch > 1 && c.fast_from < c.nch) ? 1 : 0;
                 nch_used = c.nch;
+                a.tc = RecurTcView{};
+                tc_used = false;
+                if (a.fast_agg && tc_ok(c)) {
+                    RecurTcArgs t{};
+                    t.kind = tc_kind;
+                    t.x = a.x;
+                    t.periods = d_per;
+                    t.n_lanes = nc;
+                    t.L = c.chunk;
+                    t.chunk0 = c.chunk0;
+                    t.g0 = c.fast_from;
+                    t.nc = c.tc_nc;
+                    t.geo = tc_geo(c);
+                    vta_ctx::RwEntry* ent = nullptr;
+                    if (tc_cache) {
+                        VTA_TRY(rw_get(ctx, tc_kind, c.chunk, periods, t.geo.w_bytes, &ent, &t.build_weights));
+                        t.wts = ent->dev;
+                    } else {
+                        t.wts = d_tc_w;
+                        t.build_weights = 1;
+                    }
+                    t.ws = d_tc_ws;
+                    t.done = d_tc_done;
+                    t.err = d_tc_err;
+                    VTA_TRY(launch_recur_agg_tc(t, ctx->smem_optin, st));
+                    if (ent) ent->valid = true;
+                    RecurTcView& v = a.tc;
+                    v.done = d_tc_done;
+                    v.err = d_tc_err;
+                    v.g0 = t.g0;
+                    v.nc = t.nc;
+                    const char* ws = static_cast<const char*>(t.ws);
+                    const char* wb = static_cast<const char*>(t.wts);
+                    v.part = reinterpret_cast<const float*>(ws + t.geo.part_off);
+                    v.S = t.geo.S;
+                    v.npad = t.geo.npad;
+                    v.rows = t.geo.rows;
+                    v.mpad = t.geo.mpad;
+                    v.row_scale = reinterpret_cast<const float*>(wb + t.geo.row_scale_off);
+                    v.row_sum = reinterpret_cast<const float*>(wb + t.geo.row_sum_off);
+                    v.col_scale = reinterpret_cast<const float*>(ws + t.geo.col_scale_off);
+                    v.col_ref = reinterpret_cast<const float*>(ws + t.geo.col_ref_off);
+                    tc_used = true;
+                }
                 return launch_recurrence(a, st);
             };
             int wps = 64;
             const char* tag = "default";
-            VTA_TRY(tuned_launch(ctx, (int)ind, n, nc, TK_RECUR, cand, 64, launch, &wps, &tag));
+            const int knob = (fast_kind && ctx->policy.recur_agg != 1) ? TK_RECUR_TC : TK_RECUR;
+            VTA_TRY(tuned_launch(ctx, (int)ind, n, nc, knob, cand, 64, launch, &wps, &tag));
             ctx->last_kernel = nch_used > 1 ? "recurrence_chunked" : "recurrence_sequential";
             if (nch_used > 1 && ctx->policy.recur_chunk == 0)
                 ctx->last_kernel += "(chunk=" + std::to_string(a.chunk) + ", " + std::to_string(wps) + " warps/SM, " +
-                                    tag + ")";
+                                    (tc_used ? "tc aggregates, " : "") + tag + ")";
+            else if (tc_used)
+                ctx->last_kernel += "(tc aggregates)";
             return VTA_OK;
         }
         case I_ADX: case I_SUPERTREND: {
@@ -1124,13 +1266,19 @@ static vta_status check_ctx(vta_ctx* ctx) {
     VTA_CUDA_TRY(cudaSetDevice(ctx->device));
     g_cur = ctx;
     ctx->timed = false;
-    ctx->host_stage_off = 0;  // the previous call has synchronised
+    // the pinned staging buffer is reused once the copies of the calls that
+    // staged through it (device entry points return without waiting) are done
+    if (ctx->stage_pending) {
+        VTA_CUDA_TRY(cudaEventSynchronize(ctx->stage_ev));
+        ctx->stage_pending = false;
+    }
+    ctx->host_stage_off = 0;
     return VTA_OK;
 }
 
 static vta_status sync(vta_ctx* ctx) {
     VTA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    return check_launch("stream");
+    return check_async("stream");
 }
 
 // host inputs -> device outputs (`out_dev` non-null: caller's device buffers;
@@ -1228,7 +1376,9 @@ static vta_status batch_device(vta_ctx* ctx, Ind ind, const float* const* din_p,
     DevIn din{};
     for (int k = 0; k < nin; ++k) din.p[k] = din_p[k];
     VTA_TRY(run_batch(ctx, ind, din, len, first, cs, d_out));
-    return sync(ctx);
+    // stream-ordered, not waited for (the crate's x_batch_device returns
+    // after the launch too); vta_ctx_synchronize waits
+    return check_async("batch_device");
 }
 
 static vta_status tm_validate_host(Ind ind, const float* const* hin, size_t cols, size_t rows, const Combo& c) {
@@ -1301,7 +1451,7 @@ static vta_status tm_device(vta_ctx* ctx, Ind ind, const float* const* din_p, si
     DevIn din{};
     for (int k = 0; k < nin; ++k) din.p[k] = din_p[k];
     VTA_TRY(run_tm(ctx, ind, din, cols, rows, c, d_out));
-    return sync(ctx);
+    return check_async("many_series_device");  // stream-ordered, like batch_device
 }
 
 // ------------------------------------------------------------ grids --------
@@ -1704,11 +1854,13 @@ vta_status vta_ctx_destroy(vta_ctx* ctx) {
     if (ctx->aux) ctx->async_alloc ? (void)cudaFreeAsync(ctx->aux, ctx->stream) : (void)cudaFree(ctx->aux);
     if (ctx->io) cudaFree(ctx->io);
     if (ctx->cc_dev) cudaFree(ctx->cc_dev);
+    for (auto& e : ctx->rw) cudaFree(e.dev);
     if (ctx->async_alloc) cudaStreamSynchronize(ctx->stream);
     if (ctx->err_host) cudaFreeHost(ctx->err_host);
     if (ctx->host_stage) cudaFreeHost(ctx->host_stage);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stage_ev) cudaEventDestroy(ctx->stage_ev);
     if (g_cur == ctx) g_cur = nullptr;
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -1716,12 +1868,19 @@ vta_status vta_ctx_destroy(vta_ctx* ctx) {
 }
 
 vta_status vta_ctx_synchronize(vta_ctx* ctx) {
-    VTA_TRY(check_ctx(ctx));
-    return sync(ctx);
+    // not a compute call: the last call's timing stays readable
+    if (!ctx) return fail(VTA_ERR_INVALID_INPUT, "null context");
+    VTA_CUDA_TRY(cudaSetDevice(ctx->device));
+    VTA_TRY(sync(ctx));
+    ctx->stage_pending = false;
+    return VTA_OK;
 }
 
 vta_status vta_ctx_set_stream(vta_ctx* ctx, void* stream) {
     VTA_TRY(check_ctx(ctx));
+    // work already queued on the old stream (device entry points do not wait)
+    // finishes before the context's buffers are used from another stream
+    if (ctx->stream) VTA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     if (stream) {
         if (ctx->own_stream && ctx->stream) {
             cudaStreamSynchronize(ctx->stream);
@@ -1790,6 +1949,13 @@ vta_status vta_ctx_set_policy(vta_ctx* ctx, const char* key, const char* value) 
         } else {
             return fail(VTA_ERR_INVALID_POLICY, "host_io: cached|per_call");
         }
+        return VTA_OK;
+    }
+    if (k == "recur_agg") {
+        if (v == "auto") ctx->policy.recur_agg = 0;
+        else if (v == "cuda") ctx->policy.recur_agg = 1;
+        else if (v == "tc") ctx->policy.recur_agg = 2;
+        else return fail(VTA_ERR_INVALID_POLICY, "recur_agg: auto|cuda|tc");
         return VTA_OK;
     }
     if (k == "tune") {

@@ -35,6 +35,9 @@ vta_status cuda_fail(cudaError_t e, const char* what);
 
 // Checks the launch that was just enqueued (and counts it).
 vta_status check_launch(const char* kernel);
+// The sticky / asynchronous error state after non-kernel work (a stream
+// synchronize, a copy); not counted as a launch.
+vta_status check_async(const char* what);
 
 // Event timer around a call's main output kernel, on the launching stream;
 // active only when the current context has policy "timing" = "on".
@@ -62,6 +65,10 @@ struct Policy {
     // batch-sweep autotuner: 0 = on (time candidates on the first call per
     // key), 1 = off (untuned defaults), 2 = cached choices only
     int tune = 0;
+    // chunk aggregates of the EMA / DEMA / TEMA / RSI batch sweeps: 0 = auto
+    // (tensor-core contraction where the sweep is eligible), 1 = CUDA cores
+    // only, 2 = tensor cores required (an ineligible sweep is an error)
+    int recur_agg = 0;
 };
 
 }  // namespace vta
@@ -84,6 +91,8 @@ struct vta_ctx {
     void* host_stage = nullptr;  // pinned staging of small uploads, reused per call
     size_t host_stage_bytes = 0;
     size_t host_stage_off = 0;
+    cudaEvent_t stage_ev = nullptr;  // recorded behind the last staged copy
+    bool stage_pending = false;
     vta::Policy policy;
     std::string last_kernel;
     bool timing = false;
@@ -104,6 +113,18 @@ struct vta_ctx {
         size_t off, bytes;
     };
     std::vector<CcEntry> cc;
+    // packed weights of the tensor-core recurrence aggregates, kept across
+    // calls per (kind, chunk length, periods); least recently used evicted
+    struct RwEntry {
+        int kind, L;
+        std::vector<int> periods;
+        void* dev;
+        size_t bytes;
+        uint64_t tick;
+        bool valid;  // the weights kernel ran on this buffer
+    };
+    std::vector<RwEntry> rw;
+    uint64_t rw_tick = 0;
 };
 
 namespace vta {
@@ -221,6 +242,35 @@ vta_status launch_wwma_tm(const WwmaTmArgs& a, cudaStream_t st);
 // ------------------------------------------------- chunked recurrences -----
 enum RecurKind { RK_EMA = 0, RK_DEMA = 1, RK_TEMA = 2, RK_RSI = 3, RK_WILDERS = 4, RK_ATR = 5 };
 
+// Shape of the tensor-core chunk-aggregate contraction (k_recur_tc.cu):
+// weight rows (component, lane) x columns (chunk; RSI: gains | losses), K
+// split S ways; byte offsets of the pieces in the weight and work buffers.
+struct RecurTcGeo {
+    int nsr;               // weight rows per lane: 1 (EMA, RSI), 2 (DEMA), 3 (TEMA)
+    int mpad;              // lanes rounded up to 128
+    int rows;              // nsr * mpad
+    int ncol;              // columns: nc (RSI: 2 nc)
+    int npad;              // ncol rounded up to 128
+    int S;                 // K splits
+    size_t w_bytes, row_scale_off, row_sum_off;
+    size_t ws_bytes, col_scale_off, col_ref_off, part_off;
+};
+// What the AGG pass reads of a finished contraction: for a chunk c in
+// [g0, g0 + nc) with done[c] and *err == 0, component q of lane li is
+//   (sum over s < S of part[s][j][r]) * row_scale[r] * col_scale[j] + col_ref[j] * row_sum[r]
+// with r = q mpad + li, j = c - g0 (RSI: component 1 at j + nc, r = li).
+struct RecurTcView {
+    const int* done;
+    const int* err;
+    int g0, nc;
+    const float* part;     // [S][npad][rows]
+    int S, npad, rows, mpad;
+    const float* row_scale;
+    const float* row_sum;
+    const float* col_scale;
+    const float* col_ref;
+};
+
 struct RecurArgs {
     int kind;
     int layout;            // 0 = batch (one series, lane = combo), 1 = time-major
@@ -250,8 +300,33 @@ struct RecurArgs {
     // scratch
     float* agg;            // [n_chunks][n_lanes] float4 (state, applied steps)
     float* carry;          // [n_chunks][n_lanes] float4 (carry-in state)
+    // tensor-core partial sums of the full chunks (k_recur_tc.cu); done ==
+    // null: none
+    RecurTcView tc;
 };
 vta_status launch_recurrence(const RecurArgs& a, cudaStream_t st);
+
+// Chunk aggregates of a batch EMA / DEMA / TEMA / RSI sweep as one
+// split-precision tcgen05 contraction over the full-length chunks
+// [g0, g0 + nc) (k_recur_tc.cu).
+struct RecurTcArgs {
+    int kind;              // RK_EMA, RK_DEMA, RK_TEMA or RK_RSI
+    const float* x;        // the series
+    const int* periods;    // per lane
+    int n_lanes;
+    int L;                 // chunk length (multiple of 32)
+    int chunk0;            // length of chunk 0: chunk c >= 1 starts at chunk0 + (c - 1) L
+    int g0, nc;            // g0 >= 1; every chunk of the range is L long
+    RecurTcGeo geo;        // recur_agg_tc_geo(kind, n_lanes, L, nc, SMs)
+    void* wts;             // geo.w_bytes: packed weights (a function of kind, periods, L)
+    int build_weights;     // 0: wts already holds this sweep's weights
+    void* ws;              // geo.ws_bytes: packed inputs, column scales, partial sums
+    int* done;             // [n_chunks]: 1 = the chunk's inputs are finite (partials valid)
+    int* err;              // raised on a pipeline wait timeout (partials then unusable)
+};
+RecurTcGeo recur_agg_tc_geo(int kind, int n_lanes, int L, int nc, int num_sms);
+size_t recur_agg_tc_smem();
+vta_status launch_recur_agg_tc(const RecurTcArgs& a, size_t smem_optin, cudaStream_t st);
 int recur_state_dim(int kind);
 // Time range [c0, c1) of chunk k (chunk 0 is chunk0 long, the rest chunk).
 __host__ __device__ inline void recur_chunk_bounds(const RecurArgs& a, int k, int& c0, int& c1) {

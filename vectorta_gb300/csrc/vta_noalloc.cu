@@ -115,5 +115,5 @@ extern "C" vta_status vta_sma_batch_device_noalloc(vta_ctx* ctx, const float* d_
     VTA_TRY(launch_prefix_window_batch(a, pmax, ctx->smem_optin, st));
     // Synchronous like every entry point: the scratch is free again on return.
     VTA_CUDA_TRY(cudaStreamSynchronize(st));
-    return check_launch("stream");
+    return check_async("stream");
 }

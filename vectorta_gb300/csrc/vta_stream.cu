@@ -1493,7 +1493,7 @@ vta_status vta_streams_update_device(vta_streams* S, const float* d_a, const flo
         return fail(VTA_ERR_INVALID_INPUT, "streams: null input/output pointer");
     VTA_TRY(enqueue_update(S, d_a, d_b, d_c, d_out));
     VTA_CUDA_TRY(cudaStreamSynchronize(S->ctx->stream));
-    return check_launch("stream");
+    return check_async("stream");
 }
 
 vta_status vta_streams_update_host(vta_streams* S, const float* a, const float* b, const float* c, float* out) {
@@ -1513,7 +1513,7 @@ vta_status vta_streams_update_host(vta_streams* S, const float* a, const float* 
     VTA_TRY(enqueue_update(S, da, db, dc, dout));
     VTA_CUDA_TRY(cudaMemcpyAsync(out, dout, (size_t)S->s.n_out * n * sizeof(float), cudaMemcpyDeviceToHost, cs));
     VTA_CUDA_TRY(cudaStreamSynchronize(cs));
-    return check_launch("stream");
+    return check_async("stream");
 }
 
 vta_status vta_streams_reset(vta_streams* S) {
