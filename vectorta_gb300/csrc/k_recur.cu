@@ -5,8 +5,9 @@
 //   pass A (k_recur<.., PASS_AGG>):  per (lane, chunk) run the recurrence from
 //       a zero state (or from the exact seed inside the seed chunk) and keep
 //       the chunk-end state plus the number of applied steps;
-//   pass B (k_recur_carry):          per lane, compose the chunk transforms in
-//       f64 (closed-form powers of the transition matrix) -> carry-in per chunk;
+//   pass B (k_recur_carry):          per lane, compose the chunk transforms
+//       (closed-form powers of the transition matrix) in double-single
+//       arithmetic -> carry-in per chunk;
 //   pass C (k_recur<.., PASS_EMIT>): per (lane, chunk) re-run from the carry
 //       and write the outputs.
 // A "lane" is one parameter combo of a single-series sweep (batch layout:
@@ -104,18 +105,58 @@ struct InStep {
     __device__ float L(int) const { return l0; }
 };
 
-// b^n for a whole step count n >= 0 by repeated squaring: about 2 log2(n)
-// f64 multiplies (a few ulp), instead of pow()'s log / exp evaluation, which
-// on GB300's FP64 rate made the carry scan latency-bound.
-__device__ __forceinline__ double ipow(double b, double n) {
-    unsigned long long e = (unsigned long long)n;
-    double r = 1.0;
-    while (e) {
-        if (e & 1ull) r *= b;
-        b *= b;
-        e >>= 1;
+// Double-single numbers for the carry scan and the closed-form chunk
+// transitions: value = hi + lo with |lo| <= ulp(hi) / 2, about 2^-44
+// relative after a few operations.  GB300 runs FP32 at many times its FP64
+// rate (one FP64 warp instruction holds the SM's FP64 pipe for many cycles),
+// so the scan works with FP32 error-free transformations (exact products by
+// FMA, TwoSum) instead of f64.
+struct D2 {
+    float hi, lo;
+};
+__device__ __forceinline__ D2 d2_norm(float s, float e) {
+    const float hi = s + e;
+    return {hi, e - (hi - s)};
+}
+__device__ __forceinline__ D2 d2_mul(D2 a, D2 b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+    return d2_norm(p, e);
+}
+__device__ __forceinline__ D2 d2_add(D2 a, D2 b) {
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    const float e = ((a.hi - (s - bb)) + (b.hi - bb)) + (a.lo + b.lo);
+    return d2_norm(s, e);
+}
+// a * b + c
+__device__ __forceinline__ D2 d2_fma(D2 a, D2 b, D2 c) { return d2_add(d2_mul(a, b), c); }
+__device__ __forceinline__ D2 d2_neg(D2 a) { return {-a.hi, -a.lo}; }
+// num / den for small positive integers, to double-single accuracy: the
+// FP32 quotient plus its exact remainder (FMA) divided again
+__device__ __forceinline__ D2 d2_ratio(int num, int den) {
+    const float fn = (float)num, fd = (float)den;
+    const float q = fn / fd;
+    const float r = fmaf(-q, fd, fn);
+    return d2_norm(q, r / fd);
+}
+__device__ __forceinline__ D2 d2_from_ll(long long n) {
+    const float hi = (float)n;
+    return {hi, (float)(n - (long long)hi)};
+}
+// b^n for a whole step count n >= 0 by repeated squaring
+__device__ __forceinline__ D2 d2_pow(D2 b, long long n) {
+    D2 r = {1.f, 0.f};
+    while (n > 0) {
+        if (n & 1) r = d2_mul(r, b);
+        b = d2_mul(b, b);
+        n >>= 1;
     }
     return r;
+}
+__device__ __forceinline__ D2 d2_shfl_up(D2 v, int d) {
+    return {__shfl_up_sync(0xffffffffu, v.hi, d), __shfl_up_sync(0xffffffffu, v.lo, d)};
 }
 
 // ------------------------------------------------------------ ops ----------
@@ -180,10 +221,13 @@ struct OpEma {
         applied += ok;
         return y;
     }
-    static __device__ void propagate(double* S, double n, int p) {
-        double b = 1.0 - 2.0 / ((double)p + 1.0);
-        S[0] *= ipow(b, n);
+    // closed-form transition of n steps (double-single): a = 2 / (p + 1),
+    // an = (1 - a)^n
+    static __device__ void coef(int p, D2& a, D2& b) {
+        a = d2_ratio(2, p + 1);
+        b = d2_add({1.f, 0.f}, d2_neg(a));
     }
+    static __device__ void propagate(D2* S, D2, D2, D2 an, int) { S[0] = d2_mul(S[0], an); }
 };
 
 // DEMA: dema.rs:291-354 (x86 mul_add form).  Seed x[f] at f; NaN prefix
@@ -223,12 +267,11 @@ struct OpDema {
         ++applied;
         return fmaf(e1, 2.f, -e2);
     }
-    static __device__ void propagate(double* S, double n, int p) {
-        double al = 2.0 / ((double)p + 1.0);
-        double an = ipow(1.0 - al, n);
-        double s1 = S[0];
-        S[0] = an * s1;
-        S[1] = an * (S[1] + n * al * s1);
+    static __device__ void coef(int p, D2& a, D2& b) { OpEma::coef(p, a, b); }
+    static __device__ void propagate(D2* S, D2 n, D2 al, D2 an, int) {
+        const D2 s1 = S[0];
+        S[0] = d2_mul(an, s1);
+        S[1] = d2_mul(an, d2_fma(d2_mul(n, al), s1, S[1]));
     }
 };
 
@@ -303,15 +346,19 @@ struct OpTema {
         e3 = t >= s ? n3 : e3;
         return t < warm ? qnan() : 3.f * e1 - 3.f * e2 + e3;
     }
-    static __device__ void propagate(double* S, double n, int p) {
-        if (p == 1) { S[0] = 0.0; return; }  // p==1 carries nothing (out = x)
-        double al = 2.0 / ((double)p + 1.0);
-        double an = ipow(1.0 - al, n);
-        double s1 = S[0], s2 = S[1], s3 = S[2];
-        double c2 = n * (n - 1.0) * 0.5;
-        S[0] = an * s1;
-        S[1] = an * (n * al * s1 + s2);
-        S[2] = an * ((n * al * al + c2 * al * al) * s1 + n * al * s2 + s3);
+    static __device__ void coef(int p, D2& a, D2& b) { OpEma::coef(p, a, b); }
+    static __device__ void propagate(D2* S, D2 n, D2 al, D2 an, int p) {
+        if (p == 1) {  // p==1 carries nothing (out = x)
+            S[0] = {0.f, 0.f};
+            return;
+        }
+        const D2 s1 = S[0], s2 = S[1], s3 = S[2];
+        const D2 nal = d2_mul(n, al);
+        // n a^2 + n (n - 1) / 2 a^2 = n (n + 1) / 2 a^2
+        const D2 c = d2_mul(d2_mul(d2_mul(n, d2_add(n, {1.f, 0.f})), {0.5f, 0.f}), d2_mul(al, al));
+        S[0] = d2_mul(an, s1);
+        S[1] = d2_mul(an, d2_fma(nal, s1, s2));
+        S[2] = d2_mul(an, d2_fma(c, s1, d2_fma(nal, s2, s3)));
     }
 };
 
@@ -381,10 +428,14 @@ struct OpRsi {
     }
     __device__ float get(int i) const { return i == 0 ? ag : al; }
     __device__ void set(int i, float v) { if (i == 0) ag = v; else al = v; }
-    static __device__ void propagate(double* S, double n, int p) {
-        double bn = ipow(1.0 - 1.0 / (double)p, n);
-        S[0] *= bn;
-        S[1] *= bn;
+    // a = 1 / p, an = (1 - 1/p)^n
+    static __device__ void coef(int p, D2& a, D2& b) {
+        a = d2_ratio(1, p);
+        b = d2_add({1.f, 0.f}, d2_neg(a));
+    }
+    static __device__ void propagate(D2* S, D2, D2, D2 an, int) {
+        S[0] = d2_mul(S[0], an);
+        S[1] = d2_mul(S[1], an);
     }
 };
 
@@ -420,8 +471,9 @@ struct OpWilders {
         ++applied;
         return y;
     }
-    static __device__ void propagate(double* S, double n, int p) {
-        S[0] = (p == 1) ? 0.0 : S[0] * ipow(1.0 - 1.0 / (double)p, n);
+    static __device__ void coef(int p, D2& a, D2& b) { OpRsi<true>::coef(p, a, b); }
+    static __device__ void propagate(D2* S, D2, D2, D2 an, int p) {
+        S[0] = (p == 1) ? D2{0.f, 0.f} : d2_mul(S[0], an);
     }
 };
 
@@ -471,9 +523,8 @@ struct OpAtr {
         ++applied;
         return y;
     }
-    static __device__ void propagate(double* S, double n, int p) {
-        S[0] *= ipow(1.0 - 1.0 / (double)p, n);
-    }
+    static __device__ void coef(int p, D2& a, D2& b) { OpRsi<true>::coef(p, a, b); }
+    static __device__ void propagate(D2* S, D2, D2, D2 an, int) { S[0] = d2_mul(S[0], an); }
 };
 
 // ------------------------------------------------------------ kernels ------
@@ -784,8 +835,16 @@ __device__ void agg_from_partials(const RecurArgs& a, int chunk, int len) {
         const int r = K == FK_RSI ? li : q * v.mpad + li;
         const int j = K == FK_RSI ? j0 + q * v.nc : j0;
         const float* p = v.part + (size_t)j * v.rows + r;
+        const size_t stride = (size_t)v.npad * v.rows;
+        // four independent loads in flight, summed in split order
         float acc = 0.f;
-        for (int s = 0; s < v.S; ++s) acc += __ldg(p + (size_t)s * v.npad * v.rows);
+        int s = 0;
+        for (; s + 4 <= v.S; s += 4) {
+            const float p0 = __ldg(p + (size_t)s * stride), p1 = __ldg(p + (size_t)(s + 1) * stride);
+            const float p2 = __ldg(p + (size_t)(s + 2) * stride), p3 = __ldg(p + (size_t)(s + 3) * stride);
+            acc = (((acc + p0) + p1) + p2) + p3;
+        }
+        for (; s < v.S; ++s) acc += __ldg(p + (size_t)s * stride);
         z[q] = fmaf(acc, __ldg(v.row_scale + r) * __ldg(v.col_scale + j), __ldg(v.col_ref + j) * __ldg(v.row_sum + r));
     }
     reinterpret_cast<float4*>(a.agg)[(size_t)chunk * a.n_lanes + li] = make_float4(z[0], z[1], z[2], (float)len);
@@ -1267,26 +1326,10 @@ k_recur(RecurArgs a) {
 }
 
 // Carry-in of every chunk: an exclusive scan, over the chunks of one lane, of
-// the affine chunk maps S -> M_k S + b_k (f64).  One warp per lane: each
-// thread composes a contiguous run of chunks, a Kogge-Stone scan across the
-// warp combines the runs, then each thread re-walks its run writing carries.
-// The maps are N x N with N the op's state size (GB300's FP64 rate is a small
-// fraction of FP32, so the scan does no f64 work for absent components).
-template <int N>
-struct Aff {
-    double m[N][N];
-    double b[N];
-};
-
-template <int N>
-__device__ __forceinline__ void aff_identity(Aff<N>& a) {
-#pragma unroll
-    for (int r = 0; r < N; ++r) {
-#pragma unroll
-        for (int c = 0; c < N; ++c) a.m[r][c] = r == c ? 1.0 : 0.0;
-        a.b[r] = 0.0;
-    }
-}
+// the affine chunk maps S -> M_k S + b_k.  One warp per lane: each thread
+// composes a contiguous run of chunks, a Kogge-Stone scan across the warp
+// combines the runs, then each thread re-walks its run writing carries.  The
+// maps are N x N with N the op's state size, in double-single arithmetic.
 // Structure of an op's transition matrix: every product of such matrices
 // keeps it, so the f64 work skips the structural zeros (GB300's FP64 rate
 // makes them count).  0 = full, 1 = lower triangular (DEMA, TEMA cascades),
@@ -1295,21 +1338,35 @@ template <class Op, class = void> struct ShapeOf { static constexpr int v = 0; }
 template <class Op> struct ShapeOf<Op, std::void_t<decltype(Op::kShape)>> { static constexpr int v = Op::kShape; };
 __host__ __device__ constexpr bool shape_nz(int sh, int r, int c) { return sh == 0 || (sh == 1 ? c <= r : c == r); }
 
-// returns second o first (apply `first`, then `second`)
-template <int N, int SH = 0>
-__device__ __forceinline__ Aff<N> aff_then(const Aff<N>& first, const Aff<N>& second) {
-    Aff<N> o;
+template <int N>
+struct AffD {
+    D2 m[N][N];
+    D2 b[N];
+};
+template <int N>
+__device__ __forceinline__ void affd_identity(AffD<N>& a) {
 #pragma unroll
     for (int r = 0; r < N; ++r) {
-        double br = second.b[r];
+#pragma unroll
+        for (int c = 0; c < N; ++c) a.m[r][c] = {r == c ? 1.f : 0.f, 0.f};
+        a.b[r] = {0.f, 0.f};
+    }
+}
+// second o first (apply `first`, then `second`)
+template <int N, int SH>
+__device__ __forceinline__ AffD<N> affd_then(const AffD<N>& first, const AffD<N>& second) {
+    AffD<N> o;
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+        D2 br = second.b[r];
 #pragma unroll
         for (int c = 0; c < N; ++c) {
-            double mrc = 0.0;
+            D2 mrc = {0.f, 0.f};
             if (shape_nz(SH, r, c)) {
 #pragma unroll
                 for (int q = 0; q < N; ++q)
-                    if (shape_nz(SH, r, q) && shape_nz(SH, q, c)) mrc = fma(second.m[r][q], first.m[q][c], mrc);
-                br = fma(second.m[r][c], first.b[c], br);
+                    if (shape_nz(SH, r, q) && shape_nz(SH, q, c)) mrc = d2_fma(second.m[r][q], first.m[q][c], mrc);
+                br = d2_fma(second.m[r][c], first.b[c], br);
             }
             o.m[r][c] = mrc;
         }
@@ -1317,56 +1374,59 @@ __device__ __forceinline__ Aff<N> aff_then(const Aff<N>& first, const Aff<N>& se
     }
     return o;
 }
-template <int N, int SH = 0>
-__device__ __forceinline__ Aff<N> aff_shfl_up(const Aff<N>& a, int d) {
-    Aff<N> o;
+template <int N, int SH>
+__device__ __forceinline__ AffD<N> affd_shfl_up(const AffD<N>& a, int d) {
+    AffD<N> o;
 #pragma unroll
     for (int r = 0; r < N; ++r) {
 #pragma unroll
-        for (int c = 0; c < N; ++c) o.m[r][c] = shape_nz(SH, r, c) ? __shfl_up_sync(0xffffffffu, a.m[r][c], d) : 0.0;
-        o.b[r] = __shfl_up_sync(0xffffffffu, a.b[r], d);
+        for (int c = 0; c < N; ++c) o.m[r][c] = shape_nz(SH, r, c) ? d2_shfl_up(a.m[r][c], d) : D2{0.f, 0.f};
+        o.b[r] = d2_shfl_up(a.b[r], d);
     }
     return o;
 }
 
-// M^n of the op's transition, column by column from propagate.
+// M^n of the op's transition (n steps), column by column from propagate.
 template <class Op>
-__device__ void trans_pow(double n, int p, double (&m)[Op::NS][Op::NS]) {
+__device__ void trans_pow(long long n, int p, D2 (&m)[Op::NS][Op::NS]) {
     constexpr int N = Op::NS;
+    D2 al, b;
+    Op::coef(p, al, b);
+    const D2 an = d2_pow(b, n), nd = d2_from_ll(n);
 #pragma unroll
     for (int c = 0; c < N; ++c) {
-        double e[3] = {0.0, 0.0, 0.0};
-        e[c] = 1.0;
-        Op::propagate(e, n, p);
+        D2 e[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        e[c] = {1.f, 0.f};
+        Op::propagate(e, nd, al, an, p);
 #pragma unroll
         for (int r = 0; r < N; ++r) m[r][c] = e[r];
     }
 }
 
+// The map of one chunk from its AGG record (state, applied steps or marker).
 template <class Op>
-__device__ void chunk_map(const float4 g, int p, int chunk, const double (&ml)[Op::NS][Op::NS],
-                          Aff<Op::NS>& a) {
+__device__ void chunk_map(const float4 g, int p, int chunk, const D2 (&ml)[Op::NS][Op::NS], AffD<Op::NS>& a) {
     constexpr int N = Op::NS;
     if (g.w == kBeforeSeed) {
-        aff_identity(a);
+        affd_identity(a);
         return;
     }
     if (g.w == kAbsolute) {
 #pragma unroll
         for (int r = 0; r < N; ++r)
 #pragma unroll
-            for (int c = 0; c < N; ++c) a.m[r][c] = 0.0;
+            for (int c = 0; c < N; ++c) a.m[r][c] = {0.f, 0.f};
     } else if (g.w == (float)chunk) {
 #pragma unroll
         for (int r = 0; r < N; ++r)
 #pragma unroll
             for (int c = 0; c < N; ++c) a.m[r][c] = ml[r][c];
     } else {
-        trans_pow<Op>((double)g.w, p, a.m);
+        trans_pow<Op>((long long)g.w, p, a.m);
     }
     const float gb[3] = {g.x, g.y, g.z};
 #pragma unroll
-    for (int r = 0; r < N; ++r) a.b[r] = gb[r];
+    for (int r = 0; r < N; ++r) a.b[r] = {gb[r], 0.f};
 }
 
 // Carry-in state of every (lane, chunk): one warp per lane, each thread a
@@ -1375,9 +1435,9 @@ __device__ void chunk_map(const float4 g, int p, int chunk, const double (&ml)[O
 // the maps chunk by chunk and writes the carries.  Full chunks share one
 // linear part M (the transition of `chunk` steps), so a run of them only
 // updates the offset (b <- M b + agg) and its power M^cnt is applied once
-// (trans_pow of cnt * chunk steps) when another map follows or the run ends:
-// the f64 work per chunk is a matrix-vector product, not a matrix product.
-// The chunk records are read eight at a time, ahead of the dependent math.
+// when another map follows or the run ends: the work per chunk is a
+// matrix-vector product.  The chunk records are read eight at a time, ahead
+// of the dependent math.
 template <class Op>
 __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
     constexpr int N = Op::NS;
@@ -1392,42 +1452,26 @@ __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
     const int per = (n_chunks + 31) / 32;
     const int k0 = min(lane * per, n_chunks), k1 = min(k0 + per, n_chunks);
     const float full = (float)a.chunk;
-    // transitions of one full chunk (ml) and of `per` full chunks (mper):
-    // lanes 0 and 1 compute them (the f64 powers are costly at GB300's FP64
-    // rate), the warp shares them
-    double ml[N][N], mper[N][N];
-    {
-        double t[N][N];
-#pragma unroll
-        for (int r = 0; r < N; ++r)
-#pragma unroll
-            for (int c = 0; c < N; ++c) t[r][c] = 0.0;
-        if (lane < 2) trans_pow<Op>(lane == 0 ? (double)a.chunk : (double)per * a.chunk, p, t);
-#pragma unroll
-        for (int r = 0; r < N; ++r)
-#pragma unroll
-            for (int c = 0; c < N; ++c) {
-                ml[r][c] = shape_nz(SH, r, c) ? __shfl_sync(0xffffffffu, t[r][c], 0) : 0.0;
-                mper[r][c] = shape_nz(SH, r, c) ? __shfl_sync(0xffffffffu, t[r][c], 1) : 0.0;
-            }
-    }
+    D2 ml[N][N], mper[N][N];  // transitions of one and of `per` full chunks
+    trans_pow<Op>((long long)a.chunk, p, ml);
+    trans_pow<Op>((long long)per * a.chunk, p, mper);
     // v <- M v + g (the map of a full chunk applied to a vector)
-    auto full_step = [&](double (&v)[N], const float4 g) {
+    auto full_step = [&](D2 (&v)[N], const float4 g) {
         const float gb[3] = {g.x, g.y, g.z};
-        double t[N];
+        D2 t[N];
 #pragma unroll
         for (int r = 0; r < N; ++r) {
-            double x = gb[r];
+            D2 x = {gb[r], 0.f};
 #pragma unroll
             for (int c = 0; c < N; ++c)
-                if (shape_nz(SH, r, c)) x = fma(ml[r][c], v[c], x);
+                if (shape_nz(SH, r, c)) x = d2_fma(ml[r][c], v[c], x);
             t[r] = x;
         }
 #pragma unroll
         for (int r = 0; r < N; ++r) v[r] = t[r];
     };
-    Aff<N> run;
-    aff_identity(run);
+    AffD<N> run;
+    affd_identity(run);
     int cnt = 0;          // full chunks whose linear part is not yet in run.m
     bool m_zero = false;  // run.m == 0 (after an absolute chunk): powers leave it 0
     auto flush = [&]() {
@@ -1435,25 +1479,25 @@ __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
             cnt = 0;
             return;
         }
-        double pw[N][N];
+        D2 pw[N][N];
         if (cnt == per) {
 #pragma unroll
             for (int r = 0; r < N; ++r)
 #pragma unroll
                 for (int c = 0; c < N; ++c) pw[r][c] = mper[r][c];
         } else {
-            trans_pow<Op>((double)cnt * a.chunk, p, pw);
+            trans_pow<Op>((long long)cnt * a.chunk, p, pw);
         }
-        double m2[N][N];  // run.m <- M^cnt run.m (the offset is already current)
+        D2 m2[N][N];  // run.m <- M^cnt run.m (the offset is already current)
 #pragma unroll
         for (int r = 0; r < N; ++r)
 #pragma unroll
             for (int c = 0; c < N; ++c) {
-                double v = 0.0;
+                D2 v = {0.f, 0.f};
                 if (shape_nz(SH, r, c))
 #pragma unroll
                     for (int q = 0; q < N; ++q)
-                        if (shape_nz(SH, r, q) && shape_nz(SH, q, c)) v = fma(pw[r][q], run.m[q][c], v);
+                        if (shape_nz(SH, r, q) && shape_nz(SH, q, c)) v = d2_fma(pw[r][q], run.m[q][c], v);
                 m2[r][c] = v;
             }
 #pragma unroll
@@ -1475,9 +1519,9 @@ __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
                 ++cnt;
             } else {
                 flush();
-                Aff<N> ak;
+                AffD<N> ak;
                 chunk_map<Op>(gv[u], p, a.chunk, ml, ak);
-                run = aff_then<N, SH>(run, ak);
+                run = affd_then<N, SH>(run, ak);
                 if (gv[u].w == kAbsolute) m_zero = true;
             }
         }
@@ -1485,12 +1529,12 @@ __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
     flush();
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-        const Aff<N> up = aff_shfl_up<N, SH>(run, d);
-        if (lane >= d) run = aff_then<N, SH>(up, run);
+        const AffD<N> up = affd_shfl_up<N, SH>(run, d);
+        if (lane >= d) run = affd_then<N, SH>(up, run);
     }
-    Aff<N> ex = aff_shfl_up<N, SH>(run, 1);
-    if (lane == 0) aff_identity(ex);
-    double S[N];  // state at the start of chunk k0
+    AffD<N> ex = affd_shfl_up<N, SH>(run, 1);
+    if (lane == 0) affd_identity(ex);
+    D2 S[N];  // state at the start of chunk k0
 #pragma unroll
     for (int r = 0; r < N; ++r) S[r] = ex.b[r];
     for (int kb = k0; kb < k1; kb += kB) {
@@ -1503,22 +1547,22 @@ __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
             const int k = kb + u;
             if (k >= k1) break;
             float4 cv = make_float4(0.f, 0.f, 0.f, 0.f);
-            cv.x = (float)S[0];
-            if (N > 1) cv.y = (float)S[N > 1 ? 1 : 0];
-            if (N > 2) cv.z = (float)S[N > 2 ? 2 : 0];
+            cv.x = S[0].hi + S[0].lo;
+            if (N > 1) cv.y = S[N > 1 ? 1 : 0].hi + S[N > 1 ? 1 : 0].lo;
+            if (N > 2) cv.z = S[N > 2 ? 2 : 0].hi + S[N > 2 ? 2 : 0].lo;
             carry[(size_t)k * a.n_lanes + li] = cv;
             if (gv[u].w == full) {
                 full_step(S, gv[u]);
             } else {
-                Aff<N> ak;
+                AffD<N> ak;
                 chunk_map<Op>(gv[u], p, a.chunk, ml, ak);
-                double t[N];
+                D2 t[N];
 #pragma unroll
                 for (int r = 0; r < N; ++r) {
-                    double v = ak.b[r];
+                    D2 v = ak.b[r];
 #pragma unroll
                     for (int c = 0; c < N; ++c)
-                        if (shape_nz(SH, r, c)) v = fma(ak.m[r][c], S[c], v);
+                        if (shape_nz(SH, r, c)) v = d2_fma(ak.m[r][c], S[c], v);
                     t[r] = v;
                 }
 #pragma unroll

@@ -191,16 +191,17 @@ __global__ void __launch_bounds__(256) k_agg_weights(RecurTcArgs a, Wts w) {
 // One block per column j (chunk g0 + j % nc; RSI: gains for j < nc, losses
 // after): the chunk's L inputs, centred on the chunk's first value (EMAs) and
 // scaled by a power of two, split hi / lo.  done[chunk] = every input finite.
-// The column is staged in shared memory (L <= kPackSmemL; longer chunks read
-// it twice from global memory) and written one core-matrix row (8
-// K-consecutive elements, 16 bytes per part) per thread and store.
+// The column's inputs are staged in shared memory (L <= kPackSmemL, 16-byte
+// loads; longer chunks read them from global memory in both passes) and the
+// split values written one core-matrix row (8 K-consecutive elements, 16
+// bytes per part) per thread and store.
 constexpr int kPackSmemL = 8192;
 
 __global__ void __launch_bounds__(256) k_agg_pack_x(RecurTcArgs a, Ws w) {
     const RecurTcGeo& g = a.geo;
     const int j = blockIdx.x;
     const int L = a.L;
-    extern __shared__ float colv[];  // L values when staged
+    extern __shared__ float colv[];  // L + 1 inputs when staged
     __shared__ float red[8];
     const int ngrp = L >> 3;
     auto store_row = [&](int kg, const float (&v)[8], float ref, float sc, bool fin) {
@@ -227,27 +228,42 @@ __global__ void __launch_bounds__(256) k_agg_pack_x(RecurTcArgs a, Ws w) {
     const int c = a.g0 + j % a.nc, half = j / a.nc;
     const int c0 = a.chunk0 + (c - 1) * L;  // c >= 1
     const bool staged = L <= kPackSmemL;
+    // staged: colv[0] = x[c0 - 1] (RSI), colv[1 + k] = x[c0 + k], loaded 16
+    // bytes at a time when the chunk start is 16-byte aligned
+    const float* src = a.x + c0;
+    if (staged) {
+        if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+            for (int i = threadIdx.x; i < (L >> 2); i += blockDim.x) {
+                const float4 v = __ldg(reinterpret_cast<const float4*>(src) + i);
+                colv[1 + 4 * i] = v.x;
+                colv[2 + 4 * i] = v.y;
+                colv[3 + 4 * i] = v.z;
+                colv[4 + 4 * i] = v.w;
+            }
+        } else {
+            for (int k = threadIdx.x; k < L; k += blockDim.x) colv[1 + k] = __ldg(src + k);
+        }
+        if (threadIdx.x == 0) colv[0] = rsi ? __ldg(src - 1) : 0.f;
+        __syncthreads();
+    }
+    auto xat = [&](int k) { return staged ? colv[1 + k] : __ldg(src + k); };  // k >= -1
     // EMAs: the input; RSI: the gain (half 0) or loss (half 1) of the
     // difference to the previous bar.  `bad`: a non-finite input / difference.
     auto value = [&](int k, int& bad) {
-        const float v = __ldg(a.x + c0 + k);
+        const float v = xat(k);
         if (!rsi) {
             bad |= !isfinite(v);
             return v;
         }
-        const float d = v - __ldg(a.x + c0 + k - 1);
+        const float d = v - xat(k - 1);
         bad |= !isfinite(d);
         return half == 0 ? (d > 0.f ? d : 0.f) : (d < 0.f ? -d : 0.f);
     };
-    const float ref = rsi ? 0.f : __ldg(a.x + c0);
+    const float ref = rsi ? 0.f : xat(0);
     float mx = 0.f;
     int bad = 0;
 #pragma unroll 4
-    for (int k = threadIdx.x; k < L; k += blockDim.x) {
-        const float v = value(k, bad);
-        if (staged) colv[k] = v;
-        mx = fmaxf(mx, fabsf(v - ref));
-    }
+    for (int k = threadIdx.x; k < L; k += blockDim.x) mx = fmaxf(mx, fabsf(value(k, bad) - ref));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
@@ -262,7 +278,7 @@ __global__ void __launch_bounds__(256) k_agg_pack_x(RecurTcArgs a, Ws w) {
         float v[8];
         int unused = 0;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) v[q] = staged ? colv[kg * 8 + q] : (fin ? value(kg * 8 + q, unused) : 0.f);
+        for (int q = 0; q < 8; ++q) v[q] = fin ? value(kg * 8 + q, unused) : 0.f;
         store_row(kg, v, ref, sc, fin);
     }
     if (threadIdx.x == 0) {
@@ -470,7 +486,7 @@ vta_status launch_recur_agg_tc(const RecurTcArgs& a, size_t smem_optin, cudaStre
         k_agg_weights<<<(g.rows + 7) / 8, 256, 0, st>>>(a, wt);
         VTA_TRY(check_launch("k_agg_weights"));
     }
-    k_agg_pack_x<<<g.npad, 256, a.L <= kPackSmemL ? (size_t)a.L * sizeof(float) : 0, st>>>(a, w);
+    k_agg_pack_x<<<g.npad, 256, a.L <= kPackSmemL ? (size_t)(a.L + 1) * sizeof(float) : 0, st>>>(a, w);
     VTA_TRY(check_launch("k_agg_pack_x"));
     static int smem_set_dev = -1;  // the attribute is per device; set it once
     int dev = 0;
