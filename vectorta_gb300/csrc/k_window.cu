@@ -235,9 +235,8 @@ static_assert(kPwComboGroup <= kPwThreads, "one thread per combo of a group");
 
 template <int K>
 __device__ void fast_tile(const PrefixWinArgs& a, const float2* s1, const float2* s2, int pmax, int t0,
-                          float r0) {
+                          float r0, int cb, int ce, float4* cc) {
     static_assert(kPwPer == 4, "fast_outputs is written for 4 outputs per thread");
-    __shared__ float4 cc[kPwComboGroup];
     float2 q1[4], q2[4];
     float xt[4];
     const int tid = threadIdx.x;
@@ -250,8 +249,8 @@ __device__ void fast_tile(const PrefixWinArgs& a, const float2* s1, const float2
         xt[k] = (K == WK_ZSCORE && t < a.n) ? __fsub_rn(__ldg(a.x + t), r0) : 0.f;  // y(t)
     }
     const bool tail = t0 + kPwTile > a.n;
-    for (int g0 = 0; g0 < a.n_combos; g0 += kPwComboGroup) {
-        const int gn = min(kPwComboGroup, a.n_combos - g0);
+    for (int g0 = cb; g0 < ce; g0 += kPwComboGroup) {
+        const int gn = min(kPwComboGroup, ce - g0);
         __syncthreads();  // the previous group's constants are no longer read
         if (tid < gn) {
             const int c = g0 + tid;
@@ -275,9 +274,14 @@ __device__ void fast_tile(const PrefixWinArgs& a, const float2* s1, const float2
     }
 }
 
+// Block (tile, g): the tile's kPwTile times for the combos [g cpb, (g + 1)
+// cpb); a tile's prefix is rebuilt by each of its combo groups (a few percent
+// of a group's work), so the grid fills the GPU in whole waves.
 __global__ void __launch_bounds__(kPwThreads)
-k_prefix_window_batch(PrefixWinArgs a, int pmax) {
+k_prefix_window_batch(PrefixWinArgs a, int pmax, int cpb) {
     extern __shared__ float2 psm[];
+    __shared__ float4 cc[kPwComboGroup];  // combo constants of the fast path
+    const int cb = blockIdx.y * cpb, ce = min(a.n_combos, cb + cpb);
     __shared__ DS wsum1[kPwThreads / 32], wsum2[kPwThreads / 32];
     const int t0 = blockIdx.x * kPwTile;
     const int span = kPwTile + pmax;
@@ -373,10 +377,10 @@ k_prefix_window_batch(PrefixWinArgs a, int pmax) {
             }
             __syncthreads();
             switch (a.kind) {
-                case WK_SMA: fast_tile<WK_SMA>(a, s1, s2, pmax, t0, r0); break;
-                case WK_STDDEV: fast_tile<WK_STDDEV>(a, s1, s2, pmax, t0, r0); break;
-                case WK_ZSCORE: fast_tile<WK_ZSCORE>(a, s1, s2, pmax, t0, r0); break;
-                default: fast_tile<WK_BB>(a, s1, s2, pmax, t0, r0); break;
+                case WK_SMA: fast_tile<WK_SMA>(a, s1, s2, pmax, t0, r0, cb, ce, cc); break;
+                case WK_STDDEV: fast_tile<WK_STDDEV>(a, s1, s2, pmax, t0, r0, cb, ce, cc); break;
+                case WK_ZSCORE: fast_tile<WK_ZSCORE>(a, s1, s2, pmax, t0, r0, cb, ce, cc); break;
+                default: fast_tile<WK_BB>(a, s1, s2, pmax, t0, r0, cb, ce, cc); break;
             }
             return;
         }
@@ -393,7 +397,7 @@ k_prefix_window_batch(PrefixWinArgs a, int pmax) {
         p2t[k] = two ? s2[l] : z;
         xt[k] = (a.kind == WK_ZSCORE && t < a.n) ? __fsub_rn(a.x[t], r0) : 0.f;
     }
-    for (int c = 0; c < a.n_combos; ++c) {
+    for (int c = cb; c < ce; ++c) {
         const int p = a.periods[c];
         const int warm = a.first + p - 1;
         const int poison = min(first_nan, first_inf < a.n ? first_inf + p : a.n);
@@ -502,7 +506,7 @@ constexpr int kMmThreads = 512;
 // t = t0 + tid + k * THREADS; the closes are read once for all combos.
 template <int KIND, int PER, int THREADS>
 __device__ __forceinline__ void minmax_clean(const MinMaxArgs& a, const float* mx, const float* mn,
-                                             const int4* ctab, int t0, int tile) {
+                                             const int4* ctab, int t0, int tile, int cb, int ce) {
     const int tid = threadIdx.x;
     const bool full = t0 + tile <= a.n;
     float cl[PER];
@@ -512,7 +516,7 @@ __device__ __forceinline__ void minmax_clean(const MinMaxArgs& a, const float* m
         cl[k] = (KIND == MM_WILLR && t < a.n) ? __ldg(a.c + t) : 0.f;
     }
     const int ie0 = tid + a.pmax - 1;  // local index of t0 + tid
-    for (int c = 0; c < a.n_combos; ++c) {
+    for (int c = cb; c < ce; ++c) {
         const int4 ct = ctab[c];
         const size_t o = (size_t)c * a.n + t0 + tid;
         float* r0 = a.out0 + o;
@@ -552,10 +556,14 @@ __device__ __forceinline__ void minmax_clean(const MinMaxArgs& a, const float* m
 // THREADS threads per block (the autotuner's choice with the tile): fewer
 // threads give each more times per combo, which spreads the combo's table and
 // pointer set-up over more outputs.
+// Block (tile, g): the tile's times for the combos [g cpb, (g + 1) cpb); each
+// combo group rebuilds the tile's table (a few combos' worth of work), so the
+// grid fills the GPU in whole waves.
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS)
-k_minmax_batch(MinMaxArgs a, int tile, int levels) {
+k_minmax_batch(MinMaxArgs a, int tile, int levels, int cpb) {
     extern __shared__ float sm[];
+    const int cb = blockIdx.y * cpb, ce = min(a.n_combos, cb + cpb);
     const int t0 = blockIdx.x * tile;
     const int lo_i = t0 - (a.pmax - 1);  // global index of smem slot 0
     const int nloc = tile + a.pmax - 1;
@@ -568,7 +576,7 @@ k_minmax_batch(MinMaxArgs a, int tile, int levels) {
     // t - p + 1 and t - 2^k + 1 relative to the local index of t)
     const size_t ctab_at = ((size_t)2 * levels * nloc + 2 * ((size_t)nloc + 1) + 3) & ~size_t(3);  // 16-byte aligned
     int4* ctab = reinterpret_cast<int4*>(reinterpret_cast<int*>(sm) + ctab_at);
-    for (int c = threadIdx.x; c < a.n_combos; c += blockDim.x) {
+    for (int c = cb + threadIdx.x; c < ce; c += blockDim.x) {
         const int p = a.periods[c];
         const int k = 31 - __clz(p);
         ctab[c] = make_int4(p, a.first + p - 1, k * nloc - p + 1, k * nloc - (1 << k) + 1);
@@ -596,6 +604,7 @@ k_minmax_batch(MinMaxArgs a, int tile, int levels) {
     }
     if (threadIdx.x == 0) { bad_nan[0] = 0; bad_fin[0] = 0; }
     const bool clean = !__syncthreads_or(any_bad);
+    if (clean && a.skip_clean) return;  // k_minmax_ap wrote this tile
     // prefix counts (single warp, sequential per lane-strided segments)
     if (!clean && threadIdx.x < 32) {
         const int lane = threadIdx.x;
@@ -630,15 +639,15 @@ k_minmax_batch(MinMaxArgs a, int tile, int levels) {
     if (clean && tile >= THREADS && tile <= 8 * THREADS) {
         const int per = tile / THREADS;  // 1, 2, 4 or 8
         if (a.kind == MM_DONCHIAN) {
-            if (per == 1) minmax_clean<MM_DONCHIAN, 1, THREADS>(a, mx, mn, ctab, t0, tile);
-            else if (per == 2) minmax_clean<MM_DONCHIAN, 2, THREADS>(a, mx, mn, ctab, t0, tile);
-            else if (per == 4) minmax_clean<MM_DONCHIAN, 4, THREADS>(a, mx, mn, ctab, t0, tile);
-            else minmax_clean<MM_DONCHIAN, 8, THREADS>(a, mx, mn, ctab, t0, tile);
+            if (per == 1) minmax_clean<MM_DONCHIAN, 1, THREADS>(a, mx, mn, ctab, t0, tile, cb, ce);
+            else if (per == 2) minmax_clean<MM_DONCHIAN, 2, THREADS>(a, mx, mn, ctab, t0, tile, cb, ce);
+            else if (per == 4) minmax_clean<MM_DONCHIAN, 4, THREADS>(a, mx, mn, ctab, t0, tile, cb, ce);
+            else minmax_clean<MM_DONCHIAN, 8, THREADS>(a, mx, mn, ctab, t0, tile, cb, ce);
         } else {
-            if (per == 1) minmax_clean<MM_WILLR, 1, THREADS>(a, mx, mn, ctab, t0, tile);
-            else if (per == 2) minmax_clean<MM_WILLR, 2, THREADS>(a, mx, mn, ctab, t0, tile);
-            else if (per == 4) minmax_clean<MM_WILLR, 4, THREADS>(a, mx, mn, ctab, t0, tile);
-            else minmax_clean<MM_WILLR, 8, THREADS>(a, mx, mn, ctab, t0, tile);
+            if (per == 1) minmax_clean<MM_WILLR, 1, THREADS>(a, mx, mn, ctab, t0, tile, cb, ce);
+            else if (per == 2) minmax_clean<MM_WILLR, 2, THREADS>(a, mx, mn, ctab, t0, tile, cb, ce);
+            else if (per == 4) minmax_clean<MM_WILLR, 4, THREADS>(a, mx, mn, ctab, t0, tile, cb, ce);
+            else minmax_clean<MM_WILLR, 8, THREADS>(a, mx, mn, ctab, t0, tile, cb, ce);
         }
         return;
     }
@@ -647,10 +656,10 @@ k_minmax_batch(MinMaxArgs a, int tile, int levels) {
         if (t >= a.n) break;
         const float cl = a.kind == MM_WILLR ? a.c[t] : 0.f;
         const int ie = t - lo_i;  // local index of t
-        float* o0 = a.out0 + t;
-        float* o1 = a.out1 + t;
-        float* o2 = a.out2 + t;
-        for (int c = 0; c < a.n_combos; ++c, o0 += a.n, o1 += a.n, o2 += a.n) {
+        float* o0 = a.out0 + (size_t)cb * a.n + t;
+        float* o1 = a.out1 + (size_t)cb * a.n + t;
+        float* o2 = a.out2 + (size_t)cb * a.n + t;
+        for (int c = cb; c < ce; ++c, o0 += a.n, o1 += a.n, o2 += a.n) {
             const int4 ct = ctab[c];
             const int p = ct.x;
             float r0 = qnan(), r1 = qnan(), r2 = qnan();
@@ -679,6 +688,118 @@ k_minmax_batch(MinMaxArgs a, int tile, int levels) {
             if (a.kind == MM_DONCHIAN) {
                 *o1 = r1;
                 *o2 = r2;
+            }
+        }
+    }
+}
+
+// ---- arithmetic-progression sweeps ----------------------------------------
+// Periods p_c = p_0 + c d (ascending, constant step d: the crate's range
+// grids).  The window of combo c is combo c - 1's window extended by the d
+// bars before it, so hmax_c(t) = max(hmax_{c-1}(t), M_d(t - p_{c-1})) with M_d
+// the d-bar sliding maximum, built once per tile in shared memory (likewise
+// the lows).  Per output: two shared-memory loads and two min/max (exact, so
+// the same values as the sparse-table lookups) instead of four loads and the
+// per-combo table set-up.  The first combo's window comes from p_0 mod d
+// single bars and p_0 / d blocks of M_d.  Clean tiles only (the same test as
+// k_minmax_batch); k_minmax_batch, launched after with skip_clean, computes
+// the others.
+template <int KIND, int THREADS, int PER>
+__global__ void __launch_bounds__(THREADS) k_minmax_ap(MinMaxArgs a, int tile) {
+    extern __shared__ float sm[];
+    const int t0 = blockIdx.x * tile;
+    const int lo_i = t0 - (a.pmax - 1);  // global index of slot 0
+    const int nloc = tile + a.pmax - 1;
+    const int d = a.ap_d;
+    float* xh = sm;
+    float* xl = xh + nloc;
+    float* mh = xl + nloc;
+    float* ml = mh + nloc;
+    int any_bad = 0;
+    for (int i = threadIdx.x; i < nloc; i += THREADS) {
+        const int g = lo_i + i;
+        float hv = -INFINITY, lv = INFINITY;
+        if (g >= 0 && g < a.n) {
+            const float h = __ldg(a.h + g), l = __ldg(a.l + g);
+            if (!(isnan(h) || isnan(l))) {
+                hv = h;
+                lv = l;
+            }
+            if (g >= a.first && !(isfinite(h) && isfinite(l))) any_bad = 1;
+            if (KIND == MM_WILLR && g >= a.first && i >= a.pmax - 1 && isnan(__ldg(a.c + g))) any_bad = 1;
+        }
+        xh[i] = hv;
+        xl[i] = lv;
+    }
+    if (__syncthreads_or(any_bad)) return;
+    // M_d: the d-bar sliding max / min ending at slot i (i >= d - 1)
+    for (int i = threadIdx.x; i < nloc; i += THREADS) {
+        float hv = -INFINITY, lv = INFINITY;
+        if (i >= d - 1)
+            for (int j = 0; j < d; ++j) {
+                hv = fmaxf(hv, xh[i - j]);
+                lv = fminf(lv, xl[i - j]);
+            }
+        mh[i] = hv;
+        ml[i] = lv;
+    }
+    __syncthreads();
+    const int tid = threadIdx.x;
+    const bool full = t0 + tile <= a.n;
+    const int p0 = __ldg(a.periods);
+    const int r = p0 % d, nb = p0 / d;
+    float hm[PER], lm[PER], cl[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int t = t0 + tid + k * THREADS;
+        const int ie = tid + k * THREADS + a.pmax - 1;  // slot of t
+        cl[k] = (KIND == MM_WILLR && t < a.n) ? __ldg(a.c + t) : 0.f;
+        float h = -INFINITY, l = INFINITY;
+        for (int i = 0; i < r; ++i) {
+            h = fmaxf(h, xh[ie - i]);
+            l = fminf(l, xl[ie - i]);
+        }
+        for (int j = 0; j < nb; ++j) {
+            h = fmaxf(h, mh[ie - r - j * d]);
+            l = fminf(l, ml[ie - r - j * d]);
+        }
+        hm[k] = h;
+        lm[k] = l;
+    }
+    const int ie0 = tid + a.pmax - 1;
+    int p = p0;
+    for (int c = 0; c < a.n_combos; ++c, p += d) {
+        if (c > 0) {
+            const int back = ie0 - (p - d);  // slot of t - p_{c-1} for k = 0
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                hm[k] = fmaxf(hm[k], mh[back + k * THREADS]);
+                lm[k] = fminf(lm[k], ml[back + k * THREADS]);
+            }
+        }
+        const int warm = a.first + p - 1;
+        const bool all_valid = full && t0 >= warm;
+        const size_t o = (size_t)c * a.n + t0 + tid;
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int t = t0 + tid + k * THREADS;
+            if (!all_valid && t >= a.n) break;
+            float v0 = qnan(), v1 = qnan(), v2 = qnan();
+            if (all_valid || t >= warm) {
+                if (KIND == MM_DONCHIAN) {
+                    v0 = hm[k];
+                    v2 = lm[k];
+                    v1 = fmaf(hm[k] - lm[k], 0.5f, lm[k]);
+                } else {
+                    const float den = hm[k] - lm[k];
+                    // finite prices: the fast divide is within 2 ulp
+                    v0 = den == 0.f ? 0.f : fmaf(-100.f, __fdividef(hm[k] - cl[k], den), 0.f);
+                }
+            }
+            a.out0[o + k * THREADS] = v0;
+            if (KIND == MM_DONCHIAN) {
+                a.out1[o + k * THREADS] = v1;
+                a.out2[o + k * THREADS] = v2;
             }
         }
     }
@@ -840,6 +961,32 @@ __global__ void k_percentile(PnrArgs a) {
 
 }  // namespace
 
+// Combos per block for a grid of `tiles` time tiles x combo groups: the
+// grid in (nearly) whole waves of the kernel's resident blocks, counting a
+// group's per-tile set-up (prefix or table rebuild) as ~4 combos of work.
+template <class K>
+static int wave_combos(K kern, int threads, size_t smem, long long tiles, int n_combos) {
+    int per_sm = 0, dev = 0, sms = kNumSMs;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long slots = (long long)std::max(1, per_sm) * sms;
+    int best_g = 1;
+    double best = 1e300;
+    for (int g = 1; g <= 16 && g <= n_combos; ++g) {
+        const int cpb = (n_combos + g - 1) / g;
+        const long long blocks = tiles * ((n_combos + cpb - 1) / cpb);
+        const double cost = (double)((blocks + slots - 1) / slots) * (cpb + 4);
+        if (cost < best * 0.98) {
+            best = cost;
+            best_g = g;
+        }
+    }
+    return (n_combos + best_g - 1) / best_g;
+}
+
 vta_status launch_prefix_window_batch(const PrefixWinArgs& a, int pmax, size_t smem_optin, cudaStream_t st) {
     const size_t smem = (size_t)(kPwTile + pmax) * sizeof(float2) * (a.kind == WK_SMA ? 1 : 2);
     if (smem + 2 * (kPwThreads / 32) * sizeof(DS) > smem_optin)
@@ -850,8 +997,11 @@ vta_status launch_prefix_window_batch(const PrefixWinArgs& a, int pmax, size_t s
         VTA_TRY(check_launch("k_first_bad"));
     }
     VTA_CUDA_TRY(cudaFuncSetAttribute(k_prefix_window_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const long long tiles = ceil_div(a.n, kPwTile);
+    const int cpb = wave_combos(k_prefix_window_batch, kPwThreads, smem, tiles, a.n_combos);
     ktimer_begin(st);
-    k_prefix_window_batch<<<ceil_div(a.n, kPwTile), kPwThreads, smem, st>>>(a, pmax);
+    k_prefix_window_batch<<<dim3((unsigned)tiles, (unsigned)ceil_div(a.n_combos, cpb)), kPwThreads, smem, st>>>(a, pmax,
+                                                                                                              cpb);
     ktimer_end(st);
     return check_launch("k_prefix_window_batch");
 }
@@ -873,20 +1023,52 @@ static size_t minmax_smem(const MinMaxArgs& a, int tile, int levels) {
     return nloc * levels * 2 * sizeof(float) + (2 * (nloc + 1) + 4) * sizeof(int) + (size_t)a.n_combos * sizeof(int4);
 }
 
-// Candidates encoded as tile | threads << 16.
+// Candidates encoded as tile | threads << 16 | split << 28 (split: combo
+// groups per tile from the wave model; without it one block per tile).
+constexpr int kMmSplitBit = 1 << 28;
+// bit 29: the progression kernel on clean tiles (tile kMmApTile), the
+// sparse-table kernel on the rest
+constexpr int kMmApBit = 1 << 29;
+constexpr int kMmApThreads = 256, kMmApPer = 4, kMmApTile = kMmApThreads * kMmApPer;
+static bool minmax_ap_ok(const MinMaxArgs& a, size_t smem_optin) {
+    const int levels = 32 - __builtin_clz((unsigned)a.pmax);
+    const size_t nloc = (size_t)kMmApTile + a.pmax - 1;
+    return a.ap_d >= 1 && a.ap_d <= 64 && a.n_combos >= 2 && 4 * nloc * sizeof(float) <= smem_optin &&
+           minmax_smem(a, kMmApTile, levels) <= smem_optin;
+}
+bool minmax_uses_progression(const MinMaxArgs& a, size_t smem_optin) {
+    return (a.tile_hint == 0 || (a.tile_hint & kMmApBit)) && minmax_ap_ok(a, smem_optin);
+}
 std::vector<int> minmax_tile_candidates(const MinMaxArgs& a, size_t smem_optin) {
     const int levels = 32 - __builtin_clz((unsigned)a.pmax);
     std::vector<int> c;
-    const int cfg[][2] = {{512, 512}, {512, 256}, {512, 128}, {1024, 512}, {1024, 256}};
+    const int cfg[][2] = {{512, 512}, {512, 256}, {512, 128}, {1024, 512}, {1024, 256}, {1024, 128}};
     for (const auto& tc : cfg)
         if (minmax_smem(a, tc[0], levels) <= smem_optin && (size_t)a.n >= (size_t)tc[0] * 2 * kNumSMs)
-            c.push_back(tc[0] | (tc[1] << 16));
+            for (int split : {0, kMmSplitBit}) c.push_back(tc[0] | (tc[1] << 16) | split);
+    if (minmax_ap_ok(a, smem_optin) && !c.empty()) c.push_back(kMmApTile | (512 << 16) | kMmApBit);
     return c.size() > 1 ? c : std::vector<int>{};
 }
 
-vta_status launch_minmax_batch(const MinMaxArgs& a, size_t smem_optin, cudaStream_t st) {
+vta_status launch_minmax_batch(const MinMaxArgs& a_in, size_t smem_optin, cudaStream_t st) {
+    MinMaxArgs a = a_in;
+    a.skip_clean = 0;
     const int levels = 32 - __builtin_clz((unsigned)a.pmax);  // floor(log2 pmax) + 1
-    const int hint_tile = a.tile_hint & 0xffff, hint_threads = a.tile_hint >> 16;
+    const bool ap = minmax_uses_progression(a, smem_optin);
+    if (ap) {
+        // progression kernel on the clean tiles, then the sparse-table kernel
+        // (same tiles) on the others
+        const size_t bytes = 4 * ((size_t)kMmApTile + a.pmax - 1) * sizeof(float);
+        auto kern = a.kind == MM_DONCHIAN ? k_minmax_ap<MM_DONCHIAN, kMmApThreads, kMmApPer>
+                                          : k_minmax_ap<MM_WILLR, kMmApThreads, kMmApPer>;
+        VTA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        ktimer_begin(st);
+        kern<<<ceil_div(a.n, kMmApTile), kMmApThreads, bytes, st>>>(a, kMmApTile);
+        VTA_TRY(check_launch("k_minmax_ap"));
+        a.skip_clean = 1;
+        a.tile_hint = kMmApTile | (512 << 16);
+    }
+    const int hint_tile = a.tile_hint & 0xffff, hint_threads = (a.tile_hint >> 16) & 0xfff;
     for (int tile = 2048; tile >= 256; tile >>= 1) {
         const size_t bytes = minmax_smem(a, tile, levels);
         const bool pick = hint_tile > 0 ? tile == hint_tile
@@ -896,8 +1078,24 @@ vta_status launch_minmax_batch(const MinMaxArgs& a, size_t smem_optin, cudaStrea
             auto kern = threads == 128 ? k_minmax_batch<128> : threads == 256 ? k_minmax_batch<256>
                                                                                : k_minmax_batch<kMmThreads>;
             VTA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-            ktimer_begin(st);
-            kern<<<ceil_div(a.n, tile), threads, bytes, st>>>(a, tile, levels);
+            // combo groups: as the hint says, else only when one block per
+            // tile would not give two waves (the table rebuild and its
+            // barriers are latency that few resident blocks do not hide)
+            int cpb = a.n_combos;
+            const long long tiles = ceil_div(a.n, tile);
+            bool split = (a.tile_hint & kMmSplitBit) != 0;
+            if (a.tile_hint == 0) {
+                int per_sm = 0;
+                if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, bytes) != cudaSuccess) {
+                    cudaGetLastError();
+                    per_sm = 1;
+                }
+                split = tiles < 2LL * std::max(1, per_sm) * kNumSMs;
+            }
+            if (split) cpb = wave_combos(kern, threads, bytes, tiles, a.n_combos);
+            if (!ap) ktimer_begin(st);
+            kern<<<dim3((unsigned)ceil_div(a.n, tile), (unsigned)ceil_div(a.n_combos, cpb)), threads, bytes, st>>>(
+                a, tile, levels, cpb);
             ktimer_end(st);
             return check_launch("k_minmax_batch");
         }

@@ -368,6 +368,7 @@ static int pick_chunk(vta_ctx* ctx, int n, int lanes, int warps_per_sm = 64) {
 // Policy "tune" = on (default) | off (untuned defaults) | cached (use cached
 // choices, never time); server slots never time.
 enum TuneKnob { TK_RECUR = 1, TK_MINMAX = 2, TK_RECUR_TC = 3 };
+constexpr int kMmApLabel = -1;  // last_kernel marker: the min/max progression kernel ran
 using SweepTuneKey = std::tuple<int, int, int, int>;
 static std::mutex g_stune_mu;
 static std::map<SweepTuneKey, int> g_stune;
@@ -1052,6 +1053,14 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             a.pmax = pmax;
             a.out0 = out[0];
             if (ind == I_DONCHIAN) { a.out1 = out[1]; a.out2 = out[2]; }
+            // an ascending arithmetic progression of periods (range grids)
+            a.ap_d = 0;
+            if (nc >= 2 && periods[1] > periods[0]) {
+                const int d = periods[1] - periods[0];
+                bool ap = d <= 64;
+                for (int i = 2; i < nc && ap; ++i) ap = periods[i] - periods[i - 1] == d;
+                if (ap) a.ap_d = d;
+            }
             int tile = 0;
             const char* tag = "default";
             auto launch = [&](int t) {
@@ -1060,10 +1069,14 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             };
             VTA_TRY(tuned_launch(ctx, (int)ind, n, nc, TK_MINMAX, minmax_tile_candidates(a, ctx->smem_optin), 0,
                                  launch, &tile, &tag));
+            const int thr = (tile >> 16) & 0xfff;
+            a.tile_hint = tile;
+            if (minmax_uses_progression(a, ctx->smem_optin)) tile = kMmApLabel;
             ctx->last_kernel = std::string("minmax_sparse_table(") +
-                               (tile ? "tile=" + std::to_string(tile & 0xffff) + ", threads=" +
-                                           std::to_string(tile >> 16 ? tile >> 16 : 512)
-                                     : std::string("tile=auto")) +
+                               (tile == kMmApLabel ? std::string("progression, tile=1024")
+                                : tile ? "tile=" + std::to_string(tile & 0xffff) + ", threads=" +
+                                             std::to_string(thr ? thr : 512) + ((tile >> 28) & 1 ? ", split" : "")
+                                       : std::string("tile=auto")) +
                                ", " + tag + ")";
             return VTA_OK;
         }

@@ -431,11 +431,17 @@ struct MinMaxArgs {
     float* out1;           // donchian middle
     float* out2;           // donchian lower
     int tile_hint;         // output times per block (0 = the launcher's choice)
+    // periods[c] = periods[0] + c * ap_d for every combo (an ascending
+    // arithmetic progression, 1 <= ap_d <= 64); 0 = not known to be one
+    int ap_d;
+    int skip_clean;        // (set by the launcher) leave clean tiles to the progression kernel
 };
 vta_status launch_minmax_batch(const MinMaxArgs& a, size_t smem_optin, cudaStream_t st);
 // Tiles launch_minmax_batch can run for `a` (the autotuner's candidates;
 // empty when only the launcher's own choice applies).
 std::vector<int> minmax_tile_candidates(const MinMaxArgs& a, size_t smem_optin);
+// Whether launch_minmax_batch runs the progression kernel for `a` (as hinted).
+bool minmax_uses_progression(const MinMaxArgs& a, size_t smem_optin);
 
 struct MinMaxTmArgs {
     int kind;
