@@ -524,30 +524,31 @@ __device__ __forceinline__ void minmax_clean(const MinMaxArgs& a, const float* m
         const float* mw = mx + ie0 + ct.w;
         const float* nz = mn + ie0 + ct.z;
         const float* nw = mn + ie0 + ct.w;
-        const bool all_valid = full && t0 >= ct.y;
-#pragma unroll
-        for (int k = 0; k < PER; ++k) {
-            const int t = t0 + tid + k * THREADS;
-            if (!all_valid && t >= a.n) break;
-            float v0 = qnan(), v1 = qnan(), v2 = qnan();
-            if (all_valid || t >= ct.y) {
-                const float hmax = fmaxf(mz[k * THREADS], mw[k * THREADS]);
-                const float lmin = fminf(nz[k * THREADS], nw[k * THREADS]);
-                if (KIND == MM_DONCHIAN) {
-                    v0 = hmax;
-                    v2 = lmin;
-                    v1 = fmaf(hmax - lmin, 0.5f, lmin);
-                } else {
-                    const float den = hmax - lmin;
-                    // hmax, lmin and the close are finite prices: the fast
-                    // divide is within 2 ulp
-                    v0 = den == 0.f ? 0.f : fmaf(-100.f, __fdividef(hmax - cl[k], den), 0.f);
-                }
-            }
-            r0[k * THREADS] = v0;
+        float* r1 = KIND == MM_DONCHIAN ? a.out1 + o : nullptr;
+        float* r2 = KIND == MM_DONCHIAN ? a.out2 + o : nullptr;
+        // value of slot k (hmax, lmin and the close are finite prices: the
+        // fast divide is within 2 ulp)
+        auto emit = [&](int k, bool valid) {
+            const float hmax = fmaxf(mz[k * THREADS], mw[k * THREADS]);
+            const float lmin = fminf(nz[k * THREADS], nw[k * THREADS]);
             if (KIND == MM_DONCHIAN) {
-                a.out1[o + k * THREADS] = v1;
-                a.out2[o + k * THREADS] = v2;
+                r0[k * THREADS] = valid ? hmax : qnan();
+                r1[k * THREADS] = valid ? fmaf(hmax - lmin, 0.5f, lmin) : qnan();
+                r2[k * THREADS] = valid ? lmin : qnan();
+            } else {
+                const float den = hmax - lmin;
+                const float v = den == 0.f ? 0.f : fmaf(-100.f, __fdividef(hmax - cl[k], den), 0.f);
+                r0[k * THREADS] = valid ? v : qnan();
+            }
+        };
+        if (full && t0 >= ct.y) {  // the whole tile is valid for this combo (uniform branch)
+#pragma unroll
+            for (int k = 0; k < PER; ++k) emit(k, true);
+        } else {
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int t = t0 + tid + k * THREADS;
+                if (t < a.n) emit(k, t >= ct.y);
             }
         }
     }
@@ -562,6 +563,7 @@ __device__ __forceinline__ void minmax_clean(const MinMaxArgs& a, const float* m
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS)
 k_minmax_batch(MinMaxArgs a, int tile, int levels, int cpb) {
+    if (a.skip_clean && !a.dirty[blockIdx.x]) return;  // k_minmax_ap wrote this tile
     extern __shared__ float sm[];
     const int cb = blockIdx.y * cpb, ce = min(a.n_combos, cb + cpb);
     const int t0 = blockIdx.x * tile;
@@ -604,7 +606,7 @@ k_minmax_batch(MinMaxArgs a, int tile, int levels, int cpb) {
     }
     if (threadIdx.x == 0) { bad_nan[0] = 0; bad_fin[0] = 0; }
     const bool clean = !__syncthreads_or(any_bad);
-    if (clean && a.skip_clean) return;  // k_minmax_ap wrote this tile
+
     // prefix counts (single warp, sequential per lane-strided segments)
     if (!clean && threadIdx.x < 32) {
         const int lane = threadIdx.x;
@@ -700,13 +702,14 @@ k_minmax_batch(MinMaxArgs a, int tile, int levels, int cpb) {
 // the d-bar sliding maximum, built once per tile in shared memory (likewise
 // the lows).  Per output: two shared-memory loads and two min/max (exact, so
 // the same values as the sparse-table lookups) instead of four loads and the
-// per-combo table set-up.  The first combo's window comes from p_0 mod d
-// single bars and p_0 / d blocks of M_d.  Clean tiles only (the same test as
+// per-combo table set-up.  The first combo's window (of each combo group of
+// the block) comes from p mod d single bars and p / d blocks of M_d.  Clean tiles only (the same test as
 // k_minmax_batch); k_minmax_batch, launched after with skip_clean, computes
 // the others.
 template <int KIND, int THREADS, int PER>
-__global__ void __launch_bounds__(THREADS) k_minmax_ap(MinMaxArgs a, int tile) {
+__global__ void __launch_bounds__(THREADS) k_minmax_ap(MinMaxArgs a, int tile, int cpb) {
     extern __shared__ float sm[];
+    const int cb = blockIdx.y * cpb, ce = min(a.n_combos, cb + cpb);  // this block's combos
     const int t0 = blockIdx.x * tile;
     const int lo_i = t0 - (a.pmax - 1);  // global index of slot 0
     const int nloc = tile + a.pmax - 1;
@@ -731,7 +734,9 @@ __global__ void __launch_bounds__(THREADS) k_minmax_ap(MinMaxArgs a, int tile) {
         xh[i] = hv;
         xl[i] = lv;
     }
-    if (__syncthreads_or(any_bad)) return;
+    const int bad = __syncthreads_or(any_bad);
+    if (blockIdx.y == 0 && threadIdx.x == 0) a.dirty[blockIdx.x] = bad ? 1 : 0;
+    if (bad) return;  // k_minmax_batch computes this tile
     // M_d: the d-bar sliding max / min ending at slot i (i >= d - 1)
     for (int i = threadIdx.x; i < nloc; i += THREADS) {
         float hv = -INFINITY, lv = INFINITY;
@@ -746,7 +751,7 @@ __global__ void __launch_bounds__(THREADS) k_minmax_ap(MinMaxArgs a, int tile) {
     __syncthreads();
     const int tid = threadIdx.x;
     const bool full = t0 + tile <= a.n;
-    const int p0 = __ldg(a.periods);
+    const int p0 = __ldg(a.periods + cb);  // the group's first period
     const int r = p0 % d, nb = p0 / d;
     float hm[PER], lm[PER], cl[PER];
 #pragma unroll
@@ -768,8 +773,8 @@ __global__ void __launch_bounds__(THREADS) k_minmax_ap(MinMaxArgs a, int tile) {
     }
     const int ie0 = tid + a.pmax - 1;
     int p = p0;
-    for (int c = 0; c < a.n_combos; ++c, p += d) {
-        if (c > 0) {
+    for (int c = cb; c < ce; ++c, p += d) {
+        if (c > cb) {
             const int back = ie0 - (p - d);  // slot of t - p_{c-1} for k = 0
 #pragma unroll
             for (int k = 0; k < PER; ++k) {
@@ -778,28 +783,30 @@ __global__ void __launch_bounds__(THREADS) k_minmax_ap(MinMaxArgs a, int tile) {
             }
         }
         const int warm = a.first + p - 1;
-        const bool all_valid = full && t0 >= warm;
         const size_t o = (size_t)c * a.n + t0 + tid;
-#pragma unroll
-        for (int k = 0; k < PER; ++k) {
-            const int t = t0 + tid + k * THREADS;
-            if (!all_valid && t >= a.n) break;
-            float v0 = qnan(), v1 = qnan(), v2 = qnan();
-            if (all_valid || t >= warm) {
-                if (KIND == MM_DONCHIAN) {
-                    v0 = hm[k];
-                    v2 = lm[k];
-                    v1 = fmaf(hm[k] - lm[k], 0.5f, lm[k]);
-                } else {
-                    const float den = hm[k] - lm[k];
-                    // finite prices: the fast divide is within 2 ulp
-                    v0 = den == 0.f ? 0.f : fmaf(-100.f, __fdividef(hm[k] - cl[k], den), 0.f);
-                }
-            }
-            a.out0[o + k * THREADS] = v0;
+        float* r0 = a.out0 + o;
+        float* r1 = KIND == MM_DONCHIAN ? a.out1 + o : nullptr;
+        float* r2 = KIND == MM_DONCHIAN ? a.out2 + o : nullptr;
+        // value of slot k (finite prices: the fast divide is within 2 ulp)
+        auto emit = [&](int k, bool valid) {
             if (KIND == MM_DONCHIAN) {
-                a.out1[o + k * THREADS] = v1;
-                a.out2[o + k * THREADS] = v2;
+                r0[k * THREADS] = valid ? hm[k] : qnan();
+                r1[k * THREADS] = valid ? fmaf(hm[k] - lm[k], 0.5f, lm[k]) : qnan();
+                r2[k * THREADS] = valid ? lm[k] : qnan();
+            } else {
+                const float den = hm[k] - lm[k];
+                const float v = den == 0.f ? 0.f : fmaf(-100.f, __fdividef(hm[k] - cl[k], den), 0.f);
+                r0[k * THREADS] = valid ? v : qnan();
+            }
+        };
+        if (full && t0 >= warm) {  // the whole tile is valid for this combo (uniform branch)
+#pragma unroll
+            for (int k = 0; k < PER; ++k) emit(k, true);
+        } else {
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int t = t0 + tid + k * THREADS;
+                if (t < a.n) emit(k, t >= warm);
             }
         }
     }
@@ -1033,7 +1040,7 @@ constexpr int kMmApThreads = 256, kMmApPer = 4, kMmApTile = kMmApThreads * kMmAp
 static bool minmax_ap_ok(const MinMaxArgs& a, size_t smem_optin) {
     const int levels = 32 - __builtin_clz((unsigned)a.pmax);
     const size_t nloc = (size_t)kMmApTile + a.pmax - 1;
-    return a.ap_d >= 1 && a.ap_d <= 64 && a.n_combos >= 2 && 4 * nloc * sizeof(float) <= smem_optin &&
+    return a.ap_d >= 1 && a.ap_d <= 64 && a.n_combos >= 2 && a.dirty && 4 * nloc * sizeof(float) <= smem_optin &&
            minmax_smem(a, kMmApTile, levels) <= smem_optin;
 }
 bool minmax_uses_progression(const MinMaxArgs& a, size_t smem_optin) {
@@ -1062,8 +1069,11 @@ vta_status launch_minmax_batch(const MinMaxArgs& a_in, size_t smem_optin, cudaSt
         auto kern = a.kind == MM_DONCHIAN ? k_minmax_ap<MM_DONCHIAN, kMmApThreads, kMmApPer>
                                           : k_minmax_ap<MM_WILLR, kMmApThreads, kMmApPer>;
         VTA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        const long long tiles = ceil_div(a.n, kMmApTile);
+        const int cpb = wave_combos(kern, kMmApThreads, bytes, tiles, a.n_combos);
         ktimer_begin(st);
-        kern<<<ceil_div(a.n, kMmApTile), kMmApThreads, bytes, st>>>(a, kMmApTile);
+        kern<<<dim3((unsigned)tiles, (unsigned)ceil_div(a.n_combos, cpb)), kMmApThreads, bytes, st>>>(a, kMmApTile,
+                                                                                                    cpb);
         VTA_TRY(check_launch("k_minmax_ap"));
         a.skip_clean = 1;
         a.tile_hint = kMmApTile | (512 << 16);

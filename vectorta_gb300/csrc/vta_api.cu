@@ -1038,10 +1038,12 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             return launch_prefix_window_batch(a, pmax, ctx->smem_optin, st);
         }
         case I_DONCHIAN: case I_WILLR: {
+            ar.need(((size_t)n + 1023) / 1024 * sizeof(int));  // per-tile flags of the progression kernel
             VTA_TRY(ar.commit());
             const int* d_per = nullptr;
             VTA_TRY(const_upload(ctx, periods.data(), nc, ar.take<int>(nc), &d_per));
             MinMaxArgs a{};
+            a.dirty = ar.take<int>(((size_t)n + 1023) / 1024);
             a.kind = ind == I_DONCHIAN ? MM_DONCHIAN : MM_WILLR;
             a.tile_hint = 0;
             a.h = in.p[0]; a.l = in.p[1];

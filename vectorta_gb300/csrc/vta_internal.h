@@ -435,6 +435,7 @@ struct MinMaxArgs {
     // arithmetic progression, 1 <= ap_d <= 64); 0 = not known to be one
     int ap_d;
     int skip_clean;        // (set by the launcher) leave clean tiles to the progression kernel
+    int* dirty;            // scratch, one int per 1024-bar tile: the tiles the progression kernel left
 };
 vta_status launch_minmax_batch(const MinMaxArgs& a, size_t smem_optin, cudaStream_t st);
 // Tiles launch_minmax_batch can run for `a` (the autotuner's candidates;
