@@ -24,6 +24,7 @@
 #include "vta_internal.h"
 #include "vta_plan.h"
 #include "hlc_ops.cuh"
+#include "pnr_ops.cuh"
 
 namespace vta {
 namespace {
@@ -44,61 +45,9 @@ using hlc::PAdx;
 using hlc::PSuperTrend;
 
 // ------------------------------------------------ nearest-rank percentile ---
-// percentile_nearest_rank over a window of `len` values (NaN excluded),
-// out = sorted[k], k = round(p * wl) - 1 clamped (percentile_nearest_rank.rs:
-// 190-266).  The sorted window lives in W registers padded with +inf; insertion
-// and removal are branch-free compare/select passes with constant indices.
-__device__ __forceinline__ int pnr_rank(double pf, int wl) {
-    const long long raw = (long long)round(fma(pf, (double)wl, 0.0)) - 1;
-    const int k = raw <= 0 ? 0 : (int)raw;
-    return k >= wl ? wl - 1 : k;
-}
-// Insert v (not NaN) into the ascending window, dropping the last (+inf)
-// slot: w'[i] = min(w[i], max(w[i-1], v)) -- two min/max per slot, no
-// predicates, every slot independent.
-template <int W>
-__device__ __forceinline__ void reg_insert(float (&w)[W], float v) {
-#pragma unroll
-    for (int i = W - 1; i > 0; --i) w[i] = fminf(w[i], fmaxf(w[i - 1], v));
-    w[0] = fminf(w[0], v);
-}
-// Remove one element equal to v (v is in the window): slots below v keep their
-// value, the others take their right neighbour.  "w[i] < v" is the sign of
-// w[i] - v (exact: a difference of distinct floats is never zero with
-// denormals kept, and equal values give +0), turned into a bit mask.
-template <int W>
-__device__ __forceinline__ void reg_remove(float (&w)[W], float v) {
-    constexpr unsigned kInf = 0x7f800000u;
-#pragma unroll
-    for (int i = 0; i < W; ++i) {
-        const unsigned m = (unsigned)((int)__float_as_uint(__fsub_rn(w[i], v)) >> 31);
-        const unsigned nxt = i + 1 < W ? __float_as_uint(w[i + 1]) : kInf;
-        w[i] = __uint_as_float((__float_as_uint(w[i]) & m) | (nxt & ~m));
-    }
-}
-// w[k] for a runtime k by a select tree on the bits of k (depth log2 W
-// instead of a W-long chain of dependent selects)
-template <int W>
-__device__ __forceinline__ float pick_tree(const float (&w)[W], int k) {
-    constexpr int P = W <= 16 ? 16 : (W <= 32 ? 32 : 64);
-    float v[P];
-#pragma unroll
-    for (int i = 0; i < P; ++i) v[i] = i < W ? w[i] : 0.f;
-#pragma unroll
-    for (int step = 1; step < P; step <<= 1) {
-        const bool hi = (k & step) != 0;
-#pragma unroll
-        for (int i = 0; i + step < P; i += 2 * step) v[i] = hi ? v[i + step] : v[i];
-    }
-    return v[0];
-}
-
-template <int W>
-__device__ __forceinline__ float pnr_pick(const float (&w)[W], int wl, int len, int kfull, double pf) {
-    const int k = wl == len ? kfull : (wl > 0 ? pnr_rank(pf, wl) : 0);
-    const float r = pick_tree(w, k);
-    return wl > 0 ? r : qnan();
-}
+// (the sorted register window of pnr_ops.cuh)
+using pnr::pick;
+using pnr::rank;
 
 // ------------------------------------------------ chunk runners -------------
 // Inputs are staged per warp in shared memory: a double buffer of kPB steps
@@ -177,7 +126,7 @@ __device__ void pnr_chunk(const TmIn& in, const Stage& sg, unsigned mask, int f,
     if (tend <= c0) return;  // warp-uniform
     const int tbeg = max(0, c0 - len + 1);
     const int start = f + len - 1;
-    const int kfull = pnr_rank(pf, len);
+    const int kfull = rank(pf, len);
     float w[W];
 #pragma unroll
     for (int i = 0; i < W; ++i) w[i] = __int_as_float(0x7f800000);
@@ -201,16 +150,10 @@ __device__ void pnr_chunk(const TmIn& in, const Stage& sg, unsigned mask, int f,
             const int j = u - ub, uo = u - len;
             const float vo = (uo >= tbeg && uo < L) ? *sg.at(buf, 1, j) : qnan();
             const float vi = u < L ? *sg.at(buf, 0, j) : qnan();
-            if (!isnan(vo)) {
-                reg_remove(w, vo);
-                --wl;
-            }
-            if (!isnan(vi)) {
-                reg_insert(w, vi);
-                ++wl;
-            }
+            pnr::replace(w, vo, vi);
+            wl += (isnan(vi) ? 0 : 1) - (isnan(vo) ? 0 : 1);
             if (u >= c0 && u < c1)
-                out[(size_t)u * in.cols + in.s] = u < start ? qnan() : pnr_pick(w, wl, len, kfull, pf);
+                out[(size_t)u * in.cols + in.s] = u < start ? qnan() : pick(w, wl, len, kfull, pf);
         }
     }
 }

@@ -15,6 +15,7 @@
 // every output from p steps after it (where it leaves the window: inf - inf).
 #include <algorithm>
 
+#include "pnr_ops.cuh"
 #include "vta_internal.h"
 
 namespace vta {
@@ -890,11 +891,7 @@ __global__ void k_minmax_tm(MinMaxTmArgs a) {
 constexpr int kPnrChunk = 256;
 constexpr int kPnrLocal = 64;
 
-__device__ __forceinline__ int pnr_rank(double pf, int wl) {
-    long long raw = (long long)round(fma(pf, (double)wl, 0.0)) - 1;
-    int k = raw <= 0 ? 0 : (int)raw;
-    return k >= wl ? wl - 1 : k;
-}
+using pnr::rank;
 
 __device__ __forceinline__ int lower_bound(const float* w, int n, float v) {
     int lo = 0, hi = n;
@@ -920,10 +917,10 @@ __device__ void pnr_lane(const float* x, size_t stride, int n, int f, int len, d
         win[pos] = v;
         ++wl;
     }
-    const int kfull = pnr_rank(pf, len);
+    const int kfull = rank(pf, len);
     for (;;) {
         float r = qnan();
-        if (wl > 0) r = win[wl == len ? kfull : pnr_rank(pf, wl)];
+        if (wl > 0) r = win[wl == len ? kfull : rank(pf, wl)];
         out[(size_t)t * ostride] = r;
         if (t + 1 >= c1) break;
         const float vo = x[(size_t)(t + 1 - len) * stride];
@@ -945,12 +942,63 @@ __device__ void pnr_lane(const float* x, size_t stride, int n, int f, int len, d
     }
 }
 
+// One lane's outputs [c0, c1) with the window sorted in W registers (len <=
+// W): every lane of the warp runs one step loop over [u0, c1), u0 the warp's
+// earliest window start, replacing the value leaving its window by the one
+// entering (pnr_ops.cuh); a lane whose window has not started yet adds only.
+template <int W>
+__device__ void pnr_lane_reg(const float* x, size_t stride, int f, int len, double pf, int c0, int c1, int u0,
+                             float* out, size_t ostride) {
+    const int start = f + len - 1;
+    const int tbeg = max(0, c0 - len + 1);  // this lane's first window value
+    const int kfull = pnr::rank(pf, len);
+    float w[W];
+#pragma unroll
+    for (int i = 0; i < W; ++i) w[i] = __int_as_float(0x7f800000);
+    int wl = 0;
+    for (int u = u0; u < c1; ++u) {
+        const int uo = u - len;
+        const float vi = u >= tbeg ? __ldg(x + (size_t)u * stride) : qnan();
+        const float vo = uo >= tbeg ? __ldg(x + (size_t)uo * stride) : qnan();
+        pnr::replace(w, vo, vi);
+        wl += (isnan(vi) ? 0 : 1) - (isnan(vo) ? 0 : 1);
+        if (u >= c0) out[(size_t)u * ostride] = u < start ? qnan() : pnr::pick(w, wl, len, kfull, pf);
+    }
+}
+
 __global__ void k_percentile(PnrArgs a) {
     const int li = blockIdx.x * blockDim.x + threadIdx.x;
-    if (li >= a.n_lanes) return;
     const int c0 = blockIdx.y * kPnrChunk;
     const int c1 = min(c0 + kPnrChunk, a.n);
     if (c0 >= a.n) return;
+    // windows of at most 64 values: the register window, sized by the
+    // warp's longest window (warp-uniform); longer ones: the sorted array
+    {
+        const bool live = li < a.n_lanes;
+        const int len = live ? (a.layout == 0 ? a.lengths[li] : a.length) : 1;
+        const int wmax = __reduce_max_sync(0xffffffffu, len);
+        if (wmax <= 64) {
+            const int u0 = max(0, c0 - wmax + 1);
+            const float* x = a.layout == 0 ? a.x : a.x + (live ? li : 0);
+            const size_t stride = a.layout == 0 ? 1 : (size_t)a.cols;
+            const int f = a.layout == 0 ? a.first : (live ? a.first_tm[li] : 0);
+            const double pf = a.layout == 0 ? (live ? (double)a.pfrac[li] : 0.5) : (double)a.p_frac;
+            float* out = a.layout == 0 ? a.out + (size_t)(live ? li : 0) * a.n : a.out + (live ? li : 0);
+            const size_t ostride = a.layout == 0 ? 1 : (size_t)a.cols;
+            if (!live) return;  // after the warp-wide reduction
+            switch ((wmax + 7) / 8) {
+                case 1: case 2: pnr_lane_reg<16>(x, stride, f, len, pf, c0, c1, u0, out, ostride); break;
+                case 3: pnr_lane_reg<24>(x, stride, f, len, pf, c0, c1, u0, out, ostride); break;
+                case 4: pnr_lane_reg<32>(x, stride, f, len, pf, c0, c1, u0, out, ostride); break;
+                case 5: pnr_lane_reg<40>(x, stride, f, len, pf, c0, c1, u0, out, ostride); break;
+                case 6: pnr_lane_reg<48>(x, stride, f, len, pf, c0, c1, u0, out, ostride); break;
+                case 7: pnr_lane_reg<56>(x, stride, f, len, pf, c0, c1, u0, out, ostride); break;
+                default: pnr_lane_reg<64>(x, stride, f, len, pf, c0, c1, u0, out, ostride); break;
+            }
+            return;
+        }
+    }
+    if (li >= a.n_lanes) return;
     float local[kPnrLocal];
     if (a.layout == 0) {
         const int len = a.lengths[li];
