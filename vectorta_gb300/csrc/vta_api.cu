@@ -1710,6 +1710,18 @@ int ind_by_name(const char* name) {
 }
 int ind_inputs(int ind) { return kInfo[ind].in; }
 int ind_outputs(int ind) { return kInfo[ind].n_out; }
+// Device time per output relative to an HBM-bound sweep (EMA, SMA, ALMA):
+// the sequential high/low/close recurrences and the percentile window run
+// well below the write bandwidth (measured bench figures, rounded).
+double ind_cost(int ind) {
+    switch (ind) {
+        case I_ADX: return 12.0;
+        case I_SUPERTREND: return 8.0;
+        case I_PNR: return 10.0;
+        case I_ATR: return 2.0;
+        default: return 1.0;
+    }
+}
 
 // first valid index from the per-field firsts of a stored series, as
 // host_first defines it per indicator

@@ -484,6 +484,7 @@ vta_status tm_job_enqueue(vta_ctx* ctx, int kind, int period, double param, cons
 int ind_by_name(const char* name);  // -1 if unknown
 int ind_inputs(int ind);            // 1: close, 2: high, low, 3: high, low, close
 int ind_outputs(int ind);
+double ind_cost(int ind);           // device time per output relative to an HBM-bound sweep
 size_t ind_first(int ind, size_t fh, size_t fl, size_t fc, size_t fall);
 // grid expansion + the crate's checks for a series of len with first valid `first`
 vta_status batch_check(int ind, const vta_sweep* sw, size_t len, size_t first, size_t* rows);

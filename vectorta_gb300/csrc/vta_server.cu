@@ -3,15 +3,24 @@
 //
 // One server thread owns the device work.  It
 //   * collects finished requests (an event per slot, polled without waiting),
-//   * admits queued requests in arrival order while a slot is free and the
-//     request's outputs fit the memory budget (a request that has to wait for
-//     budget is counted once as deferred), and
+//   * admits queued requests while a slot is free and the request's outputs
+//     fit the memory budget (a request that has to wait for budget is counted
+//     once as deferred), and
 //   * enqueues each admitted request's kernels on its slot's stream through
 //     the same driver the vta_X_batch_device entry points use, with outputs
 //     from a stream-ordered memory pool.
 // Slots run concurrently, so requests that arrive while others are on the
 // device overlap with them.  Submitting, polling and releasing only take the
 // server lock; none of them waits for the device.
+//
+// Requests are small or large by their estimated device time (outputs times
+// ind_cost).  Each class has its own arrival-order queue.  A quarter of the
+// slots (at least one) take small requests only and run on the device's
+// highest-priority streams, so a burst of large sweeps neither holds every
+// slot nor delays the blocks of the small ones; the other slots take small
+// requests first and large ones otherwise, and a large request that has
+// waited kLargeMaxWait goes before the small ones on those slots.  A large
+// request waiting for memory budget does not hold back the small queue.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -47,12 +56,20 @@ struct Req {
     size_t bytes = 0;
     double t_submit = 0.0;
     bool deferred = false;
+    bool large = false;  // estimated device time above kLargeWork
 };
+
+// a request with more than this many cost-weighted outputs is large (about a
+// millisecond of device time at the write bandwidth)
+constexpr double kLargeWork = 32e6;
+constexpr double kLargeMaxWait = 0.05;  // seconds
 
 struct Slot {
     vta_ctx* ctx = nullptr;
     cudaEvent_t done = nullptr;
     bool busy = false;
+    bool small_only = false;         // reserved for small requests (high-priority stream)
+    cudaStream_t prio = nullptr;     // that stream (owned here)
     Req req;
     float* out[3] = {nullptr, nullptr, nullptr};
     double t_start = 0.0;
@@ -76,7 +93,9 @@ struct vta_server {
     cudaStream_t aux_stream = nullptr;  // store uploads and releases
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::deque<Req> queue;
+    std::deque<Req> queue;                      // small requests, in arrival order
+    std::deque<Req> q_large;                    // large requests, in arrival order
+    int running_large = 0;
     std::deque<Result> ready;                   // finished, not yet polled
     std::unordered_map<uint64_t, Result> held;  // polled, not yet released
     size_t budget = 0, in_use = 0, running = 0;
@@ -169,6 +188,7 @@ void finish(vta_server* S, Slot& sl, cudaError_t q) {
     }
     ++S->n_done;
     --S->running;
+    if (sl.req.large) --S->running_large;
     sl.busy = false;
     S->ready.push_back(std::move(res));
     S->cv_done.notify_all();
@@ -186,32 +206,44 @@ void worker_main(vta_server* S) {
             finish(S, sl, q);
             progress = true;
         }
-        while (!S->draining && !S->queue.empty()) {
-            Slot* free_slot = nullptr;
-            for (Slot& sl : S->slots)
-                if (!sl.busy) {
-                    free_slot = &sl;
-                    break;
-                }
-            if (!free_slot) break;
-            Req& front = S->queue.front();
-            if (S->in_use > 0 && S->in_use + front.bytes > S->budget) {
-                if (!front.deferred) {
-                    front.deferred = true;
-                    ++S->n_def;
-                }
-                break;
+        // the head of queue q when it fits the memory budget (else it is
+        // counted as deferred, once)
+        auto fits = [&](std::deque<Req>& q) {
+            if (q.empty()) return false;
+            Req& f = q.front();
+            if (S->in_use == 0 || S->in_use + f.bytes <= S->budget) return true;
+            if (!f.deferred) {
+                f.deferred = true;
+                ++S->n_def;
             }
-            const Req r = front;
-            S->queue.pop_front();
-            S->in_use += r.bytes;
-            ++S->n_adm;
-            ++S->running;
-            free_slot->busy = true;
-            lk.unlock();
-            launch(S, *free_slot, r);
-            lk.lock();
-            progress = true;
+            return false;
+        };
+        const int large_cap = (int)S->slots.size() - (int)std::count_if(S->slots.begin(), S->slots.end(),
+                                                                         [](const Slot& x) { return x.small_only; });
+        for (bool again = true; again && !S->draining;) {
+            again = false;
+            for (Slot& sl : S->slots) {
+                if (sl.busy) continue;
+                const bool large_ok = !sl.small_only && S->running_large < large_cap;
+                const bool large_due = large_ok && !S->q_large.empty() &&
+                                       S->now() - S->q_large.front().t_submit > kLargeMaxWait;
+                std::deque<Req>* q = nullptr;
+                if (large_due && fits(S->q_large)) q = &S->q_large;
+                else if (fits(S->queue)) q = &S->queue;
+                else if (large_ok && fits(S->q_large)) q = &S->q_large;
+                if (!q) continue;
+                const Req r = q->front();
+                q->pop_front();
+                S->in_use += r.bytes;
+                ++S->n_adm;
+                ++S->running;
+                if (r.large) ++S->running_large;
+                sl.busy = true;
+                lk.unlock();
+                launch(S, sl, r);
+                lk.lock();
+                progress = again = true;
+            }
         }
         if (!progress) S->cv_work.wait_for(lk, std::chrono::microseconds(S->running ? 20 : 2000));
     }
@@ -256,10 +288,23 @@ vta_status vta_server_create(int device_id, const vta_server_config* config, vta
     }
     if (e != cudaSuccess) s = cuda_fail(e, "server pool / stream");
     S->slots.resize(n_slots);
+    const int reserve = n_slots >= 2 ? std::max(1, n_slots / 4) : 0;
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
     for (int i = 0; i < n_slots && s == VTA_OK; ++i) {
         Slot& sl = S->slots[i];
         s = vta_ctx_create(device_id, &sl.ctx);
         if (s != VTA_OK) break;
+        if (i < reserve) {
+            sl.small_only = true;
+            e = cudaStreamCreateWithPriority(&sl.prio, cudaStreamNonBlocking, prio_hi);
+            if (e != cudaSuccess) {
+                s = cuda_fail(e, "server slot stream");
+                break;
+            }
+            s = vta_ctx_set_stream(sl.ctx, sl.prio);
+            if (s != VTA_OK) break;
+        }
         sl.ctx->async_alloc = true;
         sl.ctx->pool = S->pool;
         e = cudaHostAlloc((void**)&sl.ctx->err_host, sizeof(int), cudaHostAllocDefault);
@@ -270,6 +315,7 @@ vta_status vta_server_create(int device_id, const vta_server_config* config, vta
         for (Slot& sl : S->slots) {
             if (sl.done) cudaEventDestroy(sl.done);
             if (sl.ctx) vta_ctx_destroy(sl.ctx);
+            if (sl.prio) cudaStreamDestroy(sl.prio);
         }
         if (S->aux_stream) cudaStreamDestroy(S->aux_stream);
         if (S->pool) cudaMemPoolDestroy(S->pool);
@@ -350,11 +396,12 @@ vta_status vta_server_submit(vta_server* S, const vta_request* req, uint64_t* ti
     const size_t first = ind_first(ind, se.fh, se.fl, se.fc, se.fall);
     VTA_TRY(batch_check(ind, &r.sw, se.len, first, &r.rows));
     r.bytes = r.rows * se.len * sizeof(float) * (size_t)r.n_out;
+    r.large = (double)r.rows * (double)se.len * r.n_out * ind_cost(ind) > kLargeWork;
     std::lock_guard<std::mutex> lock(S->mu);
     if (r.bytes > S->budget) return fail(VTA_ERR_OUT_OF_MEMORY, "request outputs exceed the server's memory budget");
     r.ticket = S->next_ticket++;
     r.t_submit = S->now();
-    S->queue.push_back(r);
+    (r.large ? S->q_large : S->queue).push_back(r);
     ++S->n_sub;
     *ticket = r.ticket;
     S->cv_work.notify_one();
@@ -429,7 +476,7 @@ vta_status vta_server_get_stats(vta_server* S, vta_server_stats* st) {
     st->deferred = S->n_def;
     st->completed = S->n_done;
     st->failed = S->n_fail;
-    st->queued = S->queue.size();
+    st->queued = S->queue.size() + S->q_large.size();
     st->running = S->running;
     st->bytes_in_use = S->in_use;
     st->memory_budget = S->budget;
@@ -462,6 +509,7 @@ vta_status vta_server_destroy(vta_server* S) {
     for (Slot& sl : S->slots) {
         if (sl.done) cudaEventDestroy(sl.done);
         if (sl.ctx) vta_ctx_destroy(sl.ctx);
+        if (sl.prio) cudaStreamDestroy(sl.prio);
     }
     for (Series& se : S->store)
         for (float* p : se.d)
