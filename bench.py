@@ -192,6 +192,32 @@ def workload_recur_small():
             "config": {"workload": "recur_small", "bars": n, "seed": 1, "combos": 999}}
 
 
+def workload_tema_small():
+    """Profiling case of the tensor-core chunk aggregates and the carry scan
+    with a three-component state: one TEMA sweep (periods 2..1000, 999
+    combos) on 200,000 bars (0.8 GB of outputs per call)."""
+    from vectorta_gb300 import datagen
+
+    n = 200_000
+    close = datagen.random_walk(n, seed=1, nan_lead=200)
+    return {"name": "tema_small", "n": n, "series": {"close": close.astype(np.float32)},
+            "jobs": [("tema", ["close"], {"period": (2, 1000, 1)})], "dominant": "tema",
+            "config": {"workload": "tema_small", "bars": n, "seed": 1, "combos": 999}}
+
+
+def workload_percentile_small():
+    """Profiling case of the batch percentile: window lengths 10..64 step 2 x
+    percentages 25/50/75 (84 combos) on 200,000 bars."""
+    from vectorta_gb300 import datagen
+
+    n = 200_000
+    close = datagen.random_walk(n, seed=1, nan_lead=50)
+    return {"name": "percentile_small", "n": n, "series": {"close": close.astype(np.float32)},
+            "jobs": [("percentile_nearest_rank", ["close"], {"length": (10, 64, 2), "percentage": (25.0, 75.0, 25.0)})],
+            "dominant": "percentile_nearest_rank",
+            "config": {"workload": "percentile_small", "bars": n, "seed": 1, "combos": 84}}
+
+
 def workload_windows_small():
     """Profiling case of the window kernels: StdDev and WillR sweeps (windows
     5..500 step 5, 100 combos) on 400,000 bars (160 MB of outputs per call:
@@ -275,7 +301,8 @@ def workload_served_stream():
 WORKLOADS = {"sweeps": workload_sweeps, "ragged_tm": workload_ragged_tm, "served_stream": workload_served_stream,
              "adx_sweep": workload_adx_sweep, "wwma_family": workload_wwma_family, "ragged_small": workload_ragged_small, "alma_grid": workload_alma_grid, "ema_small": workload_ema_small,
              "alma_small": workload_alma_small, "windows_small": workload_windows_small,
-             "recur_small": workload_recur_small, "wma_long": workload_wma_long}
+             "recur_small": workload_recur_small, "wma_long": workload_wma_long, "tema_small": workload_tema_small,
+             "percentile_small": workload_percentile_small}
 
 
 # ------------------------------------------------------------- clocks -------
@@ -1024,7 +1051,8 @@ KERNEL_NAME = {"recurrence_window_sweeps": "k_recur<OpEma, batch, EMIT>", "alma_
                "ema_small": "k_recur<OpEma, batch, EMIT>", "alma_small": "k_wwma_tc<fp16x3>",
                "adx_sweep": "k_hlc_chunk<adx> + fix-up", "wwma_family": "k_wwma_tc<fp16x3> (CWMA)",
                "windows_small": "k_prefix_window_batch (StdDev)", "recur_small": "k_recur<OpEma, batch, EMIT>",
-               "wma_long": "k_wwma_tc<fp16x3> (K slices)"}
+               "wma_long": "k_wwma_tc<fp16x3> (K slices)", "tema_small": "k_recur<OpTema, batch, EMIT>",
+               "percentile_small": "k_percentile (register window)"}
 
 
 def main():

@@ -1436,13 +1436,11 @@ __device__ void chunk_map(const float4 g, int p, int chunk, const D2 (&ml)[Op::N
 // linear part M (the transition of `chunk` steps), so a run of them only
 // updates the offset (b <- M b + agg) and its power M^cnt is applied once
 // when another map follows or the run ends: the work per chunk is a
-// matrix-vector product.  The chunk records are read eight at a time, ahead
-// of the dependent math.
+// matrix-vector product.
 template <class Op>
 __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
     constexpr int N = Op::NS;
     constexpr int SH = ShapeOf<Op>::v;
-    constexpr int kB = 8;
     const int lane = threadIdx.x & 31;
     const int li = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // one warp per lane of the scan
     if (li >= a.n_lanes) return;
@@ -1506,28 +1504,32 @@ __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
             for (int c = 0; c < N; ++c) run.m[r][c] = m2[r][c];
         cnt = 0;
     };
-    for (int kb = k0; kb < k1; kb += kB) {
-        float4 gv[kB];
-#pragma unroll
-        for (int u = 0; u < kB; ++u)
-            if (kb + u < k1) gv[u] = __ldg(agg + (size_t)(kb + u) * a.n_lanes + li);
-#pragma unroll
-        for (int u = 0; u < kB; ++u) {
-            if (kb + u >= k1) break;
-            if (gv[u].w == full) {
-                full_step(run.b, gv[u]);
-                ++cnt;
-            } else {
-                flush();
-                AffD<N> ak;
-                chunk_map<Op>(gv[u], p, a.chunk, ml, ak);
-                run = affd_then<N, SH>(run, ak);
-                if (gv[u].w == kAbsolute) m_zero = true;
-            }
+    // the chunk records in a 4-deep register queue: loads run ahead of the
+    // dependent math without an unrolled batch (the scan's double-single code
+    // is large, and unrolled copies of it overflowed the instruction cache)
+    const float4 kNone = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto rec = [&](int k) { return k < k1 ? __ldg(agg + (size_t)k * a.n_lanes + li) : kNone; };
+    float4 q0 = rec(k0), q1 = rec(k0 + 1), q2 = rec(k0 + 2), q3 = rec(k0 + 3);
+#pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+        const float4 g = q0;
+        q0 = q1;
+        q1 = q2;
+        q2 = q3;
+        q3 = rec(k + 4);
+        if (g.w == full) {
+            full_step(run.b, g);
+            ++cnt;
+        } else {
+            flush();
+            AffD<N> ak;
+            chunk_map<Op>(g, p, a.chunk, ml, ak);
+            run = affd_then<N, SH>(run, ak);
+            if (g.w == kAbsolute) m_zero = true;
         }
     }
     flush();
-#pragma unroll
+#pragma unroll 1
     for (int d = 1; d < 32; d <<= 1) {
         const AffD<N> up = affd_shfl_up<N, SH>(run, d);
         if (lane >= d) run = affd_then<N, SH>(up, run);
@@ -1537,25 +1539,28 @@ __global__ void k_recur_carry(RecurArgs a, int n_chunks) {
     D2 S[N];  // state at the start of chunk k0
 #pragma unroll
     for (int r = 0; r < N; ++r) S[r] = ex.b[r];
-    for (int kb = k0; kb < k1; kb += kB) {
-        float4 gv[kB];
-#pragma unroll
-        for (int u = 0; u < kB; ++u)
-            if (kb + u < k1) gv[u] = __ldg(agg + (size_t)(kb + u) * a.n_lanes + li);
-#pragma unroll
-        for (int u = 0; u < kB; ++u) {
-            const int k = kb + u;
-            if (k >= k1) break;
+    q0 = rec(k0);
+    q1 = rec(k0 + 1);
+    q2 = rec(k0 + 2);
+    q3 = rec(k0 + 3);
+#pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+        const float4 g = q0;
+        q0 = q1;
+        q1 = q2;
+        q2 = q3;
+        q3 = rec(k + 4);
+        {
             float4 cv = make_float4(0.f, 0.f, 0.f, 0.f);
             cv.x = S[0].hi + S[0].lo;
             if (N > 1) cv.y = S[N > 1 ? 1 : 0].hi + S[N > 1 ? 1 : 0].lo;
             if (N > 2) cv.z = S[N > 2 ? 2 : 0].hi + S[N > 2 ? 2 : 0].lo;
             carry[(size_t)k * a.n_lanes + li] = cv;
-            if (gv[u].w == full) {
-                full_step(S, gv[u]);
+            if (g.w == full) {
+                full_step(S, g);
             } else {
                 AffD<N> ak;
-                chunk_map<Op>(gv[u], p, a.chunk, ml, ak);
+                chunk_map<Op>(g, p, a.chunk, ml, ak);
                 D2 t[N];
 #pragma unroll
                 for (int r = 0; r < N; ++r) {
