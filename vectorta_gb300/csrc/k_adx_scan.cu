@@ -1,0 +1,202 @@
+// Exact chunked scan of batch ADX sweeps with long periods.
+//
+// Past its seeding phase (t >= f + 2p) ADX is two linear Wilder levels with a
+// pointwise function between them:
+//   s <- s * omr + u        s = (atr, +DM, -DM) sums, u = (TR, +DM, -DM) of bar t
+//   dx = DX(s)              adx_dx (hlc_ops.cuh)
+//   adx <- (adx * pm1 + dx) * rp
+// (omr = 1 - 1/p, pm1 = p - 1, rp = 1/p, all f32 as in PAdx).  The
+// warm-restart chunking of k_hlc_chunk.cu runs 32 p + 64 steps before every
+// chunk, which for periods in the thousands is many times the chunk itself.
+// Here a 32-combo group's time axis after its seeding is cut into chunks of L
+// steps and processed exactly, like the chunked linear recurrences:
+//   AGG1   per (group, chunk): the first level from a zero state over the chunk;
+//   CARRY1 per lane: chunk-entry first-level states, s_{k+1} = omr^L s_k + a_k
+//          (double-single; s_1 is the seeding run's end state);
+//   AGG2   per (group, chunk): the first level from its exact entry state, DX,
+//          and the second level from a zero state;
+//   CARRY2 per lane: chunk-entry ADX, adx_{k+1} = (pm1 rp)^L adx_k + b_k;
+//   EMIT   per (group, chunk): both levels from their entry states, outputs.
+// The seeding run (chunk 0, up to the group's s0) is k_hlc_chunk's exact
+// chunk-0 item.  Outputs differ from one sequential f32 pass by the rounding
+// of the composed carries (a few 1e-7 relative); a NaN input propagates to
+// every later output as in the sequential pass.
+#include <algorithm>
+
+#include "hlc_ops.cuh"
+#include "vta_internal.h"
+
+namespace vta {
+namespace {
+
+constexpr int kSW = 4;  // warps per block
+
+struct D2s {
+    float hi, lo;
+};
+__device__ __forceinline__ D2s ds_norm(float s, float e) {
+    const float hi = s + e;
+    return {hi, e - (hi - s)};
+}
+__device__ __forceinline__ D2s ds_mul(D2s a, D2s b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+    return ds_norm(p, e);
+}
+__device__ __forceinline__ D2s ds_add(D2s a, D2s b) {
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    const float e = ((a.hi - (s - bb)) + (b.hi - bb)) + (a.lo + b.lo);
+    return ds_norm(s, e);
+}
+__device__ __forceinline__ D2s ds_pow(D2s b, long long n) {
+    D2s r = {1.f, 0.f};
+    while (n > 0) {
+        if (n & 1) r = ds_mul(r, b);
+        b = ds_mul(b, b);
+        n >>= 1;
+    }
+    return r;
+}
+
+struct Lane {
+    float omr, pm1, rp;
+    __device__ void init(int p) {
+        rp = (float)(1.0 / (double)p);
+        omr = (float)(1.0 - 1.0 / (double)p);
+        pm1 = (float)p - 1.f;
+    }
+};
+
+enum { PASS_AGG1 = 0, PASS_AGG2 = 1, PASS_EMIT = 2 };
+
+// One (group, chunk >= 1) item per warp; lane = combo of the group.
+template <int PASS>
+__global__ void __launch_bounds__(kSW * 32) k_adx_scan(AdxScanArgs a) {
+    __shared__ float stage[kSW][32][33];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int item = blockIdx.x * kSW + warp;
+    if (item >= a.n_items) return;
+    const int2 it = a.items[item];
+    const int gi = it.x, k = it.y;
+    const int g = a.groups[gi];
+    const int c0 = a.group_s0[gi] + (k - 1) * a.L;
+    const int c1 = min(c0 + a.L, a.n);
+    const int ci = g * 32 + lane;  // combo
+    const bool valid = ci < a.n_combos;
+    const size_t si = (size_t)k * a.n_slots + gi * 32 + lane;  // state slot
+    Lane ln;
+    ln.init(__ldg(a.periods + (valid ? ci : g * 32)));
+    float atr = 0.f, pdm = 0.f, mdm = 0.f, adx = 0.f;
+    if (PASS != PASS_AGG1) {
+        const float4 s = a.carry1[si];
+        atr = s.x;
+        pdm = s.y;
+        mdm = s.z;
+    }
+    if (PASS == PASS_EMIT) adx = a.carry2[si];
+    // inputs of the bar before the chunk (c0 >= 1)
+    float ph = __ldg(a.h + c0 - 1), pl = __ldg(a.l + c0 - 1), pc = __ldg(a.c + c0 - 1);
+    for (int tb = c0; tb < c1; tb += 32) {
+        const int nt = min(32, c1 - tb);
+        float xh = 0.f, xl = 0.f, xc = 0.f;
+        if (lane < nt) {
+            xh = __ldg(a.h + tb + lane);
+            xl = __ldg(a.l + tb + lane);
+            xc = __ldg(a.c + tb + lane);
+        }
+        for (int j = 0; j < nt; ++j) {
+            const float ch = __shfl_sync(0xffffffffu, xh, j);
+            const float cl = __shfl_sync(0xffffffffu, xl, j);
+            const float cc = __shfl_sync(0xffffffffu, xc, j);
+            // PAdx::step_run's arithmetic
+            const float tr = fmaxf(fmaxf(ch - cl, fabsf(ch - pc)), fabsf(cl - pc));
+            const float up = ch - ph, down = pl - cl;
+            const float dp = (up > down && up > 0.f) ? up : 0.f;
+            const float dm = (down > up && down > 0.f) ? down : 0.f;
+            atr = atr * ln.omr + tr;
+            pdm = pdm * ln.omr + dp;
+            mdm = mdm * ln.omr + dm;
+            if (PASS != PASS_AGG1) adx = (adx * ln.pm1 + hlc::adx_dx(pdm, mdm, atr)) * ln.rp;
+            if (PASS == PASS_EMIT) stage[warp][lane][j] = adx;
+            ph = ch;
+            pl = cl;
+            pc = cc;
+        }
+        if (PASS == PASS_EMIT) {
+            __syncwarp();
+            if (lane < nt)
+                for (int r = 0; r < 32; ++r) {
+                    const int row = g * 32 + r;
+                    if (row >= a.n_combos) break;
+                    a.out[(size_t)row * a.n + tb + lane] = stage[warp][r][lane];
+                }
+            __syncwarp();
+        }
+    }
+    if (PASS == PASS_AGG1) a.agg1[si] = make_float4(atr, pdm, mdm, 0.f);
+    if (PASS == PASS_AGG2) a.agg2[si] = adx;
+}
+
+// Chunk-entry states per lane (one thread per lane slot), in double-single:
+// LEVEL 1: s_1 = the seeding run's end state, s_{k+1} = omr^len_k s_k + agg1_k;
+// LEVEL 2: adx_1 likewise, adx_{k+1} = (pm1 rp)^len_k adx_k + agg2_k.
+template <int LEVEL>
+__global__ void k_adx_carry(AdxScanArgs a) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= a.n_slots) return;
+    const int gi = slot >> 5;
+    const int ci = a.groups[gi] * 32 + (slot & 31);
+    if (ci >= a.n_combos) return;
+    Lane ln;
+    ln.init(__ldg(a.periods + ci));
+    const int s0 = a.group_s0[gi];
+    const int nch = 1 + (a.n - s0 + a.L - 1) / a.L;  // chunks of the group, chunk 0 included
+    const float* seed = a.seed_state + (size_t)ci * 8;  // k_hlc_chunk's chunk-0 end state
+    const D2s m = LEVEL == 1 ? D2s{ln.omr, 0.f} : ds_mul({ln.pm1, 0.f}, {ln.rp, 0.f});
+    const D2s mL = ds_pow(m, a.L);
+    D2s s[3];
+    if (LEVEL == 1) {
+        s[0] = {seed[0], 0.f};
+        s[1] = {seed[1], 0.f};
+        s[2] = {seed[2], 0.f};
+    } else {
+        s[0] = {seed[3], 0.f};
+    }
+    for (int k = 1; k < nch; ++k) {
+        const size_t si = (size_t)k * a.n_slots + slot;
+        if (LEVEL == 1) {
+            a.carry1[si] = make_float4(s[0].hi + s[0].lo, s[1].hi + s[1].lo, s[2].hi + s[2].lo, 0.f);
+            if (k + 1 < nch) {
+                const float4 g = a.agg1[si];
+                s[0] = ds_add(ds_mul(mL, s[0]), {g.x, 0.f});
+                s[1] = ds_add(ds_mul(mL, s[1]), {g.y, 0.f});
+                s[2] = ds_add(ds_mul(mL, s[2]), {g.z, 0.f});
+            }
+        } else {
+            a.carry2[si] = s[0].hi + s[0].lo;
+            if (k + 1 < nch) s[0] = ds_add(ds_mul(mL, s[0]), {a.agg2[si], 0.f});
+        }
+    }
+}
+
+}  // namespace
+
+vta_status launch_adx_scan(const AdxScanArgs& a, cudaStream_t st) {
+    if (a.n_items <= 0) return VTA_OK;
+    const unsigned blocks = ceil_div(a.n_items, kSW);
+    const unsigned cblocks = ceil_div(a.n_slots, 128);
+    k_adx_scan<PASS_AGG1><<<blocks, kSW * 32, 0, st>>>(a);
+    VTA_TRY(check_launch("k_adx_scan<agg1>"));
+    k_adx_carry<1><<<cblocks, 128, 0, st>>>(a);
+    VTA_TRY(check_launch("k_adx_carry<1>"));
+    k_adx_scan<PASS_AGG2><<<blocks, kSW * 32, 0, st>>>(a);
+    VTA_TRY(check_launch("k_adx_scan<agg2>"));
+    k_adx_carry<2><<<cblocks, 128, 0, st>>>(a);
+    VTA_TRY(check_launch("k_adx_carry<2>"));
+    k_adx_scan<PASS_EMIT><<<blocks, kSW * 32, 0, st>>>(a);
+    return check_launch("k_adx_scan<emit>");
+}
+
+}  // namespace vta

@@ -369,6 +369,10 @@ static int pick_chunk(vta_ctx* ctx, int n, int lanes, int warps_per_sm = 64) {
 // choices, never time); server slots never time.
 enum TuneKnob { TK_RECUR = 1, TK_MINMAX = 2, TK_RECUR_TC = 3 };
 constexpr int kMmApLabel = -1;  // last_kernel marker: the min/max progression kernel ran
+// ADX groups whose warm-restart run would exceed this many steps take the
+// exact chunked scan; its chunks are at least kAdxScanMinL steps long
+constexpr long long kAdxExactWarm = 4096;
+constexpr long long kAdxScanMinL = 1024;
 using SweepTuneKey = std::tuple<int, int, int, int>;
 static std::mutex g_stune_mu;
 static std::map<SweepTuneKey, int> g_stune;
@@ -904,6 +908,8 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
             std::vector<int2> items;
             int max_nch = 1;
             bool chunked = false;
+            std::vector<int> adx_groups, adx_s0;  // groups on the exact scan and their s0
+            int adx_L = 0;
             if (ctx->policy.recur_chunk != 1) {
                 // warm length per group: 32 p steps shrink the guessed state's
                 // error by (1 - 1/p)^(32 p) < e^-32, far below an f32 ulp, so the
@@ -916,13 +922,51 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
                     if (ctx->policy.tm_warm > 0) w = ((long long)ctx->policy.tm_warm + 31) & ~31LL;
                     return w;
                 };
+                // ADX groups whose warm run would be long take the exact
+                // chunked scan (k_adx_scan.cu) after a seeding chunk [0, s0)
+                // run here as the group's only item
+                if (ind == I_ADX && ctx->policy.tm_warm == 0) {
+                    std::vector<int> cand_g, cand_s0;
+                    for (int g = 0; g < G; ++g) {
+                        int pm = 1;
+                        for (int i = g * 32; i < std::min(nc, g * 32 + 32); ++i) pm = std::max(pm, periods[i]);
+                        const long long s0 = (((long long)first + 2LL * pm) + 31) & ~31LL;
+                        if (32LL * pm + 64 > kAdxExactWarm && s0 + 2LL * kAdxScanMinL <= n) {
+                            cand_g.push_back(g);
+                            cand_s0.push_back((int)s0);
+                        }
+                    }
+                    if (!cand_g.empty()) {
+                        // chunk length: about 2,400 warp items over the scan
+                        long long work = 0;
+                        for (int s0v : cand_s0) work += n - s0v;
+                        long long L = ((work / 2400) + 31) & ~31LL;
+                        L = std::max<long long>(kAdxScanMinL, std::min<long long>(16384, L));
+                        adx_L = (int)L;
+                        adx_groups = cand_g;
+                        adx_s0 = cand_s0;
+                    }
+                }
+                auto is_scan = [&](int g) {
+                    return std::find(adx_groups.begin(), adx_groups.end(), g) != adx_groups.end();
+                };
                 long long w_max = 0;
-                for (int g = 0; g < G; ++g) w_max = std::max(w_max, warm_of(g));
+                for (int g = 0; g < G; ++g)
+                    if (!is_scan(g)) w_max = std::max(w_max, warm_of(g));
                 // an item runs warm + chunk steps; the items of every group are
                 // made about equally long (1.5 x the longest warm), so the
                 // large-period groups' items do not form the critical path
                 const long long item_len = w_max + w_max / 2;
                 for (int g = 0; g < G; ++g) {
+                    if (is_scan(g)) {
+                        const size_t gi = (size_t)(std::find(adx_groups.begin(), adx_groups.end(), g) -
+                                                   adx_groups.begin());
+                        gchunk[g] = adx_s0[gi];  // chunk 0 = the seeding run; the scan does the rest
+                        gwarm[g] = 0;
+                        items.push_back(make_int2(g, 0));
+                        chunked = true;
+                        continue;
+                    }
                     const long long w = warm_of(g);
                     long long c = std::max<long long>(1024, item_len - w);
                     if (ctx->policy.recur_chunk > 1) c = std::max<long long>(ctx->policy.recur_chunk, w);
@@ -941,6 +985,15 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
                     return (long long)gchunk[x.x] + gwarm[x.x] > (long long)gchunk[y.x] + gwarm[y.x];
                 });
             }
+            // the exact scan's items and state slots
+            std::vector<int2> scan_items;
+            int scan_nch = 1;
+            for (size_t gi = 0; gi < adx_groups.size(); ++gi) {
+                const int nch_g = 1 + (int)((n - adx_s0[gi] + adx_L - 1) / adx_L);
+                scan_nch = std::max(scan_nch, nch_g);
+                for (int k = 1; k < nch_g; ++k) scan_items.push_back(make_int2((int)gi, k));
+            }
+            const size_t scan_slots = adx_groups.size() * 32;
             if (chunked) {
                 const size_t states = (size_t)max_nch * nc;
                 ar.need(G * sizeof(int));
@@ -951,6 +1004,15 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
                 ar.need(states);
                 ar.need(sizeof(int));
                 ar.need(nc * sizeof(int));
+                if (!adx_groups.empty()) {
+                    ar.need(adx_groups.size() * sizeof(int));
+                    ar.need(adx_groups.size() * sizeof(int));
+                    ar.need(scan_items.size() * sizeof(int2));
+                    ar.need((size_t)scan_nch * scan_slots * sizeof(float4));
+                    ar.need((size_t)scan_nch * scan_slots * sizeof(float4));
+                    ar.need((size_t)scan_nch * scan_slots * sizeof(float));
+                    ar.need((size_t)scan_nch * scan_slots * sizeof(float));
+                }
             }
             VTA_TRY(ar.commit());
             int* d_per = ar.take<int>(nc);
@@ -980,6 +1042,9 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
                 c.need = ar.take<int>(nc);
                 c.max_chunks = max_nch;
                 VTA_CUDA_TRY(cudaMemsetAsync(c.need, 0, nc * sizeof(int), st));
+                // chunks the warm-restart kernel does not write (the exact
+                // scan's groups) read as exact, so the fix-up leaves them alone
+                if (!adx_groups.empty()) VTA_CUDA_TRY(cudaMemsetAsync(c.exact, 1, states, st));
                 VTA_TRY(upload(ctx, d_gc, gchunk.data(), G * sizeof(int)));
                 VTA_TRY(upload(ctx, d_gw, gwarm.data(), G * sizeof(int)));
                 VTA_TRY(upload(ctx, d_items, items.data(), items.size() * sizeof(int2)));
@@ -991,7 +1056,38 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
                 c.out0 = out[0];
                 c.out1 = ind == I_SUPERTREND ? out[1] : nullptr;
                 ctx->last_kernel = ind == I_ADX ? "adx_chunked" : "supertrend_chunked";
-                return launch_hlc_chunk(c, st);
+                VTA_TRY(launch_hlc_chunk(c, st));
+                if (adx_groups.empty()) return VTA_OK;
+                AdxScanArgs x{};
+                x.h = in.p[0]; x.l = in.p[1]; x.c = in.p[2];
+                x.n = n;
+                x.periods = d_per;
+                x.n_combos = nc;
+                int* d_sg = ar.take<int>(adx_groups.size());
+                int* d_ss = ar.take<int>(adx_groups.size());
+                int2* d_si = ar.take<int2>(scan_items.size());
+                VTA_TRY(upload(ctx, d_sg, adx_groups.data(), adx_groups.size() * sizeof(int)));
+                VTA_TRY(upload(ctx, d_ss, adx_s0.data(), adx_s0.size() * sizeof(int)));
+                if (!scan_items.empty())
+                    VTA_TRY(upload(ctx, d_si, scan_items.data(), scan_items.size() * sizeof(int2)));
+                x.groups = d_sg;
+                x.group_s0 = d_ss;
+                x.n_groups = (int)adx_groups.size();
+                x.n_slots = (int)scan_slots;
+                x.L = adx_L;
+                x.items = d_si;
+                x.n_items = (int)scan_items.size();
+                x.seed_state = c.st_end;
+                x.agg1 = ar.take<float4>((size_t)scan_nch * scan_slots);
+                x.carry1 = ar.take<float4>((size_t)scan_nch * scan_slots);
+                x.agg2 = ar.take<float>((size_t)scan_nch * scan_slots);
+                x.carry2 = ar.take<float>((size_t)scan_nch * scan_slots);
+                x.out = out[0];
+                VTA_TRY(launch_adx_scan(x, st));
+                ktimer_end(st);  // the call's timing covers the scan too
+                ctx->last_kernel = "adx_chunked(" + std::to_string(adx_groups.size()) + " of " + std::to_string(G) +
+                                   " groups on the exact scan, L=" + std::to_string(adx_L) + ")";
+                return VTA_OK;
             }
             HlcArgs a{};
             a.layout = 0;

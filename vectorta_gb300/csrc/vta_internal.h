@@ -382,6 +382,33 @@ struct HlcChunkArgs {
     int max_chunks;
 };
 vta_status launch_hlc_chunk(const HlcChunkArgs& a, cudaStream_t st);
+// Exact chunked scan of batch ADX for 32-combo groups with long periods
+// (k_adx_scan.cu).  Group gi (combos groups[gi] * 32 ..) is seeded by
+// k_hlc_chunk's exact chunk-0 item over [0, group_s0[gi]); its chunks k >= 1
+// start at group_s0[gi] + (k - 1) L.  State slots: [chunk][n_slots], slot =
+// gi * 32 + lane.
+struct AdxScanArgs {
+    const float* h;
+    const float* l;
+    const float* c;
+    int n;
+    const int* periods;
+    int n_combos;
+    const int* groups;      // [n_groups] 32-combo group ids
+    const int* group_s0;    // [n_groups] start of chunk 1 (multiple of 32, past every lane's seeding)
+    int n_groups;
+    int n_slots;            // n_groups * 32
+    int L;                  // chunk length, multiple of 32
+    const int2* items;      // {group index, chunk >= 1}
+    int n_items;
+    const float* seed_state;  // [n_combos][8]: the chunk-0 end state (atr, +DM, -DM, adx)
+    float4* agg1;
+    float* agg2;
+    float4* carry1;
+    float* carry2;
+    float* out;             // [n_combos][n]
+};
+vta_status launch_adx_scan(const AdxScanArgs& a, cudaStream_t st);
 vta_status launch_supertrend(const HlcArgs& a, cudaStream_t st);
 
 // ------------------------------------------------- prefix-sum windows ------
