@@ -560,9 +560,10 @@ __device__ __forceinline__ void run_tile(Op& op, const InTile& ti, float* row, i
 }
 
 // RSI emit tile with finite inputs, in the scaled domain gs = ag p,
-// ls = al p: each lane forms its step's gain and loss once, then a step is two
-// shuffles and two FMAs; the output ratio gs / (gs + ls) is scale-free and the
-// state is scaled back at the end of the tile.
+// ls = al p: each lane forms its step's price difference once, then a step is
+// one shuffle, the gain / loss split and two FMAs; the output ratio
+// gs / (gs + ls) is scale-free and the state is scaled back at the end of the
+// tile.
 template <bool FIN, int PASS, bool kB>
 __device__ __forceinline__ void run_tile(OpRsi<kB>& op, const InTile& ti, float* row, int sw, int& steps) {
     if constexpr (!(FIN && PASS == PASS_EMIT)) {
@@ -575,13 +576,15 @@ __device__ __forceinline__ void run_tile(OpRsi<kB>& op, const InTile& ti, float*
         float xp = __shfl_up_sync(0xffffffffu, ti.xv, 1);
         if ((threadIdx.x & 31) == 0) xp = ti.xb;
         const float d = ti.xv - xp;
-        const float gl = d > 0.f ? d : 0.f, ll = d < 0.f ? -d : 0.f;
         float gs = op.ag * op.pf, ls = op.al * op.pf;
         const float b = op.beta;
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
-            gs = fmaf(b, gs, __shfl_sync(0xffffffffu, gl, j));
-            ls = fmaf(b, ls, __shfl_sync(0xffffffffu, ll, j));
+            // one shuffle of the signed difference per step: the gain is
+            // max(d, 0) and the loss -min(d, 0) (one of them is zero)
+            const float dj = __shfl_sync(0xffffffffu, d, j);
+            gs = fmaf(b, gs, fmaxf(dj, 0.f));
+            ls = fmaf(b, ls, -fminf(dj, 0.f));
             const float den = gs + ls;
             stage_put(row, sw, j, den == 0.f ? 50.f : __fdividef(100.f * gs, den));
         }
