@@ -19,8 +19,9 @@
 //   EMIT   per (group, chunk): both levels from their entry states, outputs.
 // The seeding run (chunk 0, up to the group's s0) is k_hlc_chunk's exact
 // chunk-0 item.  Outputs differ from one sequential f32 pass by the rounding
-// of the composed carries (a few 1e-7 relative); a NaN input propagates to
-// every later output as in the sequential pass.
+// of the composed carries (a few 1e-7 relative); a NaN bar enters the sums
+// through the same NaN-skipping max and comparisons as in the sequential
+// pass.
 #include <algorithm>
 
 #include "hlc_ops.cuh"
@@ -164,19 +165,30 @@ __global__ void k_adx_carry(AdxScanArgs a) {
     } else {
         s[0] = {seed[3], 0.f};
     }
+    // the chunk aggregates come through a 4-deep register queue, so their
+    // loads run ahead of the dependent double-single updates
+    auto rec = [&](int k) {
+        const size_t si = (size_t)k * a.n_slots + slot;
+        if (k + 1 >= nch) return make_float4(0.f, 0.f, 0.f, 0.f);
+        return LEVEL == 1 ? __ldg(a.agg1 + si) : make_float4(__ldg(a.agg2 + si), 0.f, 0.f, 0.f);
+    };
+    float4 q0 = rec(1), q1 = rec(2), q2 = rec(3), q3 = rec(4);
+#pragma unroll 1
     for (int k = 1; k < nch; ++k) {
+        const float4 g = q0;
+        q0 = q1;
+        q1 = q2;
+        q2 = q3;
+        q3 = rec(k + 4);
         const size_t si = (size_t)k * a.n_slots + slot;
         if (LEVEL == 1) {
             a.carry1[si] = make_float4(s[0].hi + s[0].lo, s[1].hi + s[1].lo, s[2].hi + s[2].lo, 0.f);
-            if (k + 1 < nch) {
-                const float4 g = a.agg1[si];
-                s[0] = ds_add(ds_mul(mL, s[0]), {g.x, 0.f});
-                s[1] = ds_add(ds_mul(mL, s[1]), {g.y, 0.f});
-                s[2] = ds_add(ds_mul(mL, s[2]), {g.z, 0.f});
-            }
+            s[0] = ds_add(ds_mul(mL, s[0]), {g.x, 0.f});
+            s[1] = ds_add(ds_mul(mL, s[1]), {g.y, 0.f});
+            s[2] = ds_add(ds_mul(mL, s[2]), {g.z, 0.f});
         } else {
             a.carry2[si] = s[0].hi + s[0].lo;
-            if (k + 1 < nch) s[0] = ds_add(ds_mul(mL, s[0]), {a.agg2[si], 0.f});
+            s[0] = ds_add(ds_mul(mL, s[0]), {g.x, 0.f});
         }
     }
 }
