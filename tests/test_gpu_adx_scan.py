@@ -65,6 +65,24 @@ def test_scan_with_nan_gap():
     close(got, seq, 1e-5, 1e-4, "scan vs sequential with NaN bars")
 
 
+@pytest.mark.parametrize("chunk", ["1024", "3008"])
+def test_scan_chunk_lengths(chunk):
+    # the chunk length changes only how the carries compose
+    h, l, c = hlc(70_000, 87)
+    sweep = {"period": (180, 300, 4)}
+    got, kern = run(h, l, c, sweep, ("scan_chunk", chunk))
+    assert f"L={chunk}" in kern, kern
+    seq, _ = run(h, l, c, sweep, ("recur_chunk", "sequential"))
+    close(got, seq, 1e-5, 1e-4, f"scan L={chunk} vs sequential")
+
+
+def test_scan_chunk_policy_rejects_bad_lengths():
+    ind = V.CLASSES["adx"](0)
+    for bad in ("1000", "512", "x"):
+        with pytest.raises(Exception):
+            ind.set_policy("scan_chunk", bad)
+
+
 def test_short_periods_stay_bit_identical():
     # every group below the threshold: the warm-restart path alone
     h, l, c = hlc(40_000, 85)

@@ -942,6 +942,7 @@ static vta_status run_batch(vta_ctx* ctx, Ind ind, const DevIn& in, size_t len, 
                         for (int s0v : cand_s0) work += n - s0v;
                         long long L = ((work / 2400) + 31) & ~31LL;
                         L = std::max<long long>(kAdxScanMinL, std::min<long long>(16384, L));
+                        if (ctx->policy.scan_chunk > 0) L = ctx->policy.scan_chunk;
                         adx_L = (int)L;
                         adx_groups = cand_g;
                         adx_s0 = cand_s0;
@@ -2086,6 +2087,20 @@ vta_status vta_ctx_set_policy(vta_ctx* ctx, const char* key, const char* value) 
         else if (v == "off") ctx->policy.tune = 1;
         else if (v == "cached") ctx->policy.tune = 2;
         else return fail(VTA_ERR_INVALID_POLICY, "tune: on|off|cached");
+        return VTA_OK;
+    }
+    if (k == "scan_chunk") {
+        // chunk length of the exact ADX scan: "auto" or a multiple of 32 of
+        // at least 1,024 steps
+        if (v == "auto") {
+            ctx->policy.scan_chunk = 0;
+            return VTA_OK;
+        }
+        char* end = nullptr;
+        long x = std::strtol(v.c_str(), &end, 10);
+        if (!end || *end || x < kAdxScanMinL || x > (1L << 24) || x % 32)
+            return fail(VTA_ERR_INVALID_POLICY, "scan_chunk: auto | multiple of 32 >= 1024");
+        ctx->policy.scan_chunk = (int)x;
         return VTA_OK;
     }
     if (k == "tm_chunk" || k == "tm_warm") {

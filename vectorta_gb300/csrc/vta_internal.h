@@ -69,6 +69,8 @@ struct Policy {
     // (tensor-core contraction where the sweep is eligible), 1 = CUDA cores
     // only, 2 = tensor cores required (an ineligible sweep is an error)
     int recur_agg = 0;
+    // chunk length of the exact ADX scan (0 = auto: about 2,400 warp items)
+    int scan_chunk = 0;
 };
 
 }  // namespace vta
