@@ -79,6 +79,7 @@ struct InTile {
     float xv, hv, lv, cv;  // this lane's element of the tile
     float xb, cb;          // x[tb-1], c[tb-1]
     int tb;
+    float4* xs;  // this warp's 2 x 32-float input scratch in shared memory
     __device__ float X(int t) const {
         const int j = t - tb;
         const float v = __shfl_sync(0xffffffffu, xv, j & 31);
@@ -372,16 +373,17 @@ struct OpRsi {
     static constexpr int NS = 2;
     static constexpr int kShape = 2;
     float inv_p, beta, ag, al, xprev, pf;
+    float sN, sD;  // the emit tiles' scaled state while sc (run_tile below)
     int f, s, warm;
     Acc sg, sl;
-    bool wnan;
+    bool wnan, sc;
     __device__ void init(int p, int first) {
         double ip = 1.0 / (double)p;
         inv_p = (float)ip;
         pf = (float)p;
         beta = (float)(1.0 - ip);
         f = first; s = first + p; warm = s;
-        sg.zero(); sl.zero(); wnan = false;
+        sg.zero(); sl.zero(); wnan = false; sc = false;
     }
     template <class In> __device__ void accum(const In& in, int t) {
         float v = in.X(t);
@@ -559,11 +561,46 @@ __device__ __forceinline__ void run_tile(Op& op, const InTile& ti, float* row, i
     }
 }
 
-// RSI emit tile with finite inputs, in the scaled domain gs = ag p,
-// ls = al p: each lane forms its step's price difference once, then a step is
-// one shuffle, the gain / loss split and two FMAs; the output ratio
-// gs / (gs + ls) is scale-free and the state is scaled back at the end of the
-// tile.
+// 1 / x by the hardware approximation (relative error within about 2^-23;
+// subnormal x is read as zero), one instruction
+__device__ __forceinline__ float rcp_approx_ftz(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// The 32 steps of an RSI emit tile on the scaled state (see run_tile below);
+// NORMAL: D stays normal over the tile.
+template <bool NORMAL, bool kB>
+__device__ __forceinline__ void rsi_emit_steps(OpRsi<kB>& op, const InTile& ti, float* row, int sw) {
+    float N = op.sN, D = op.sD;
+    const float b = op.beta;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const float4 e4 = ti.xs[q], a4 = ti.xs[8 + q];
+        const float ev[4] = {e4.x, e4.y, e4.z, e4.w}, av[4] = {a4.x, a4.y, a4.z, a4.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            N = fmaf(b, N, fmaxf(ev[u], 0.f));
+            D = fmaf(b, D, av[u]);
+            const float y = NORMAL ? N * rcp_approx_ftz(D) : (D == 0.f ? 50.f : __fdividef(N, D));
+            stage_put(row, sw, 4 * q + u, y);
+        }
+    }
+    op.sN = N;
+    op.sD = D;
+}
+
+// RSI emit tile with finite inputs.  Across consecutive such tiles the state
+// is held as
+//   N = 100 ag p       (the gain sum, scaled by 100 p)
+//   D = (ag + al) p    (the gain + loss sum: its input is |d|)
+// so a step is N <- b N + max(100 d, 0), D <- b D + |d| and the output
+// 100 ag / (ag + al) = N / D: two FMAs and a max, no per-step scaling.  Each
+// lane forms its step's 100 d and |d| once; the warp reads them back from
+// shared memory four steps per 16-byte broadcast load.  The state goes back
+// to (ag, al) only when the lane leaves these tiles (rsi_fast_exit), so the
+// scale factors' roundings do not build up from tile to tile.
 template <bool FIN, int PASS, bool kB>
 __device__ __forceinline__ void run_tile(OpRsi<kB>& op, const InTile& ti, float* row, int sw, int& steps) {
     if constexpr (!(FIN && PASS == PASS_EMIT)) {
@@ -573,24 +610,39 @@ __device__ __forceinline__ void run_tile(OpRsi<kB>& op, const InTile& ti, float*
             if (PASS == PASS_EMIT) stage_put(row, sw, j, y);
         }
     } else {
+        const int lane = threadIdx.x & 31;
         float xp = __shfl_up_sync(0xffffffffu, ti.xv, 1);
-        if ((threadIdx.x & 31) == 0) xp = ti.xb;
+        if (lane == 0) xp = ti.xb;
         const float d = ti.xv - xp;
-        float gs = op.ag * op.pf, ls = op.al * op.pf;
-        const float b = op.beta;
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            // one shuffle of the signed difference per step: the gain is
-            // max(d, 0) and the loss -min(d, 0) (one of them is zero)
-            const float dj = __shfl_sync(0xffffffffu, d, j);
-            gs = fmaf(b, gs, fmaxf(dj, 0.f));
-            ls = fmaf(b, ls, -fminf(dj, 0.f));
-            const float den = gs + ls;
-            stage_put(row, sw, j, den == 0.f ? 50.f : __fdividef(100.f * gs, den));
+        float* xs = reinterpret_cast<float*>(ti.xs);
+        __syncwarp();  // the previous tile's reads are done
+        xs[lane] = 100.f * d;
+        xs[32 + lane] = fabsf(d);
+        __syncwarp();
+        if (!op.sc) {
+            op.sN = op.ag * (100.f * op.pf);  // 100 p is exact
+            op.sD = (op.ag + op.al) * op.pf;
+            op.sc = true;
         }
-        op.ag = gs * op.inv_p;
-        op.al = ls * op.inv_p;
+        // D never shrinks by more than b^32 >= 2^-32 over a tile (its inputs
+        // are >= 0), so a tile entered with D >= 2^-60 keeps D normal and
+        // nonzero: the output is N times the hardware reciprocal, with no
+        // zero guard or subnormal handling
+        if (__all_sync(0xffffffffu, op.sD >= 0x1p-60f))
+            rsi_emit_steps<true>(op, ti, row, sw);
+        else
+            rsi_emit_steps<false>(op, ti, row, sw);
         steps += 32;
+    }
+}
+
+// (ag, al) from the scaled emit-tile state, before any other step reads them
+template <class Op> __device__ __forceinline__ void rsi_fast_exit(Op&) {}
+template <bool kB> __device__ __forceinline__ void rsi_fast_exit(OpRsi<kB>& op) {
+    if (op.sc) {
+        op.ag = (op.sN * 0.01f) * op.inv_p;
+        op.al = fmaf(op.sD, op.inv_p, -op.ag);
+        op.sc = false;
     }
 }
 
@@ -1088,6 +1140,8 @@ template <class Op, bool TM, int PASS>
 __global__ void __launch_bounds__(kWarps * 32)
 k_recur(RecurArgs a) {
     __shared__ __align__(16) float stage[kWarps][32][(PASS == PASS_EMIT && !TM) ? kStageW : 33];
+    // per warp: a fast tile's broadcast inputs (EMIT), 2 x 32 floats
+    __shared__ float4 xin[kWarps][PASS == PASS_EMIT ? 16 : 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int group = blockIdx.x * kWarps + warp;
     const int li = group * 32 + lane;
@@ -1217,6 +1271,7 @@ k_recur(RecurArgs a) {
                 // the tile's inputs in registers, one coalesced load per lane
                 InTile ti;
                 ti.tb = tb;
+                ti.xs = &xin[warp][0];
                 if constexpr (Op::kHlc) {
                     ti.hv = __ldg(a.h + tb + lane);
                     ti.lv = __ldg(a.l + tb + lane);
@@ -1240,9 +1295,11 @@ k_recur(RecurArgs a) {
                 if (fin) {
                     run_tile<true, PASS>(op, ti, srow, sw, steps);
                 } else {
+                    rsi_fast_exit(op);
                     run_tile<false, PASS>(op, ti, srow, sw, steps);
                 }
             } else if (PASS == PASS_EMIT && !TM) {
+                rsi_fast_exit(op);
 #pragma unroll 8
                 for (int t = tb; t < te; ++t) srow[(t - tb) ^ sw] = op.fast(in, t, steps);
             } else if (PASS == PASS_EMIT) {
@@ -1257,6 +1314,7 @@ k_recur(RecurArgs a) {
             }
         } else {
             // ---- general path: per-step phase logic
+            rsi_fast_exit(op);  // (a no-op: general tiles come before the fast ones)
             auto gen_step = [&](const auto& in_, int t) -> float {
                 return general_step(op, active, seeded_ever, running, steps, in_, t);
             };
