@@ -625,10 +625,11 @@ __device__ __forceinline__ void run_tile(OpRsi<kB>& op, const InTile& ti, float*
             op.sc = true;
         }
         // D never shrinks by more than b^32 >= 2^-32 over a tile (its inputs
-        // are >= 0), so a tile entered with D >= 2^-60 keeps D normal and
-        // nonzero: the output is N times the hardware reciprocal, with no
-        // zero guard or subnormal handling
-        if (__all_sync(0xffffffffu, op.sD >= 0x1p-60f))
+        // are >= 0) nor grows past D + 32 max|d|, so a tile entered with D in
+        // [2^-60, 2^100] and every |d| <= 2^100 keeps D and 1 / D normal: the
+        // output is N times the hardware reciprocal, with no zero guard or
+        // subnormal handling
+        if (__all_sync(0xffffffffu, op.sD >= 0x1p-60f && op.sD <= 0x1p100f && fabsf(d) <= 0x1p100f))
             rsi_emit_steps<true>(op, ti, row, sw);
         else
             rsi_emit_steps<false>(op, ti, row, sw);

@@ -502,6 +502,20 @@ __global__ void k_first_nan_after_tm(const float* __restrict__ x, int cols, int 
 // non-finite rule for Donchian p > 32, donchian.rs:327-346 / 413-480).
 constexpr int kMmThreads = 512;
 
+// WillR of a slot whose range hmax - lmin lies in [2^-100, 2^120]
+// (willr_wide_ok): the hardware reciprocal of a range whose reciprocal is
+// normal (relative error within about 2^-23, like the fast divide) with no
+// zero guard or subnormal handling.  Tiles use it when every slot of the warp
+// qualifies; the others take the guarded form.
+__device__ __forceinline__ bool willr_wide_ok(float range) {
+    return range >= 0x1p-100f && range <= 0x1p120f;
+}
+__device__ __forceinline__ float willr_wide(float hmax, float lmin, float c) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(hmax - lmin));
+    return fmaf(-100.f, (hmax - c) * r, 0.f);
+}
+
 // Outputs of a clean tile (every window past its warm-up is valid): combo-
 // outer, so a combo's table offsets are read once for the thread's PER times
 // t = t0 + tid + k * THREADS; the closes are read once for all combos.
@@ -543,8 +557,26 @@ __device__ __forceinline__ void minmax_clean(const MinMaxArgs& a, const float* m
             }
         };
         if (full && t0 >= ct.y) {  // the whole tile is valid for this combo (uniform branch)
+            bool fast = KIND == MM_WILLR;
+            if (KIND == MM_WILLR) {
+                bool wide = true;
 #pragma unroll
-            for (int k = 0; k < PER; ++k) emit(k, true);
+                for (int k = 0; k < PER; ++k)
+                    wide = wide && willr_wide_ok(fmaxf(mz[k * THREADS], mw[k * THREADS]) -
+                                                 fminf(nz[k * THREADS], nw[k * THREADS]));
+                fast = __all_sync(0xffffffffu, wide);
+            }
+            if (fast) {
+#pragma unroll
+                for (int k = 0; k < PER; ++k) {
+                    const float hmax = fmaxf(mz[k * THREADS], mw[k * THREADS]);
+                    const float lmin = fminf(nz[k * THREADS], nw[k * THREADS]);
+                    r0[k * THREADS] = willr_wide(hmax, lmin, cl[k]);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < PER; ++k) emit(k, true);
+            }
         } else {
 #pragma unroll
             for (int k = 0; k < PER; ++k) {
@@ -801,8 +833,20 @@ __global__ void __launch_bounds__(THREADS) k_minmax_ap(MinMaxArgs a, int tile, i
             }
         };
         if (full && t0 >= warm) {  // the whole tile is valid for this combo (uniform branch)
+            bool fast = KIND == MM_WILLR;
+            if (KIND == MM_WILLR) {
+                bool wide = true;
 #pragma unroll
-            for (int k = 0; k < PER; ++k) emit(k, true);
+                for (int k = 0; k < PER; ++k) wide = wide && willr_wide_ok(hm[k] - lm[k]);
+                fast = __all_sync(0xffffffffu, wide);
+            }
+            if (fast) {
+#pragma unroll
+                for (int k = 0; k < PER; ++k) r0[k * THREADS] = willr_wide(hm[k], lm[k], cl[k]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < PER; ++k) emit(k, true);
+            }
         } else {
 #pragma unroll
             for (int k = 0; k < PER; ++k) {
