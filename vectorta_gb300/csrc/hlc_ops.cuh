@@ -13,6 +13,8 @@
 //   step(in, t, o1) -> o0        process t (any phase), outputs for t
 //   stepv(t, h, l, c, o1) -> o0  the same with the inputs of t given
 //   step_run(h, l, c, o1) -> o0  stepv for t >= run_from() without phase checks
+//   (ADX also: wide_ok(h, l, c) and step_run<true> for tiles of up to 32 steps
+//   whose sums stay normal, with DX by the hardware reciprocal)
 // `In` provides H(t), L(t), C(t).  The arithmetic of each op is that of the
 // sequential kernels in k_hlc.cu, so a run that starts at the series start is
 // bit-identical to them.
@@ -43,6 +45,32 @@ __device__ __forceinline__ float true_range(float hi, float lo, float pc) {
 // the ADX sweeps and plans are issue-bound and the IEEE divide was a third of
 // a step); every ADX kernel shares this function, so the chunked and the
 // sequential kernels stay bit-identical.
+// 1 / x by the hardware approximation (relative error within about 2^-23;
+// subnormal x is read as zero), one instruction
+__device__ __forceinline__ float rcp_approx_ftz(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Whether up to 32 running ADX steps from this state keep atr and
+// pdm + mdm normal and nonzero, given the inputs of those steps and of the
+// bar before them (x*, p*): the sums shrink by at most omr^32 >= 2^-32 and
+// grow by at most 32 x 2^100 when every price is within 2^98 in magnitude,
+// so sums in [2^-60, 2^100] at the start stay within [2^-92, 2^106].  On such
+// steps DX = |pdm - mdm| / (pdm + mdm) 100 needs none of adx_dx's guards
+// (adx_dx_wide).  NaN prices or sums fail the test.
+__device__ __forceinline__ bool adx_wide_ok(float atr, float pdm, float mdm, float xh, float xl, float xc,
+                                            float ph, float pl, float pc) {
+    const float s = pdm + mdm;
+    const bool in_range = fabsf(xh) <= 0x1p98f && fabsf(xl) <= 0x1p98f && fabsf(xc) <= 0x1p98f &&
+                          fabsf(ph) <= 0x1p98f && fabsf(pl) <= 0x1p98f && fabsf(pc) <= 0x1p98f;
+    return in_range && atr >= 0x1p-60f && atr <= 0x1p100f && s >= 0x1p-60f && s <= 0x1p100f;
+}
+__device__ __forceinline__ float adx_dx_wide(float pdm, float mdm) {
+    return fabsf(pdm - mdm) * rcp_approx_ftz(pdm + mdm) * 100.f;
+}
+
 __device__ __forceinline__ float adx_dx(float pdm, float mdm, float atr) {
     if (atr == 0.f) return 0.f;
     const float s = pdm + mdm;
@@ -98,6 +126,7 @@ struct PAtr {
         return rma;
     }
     // stepv for t >= run_from(): the running update alone
+    template <bool WIDE = false>  // (no division: one form)
     __device__ __forceinline__ float step_run(float hi, float lo, float cl, float&) {
         const float tr = true_range(hi, lo, pc);
         pc = cl;
@@ -188,7 +217,9 @@ struct PAdx {
         ph = ch; pl = cl; pc = cc;
         return v;
     }
-    // stepv for t >= run_from(): the running update alone
+    // stepv for t >= run_from(): the running update alone; WIDE: the steps
+    // of a tile for which wide_ok held on every lane at its start
+    template <bool WIDE = false>
     __device__ __forceinline__ float step_run(float ch, float cl, float cc, float&) {
         const float tr = fmaxf(fmaxf(ch - cl, fabsf(ch - pc)), fabsf(cl - pc));
         const float up = ch - ph, down = pl - cl;
@@ -197,9 +228,13 @@ struct PAdx {
         atr = atr * omr + tr;
         pdm = pdm * omr + dp;
         mdm = mdm * omr + dm;
-        adx = (adx * pm1 + adx_dx(pdm, mdm, atr)) * rp;
+        adx = (adx * pm1 + (WIDE ? adx_dx_wide(pdm, mdm) : adx_dx(pdm, mdm, atr))) * rp;
         ph = ch; pl = cl; pc = cc;
         return adx;
+    }
+    static constexpr bool kWide = true;
+    __device__ bool wide_ok(float xh, float xl, float xc) const {
+        return adx_wide_ok(atr, pdm, mdm, xh, xl, xc, ph, pl, pc);
     }
 };
 
@@ -292,6 +327,7 @@ struct PSuperTrend {
         return v0;
     }
     // stepv for t >= run_from(): the running update alone
+    template <bool WIDE = false>  // (no division: one form)
     __device__ __forceinline__ float step_run(float hi, float lo, float cl, float& v1) {
         float tr = hi - lo;
         const float hc = fabsf(hi - pc);

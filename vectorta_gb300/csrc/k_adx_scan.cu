@@ -73,13 +73,6 @@ struct Lane {
 
 enum { PASS_AGG1 = 0, PASS_AGG2 = 1, PASS_EMIT = 2 };
 
-// 1 / x by the hardware approximation (relative error within about 2^-23;
-// subnormal x is read as zero), one instruction
-__device__ __forceinline__ float rcp_approx_ftz(float x) {
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
 
 // One (group, chunk >= 1) item per warp; lane = combo of the group.
 template <int PASS>
@@ -131,8 +124,7 @@ __global__ void __launch_bounds__(kSW * 32) k_adx_scan(AdxScanArgs a) {
                 pdm = pdm * ln.omr + dp;
                 mdm = mdm * ln.omr + dm;
                 if (PASS != PASS_AGG1) {
-                    const float dx = WIDE ? fabsf(pdm - mdm) * rcp_approx_ftz(pdm + mdm) * 100.f
-                                          : hlc::adx_dx(pdm, mdm, atr);
+                    const float dx = WIDE ? hlc::adx_dx_wide(pdm, mdm) : hlc::adx_dx(pdm, mdm, atr);
                     adx = (adx * ln.pm1 + dx) * ln.rp;
                 }
                 if (PASS == PASS_EMIT) stage[warp][lane][j] = adx;
@@ -141,19 +133,10 @@ __global__ void __launch_bounds__(kSW * 32) k_adx_scan(AdxScanArgs a) {
                 pc = cc;
             }
         };
-        // The sums shrink by at most omr^32 >= 2^-32 over these <= 32 steps
-        // and grow by at most 32 x 2^100 when every price is within 2^98 in
-        // magnitude, so with atr and pdm + mdm in [2^-60, 2^100] at the start
-        // both stay normal and nonzero: DX = |pdm - mdm| / (pdm + mdm) 100
-        // takes the hardware reciprocal without adx_dx's guards.
-        bool wide = false;
-        if (PASS != PASS_AGG1) {
-            const float s = pdm + mdm;
-            const bool in_range = fabsf(xh) <= 0x1p98f && fabsf(xl) <= 0x1p98f && fabsf(xc) <= 0x1p98f &&
-                                  fabsf(ph) <= 0x1p98f && fabsf(pl) <= 0x1p98f && fabsf(pc) <= 0x1p98f;
-            wide = __all_sync(0xffffffffu, in_range && atr >= 0x1p-60f && atr <= 0x1p100f && s >= 0x1p-60f &&
-                                               s <= 0x1p100f);
-        }
+        // DX by the hardware reciprocal where the sums stay normal over
+        // these steps (hlc::adx_wide_ok)
+        const bool wide = PASS != PASS_AGG1 &&
+                          __all_sync(0xffffffffu, hlc::adx_wide_ok(atr, pdm, mdm, xh, xl, xc, ph, pl, pc));
         if (wide)
             steps(std::true_type{});
         else

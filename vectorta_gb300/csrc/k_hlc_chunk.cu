@@ -17,6 +17,7 @@
 // row per array) and broadcast step by step with shuffles; outputs are staged
 // per warp in shared memory and written as 32 rows x 128 bytes.
 #include <algorithm>
+#include <type_traits>
 
 #include "hlc_ops.cuh"
 #include "vta_internal.h"
@@ -25,6 +26,10 @@ namespace vta {
 namespace {
 
 constexpr int kCW = 4;  // warps per block
+
+// ops with a wide-tile step form (hlc_ops.cuh)
+template <class Op, class = void> struct HasWide : std::false_type {};
+template <class Op> struct HasWide<Op, std::void_t<decltype(Op::kWide)>> : std::true_type {};
 
 struct In1 {
     const float *h, *l, *c;
@@ -81,18 +86,26 @@ __global__ void __launch_bounds__(kCW * 32) k_hlc_chunk(HlcChunkArgs a) {
                 xc = __ldg(a.c + tj);
             }
             if (tb >= rf && nt == 32) {
+                auto run32 = [&](auto wide_tag) {
 #pragma unroll 8
-                for (int j = 0; j < 32; ++j) {
-                    const float hv = __shfl_sync(0xffffffffu, xh, j);
-                    const float lv = __shfl_sync(0xffffffffu, xl, j);
-                    const float cv = __shfl_sync(0xffffffffu, xc, j);
-                    float o1;
-                    const float o0 = op.step_run(hv, lv, cv, o1);
-                    if (emit) {
-                        stage0[warp][lane][j] = o0;
-                        if (Op::kTwo) stage1[warp][lane][j] = o1;
+                    for (int j = 0; j < 32; ++j) {
+                        const float hv = __shfl_sync(0xffffffffu, xh, j);
+                        const float lv = __shfl_sync(0xffffffffu, xl, j);
+                        const float cv = __shfl_sync(0xffffffffu, xc, j);
+                        float o1;
+                        const float o0 = op.template step_run<decltype(wide_tag)::value>(hv, lv, cv, o1);
+                        if (emit) {
+                            stage0[warp][lane][j] = o0;
+                            if (Op::kTwo) stage1[warp][lane][j] = o1;
+                        }
                     }
-                }
+                };
+                bool wide = false;
+                if constexpr (HasWide<Op>::value) wide = __all_sync(0xffffffffu, op.wide_ok(xh, xl, xc));
+                if (wide)
+                    run32(std::true_type{});
+                else
+                    run32(std::false_type{});
             } else {
                 for (int j = 0; j < nt; ++j) {
                     const float hv = __shfl_sync(0xffffffffu, xh, j);
