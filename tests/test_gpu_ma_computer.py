@@ -87,3 +87,27 @@ def test_ma_selector_single_and_sweep(series):
     assert_close(d, np.stack([O.epma(xd, p, 3) for p in (12, 16, 20)]), TOL["epma"], "selector epma")
     h1 = sel.ma_to_host_f32("ema", x, 21)
     assert_close(h1, O.ema(xd, 21), TOL["ema"], "selector to host")
+
+
+def test_shared_context_buffers_survive_host_io_growth(series):
+    # the MA computer's time-major staging buffer and the into-host I/O buffer
+    # live in the same context: growing one leaves the other usable
+    import torch
+
+    x, dx = series
+    ctx = V.Context(0)
+    mc = V.VramMaComputer(0, ctx=ctx)
+    first = int(np.argmax(~np.isnan(x)))
+    periods = [5, 9, 30]
+    tm1 = torch.empty(x.size, len(periods), device="cuda")
+    mc.compute_period_ma_into("ema", {}, dx, x.size, first, periods, tm1, time_major=True)
+    ema = V.CLASSES["ema"](0, ctx=ctx)
+    for hi in (50, 400):  # the second call needs a larger I/O buffer
+        h, rows, cols = ema.batch_into_host_f32(x, sweep={"period": (2, hi, 1)})
+        assert rows == hi - 1 and cols == x.size
+    tm2 = torch.empty(x.size, len(periods), device="cuda")
+    mc.compute_period_ma_into("ema", {}, dx, x.size, first, periods, tm2, time_major=True)
+    ctx.synchronize()
+    assert np.array_equal(tm1.cpu().numpy(), tm2.cpu().numpy(), equal_nan=True)
+    exp = np.stack([O.ema(x.astype(np.float64), p) for p in periods])
+    assert_close(tm2.cpu().numpy().T, exp, TOL["ema"], "ma computer after host I/O growth")

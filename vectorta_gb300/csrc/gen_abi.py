@@ -246,7 +246,10 @@ vta_status vta_streams_reset(vta_streams* s);
 vta_status vta_streams_destroy(vta_streams* s);
 
 /* Page-locked host buffers for fast copies (the crate's LockedBuffer,
- * alma_wrapper.rs:810-815). */
+ * alma_wrapper.rs:810-815).  They are mapped into the device address space:
+ * a *_batch_into_host_f32 output buffer that lies inside one takes the
+ * kernels' stores directly, with no device buffer or copy (policy "host_out"
+ * = "direct", the default; "copy" stages through the device). */
 vta_status vta_pinned_alloc(size_t bytes, void** out);
 vta_status vta_pinned_free(void* p);
 /* Plain device buffers for callers without their own allocator. */

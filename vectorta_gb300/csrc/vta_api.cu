@@ -1393,6 +1393,27 @@ static vta_status sync(vta_ctx* ctx) {
     return check_async("stream");
 }
 
+// Blocks from vta_pinned_alloc are mapped into every device's address space;
+// the registry lets the into-host calls recognise an output buffer that lies
+// wholly inside one and have the kernels store into it directly.
+struct PinnedBlock {
+    size_t bytes;
+    char* dev;
+};
+static std::mutex g_pin_mu;
+static std::map<uintptr_t, PinnedBlock> g_pin;
+
+float* pinned_device_view(const void* p, size_t bytes) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    auto it = g_pin.upper_bound(a);
+    if (it == g_pin.begin()) return nullptr;
+    --it;
+    const uintptr_t off = a - it->first;
+    if (off > it->second.bytes || bytes > it->second.bytes - off) return nullptr;
+    return reinterpret_cast<float*>(it->second.dev + off);
+}
+
 // host inputs -> device outputs (`out_dev` non-null: caller's device buffers;
 // `out_host` non-null: copy results into host buffers of out_len floats)
 static vta_status batch_host(vta_ctx* ctx, Ind ind, const float* const* hin, size_t len,
@@ -1411,6 +1432,18 @@ static vta_status batch_host(vta_ctx* ctx, Ind ind, const float* const* hin, siz
     if (out_host && out_len < out_elems) return fail(VTA_ERR_INVALID_INPUT, "output buffer too small");
     const size_t in_bytes = len * sizeof(float) * nin;
     const size_t out_bytes = out_elems * sizeof(float);
+    // an output buffer from vta_pinned_alloc takes the kernels' stores
+    // directly (one pass over the host link instead of a device buffer and a
+    // copy); the others go through device buffers and a copy
+    float* direct[3] = {nullptr, nullptr, nullptr};
+    int n_staged = nout;
+    if (out_host && ctx->policy.host_out == 0) {
+        n_staged = 0;
+        for (int k = 0; k < nout; ++k) {
+            direct[k] = pinned_device_view(out_host[k], out_bytes);
+            if (!direct[k]) ++n_staged;
+        }
+    }
     // into-host calls with the cached policy keep one device buffer for the
     // inputs and outputs in the context (grown when too small), so repeated
     // calls do not pay a cudaMalloc / cudaFree of their outputs each time
@@ -1421,11 +1454,10 @@ static vta_status batch_host(vta_ctx* ctx, Ind ind, const float* const* hin, siz
     if (cached) {
         const size_t in_al = (in_bytes + 255) & ~size_t(255);
         const size_t out_al = (out_bytes + 255) & ~size_t(255);
-        const size_t need = in_al + out_al * nout;
+        const size_t need = in_al + out_al * n_staged;
         if (need > ctx->io_bytes) {
             VTA_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
             if (ctx->io) cudaFree(ctx->io);
-    if (ctx->tmp) cudaFree(ctx->tmp);
             ctx->io = nullptr;
             ctx->io_bytes = 0;
             VTA_TRY(vram_check(need));
@@ -1434,12 +1466,14 @@ static vta_status batch_host(vta_ctx* ctx, Ind ind, const float* const* hin, siz
         }
         char* base = static_cast<char*>(ctx->io);
         d_in = reinterpret_cast<float*>(base);
-        for (int k = 0; k < nout; ++k) d_out[k] = reinterpret_cast<float*>(base + in_al + out_al * k);
+        for (int k = 0, j = 0; k < nout; ++k)
+            if (!direct[k]) d_out[k] = reinterpret_cast<float*>(base + in_al + out_al * j++);
     } else {
-        VTA_TRY(vram_check(out_bytes * nout + in_bytes));
+        VTA_TRY(vram_check(out_bytes * n_staged + in_bytes));
         VTA_CUDA_TRY(cudaMalloc((void**)&d_in, in_bytes));
         in_guard.reset(d_in);
         for (int k = 0; k < nout; ++k) {
+            if (direct[k]) continue;
             cudaError_t e = cudaMalloc((void**)&d_out[k], out_bytes);
             if (e != cudaSuccess) {
                 for (int j = 0; j < k; ++j) cudaFree(d_out[j]);
@@ -1447,15 +1481,18 @@ static vta_status batch_host(vta_ctx* ctx, Ind ind, const float* const* hin, siz
             }
         }
     }
+    float* k_out[3] = {nullptr, nullptr, nullptr};  // where the kernels write
+    for (int k = 0; k < nout; ++k) k_out[k] = direct[k] ? direct[k] : d_out[k];
     // inputs -> device
     DevIn din{};
     for (int k = 0; k < nin; ++k) {
         din.p[k] = d_in + (size_t)k * len;
         VTA_TRY(upload(ctx, d_in + (size_t)k * len, hin[k], len * sizeof(float)));
     }
-    vta_status s = run_batch(ctx, ind, din, len, first, cs, d_out);
+    vta_status s = run_batch(ctx, ind, din, len, first, cs, k_out);
     if (s == VTA_OK && out_host) {
         for (int k = 0; k < nout && s == VTA_OK; ++k) {
+            if (direct[k]) continue;
             cudaError_t e = cudaMemcpyAsync(out_host[k], d_out[k], out_elems * sizeof(float),
                                             cudaMemcpyDeviceToHost, ctx->stream);
             if (e != cudaSuccess) s = cuda_fail(e, "cudaMemcpyAsync(D2H)");
@@ -1465,7 +1502,8 @@ static vta_status batch_host(vta_ctx* ctx, Ind ind, const float* const* hin, siz
     cudaStreamSynchronize(ctx->stream);
     if (s != VTA_OK || out_host) {
         if (!cached)
-            for (int k = 0; k < nout; ++k) cudaFree(d_out[k]);
+            for (int k = 0; k < nout; ++k)
+                if (d_out[k]) cudaFree(d_out[k]);
         if (s != VTA_OK) return s;
     } else {
         for (int k = 0; k < nout; ++k) *out_arr[k] = vta_device_array{d_out[k], nc, len, ctx->device};
@@ -1977,6 +2015,7 @@ vta_status vta_ctx_destroy(vta_ctx* ctx) {
     if (ctx->scratch) ctx->async_alloc ? (void)cudaFreeAsync(ctx->scratch, ctx->stream) : (void)cudaFree(ctx->scratch);
     if (ctx->aux) ctx->async_alloc ? (void)cudaFreeAsync(ctx->aux, ctx->stream) : (void)cudaFree(ctx->aux);
     if (ctx->io) cudaFree(ctx->io);
+    if (ctx->tmp) cudaFree(ctx->tmp);
     if (ctx->cc_dev) cudaFree(ctx->cc_dev);
     for (auto& e : ctx->rw) cudaFree(e.dev);
     if (ctx->async_alloc) cudaStreamSynchronize(ctx->stream);
@@ -2075,6 +2114,14 @@ vta_status vta_ctx_set_policy(vta_ctx* ctx, const char* key, const char* value) 
         }
         return VTA_OK;
     }
+    if (k == "host_out") {
+        // *_batch_into_host_f32 outputs in vta_pinned_alloc buffers: "direct"
+        // (the kernels store into them) or "copy" (device buffer + copy)
+        if (v == "direct") ctx->policy.host_out = 0;
+        else if (v == "copy") ctx->policy.host_out = 1;
+        else return fail(VTA_ERR_INVALID_POLICY, "host_out: direct|copy");
+        return VTA_OK;
+    }
     if (k == "recur_agg") {
         if (v == "auto") ctx->policy.recur_agg = 0;
         else if (v == "cuda") ctx->policy.recur_agg = 1;
@@ -2164,11 +2211,26 @@ vta_status vta_device_array_copy_to_host(vta_ctx* ctx, const vta_device_array* a
 
 vta_status vta_pinned_alloc(size_t bytes, void** out) {
     if (!out) return fail(VTA_ERR_INVALID_INPUT, "null out");
-    VTA_CUDA_TRY(cudaHostAlloc(out, bytes, cudaHostAllocDefault));
+    *out = nullptr;
+    VTA_CUDA_TRY(cudaHostAlloc(out, bytes, cudaHostAllocMapped | cudaHostAllocPortable));
+    void* dev = nullptr;
+    if (cudaHostGetDevicePointer(&dev, *out, 0) != cudaSuccess) {
+        cudaGetLastError();
+        dev = nullptr;  // copies only
+    }
+    if (dev) {
+        std::lock_guard<std::mutex> lk(g_pin_mu);
+        g_pin[reinterpret_cast<uintptr_t>(*out)] = PinnedBlock{bytes, static_cast<char*>(dev)};
+    }
     return VTA_OK;
 }
 vta_status vta_pinned_free(void* p) {
-    if (p) VTA_CUDA_TRY(cudaFreeHost(p));
+    if (!p) return VTA_OK;
+    {
+        std::lock_guard<std::mutex> lk(g_pin_mu);
+        g_pin.erase(reinterpret_cast<uintptr_t>(p));
+    }
+    VTA_CUDA_TRY(cudaFreeHost(p));
     return VTA_OK;
 }
 vta_status vta_device_alloc(vta_ctx* ctx, size_t bytes, void** out) {

@@ -71,6 +71,9 @@ struct Policy {
     int recur_agg = 0;
     // chunk length of the exact ADX scan (0 = auto: about 2,400 warp items)
     int scan_chunk = 0;
+    // *_batch_into_host_f32 outputs in vta_pinned_alloc buffers: 0 = the
+    // kernels store into them directly, 1 = device buffer and a copy
+    int host_out = 0;
 };
 
 }  // namespace vta
@@ -165,6 +168,9 @@ vta_status upload_async(vta_ctx* ctx, void* dst, const void* src, size_t bytes, 
 // constant cache when an earlier call uploaded the same bytes, else uploaded
 // into the cache (or, for server slots and large arrays, into `fallback`).
 vta_status const_upload_bytes(vta_ctx* ctx, const void* src, size_t bytes, void* fallback, const void** out);
+// The device address of [p, p + bytes) when it lies inside one block from
+// vta_pinned_alloc, else null
+float* pinned_device_view(const void* p, size_t bytes);
 template <class T>
 inline vta_status const_upload(vta_ctx* ctx, const T* src, size_t count, T* fallback, const T** out) {
     const void* p = nullptr;

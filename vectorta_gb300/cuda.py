@@ -194,6 +194,22 @@ def _dptr(obj) -> int:
 
 
 # ------------------------------------------------------------------ context --
+def pinned_empty(shape, dtype=np.float32) -> np.ndarray:
+    """A numpy array in page-locked host memory from vta_pinned_alloc (the
+    crate's LockedBuffer); freed when the array is collected.  As the output
+    of batch_into_host_f32 it takes the kernels' stores directly."""
+    import weakref
+
+    dt = np.dtype(dtype)
+    shape = (shape,) if isinstance(shape, int) else tuple(shape)
+    nbytes = int(np.prod(shape, dtype=np.int64)) * dt.itemsize
+    p = C.c_void_p()
+    N.check(N.lib().vta_pinned_alloc(max(nbytes, 1), C.byref(p)))
+    raw = (C.c_char * max(nbytes, 1)).from_address(p.value)
+    weakref.finalize(raw, N.lib().vta_pinned_free, C.c_void_p(p.value))
+    return np.frombuffer(raw, dtype=dt, count=int(np.prod(shape, dtype=np.int64))).reshape(shape)
+
+
 class Context:
     """Owns a vta_ctx (one stream and a scratch workspace on one device)."""
 
