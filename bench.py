@@ -1049,7 +1049,7 @@ TRAFFIC = {
 }
 KERNEL_NAME = {"recurrence_window_sweeps": "k_recur<OpEma, batch, EMIT>", "alma_grid": "k_wwma_tc<fp16x3>",
                "ema_small": "k_recur<OpEma, batch, EMIT>", "alma_small": "k_wwma_tc<fp16x3>",
-               "adx_sweep": "k_hlc_chunk<adx> + fix-up", "wwma_family": "k_wwma_tc<fp16x3> (CWMA)",
+               "adx_sweep": "k_hlc_chunk<adx> + k_adx_scan passes + fix-up", "wwma_family": "k_wwma_tc<fp16x3> (CWMA)",
                "windows_small": "k_prefix_window_batch (StdDev)", "recur_small": "k_recur<OpEma, batch, EMIT>",
                "wma_long": "k_wwma_tc<fp16x3> (K slices)", "tema_small": "k_recur<OpTema, batch, EMIT>",
                "percentile_small": "k_percentile (register window)"}
