@@ -156,16 +156,29 @@ __global__ void __launch_bounds__(kSW * 32) k_adx_scan(AdxScanArgs a) {
     if (PASS == PASS_AGG2) a.agg2[si] = adx;
 }
 
-// Chunk-entry states per lane (one thread per lane slot), in double-single:
-// LEVEL 1: s_1 = the seeding run's end state, s_{k+1} = omr^len_k s_k + agg1_k;
-// LEVEL 2: adx_1 likewise, adx_{k+1} = (pm1 rp)^len_k adx_k + agg2_k.
+// Chunk-entry states per lane slot, in double-single: one warp per slot.
+// LEVEL 1: s_1 = the seeding run's end state, s_{k+1} = m s_k + agg1_k with
+// m = omr^L; LEVEL 2: adx_1 likewise with m = (pm1 rp)^L and agg2.  Every
+// transition k = 1 .. nch - 2 is over a full chunk, so all share m: the warp
+// splits them into 32 consecutive blocks, each thread composes its block into
+// one affine map x -> A x + B, the maps are scanned across the warp (five
+// shuffle levels), and each thread then walks its block again from its
+// entry state, writing the entries.
+struct Aff {
+    D2s A, B[3];
+};
+__device__ __forceinline__ D2s ds_shfl_up(D2s v, int o) {
+    return {__shfl_up_sync(0xffffffffu, v.hi, o), __shfl_up_sync(0xffffffffu, v.lo, o)};
+}
 template <int LEVEL>
-__global__ void k_adx_carry(AdxScanArgs a) {
-    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= a.n_slots) return;
+__global__ void __launch_bounds__(128) k_adx_carry(AdxScanArgs a) {
+    constexpr int NC = LEVEL == 1 ? 3 : 1;
+    const int slot = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (slot >= a.n_slots) return;  // warp-uniform
     const int gi = slot >> 5;
     const int ci = a.groups[gi] * 32 + (slot & 31);
-    if (ci >= a.n_combos) return;
+    if (ci >= a.n_combos) return;  // warp-uniform
     Lane ln;
     ln.init(__ldg(a.periods + ci));
     const int s0 = a.group_s0[gi];
@@ -173,40 +186,67 @@ __global__ void k_adx_carry(AdxScanArgs a) {
     const float* seed = a.seed_state + (size_t)ci * 8;  // k_hlc_chunk's chunk-0 end state
     const D2s m = LEVEL == 1 ? D2s{ln.omr, 0.f} : ds_mul({ln.pm1, 0.f}, {ln.rp, 0.f});
     const D2s mL = ds_pow(m, a.L);
-    D2s s[3];
-    if (LEVEL == 1) {
-        s[0] = {seed[0], 0.f};
-        s[1] = {seed[1], 0.f};
-        s[2] = {seed[2], 0.f};
-    } else {
-        s[0] = {seed[3], 0.f};
-    }
-    // the chunk aggregates come through a 4-deep register queue, so their
-    // loads run ahead of the dependent double-single updates
-    auto rec = [&](int k) {
+    auto agg = [&](int k) {
         const size_t si = (size_t)k * a.n_slots + slot;
-        if (k + 1 >= nch) return make_float4(0.f, 0.f, 0.f, 0.f);
         return LEVEL == 1 ? __ldg(a.agg1 + si) : make_float4(__ldg(a.agg2 + si), 0.f, 0.f, 0.f);
     };
-    float4 q0 = rec(1), q1 = rec(2), q2 = rec(3), q3 = rec(4);
-#pragma unroll 1
-    for (int k = 1; k < nch; ++k) {
-        const float4 g = q0;
-        q0 = q1;
-        q1 = q2;
-        q2 = q3;
-        q3 = rec(k + 4);
+    auto put = [&](int k, const D2s (&x)[NC]) {
         const size_t si = (size_t)k * a.n_slots + slot;
-        if (LEVEL == 1) {
-            a.carry1[si] = make_float4(s[0].hi + s[0].lo, s[1].hi + s[1].lo, s[2].hi + s[2].lo, 0.f);
-            s[0] = ds_add(ds_mul(mL, s[0]), {g.x, 0.f});
-            s[1] = ds_add(ds_mul(mL, s[1]), {g.y, 0.f});
-            s[2] = ds_add(ds_mul(mL, s[2]), {g.z, 0.f});
-        } else {
-            a.carry2[si] = s[0].hi + s[0].lo;
-            s[0] = ds_add(ds_mul(mL, s[0]), {g.x, 0.f});
+        if (LEVEL == 1)
+            a.carry1[si] = make_float4(x[0].hi + x[0].lo, x[1].hi + x[1].lo, x[2].hi + x[2].lo, 0.f);
+        else
+            a.carry2[si] = x[0].hi + x[0].lo;
+    };
+    // transitions 1 .. T, T = nch - 2; this thread's block [k0, k1)
+    const int T = nch - 2;
+    const int per = T > 0 ? (T + 31) / 32 : 0;
+    const int k0 = 1 + min(T, lane * per), k1 = 1 + min(T, (lane + 1) * per);
+    Aff f;
+    f.A = {1.f, 0.f};
+#pragma unroll
+    for (int c = 0; c < NC; ++c) f.B[c] = {0.f, 0.f};
+#pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+        const float4 g4 = agg(k);
+        const float g[3] = {g4.x, g4.y, g4.z};
+        f.A = ds_mul(mL, f.A);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) f.B[c] = ds_add(ds_mul(mL, f.B[c]), {g[c], 0.f});
+    }
+    // inclusive scan of the maps in lane order: (later) o (earlier)
+#pragma unroll 1
+    for (int o = 1; o < 32; o <<= 1) {
+        Aff e;
+        e.A = ds_shfl_up(f.A, o);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) e.B[c] = ds_shfl_up(f.B[c], o);
+        if (lane >= o) {
+#pragma unroll
+            for (int c = 0; c < NC; ++c) f.B[c] = ds_add(ds_mul(f.A, e.B[c]), f.B[c]);
+            f.A = ds_mul(f.A, e.A);
         }
     }
+    // exclusive map of this thread: the previous lane's inclusive one
+    Aff x;
+    x.A = ds_shfl_up(f.A, 1);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) x.B[c] = ds_shfl_up(f.B[c], 1);
+    D2s st[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        const D2s sd = {seed[LEVEL == 1 ? c : 3], 0.f};
+        st[c] = lane == 0 ? sd : ds_add(ds_mul(x.A, sd), x.B[c]);
+    }
+#pragma unroll 1
+    for (int k = k0; k < k1; ++k) {
+        put(k, st);
+        const float4 g4 = agg(k);
+        const float g[3] = {g4.x, g4.y, g4.z};
+#pragma unroll
+        for (int c = 0; c < NC; ++c) st[c] = ds_add(ds_mul(mL, st[c]), {g[c], 0.f});
+    }
+    // the last chunk's entry (k = nch - 1) from the thread whose block ends there
+    if (nch >= 2 && k1 == nch - 1 && (k0 < k1 || lane == 0)) put(nch - 1, st);
 }
 
 }  // namespace
@@ -214,7 +254,7 @@ __global__ void k_adx_carry(AdxScanArgs a) {
 vta_status launch_adx_scan(const AdxScanArgs& a, cudaStream_t st) {
     if (a.n_items <= 0) return VTA_OK;
     const unsigned blocks = ceil_div(a.n_items, kSW);
-    const unsigned cblocks = ceil_div(a.n_slots, 128);
+    const unsigned cblocks = ceil_div((size_t)a.n_slots * 32, 128);  // a warp per lane slot
     k_adx_scan<PASS_AGG1><<<blocks, kSW * 32, 0, st>>>(a);
     VTA_TRY(check_launch("k_adx_scan<agg1>"));
     k_adx_carry<1><<<cblocks, 128, 0, st>>>(a);
