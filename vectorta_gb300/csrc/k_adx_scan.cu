@@ -78,6 +78,7 @@ enum { PASS_AGG1 = 0, PASS_AGG2 = 1, PASS_EMIT = 2 };
 template <int PASS>
 __global__ void __launch_bounds__(kSW * 32) k_adx_scan(AdxScanArgs a) {
     __shared__ float stage[kSW][32][33];
+    __shared__ float4 xin[kSW][3][8];  // a full tile's high, low and close
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int item = blockIdx.x * kSW + warp;
     if (item >= a.n_items) return;
@@ -109,28 +110,48 @@ __global__ void __launch_bounds__(kSW * 32) k_adx_scan(AdxScanArgs a) {
             xl = __ldg(a.l + tb + lane);
             xc = __ldg(a.c + tb + lane);
         }
-        auto steps = [&](auto wide_tag) {
+        // one step on the bar (ch, cl, cc): PAdx::step_run's arithmetic
+        auto step = [&](int j, float ch, float cl, float cc, auto wide_tag) {
             constexpr bool WIDE = decltype(wide_tag)::value;
-            for (int j = 0; j < nt; ++j) {
-                const float ch = __shfl_sync(0xffffffffu, xh, j);
-                const float cl = __shfl_sync(0xffffffffu, xl, j);
-                const float cc = __shfl_sync(0xffffffffu, xc, j);
-                // PAdx::step_run's arithmetic
-                const float tr = fmaxf(fmaxf(ch - cl, fabsf(ch - pc)), fabsf(cl - pc));
-                const float up = ch - ph, down = pl - cl;
-                const float dp = (up > down && up > 0.f) ? up : 0.f;
-                const float dm = (down > up && down > 0.f) ? down : 0.f;
-                atr = atr * ln.omr + tr;
-                pdm = pdm * ln.omr + dp;
-                mdm = mdm * ln.omr + dm;
-                if (PASS != PASS_AGG1) {
-                    const float dx = WIDE ? hlc::adx_dx_wide(pdm, mdm) : hlc::adx_dx(pdm, mdm, atr);
-                    adx = (adx * ln.pm1 + dx) * ln.rp;
+            const float tr = fmaxf(fmaxf(ch - cl, fabsf(ch - pc)), fabsf(cl - pc));
+            const float up = ch - ph, down = pl - cl;
+            const float dp = (up > down && up > 0.f) ? up : 0.f;
+            const float dm = (down > up && down > 0.f) ? down : 0.f;
+            atr = atr * ln.omr + tr;
+            pdm = pdm * ln.omr + dp;
+            mdm = mdm * ln.omr + dm;
+            if (PASS != PASS_AGG1) {
+                const float dx = WIDE ? hlc::adx_dx_wide(pdm, mdm) : hlc::adx_dx(pdm, mdm, atr);
+                adx = (adx * ln.pm1 + dx) * ln.rp;
+            }
+            if (PASS == PASS_EMIT) stage[warp][lane][j] = adx;
+            ph = ch;
+            pl = cl;
+            pc = cc;
+        };
+        // A full tile reads its bars from shared memory, four steps per
+        // 16-byte broadcast load, in a fully unrolled loop; a partial tile
+        // broadcasts them by shuffles.
+        auto steps = [&](auto wide_tag) {
+            if (nt == 32) {
+                float* xs = reinterpret_cast<float*>(&xin[warp][0][0]);
+                __syncwarp();  // the previous tile's reads are done
+                xs[lane] = xh;
+                xs[32 + lane] = xl;
+                xs[64 + lane] = xc;
+                __syncwarp();
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const float4 h4 = xin[warp][0][q], l4 = xin[warp][1][q], c4 = xin[warp][2][q];
+                    step(4 * q, h4.x, l4.x, c4.x, wide_tag);
+                    step(4 * q + 1, h4.y, l4.y, c4.y, wide_tag);
+                    step(4 * q + 2, h4.z, l4.z, c4.z, wide_tag);
+                    step(4 * q + 3, h4.w, l4.w, c4.w, wide_tag);
                 }
-                if (PASS == PASS_EMIT) stage[warp][lane][j] = adx;
-                ph = ch;
-                pl = cl;
-                pc = cc;
+            } else {
+                for (int j = 0; j < nt; ++j)
+                    step(j, __shfl_sync(0xffffffffu, xh, j), __shfl_sync(0xffffffffu, xl, j),
+                         __shfl_sync(0xffffffffu, xc, j), wide_tag);
             }
         };
         // DX by the hardware reciprocal where the sums stay normal over

@@ -48,6 +48,7 @@ template <class Op>
 __global__ void __launch_bounds__(kCW * 32) k_hlc_chunk(HlcChunkArgs a) {
     __shared__ float stage0[kCW][32][33];
     __shared__ float stage1[kCW][Op::kTwo ? 32 : 1][33];
+    __shared__ float4 xin[kCW][3][8];  // a running tile's high, low and close
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int item = blockIdx.x * kCW + warp;
     if (item >= a.n_items) return;
@@ -86,17 +87,29 @@ __global__ void __launch_bounds__(kCW * 32) k_hlc_chunk(HlcChunkArgs a) {
                 xc = __ldg(a.c + tj);
             }
             if (tb >= rf && nt == 32) {
+                // the tile's bars from shared memory, four steps per 16-byte
+                // broadcast load
+                float* xs = reinterpret_cast<float*>(&xin[warp][0][0]);
+                __syncwarp();  // the previous tile's reads are done
+                xs[lane] = xh;
+                xs[32 + lane] = xl;
+                xs[64 + lane] = xc;
+                __syncwarp();
                 auto run32 = [&](auto wide_tag) {
-#pragma unroll 8
-                    for (int j = 0; j < 32; ++j) {
-                        const float hv = __shfl_sync(0xffffffffu, xh, j);
-                        const float lv = __shfl_sync(0xffffffffu, xl, j);
-                        const float cv = __shfl_sync(0xffffffffu, xc, j);
-                        float o1;
-                        const float o0 = op.template step_run<decltype(wide_tag)::value>(hv, lv, cv, o1);
-                        if (emit) {
-                            stage0[warp][lane][j] = o0;
-                            if (Op::kTwo) stage1[warp][lane][j] = o1;
+#pragma unroll 2
+                    for (int q = 0; q < 8; ++q) {
+                        const float4 h4 = xin[warp][0][q], l4 = xin[warp][1][q], c4 = xin[warp][2][q];
+                        const float hv[4] = {h4.x, h4.y, h4.z, h4.w}, lv[4] = {l4.x, l4.y, l4.z, l4.w},
+                                    cv[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            float o1;
+                            const float o0 =
+                                op.template step_run<decltype(wide_tag)::value>(hv[u], lv[u], cv[u], o1);
+                            if (emit) {
+                                stage0[warp][lane][4 * q + u] = o0;
+                                if (Op::kTwo) stage1[warp][lane][4 * q + u] = o1;
+                            }
                         }
                     }
                 };
