@@ -621,7 +621,7 @@ __all__ += ["AlmaBatchRange", "PeriodBatchRange", "StdDevBatchRange", "ZscoreBat
             "SuperTrendParams", "PercentileNearestRankParams", "EpmaBatchRange", "EpmaParams", "VpwmaBatchRange",
             "VpwmaParams", "VramMaComputer",
             "CudaMaSelector", "StreamBank",
-            "CLASSES",
+            "CLASSES", "pinned_empty",
             "device_count", "launch_count"]
 
 
